@@ -1,0 +1,377 @@
+"""Benchmark: ms per pressure projection (MGPCG to relative residual 1e-6) on
+the 256^3 sphere configuration, on GB300.
+
+A step is one projection of the same synthetic velocity field from a cold
+start (pressure reset to zero): build b, PCG to 1e-6, circuit breaker,
+velocity correction.  `value` is device time per step with the inputs
+resident in HBM; `e2e` adds the host->device upload of u, v, w from pinned
+memory and the device->host read of the corrected u, v, w, all through the
+C ABI.  The timed inputs (about 1.7 GB of fields) are larger than the 129 MB
+L2, so no flush is needed between steps.
+
+--impl reference times the FP64 CPU restatement of the same path (the
+reference is JavaScript + WebGPU and cannot run on this machine) on the
+host cores, on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ms/solve to 1e-6 residual at 256^3 (MGPCG pressure projection, sphere r=24)"
+UNIT = "ms/solve"
+
+# Algorithmic bytes per cell per launch (each array the kernel reads or
+# writes counted once over the domain; FP32 4 B, BF16 2 B, coefficients
+# 16 B FP32 / 8 B BF16, the double-single iterate 8 B).
+def kernel_bytes_per_cell(precision):
+    vb = 2 if precision == "mixed" else 4
+    xb = 8 if precision == "mixed" else 4
+    return {
+        "p_pAp": vb + 4 + 16 + 4,                 # z, p, coef32 -> p
+        "x_residual": xb + 4 + 4 + 16 + xb + 4,   # x, p, b, coef32 -> x, r
+        "relax": vb + 4 + (8 if vb == 2 else 16) + vb / 2,   # x, b(=r, fp32), coef, half of x written
+        "residual": vb + 4 + (8 if vb == 2 else 16) + vb,
+        "restrict": vb + vb / 8,
+        "prolong": vb / 8 + 2 * vb,
+        "rz": 4 + vb,
+    }
+
+
+PROF_IDS = {"p_pAp": 0, "x_residual": 1, "relax": 2, "residual": 3, "restrict": 4, "prolong": 5,
+            "rz": 6}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        p = json.load(open(path))
+        return p["hbm_gbs"], "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200", "-i", str(os.environ.get("LOCAL_RANK", 0))],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = max(float(r[2]) for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def dist_setup(n_gpus):
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return rank, world, dist
+    return rank, world, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ ours --
+def run_gb300(args):
+    rank, world, dist = dist_setup(args.gpus)
+    device = int(os.environ.get("LOCAL_RANK", 0))
+    from tsl_array_n_gb300 import build as B
+    B.build()
+    import ctypes as C
+    from tsl_array_n_gb300 import _lib, fluxflow as ff, scenes
+    from tsl_array_n_gb300.tsl_array_n import init
+
+    ctx = init(device)
+    lib = _lib.load()
+    n = args.size
+    sc = scenes.sphere_scene(n=n, radius_cells=24 * n // 256, modes=32, seed=1)
+    shape, h = sc["shape"], sc["h"]
+    col = ff.create_sdf_static_collider3(*shape, *h)
+    col.add_shapes(sc["shapes"])
+    cw = col.compute_face_weights()
+    grid = ff.FaceCenteredGrid3(shape, h).set(sc["u"], sc["v"], sc["w"])
+    out = ff.FaceCenteredGrid3(shape, h)
+    levels = max(1, int(np.log2(n)) - 2)          # 256 -> 6 levels, 8^3 coarsest
+    solver = ff.create_grid_pressure_solver3(
+        shape, h, collider_weights=cw, dirichlet=(sc["active"], sc["target"]),
+        multigrid={"numberOfLevels": levels, "coarseSolve": args.coarse},
+        precision=args.precision, tolerance=1e-6)
+    dispatch = solver.project(grid, out)
+
+    def step():
+        solver.pressure.fill(0.0)
+        return dispatch()
+
+    for _ in range(args.warmup):
+        d = step()
+    iters = d["iterations"]
+
+    # device-resident timing
+    clocks = Clocks()
+    barrier(dist)
+    ctx.synchronize()
+    clocks.start()
+    _lib.check(lib.ff_ctx_event_record(ctx.handle, 0))
+    launches = 0
+    diags = []
+    for _ in range(args.steps):
+        d = step()
+        launches += d["kernelLaunches"] + 1
+        diags.append(dict(d))
+    _lib.check(lib.ff_ctx_event_record(ctx.handle, 1))
+    ms = C.c_float()
+    _lib.check(lib.ff_ctx_event_elapsed(ctx.handle, 0, 1, C.byref(ms)))
+    ctx.synchronize()
+    clk = clocks.stop()
+    barrier(dist)
+    ms_step = max_over_ranks(dist, ms.value / args.steps)
+
+    # end-to-end through the C ABI with host buffers
+    nb = [sc["u"].nbytes, sc["v"].nbytes, sc["w"].nbytes]
+    hin, hout = [], []
+    for b in nb:
+        p = C.c_void_p()
+        _lib.check(lib.ff_host_alloc(b, C.byref(p)))
+        hin.append(p)
+        q = C.c_void_p()
+        _lib.check(lib.ff_host_alloc(b, C.byref(q)))
+        hout.append(q)
+    for p, a in zip(hin, (sc["u"], sc["v"], sc["w"])):
+        C.memmove(p, a.ctypes.data, a.nbytes)
+    fields_in = (grid.data_u, grid.data_v, grid.data_w)
+    fields_out = (out.data_u, out.data_v, out.data_w)
+
+    def e2e_step():
+        for f, p, b in zip(fields_in, hin, nb):
+            _lib.check(lib.ff_field_upload_async(f.handle, p, b))
+        r = step()
+        for f, p, b in zip(fields_out, hout, nb):
+            _lib.check(lib.ff_field_download_async(f.handle, p, b))
+        return r
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    barrier(dist)
+    ctx.synchronize()
+    _lib.check(lib.ff_ctx_event_record(ctx.handle, 2))
+    for _ in range(args.steps):
+        e2e_step()
+    _lib.check(lib.ff_ctx_event_record(ctx.handle, 3))
+    e2e_ms = C.c_float()
+    _lib.check(lib.ff_ctx_event_elapsed(ctx.handle, 2, 3, C.byref(e2e_ms)))
+    e2e_ms_step = max_over_ranks(dist, e2e_ms.value / args.steps)
+    uo = np.empty(sc["u"].size, np.float32)
+    C.memmove(uo.ctypes.data, hout[0], uo.nbytes)
+    assert np.all(np.isfinite(uo))
+    for p in hin + hout:
+        lib.ff_host_free(p)
+
+    # per-kernel roofline (device events around single launches)
+    peak, peak_kind = peaks()
+    cells = n ** 3
+    bpc = kernel_bytes_per_cell(args.precision)
+    kern = {}
+    for name, kid in PROF_IDS.items():
+        avg = C.c_float()
+        _lib.check(lib.ff_pressure3_profile(solver.handle, kid, 10, C.byref(avg)))
+        kern[name] = {"ms": avg.value, "gbs": bpc[name] * cells / (avg.value * 1e-3) / 1e9}
+    it_ms = C.c_float()
+    _lib.check(lib.ff_pressure3_profile(solver.handle, 8, 5, C.byref(it_ms)))
+    vc_ms = C.c_float()
+    _lib.check(lib.ff_pressure3_profile(solver.handle, 7, 5, C.byref(vc_ms)))
+    # share of the iteration: relax runs 2*(down+final) passes at level 0
+    passes0 = 2 * (2 + 2)
+    shares = {"relax": kern["relax"]["ms"] * passes0, "x_residual": kern["x_residual"]["ms"],
+              "p_pAp": kern["p_pAp"]["ms"]}
+    dom = max(shares, key=shares.get)
+    traffic = None
+    prof_path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(prof_path):
+        t = json.load(open(prof_path)).get(f"{dom}_{args.precision}_bytes_per_cell")
+        traffic = t * cells if t else None
+    roof = {"bound": "hbm", "kernel": dom, "achieved": round(kern[dom]["gbs"], 1), "peak": peak,
+            "unit": "GB/s", "frac": round(kern[dom]["gbs"] / peak, 4), "peak_kind": peak_kind,
+            "traffic": traffic, "algorithmic_bytes": bpc[dom] * cells,
+            "kernels": {k: {"ms": round(v["ms"], 4), "GB/s": round(v["gbs"], 1),
+                            "frac": round(v["gbs"] / peak, 3)} for k, v in kern.items()},
+            "iteration_ms": round(it_ms.value, 4), "vcycle_ms": round(vc_ms.value, 4)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(sc, levels, iters, budget_s=args.cpu_budget)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(ms_step / 1.0, 4), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+bf16+f64" if args.precision == "mixed" else "f32+f64",
+            "data": "synthetic (seeded 32-mode Fourier velocity, sphere collider)",
+            "config": {"workload": f"3D MGPCG pressure projection {n}^3, sphere r={24 * n // 256} cells, "
+                                   f"closed walls + one pinned cell, {levels} levels, coarsest {args.coarse}, "
+                                   f"precision {args.precision}, tol 1e-6 relative, cold start",
+                       "cells": cells, "iterations": iters,
+                       "converged": all(x["converged"] for x in diags),
+                       "residual_rel": diags[-1]["residual"] / diags[-1]["bNorm"],
+                       "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
+            "e2e": {"value": round(e2e_ms_step, 4), "unit": UNIT,
+                    "h2d_bytes_per_step": int(sum(nb)), "d2h_bytes_per_step": int(sum(nb))},
+            "gpu_launches": launches,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+# --------------------------------------------------------- CPU baseline --
+def _oracle_system(sc, levels):
+    """The same system on the FP64 oracle: collider bake, build, operator,
+    V-cycle and PCG all restated on the CPU (none of libff on this path)."""
+    from oracle import oracle as O
+    shape, h = sc["shape"], sc["h"]
+    _, wu, wv, ww = O.collider_bake(sc["shapes"], shape, h)
+    w = tuple(x.astype(np.float64) for x in (wu, wv, ww))
+    mask, tgt, vent = O.dirichlet_fields(shape, sc["active"], sc["target"], w)
+    b, _ = O.build_system(shape, h, sc["u"], sc["v"], sc["w"], collider_weights=w, mask=mask, target=tgt)
+    return O, shape, h, w, mask, vent, b
+
+
+def cpu_baseline(sc, levels, gpu_iters, budget_s=30.0):
+    """FP64 CPU restatement on all host cores: time the setup plus one and
+    three PCG iterations, extrapolate to the GPU's iteration count."""
+    O, shape, h, w, mask, vent, b = _oracle_system(sc, levels)
+    cores = os.cpu_count()
+    t0 = time.perf_counter()
+    mg = O.Multigrid(shape, h, mask, vent, w, levels=levels, coarse_direct=True)
+    t_mg = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.pcg_solve(shape, h, b, None, mask, w, mg, "multigrid", tol=1e-6, max_iter=1)
+    t1 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.pcg_solve(shape, h, b, None, mask, w, mg, "multigrid", tol=1e-6, max_iter=3)
+    t3 = time.perf_counter() - t0
+    per_iter = max((t3 - t1) / 2.0, 1e-9)
+    setup = max(t1 - per_iter, 0.0) + t_mg
+    est = (setup + gpu_iters * per_iter) * 1e3
+    return {"value": round(est, 1), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"FP64 oracle MGPCG on the same {shape[0]}^3 system: hierarchy build + 1 and 3 "
+                      f"iterations timed ({t1 + t3 + t_mg:.1f} s), extrapolated to {gpu_iters} iterations"}
+
+
+def run_reference(args):
+    """--impl reference: the CPU restatement of the path (the reference is
+    JS/WebGPU), rank 0 only, each step a bounded sample (one PCG iteration
+    at the full size on a prepared system)."""
+    rank = int(os.environ.get("RANK", 0))
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    from tsl_array_n_gb300 import scenes
+    n = args.size
+    sc = scenes.sphere_scene(n=n, radius_cells=24 * n // 256, modes=32, seed=1)
+    levels = max(1, int(np.log2(n)) - 2)
+    O, shape, h, w, mask, vent, b = _oracle_system(sc, levels)
+    t0 = time.perf_counter()
+    mg = O.Multigrid(shape, h, mask, vent, w, levels=levels, coarse_direct=True)
+    x, res, _ = O.pcg_solve(shape, h, b, None, mask, w, mg, "multigrid", tol=1e-6, max_iter=1)
+    setup_s = time.perf_counter() - t0
+    iters_needed = args.ref_iters
+    samples = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        O.pcg_solve(shape, h, b, None, mask, w, mg, "multigrid", tol=1e-6, max_iter=1)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            samples.append(dt)
+    per_iter = float(np.median(samples))
+    value = (setup_s + iters_needed * per_iter) * 1e3
+    cores = os.cpu_count()
+    cpu = {"value": round(value, 1), "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": f"FP64 CPU restatement (oracle/), {shape[0]}^3: per step one setup+iteration "
+                     f"pass timed, extrapolated to {iters_needed} iterations"}
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value, 1),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded 32-mode Fourier velocity, sphere collider)",
+        "config": {"workload": f"3D MGPCG pressure projection {n}^3 (CPU FP64 restatement)", "cells": n ** 3},
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32"])
+    ap.add_argument("--coarse", default="direct", choices=["direct", "sweeps"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=30.0)
+    ap.add_argument("--ref-iters", type=int, default=12)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

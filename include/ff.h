@@ -1,0 +1,218 @@
+/*
+ * ff.h -- C ABI of libff, the GB300 (sm_103a) implementation of fluxflow's
+ * grid-fluid hot path.  This is the drop-in boundary: a Node N-API addon (or
+ * any FFI: ctypes, cffi, JNI) binds exactly these symbols.  Plain pointers,
+ * sizes and opaque handles; no C++ or torch types cross it.
+ *
+ * Conventions
+ *   - Every function returns an int status: 0 ok, negative FF_E_* on error.
+ *     ff_last_error() gives a one-line description (thread-local).
+ *   - Handles are opaque.  Device buffers are owned by the library and freed
+ *     by the matching *_destroy (the reference has no disposal API,
+ *     fluxflow src/linalg/linalg.js:43-53; this is an addition).
+ *   - One CUDA stream per context.  A context is not thread-safe, matching
+ *     the reference's single JS thread.
+ *   - Layout is the reference's i-fastest layout (tsl_array_n
+ *     src/array.js:24-38): element (i,j,k) of shape (nx,ny,nz) is at
+ *     i + nx*(j + ny*k).  MAC faces: u is (nx+1,ny,nz), v (nx,ny+1,nz),
+ *     w (nx,ny,nz+1) (fluxflow src/grid/grid_data3.js:121-176).
+ *   - There is no CPU fallback: without a CUDA device every entry point that
+ *     needs one returns FF_E_CUDA.
+ */
+#ifndef FF_H
+#define FF_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FF_OK 0
+#define FF_E_ARG (-1)      /* bad argument / shape mismatch (reference throws) */
+#define FF_E_CUDA (-2)     /* CUDA runtime error or no device                 */
+#define FF_E_NOMEM (-3)
+#define FF_E_STATE (-4)    /* call out of order                               */
+#define FF_E_LIMIT (-5)    /* size beyond a stated limit                      */
+
+typedef struct ff_ctx_s *ff_ctx;
+typedef struct ff_field_s *ff_field;
+typedef struct ff_pressure_s *ff_pressure;
+
+const char *ff_last_error(void);
+/* Library build identification ("ff <version> sm_103a"). */
+const char *ff_version(void);
+
+/* ---- context: replaces tsl_array_n init() (src/context.js:74-132), which
+ * brings up a WebGPU device; here it selects a CUDA device and stream. ---- */
+int ff_ctx_create(int device, ff_ctx *out);
+int ff_ctx_destroy(ff_ctx ctx);
+int ff_ctx_synchronize(ff_ctx ctx);
+/* Page-locked host memory for fast uploads/downloads (no reference
+ * counterpart; the reference's host arrays are JS TypedArrays). */
+int ff_host_alloc(size_t bytes, void **out);
+int ff_host_free(void *p);
+/* CUDA events on the context stream, for device-side timing by callers
+ * (replaces the WebGPU timestamp queries of fluxflow src/profiling.js:302-330).
+ * Slots 0..15.  elapsed waits for event b.                                  */
+int ff_ctx_event_record(ff_ctx ctx, int slot);
+int ff_ctx_event_elapsed(ff_ctx ctx, int slot_a, int slot_b, float *ms);
+
+/* ---- fields: replace tsl_array_n arrayN (src/array.js:94-133) ---------- */
+#define FF_FLOAT 0   /* 'float'  -> f32          */
+#define FF_INT 1     /* 'int'    -> i32          */
+#define FF_UINT8 2   /* masks    -> u8           */
+#define FF_VEC3 3    /* 'vec3'   -> 3 x f32, AoS */
+/* arrayN(type, shape): ndim 1..3 (array.js:4-20 rejects 4D) */
+int ff_field_create(ff_ctx ctx, int dtype, int ndim, const int *shape, ff_field *out);
+int ff_field_destroy(ff_field f);
+/* fromArray (array.js:124-129): host -> device, bytes must equal the field size */
+int ff_field_upload(ff_field f, const void *host, size_t bytes);
+/* toArray (array.js:114-122): device -> host; synchronous like the awaited promise */
+int ff_field_download(ff_field f, void *host, size_t bytes);
+/* Asynchronous variants on the context stream (host memory should be pinned). */
+int ff_field_upload_async(ff_field f, const void *host, size_t bytes);
+int ff_field_download_async(ff_field f, void *host, size_t bytes);
+int ff_field_fill(ff_field f, float value);
+int ff_field_info(ff_field f, int *dtype, int *ndim, int *shape3, int64_t *count);
+void *ff_field_device_ptr(ff_field f);
+
+/* ---- pressure projection: replaces createGridPressureSolver3
+ * (fluxflow src/grid/grid_pressure_solver3.js:66-574) and, with nz == 1,
+ * createGridPressureSolver2 (grid_pressure_solver2.js:223-981). ---------- */
+#define FF_PRE_MULTIGRID 0
+#define FF_PRE_JACOBI 1
+#define FF_PRE_NONE 2
+#define FF_COARSE_SWEEPS 0   /* numberOfCoarsestIterations RB sweeps (reference) */
+#define FF_COARSE_DIRECT 1   /* FP64 direct solve of the coarsest level          */
+#define FF_STORE_FP32 0      /* V-cycle arrays in FP32                            */
+#define FF_STORE_BF16 1      /* V-cycle arrays in BF16, FP32 arithmetic           */
+#define FF_ITERATE_FP32 0    /* CG iterate x in FP32 (reference)                  */
+#define FF_ITERATE_DS 1      /* x as hi+lo FP32 pair, compensated residual        */
+
+typedef struct {
+    int resolution[3];          /* nz == 1 selects the 2D solver              */
+    double grid_spacing[3];
+    double origin[3];
+    int preconditioner;         /* FF_PRE_*                       (:72)       */
+    double tolerance;           /* default 1e-6                   (:73)       */
+    int max_iterations;         /* <=0: ceil(factor*max(res)*(3D?1:4)) (:133) */
+    double max_iterations_factor;   /* default 1.5                (:76)       */
+    int relative_tolerance;     /* default 1                      (:77)       */
+    double max_plausible_pressure;  /* default 1e6                (:36)       */
+    /* multigrid options (multigrid.js:1186-1250) */
+    int mg_levels;              /* numberOfLevels, default 1                   */
+    int mg_down, mg_up;         /* numberOfSmoothingIterationsDown/Up, 2       */
+    int mg_coarsest;            /* numberOfCoarsestIterations, 20              */
+    int mg_final;               /* numberOfFinalIterations, 2                  */
+    double mg_sor;              /* sorFactor, 1.0                              */
+    int mg_coarsen_mask;        /* coarsenDirichletMask, 1                     */
+    int mg_coarsen_weights;     /* coarsenFaceWeights, 1                       */
+    int mg_coarse_mode;         /* FF_COARSE_*                                 */
+    /* precision (no reference counterpart: the reference is FP32 only) */
+    int vcycle_storage;         /* FF_STORE_*                                  */
+    int iterate;                /* FF_ITERATE_*                                */
+} ff_pressure_desc;
+
+/* Fills the reference defaults for a resolution/spacing. */
+void ff_pressure_desc_default(ff_pressure_desc *d, const int *resolution, const double *spacing);
+
+typedef struct {
+    int converged;              /* diagnostics.converged                       */
+    int rejected;               /* circuit breaker fired (:547-554)            */
+    int iterations;             /* diagnostics.iterations                      */
+    int stopped_by;             /* FF_STOP_* (linalg.js:1056-1103)             */
+    double residual;            /* sqrt|r.r| of the last true residual         */
+    double b_norm;              /* sqrt(b.b)                                   */
+    int bad_cells;              /* non-finite or |p| > maxPlausiblePressure    */
+    int max_iterations;         /* the cap that applied                        */
+    int kernel_launches;        /* libff kernels launched by the call          */
+} ff_diag;
+
+#define FF_STOP_NONE 0
+#define FF_STOP_DEGENERATE_PAP 1
+#define FF_STOP_PAP_GROWTH 2
+#define FF_STOP_ALPHA_MAGNITUDE 3
+#define FF_STOP_DEGENERATE_OLD_RZ 4
+#define FF_STOP_CONVERGED 5
+#define FF_STOP_RESIDUAL_GROWING 6
+
+int ff_pressure3_create(ff_ctx ctx, const ff_pressure_desc *desc, ff_pressure *out);
+int ff_pressure3_destroy(ff_pressure ps);
+/* colliderWeights {u,v,w} (:69, :163-230): face fields, or NULL to clear.  */
+int ff_pressure3_set_collider_weights(ff_pressure ps, ff_field u, ff_field v, ff_field w);
+/* faceWeights {u,v,w} (beta, :68, :217-229), or NULL to clear.            */
+int ff_pressure3_set_face_weights(ff_pressure ps, ff_field u, ff_field v, ff_field w);
+/* dirichlet(pos) -> {active, target} (:68, :171-206) evaluated per cell:
+ * active is a FF_UINT8 cell field, target a FF_FLOAT cell field (or NULL
+ * for 0).  active == NULL clears the Dirichlet condition.                 */
+int ff_pressure3_set_dirichlet(ff_pressure ps, ff_field active, ff_field target);
+/* Runtime settings object (:135): key names as in the reference. */
+int ff_pressure3_set(ff_pressure ps, const char *key, double value);
+/* project(inGrid, outGrid)() (:339-556).  u_out may equal u_in.  The
+ * pressure field persists between calls and is the warm start.           */
+int ff_pressure3_project(ff_pressure ps, ff_field u_in, ff_field v_in, ff_field w_in,
+                         ff_field u_out, ff_field v_out, ff_field w_out, ff_diag *diag);
+/* PCG solve of A p = b for a caller-given b on the solver's current system
+ * (createPreconditionedConjugateGradientSolver(...).solve, linalg.js:2176
+ * with the GPU-resident path of :1651).  The pressure field is the initial
+ * guess and the result; the circuit breaker applies as in project().      */
+int ff_pressure3_solve(ff_pressure ps, ff_field b, ff_diag *diag);
+/* The solver's own fields: pressure (:142), b (:143), dirichletMask and
+ * ventMask (:572, as u8 here).  Borrowed handles, valid until destroy.     */
+int ff_pressure3_fields(ff_pressure ps, ff_field *pressure, ff_field *b,
+                        ff_field *dirichlet_mask, ff_field *vent_mask);
+
+/* ---- static SDF collider: replaces createSDFStaticCollider3.addShapes
+ * (fluxflow src/grid/sdf_collider3.js:69-99) and computeFaceWeights
+ * (:131-254), which the reference runs on the CPU; here FP64 on the device.
+ * phi: cell field (nx,ny,nz) of signed distance (solid where phi < 0);
+ * wu/wv/ww: face-open fractions (MIN_FACE_WEIGHT 0.01, :23).  Any of the
+ * output fields may be NULL.                                              */
+#define FF_SHAPE_SPHERE 0
+#define FF_SHAPE_BOX 1
+typedef struct {
+    int type;                 /* FF_SHAPE_*   (primitive_sdf3.js:169-200) */
+    int has_rotation;
+    double center[3];
+    double radius;            /* sphere */
+    double half_extents[3];   /* box    */
+    double rotation_axis[3];
+    double rotation_angle;
+} ff_shape;
+int ff_collider3_bake(ff_ctx ctx, const ff_shape *shapes, int nshapes, int invert,
+                      const int *resolution, const double *grid_spacing, const double *origin,
+                      ff_field phi, ff_field wu, ff_field wv, ff_field ww);
+
+/* ---- test hooks mirroring the exported multigrid.js / linalg.js pieces -- */
+/* createLaplacianOperator (multigrid.js:457-471): y = A x with the solver's
+ * current level-0 system (call ff_pressure3_prepare first).                 */
+int ff_pressure3_prepare(ff_pressure ps, ff_field u_in, ff_field v_in, ff_field w_in);
+int ff_laplacian_apply(ff_pressure ps, ff_field x, ff_field y);
+/* One application of the preconditioner z = M r (the V-cycle,
+ * multigrid.js:1589-1642, or Jacobi / identity, :568-619).                 */
+int ff_precondition_apply(ff_pressure ps, ff_field r, ff_field z);
+/* buildRestrictKernel / buildCorrectKernel (multigrid.js:866-914, 990-1040)
+ * on a level of the prepared hierarchy: coarse = R fine, fine += P coarse.  */
+int ff_mg_restrict(ff_pressure ps, int fine_level, ff_field fine, ff_field coarse);
+int ff_mg_prolong_add(ff_pressure ps, int fine_level, ff_field coarse, ff_field fine);
+/* Coarsened mask / weights of a level (refreshCoarseLevels, :1416-1452).   */
+int ff_mg_level_info(ff_pressure ps, int level, int *shape3);
+/* Average device time (CUDA events, context stream) of one launch of a
+ * kernel family on the solver's level-0 buffers: the per-dispatch timing of
+ * fluxflow src/profiling.js:92-149.  Call after a project() or prepare().  */
+#define FF_PROF_P_PAP 0          /* p = z + beta p, A p, p.Ap           */
+#define FF_PROF_X_RESIDUAL 1     /* x += alpha p, r = b - A x, r.r      */
+#define FF_PROF_RELAX 2          /* one red-black colour pass, level 0  */
+#define FF_PROF_RESIDUAL 3       /* V-cycle residual, level 0           */
+#define FF_PROF_RESTRICT 4       /* level 0 -> 1                        */
+#define FF_PROF_PROLONG 5        /* level 1 -> 0                        */
+#define FF_PROF_RZ 6             /* r.z and beta                        */
+#define FF_PROF_PRECONDITIONER 7 /* one whole V-cycle                   */
+#define FF_PROF_ITERATION 8      /* one whole PCG iteration             */
+int ff_pressure3_profile(ff_pressure ps, int which, int reps, float *avg_ms);
+int ff_mg_level_download(ff_pressure ps, int level, uint8_t *mask, float *wu, float *wv, float *ww);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,348 @@
+"""ctypes front end of the FP64 CPU oracle (test infrastructure only).
+
+Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline arm of bench.py
+import this module, and only as the checker.  The product library never
+loads it.  Arrays are numpy, i-fastest (Fortran order of (nx, ny, nz)),
+flattened: cell (i,j,k) -> i + nx*(j + ny*k).
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+_dp = C.POINTER(C.c_double)
+_u8p = C.POINTER(C.c_uint8)
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "liboracle.so")
+        srcs = [os.path.join(_HERE, f) for f in os.listdir(_HERE) if f.endswith((".c", ".h"))]
+        if not os.path.exists(path) or any(os.path.getmtime(s) > os.path.getmtime(path) for s in srcs):
+            build()
+        _LIB = C.CDLL(path)
+        _declare(_LIB)
+    return _LIB
+
+
+class MgOpts(C.Structure):
+    _fields_ = [("levels", C.c_int), ("down", C.c_int), ("up", C.c_int),
+                ("coarsest", C.c_int), ("final_iters", C.c_int), ("sor", C.c_double),
+                ("coarsen_mask", C.c_int), ("coarsen_weights", C.c_int),
+                ("coarse_direct", C.c_int), ("store_bf16", C.c_int)]
+
+
+class PcgResult(C.Structure):
+    _fields_ = [("converged", C.c_int), ("iterations", C.c_int), ("stop_code", C.c_int),
+                ("stopped_by", C.c_int), ("rr", C.c_double), ("bb", C.c_double),
+                ("residual", C.c_double)]
+
+
+def _declare(L):
+    I, D = C.c_int, C.c_double
+    L.orc_laplacian.argtypes = [I, I, I, D, D, D, _dp, _u8p, _dp, _dp, _dp, _dp]
+    L.orc_laplacian_diag.argtypes = [I, I, I, D, D, D, _u8p, _dp, _dp, _dp, _dp]
+    L.orc_cpuref_apply.argtypes = [I, I, D, D, _dp, _u8p, _dp, I]
+    L.orc_cpuref_cg.argtypes = [I, I, D, D, _dp, _u8p, _dp, _dp, I, I, I, I, _dp]
+    L.orc_cpuref_cg.restype = I
+    L.orc_mg_create.argtypes = [I, I, I, D, D, D, C.POINTER(MgOpts)]
+    L.orc_mg_create.restype = C.c_void_p
+    L.orc_mg_destroy.argtypes = [C.c_void_p]
+    L.orc_mg_set_system.argtypes = [C.c_void_p, _u8p, _u8p, _dp, _dp, _dp]
+    L.orc_mg_refresh.argtypes = [C.c_void_p]
+    L.orc_mg_apply.argtypes = [C.c_void_p, _dp, _dp]
+    L.orc_mg_level_shape.argtypes = [C.c_void_p, I, C.POINTER(C.c_int)]
+    L.orc_mg_level_mask.argtypes = [C.c_void_p, I, _u8p]
+    L.orc_mg_level_weights.argtypes = [C.c_void_p, I, I, _dp]
+    L.orc_restrict.argtypes = [I, I, I, _dp, _u8p, _u8p, _dp]
+    L.orc_prolong_add.argtypes = [I, I, I, _dp, _u8p, _dp]
+    L.orc_pcg_solve.argtypes = [I, I, I, D, D, D, _u8p, _dp, _dp, _dp, C.c_void_p, I, _dp,
+                                _dp, D, I, I, C.POINTER(C.c_int), C.POINTER(PcgResult)]
+    L.orc_pcg_solve.restype = I
+    L.orc_dirichlet_fields.argtypes = [I, I, I, _u8p, _dp, _dp, _dp, _dp, _u8p, _dp, _u8p]
+    L.orc_build_system.argtypes = [I, I, I, D, D, D, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                                   _dp, _u8p, _dp, _dp, _dp]
+    L.orc_correct.argtypes = [I, I, I, D, D, D, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                              _dp, _dp, _dp, _dp]
+    L.orc_count_bad.argtypes = [I, _dp, D]
+    L.orc_count_bad.restype = I
+    L.orc_round_bf16.argtypes = [C.c_float]
+    L.orc_round_bf16.restype = C.c_float
+    L.orc_fraction_inside.argtypes = [D, D, D, D]
+    L.orc_fraction_inside.restype = D
+    fp = C.POINTER(C.c_float)
+    L.orc_collider_bake.argtypes = [_dp, I, I, I, I, I, D, D, D, D, D, D, fp, fp, fp, fp]
+
+
+def _shape_row(s):
+    row = [0.0] * 13
+    row[0] = 0.0 if s["type"] == "sphere" else 1.0
+    row[1:4] = [float(v) for v in s["center"]]
+    if s["type"] == "sphere":
+        row[4] = float(s["radius"])
+    else:
+        row[5:8] = [float(v) for v in s["halfExtents"]]
+        rot = s.get("rotation")
+        if rot:
+            row[8] = 1.0
+            row[9:12] = [float(v) for v in rot["axis"]]
+            row[12] = float(rot["angle"])
+    return row
+
+
+def collider_bake(shapes, shape, h, origin=(0.0, 0.0, 0.0), invert=False):
+    """createSDFStaticCollider3.addShapes + computeFaceWeights restated:
+    returns (phi, wu, wv, ww) as float32 arrays."""
+    nx, ny, nz = shape
+    rows = np.array([_shape_row(s) for s in shapes] or [[0.0] * 13], np.float64).ravel()
+    phi = np.empty(nx * ny * nz, np.float32)
+    wu = np.empty((nx + 1) * ny * nz, np.float32)
+    wv = np.empty(nx * (ny + 1) * nz, np.float32)
+    ww = np.empty(nx * ny * (nz + 1), np.float32)
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    lib().orc_collider_bake(rows.ctypes.data_as(_dp), len(shapes), int(invert), nx, ny, nz,
+                            *h, *origin, fp(phi), fp(wu), fp(wv), fp(ww))
+    return phi, wu, wv, ww
+
+
+def _d(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def _u8(a):
+    if a is None:
+        return None
+    assert a.dtype == np.uint8 and a.flags.c_contiguous
+    return a.ctypes.data_as(_u8p)
+
+
+def f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64).ravel()
+
+
+def u8(a):
+    return None if a is None else np.ascontiguousarray(np.asarray(a) != 0, dtype=np.uint8).ravel()
+
+
+def shape3(shape):
+    return (shape[0], shape[1], shape[2] if len(shape) > 2 else 1)
+
+
+def spacing3(h):
+    h = list(h) if hasattr(h, "__len__") else [h, h, h]
+    return (h[0], h[1], h[2] if len(h) > 2 else 1.0)
+
+
+def laplacian(shape, h, x, mask=None, weights=None):
+    nx, ny, nz = shape3(shape)
+    hx, hy, hz = spacing3(h)
+    x = f64(x)
+    out = np.empty_like(x)
+    wu, wv, ww = (f64(w) for w in weights) if weights is not None else (None, None, None)
+    if weights is not None and nz == 1:
+        ww = None
+    lib().orc_laplacian(nx, ny, nz, hx, hy, hz, _d(x), _u8(u8(mask)), _d(wu), _d(wv), _d(ww), _d(out))
+    return out
+
+
+def laplacian_diag(shape, h, mask=None, weights=None):
+    nx, ny, nz = shape3(shape)
+    hx, hy, hz = spacing3(h)
+    out = np.empty(nx * ny * nz)
+    wu, wv, ww = (f64(w) for w in weights) if weights is not None else (None, None, None)
+    lib().orc_laplacian_diag(nx, ny, nz, hx, hy, hz, _u8(u8(mask)), _d(wu), _d(wv), _d(ww), _d(out))
+    return out
+
+
+def cpuref_apply(shape, h, x, pinned, round_f32=False):
+    nx, ny = shape[0], shape[1]
+    x = f64(x)
+    out = np.empty_like(x)
+    lib().orc_cpuref_apply(nx, ny, h[0], h[1], _d(x), _u8(u8(pinned)), _d(out), int(round_f32))
+    return out
+
+
+def cpuref_cg(shape, h, b, pinned, x0=None, round_f32=False, dot_kind=0, max_iter=40000,
+              recompute_every=0):
+    nx, ny = shape[0], shape[1]
+    b = f64(b)
+    xo = np.empty_like(b)
+    rel = C.c_double()
+    it = lib().orc_cpuref_cg(nx, ny, h[0], h[1], _d(b), _u8(u8(pinned)), _d(f64(x0)), _d(xo),
+                             int(round_f32), dot_kind, max_iter, recompute_every, C.byref(rel))
+    return it, rel.value, xo
+
+
+def mg_opts(levels=1, down=2, up=2, coarsest=20, final_iters=2, sor=1.0, coarsen_mask=True,
+            coarsen_weights=True, coarse_direct=False, store_bf16=False):
+    return MgOpts(levels, down, up, coarsest, final_iters, sor, int(coarsen_mask),
+                  int(coarsen_weights), int(coarse_direct), int(store_bf16))
+
+
+class Multigrid:
+    """createMultigridPreconditioner (multigrid.js:1213-1735) restated in FP64."""
+
+    def __init__(self, shape, h, mask=None, vent=None, weights=None, **opts):
+        self.shape = shape3(shape)
+        self.h = spacing3(h)
+        self._o = mg_opts(**opts)
+        self._p = lib().orc_mg_create(*self.shape, *self.h, C.byref(self._o))
+        if not self._p:
+            raise ValueError("multigrid: shape not divisible by 2^(levels-1)")
+        self._keep = []
+        self.set_system(mask, vent, weights)
+
+    def set_system(self, mask=None, vent=None, weights=None):
+        m, v = u8(mask), u8(vent)
+        if weights is not None:
+            wu, wv = f64(weights[0]), f64(weights[1])
+            ww = f64(weights[2]) if self.shape[2] > 1 else None
+        else:
+            wu = wv = ww = None
+        self._keep = [m, v, wu, wv, ww]
+        lib().orc_mg_set_system(self._p, _u8(m), _u8(v), _d(wu), _d(wv), _d(ww))
+        lib().orc_mg_refresh(self._p)
+
+    def apply(self, r):
+        r = f64(r)
+        z = np.empty_like(r)
+        lib().orc_mg_apply(self._p, _d(r), _d(z))
+        return z
+
+    def level_shape(self, level):
+        s = (C.c_int * 3)()
+        lib().orc_mg_level_shape(self._p, level, s)
+        return tuple(s)
+
+    def level_mask(self, level):
+        nx, ny, nz = self.level_shape(level)
+        out = np.empty(nx * ny * nz, np.uint8)
+        lib().orc_mg_level_mask(self._p, level, _u8(out))
+        return out
+
+    def level_weights(self, level, axis):
+        nx, ny, nz = self.level_shape(level)
+        n = (nx + (axis == 0)) * (ny + (axis == 1)) * (nz + (axis == 2))
+        out = np.empty(n)
+        lib().orc_mg_level_weights(self._p, level, axis, _d(out))
+        return out
+
+    def __del__(self):
+        try:
+            if self._p:
+                lib().orc_mg_destroy(self._p)
+                self._p = None
+        except Exception:
+            pass
+
+
+def restrict(fine_shape, fine, fine_mask=None, coarse_mask=None):
+    nx, ny, nz = shape3(fine_shape)
+    cn = (nx // 2) * (ny // 2) * (nz // 2 if nz > 1 else 1)
+    out = np.empty(cn)
+    lib().orc_restrict(nx, ny, nz, _d(f64(fine)), _u8(u8(fine_mask)), _u8(u8(coarse_mask)), _d(out))
+    return out
+
+
+def prolong_add(fine_shape, coarse, fine, fine_mask=None):
+    nx, ny, nz = shape3(fine_shape)
+    fine = f64(fine).copy()
+    lib().orc_prolong_add(nx, ny, nz, _d(f64(coarse)), _u8(u8(fine_mask)), _d(fine))
+    return fine
+
+
+PRE = {"multigrid": 0, "jacobi": 1, "none": 2}
+STOP_NAMES = {0: "none", 1: "degenerate-pAp", 2: "pAp-growth", 3: "alpha-magnitude",
+              4: "degenerate-oldRZ", 5: "converged", 6: "residual-growing"}
+
+
+def pcg_solve(shape, h, b, x0=None, mask=None, weights=None, mg=None, preconditioner="multigrid",
+              tol=1e-6, max_iter=100, relative=True, last_iters=4):
+    """GPU-resident chunked PCG (linalg.js:1651-1911) in FP64.  Returns
+    (x, result dict, last_iters)."""
+    nx, ny, nz = shape3(shape)
+    hx, hy, hz = spacing3(h)
+    b = f64(b)
+    x = np.zeros_like(b) if x0 is None else f64(x0).copy()
+    m = u8(mask)
+    if weights is not None:
+        wu, wv = f64(weights[0]), f64(weights[1])
+        ww = f64(weights[2]) if nz > 1 else None
+    else:
+        wu = wv = ww = None
+    last = C.c_int(last_iters)
+    res = PcgResult()
+    lib().orc_pcg_solve(nx, ny, nz, hx, hy, hz, _u8(m), _d(wu), _d(wv), _d(ww),
+                        mg._p if mg is not None else None, PRE[preconditioner], _d(b), _d(x),
+                        tol, max_iter, int(relative), C.byref(last), C.byref(res))
+    out = dict(converged=bool(res.converged), iterations=res.iterations,
+               stop_code=res.stop_code, stopped_by=STOP_NAMES[res.stopped_by],
+               rr=res.rr, bb=res.bb, residual=res.residual)
+    return x, out, last.value
+
+
+def dirichlet_fields(shape, active=None, target=None, collider_weights=None):
+    nx, ny, nz = shape3(shape)
+    n = nx * ny * nz
+    mask, vent, tgt = np.empty(n, np.uint8), np.empty(n, np.uint8), np.empty(n)
+    cw = [f64(w) for w in collider_weights] if collider_weights is not None else [None] * 3
+    if nz == 1:
+        cw[2] = None
+    lib().orc_dirichlet_fields(nx, ny, nz, _u8(u8(active)), _d(f64(target)), _d(cw[0]), _d(cw[1]),
+                               _d(cw[2]), _u8(mask), _d(tgt), _u8(vent))
+    return mask, tgt, vent
+
+
+def build_system(shape, h, u, v, w, collider_weights=None, face_weights=None, mask=None,
+                 target=None, p=None):
+    nx, ny, nz = shape3(shape)
+    hx, hy, hz = spacing3(h)
+    n = nx * ny * nz
+    b = np.empty(n)
+    p = np.zeros(n) if p is None else f64(p).copy()
+    cw = [f64(a) for a in collider_weights] if collider_weights is not None else [None] * 3
+    fw = [f64(a) for a in face_weights] if face_weights is not None else [None] * 3
+    w = f64(w) if w is not None else None
+    lib().orc_build_system(nx, ny, nz, hx, hy, hz, _d(f64(u)), _d(f64(v)), _d(w),
+                           _d(cw[0]), _d(cw[1]), _d(cw[2]), _d(fw[0]), _d(fw[1]), _d(fw[2]),
+                           _u8(u8(mask)), _d(f64(target) if target is not None else np.zeros(n)),
+                           _d(b), _d(p))
+    return b, p
+
+
+def correct(shape, h, p, u, v, w, face_weights=None, collider_weights=None):
+    nx, ny, nz = shape3(shape)
+    hx, hy, hz = spacing3(h)
+    u, v = f64(u), f64(v)
+    w = f64(w) if w is not None else np.zeros(1)
+    uo, vo, wo = u.copy(), v.copy(), w.copy()
+    cw = [f64(a) for a in collider_weights] if collider_weights is not None else [None] * 3
+    fw = [f64(a) for a in face_weights] if face_weights is not None else [None] * 3
+    lib().orc_correct(nx, ny, nz, hx, hy, hz, _d(f64(p)), _d(fw[0]), _d(fw[1]), _d(fw[2]),
+                      _d(cw[0]), _d(cw[1]), _d(cw[2]), _d(u), _d(v), _d(w), _d(uo), _d(vo), _d(wo))
+    return uo, vo, wo
+
+
+def count_bad(p, max_plausible=1e6):
+    p = f64(p)
+    return lib().orc_count_bad(p.size, _d(p), max_plausible)
+
+
+def round_bf16(a):
+    a = np.asarray(a, np.float32)
+    u = a.view(np.uint32).astype(np.uint64)
+    lsb = (u >> 16) & 1
+    r = ((u + 0x7FFF + lsb) & 0xFFFF0000).astype(np.uint32)
+    return r.view(np.float32)

@@ -1,0 +1,173 @@
+"""Pressure projection on the GPU through the C ABI, compared with the FP64
+oracle on the same inputs.  Tolerances are stated per test: FP32 kernels
+against FP64 restatements agree to FP32 rounding; BF16 V-cycle storage to
+its 8-bit mantissa; solutions to the solver tolerance."""
+import numpy as np
+import pytest
+
+from conftest import load_stalled
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def stalled_solver(frame, levels=4, down=3, up=3, coarsest=30, coarse="sweeps", precision="fp32",
+                   preconditioner="multigrid", tol=1e-5):
+    from tsl_array_n_gb300 import fluxflow as ff
+    from tsl_array_n_gb300.tsl_array_n import Field
+    meta, a = load_stalled(frame)
+    shape = tuple(meta["resolution"])
+    cw = {"u": Field("float", meta["dataSizeU"]).from_array(a["weightU"]),
+          "v": Field("float", meta["dataSizeV"]).from_array(a["weightV"]),
+          "w": Field("float", meta["dataSizeW"]).from_array(a["weightW"])}
+    vent = a["ventMask"] > 0.5
+    s = ff.create_grid_pressure_solver3(
+        shape, meta["gridSpacing"], collider_weights=cw, dirichlet=(vent, np.zeros(vent.size)),
+        multigrid={"numberOfLevels": levels, "numberOfSmoothingIterationsDown": down,
+                   "numberOfSmoothingIterationsUp": up, "numberOfCoarsestIterations": coarsest,
+                   "coarseSolve": coarse},
+        precision=precision, preconditioner=preconditioner, tolerance=tol, max_iterations=3000)
+    s.prepare()
+    return s, meta, a, cw
+
+
+def test_level0_system_matches_fixture(gpu):
+    s, meta, a, _ = stalled_solver(110)
+    mask = s.dirichlet_mask.to_array()
+    assert np.array_equal(mask.astype(bool), a["dirichletMask"] > 0.5)
+
+
+def test_laplacian_parity(gpu, oracle):
+    from tsl_array_n_gb300.tsl_array_n import Field
+    s, meta, a, _ = stalled_solver(110)
+    shape = tuple(meta["resolution"])
+    mask = a["dirichletMask"] > 0.5
+    w = (a["weightU"], a["weightV"], a["weightW"])
+    for x in (a["pressure"], np.random.default_rng(0).standard_normal(a["b"].size)):
+        xf = Field("float", shape).from_array(x.astype(np.float32))
+        yf = Field("float", shape)
+        s.apply_laplacian(xf, yf)
+        ref = oracle.laplacian(shape, meta["gridSpacing"], x.astype(np.float32).astype(np.float64), mask, w)
+        assert rel(yf.to_array(), ref) < 2e-6
+
+
+@pytest.mark.parametrize("coarse", ["sweeps", "direct"])
+def test_coarsened_levels_match_oracle(gpu, oracle, coarse):
+    s, meta, a, _ = stalled_solver(110, coarse=coarse)
+    shape = tuple(meta["resolution"])
+    mask, vent = a["dirichletMask"] > 0.5, a["ventMask"] > 0.5
+    w = (a["weightU"], a["weightV"], a["weightW"])
+    mg = oracle.Multigrid(shape, meta["gridSpacing"], mask, vent, w, levels=4)
+    for level in range(1, 4):
+        m, ws = s.level_data(level)
+        assert np.array_equal(m, mg.level_mask(level)), level
+        for axis in range(3):
+            np.testing.assert_allclose(ws[axis], mg.level_weights(level, axis), rtol=1e-6, atol=1e-7)
+
+
+@pytest.mark.parametrize("coarse,tol", [("sweeps", 2e-5), ("direct", 2e-5)])
+def test_vcycle_parity_fp32(gpu, oracle, coarse, tol):
+    """One application of the V-cycle, FP32 GPU against the FP64 oracle."""
+    from tsl_array_n_gb300.tsl_array_n import Field
+    s, meta, a, _ = stalled_solver(110, coarse=coarse)
+    shape = tuple(meta["resolution"])
+    mask, vent = a["dirichletMask"] > 0.5, a["ventMask"] > 0.5
+    w = (a["weightU"], a["weightV"], a["weightW"])
+    mg = oracle.Multigrid(shape, meta["gridSpacing"], mask, vent, w, levels=4, down=3, up=3,
+                          coarsest=30, final_iters=2, coarse_direct=(coarse == "direct"))
+    r = a["b"].astype(np.float32)
+    rf, zf = Field("float", shape).from_array(r), Field("float", shape)
+    s.apply_preconditioner(rf, zf)
+    z_ref = mg.apply(r.astype(np.float64))
+    assert rel(zf.to_array(), z_ref) < tol
+
+
+def test_vcycle_parity_bf16(gpu, oracle):
+    """BF16 storage: the oracle rounds the same arrays to BF16; agreement is
+    limited by BF16's 8-bit mantissa."""
+    from tsl_array_n_gb300.tsl_array_n import Field
+    s, meta, a, _ = stalled_solver(110, coarse="direct", precision="mixed")
+    shape = tuple(meta["resolution"])
+    mask, vent = a["dirichletMask"] > 0.5, a["ventMask"] > 0.5
+    w = (a["weightU"], a["weightV"], a["weightW"])
+    mg = oracle.Multigrid(shape, meta["gridSpacing"], mask, vent, w, levels=4, down=3, up=3,
+                          final_iters=2, coarse_direct=True, store_bf16=True)
+    r = a["b"].astype(np.float32)
+    rf, zf = Field("float", shape).from_array(r), Field("float", shape)
+    s.apply_preconditioner(rf, zf)
+    assert rel(zf.to_array(), mg.apply(r.astype(np.float64))) < 2e-2
+
+
+@pytest.mark.parametrize("precision,coarse", [("fp32", "sweeps"), ("fp32", "direct"),
+                                              ("mixed", "direct")])
+def test_solve_frame112(gpu, oracle, precision, coarse):
+    """The frozen frame-112 system: converges to 1e-5 relative like the FP64
+    oracle, in a comparable number of iterations, and the returned pressure's
+    true FP64 residual meets the tolerance."""
+    from tsl_array_n_gb300.tsl_array_n import Field
+    s, meta, a, _ = stalled_solver(112, coarse=coarse, precision=precision)
+    shape, h = tuple(meta["resolution"]), meta["gridSpacing"]
+    mask, vent = a["dirichletMask"] > 0.5, a["ventMask"] > 0.5
+    w = (a["weightU"], a["weightV"], a["weightW"])
+    s.pressure.fill(0.0)
+    bf = Field("float", shape).from_array(a["b"].astype(np.float32))
+    d = s.solve(bf)
+    assert d["converged"] and not d["rejected"], d
+    mg = oracle.Multigrid(shape, h, mask, vent, w, levels=4, down=3, up=3, coarsest=30,
+                          final_iters=2, coarse_direct=(coarse == "direct"))
+    _, ro, _ = oracle.pcg_solve(shape, h, a["b"].astype(np.float32).astype(np.float64), None, mask, w,
+                                mg, "multigrid", tol=1e-5, max_iter=3000)
+    assert abs(d["iterations"] - ro["iterations"]) <= 3
+    p = s.pressure.to_array().astype(np.float64)
+    b64 = a["b"].astype(np.float32).astype(np.float64)
+    true_rel = np.linalg.norm(b64 - oracle.laplacian(shape, h, p, mask, w)) / np.linalg.norm(b64)
+    assert true_rel < 1.2e-5
+
+
+@pytest.mark.parametrize("pre", ["jacobi", "none"])
+def test_cheap_preconditioners(gpu, oracle, pre):
+    from tsl_array_n_gb300.tsl_array_n import Field
+    s, meta, a, _ = stalled_solver(110, preconditioner=pre)
+    shape, h = tuple(meta["resolution"]), meta["gridSpacing"]
+    mask = a["dirichletMask"] > 0.5
+    w = (a["weightU"], a["weightV"], a["weightW"])
+    s.pressure.fill(0.0)
+    d = s.solve(Field("float", shape).from_array(a["b"].astype(np.float32)))
+    _, ro, _ = oracle.pcg_solve(shape, h, a["b"].astype(np.float32).astype(np.float64), None, mask, w,
+                                None, pre, tol=1e-5, max_iter=3000)
+    assert d["converged"] == ro["converged"]
+    assert abs(d["iterations"] - ro["iterations"]) <= max(3, 0.1 * ro["iterations"])
+
+
+def test_guard_nan_rhs_is_reported_not_thrown(gpu, oracle):
+    """A NaN right-hand side trips a guard (degenerate pAp) and leaves the
+    pressure untouched; the oracle reports the same stop code."""
+    from tsl_array_n_gb300.tsl_array_n import Field
+    s, meta, a, _ = stalled_solver(110)
+    shape, h = tuple(meta["resolution"]), meta["gridSpacing"]
+    b = a["b"].astype(np.float32).copy()
+    b[100] = np.nan
+    s.pressure.fill(0.5)
+    d = s.solve(Field("float", shape).from_array(b))
+    assert not d["converged"]
+    assert d["stoppedBy"] == "degenerate-pAp"
+    assert np.all(s.pressure.to_array() == 0.5)
+
+
+def test_circuit_breaker_restores_snapshot(gpu):
+    """A right-hand side that drives |p| past maxPlausiblePressure is
+    rejected and the previous accepted pressure is restored
+    (grid_pressure_solver3.js:547-554)."""
+    from tsl_array_n_gb300.tsl_array_n import Field
+    s, meta, a, _ = stalled_solver(110)
+    shape = tuple(meta["resolution"])
+    s.pressure.fill(0.0)
+    d = s.solve(Field("float", shape).from_array(a["b"].astype(np.float32)))
+    assert d["converged"] and not d["rejected"]
+    good = s.pressure.to_array().copy()
+    d = s.solve(Field("float", shape).from_array((a["b"] * 1e9).astype(np.float32)))
+    assert d["rejected"] and d["badCells"] > 0
+    np.testing.assert_array_equal(s.pressure.to_array(), good)

@@ -1,0 +1,614 @@
+// CG vector kernels with fused FP64 reductions and the GPU-resident scalar
+// logic of fluxflow's PCG (src/linalg/linalg.js:1147-1311), plus the
+// pressure-projection build / correct / circuit-breaker kernels
+// (src/grid/grid_pressure_solver3.js:163-494).
+#include "ff_device.cuh"
+#include <cstdio>
+
+using namespace ffd;
+
+namespace {
+
+constexpr double MAX_BETA_MAGNITUDE = 10.0;     // linalg.js:226
+constexpr double MAX_ALPHA_MAGNITUDE = 1e6;     // linalg.js:244
+constexpr double MAX_PAP_GROWTH_FACTOR = 1e8;   // linalg.js:284
+constexpr double PAP_BASELINE_FLOOR = 1e-12;    // linalg.js:1052
+constexpr double MAX_RESIDUAL_GROWTH = 100.0;   // linalg.js:1095
+
+struct Cell {
+    int i, j, k;
+    long long c;
+    bool ok;
+};
+__device__ __forceinline__ Cell cell3(const Dims &d) {
+    Cell q;
+    q.i = blockIdx.x * blockDim.x + threadIdx.x;
+    q.j = blockIdx.y * blockDim.y + threadIdx.y;
+    q.k = blockIdx.z;
+    q.ok = q.i < d.nx && q.j < d.ny;
+    q.c = (long long)q.i + (long long)d.nx * ((long long)q.j + (long long)d.ny * q.k);
+    return q;
+}
+
+// Plain FP32 operator, difference form: sum_f K_f (v_n - v_c) - E v_c.
+// V(idx) must return the operand at a linear cell index.
+template <class VF>
+__device__ __forceinline__ float apply_plain(const Dims &d, const Cell &q, const float4 *coef,
+                                             float vc, VF V) {
+    const long long sy = d.nx, sz = (long long)d.nx * d.ny;
+    float4 kc = __ldg(coef + q.c);
+    float s = -kc.w * vc;
+    if (q.i > 0) s += kc.x * (V(q.c - 1) - vc);
+    if (q.i < d.nx - 1) s += __ldg(&coef[q.c + 1].x) * (V(q.c + 1) - vc);
+    if (q.j > 0) s += kc.y * (V(q.c - sy) - vc);
+    if (q.j < d.ny - 1) s += __ldg(&coef[q.c + sy].y) * (V(q.c + sy) - vc);
+    if (q.k > 0) s += kc.z * (V(q.c - sz) - vc);
+    if (q.k < d.nz - 1) s += __ldg(&coef[q.c + sz].z) * (V(q.c + sz) - vc);
+    return s;
+}
+
+// Compensated operator on a double-single operand (hi + lo): every product
+// and sum is carried as an unevaluated pair (TwoProd / TwoSum), so the
+// result is accurate to ~eps^2 of the individual flux terms.  Returns b - Ax
+// rounded to FP32.
+template <class XF>
+__device__ __forceinline__ float residual_ds(const Dims &d, const Cell &q, const float4 *coef,
+                                             float b, float hc, float lc, XF X) {
+    const long long sy = d.nx, sz = (long long)d.nx * d.ny;
+    float4 kc = __ldg(coef + q.c);
+    float S = 0.f, Se = 0.f;
+    auto term = [&](float K, long long n) {
+        float hn, ln;
+        X(n, hn, ln);
+        float dh, de;
+        two_sum(hn, -hc, dh, de);
+        de = __fadd_rn(de, __fsub_rn(ln, lc));
+        float p, pe;
+        two_prod(K, dh, p, pe);
+        pe = __fmaf_rn(K, de, pe);
+        float s, e;
+        two_sum(S, p, s, e);
+        S = s;
+        Se = __fadd_rn(Se, __fadd_rn(e, pe));
+    };
+    if (q.i > 0) term(kc.x, q.c - 1);
+    if (q.i < d.nx - 1) term(__ldg(&coef[q.c + 1].x), q.c + 1);
+    if (q.j > 0) term(kc.y, q.c - sy);
+    if (q.j < d.ny - 1) term(__ldg(&coef[q.c + sy].y), q.c + sy);
+    if (q.k > 0) term(kc.z, q.c - sz);
+    if (q.k < d.nz - 1) term(__ldg(&coef[q.c + sz].z), q.c + sz);
+    {   // - E * (hc + lc)
+        float p, pe;
+        two_prod(-kc.w, hc, p, pe);
+        pe = __fmaf_rn(-kc.w, lc, pe);
+        float s, e;
+        two_sum(S, p, s, e);
+        S = s;
+        Se = __fadd_rn(Se, __fadd_rn(e, pe));
+    }
+    float r0, e0;
+    two_sum(b, -S, r0, e0);
+    return __fadd_rn(r0, __fsub_rn(e0, Se));
+}
+
+// ----------------------------------------------------------------- setup --
+// Ax, r = b - Ax, r.r and b.b (linalg.js:1627-1637 setupSequence, first half).
+__global__ void k_setup_residual(Dims d, const float4 *__restrict__ coef,
+                                 const float *__restrict__ b, const float *__restrict__ xh,
+                                 const float *__restrict__ xl, float *__restrict__ r,
+                                 PcgState *st, double *partials, int ds) {
+    Cell q = cell3(d);
+    double v[2] = {0.0, 0.0};
+    if (q.ok) {
+        float bc = __ldg(b + q.c);
+        float rc;
+        if (ds) {
+            rc = residual_ds(d, q, coef, bc, __ldg(xh + q.c), __ldg(xl + q.c),
+                             [&](long long n, float &h, float &l) { h = __ldg(xh + n); l = __ldg(xl + n); });
+        } else {
+            float xc = __ldg(xh + q.c);
+            rc = bc - apply_plain(d, q, coef, xc, [&](long long n) { return __ldg(xh + n); });
+        }
+        r[q.c] = rc;
+        v[0] = (double)rc * (double)rc;
+        v[1] = (double)bc * (double)bc;
+    }
+    double tot[2];
+    if (grid_reduce<2>(v, partials, &st->ticket[0], tot)) {
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            st->rr = tot[0];
+            st->bb = tot[1];
+            double nb = sqrt(fabs(tot[1]));
+            st->thr = st->relative ? fmax(st->tol * nb, st->tol) : st->tol;
+        }
+    }
+}
+
+// ------------------------------------------------------ p = z + beta p; pAp --
+template <class ZT>
+__global__ void k_update_p_pap(Dims d, const float4 *__restrict__ coef, const ZT *__restrict__ z,
+                               float *p0, float *p1, PcgState *st, double *partials) {
+    if (st->stop) return;
+    const int pc = st->p_cur;
+    const float *pold = pc ? p1 : p0;
+    float *pnew = pc ? p0 : p1;
+    const float beta = (float)st->beta;
+    const bool first = st->first != 0;
+    Cell q = cell3(d);
+    double v[1] = {0.0};
+    if (q.ok) {
+        auto P = [&](long long n) {
+            float zn = ld(z, n);
+            return first ? zn : __fmaf_rn(beta, __ldg(pold + n), zn);
+        };
+        float pc_ = P(q.c);
+        float ap = apply_plain(d, q, coef, pc_, P);
+        pnew[q.c] = pc_;
+        v[0] = (double)pc_ * (double)ap;
+    }
+    double tot[1];
+    if (grid_reduce<1>(v, partials, &st->ticket[1], tot)) {
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            // alphaKernel (linalg.js:1147-1199)
+            double pAp = tot[0];
+            double value = st->rz_old / pAp;
+            int code = 0;
+            if (nonfinite_d(pAp) || pAp == 0.0) code = FF_STOP_DEGENERATE_PAP;
+            else if (fabs(pAp) > st->pap_baseline * MAX_PAP_GROWTH_FACTOR) code = FF_STOP_PAP_GROWTH;
+            else if (nonfinite_or_above(value, MAX_ALPHA_MAGNITUDE)) code = FF_STOP_ALPHA_MAGNITUDE;
+            st->pAp = pAp;
+            st->alpha = (st->stop != 0 || code != 0) ? 0.0 : value;
+            if (st->stop == 0) st->stop = code;
+            st->p_cur = pc ^ 1;
+            st->first = 0;
+        }
+    }
+}
+
+// ------------------------------------ x += alpha p; r = b - A x; r.r; stop test
+__global__ void k_update_x_residual(Dims d, const float4 *__restrict__ coef,
+                                    const float *__restrict__ b, const float *p0,
+                                    const float *p1, float *xh0, float *xl0, float *xh1,
+                                    float *xl1, float *__restrict__ r, PcgState *st,
+                                    double *partials, int ds) {
+    if (st->stop) return;
+    const int xc = st->x_cur;
+    const float *p = st->p_cur ? p1 : p0;
+    const float *xh = xc ? xh1 : xh0;
+    const float *xl = xc ? xl1 : xl0;
+    float *oh = xc ? xh0 : xh1;
+    float *ol = xc ? xl0 : xl1;
+    const double alpha = st->alpha;
+    const float ahi = (float)alpha;
+    const float alo = (float)(alpha - (double)ahi);
+    Cell q = cell3(d);
+    double v[1] = {0.0};
+    if (q.ok) {
+        float bc = __ldg(b + q.c);
+        float rc;
+        if (ds) {
+            auto XN = [&](long long n, float &h, float &l) {
+                ds_axpy(xh[n], xl[n], ahi, alo, p[n], h, l);
+            };
+            float hc, lc;
+            XN(q.c, hc, lc);
+            rc = residual_ds(d, q, coef, bc, hc, lc, XN);
+            oh[q.c] = hc;
+            ol[q.c] = lc;
+        } else {
+            auto XN = [&](long long n) { return __fmaf_rn(ahi, p[n], xh[n]); };
+            float x_c = XN(q.c);
+            rc = bc - apply_plain(d, q, coef, x_c, XN);
+            oh[q.c] = x_c;
+        }
+        r[q.c] = rc;
+        v[0] = (double)rc * (double)rc;
+    }
+    double tot[1];
+    if (grid_reduce<1>(v, partials, &st->ticket[2], tot)) {
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            double rr = tot[0];
+            st->rr = rr;
+            st->x_cur = xc ^ 1;
+            st->iter += 1;
+            // residual-growing (linalg.js:1839-1852), checked every iteration
+            if (!nonfinite_d(rr)) {
+                if (st->best_rr < 0.0 || fabs(rr) < st->best_rr) st->best_rr = fabs(rr);
+                else if (st->best_rr > 0.0 && fabs(rr) > st->best_rr * MAX_RESIDUAL_GROWTH &&
+                         st->stop == 0) {
+                    st->growth_stop = 1;
+                }
+            }
+            // convergenceKernel (linalg.js:1283-1311)
+            double res = sqrt(fabs(rr));
+            bool conv = !nonfinite_or_above(res, st->thr);
+            if (conv && st->stop == 0) {
+                st->stop = FF_STOP_CONVERGED;
+                st->stop_iter = st->iter;
+            } else if (st->growth_stop && st->stop == 0) {
+                st->stop = FF_STOP_RESIDUAL_GROWING;
+            }
+        }
+    }
+}
+
+// ----------------------------------------------------------- r.z and beta --
+template <class ZT>
+__global__ void k_rz_beta(Dims d, const float *__restrict__ r, const ZT *__restrict__ z,
+                          PcgState *st, double *partials, int setup) {
+    if (!setup && st->stop) return;
+    long long n = d.n();
+    long long i0 = (long long)blockIdx.x * blockDim.x * 4 + threadIdx.x;
+    double v[1] = {0.0};
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        long long i = i0 + (long long)u * blockDim.x;
+        if (i < n) v[0] += (double)__ldg(r + i) * (double)ld(z, i);
+    }
+    double tot[1];
+    if (grid_reduce<1>(v, partials, &st->ticket[3], tot)) {
+        if (threadIdx.x == 0) {
+            double rz = tot[0];
+            st->rz = rz;
+            if (setup) {
+                // seedScalarsKernel (linalg.js:1259-1267)
+                st->rz_old = rz;
+                st->pap_baseline = fmax(fabs(st->rr), PAP_BASELINE_FLOOR);
+                st->stop = 0;
+                st->iter = 0;
+                st->stop_iter = 0;
+                st->first = 1;
+                st->best_rr = -1.0;
+            } else {
+                // betaKernel (linalg.js:1201-1240)
+                double rz_old = st->rz_old;
+                double value = rz / rz_old;
+                bool degenerate = nonfinite_d(rz_old) || rz_old == 0.0;
+                bool restart = (rz_old * rz < 0.0) || nonfinite_or_above(value, MAX_BETA_MAGNITUDE);
+                bool already = st->stop != 0;
+                st->beta = (already || restart) ? 0.0 : value;
+                if (degenerate && st->stop == 0) st->stop = FF_STOP_DEGENERATE_OLD_RZ;
+                st->rz_old = rz;
+            }
+        }
+    }
+}
+
+__global__ void k_state_init(PcgState *st, double tol, int maxiter, int relative) {
+    PcgState s = {};
+    s.tol = tol;
+    s.maxiter = maxiter;
+    s.relative = relative;
+    s.best_rr = -1.0;
+    *st = s;
+}
+
+__global__ void k_loop_control(PcgState *st, cudaGraphConditionalHandle h, int use_handle) {
+    if (threadIdx.x != 0) return;
+    st->launched += 1;
+    int cont = (st->stop == 0) && (st->iter < st->maxiter) && (st->launched < st->maxiter + 4);
+    if (use_handle) cudaGraphSetConditional(h, cont ? 1u : 0u);
+}
+
+__global__ void k_laplacian(Dims d, const float4 *__restrict__ coef, const float *__restrict__ x,
+                            float *__restrict__ y) {
+    Cell q = cell3(d);
+    if (!q.ok) return;
+    float xc = __ldg(x + q.c);
+    y[q.c] = apply_plain(d, q, coef, xc, [&](long long n) { return __ldg(x + n); });
+}
+
+// createJacobiPreconditioner (multigrid.js:568-604): z = r / diag, identity
+// where the diagonal is zero.
+template <class ZT>
+__global__ void k_jacobi(Dims d, const float4 *__restrict__ coef, const float *__restrict__ r,
+                         ZT *__restrict__ z, const PcgState *st) {
+    if (st && st->stop) return;
+    Cell q = cell3(d);
+    if (!q.ok) return;
+    const long long sy = d.nx, sz = (long long)d.nx * d.ny;
+    float4 kc = __ldg(coef + q.c);
+    float D = -(kc.x + kc.y + kc.z + kc.w);
+    if (q.i < d.nx - 1) D -= __ldg(&coef[q.c + 1].x);
+    if (q.j < d.ny - 1) D -= __ldg(&coef[q.c + sy].y);
+    if (q.k < d.nz - 1) D -= __ldg(&coef[q.c + sz].z);
+    float rc = __ldg(r + q.c);
+    ffd::st(z, q.c, fabsf(D) > 0.f ? rc / D : rc);
+}
+
+template <class ZT>
+__global__ void k_identity(long long n, const float *__restrict__ r, ZT *__restrict__ z,
+                           const PcgState *st) {
+    if (st && st->stop) return;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) ffd::st(z, i, __ldg(r + i));
+}
+
+__global__ void k_fill(float *p, long long n, float v) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+
+// ------------------------------------------------------ pressure build etc --
+// updateDirichletFields (grid_pressure_solver3.js:163-206)
+__global__ void k_dirichlet_fields(Dims d, const uint8_t *active, const float *target,
+                                   const float *cwu, const float *cwv, const float *cww,
+                                   uint8_t *mask, float *tgt, uint8_t *vent) {
+    Cell q = cell3(d);
+    if (!q.ok) return;
+    bool enclosed = false;
+    if (cwu) {
+        long long fu = q.i + (long long)(d.nx + 1) * (q.j + (long long)d.ny * q.k);
+        long long fv = q.i + (long long)d.nx * (q.j + (long long)(d.ny + 1) * q.k);
+        float t = cwu[fu] + cwu[fu + 1] + cwv[fv] + cwv[fv + d.nx];
+        if (d.nz > 1) t += cww[q.c] + cww[q.c + (long long)d.nx * d.ny];
+        enclosed = t < 1e-6f;
+    }
+    bool act = active ? active[q.c] != 0 : false;
+    mask[q.c] = (act || enclosed) ? 1 : 0;
+    tgt[q.c] = act ? (target ? target[q.c] : 0.f) : 0.f;
+    vent[q.c] = act ? 1 : 0;
+}
+
+// systemFaceWeights = faceWeights * colliderWeights (:217-229)
+__global__ void k_system_weights(long long n, const float *fw, const float *cw, float *sw) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float a = fw ? fw[i] : 1.f, c = cw ? cw[i] : 1.f;
+    sw[i] = (fw && cw) ? a * c : (fw ? a : c);
+}
+
+// dispatchBuildSystem (:350-453)
+__global__ void k_build_system(Dims d, float hx, float hy, float hz, const float *u,
+                               const float *v, const float *w, const float *cwu,
+                               const float *cwv, const float *cww, const float *swu,
+                               const float *swv, const float *sww, const uint8_t *mask,
+                               const float *tgt, float *b, float *xh, float *xl) {
+    Cell q = cell3(d);
+    if (!q.ok) return;
+    const long long s = (long long)d.nx * d.ny;
+    long long fu = q.i + (long long)(d.nx + 1) * (q.j + (long long)d.ny * q.k);
+    long long fv = q.i + (long long)d.nx * (q.j + (long long)(d.ny + 1) * q.k);
+    long long fw = q.c;
+    float div;
+    if (cwu) {
+        float lu = u[fu] * cwu[fu], ru = u[fu + 1] * cwu[fu + 1];
+        float lv = v[fv] * cwv[fv], rv = v[fv + d.nx] * cwv[fv + d.nx];
+        div = (ru - lu) / hx + (rv - lv) / hy;
+        if (d.nz > 1) {
+            float lw = w[fw] * cww[fw], rw = w[fw + s] * cww[fw + s];
+            div += (rw - lw) / hz;
+        }
+    } else {
+        div = (u[fu + 1] - u[fu]) / hx + (v[fv + d.nx] - v[fv]) / hy;
+        if (d.nz > 1) div += (w[fw + s] - w[fw]) / hz;
+    }
+    if (!mask) {
+        b[q.c] = div;
+        return;
+    }
+    if (mask[q.c]) {
+        float t = tgt[q.c];
+        b[q.c] = -t;
+        xh[q.c] = t;
+        if (xl) xl[q.c] = 0.f;
+        return;
+    }
+    const float ihx = (float)(1.0 / ((double)hx * hx)), ihy = (float)(1.0 / ((double)hy * hy)),
+                ihz = (float)(1.0 / ((double)hz * hz));
+    float acc = 0.f;
+    if (q.i > 0 && mask[q.c - 1]) acc += (swu ? swu[fu] : 1.f) * tgt[q.c - 1] * ihx;
+    if (q.i < d.nx - 1 && mask[q.c + 1]) acc += (swu ? swu[fu + 1] : 1.f) * tgt[q.c + 1] * ihx;
+    if (q.j > 0 && mask[q.c - d.nx]) acc += (swv ? swv[fv] : 1.f) * tgt[q.c - d.nx] * ihy;
+    if (q.j < d.ny - 1 && mask[q.c + d.nx]) acc += (swv ? swv[fv + d.nx] : 1.f) * tgt[q.c + d.nx] * ihy;
+    if (d.nz > 1) {
+        if (q.k > 0 && mask[q.c - s]) acc += (sww ? sww[fw] : 1.f) * tgt[q.c - s] * ihz;
+        if (q.k < d.nz - 1 && mask[q.c + s]) acc += (sww ? sww[fw + s] : 1.f) * tgt[q.c + s] * ihz;
+    }
+    b[q.c] = div - acc;
+}
+
+// countBadPressureCells (:297-304): non-finite or |p| > maxPlausiblePressure
+__global__ void k_count_bad(long long n, const float *xh0, const float *xh1, PcgState *st,
+                            float maxp) {
+    const float *x = st->x_cur ? xh1 : xh0;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int bad = 0;
+    if (i < n) {
+        float v = x[i];
+        bad = nonfinite_f(v) || !(fabsf(v) <= maxp);
+    }
+    unsigned m = __ballot_sync(0xffffffffu, bad);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(&st->bad_cells, __popc(m));
+}
+
+// finishAccepted / finishRejected (:499-500, :553-554): restore the snapshot
+// when the breaker fired, else take a new one; leave the result in slot 0.
+__global__ void k_commit(long long n, float *xh0, float *xl0, const float *xh1,
+                         const float *xl1, float *sh, float *sl, const PcgState *st) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (st->bad_cells > 0) {
+        xh0[i] = sh[i];
+        if (xl0) xl0[i] = sl ? sl[i] : 0.f;
+    } else {
+        float h = st->x_cur ? xh1[i] : xh0[i];
+        float l = xl0 ? (st->x_cur ? xl1[i] : xl0[i]) : 0.f;
+        xh0[i] = h;
+        if (xl0) xl0[i] = l;
+        sh[i] = h;
+        if (sl) sl[i] = l;
+    }
+}
+
+// dispatchCorrectU/V/W (:457-494): interior faces only, gated by the
+// collider weight, scaled by the face weight (beta).
+__global__ void k_correct_axis(Dims d, int axis, float h, const float *xh, const float *xl,
+                               const float *fw, const float *cw, const float *in, float *out) {
+    int fx = d.nx + (axis == 0), fy = d.ny + (axis == 1);
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    int k = blockIdx.z;
+    if (i >= fx || j >= fy) return;
+    int m = axis == 0 ? i : axis == 1 ? j : k;
+    int nm = axis == 0 ? d.nx : axis == 1 ? d.ny : d.nz;
+    long long f = i + (long long)fx * (j + (long long)fy * k);
+    if (m <= 0 || m >= nm) {
+        if (in != out) out[f] = in[f];
+        return;
+    }
+    long long c = i + (long long)d.nx * (j + (long long)d.ny * k);
+    long long off = axis == 0 ? 1 : axis == 1 ? d.nx : (long long)d.nx * d.ny;
+    float dp = xh[c] - xh[c - off];
+    if (xl) dp += xl[c] - xl[c - off];
+    float g = dp / h;
+    if (fw) g = g * fw[f];
+    if (cw) g = g * (cw[f] > 0.f ? 1.f : 0.f);
+    out[f] = in[f] - g;
+}
+
+}  // namespace
+
+namespace ffk {
+
+static int post(const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return ff_set_error(FF_E_CUDA, "%s launch: %s", what, cudaGetErrorString(e));
+    return FF_OK;
+}
+static unsigned nblocks1(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+int fill_f32(float *p, long long n, float v, cudaStream_t s) {
+    if (n <= 0) return FF_OK;
+    k_fill<<<nblocks1(n, 256), 256, 0, s>>>(p, n, v);
+    return post("fill");
+}
+int copy_bytes(void *dst, const void *src, size_t bytes, cudaStream_t s) {
+    FF_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, s));
+    return FF_OK;
+}
+
+int dirichlet_fields(Dims d, const uint8_t *active, const float *target, const float *cwu,
+                     const float *cwv, const float *cww, uint8_t *mask, float *tgt,
+                     uint8_t *vent, cudaStream_t s) {
+    auto L = launch3(d.nx, d.ny, d.nz);
+    k_dirichlet_fields<<<L.grid, L.block, 0, s>>>(d, active, target, cwu, cwv, cww, mask, tgt, vent);
+    return post("dirichlet_fields");
+}
+
+int system_weights(Dims d, const float *fw[3], const float *cw[3], float *sw[3], cudaStream_t s) {
+    long long nf[3] = {d.nu(), d.nv(), d.nw()};
+    for (int a = 0; a < 3; ++a) {
+        if (!sw[a]) continue;
+        k_system_weights<<<nblocks1(nf[a], 256), 256, 0, s>>>(nf[a], fw[a], cw[a], sw[a]);
+    }
+    return post("system_weights");
+}
+
+int build_system(Dims d, float hx, float hy, float hz, const float *u, const float *v,
+                 const float *w, const float *cw[3], const float *fw[3], const float *sw[3],
+                 const uint8_t *mask, const float *tgt, float *b, float *x_hi, float *x_lo,
+                 cudaStream_t s) {
+    (void)fw;
+    auto L = launch3(d.nx, d.ny, d.nz);
+    k_build_system<<<L.grid, L.block, 0, s>>>(d, hx, hy, hz, u, v, w, cw[0], cw[1], cw[2],
+                                              sw[0], sw[1], sw[2], mask, tgt, b, x_hi, x_lo);
+    return post("build_system");
+}
+
+int count_bad_and_commit(Dims d, float *x_hi0, float *x_lo0, float *x_hi1, float *x_lo1,
+                         float *snap_hi, float *snap_lo, PcgState *st, float max_plausible,
+                         int *bad_count, cudaStream_t s) {
+    (void)bad_count;
+    long long n = d.n();
+    FF_CUDA(cudaMemsetAsync(&st->bad_cells, 0, sizeof(int), s));
+    k_count_bad<<<nblocks1(n, 256), 256, 0, s>>>(n, x_hi0, x_hi1, st, max_plausible);
+    FF_TRY(post("count_bad"));
+    k_commit<<<nblocks1(n, 256), 256, 0, s>>>(n, x_hi0, x_lo0, x_hi1, x_lo1, snap_hi, snap_lo, st);
+    return post("commit");
+}
+
+int correct(Dims d, float hx, float hy, float hz, const float *x_hi, const float *x_lo,
+            const float *fw[3], const float *cw[3], const float *uin, const float *vin,
+            const float *win, float *uout, float *vout, float *wout, cudaStream_t s) {
+    const float hs[3] = {hx, hy, hz};
+    const float *ins[3] = {uin, vin, win};
+    float *outs[3] = {uout, vout, wout};
+    int naxes = d.nz > 1 ? 3 : 2;
+    for (int a = 0; a < naxes; ++a) {
+        auto L = launch3(d.nx + (a == 0), d.ny + (a == 1), d.nz + (a == 2));
+        k_correct_axis<<<L.grid, L.block, 0, s>>>(d, a, hs[a], x_hi, x_lo, fw[a], cw[a], ins[a], outs[a]);
+    }
+    return post("correct");
+}
+
+int cg_setup_residual(Dims d, const float4 *coef, const float *b, const float *xh,
+                      const float *xl, float *r, PcgState *st, double *partials, int ds,
+                      cudaStream_t s) {
+    auto L = launch3(d.nx, d.ny, d.nz);
+    k_setup_residual<<<L.grid, L.block, 0, s>>>(d, coef, b, xh, xl, r, st, partials, ds);
+    return post("setup_residual");
+}
+
+int cg_update_p_pap(Dims d, const float4 *coef, const void *z, int zbf16, float *p0, float *p1,
+                    PcgState *st, double *partials, cudaStream_t s) {
+    auto L = launch3(d.nx, d.ny, d.nz);
+    if (zbf16)
+        k_update_p_pap<__nv_bfloat16><<<L.grid, L.block, 0, s>>>(d, coef, (const __nv_bfloat16 *)z, p0, p1, st, partials);
+    else
+        k_update_p_pap<float><<<L.grid, L.block, 0, s>>>(d, coef, (const float *)z, p0, p1, st, partials);
+    return post("update_p_pap");
+}
+
+int cg_update_x_residual(Dims d, const float4 *coef, const float *b, const float *p0,
+                         const float *p1, float *xh0, float *xl0, float *xh1, float *xl1,
+                         float *r, PcgState *st, double *partials, int ds, cudaStream_t s) {
+    auto L = launch3(d.nx, d.ny, d.nz);
+    k_update_x_residual<<<L.grid, L.block, 0, s>>>(d, coef, b, p0, p1, xh0, xl0, xh1, xl1, r, st, partials, ds);
+    return post("update_x_residual");
+}
+
+int cg_rz_beta(Dims d, const float *r, const void *z, int zbf16, PcgState *st,
+               double *partials, int setup, cudaStream_t s) {
+    long long n = d.n();
+    unsigned g = nblocks1(n, 256 * 4);
+    if (zbf16)
+        k_rz_beta<__nv_bfloat16><<<g, 256, 0, s>>>(d, r, (const __nv_bfloat16 *)z, st, partials, setup);
+    else
+        k_rz_beta<float><<<g, 256, 0, s>>>(d, r, (const float *)z, st, partials, setup);
+    return post("rz_beta");
+}
+
+int state_init(PcgState *st, double tol, int maxiter, int relative, cudaStream_t s) {
+    k_state_init<<<1, 1, 0, s>>>(st, tol, maxiter, relative);
+    return post("state_init");
+}
+
+int loop_control(PcgState *st, unsigned long long handle, int use_handle, cudaStream_t s) {
+    k_loop_control<<<1, 32, 0, s>>>(st, (cudaGraphConditionalHandle)handle, use_handle);
+    return post("loop_control");
+}
+
+int laplacian_apply(Dims d, const float4 *coef, const float *x, float *y, cudaStream_t s) {
+    auto L = launch3(d.nx, d.ny, d.nz);
+    k_laplacian<<<L.grid, L.block, 0, s>>>(d, coef, x, y);
+    return post("laplacian");
+}
+
+int jacobi_apply(Dims d, const float4 *coef, const float *r, void *z, int zbf16,
+                 const PcgState *st, cudaStream_t s) {
+    auto L = launch3(d.nx, d.ny, d.nz);
+    if (zbf16) k_jacobi<__nv_bfloat16><<<L.grid, L.block, 0, s>>>(d, coef, r, (__nv_bfloat16 *)z, st);
+    else k_jacobi<float><<<L.grid, L.block, 0, s>>>(d, coef, r, (float *)z, st);
+    return post("jacobi");
+}
+
+int identity_apply(Dims d, const float *r, void *z, int zbf16, const PcgState *st,
+                   cudaStream_t s) {
+    long long n = d.n();
+    if (zbf16) k_identity<__nv_bfloat16><<<nblocks1(n, 256), 256, 0, s>>>(n, r, (__nv_bfloat16 *)z, st);
+    else k_identity<float><<<nblocks1(n, 256), 256, 0, s>>>(n, r, (float *)z, st);
+    return post("identity");
+}
+
+}  // namespace ffk

@@ -1,0 +1,209 @@
+// Static SDF collider bake and fractional face weights, on the device in
+// FP64 (the reference does both on the CPU in JS doubles and stores f32):
+//   createSDFStaticCollider3.addShapes  (fluxflow src/grid/sdf_collider3.js:69-99)
+//   computeFaceWeights                  (sdf_collider3.js:131-254)
+//   fractionInsideCpu / fractionInsideSdfCpu (src/grid/level_set_utils.js:51-161)
+//   primitiveDistanceCpu                (src/grid/primitive_sdf3.js:169-208)
+#include "ff_internal.h"
+#include <cmath>
+
+namespace {
+
+constexpr double MIN_FACE_WEIGHT = 0.01;   // sdf_collider3.js:23
+
+struct Shape {
+    int type;            // 0 sphere, 1 box
+    int has_rotation;
+    double center[3];
+    double radius;
+    double half[3];
+    double axis[3];      // normalised
+    double angle;
+};
+
+__device__ double prim_distance(const Shape &s, double x, double y, double z) {
+    double lx = x - s.center[0], ly = y - s.center[1], lz = z - s.center[2];
+    if (s.type == 0) return sqrt(lx * lx + ly * ly + lz * lz) - s.radius;
+    double qx = lx, qy = ly, qz = lz;
+    if (s.has_rotation) {
+        // rotateAroundAxisCpu(v, axis, -angle): Rodrigues rotation
+        double a = -s.angle, c = cos(a), sn = sin(a);
+        double kx = s.axis[0], ky = s.axis[1], kz = s.axis[2];
+        double cx = ky * lz - kz * ly, cy = kz * lx - kx * lz, cz = kx * ly - ky * lx;
+        double kd = kx * lx + ky * ly + kz * lz;
+        qx = lx * c + cx * sn + kx * kd * (1 - c);
+        qy = ly * c + cy * sn + ky * kd * (1 - c);
+        qz = lz * c + cz * sn + kz * kd * (1 - c);
+    }
+    double dx = fabs(qx) - s.half[0], dy = fabs(qy) - s.half[1], dz = fabs(qz) - s.half[2];
+    double mx = fmax(dx, 0.0), my = fmax(dy, 0.0), mz = fmax(dz, 0.0);
+    double outside = sqrt(mx * mx + my * my + mz * mz);
+    double inside = fmin(fmax(dx, fmax(dy, dz)), 0.0);
+    return outside + inside;
+}
+
+__device__ double shapes_distance(const Shape *sh, int n, double x, double y, double z, double sign) {
+    double d = INFINITY;
+    for (int q = 0; q < n; ++q) d = fmin(d, prim_distance(sh[q], x, y, z));
+    return sign * d;
+}
+
+__device__ double frac_sdf(double p0, double p1) {
+    bool i0 = p0 < 0, i1 = p1 < 0;
+    if (i0 && i1) return 1.0;
+    if (i0 && !i1) return p0 / (p0 - p1);
+    if (!i0 && i1) return p1 / (p1 - p0);
+    return 0.0;
+}
+
+__device__ void cycle4(double *a) {
+    double t = a[0];
+    a[0] = a[1]; a[1] = a[2]; a[2] = a[3]; a[3] = t;
+}
+
+// fractionInsideCpu (level_set_utils.js:89-161)
+__device__ double fraction_inside(double bl, double br, double tl, double tr) {
+    int cnt = (bl < 0) + (tl < 0) + (br < 0) + (tr < 0);
+    double L[4] = {bl, br, tr, tl};
+    if (cnt == 4) return 1.0;
+    if (cnt == 3) {
+        for (int g = 0; g < 4 && L[0] < 0; ++g) cycle4(L);
+        double s0 = 1 - frac_sdf(L[0], L[3]);
+        double s1 = 1 - frac_sdf(L[0], L[1]);
+        return 1 - 0.5 * s0 * s1;
+    }
+    if (cnt == 2) {
+        for (int g = 0; g < 4 && (L[0] >= 0 || !(L[1] < 0 || L[2] < 0)); ++g) cycle4(L);
+        if (L[1] < 0) {
+            double sl = frac_sdf(L[0], L[3]);
+            double sr = frac_sdf(L[1], L[2]);
+            return 0.5 * (sl + sr);
+        }
+        double mid = 0.25 * (L[0] + L[1] + L[2] + L[3]);
+        if (mid < 0) {
+            double area = 0;
+            double s1 = 1 - frac_sdf(L[0], L[3]);
+            double s3 = 1 - frac_sdf(L[2], L[3]);
+            area += 0.5 * s1 * s3;
+            double s2 = 1 - frac_sdf(L[2], L[1]);
+            double s0 = 1 - frac_sdf(L[0], L[1]);
+            area += 0.5 * s0 * s2;
+            return 1 - area;
+        }
+        double area = 0;
+        double s0 = frac_sdf(L[0], L[1]);
+        double s1 = frac_sdf(L[0], L[3]);
+        area += 0.5 * s0 * s1;
+        double s2 = frac_sdf(L[2], L[1]);
+        double s3 = frac_sdf(L[2], L[3]);
+        area += 0.5 * s2 * s3;
+        return area;
+    }
+    if (cnt == 1) {
+        for (int g = 0; g < 4 && L[0] >= 0; ++g) cycle4(L);
+        double s0 = frac_sdf(L[0], L[3]);
+        double s1 = frac_sdf(L[0], L[1]);
+        return 0.5 * s0 * s1;
+    }
+    return 0.0;
+}
+
+__global__ void k_bake_phi(const Shape *sh, int ns, double sign, int nx, int ny, int nz,
+                           double ox, double oy, double oz, double hx, double hy, double hz,
+                           float *phi) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y,
+        k = blockIdx.z;
+    if (i >= nx || j >= ny) return;
+    // originXCpu = originX + 0.5 gridSpacingX; x = originXCpu + i gridSpacingX
+    double x = (ox + 0.5 * hx) + i * hx, y = (oy + 0.5 * hy) + j * hy, z = (oz + 0.5 * hz) + k * hz;
+    phi[i + (long long)nx * (j + (long long)ny * k)] = (float)shapes_distance(sh, ns, x, y, z, sign);
+}
+
+__global__ void k_face_weights(const Shape *sh, int ns, double sign, int axis, int fx, int fy,
+                               int fz, double ox, double oy, double oz, double gx, double gy,
+                               double gz, float *w) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y,
+        k = blockIdx.z;
+    if (i >= fx || j >= fy) return;
+    const double hx = 0.5 * gx, hy = 0.5 * gy, hz = 0.5 * gz;
+    double x = ox + i * gx, y = oy + j * gy, z = oz + k * gz;
+    double off[4][3];
+    if (axis == 0) {
+        double o[4][3] = {{0, -hy, -hz}, {0, hy, -hz}, {0, -hy, hz}, {0, hy, hz}};
+        memcpy(off, o, sizeof o);
+    } else if (axis == 1) {
+        double o[4][3] = {{-hx, 0, -hz}, {hx, 0, -hz}, {-hx, 0, hz}, {hx, 0, hz}};
+        memcpy(off, o, sizeof o);
+    } else {
+        double o[4][3] = {{-hx, -hy, 0}, {hx, -hy, 0}, {-hx, hy, 0}, {hx, hy, 0}};
+        memcpy(off, o, sizeof o);
+    }
+    double c[4];
+    for (int q = 0; q < 4; ++q)
+        c[q] = shapes_distance(sh, ns, x + off[q][0], y + off[q][1], z + off[q][2], sign);
+    double frac = fraction_inside(c[0], c[1], c[2], c[3]);
+    double wv = fmin(1.0, fmax(0.0, 1.0 - frac));
+    if (c[0] <= 0 && c[1] <= 0 && c[2] <= 0 && c[3] <= 0) wv = 0.0;
+    else if (wv > 0 && wv < MIN_FACE_WEIGHT) wv = MIN_FACE_WEIGHT;
+    w[i + (long long)fx * (j + (long long)fy * k)] = (float)wv;
+}
+
+}  // namespace
+
+extern "C" int ff_collider3_bake(ff_ctx ctx, const ff_shape *shapes, int nshapes, int invert,
+                                 const int *res, const double *h, const double *origin,
+                                 ff_field phi, ff_field wu, ff_field wv, ff_field ww) {
+    FF_CHECK(ctx && res && h && origin, FF_E_ARG, "ff_collider3_bake: NULL argument");
+    FF_CHECK(nshapes >= 0 && nshapes <= 64, FF_E_LIMIT, "ff_collider3_bake: at most 64 shapes");
+    FF_CHECK(nshapes == 0 || shapes, FF_E_ARG, "ff_collider3_bake: shapes is NULL");
+    const int nx = res[0], ny = res[1], nz = res[2];
+    cudaStream_t s = ctx->stream;
+    Shape hs[64];
+    for (int q = 0; q < nshapes; ++q) {
+        const ff_shape &a = shapes[q];
+        FF_CHECK(a.type == FF_SHAPE_SPHERE || a.type == FF_SHAPE_BOX, FF_E_ARG,
+                 "primitive_sdf3: unknown shape type '%d'.", a.type);
+        Shape &b = hs[q];
+        b.type = a.type == FF_SHAPE_SPHERE ? 0 : 1;
+        for (int c = 0; c < 3; ++c) { b.center[c] = a.center[c]; b.half[c] = a.half_extents[c]; }
+        b.radius = a.radius;
+        b.has_rotation = a.has_rotation;
+        double len = std::sqrt(a.rotation_axis[0] * a.rotation_axis[0] + a.rotation_axis[1] * a.rotation_axis[1] +
+                               a.rotation_axis[2] * a.rotation_axis[2]);
+        for (int c = 0; c < 3; ++c) b.axis[c] = len > 0 ? a.rotation_axis[c] / len : (c == 2 ? 1.0 : 0.0);
+        b.angle = a.rotation_angle;
+    }
+    Shape *dsh = nullptr;
+    FF_CUDA(cudaMalloc(&dsh, sizeof(Shape) * (nshapes > 0 ? nshapes : 1)));
+    if (nshapes) FF_CUDA(cudaMemcpyAsync(dsh, hs, sizeof(Shape) * nshapes, cudaMemcpyHostToDevice, s));
+    const double sign = invert ? -1.0 : 1.0;
+    auto launch = [&](int fx, int fy, int fz, auto &&fn) {
+        dim3 b(64, 4, 1), g((fx + 63) / 64, (fy + 3) / 4, fz);
+        fn(g, b);
+    };
+    if (phi) {
+        FF_CHECK(phi->count == (long long)nx * ny * nz && phi->dtype == FF_FLOAT, FF_E_ARG, "phi field shape");
+        launch(nx, ny, nz, [&](dim3 g, dim3 b) {
+            k_bake_phi<<<g, b, 0, s>>>(dsh, nshapes, sign, nx, ny, nz, origin[0], origin[1], origin[2], h[0], h[1], h[2],
+                                       (float *)phi->d);
+        });
+    }
+    ff_field ws[3] = {wu, wv, ww};
+    for (int a = 0; a < 3; ++a) {
+        if (!ws[a]) continue;
+        int fx = nx + (a == 0), fy = ny + (a == 1), fz = nz + (a == 2);
+        FF_CHECK(ws[a]->count == (long long)fx * fy * fz && ws[a]->dtype == FF_FLOAT, FF_E_ARG,
+                 "face weight field %d shape", a);
+        // dataOriginU/V/W (sdf_collider3.js:226-228)
+        double o[3] = {origin[0] + (a != 0 ? 0.5 * h[0] : 0.0), origin[1] + (a != 1 ? 0.5 * h[1] : 0.0),
+                       origin[2] + (a != 2 ? 0.5 * h[2] : 0.0)};
+        launch(fx, fy, fz, [&](dim3 g, dim3 b) {
+            k_face_weights<<<g, b, 0, s>>>(dsh, nshapes, sign, a, fx, fy, fz, o[0], o[1], o[2], h[0], h[1], h[2],
+                                           (float *)ws[a]->d);
+        });
+    }
+    FF_CUDA(cudaGetLastError());
+    FF_CUDA(cudaStreamSynchronize(s));
+    cudaFree(dsh);
+    return FF_OK;
+}

@@ -1,0 +1,164 @@
+// Internal declarations shared by the libff translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+#include "../../include/ff.h"
+
+// ---------------------------------------------------------------- errors --
+int ff_set_error(int code, const char *fmt, ...);
+#define FF_CUDA(call)                                                            \
+    do {                                                                         \
+        cudaError_t _e = (call);                                                 \
+        if (_e != cudaSuccess)                                                   \
+            return ff_set_error(FF_E_CUDA, "%s:%d %s: %s", __FILE__, __LINE__,   \
+                                #call, cudaGetErrorString(_e));                  \
+    } while (0)
+#define FF_CHECK(cond, code, ...)                                                \
+    do {                                                                         \
+        if (!(cond)) return ff_set_error(code, __VA_ARGS__);                     \
+    } while (0)
+#define FF_TRY(call)                                                             \
+    do {                                                                         \
+        int _s = (call);                                                         \
+        if (_s != FF_OK) return _s;                                              \
+    } while (0)
+
+// --------------------------------------------------------------- handles --
+struct ff_ctx_s {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t events[16] = {};
+};
+
+struct ff_field_s {
+    ff_ctx ctx = nullptr;
+    int dtype = FF_FLOAT;
+    int ndim = 1;
+    int shape[3] = {1, 1, 1};
+    int64_t count = 0;
+    size_t bytes = 0;
+    void *d = nullptr;
+    bool owned = true;
+};
+
+size_t ff_dtype_size(int dtype);
+// device allocation with 256-byte alignment and zero fill
+int ff_dev_alloc(void **p, size_t bytes, cudaStream_t s);
+void ff_dev_free(void *p);
+
+// ------------------------------------------------------------ grid shapes --
+#ifdef __CUDACC__
+#define FF_HD __host__ __device__
+#else
+#define FF_HD
+#endif
+struct Dims {
+    int nx, ny, nz;
+    FF_HD long long n() const { return (long long)nx * ny * nz; }
+    FF_HD long long nu() const { return (long long)(nx + 1) * ny * nz; }
+    FF_HD long long nv() const { return (long long)nx * (ny + 1) * nz; }
+    FF_HD long long nw() const { return (long long)nx * ny * (nz + 1); }
+};
+
+// ------------------------------------------------------- PCG device state --
+// One struct in device memory holds every scalar the iteration needs; the
+// host reads it once at the end of a solve.  Mirrors the reference's 9-slot
+// scalar buffer (fluxflow src/linalg/linalg.js:1030-1065) in FP64.
+struct PcgState {
+    double pAp, rr, rz, rz_old, pap_baseline, bb;
+    double alpha, beta, thr, tol, best_rr;
+    int stop, iter, stop_iter, first;
+    int maxiter, relative, p_cur, x_cur;
+    int launched, bad_cells, growth_stop, pad;
+    unsigned ticket[4];
+};
+
+// Per-level data of the multigrid hierarchy.  Coefficients are stored per
+// cell as (Kx, Ky, Kz, E): K_a is the coupling through the cell's LOWER face
+// on axis a (w_face / h_a^2, zero when either cell is pinned or the face is a
+// domain edge) and E collects the faces to pinned neighbours (1 for a pinned
+// cell).  (A x)_c = sum_f K_f (x_n - x_c) - E_c x_c reproduces laplacianAt
+// (fluxflow src/linalg/multigrid.js:273-339) exactly, and the diagonal is
+// -(sum of the six K + E), laplacianDiagonalAt (:399-437).
+struct Level {
+    Dims d{};
+    float h2inv[3] = {1, 1, 1};
+    float *w[3] = {nullptr, nullptr, nullptr};   // face weights (fp32), may be null
+    uint8_t *mask = nullptr;                       // may be null
+    float4 *coef = nullptr;                        // fp32 coefficients
+    uint2 *coef16 = nullptr;                       // bf16 coefficients (4 x bf16)
+    void *x = nullptr, *b = nullptr, *buf = nullptr;  // storage type per mode
+};
+
+// --------------------------------------------------------- kernel launchers --
+namespace ffk {
+// generic
+int fill_f32(float *p, long long n, float v, cudaStream_t s);
+int copy_bytes(void *dst, const void *src, size_t bytes, cudaStream_t s);
+
+// coefficient / hierarchy preparation
+int dirichlet_fields(Dims d, const uint8_t *active, const float *target, const float *cwu,
+                     const float *cwv, const float *cww, uint8_t *mask, float *tgt,
+                     uint8_t *vent, cudaStream_t s);
+int system_weights(Dims d, const float *fw[3], const float *cw[3], float *sw[3], cudaStream_t s);
+int build_coef(const Level &L, int dims, int want16, cudaStream_t s);
+int coarsen_weights(const Level &f, Level &c, int dims, cudaStream_t s);
+int coarsen_mask(const Level &f, const uint8_t *src, Level &c, int dims, cudaStream_t s);
+
+// pressure build / correct / breaker
+int build_system(Dims d, float hx, float hy, float hz, const float *u, const float *v,
+                 const float *w, const float *cw[3], const float *fw[3], const float *sw[3],
+                 const uint8_t *mask, const float *tgt, float *b, float *x_hi, float *x_lo,
+                 cudaStream_t s);
+int count_bad_and_commit(Dims d, float *x_hi0, float *x_lo0, float *x_hi1, float *x_lo1,
+                         float *snap_hi, float *snap_lo, PcgState *st, float max_plausible,
+                         int *bad_count, cudaStream_t s);
+int correct(Dims d, float hx, float hy, float hz, const float *x_hi, const float *x_lo,
+            const float *fw[3], const float *cw[3], const float *uin, const float *vin,
+            const float *win, float *uout, float *vout, float *wout, cudaStream_t s);
+
+// CG kernels (storage: 0 fp32, 1 bf16 for z)
+int cg_setup_residual(Dims d, const float4 *coef, const float *b, const float *xh,
+                      const float *xl, float *r, PcgState *st, double *partials, int ds,
+                      cudaStream_t s);
+int cg_update_p_pap(Dims d, const float4 *coef, const void *z, int zbf16, float *p0,
+                    float *p1, PcgState *st, double *partials, cudaStream_t s);
+int cg_update_x_residual(Dims d, const float4 *coef, const float *b, const float *p0,
+                         const float *p1, float *xh0, float *xl0, float *xh1, float *xl1,
+                         float *r, PcgState *st, double *partials, int ds, cudaStream_t s);
+int cg_rz_beta(Dims d, const float *r, const void *z, int zbf16, PcgState *st,
+               double *partials, int setup, cudaStream_t s);
+int state_init(PcgState *st, double tol, int maxiter, int relative, cudaStream_t s);
+int loop_control(PcgState *st, unsigned long long handle, int use_handle, cudaStream_t s);
+int laplacian_apply(Dims d, const float4 *coef, const float *x, float *y, cudaStream_t s);
+int jacobi_apply(Dims d, const float4 *coef, const float *r, void *z, int zbf16,
+                 const PcgState *st, cudaStream_t s);
+int identity_apply(Dims d, const float *r, void *z, int zbf16, const PcgState *st,
+                   cudaStream_t s);
+
+// multigrid kernels.  xbf/bbf: storage is bf16 when set.
+int mg_relax(const Level &L, int dims, int colour, float sor, int first, int xbf, int bbf,
+             int coef16, const PcgState *st, cudaStream_t s);
+int mg_residual(const Level &L, int dims, int xbf, int bbf, int coef16, const PcgState *st,
+                cudaStream_t s);
+int mg_restrict(const Level &f, Level &c, int dims, int fbf, int cbf, int zero_x,
+                const PcgState *st, cudaStream_t s);
+int mg_prolong(const Level &c, Level &f, int dims, int cbf, int fbf, const PcgState *st,
+               cudaStream_t s);
+int mg_coarse_sweeps(const Level &L, int dims, int sweeps, float sor, int xbf, int bbf,
+                     int coef16, const PcgState *st, cudaStream_t s);
+int mg_coarse_direct(const Level &L, const double *G, int n, int xbf, int bbf,
+                     const PcgState *st, cudaStream_t s);
+// standalone restrict/prolong on fp32 fields (test hooks)
+int mg_restrict_f32(Dims fd, int dims, const float *fine, const uint8_t *fmask,
+                    const uint8_t *cmask, float *coarse, cudaStream_t s);
+int mg_prolong_f32(Dims fd, int dims, const float *coarse, const uint8_t *fmask, float *fine,
+                   cudaStream_t s);
+}  // namespace ffk
+
+// host-side FP64 factorisation of the coarsest level (ff_coarse.cpp)
+int ff_coarse_inverse(int nx, int ny, int nz, const float4 *coef, std::vector<double> &G);

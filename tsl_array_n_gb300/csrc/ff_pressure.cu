@@ -1,0 +1,809 @@
+// Pressure projection: the host side of createGridPressureSolver3
+// (fluxflow src/grid/grid_pressure_solver3.js:66-574) and of the GPU-resident
+// PCG it drives (src/linalg/linalg.js:782-2469).
+//
+// A solve is two CUDA graphs: the setup sequence (linalg.js:1627-1637) and a
+// conditional WHILE node whose body is one PCG iteration (linalg.js:1404-1436
+// order).  The loop stops itself on the device (convergence, a guard, or the
+// iteration cap), so the host waits once per solve instead of once per chunk
+// (linalg.js:1817-1911).
+#include "ff_internal.h"
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <cstdio>
+
+namespace {
+int div_up(long long a, long long b) { return (int)((a + b - 1) / b); }
+}
+
+struct ff_pressure_s {
+    ff_ctx ctx = nullptr;
+    ff_pressure_desc desc{};
+    Dims d{};
+    int dims = 3;
+    float hx = 1, hy = 1, hz = 1;
+    int maxiter = 0;
+    int check_bad = 1;
+    int use_graph = 1;
+
+    // caller-owned inputs (borrowed handles)
+    ff_field cw[3] = {nullptr, nullptr, nullptr};
+    ff_field fw[3] = {nullptr, nullptr, nullptr};
+    ff_field active = nullptr, target = nullptr;
+
+    // owned fields
+    ff_field pressure = nullptr, bfield = nullptr, maskf = nullptr, ventf = nullptr;
+    float *tgt = nullptr;
+    float *x_lo0 = nullptr, *x_hi1 = nullptr, *x_lo1 = nullptr;
+    float *r = nullptr, *p0 = nullptr, *p1 = nullptr, *snap_hi = nullptr, *snap_lo = nullptr;
+    void *z = nullptr;
+    float *sw[3] = {nullptr, nullptr, nullptr};
+    std::vector<Level> lv;
+    bool has_mask = false, has_w = false;
+    PcgState *st = nullptr;
+    PcgState *st_host = nullptr;
+    double *partials = nullptr;
+
+    // coarsest direct solve
+    double *G = nullptr;
+    int nG = 0;
+    std::vector<float4> coarse_key;
+
+    // graphs
+    cudaGraphExec_t setup_exec = nullptr, loop_exec = nullptr;
+    cudaGraph_t setup_graph = nullptr, loop_graph = nullptr;
+    bool prepared = false;
+
+    int vbf() const { return desc.vcycle_storage == FF_STORE_BF16; }
+    int ds() const { return desc.iterate == FF_ITERATE_DS; }
+    cudaStream_t s() const { return ctx->stream; }
+    float *xh0() const { return (float *)pressure->d; }
+};
+
+static void destroy_graphs(ff_pressure ps) {
+    if (ps->setup_exec) cudaGraphExecDestroy(ps->setup_exec);
+    if (ps->loop_exec) cudaGraphExecDestroy(ps->loop_exec);
+    if (ps->setup_graph) cudaGraphDestroy(ps->setup_graph);
+    if (ps->loop_graph) cudaGraphDestroy(ps->loop_graph);
+    ps->setup_exec = ps->loop_exec = nullptr;
+    ps->setup_graph = ps->loop_graph = nullptr;
+}
+
+extern "C" void ff_pressure_desc_default(ff_pressure_desc *d, const int *res, const double *h) {
+    std::memset(d, 0, sizeof *d);
+    for (int a = 0; a < 3; ++a) {
+        d->resolution[a] = res ? res[a] : 1;
+        d->grid_spacing[a] = h ? h[a] : 1.0;
+    }
+    d->preconditioner = FF_PRE_MULTIGRID;
+    d->tolerance = 1e-6;
+    d->max_iterations = 0;
+    d->max_iterations_factor = 1.5;
+    d->relative_tolerance = 1;
+    d->max_plausible_pressure = 1e6;
+    d->mg_levels = 1;
+    d->mg_down = 2;
+    d->mg_up = 2;
+    d->mg_coarsest = 20;
+    d->mg_final = 2;
+    d->mg_sor = 1.0;
+    d->mg_coarsen_mask = 1;
+    d->mg_coarsen_weights = 1;
+    d->mg_coarse_mode = FF_COARSE_SWEEPS;
+    d->vcycle_storage = FF_STORE_FP32;
+    d->iterate = FF_ITERATE_FP32;
+}
+
+static int alloc_f(float **p, long long n, cudaStream_t s) { return ff_dev_alloc((void **)p, (size_t)n * 4, s); }
+
+static int compute_maxiter(const ff_pressure_desc &d, int dims) {
+    if (d.max_iterations > 0) return d.max_iterations;
+    int m = std::max(d.resolution[0], std::max(d.resolution[1], dims == 3 ? d.resolution[2] : 0));
+    // grid_pressure_solver3.js:133 (factor 1 in 3D), grid_pressure_solver2.js:398 (4 in 2D)
+    return (int)std::ceil(d.max_iterations_factor * m * (dims == 3 ? 1 : 4));
+}
+
+extern "C" int ff_pressure3_create(ff_ctx ctx, const ff_pressure_desc *desc, ff_pressure *out) {
+    FF_CHECK(ctx && desc && out, FF_E_ARG, "ff_pressure3_create: NULL argument");
+    *out = nullptr;
+    const int *r = desc->resolution;
+    FF_CHECK(r[0] > 0 && r[1] > 0 && r[2] > 0, FF_E_ARG, "grid_pressure_solver3: resolution must be positive");
+    FF_CHECK(desc->preconditioner >= 0 && desc->preconditioner <= 2, FF_E_ARG,
+             "grid_pressure_solver3: unknown preconditioner '%d' (expected multigrid, jacobi, none)",
+             desc->preconditioner);
+    int dims = r[2] > 1 ? 3 : 2;
+    int L = std::max(1, desc->mg_levels);
+    int div = 1 << (L - 1);
+    FF_CHECK(r[0] % div == 0 && r[1] % div == 0 && (dims == 2 || r[2] % div == 0), FF_E_ARG,
+             "multigrid: shape [%d, %d, %d] is not divisible by 2^(numberOfLevels-1)=%d (numberOfLevels=%d).",
+             r[0], r[1], r[2], div, L);
+    FF_CHECK(L <= 12, FF_E_LIMIT, "multigrid: at most 12 levels");
+    if (desc->mg_coarse_mode == FF_COARSE_DIRECT) {
+        long long nc = (long long)(r[0] / div) * (r[1] / div) * (dims == 3 ? r[2] / div : 1);
+        FF_CHECK(nc <= 4096, FF_E_LIMIT, "multigrid: direct coarsest solve limited to 4096 cells, got %lld", nc);
+    }
+    cudaSetDevice(ctx->device);
+    ff_pressure ps = new ff_pressure_s();
+    ps->ctx = ctx;
+    ps->desc = *desc;
+    ps->desc.mg_levels = L;
+    ps->d = Dims{r[0], r[1], r[2]};
+    ps->dims = dims;
+    ps->hx = (float)desc->grid_spacing[0];
+    ps->hy = (float)desc->grid_spacing[1];
+    ps->hz = (float)desc->grid_spacing[2];
+    ps->maxiter = compute_maxiter(*desc, dims);
+    cudaStream_t s = ctx->stream;
+    const long long n = ps->d.n();
+    int shape[3] = {r[0], r[1], r[2]};
+    int st = FF_OK;
+    auto bail = [&](int code) { ff_pressure3_destroy(ps); return code; };
+    if ((st = ff_field_create(ctx, FF_FLOAT, 3, shape, &ps->pressure))) return bail(st);
+    if ((st = ff_field_create(ctx, FF_FLOAT, 3, shape, &ps->bfield))) return bail(st);
+    if ((st = ff_field_create(ctx, FF_UINT8, 3, shape, &ps->maskf))) return bail(st);
+    if ((st = ff_field_create(ctx, FF_UINT8, 3, shape, &ps->ventf))) return bail(st);
+    if ((st = alloc_f(&ps->tgt, n, s))) return bail(st);
+    if ((st = alloc_f(&ps->x_hi1, n, s))) return bail(st);
+    if (ps->ds()) {
+        if ((st = alloc_f(&ps->x_lo0, n, s))) return bail(st);
+        if ((st = alloc_f(&ps->x_lo1, n, s))) return bail(st);
+        if ((st = alloc_f(&ps->snap_lo, n, s))) return bail(st);
+    }
+    if ((st = alloc_f(&ps->r, n, s))) return bail(st);
+    if ((st = alloc_f(&ps->p0, n, s))) return bail(st);
+    if ((st = alloc_f(&ps->p1, n, s))) return bail(st);
+    if ((st = alloc_f(&ps->snap_hi, n, s))) return bail(st);
+    const size_t vsz = ps->vbf() ? 2 : 4;
+    if ((st = ff_dev_alloc(&ps->z, (size_t)n * vsz, s))) return bail(st);
+    long long nf[3] = {ps->d.nu(), ps->d.nv(), ps->d.nw()};
+    for (int a = 0; a < dims; ++a)
+        if ((st = alloc_f(&ps->sw[a], nf[a], s))) return bail(st);
+    // hierarchy
+    ps->lv.resize(L);
+    for (int l = 0; l < L; ++l) {
+        Level &v = ps->lv[l];
+        int sc = 1 << l;
+        v.d = Dims{r[0] / sc, r[1] / sc, dims == 3 ? r[2] / sc : 1};
+        double hs[3] = {desc->grid_spacing[0] * sc, desc->grid_spacing[1] * sc, desc->grid_spacing[2] * sc};
+        for (int a = 0; a < 3; ++a) v.h2inv[a] = (float)(1.0 / (hs[a] * hs[a]));
+        long long ln = v.d.n();
+        if ((st = ff_dev_alloc((void **)&v.coef, (size_t)ln * sizeof(float4), s))) return bail(st);
+        if (ps->vbf() && (st = ff_dev_alloc((void **)&v.coef16, (size_t)ln * sizeof(uint2), s))) return bail(st);
+        if (l > 0) {
+            if ((st = ff_dev_alloc(&v.x, (size_t)ln * vsz, s))) return bail(st);
+            if ((st = ff_dev_alloc(&v.b, (size_t)ln * vsz, s))) return bail(st);
+            if ((st = ff_dev_alloc((void **)&v.mask, (size_t)ln, s))) return bail(st);
+            long long lf[3] = {v.d.nu(), v.d.nv(), v.d.nw()};
+            for (int a = 0; a < dims; ++a)
+                if ((st = alloc_f(&v.w[a], lf[a], s))) return bail(st);
+        } else {
+            v.x = ps->z;
+            v.b = ps->r;
+        }
+        if (l < L - 1 && (st = ff_dev_alloc(&v.buf, (size_t)ln * vsz, s))) return bail(st);
+    }
+    if ((st = ff_dev_alloc((void **)&ps->st, sizeof(PcgState), s))) return bail(st);
+    if (cudaMallocHost(&ps->st_host, sizeof(PcgState)) != cudaSuccess) return bail(ff_set_error(FF_E_NOMEM, "cudaMallocHost"));
+    auto g = Dims{r[0], r[1], r[2]};
+    long long blocks = (long long)div_up(g.nx, g.nx >= 128 ? 128 : g.nx >= 64 ? 64 : 32) *
+                       div_up(g.ny, 256 / (g.nx >= 128 ? 128 : g.nx >= 64 ? 64 : 32)) * g.nz;
+    blocks = std::max(blocks, (long long)div_up(n, 1024));
+    if ((st = ff_dev_alloc((void **)&ps->partials, (size_t)blocks * 2 * sizeof(double), s))) return bail(st);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return bail(ff_set_error(FF_E_CUDA, "sync after create"));
+    *out = ps;
+    return FF_OK;
+}
+
+extern "C" int ff_pressure3_destroy(ff_pressure ps) {
+    if (!ps) return FF_OK;
+    cudaStreamSynchronize(ps->ctx->stream);
+    destroy_graphs(ps);
+    ff_field_destroy(ps->pressure);
+    ff_field_destroy(ps->bfield);
+    ff_field_destroy(ps->maskf);
+    ff_field_destroy(ps->ventf);
+    float *fs[] = {ps->tgt, ps->x_lo0, ps->x_hi1, ps->x_lo1, ps->r, ps->p0, ps->p1, ps->snap_hi, ps->snap_lo};
+    for (float *p : fs) ff_dev_free(p);
+    ff_dev_free(ps->z);
+    for (int a = 0; a < 3; ++a) ff_dev_free(ps->sw[a]);
+    for (size_t l = 0; l < ps->lv.size(); ++l) {
+        Level &v = ps->lv[l];
+        ff_dev_free(v.coef);
+        ff_dev_free(v.coef16);
+        ff_dev_free(v.buf);
+        if (l > 0) {
+            ff_dev_free(v.x);
+            ff_dev_free(v.b);
+            ff_dev_free(v.mask);
+            for (int a = 0; a < 3; ++a) ff_dev_free(v.w[a]);
+        }
+    }
+    ff_dev_free(ps->st);
+    if (ps->st_host) cudaFreeHost(ps->st_host);
+    ff_dev_free(ps->partials);
+    ff_dev_free(ps->G);
+    delete ps;
+    return FF_OK;
+}
+
+static int check_face_field(ff_pressure ps, ff_field f, int axis) {
+    if (!f) return FF_OK;
+    int want[3] = {ps->d.nx + (axis == 0), ps->d.ny + (axis == 1), ps->d.nz + (axis == 2)};
+    if (ps->dims == 2 && axis == 2) return FF_OK;
+    FF_CHECK(f->dtype == FF_FLOAT, FF_E_ARG, "face weights must be float fields");
+    FF_CHECK(f->shape[0] == want[0] && f->shape[1] == want[1] && f->shape[2] == want[2], FF_E_ARG,
+             "face field for axis %d has shape [%d, %d, %d], expected [%d, %d, %d]", axis, f->shape[0],
+             f->shape[1], f->shape[2], want[0], want[1], want[2]);
+    return FF_OK;
+}
+
+extern "C" int ff_pressure3_set_collider_weights(ff_pressure ps, ff_field u, ff_field v, ff_field w) {
+    FF_CHECK(ps, FF_E_ARG, "NULL solver");
+    FF_CHECK((u && v && (w || ps->dims == 2)) || (!u && !v && !w), FF_E_ARG,
+             "collider weights need all of u, v%s or none", ps->dims == 3 ? ", w" : "");
+    FF_TRY(check_face_field(ps, u, 0));
+    FF_TRY(check_face_field(ps, v, 1));
+    FF_TRY(check_face_field(ps, w, 2));
+    ps->cw[0] = u; ps->cw[1] = v; ps->cw[2] = ps->dims == 3 ? w : nullptr;
+    ps->prepared = false;
+    return FF_OK;
+}
+
+extern "C" int ff_pressure3_set_face_weights(ff_pressure ps, ff_field u, ff_field v, ff_field w) {
+    FF_CHECK(ps, FF_E_ARG, "NULL solver");
+    FF_CHECK((u && v && (w || ps->dims == 2)) || (!u && !v && !w), FF_E_ARG,
+             "face weights need all of u, v%s or none", ps->dims == 3 ? ", w" : "");
+    FF_TRY(check_face_field(ps, u, 0));
+    FF_TRY(check_face_field(ps, v, 1));
+    FF_TRY(check_face_field(ps, w, 2));
+    ps->fw[0] = u; ps->fw[1] = v; ps->fw[2] = ps->dims == 3 ? w : nullptr;
+    ps->prepared = false;
+    return FF_OK;
+}
+
+extern "C" int ff_pressure3_set_dirichlet(ff_pressure ps, ff_field active, ff_field target) {
+    FF_CHECK(ps, FF_E_ARG, "NULL solver");
+    if (active) {
+        FF_CHECK(active->dtype == FF_UINT8 && active->count == ps->d.n(), FF_E_ARG,
+                 "dirichlet active must be a u8 cell field of the solver's resolution");
+    }
+    if (target) {
+        FF_CHECK(active, FF_E_ARG, "dirichlet target given without active");
+        FF_CHECK(target->dtype == FF_FLOAT && target->count == ps->d.n(), FF_E_ARG,
+                 "dirichlet target must be a float cell field of the solver's resolution");
+    }
+    ps->active = active;
+    ps->target = target;
+    ps->prepared = false;
+    return FF_OK;
+}
+
+extern "C" int ff_pressure3_set(ff_pressure ps, const char *key, double value) {
+    FF_CHECK(ps && key, FF_E_ARG, "NULL argument");
+    std::string k(key);
+    if (k == "tolerance") { ps->desc.tolerance = value; destroy_graphs(ps); }
+    else if (k == "maxIterations") { ps->maxiter = (int)value; destroy_graphs(ps); }
+    else if (k == "relativeTolerance") { ps->desc.relative_tolerance = value != 0; destroy_graphs(ps); }
+    else if (k == "checkBadCells") ps->check_bad = value != 0;
+    else if (k == "useGraph") { ps->use_graph = value != 0; }
+    else if (k == "preconditioner") {
+        FF_CHECK(value >= 0 && value <= 2, FF_E_ARG, "unknown preconditioner %g", value);
+        ps->desc.preconditioner = (int)value;
+        destroy_graphs(ps);
+    } else if (k == "sorFactor") { ps->desc.mg_sor = value; destroy_graphs(ps); }
+    else return ff_set_error(FF_E_ARG, "unknown setting '%s'", key);
+    return FF_OK;
+}
+
+extern "C" int ff_pressure3_fields(ff_pressure ps, ff_field *pressure, ff_field *b, ff_field *mask,
+                                   ff_field *vent) {
+    FF_CHECK(ps, FF_E_ARG, "NULL solver");
+    if (pressure) *pressure = ps->pressure;
+    if (b) *b = ps->bfield;
+    if (mask) *mask = ps->maskf;
+    if (vent) *vent = ps->ventf;
+    return FF_OK;
+}
+
+// --------------------------------------------------------------- prepare --
+static const float *fptr(ff_field f) { return f ? (const float *)f->d : nullptr; }
+
+static int prepare(ff_pressure ps, ff_field u, ff_field v, ff_field w) {
+    cudaStream_t s = ps->s();
+    const Dims &d = ps->d;
+    Level &L0 = ps->lv[0];
+    const float *cw[3] = {fptr(ps->cw[0]), fptr(ps->cw[1]), fptr(ps->cw[2])};
+    const float *fw[3] = {fptr(ps->fw[0]), fptr(ps->fw[1]), fptr(ps->fw[2])};
+    // updateDirichletFields (grid_pressure_solver3.js:171-206)
+    ps->has_mask = ps->active || cw[0];
+    // a zero mask is the same operator as no mask, so level 0 always reads
+    // the solver's mask field and the graph's pointers never change
+    uint8_t *mask = (uint8_t *)ps->maskf->d;
+    if (ps->has_mask) {
+        FF_TRY(ffk::dirichlet_fields(d, ps->active ? (const uint8_t *)ps->active->d : nullptr,
+                                     fptr(ps->target), cw[0], cw[1], cw[2], mask, ps->tgt,
+                                     (uint8_t *)ps->ventf->d, s));
+    } else {
+        FF_CUDA(cudaMemsetAsync(ps->maskf->d, 0, ps->maskf->bytes, s));
+        FF_CUDA(cudaMemsetAsync(ps->ventf->d, 0, ps->ventf->bytes, s));
+    }
+    // systemFaceWeights (:217-229)
+    ps->has_w = fw[0] || cw[0];
+    float *sw[3] = {nullptr, nullptr, nullptr};
+    if (ps->has_w) {
+        for (int a = 0; a < ps->dims; ++a) sw[a] = ps->sw[a];
+        FF_TRY(ffk::system_weights(d, fw, cw, sw, s));
+    }
+    // dispatchBuildSystem (:429-453); pins p at Dirichlet cells
+    if (u) {
+        FF_TRY(ffk::build_system(d, ps->hx, ps->hy, ps->hz, fptr(u), fptr(v), fptr(w), cw, fw,
+                                 (const float **)sw, mask, ps->tgt, (float *)ps->bfield->d,
+                                 ps->xh0(), ps->x_lo0, s));
+    }
+    // level 0 of the hierarchy reads the caller's mask and the system weights
+    L0.mask = mask;
+    for (int a = 0; a < 3; ++a) L0.w[a] = sw[a];
+    const int Ln = (int)ps->lv.size();
+    const bool cmask = ps->desc.mg_coarsen_mask != 0, cwgt = ps->desc.mg_coarsen_weights != 0;
+    const bool coarsening_masks = (ps->has_mask && cmask) || (ps->has_w && cwgt);
+    const bool use_coarse_w = ps->has_w && cwgt;
+    // refreshCoarseLevels (multigrid.js:416-452): weights before masks
+    for (int l = 1; l < Ln; ++l) {
+        Level &f = ps->lv[l - 1], &c = ps->lv[l];
+        // unweighted coarse levels are weight 1 everywhere (multigrid.js:360-380)
+        if (use_coarse_w) {
+            FF_TRY(ffk::coarsen_weights(f, c, ps->dims, s));
+        } else {
+            long long lf[3] = {c.d.nu(), c.d.nv(), c.d.nw()};
+            for (int a = 0; a < ps->dims; ++a) FF_TRY(ffk::fill_f32(c.w[a], lf[a], 1.f, s));
+        }
+        if (coarsening_masks) {
+            const uint8_t *src = (!ps->has_mask || !cmask) ? nullptr
+                                 : (l == 1 ? (const uint8_t *)ps->ventf->d : f.mask);
+            // coarsen_mask reads the level's own weights for the enclosed guard
+            // only when the level is weighted
+            float *keep[3] = {c.w[0], c.w[1], c.w[2]};
+            if (!use_coarse_w) c.w[0] = c.w[1] = c.w[2] = nullptr;
+            int rc = ffk::coarsen_mask(f, src, c, ps->dims, s);
+            for (int a = 0; a < 3; ++a) c.w[a] = keep[a];
+            FF_TRY(rc);
+        } else {
+            FF_CUDA(cudaMemsetAsync(c.mask, 0, (size_t)c.d.n(), s));
+        }
+        FF_TRY(ffk::build_coef(c, ps->dims, ps->vbf(), s));
+    }
+    FF_TRY(ffk::build_coef(L0, ps->dims, ps->vbf(), s));
+    ps->prepared = true;
+    // FP64 direct coarsest solve: refactor when the coarsest operator changed
+    if (ps->desc.preconditioner == FF_PRE_MULTIGRID && ps->desc.mg_coarse_mode == FF_COARSE_DIRECT) {
+        Level &c = ps->lv[Ln - 1];
+        int nc = (int)c.d.n();
+        std::vector<float4> key(nc);
+        FF_CUDA(cudaMemcpyAsync(key.data(), c.coef, nc * sizeof(float4), cudaMemcpyDeviceToHost, s));
+        FF_CUDA(cudaStreamSynchronize(s));
+        bool same = ps->G && (int)ps->coarse_key.size() == nc &&
+                    std::memcmp(key.data(), ps->coarse_key.data(), nc * sizeof(float4)) == 0;
+        if (!same) {
+            std::vector<double> G;
+            FF_TRY(ff_coarse_inverse(c.d.nx, c.d.ny, c.d.nz, key.data(), G));
+            if (!ps->G) FF_TRY(ff_dev_alloc((void **)&ps->G, (size_t)nc * nc * sizeof(double), s));
+            FF_CUDA(cudaMemcpyAsync(ps->G, G.data(), (size_t)nc * nc * sizeof(double), cudaMemcpyHostToDevice, s));
+            FF_CUDA(cudaStreamSynchronize(s));
+            ps->nG = nc;
+            ps->coarse_key.swap(key);
+        }
+    }
+    return FF_OK;
+}
+
+extern "C" int ff_pressure3_prepare(ff_pressure ps, ff_field u, ff_field v, ff_field w) {
+    FF_CHECK(ps, FF_E_ARG, "NULL solver");
+    cudaSetDevice(ps->ctx->device);
+    return prepare(ps, u, v, w);
+}
+
+// --------------------------------------------------------------- V-cycle --
+static int relax_level(ff_pressure ps, int l, int iters, bool reversed, bool &first,
+                       const PcgState *st) {
+    Level &v = ps->lv[l];
+    const int xbf = ps->vbf(), bbf = l == 0 ? 0 : ps->vbf();
+    const float sor = (float)ps->desc.mg_sor;
+    for (int it = 0; it < iters; ++it) {
+        for (int h = 0; h < 2; ++h) {
+            int colour = reversed ? 1 - h : h;
+            FF_TRY(ffk::mg_relax(v, ps->dims, colour, sor, first ? 1 : 0, xbf, bbf, xbf, st, ps->s()));
+            first = false;
+        }
+    }
+    return FF_OK;
+}
+
+static int zero_x(ff_pressure ps, int l) {
+    Level &v = ps->lv[l];
+    FF_CUDA(cudaMemsetAsync(v.x, 0, (size_t)v.d.n() * (ps->vbf() ? 2 : 4), ps->s()));
+    return FF_OK;
+}
+
+// vCycle (multigrid.js:1609-1642); x of `l` is zero on entry
+static int vcycle(ff_pressure ps, int l, const PcgState *st) {
+    const int Ln = (int)ps->lv.size();
+    const int vb = ps->vbf();
+    Level &v = ps->lv[l];
+    const int bbf = l == 0 ? 0 : vb;
+    if (l == Ln - 1) {
+        if (ps->desc.mg_coarse_mode == FF_COARSE_DIRECT) {
+            return ffk::mg_coarse_direct(v, ps->G, ps->nG, vb, bbf, st, ps->s());
+        }
+        long long n = v.d.n();
+        if (n <= 16384) {
+            if (l == 0) FF_TRY(zero_x(ps, 0));
+            return ffk::mg_coarse_sweeps(v, ps->dims, ps->desc.mg_coarsest, (float)ps->desc.mg_sor, vb,
+                                         bbf, vb, st, ps->s());
+        }
+        bool first = true;
+        return relax_level(ps, l, ps->desc.mg_coarsest, false, first, st);
+    }
+    Level &c = ps->lv[l + 1];
+    bool first = true;
+    if (ps->desc.mg_down <= 0 && l == 0) FF_TRY(zero_x(ps, 0));
+    if (ps->desc.mg_down <= 0) first = false;
+    FF_TRY(relax_level(ps, l, ps->desc.mg_down, false, first, st));
+    FF_TRY(ffk::mg_residual(v, ps->dims, vb, bbf, vb, st, ps->s()));
+    // the next level's x must be zero unless its own first relax pass or a
+    // direct solve overwrites it
+    bool next_is_coarsest = (l + 1 == Ln - 1);
+    bool need_zero = next_is_coarsest ? (ps->desc.mg_coarse_mode != FF_COARSE_DIRECT &&
+                                         c.d.n() <= 16384)
+                                      : (ps->desc.mg_down <= 0);
+    FF_TRY(ffk::mg_restrict(v, c, ps->dims, vb, vb, need_zero ? 1 : 0, st, ps->s()));
+    FF_TRY(vcycle(ps, l + 1, st));
+    FF_TRY(ffk::mg_prolong(c, v, ps->dims, vb, vb, st, ps->s()));
+    bool nf = false;
+    return relax_level(ps, l, l > 0 ? ps->desc.mg_up : ps->desc.mg_final, true, nf, st);
+}
+
+static int precondition(ff_pressure ps, const PcgState *st) {
+    const Dims &d = ps->d;
+    switch (ps->desc.preconditioner) {
+    case FF_PRE_MULTIGRID: return vcycle(ps, 0, st);
+    case FF_PRE_JACOBI: return ffk::jacobi_apply(d, ps->lv[0].coef, ps->r, ps->z, ps->vbf(), st, ps->s());
+    default: return ffk::identity_apply(d, ps->r, ps->z, ps->vbf(), st, ps->s());
+    }
+}
+
+// ------------------------------------------------------------------ solve --
+static int enqueue_setup(ff_pressure ps) {
+    const Dims &d = ps->d;
+    cudaStream_t s = ps->s();
+    FF_TRY(ffk::state_init(ps->st, ps->desc.tolerance, ps->maxiter, ps->desc.relative_tolerance, s));
+    FF_TRY(ffk::cg_setup_residual(d, ps->lv[0].coef, (const float *)ps->bfield->d, ps->xh0(),
+                                  ps->x_lo0, ps->r, ps->st, ps->partials, ps->ds(), s));
+    FF_TRY(precondition(ps, ps->st));
+    FF_TRY(ffk::cg_rz_beta(d, ps->r, ps->z, ps->vbf(), ps->st, ps->partials, 1, s));
+    return FF_OK;
+}
+
+static int enqueue_iteration(ff_pressure ps, unsigned long long handle, int use_handle) {
+    const Dims &d = ps->d;
+    cudaStream_t s = ps->s();
+    FF_TRY(ffk::cg_update_p_pap(d, ps->lv[0].coef, ps->z, ps->vbf(), ps->p0, ps->p1, ps->st,
+                                ps->partials, s));
+    FF_TRY(ffk::cg_update_x_residual(d, ps->lv[0].coef, (const float *)ps->bfield->d, ps->p0,
+                                     ps->p1, ps->xh0(), ps->x_lo0, ps->x_hi1, ps->x_lo1, ps->r,
+                                     ps->st, ps->partials, ps->ds(), s));
+    FF_TRY(precondition(ps, ps->st));
+    FF_TRY(ffk::cg_rz_beta(d, ps->r, ps->z, ps->vbf(), ps->st, ps->partials, 0, s));
+    FF_TRY(ffk::loop_control(ps->st, handle, use_handle, s));
+    return FF_OK;
+}
+
+static int build_graphs(ff_pressure ps) {
+    destroy_graphs(ps);
+    cudaStream_t s = ps->s();
+    // setup graph
+    FF_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int st = enqueue_setup(ps);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (st != FF_OK) { if (g) cudaGraphDestroy(g); return st; }
+    FF_CUDA(e);
+    ps->setup_graph = g;
+    FF_CUDA(cudaGraphInstantiate(&ps->setup_exec, g, 0));
+    // loop graph: one conditional WHILE node
+    cudaGraph_t lg = nullptr;
+    FF_CUDA(cudaGraphCreate(&lg, 0));
+    ps->loop_graph = lg;
+    cudaGraphConditionalHandle h;
+    FF_CUDA(cudaGraphConditionalHandleCreate(&h, lg, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    FF_CUDA(cudaGraphAddNode(&node, lg, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    FF_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    st = enqueue_iteration(ps, (unsigned long long)h, 1);
+    e = cudaStreamEndCapture(s, &body);
+    FF_TRY(st);
+    FF_CUDA(e);
+    FF_CUDA(cudaGraphInstantiate(&ps->loop_exec, lg, 0));
+    return FF_OK;
+}
+
+static int run_solve(ff_pressure ps) {
+    cudaStream_t s = ps->s();
+    if (ps->use_graph) {
+        if (!ps->setup_exec) FF_TRY(build_graphs(ps));
+        FF_CUDA(cudaGraphLaunch(ps->setup_exec, s));
+        if (ps->maxiter > 0) FF_CUDA(cudaGraphLaunch(ps->loop_exec, s));
+        return FF_OK;
+    }
+    // host-driven chunks (linalg.js:1817-1911), for comparison and fallback
+    FF_TRY(enqueue_setup(ps));
+    int ran = 0;
+    while (ran < ps->maxiter) {
+        int chunk = std::min(8, ps->maxiter - ran);
+        for (int i = 0; i < chunk; ++i) FF_TRY(enqueue_iteration(ps, 0, 0));
+        ran += chunk;
+        FF_CUDA(cudaMemcpyAsync(ps->st_host, ps->st, sizeof(PcgState), cudaMemcpyDeviceToHost, s));
+        FF_CUDA(cudaStreamSynchronize(s));
+        if (ps->st_host->stop != 0) break;
+    }
+    return FF_OK;
+}
+
+static int read_diag(ff_pressure ps, ff_diag *diag, int extra_launches);
+static int prepare_launches(ff_pressure ps, bool build);
+
+extern "C" int ff_pressure3_project(ff_pressure ps, ff_field u_in, ff_field v_in, ff_field w_in,
+                                    ff_field u_out, ff_field v_out, ff_field w_out, ff_diag *diag) {
+    FF_CHECK(ps && u_in && v_in && u_out && v_out, FF_E_ARG, "project: NULL field");
+    FF_CHECK(ps->dims == 2 || (w_in && w_out), FF_E_ARG, "project: 3D needs w fields");
+    const Dims &d = ps->d;
+    FF_CHECK(u_in->count == d.nu() && v_in->count == d.nv() && u_out->count == d.nu() &&
+                 v_out->count == d.nv() && (ps->dims == 2 || (w_in->count == d.nw() && w_out->count == d.nw())),
+             FF_E_ARG,
+             "createGridPressureSolver3: project() input resolution does not match constructed resolution [%d, %d, %d].",
+             d.nx, d.ny, d.nz);
+    cudaSetDevice(ps->ctx->device);
+    cudaStream_t s = ps->s();
+    FF_TRY(prepare(ps, u_in, v_in, w_in));
+    FF_TRY(run_solve(ps));
+    // circuit breaker + snapshot (:289-336, :547-554), then the correction
+    FF_TRY(ffk::count_bad_and_commit(d, ps->xh0(), ps->x_lo0, ps->x_hi1, ps->x_lo1, ps->snap_hi,
+                                     ps->snap_lo, ps->st,
+                                     ps->check_bad ? (float)ps->desc.max_plausible_pressure : INFINITY,
+                                     nullptr, s));
+    const float *cw[3] = {fptr(ps->cw[0]), fptr(ps->cw[1]), fptr(ps->cw[2])};
+    const float *fw[3] = {fptr(ps->fw[0]), fptr(ps->fw[1]), fptr(ps->fw[2])};
+    FF_TRY(ffk::correct(d, ps->hx, ps->hy, ps->hz, ps->xh0(), ps->x_lo0, fw, cw, fptr(u_in),
+                        fptr(v_in), fptr(w_in), (float *)u_out->d, (float *)v_out->d,
+                        w_out ? (float *)w_out->d : nullptr, s));
+    // prepare + finish (count, commit, correct per axis)
+    return read_diag(ps, diag, prepare_launches(ps, true) + 2 + ps->dims);
+}
+
+// kernel launches of one V-cycle, as vcycle() below enqueues them
+static int vcycle_launches(ff_pressure ps) {
+    const int Ln = (int)ps->lv.size();
+    int n = 0;
+    for (int l = 0; l < Ln - 1; ++l) {
+        n += 2 * ps->desc.mg_down + 3 + 2 * (l > 0 ? ps->desc.mg_up : ps->desc.mg_final);
+    }
+    const Level &c = ps->lv[Ln - 1];
+    if (ps->desc.mg_coarse_mode == FF_COARSE_DIRECT || c.d.n() <= 16384) n += 1;
+    else n += 2 * ps->desc.mg_coarsest;
+    return n;
+}
+
+static int precond_launches(ff_pressure ps) {
+    return ps->desc.preconditioner == FF_PRE_MULTIGRID ? vcycle_launches(ps) : 1;
+}
+
+// prepare(): Dirichlet fields, system weights, build, per-level coarsening
+static int prepare_launches(ff_pressure ps, bool build) {
+    int n = (ps->has_mask ? 1 : 0) + (ps->has_w ? 1 : 0) + (build ? 1 : 0) + 1;
+    n += ((int)ps->lv.size() - 1) * 2;   // coarsen weights (or fill), build_coef
+    if ((ps->has_mask && ps->desc.mg_coarsen_mask) || (ps->has_w && ps->desc.mg_coarsen_weights))
+        n += (int)ps->lv.size() - 1;
+    return n;
+}
+
+static int read_diag(ff_pressure ps, ff_diag *diag, int extra_launches) {
+    cudaStream_t s = ps->s();
+    FF_CUDA(cudaMemcpyAsync(ps->st_host, ps->st, sizeof(PcgState), cudaMemcpyDeviceToHost, s));
+    FF_CUDA(cudaStreamSynchronize(s));
+    if (diag) {
+        const PcgState &h = *ps->st_host;
+        diag->converged = h.stop == FF_STOP_CONVERGED;
+        diag->iterations = h.stop == FF_STOP_CONVERGED ? h.stop_iter : h.iter;
+        diag->residual = std::sqrt(std::fabs(h.rr));
+        diag->b_norm = std::sqrt(std::fabs(h.bb));
+        // a guard that fired below the tolerance is a non-event (linalg.js:1702-1710)
+        int sb = FF_STOP_NONE;
+        if (h.stop != FF_STOP_NONE && h.stop != FF_STOP_CONVERGED && !(diag->residual < h.thr)) sb = h.stop;
+        diag->stopped_by = sb;
+        diag->bad_cells = h.bad_cells;
+        diag->rejected = ps->check_bad && h.bad_cells > 0;
+        diag->max_iterations = ps->maxiter;
+        // setup: state init, residual, preconditioner, r.z; then each loop
+        // body the device ran: p/pAp, x/residual, preconditioner, r.z, control
+        int per_iter = 4 + precond_launches(ps);
+        diag->kernel_launches = extra_launches + 3 + precond_launches(ps) + h.launched * per_iter;
+    }
+    return FF_OK;
+}
+
+// solve(A p = b) for a given right-hand side: createPreconditionedConjugate-
+// GradientSolver(...).solve (linalg.js:2176) on the solver's current system.
+extern "C" int ff_pressure3_solve(ff_pressure ps, ff_field b, ff_diag *diag) {
+    FF_CHECK(ps && b, FF_E_ARG, "NULL argument");
+    FF_CHECK(b->count == ps->d.n() && b->dtype == FF_FLOAT, FF_E_ARG, "b must be a float cell field");
+    cudaSetDevice(ps->ctx->device);
+    cudaStream_t s = ps->s();
+    FF_TRY(prepare(ps, nullptr, nullptr, nullptr));
+    FF_CUDA(cudaMemcpyAsync(ps->bfield->d, b->d, b->bytes, cudaMemcpyDeviceToDevice, s));
+    FF_TRY(run_solve(ps));
+    FF_TRY(ffk::count_bad_and_commit(ps->d, ps->xh0(), ps->x_lo0, ps->x_hi1, ps->x_lo1, ps->snap_hi,
+                                     ps->snap_lo, ps->st,
+                                     ps->check_bad ? (float)ps->desc.max_plausible_pressure : INFINITY,
+                                     nullptr, s));
+    return read_diag(ps, diag, prepare_launches(ps, false) + 2);
+}
+
+// ------------------------------------------------------------- test hooks --
+extern "C" int ff_laplacian_apply(ff_pressure ps, ff_field x, ff_field y) {
+    FF_CHECK(ps && x && y, FF_E_ARG, "NULL argument");
+    FF_CHECK(ps->prepared, FF_E_STATE, "call ff_pressure3_prepare first");
+    FF_CHECK(x->count == ps->d.n() && y->count == ps->d.n(), FF_E_ARG, "field size mismatch");
+    FF_TRY(ffk::laplacian_apply(ps->d, ps->lv[0].coef, (const float *)x->d, (float *)y->d, ps->s()));
+    FF_CUDA(cudaStreamSynchronize(ps->s()));
+    return FF_OK;
+}
+
+namespace {
+__global__ void k_bf16_to_f32(long long n, const __nv_bfloat16 *a, float *b) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = __bfloat162float(a[i]);
+}
+}
+
+extern "C" int ff_precondition_apply(ff_pressure ps, ff_field r, ff_field z) {
+    FF_CHECK(ps && r && z, FF_E_ARG, "NULL argument");
+    FF_CHECK(ps->prepared, FF_E_STATE, "call ff_pressure3_prepare first");
+    FF_CHECK(r->count == ps->d.n() && z->count == ps->d.n(), FF_E_ARG, "field size mismatch");
+    cudaStream_t s = ps->s();
+    FF_CUDA(cudaMemcpyAsync(ps->r, r->d, r->bytes, cudaMemcpyDeviceToDevice, s));
+    FF_TRY(precondition(ps, nullptr));
+    long long n = ps->d.n();
+    if (ps->vbf()) {
+        k_bf16_to_f32<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, (const __nv_bfloat16 *)ps->z, (float *)z->d);
+        FF_CUDA(cudaGetLastError());
+    } else {
+        FF_CUDA(cudaMemcpyAsync(z->d, ps->z, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+    }
+    FF_CUDA(cudaStreamSynchronize(s));
+    return FF_OK;
+}
+
+extern "C" int ff_mg_level_info(ff_pressure ps, int level, int *shape3) {
+    FF_CHECK(ps && shape3, FF_E_ARG, "NULL argument");
+    FF_CHECK(level >= 0 && level < (int)ps->lv.size(), FF_E_ARG, "level %d out of range", level);
+    shape3[0] = ps->lv[level].d.nx;
+    shape3[1] = ps->lv[level].d.ny;
+    shape3[2] = ps->lv[level].d.nz;
+    return FF_OK;
+}
+
+extern "C" int ff_mg_level_download(ff_pressure ps, int level, uint8_t *mask, float *wu, float *wv,
+                                    float *ww) {
+    FF_CHECK(ps, FF_E_ARG, "NULL solver");
+    FF_CHECK(ps->prepared, FF_E_STATE, "call ff_pressure3_prepare first");
+    FF_CHECK(level >= 0 && level < (int)ps->lv.size(), FF_E_ARG, "level %d out of range", level);
+    Level &v = ps->lv[level];
+    cudaStream_t s = ps->s();
+    const Dims &d = v.d;
+    if (mask) {
+        if (v.mask) FF_CUDA(cudaMemcpyAsync(mask, v.mask, (size_t)d.n(), cudaMemcpyDeviceToHost, s));
+        else std::memset(mask, 0, (size_t)d.n());
+    }
+    float *outs[3] = {wu, wv, ww};
+    long long nf[3] = {d.nu(), d.nv(), d.nw()};
+    bool weighted = ps->has_w && (level == 0 || ps->desc.mg_coarsen_weights);
+    for (int a = 0; a < 3; ++a) {
+        if (!outs[a]) continue;
+        if (weighted && v.w[a]) FF_CUDA(cudaMemcpyAsync(outs[a], v.w[a], (size_t)nf[a] * 4, cudaMemcpyDeviceToHost, s));
+        else std::fill(outs[a], outs[a] + nf[a], 1.0f);
+    }
+    FF_CUDA(cudaStreamSynchronize(s));
+    return FF_OK;
+}
+
+extern "C" int ff_mg_restrict(ff_pressure ps, int fine_level, ff_field fine, ff_field coarse) {
+    FF_CHECK(ps && fine && coarse, FF_E_ARG, "NULL argument");
+    FF_CHECK(ps->prepared, FF_E_STATE, "call ff_pressure3_prepare first");
+    FF_CHECK(fine_level >= 0 && fine_level + 1 < (int)ps->lv.size(), FF_E_ARG, "bad level");
+    Level &f = ps->lv[fine_level], &c = ps->lv[fine_level + 1];
+    FF_CHECK(fine->count == f.d.n() && coarse->count == c.d.n(), FF_E_ARG, "field size mismatch");
+    FF_TRY(ffk::mg_restrict_f32(f.d, ps->dims, (const float *)fine->d, f.mask, c.mask, (float *)coarse->d, ps->s()));
+    FF_CUDA(cudaStreamSynchronize(ps->s()));
+    return FF_OK;
+}
+
+extern "C" int ff_mg_prolong_add(ff_pressure ps, int fine_level, ff_field coarse, ff_field fine) {
+    FF_CHECK(ps && fine && coarse, FF_E_ARG, "NULL argument");
+    FF_CHECK(ps->prepared, FF_E_STATE, "call ff_pressure3_prepare first");
+    FF_CHECK(fine_level >= 0 && fine_level + 1 < (int)ps->lv.size(), FF_E_ARG, "bad level");
+    Level &f = ps->lv[fine_level], &c = ps->lv[fine_level + 1];
+    FF_CHECK(fine->count == f.d.n() && coarse->count == c.d.n(), FF_E_ARG, "field size mismatch");
+    FF_TRY(ffk::mg_prolong_f32(f.d, ps->dims, (const float *)coarse->d, f.mask, (float *)fine->d, ps->s()));
+    FF_CUDA(cudaStreamSynchronize(ps->s()));
+    return FF_OK;
+}
+
+// Per-kernel device timing on the solver's own buffers (the role of
+// fluxflow src/profiling.js:92-149 dispatch timing).  Each repetition is
+// bracketed by CUDA events on the context stream; the PCG stop flag is
+// cleared between repetitions so no launch exits early.
+extern "C" int ff_pressure3_profile(ff_pressure ps, int which, int reps, float *avg_ms) {
+    FF_CHECK(ps && avg_ms && reps > 0, FF_E_ARG, "NULL argument");
+    FF_CHECK(ps->prepared, FF_E_STATE, "call ff_pressure3_prepare or project first");
+    FF_CHECK(which >= 0 && which <= FF_PROF_ITERATION, FF_E_ARG, "unknown kernel id %d", which);
+    cudaStream_t s = ps->s();
+    const Dims &d = ps->d;
+    Level &L0 = ps->lv[0];
+    cudaEvent_t a, b;
+    FF_CUDA(cudaEventCreate(&a));
+    FF_CUDA(cudaEventCreate(&b));
+    float total = 0.f;
+    const int vb = ps->vbf();
+    for (int r = 0; r < reps; ++r) {
+        FF_CUDA(cudaMemsetAsync(&ps->st->stop, 0, sizeof(int), s));
+        FF_CUDA(cudaEventRecord(a, s));
+        int rc = FF_OK;
+        switch (which) {
+        case FF_PROF_P_PAP:
+            rc = ffk::cg_update_p_pap(d, L0.coef, ps->z, vb, ps->p0, ps->p1, ps->st, ps->partials, s);
+            break;
+        case FF_PROF_X_RESIDUAL:
+            rc = ffk::cg_update_x_residual(d, L0.coef, (const float *)ps->bfield->d, ps->p0, ps->p1, ps->xh0(),
+                                           ps->x_lo0, ps->x_hi1, ps->x_lo1, ps->r, ps->st, ps->partials,
+                                           ps->ds(), s);
+            break;
+        case FF_PROF_RELAX:
+            rc = ffk::mg_relax(L0, ps->dims, r & 1, (float)ps->desc.mg_sor, 0, vb, 0, vb, ps->st, s);
+            break;
+        case FF_PROF_RESIDUAL:
+            rc = ffk::mg_residual(L0, ps->dims, vb, 0, vb, ps->st, s);
+            break;
+        case FF_PROF_RESTRICT:
+            rc = ps->lv.size() > 1 ? ffk::mg_restrict(L0, ps->lv[1], ps->dims, vb, vb, 0, ps->st, s) : FF_OK;
+            break;
+        case FF_PROF_PROLONG:
+            rc = ps->lv.size() > 1 ? ffk::mg_prolong(ps->lv[1], L0, ps->dims, vb, vb, ps->st, s) : FF_OK;
+            break;
+        case FF_PROF_RZ:
+            rc = ffk::cg_rz_beta(d, ps->r, ps->z, vb, ps->st, ps->partials, 0, s);
+            break;
+        case FF_PROF_PRECONDITIONER:
+            rc = precondition(ps, ps->st);
+            break;
+        case FF_PROF_ITERATION:
+            rc = enqueue_iteration(ps, 0, 0);
+            break;
+        }
+        FF_TRY(rc);
+        FF_CUDA(cudaEventRecord(b, s));
+        FF_CUDA(cudaEventSynchronize(b));
+        float ms = 0.f;
+        FF_CUDA(cudaEventElapsedTime(&ms, a, b));
+        total += ms;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *avg_ms = total / reps;
+    return FF_OK;
+}

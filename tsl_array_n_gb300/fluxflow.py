@@ -1,0 +1,360 @@
+"""Host-side mirror of fluxflow's grid/ API for the GB300 path.
+
+Names, option names, defaults and error behaviour follow the reference
+(packages/fluxflow/src/grid/*.js); the work runs in libff (include/ff.h).
+
+  create_face_centered_grid3      grid_data3.js:121-176
+  create_cell_centered_grid3      grid_data3.js:205-216
+  create_sdf_static_collider3     sdf_collider3.js:25-264 (addShapes, computeFaceWeights)
+  create_grid_pressure_solver3    grid_pressure_solver3.js:66-574
+  create_grid_pressure_solver2    grid_pressure_solver2.js:223-981 (nz == 1)
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .tsl_array_n import BorrowedField, Field, context
+
+PRECONDITIONERS = {"multigrid": 0, "jacobi": 1, "none": 2}
+STOP_REASONS = {0: "none", 1: "degenerate-pAp", 2: "pAp-growth", 3: "alpha-magnitude",
+                4: "degenerate-oldRZ", 5: "converged", 6: "residual-growing"}
+
+
+class FaceCenteredGrid3:
+    """createFaceCenteredGrid3 (grid_data3.js:121-176): u (nx+1,ny,nz),
+    v (nx,ny+1,nz), w (nx,ny,nz+1), staggered origins."""
+
+    def __init__(self, resolution, grid_spacing=(1.0, 1.0, 1.0), origin=(0.0, 0.0, 0.0)):
+        nx, ny, nz = resolution
+        self.resolution = (nx, ny, nz)
+        self.grid_spacing = tuple(float(h) for h in grid_spacing)
+        self.origin = tuple(float(o) for o in origin)
+        self.data_size_u = (nx + 1, ny, nz)
+        self.data_size_v = (nx, ny + 1, nz)
+        self.data_size_w = (nx, ny, nz + 1)
+        self.data_u = Field("float", self.data_size_u)
+        self.data_v = Field("float", self.data_size_v)
+        self.data_w = Field("float", self.data_size_w)
+        hx, hy, hz = self.grid_spacing
+        ox, oy, oz = self.origin
+        self.data_origin_u = (ox, oy + 0.5 * hy, oz + 0.5 * hz)
+        self.data_origin_v = (ox + 0.5 * hx, oy, oz + 0.5 * hz)
+        self.data_origin_w = (ox + 0.5 * hx, oy + 0.5 * hy, oz)
+
+    def set(self, u, v, w):
+        self.data_u.from_array(u)
+        self.data_v.from_array(v)
+        self.data_w.from_array(w)
+        return self
+
+    def get(self):
+        return self.data_u.to_array(), self.data_v.to_array(), self.data_w.to_array()
+
+
+def create_face_centered_grid3(nx, ny, nz, hx=1.0, hy=1.0, hz=1.0, ox=0.0, oy=0.0, oz=0.0):
+    return FaceCenteredGrid3((nx, ny, nz), (hx, hy, hz), (ox, oy, oz))
+
+
+def cell_positions(resolution, grid_spacing, origin):
+    """dataPosition of a cell-centred grid (origin + h/2), as numpy arrays in
+    i-fastest order (grid_data3.js:205-216)."""
+    nx, ny, nz = resolution
+    hx, hy, hz = grid_spacing
+    ox, oy, oz = origin
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    return (ox + (i + 0.5) * hx).ravel(), (oy + (j + 0.5) * hy).ravel(), (oz + (k + 0.5) * hz).ravel()
+
+
+class SDFStaticCollider3:
+    """createSDFStaticCollider3 (sdf_collider3.js:25-264): the cell-centred SDF
+    (solid where phi < 0, isInside :49-53) and fractional face weights."""
+
+    FRICTION = 0.5   # sdf_collider3.js:16
+
+    def __init__(self, resolution, grid_spacing, origin=(0.0, 0.0, 0.0)):
+        self.resolution = tuple(resolution)
+        self.grid_spacing = tuple(float(h) for h in grid_spacing)
+        self.origin = tuple(float(o) for o in origin)
+        self.phi = Field("float", self.resolution)
+        self.shapes = []
+        self.invert = False
+
+    @staticmethod
+    def _shape(s):
+        sh = _lib.Shape()
+        if s["type"] == "sphere":
+            sh.type = 0
+            sh.radius = float(s["radius"])
+        elif s["type"] == "box":
+            sh.type = 1
+            sh.half_extents[:] = [float(v) for v in s["halfExtents"]]
+            rot = s.get("rotation")
+            if rot:
+                sh.has_rotation = 1
+                sh.rotation_axis[:] = [float(v) for v in rot["axis"]]
+                sh.rotation_angle = float(rot["angle"])
+        else:
+            raise ValueError(f"primitive_sdf3: unknown shape type '{s['type']}'.")
+        sh.center[:] = [float(v) for v in s["center"]]
+        return sh
+
+    def _bake(self, phi, wu, wv, ww, resolution, spacing, origin):
+        arr = (_lib.Shape * max(1, len(self.shapes)))(*[self._shape(s) for s in self.shapes])
+        res = (C.c_int * 3)(*resolution)
+        h = (C.c_double * 3)(*spacing)
+        o = (C.c_double * 3)(*origin)
+        hnd = lambda f: f.handle if f is not None else None
+        _lib.check(_lib.load().ff_collider3_bake(context().handle, arr, len(self.shapes), int(self.invert),
+                                                 res, h, o, hnd(phi), hnd(wu), hnd(wv), hnd(ww)))
+
+    def add_shapes(self, shapes, invert=False):
+        """addShapes (sdf_collider3.js:69-99)."""
+        self.shapes = list(shapes)
+        self.invert = bool(invert)
+        self._bake(self.phi, None, None, None, self.resolution, self.grid_spacing, self.origin)
+
+    def add_shape(self, shape, invert=False):
+        self.add_shapes([shape], invert=invert)
+
+    def compute_face_weights(self, resolution=None, grid_spacing=None, origin=None):
+        """computeFaceWeights (sdf_collider3.js:131-254): {u, v, w} fields."""
+        resolution = tuple(resolution or self.resolution)
+        grid_spacing = tuple(grid_spacing or self.grid_spacing)
+        origin = tuple(origin or self.origin)
+        nx, ny, nz = resolution
+        w = {"u": Field("float", (nx + 1, ny, nz)), "v": Field("float", (nx, ny + 1, nz)),
+             "w": Field("float", (nx, ny, nz + 1))}
+        self._bake(None, w["u"], w["v"], w["w"], resolution, grid_spacing, origin)
+        return w
+
+
+def create_sdf_static_collider3(nx, ny, nz, hx, hy, hz, ox=0.0, oy=0.0, oz=0.0):
+    return SDFStaticCollider3((nx, ny, nz), (hx, hy, hz), (ox, oy, oz))
+
+
+class GridPressureSolver3:
+    """createGridPressureSolver3 (grid_pressure_solver3.js:66-574).
+
+    ``dirichlet`` is either a callable ``f(x, y, z) -> (active, target)`` on
+    numpy arrays of cell-centre positions (the reference's ``dirichlet(pos)``
+    closure, evaluated once per call of ``update_dirichlet``) or a tuple of
+    arrays ``(active, target)``.  ``face_weights`` / ``collider_weights`` are
+    dicts {u, v, w} of face Fields.  ``multigrid`` takes the reference's
+    option names (multigrid.js:1186-1250) plus ``coarseSolve`` ('sweeps' or
+    'direct').  ``precision`` is 'fp32' (the reference's arithmetic) or
+    'mixed' (BF16 V-cycle storage, double-single CG iterate, FP64 scalars).
+    """
+
+    def __init__(self, resolution, grid_spacing, origin=(0.0, 0.0, 0.0), dirichlet=None,
+                 face_weights=None, collider_weights=None, multigrid=None, preconditioner="multigrid",
+                 tolerance=1e-6, max_iterations=None, max_iterations_factor=1.5,
+                 relative_tolerance=True, max_plausible_pressure=1e6, precision="fp32",
+                 vcycle_storage=None, iterate=None, **ignored):
+        if preconditioner not in PRECONDITIONERS:
+            raise ValueError(f"grid_pressure_solver3: unknown preconditioner '{preconditioner}' "
+                             f"(expected {', '.join(PRECONDITIONERS)}).")
+        resolution = tuple(int(n) for n in resolution)
+        if len(resolution) == 2:
+            resolution = resolution + (1,)
+        grid_spacing = tuple(float(h) for h in grid_spacing)
+        if len(grid_spacing) == 2:
+            grid_spacing = grid_spacing + (1.0,)
+        origin = tuple(float(o) for o in origin) + (0.0,) * (3 - len(origin))
+        self.resolution, self.grid_spacing, self.origin = resolution, grid_spacing, origin
+        mg = dict(multigrid or {})
+        lib = _lib.load()
+        d = _lib.PressureDesc()
+        lib.ff_pressure_desc_default(C.byref(d), (C.c_int * 3)(*resolution),
+                                     (C.c_double * 3)(*grid_spacing))
+        d.origin[:] = origin
+        d.preconditioner = PRECONDITIONERS[preconditioner]
+        d.tolerance = tolerance
+        d.max_iterations = int(max_iterations or 0)
+        d.max_iterations_factor = max_iterations_factor
+        d.relative_tolerance = int(bool(relative_tolerance))
+        d.max_plausible_pressure = max_plausible_pressure
+        d.mg_levels = int(mg.get("numberOfLevels", 1))
+        d.mg_down = int(mg.get("numberOfSmoothingIterationsDown", 2))
+        d.mg_up = int(mg.get("numberOfSmoothingIterationsUp", 2))
+        d.mg_coarsest = int(mg.get("numberOfCoarsestIterations", 20))
+        d.mg_final = int(mg.get("numberOfFinalIterations", 2))
+        d.mg_sor = float(mg.get("sorFactor", 1.0))
+        d.mg_coarsen_mask = int(mg.get("coarsenDirichletMask", True))
+        d.mg_coarsen_weights = int(mg.get("coarsenFaceWeights", True))
+        d.mg_coarse_mode = 1 if mg.get("coarseSolve", "sweeps") == "direct" else 0
+        if precision not in ("fp32", "mixed"):
+            raise ValueError(f"unknown precision '{precision}'")
+        vs = vcycle_storage or ("bf16" if precision == "mixed" else "fp32")
+        it = iterate or ("ds" if precision == "mixed" else "fp32")
+        d.vcycle_storage = 1 if vs == "bf16" else 0
+        d.iterate = 1 if it == "ds" else 0
+        self.desc = d
+        h = C.c_void_p()
+        _lib.check(lib.ff_pressure3_create(context().handle, C.byref(d), C.byref(h)))
+        self.handle = h
+        p, b, m, v = C.c_void_p(), C.c_void_p(), C.c_void_p(), C.c_void_p()
+        _lib.check(lib.ff_pressure3_fields(h, C.byref(p), C.byref(b), C.byref(m), C.byref(v)))
+        ctx = context()
+        self.pressure = BorrowedField(p, ctx)
+        self.b = BorrowedField(b, ctx)
+        self.dirichlet_mask = BorrowedField(m, ctx)
+        self.vent_mask = BorrowedField(v, ctx)
+        self.diagnostics = {"converged": None, "rejected": False, "iterations": None,
+                            "stoppedBy": None}
+        self._keep = {}
+        self._dirichlet = dirichlet
+        if face_weights is not None:
+            self.set_face_weights(face_weights)
+        if collider_weights is not None:
+            self.set_collider_weights(collider_weights)
+        if dirichlet is not None:
+            self.update_dirichlet()
+
+    # -- inputs ------------------------------------------------------------
+    def set_face_weights(self, fw):
+        self._keep["fw"] = fw
+        h = (fw["u"].handle, fw["v"].handle, fw.get("w").handle if fw.get("w") is not None else None) \
+            if fw is not None else (None, None, None)
+        _lib.check(_lib.load().ff_pressure3_set_face_weights(self.handle, *h))
+
+    def set_collider_weights(self, cw):
+        self._keep["cw"] = cw
+        h = (cw["u"].handle, cw["v"].handle, cw.get("w").handle if cw.get("w") is not None else None) \
+            if cw is not None else (None, None, None)
+        _lib.check(_lib.load().ff_pressure3_set_collider_weights(self.handle, *h))
+
+    def update_dirichlet(self, dirichlet=None):
+        """Evaluate the Dirichlet condition on the cell centres
+        (updateDirichletFields, grid_pressure_solver3.js:171-206)."""
+        if dirichlet is not None:
+            self._dirichlet = dirichlet
+        dl = self._dirichlet
+        if dl is None:
+            _lib.check(_lib.load().ff_pressure3_set_dirichlet(self.handle, None, None))
+            return
+        if callable(dl):
+            x, y, z = cell_positions(self.resolution, self.grid_spacing, self.origin)
+            active, target = dl(x, y, z)
+        else:
+            active, target = dl
+        n = int(np.prod(self.resolution))
+        a = Field("uint8", self.resolution).from_array(np.broadcast_to(np.asarray(active, bool), (n,)).astype(np.uint8))
+        t = Field("float", self.resolution).from_array(np.broadcast_to(np.asarray(target, np.float32), (n,)))
+        self._keep["dirichlet"] = (a, t)
+        _lib.check(_lib.load().ff_pressure3_set_dirichlet(self.handle, a.handle, t.handle))
+
+    @property
+    def settings(self):
+        return _Settings(self)
+
+    # -- projection ----------------------------------------------------------
+    def project(self, input_grid, output_grid):
+        """project(inGrid, outGrid) -> dispatch() (grid_pressure_solver3.js:339-556)."""
+        if tuple(input_grid.resolution) != self.resolution[: len(input_grid.resolution)] and \
+                tuple(input_grid.resolution) + (1,) != self.resolution:
+            raise ValueError(f"createGridPressureSolver3: project() input resolution "
+                             f"{list(input_grid.resolution)} does not match constructed resolution "
+                             f"{list(self.resolution)}.")
+
+        def dispatch():
+            diag = _lib.Diag()
+            w_in = input_grid.data_w.handle if getattr(input_grid, "data_w", None) is not None else None
+            w_out = output_grid.data_w.handle if getattr(output_grid, "data_w", None) is not None else None
+            _lib.check(_lib.load().ff_pressure3_project(
+                self.handle, input_grid.data_u.handle, input_grid.data_v.handle, w_in,
+                output_grid.data_u.handle, output_grid.data_v.handle, w_out, C.byref(diag)))
+            self.diagnostics.update(
+                converged=bool(diag.converged), rejected=bool(diag.rejected),
+                iterations=int(diag.iterations), stoppedBy=STOP_REASONS[diag.stopped_by],
+                residual=float(diag.residual), bNorm=float(diag.b_norm),
+                badCells=int(diag.bad_cells), maxIterations=int(diag.max_iterations),
+                kernelLaunches=int(diag.kernel_launches))
+            return self.diagnostics
+
+        return dispatch
+
+    def solve(self, b):
+        """cg.solve on A p = b for a given b Field; returns diagnostics."""
+        diag = _lib.Diag()
+        _lib.check(_lib.load().ff_pressure3_solve(self.handle, b.handle, C.byref(diag)))
+        self.diagnostics.update(
+            converged=bool(diag.converged), rejected=bool(diag.rejected),
+            iterations=int(diag.iterations), stoppedBy=STOP_REASONS[diag.stopped_by],
+            residual=float(diag.residual), bNorm=float(diag.b_norm),
+            badCells=int(diag.bad_cells), maxIterations=int(diag.max_iterations))
+        return dict(self.diagnostics)
+
+    # -- test hooks -----------------------------------------------------------
+    def prepare(self, input_grid=None):
+        g = input_grid
+        args = (g.data_u.handle, g.data_v.handle,
+                g.data_w.handle if getattr(g, "data_w", None) is not None else None) if g else (None,) * 3
+        _lib.check(_lib.load().ff_pressure3_prepare(self.handle, *args))
+
+    def apply_laplacian(self, x, y):
+        _lib.check(_lib.load().ff_laplacian_apply(self.handle, x.handle, y.handle))
+
+    def apply_preconditioner(self, r, z):
+        _lib.check(_lib.load().ff_precondition_apply(self.handle, r.handle, z.handle))
+
+    def level_shape(self, level):
+        s = (C.c_int * 3)()
+        _lib.check(_lib.load().ff_mg_level_info(self.handle, level, s))
+        return tuple(s)
+
+    def level_data(self, level):
+        nx, ny, nz = self.level_shape(level)
+        mask = np.empty(nx * ny * nz, np.uint8)
+        ws = [np.empty((nx + (a == 0)) * (ny + (a == 1)) * (nz + (a == 2)), np.float32) for a in range(3)]
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        _lib.check(_lib.load().ff_mg_level_download(self.handle, level, mask.ctypes.data_as(C.POINTER(C.c_uint8)),
+                                                    fp(ws[0]), fp(ws[1]), fp(ws[2])))
+        return mask, ws
+
+    def restrict(self, fine_level, fine, coarse):
+        _lib.check(_lib.load().ff_mg_restrict(self.handle, fine_level, fine.handle, coarse.handle))
+
+    def prolong_add(self, fine_level, coarse, fine):
+        _lib.check(_lib.load().ff_mg_prolong_add(self.handle, fine_level, coarse.handle, fine.handle))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.load().ff_pressure3_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _Settings:
+    """The runtime ``settings`` object (grid_pressure_solver3.js:135)."""
+
+    _KEYS = {"tolerance", "maxIterations", "relativeTolerance", "checkBadCells", "useGraph",
+             "preconditioner", "sorFactor"}
+
+    def __init__(self, solver):
+        object.__setattr__(self, "_s", solver)
+
+    def __setattr__(self, key, value):
+        if key not in self._KEYS:
+            raise AttributeError(f"unknown setting '{key}'")
+        if key == "preconditioner":
+            value = PRECONDITIONERS[value]
+        _lib.check(_lib.load().ff_pressure3_set(self._s.handle, key.encode(), float(value)))
+
+    __setitem__ = __setattr__
+
+
+def create_grid_pressure_solver3(resolution, grid_spacing, origin=(0.0, 0.0, 0.0), **options):
+    return GridPressureSolver3(resolution, grid_spacing, origin, **options)
+
+
+def create_grid_pressure_solver2(resolution, grid_spacing, origin=(0.0, 0.0), **options):
+    """createGridPressureSolver2 (grid_pressure_solver2.js:223-981): the same
+    solver with nz = 1 (no z axis)."""
+    return GridPressureSolver3(tuple(resolution) + (1,), tuple(grid_spacing) + (1.0,),
+                               tuple(origin) + (0.0,), **options)
