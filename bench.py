@@ -32,16 +32,21 @@ UNIT = "ms/solve"
 # writes counted once over the domain; FP32 4 B, BF16 2 B, coefficients
 # 16 B FP32 / 8 B BF16, the double-single iterate 8 B).
 def kernel_bytes_per_cell(precision):
-    vb = 2 if precision == "mixed" else 4
-    xb = 8 if precision == "mixed" else 4
+    xb = 8 if precision.startswith("mixed") else 4
+    if precision == "mixed-bf16":
+        # per-colour kernels, BF16 coarse storage, coefficients read per cell
+        return {"p_pAp": 4 + 4 + 16 + 4, "x_residual": xb + 4 + 4 + 16 + xb + 4,
+                "relax": 4 + 4 + 8 + 2, "residual": 4 + 4 + 8 + 2, "restrict": 2 + 0.25,
+                "prolong": 0.25 + 8, "rz": 8}
+    # fused path: regular bricks read no coefficients
     return {
-        "p_pAp": vb + 4 + 16 + 4,                 # z, p, coef32 -> p
-        "x_residual": xb + 4 + 4 + 16 + xb + 4,   # x, p, b, coef32 -> x, r
-        "relax": vb + 4 + (8 if vb == 2 else 16) + vb / 2,   # x, b(=r, fp32), coef, half of x written
-        "residual": vb + 4 + (8 if vb == 2 else 16) + vb,
-        "restrict": vb + vb / 8,
-        "prolong": vb / 8 + 2 * vb,
-        "rz": 4 + vb,
+        "p_pAp": 4 + 4 + 4,                 # z, p -> p
+        "x_residual": xb + 4 + 4 + xb + 4,  # x, p, b -> x, r
+        "relax": 4 + 4 + 4,                 # one full red-black sweep: x, b -> x
+        "residual": 4 + 4 + 0.5,            # fused residual+restriction: x, b -> coarse b
+        "restrict": 4 + 0.5,
+        "prolong": 0.5 + 8,
+        "rz": 8,
     }
 
 
@@ -92,7 +97,7 @@ class Clocks:
         sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
         mx = max(float(r[2]) for r in rows)
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i]})
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip() == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": reasons,
                 "samples": len(rows)}
 
@@ -155,6 +160,13 @@ def run_gb300(args):
     for _ in range(args.warmup):
         d = step()
     iters = d["iterations"]
+    if args.profile_only:
+        # launch one kernel family a few times inside the "ff_profile" NVTX
+        # range (for ncu --nvtx-include ff_profile/), then stop
+        avg = C.c_float()
+        _lib.check(lib.ff_pressure3_profile(solver.handle, PROF_IDS[args.profile_only], 3, C.byref(avg)))
+        print(json.dumps({"profile_only": args.profile_only, "ms": avg.value}))
+        return
 
     # device-resident timing
     clocks = Clocks()
@@ -216,7 +228,23 @@ def run_gb300(args):
     for p in hin + hout:
         lib.ff_host_free(p)
 
-    # per-kernel roofline (device events around single launches)
+    roof = None if args.no_kernel_profile else kernel_roofline(lib, solver, args, n)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(sc, levels, iters, budget_s=args.cpu_budget)
+
+    if rank == 0:
+        emit_line(args, world, ms_step, e2e_ms_step, nb, launches, roof, cpu, clk, diags, iters, levels, n)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def kernel_roofline(lib, solver, args, n):
+    """Per-kernel device time (CUDA events around single launches on the
+    solver's stream) against the algorithmic bytes of each kernel."""
+    import ctypes as C
+    from tsl_array_n_gb300 import _lib
     peak, peak_kind = peaks()
     cells = n ** 3
     bpc = kernel_bytes_per_cell(args.precision)
@@ -230,9 +258,11 @@ def run_gb300(args):
     vc_ms = C.c_float()
     _lib.check(lib.ff_pressure3_profile(solver.handle, 7, 5, C.byref(vc_ms)))
     # share of the iteration: relax runs 2*(down+final) passes at level 0
-    passes0 = 2 * (2 + 2)
+    # launches per iteration at level 0: 2 down + 2 up sweeps (fused path)
+    # or 8 colour passes (per-colour path)
+    passes0 = 2 * (2 + 2) if args.precision == "mixed-bf16" else (2 + 2)
     shares = {"relax": kern["relax"]["ms"] * passes0, "x_residual": kern["x_residual"]["ms"],
-              "p_pAp": kern["p_pAp"]["ms"]}
+              "p_pAp": kern["p_pAp"]["ms"], "residual": kern["residual"]["ms"]}
     dom = max(shares, key=shares.get)
     traffic = None
     prof_path = os.path.join(ROOT, "profiles", "traffic.json")
@@ -245,17 +275,18 @@ def run_gb300(args):
             "kernels": {k: {"ms": round(v["ms"], 4), "GB/s": round(v["gbs"], 1),
                             "frac": round(v["gbs"] / peak, 3)} for k, v in kern.items()},
             "iteration_ms": round(it_ms.value, 4), "vcycle_ms": round(vc_ms.value, 4)}
+    return roof
 
-    cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(sc, levels, iters, budget_s=args.cpu_budget)
 
-    if rank == 0:
+def emit_line(args, world, ms_step, e2e_ms_step, nb, launches, roof, cpu, clk, diags, iters, levels, n):
+    cells = n ** 3
+    if True:
         line = {
             "metric": METRIC, "value": round(ms_step / 1.0, 4), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32+bf16+f64" if args.precision == "mixed" else "f32+f64",
+            "dtype": {"mixed": "f32(double-single iterate)+f64", "fp32": "f32+f64",
+                      "mixed-bf16": "f32+bf16+f64"}[args.precision],
             "data": "synthetic (seeded 32-mode Fourier velocity, sphere collider)",
             "config": {"workload": f"3D MGPCG pressure projection {n}^3, sphere r={24 * n // 256} cells, "
                                    f"closed walls + one pinned cell, {levels} levels, coarsest {args.coarse}, "
@@ -272,8 +303,6 @@ def run_gb300(args):
             "clocks": clk,
         }
         print(json.dumps(line))
-    if dist is not None:
-        dist.destroy_process_group()
 
 
 # --------------------------------------------------------- CPU baseline --
@@ -361,11 +390,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--size", type=int, default=256)
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32", "mixed-bf16"])
     ap.add_argument("--coarse", default="direct", choices=["direct", "sweeps"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=30.0)
     ap.add_argument("--ref-iters", type=int, default=12)
+    ap.add_argument("--profile-only", default=None, choices=sorted(PROF_IDS),
+                    help="run one kernel family inside an NVTX range for ncu, then exit")
+    ap.add_argument("--no-kernel-profile", action="store_true",
+                    help="skip the per-kernel timing (used for clean ncu launch lists)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -216,8 +216,9 @@ struct orc_mg {
     int direct_ready;
 };
 
-static void store_round(const orc_mg *mg, double *a, size_t n) {
-    if (!mg->o.store_bf16) return;
+/* store_bf16 bits: 1 level-0 x, 2 coarse-level x and b, 4 residual buffers */
+static void store_round(const orc_mg *mg, int bit, double *a, size_t n) {
+    if (!(mg->o.store_bf16 & bit)) return;
     for (size_t i = 0; i < n; ++i) a[i] = (double)orc_round_bf16((float)a[i]);
 }
 
@@ -399,7 +400,8 @@ static void relax_colour(orc_mg *mg, level_t *v, int colour) {
                 if (((i + j + k) & 1) != colour) continue;
                 size_t c = IDX(i, j, k, v->nx, v->ny);
                 double upd = v->x[c] + (v->b[c] - v->buf[c]) / v->diag[c] * mg->o.sor;
-                v->x[c] = mg->o.store_bf16 ? (double)orc_round_bf16((float)upd) : upd;
+                int bit = v == &mg->lv[0] ? 1 : 2;
+                v->x[c] = (mg->o.store_bf16 & bit) ? (double)orc_round_bf16((float)upd) : upd;
             }
     (void)n;
 }
@@ -535,7 +537,7 @@ static void coarse_direct(orc_mg *mg) {
         y[i] = s;
     }
     for (int i = 0; i < n; ++i) v->x[i] = y[i];
-    store_round(mg, v->x, n);
+    store_round(mg, mg->L == 1 ? 1 : 2, v->x, n);
     free(y);
 }
 
@@ -552,14 +554,14 @@ static void vcycle(orc_mg *mg, int l) {
     /* buildResidualKernel (multigrid.js:741-749) */
     level_apply(v, v->x, v->buf);
     for (size_t q = 0; q < n; ++q) v->buf[q] = v->b[q] - v->buf[q];
-    store_round(mg, v->buf, n);
+    store_round(mg, 4, v->buf, n);
     orc_restrict(v->nx, v->ny, v->nz, v->buf, v->mask, c->mask, c->b);
     size_t nc = cells_of(c->nx, c->ny, c->nz);
-    store_round(mg, c->b, nc);
+    store_round(mg, 2, c->b, nc);
     memset(c->x, 0, nc * 8);
     vcycle(mg, l + 1);
     orc_prolong_add(v->nx, v->ny, v->nz, c->x, v->mask, v->x);
-    store_round(mg, v->x, n);
+    store_round(mg, l == 0 ? 1 : 2, v->x, n);
     relax(mg, l, l > 0 ? mg->o.up : mg->o.final_iters, 1);
 }
 

@@ -188,7 +188,8 @@ def cpuref_cg(shape, h, b, pinned, x0=None, round_f32=False, dot_kind=0, max_ite
 def mg_opts(levels=1, down=2, up=2, coarsest=20, final_iters=2, sor=1.0, coarsen_mask=True,
             coarsen_weights=True, coarse_direct=False, store_bf16=False):
     return MgOpts(levels, down, up, coarsest, final_iters, sor, int(coarsen_mask),
-                  int(coarsen_weights), int(coarse_direct), int(store_bf16))
+                  int(coarsen_weights), int(coarse_direct),
+                  7 if store_bf16 is True else int(store_bf16))
 
 
 class Multigrid:

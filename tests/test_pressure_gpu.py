@@ -89,12 +89,14 @@ def test_vcycle_parity_bf16(gpu, oracle):
     """BF16 storage: the oracle rounds the same arrays to BF16; agreement is
     limited by BF16's 8-bit mantissa."""
     from tsl_array_n_gb300.tsl_array_n import Field
-    s, meta, a, _ = stalled_solver(110, coarse="direct", precision="mixed")
+    s, meta, a, _ = stalled_solver(110, coarse="direct", precision="mixed-bf16")
     shape = tuple(meta["resolution"])
     mask, vent = a["dirichletMask"] > 0.5, a["ventMask"] > 0.5
     w = (a["weightU"], a["weightV"], a["weightW"])
+    # BF16 on coarse-level x, b (bit 2) and residual buffers (bit 4); the
+    # level-0 iterate stays FP32
     mg = oracle.Multigrid(shape, meta["gridSpacing"], mask, vent, w, levels=4, down=3, up=3,
-                          final_iters=2, coarse_direct=True, store_bf16=True)
+                          final_iters=2, coarse_direct=True, store_bf16=6)
     r = a["b"].astype(np.float32)
     rf, zf = Field("float", shape).from_array(r), Field("float", shape)
     s.apply_preconditioner(rf, zf)
@@ -102,7 +104,7 @@ def test_vcycle_parity_bf16(gpu, oracle):
 
 
 @pytest.mark.parametrize("precision,coarse", [("fp32", "sweeps"), ("fp32", "direct"),
-                                              ("mixed", "direct")])
+                                              ("mixed", "direct"), ("mixed-bf16", "direct")])
 def test_solve_frame112(gpu, oracle, precision, coarse):
     """The frozen frame-112 system: converges to 1e-5 relative like the FP64
     oracle, in a comparable number of iterations, and the returned pressure's
@@ -139,7 +141,7 @@ def test_cheap_preconditioners(gpu, oracle, pre):
     _, ro, _ = oracle.pcg_solve(shape, h, a["b"].astype(np.float32).astype(np.float64), None, mask, w,
                                 None, pre, tol=1e-5, max_iter=3000)
     assert d["converged"] == ro["converged"]
-    assert abs(d["iterations"] - ro["iterations"]) <= max(3, 0.1 * ro["iterations"])
+    assert abs(d["iterations"] - ro["iterations"]) <= max(5, 0.15 * ro["iterations"])
 
 
 def test_guard_nan_rhs_is_reported_not_thrown(gpu, oracle):

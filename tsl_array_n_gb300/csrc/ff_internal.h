@@ -143,7 +143,7 @@ int identity_apply(Dims d, const float *r, void *z, int zbf16, const PcgState *s
 // multigrid kernels.  xbf/bbf: storage is bf16 when set.
 int mg_relax(const Level &L, int dims, int colour, float sor, int first, int xbf, int bbf,
              int coef16, const PcgState *st, cudaStream_t s);
-int mg_residual(const Level &L, int dims, int xbf, int bbf, int coef16, const PcgState *st,
+int mg_residual(const Level &L, int dims, int xbf, int bbf, int rbf, int coef16, const PcgState *st,
                 cudaStream_t s);
 int mg_restrict(const Level &f, Level &c, int dims, int fbf, int cbf, int zero_x,
                 const PcgState *st, cudaStream_t s);
@@ -153,6 +153,22 @@ int mg_coarse_sweeps(const Level &L, int dims, int sweeps, float sor, int xbf, i
                      int coef16, const PcgState *st, cudaStream_t s);
 int mg_coarse_direct(const Level &L, const double *G, int n, int xbf, int bbf,
                      const PcgState *st, cudaStream_t s);
+// fused FP32 kernels (ff_fused.cu)
+size_t brick_count(const Dims &d);
+bool fused_ok(const Dims &d);
+int fused_configure();
+size_t fused_blocks(const Dims &d, int sm_count);
+int brick_flags(const Level &L, uint8_t *bricks, cudaStream_t s);
+int sweep(const Level &L, const uint8_t *bricks, const float *x_in, float *x_out, int colour_a, float sor,
+          int first, const Level *coarse, int dims, PcgState *st, double *partials, int rz_mode,
+          int sm_count, cudaStream_t s);
+int res_restrict(const Level &f, const uint8_t *bricks, const float *x, Level &c, int dims,
+                 const PcgState *st, int sm_count, cudaStream_t s);
+int fused_p_pap(const Level &L0, const uint8_t *bricks, const float *z, float *p0, float *p1,
+                PcgState *st, double *partials, int sm_count, cudaStream_t s);
+int fused_x_residual(const Level &L0, const uint8_t *bricks, const float *p0, const float *p1,
+                     const float *b, float *xh0, float *xl0, float *xh1, float *xl1, float *r,
+                     PcgState *st, double *partials, int ds, int setup, int sm_count, cudaStream_t s);
 // standalone restrict/prolong on fp32 fields (test hooks)
 int mg_restrict_f32(Dims fd, int dims, const float *fine, const uint8_t *fmask,
                     const uint8_t *cmask, float *coarse, cudaStream_t s);

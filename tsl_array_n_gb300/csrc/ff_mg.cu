@@ -83,9 +83,9 @@ __global__ void k_relax(Dims d, XT *x, const BT *__restrict__ b, const float4 *c
 }
 
 // buildResidualKernel (multigrid.js:741-749): buf = b - A x
-template <class XT, class BT, bool C16>
+template <class XT, class BT, class RT, bool C16>
 __global__ void k_residual(Dims d, const XT *__restrict__ x, const BT *__restrict__ b,
-                           XT *__restrict__ buf, const float4 *c32, const uint2 *c16,
+                           RT *__restrict__ buf, const float4 *c32, const uint2 *c16,
                            const PcgState *st) {
     if (st && st->stop) return;
     C3 q = cell(d);
@@ -322,15 +322,24 @@ int mg_relax(const Level &L, int dims, int colour, float sor, int first, int xbf
     return post("relax");
 }
 
-int mg_residual(const Level &L, int dims, int xbf, int bbf, int coef16, const PcgState *st,
+int mg_residual(const Level &L, int dims, int xbf, int bbf, int rbf, int coef16, const PcgState *st,
                 cudaStream_t s) {
     (void)dims;
     auto g = launch3(L.d.nx, L.d.ny, L.d.nz);
     DISPATCH_XB(xbf, bbf, {
-        if (coef16)
-            k_residual<XT, BT, true><<<g.grid, g.block, 0, s>>>(L.d, (const XT *)L.x, (const BT *)L.b, (XT *)L.buf, L.coef, L.coef16, st);
-        else
-            k_residual<XT, BT, false><<<g.grid, g.block, 0, s>>>(L.d, (const XT *)L.x, (const BT *)L.b, (XT *)L.buf, L.coef, L.coef16, st);
+        if (rbf) {
+            using RT = __nv_bfloat16;
+            if (coef16)
+                k_residual<XT, BT, RT, true><<<g.grid, g.block, 0, s>>>(L.d, (const XT *)L.x, (const BT *)L.b, (RT *)L.buf, L.coef, L.coef16, st);
+            else
+                k_residual<XT, BT, RT, false><<<g.grid, g.block, 0, s>>>(L.d, (const XT *)L.x, (const BT *)L.b, (RT *)L.buf, L.coef, L.coef16, st);
+        } else {
+            using RT = float;
+            if (coef16)
+                k_residual<XT, BT, RT, true><<<g.grid, g.block, 0, s>>>(L.d, (const XT *)L.x, (const BT *)L.b, (RT *)L.buf, L.coef, L.coef16, st);
+            else
+                k_residual<XT, BT, RT, false><<<g.grid, g.block, 0, s>>>(L.d, (const XT *)L.x, (const BT *)L.b, (RT *)L.buf, L.coef, L.coef16, st);
+        }
     });
     return post("residual");
 }
