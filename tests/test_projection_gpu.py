@@ -1,0 +1,126 @@
+"""Whole-projection parity on the synthetic sphere scene and the collider
+bake, GPU through the C ABI against the FP64 oracle on the same seeded
+inputs; and the TMA-staged sweep against the cp.async sweep."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-300))
+
+
+SHAPES = [
+    {"type": "sphere", "center": [0.5, 0.45, 0.52], "radius": 0.17},
+    {"type": "box", "center": [0.25, 0.7, 0.3], "halfExtents": [0.08, 0.05, 0.11],
+     "rotation": {"axis": [0.3, 1.0, 0.2], "angle": 0.7}},
+]
+
+
+def test_collider_bake_matches_oracle(gpu, oracle):
+    """SDF and face weights (sdf_collider3.js:69-254): both FP64, stored as
+    FP32; the device uses sqrt for Math.hypot, so a few values differ in the
+    last FP32 bit."""
+    from tsl_array_n_gb300 import fluxflow as ff
+    shape, h = (40, 36, 44), (1 / 40, 1 / 36, 1 / 44)
+    col = ff.create_sdf_static_collider3(*shape, *h)
+    col.add_shapes(SHAPES)
+    w = col.compute_face_weights()
+    phi, wu, wv, ww = oracle.collider_bake(SHAPES, shape, h)
+    np.testing.assert_allclose(col.phi.to_array(), phi, rtol=0, atol=2e-7)
+    for got, ref in ((w["u"], wu), (w["v"], wv), (w["w"], ww)):
+        g = got.to_array()
+        np.testing.assert_allclose(g, ref, rtol=0, atol=2e-6)
+        # solid / open classification is exact
+        assert np.array_equal(g == 0, ref == 0)
+        assert np.array_equal(g == 1, ref == 1)
+
+
+def sphere_setup(n, levels, precision="mixed", coarse="direct"):
+    from tsl_array_n_gb300 import fluxflow as ff, scenes
+    sc = scenes.sphere_scene(n=n, radius_cells=max(2, 24 * n // 256), modes=16, seed=1)
+    shape, h = sc["shape"], sc["h"]
+    col = ff.create_sdf_static_collider3(*shape, *h)
+    col.add_shapes(sc["shapes"])
+    cw = col.compute_face_weights()
+    grid = ff.FaceCenteredGrid3(shape, h).set(sc["u"], sc["v"], sc["w"])
+    out = ff.FaceCenteredGrid3(shape, h)
+    solver = ff.create_grid_pressure_solver3(
+        shape, h, collider_weights=cw, dirichlet=(sc["active"], sc["target"]),
+        multigrid={"numberOfLevels": levels, "coarseSolve": coarse}, precision=precision, tolerance=1e-6)
+    return sc, cw, grid, out, solver
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp32"])
+def test_sphere_projection_matches_oracle(gpu, oracle, precision):
+    """One projection of the 64^3 sphere scene: b equals the oracle's build,
+    the pressure meets the 1e-6 tolerance under the oracle's FP64 operator
+    (the mixed iterate; plain FP32 floors higher), and the corrected
+    velocity equals the oracle's correction of the same pressure."""
+    n = 64
+    sc, cw, grid, out, solver = sphere_setup(n, 4, precision)
+    shape, h = sc["shape"], sc["h"]
+    d = solver.project(grid, out)()
+    wts = tuple(w.to_array().astype(np.float64) for w in (cw["u"], cw["v"], cw["w"]))
+    mask, tgt, vent = oracle.dirichlet_fields(shape, sc["active"], sc["target"], wts)
+    assert np.array_equal(solver.dirichlet_mask.to_array().astype(bool), mask.astype(bool))
+    b, _ = oracle.build_system(shape, h, sc["u"], sc["v"], sc["w"], collider_weights=wts, mask=mask, target=tgt)
+    assert rel(solver.b.to_array(), b) < 1e-6
+    p = solver.pressure.to_array().astype(np.float64)
+    res = rel(oracle.laplacian(shape, h, p, mask, wts), b)
+    if precision == "mixed":
+        assert d["converged"] and not d["rejected"], d
+        assert res < 2e-6, res
+    else:
+        assert res < 5e-5, res
+    uo, vo, wo = oracle.correct(shape, h, p, sc["u"], sc["v"], sc["w"], collider_weights=wts)
+    ug, vg, wg = (f.to_array() for f in (out.data_u, out.data_v, out.data_w))
+    for g, r in ((ug, uo), (vg, vo), (wg, wo)):
+        assert rel(g, r) < 1e-6
+    # divergence left after the projection, relative to before
+    b_after, _ = oracle.build_system(shape, h, ug, vg, wg, collider_weights=wts, mask=mask, target=tgt)
+    b_after[mask.astype(bool)] = 0.0
+    assert np.linalg.norm(b_after) < 1e-4 * np.linalg.norm(b)
+
+
+def test_tma_sweep_matches_cp_async_sweep(gpu):
+    """The TMA-staged sweep (64 x 16 tiles) against the cp.async sweep (32 x
+    16 tiles) for one V-cycle application.  Cells next to a tile seam are
+    relaxed with the brick flag of the block that owns them, so a cell whose
+    neighbouring brick differs in regularity takes the other (equally
+    correct) arithmetic path; the results agree to FP32 rounding."""
+    from tsl_array_n_gb300.tsl_array_n import Field
+    n = 64
+    sc, cw, grid, out, solver = sphere_setup(n, 4, "mixed")
+    solver.prepare(grid)
+    r = np.random.default_rng(3).standard_normal(n ** 3).astype(np.float32)
+    rf = Field("float", sc["shape"]).from_array(r)
+    z1, z2 = Field("float", sc["shape"]), Field("float", sc["shape"])
+    solver.settings.useTma = True
+    solver.apply_preconditioner(rf, z1)
+    solver.settings.useTma = False
+    solver.apply_preconditioner(rf, z2)
+    a1, a2 = z1.to_array(), z2.to_array()
+    assert np.all(np.isfinite(a1))
+    assert rel(a1, a2) < 1e-6
+    assert np.max(np.abs(a1 - a2)) < 1e-5 * np.max(np.abs(a2))
+
+
+def test_tma_and_cp_async_solves_agree(gpu):
+    """Full solves with either sweep: same iteration count, pressures equal
+    to FP32 rounding (the fused r.z sums come from different block grids)."""
+    n = 64
+    sc, cw, grid, out, solver = sphere_setup(n, 4, "mixed")
+    solver.settings.useTma = True
+    solver.pressure.fill(0.0)
+    d1 = solver.project(grid, out)()
+    p1 = solver.pressure.to_array().copy()
+    solver.settings.useTma = False
+    solver.pressure.fill(0.0)
+    d2 = solver.project(grid, out)()
+    p2 = solver.pressure.to_array()
+    assert d1["converged"] and d2["converged"]
+    assert d1["iterations"] == d2["iterations"]
+    assert rel(p1, p2) < 1e-5

@@ -286,7 +286,7 @@ __global__ void k_state_init(PcgState *st, double tol, int maxiter, int relative
 __global__ void k_loop_control(PcgState *st, cudaGraphConditionalHandle h, int use_handle) {
     if (threadIdx.x != 0) return;
     st->launched += 1;
-    int cont = (st->stop == 0) && (st->iter < st->maxiter) && (st->launched < st->maxiter + 4);
+    int cont = (st->stop == 0) && (st->err == 0) && (st->iter < st->maxiter) && (st->launched < st->maxiter + 4);
     if (use_handle) cudaGraphSetConditional(h, cont ? 1u : 0u);
 }
 

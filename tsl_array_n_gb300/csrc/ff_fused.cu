@@ -23,6 +23,7 @@
 //    no coefficient memory, no branches, a reciprocal instead of a divide.
 // Requires nx % 4 == 0 (16-byte rows); other levels use the per-colour path.
 #include "ff_device.cuh"
+#include <cudaTypedefs.h>
 #include <algorithm>
 
 using namespace ffd;
@@ -290,6 +291,377 @@ __global__ void __launch_bounds__(NT, 4) k_sweep(SweepArgs a) {
         __syncthreads();
     }
     cp_wait<0>();
+    if (RZ) {
+        double v[1] = {acc.value()};
+        double tot[1];
+        if (grid_reduce<1>(v, a.partials, &a.st->ticket[3], tot)) {
+            if (tid == 0) {
+                PcgState *st = a.st;
+                double rz = tot[0];
+                st->rz = rz;
+                if (a.rz_mode == 2) {
+                    // seedScalarsKernel (linalg.js:1259-1267)
+                    st->rz_old = rz;
+                    st->pap_baseline = fmax(fabs(st->rr), PAP_BASELINE_FLOOR);
+                    st->stop = 0;
+                    st->iter = 0;
+                    st->stop_iter = 0;
+                    st->first = 1;
+                    st->best_rr = -1.0;
+                } else {
+                    // betaKernel (linalg.js:1201-1240)
+                    double rz_old = st->rz_old;
+                    double value = rz / rz_old;
+                    bool degenerate = nonfinite_d(rz_old) || rz_old == 0.0;
+                    bool restart = (rz_old * rz < 0.0) || nonfinite_or_above(value, MAX_BETA_MAGNITUDE);
+                    bool already = st->stop != 0;
+                    st->beta = (already || restart) ? 0.0 : value;
+                    if (degenerate && st->stop == 0) st->stop = FF_STOP_DEGENERATE_OLD_RZ;
+                    st->rz_old = rz;
+                }
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------- TMA-staged sweep --
+// The red-black sweep as a z-marching wavefront on a 64 x 16 tile, one
+// barrier per plane: step m relaxes the second colour on plane m and the
+// first colour on plane m+2 (plus the tile's one-cell halo ring on m+2) in
+// one phase.  The two touch disjoint cells: the second colour on m reads
+// first-colour values of planes m-1..m+1 (final since steps m-3..m-1), the
+// first colour on m+2 reads second-colour values of planes m+1..m+3 (not
+// yet relaxed), so every cell sees exactly the neighbour values of the
+// reference's two colour dispatches (fluxflow src/linalg/multigrid.js:626-640).
+// Plane regions of x (rows j0-2 .. j0+17) and b (rows j0-1 .. j0+16),
+// columns i0-4 .. i0+67, come into shared-memory rings through
+// cp.async.bulk.tensor copies issued by one thread, completing on one
+// mbarrier per stage; the tensor map zero-fills everything outside the
+// domain.  Each thread owns an x-quad; a warp holds two rows of the same
+// parity, so the colour offset inside a quad is uniform across the warp.
+// Waits are bounded in time: a block that gives up records bit 0 of
+// PcgState::err and stops (the host then reports the solve as failed).
+namespace tq {
+constexpr int TX = 64, TY = 16, QX = TX / 4, NT = QX * TY;   // 16 x 16 threads
+constexpr int RW = TX + 8;                  // staged columns i0-4 .. i0+TX+3
+constexpr int XR = TY + 4, BR = TY + 2;     // staged rows of x and of b
+constexpr int SD = 3;                       // stages in flight
+constexpr int XS = SD + 4, BS = SD + 2;     // ring slots: x planes m-1..m+3+SD-1, b planes m..m+2+SD-1
+constexpr int XPL = XR * RW;                // 1440 floats, 45 x 128 B
+constexpr int BPL = ((BR * RW * 4 + 127) / 128) * 32;   // b slot padded to 128 B (1312 floats)
+constexpr unsigned XBYTES = XR * RW * 4, BBYTES = BR * RW * 4;
+constexpr int RING = 2 * (TX / 2 + 1) + 2 * (TY / 2);   // first-colour cells of the halo ring (82)
+constexpr int CW = 48, CR = TY + 2;         // staged class bytes: quads i0/4-16 .. i0/4+31, rows j0-1 ..
+constexpr int CPL = ((CW * CR + 127) / 128) * 128;      // class slot padded to 128 B (896)
+constexpr unsigned CBYTES = CW * CR;
+constexpr int MAXZC = 256;                  // planes per block
+constexpr size_t SMEM = 128 + sizeof(float) * ((size_t)XS * XPL + (size_t)BS * BPL) + (size_t)BS * CPL + 8 * SD;
+static_assert(RING <= NT, "one ring cell per thread");
+static_assert((XPL * 4) % 128 == 0 && (BPL * 4) % 128 == 0, "TMA destinations stay 128-byte aligned");
+}  // namespace tq
+
+struct TqArgs {
+    Geo g;
+    float *x_out;
+    const float4 *coef;
+    const uint8_t *bricks;
+    float sor, rdreg_sor;
+    int colour_a, zc;
+    PcgState *st;
+    double *partials;
+    int rz_mode;
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Wait for the phase with the given parity to complete; false after 0.5 s.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity) {
+    if (mbar_test(bar, parity)) return true;
+    const unsigned long long t0 = globaltimer_ns();
+    while (!mbar_test(bar, parity))
+        if (globaltimer_ns() - t0 > 500000000ull) return false;
+    return true;
+}
+__device__ __forceinline__ void tma_load_3d(unsigned dst, const CUtensorMap *map, int x, int y, int z,
+                                            unsigned bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+        "l"(map), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// One relaxation with coefficients from memory (cells next to a solid, a
+// Dirichlet cell or the domain edge).
+__device__ __forceinline__ float relax_general(const float4 *coef, float h2x, float h2y, float h2z, int nx, int ny,
+                                            int nz, long long sy, long long sz, bool reg, float sor, int i, int j,
+                                            int k, float vc, float xm, float xp, float ym, float yp, float zm,
+                                            float zp, float bval) {
+    Geo g;
+    g.d = Dims{nx, ny, nz};
+    g.h2x = h2x;
+    g.h2y = h2y;
+    g.h2z = h2z;
+    g.sy = sy;
+    g.sz = sz;
+    const long long c = i + sy * j + sz * k;
+    Coef q = coef_at(g, coef, reg, i, j, k, c);
+    return vc + ((bval - apply_q(q, vc, xm, xp, ym, yp, zm, zp)) / diag_q(q)) * sor;
+}
+
+// One relaxation by cell class (see SweepMaps): the short formula for an
+// interior cell with the plain coefficients, the closed form of a Dirichlet
+// row (A x = -x), or the coefficient form (plain values at the domain edge,
+// stored coefficients elsewhere).
+__device__ __forceinline__ float relax_cls(const Geo &g, const TqArgs &a, unsigned cls, int i, int j, int k,
+                                           float vc, float xm, float xp, float ym, float yp, float zm, float zp,
+                                           float bval) {
+    if (cls == 0) return __fmaf_rn(bval - apply_reg(g, vc, xm, xp, ym, yp, zm, zp), a.rdreg_sor, vc);
+    if (cls == 1) return vc - (bval + vc) * a.sor;
+    return relax_general(a.coef, g.h2x, g.h2y, g.h2z, g.d.nx, g.d.ny, g.d.nz, g.sy, g.sz, cls == 2, a.sor, i, j, k,
+                         vc, xm, xp, ym, yp, zm, zp, bval);
+}
+
+// Relax the two cells of colour offset P (cells P and P+2) of the quad whose
+// first cell sits at offset o of plane X; Xm/Xp are the planes below and
+// above, B the b plane (offset bo), cq the quad's class byte.  Writes the
+// quad back and returns it.
+template <int P>
+__device__ __forceinline__ float4 relax_quad(const Geo &g, const TqArgs &a, float *X, const float *Xm,
+                                             const float *Xp, const float *B, int o, int bo, unsigned cq, int gi,
+                                             int gj, int k, float4 &bq) {
+    float4 c = *reinterpret_cast<const float4 *>(X + o);
+    const float s = X[o + (P ? 4 : -1)];
+    const float4 ym = *reinterpret_cast<const float4 *>(X + o - tq::RW);
+    const float4 yp = *reinterpret_cast<const float4 *>(X + o + tq::RW);
+    const float4 zm = *reinterpret_cast<const float4 *>(Xm + o);
+    const float4 zp = *reinterpret_cast<const float4 *>(Xp + o);
+    bq = *reinterpret_cast<const float4 *>(B + bo);
+    const float v0 = P ? c.y : c.x, l0 = P ? c.x : s, r0 = P ? c.z : c.y;
+    const float v1 = P ? c.w : c.z, l1 = P ? c.z : c.y, r1 = P ? s : c.w;
+    const float ym0 = P ? ym.y : ym.x, ym1 = P ? ym.w : ym.z, yp0 = P ? yp.y : yp.x, yp1 = P ? yp.w : yp.z;
+    const float zm0 = P ? zm.y : zm.x, zm1 = P ? zm.w : zm.z, zp0 = P ? zp.y : zp.x, zp1 = P ? zp.w : zp.z;
+    const float b0 = P ? bq.y : bq.x, b1 = P ? bq.w : bq.z;
+    const unsigned c0 = (cq >> (2 * P)) & 3u, c1 = (cq >> (2 * P + 4)) & 3u;
+    float n0, n1;
+    if ((c0 | c1) == 0) {
+        n0 = __fmaf_rn(b0 - apply_reg(g, v0, l0, r0, ym0, yp0, zm0, zp0), a.rdreg_sor, v0);
+        n1 = __fmaf_rn(b1 - apply_reg(g, v1, l1, r1, ym1, yp1, zm1, zp1), a.rdreg_sor, v1);
+    } else {
+        n0 = relax_cls(g, a, c0, gi + P, gj, k, v0, l0, r0, ym0, yp0, zm0, zp0, b0);
+        n1 = relax_cls(g, a, c1, gi + P + 2, gj, k, v1, l1, r1, ym1, yp1, zm1, zp1, b1);
+    }
+    if (P) {
+        c.y = n0;
+        c.w = n1;
+    } else {
+        c.x = n0;
+        c.z = n1;
+    }
+    *reinterpret_cast<float4 *>(X + o) = c;
+    return c;
+}
+
+template <bool FIRST, bool RZ>
+__global__ void __launch_bounds__(tq::NT, 3)
+    k_sweep_tma(TqArgs a, const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap bmap,
+                const __grid_constant__ CUtensorMap cmap) {
+    constexpr int TX = tq::TX, TY = tq::TY, QX = tq::QX, RW = tq::RW, SD = tq::SD, XS = tq::XS, BS = tq::BS;
+    constexpr int XPL = tq::XPL, BPL = tq::BPL, RING = tq::RING;
+    constexpr unsigned XBYTES = tq::XBYTES, BBYTES = tq::BBYTES + tq::CBYTES;
+    constexpr int CW = tq::CW, CPL = tq::CPL;
+    if (a.st && a.rz_mode != 2 && (a.st->stop || a.st->err)) return;
+    extern __shared__ __align__(16) unsigned char dyn_raw[];
+    // 128-byte alignment by pointer arithmetic on the shared array (keeps the
+    // shared address space visible to the compiler: LDS/STS, not generic)
+    float *xs = reinterpret_cast<float *>(dyn_raw + ((128u - (smem_u32(dyn_raw) & 127u)) & 127u));
+    float *bs = xs + XS * XPL;
+    uint8_t *cs = reinterpret_cast<uint8_t *>(bs + BS * BPL);
+    const unsigned bar0 = smem_u32(cs + BS * CPL);
+    const Geo &g = a.g;
+    // warp w holds rows r and r+2 (same colour parity), r = 4(w/2) + w%2
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int qx = lane & (QX - 1), ty = 4 * (warp >> 1) + (warp & 1) + 2 * (lane >> 4);
+    // the TMA issuer is a thread of the last warp, which has no ring cells
+    constexpr int ISSUER = tq::NT - 32;
+    static_assert(ISSUER >= RING, "issuer warp carries no ring cell");
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+    const int k0 = blockIdx.z * a.zc, k1 = min(k0 + a.zc, g.d.nz);
+    // steps k0-3 .. k1-1; step m's stage brings x(m+3) and b(m+2)
+    const int mstart = k0 - 3;
+    // x planes are read at z = -64 (entirely outside: zero fill) when the
+    // input is identically zero
+    auto xz = [&](int p) { return FIRST ? -64 : p; };
+    if (tid == ISSUER) {
+        asm volatile("prefetch.tensormap [%0];" ::"l"(&xmap) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(&bmap) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(&cmap) : "memory");
+        for (int q = 0; q < SD; ++q) mbar_init(bar0 + 8 * q, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        // x plane p lives in slot (p - k0 + 3) mod XS, b plane p in (p - k0 + 1) mod BS.
+        // Stage of step mstart: x(k0-2), x(k0-1), x(k0), b(k0-1);
+        // stage of step mstart+q: x(k0+q), b(k0-1+q).
+        mbar_expect_tx(bar0, 3 * XBYTES + BBYTES);
+        for (int q = 0; q < 3; ++q) tma_load_3d(smem_u32(xs + (1 + q) * XPL), &xmap, i0 - 4, j0 - 2, xz(k0 - 2 + q), bar0);
+        tma_load_3d(smem_u32(bs), &bmap, i0 - 4, j0 - 1, k0 - 1, bar0);
+        tma_load_3d(smem_u32(cs), &cmap, i0 / 4 - 16, j0 - 1, k0 - 1, bar0);
+        for (int q = 1; q < SD && mstart + q < k1; ++q) {
+            mbar_expect_tx(bar0 + 8 * q, XBYTES + BBYTES);
+            tma_load_3d(smem_u32(xs + (3 + q) * XPL), &xmap, i0 - 4, j0 - 2, xz(k0 + q), bar0 + 8 * q);
+            tma_load_3d(smem_u32(bs + q * BPL), &bmap, i0 - 4, j0 - 1, k0 - 1 + q, bar0 + 8 * q);
+            tma_load_3d(smem_u32(cs + q * CPL), &cmap, i0 / 4 - 16, j0 - 1, k0 - 1 + q, bar0 + 8 * q);
+        }
+    }
+    __syncthreads();
+
+    // slot indices of x planes m-1..m+3 and b planes m..m+2 at step m = mstart
+    int sxm1 = XS - 1, sx0 = 0, sxp1 = 1, sxp2 = 2, sxp3 = 3;
+    int sb0 = BS - 2, sbp1 = BS - 1, sbp2 = 0;
+    int bi = 0;
+    unsigned ph = 0;
+    const int ca = a.colour_a, cb = 1 - ca;
+    const int lx = 4 * qx, gi = i0 + lx, gj = j0 + ty;
+    const bool quad_in = gi < g.d.nx && gj < g.d.ny;
+    const int o = (ty + 2) * RW + 4 + lx, bo = (ty + 1) * RW + 4 + lx;
+    float *outp = a.x_out + (gi + g.sy * gj) + g.sz * k0;
+    const int co = (ty + 1) * CW + 16 + qx;   // this quad's class byte in a class plane
+    // Coefficient lines of quads in irregular bricks are prefetched into L2
+    // one plane ahead of their first use (the first colour on plane m+3 runs
+    // in step m+1): regular-brick flags of this thread's brick column for
+    // brick planes bz0.. of planes k0-1..k1+2, as a bitmask (bit = bz - bz0).
+    const long long bplane = (long long)g.bnx * g.bny;
+    const int bz0 = max(0, (k0 - 1) >> 3), bz1 = min((g.d.nz + 7) / 8 - 1, (k1 + 2) >> 3);
+    unsigned long long qmask = ~0ull;
+    if (a.bricks && quad_in) {
+        const uint8_t *col = a.bricks + (gi >> 5) + (long long)g.bnx * (gj >> 4);
+        qmask = 0;
+        for (int bz = bz0; bz <= bz1; ++bz) qmask |= (unsigned long long)(col[bplane * bz] != 0) << (bz - bz0);
+    }
+    const float4 *qcoef = a.coef + (gi + g.sy * gj);
+    // this thread's ring cell (tid < RING): rows above and below the tile
+    // step along x, columns left and right step along y; the first-colour
+    // cell of each pair sits at offset (c + j0 + k + rpar) & 1
+    int rlx = 0, rly = 0, rpar = 0;
+    bool rrow = false;
+    if (tid < RING) {
+        int t = tid;
+        if (t < TX / 2 + 1) {
+            rly = -1; rlx = -1 + 2 * t; rpar = 0; rrow = true;
+        } else if ((t -= TX / 2 + 1) < TX / 2 + 1) {
+            rly = TY; rlx = -1 + 2 * t; rpar = TY + 1; rrow = true;
+        } else if ((t -= TX / 2 + 1) < TY / 2) {
+            rlx = -1; rly = 2 * t; rpar = 1;
+        } else {
+            t -= TY / 2;
+            rlx = TX; rly = 2 * t; rpar = TX;
+        }
+    }
+    Acc acc;
+    bool failed = false;
+    for (int m = mstart; m < k1; ++m) {
+        const bool got = mbar_wait_bounded(bar0 + 8 * bi, ph);
+        float *Xm1 = xs + sxm1 * XPL, *X0 = xs + sx0 * XPL, *Xp1 = xs + sxp1 * XPL, *Xp2 = xs + sxp2 * XPL,
+              *Xp3 = xs + sxp3 * XPL;
+        const float *B0 = bs + sb0 * BPL, *Bp2 = bs + sbp2 * BPL;
+        const uint8_t *C0 = cs + sb0 * CPL, *Cp2 = cs + sbp2 * CPL;
+        if (got && m >= k0) {
+            if (quad_in) {
+                // second colour on plane m, then plane m is final
+                const unsigned cq = C0[co];
+                float4 bq, v;
+                if ((cb ^ gj ^ m) & 1) v = relax_quad<1>(g, a, X0, Xm1, Xp1, B0, o, bo, cq, gi, gj, m, bq);
+                else v = relax_quad<0>(g, a, X0, Xm1, Xp1, B0, o, bo, cq, gi, gj, m, bq);
+                *reinterpret_cast<float4 *>(outp) = v;
+                if (RZ) {
+                    acc.add(bq.x * v.x);
+                    acc.add(bq.y * v.y);
+                    acc.add(bq.z * v.z);
+                    acc.add(bq.w * v.w);
+                }
+            }
+            outp += g.sz;
+        }
+        const int kp = m + 3;
+        if (quad_in && kp >= k0 - 1 && kp <= k1 && kp < g.d.nz && !((qmask >> ((kp >> 3) - bz0)) & 1ull))
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(qcoef + g.sz * kp));
+        const int ka = m + 2;
+        if (got && ka >= 0 && ka <= k1 && ka < g.d.nz) {
+            // first colour on plane m+2: this thread's quad, then its ring cell
+            if (quad_in) {
+                const unsigned cq = Cp2[co];
+                float4 bq;
+                if ((ca ^ gj ^ ka) & 1) relax_quad<1>(g, a, Xp2, Xp1, Xp3, Bp2, o, bo, cq, gi, gj, ka, bq);
+                else relax_quad<0>(g, a, Xp2, Xp1, Xp3, Bp2, o, bo, cq, gi, gj, ka, bq);
+            }
+            if (tid < RING) {
+                const int sh = (ca + j0 + ka + rpar) & 1;
+                const int lxr = rlx + (rrow ? sh : 0), lyr = rly + (rrow ? 0 : sh);
+                const int ri = i0 + lxr, rj = j0 + lyr;
+                if (ri >= 0 && ri < g.d.nx && rj >= 0 && rj < g.d.ny) {
+                    const int ro = (lyr + 2) * RW + lxr + 4;
+                    const float xc = Xp2[ro];
+                    const float bval = Bp2[(lyr + 1) * RW + lxr + 4];
+                    const unsigned rc = (Cp2[(lyr + 1) * CW + 16 + (lxr >> 2)] >> (2 * (lxr & 3))) & 3u;
+                    Xp2[ro] = relax_cls(g, a, rc, ri, rj, ka, xc, Xp2[ro - 1], Xp2[ro + 1], Xp2[ro - RW], Xp2[ro + RW],
+                                        Xp1[ro], Xp3[ro], bval);
+                }
+            }
+        }
+        // x plane m-1 and b plane m are dead: refill them with step m+SD's data
+        fence_proxy_async_smem();
+        if (__syncthreads_or(!got)) {
+            failed = true;
+            break;
+        }
+        if (tid == ISSUER && m + SD < k1) {
+            const int mn = m + SD;
+            mbar_expect_tx(bar0 + 8 * bi, XBYTES + BBYTES);
+            tma_load_3d(smem_u32(Xm1), &xmap, i0 - 4, j0 - 2, xz(mn + 3), bar0 + 8 * bi);
+            tma_load_3d(smem_u32(bs + sb0 * BPL), &bmap, i0 - 4, j0 - 1, mn + 2, bar0 + 8 * bi);
+            tma_load_3d(smem_u32(cs + sb0 * CPL), &cmap, i0 / 4 - 16, j0 - 1, mn + 2, bar0 + 8 * bi);
+        }
+        sxm1 = sx0; sx0 = sxp1; sxp1 = sxp2; sxp2 = sxp3; sxp3 = sxp3 + 1 == XS ? 0 : sxp3 + 1;
+        sb0 = sbp1; sbp1 = sbp2; sbp2 = sbp2 + 1 == BS ? 0 : sbp2 + 1;
+        if (++bi == SD) { bi = 0; ph ^= 1; }
+    }
+    if (failed) {
+        // record the failure, then wait (bounded) for the copies still in
+        // flight to this block's shared memory before leaving
+        if (tid == ISSUER) {
+            if (a.st) atomicOr(&a.st->err, 1);
+            for (int q = 0; q < SD; ++q) {
+                const int b2 = (bi + q) % SD;
+                const unsigned p2 = ph ^ (unsigned)((bi + q) / SD);
+                mbar_wait_bounded(bar0 + 8 * b2, p2);
+            }
+        }
+        __syncthreads();
+        return;
+    }
     if (RZ) {
         double v[1] = {acc.value()};
         double tot[1];
@@ -796,6 +1168,36 @@ __global__ void __launch_bounds__(NT, 4) k_res_restrict(RrArgs a) {
     cp_wait<0>();
 }
 
+// ----------------------------------------------------------- cell classes --
+// Two bits per cell, one byte per x-quad (rows `pitch` bytes apart): 0 an
+// interior cell whose six couplings are the plain h^-2 and E = 0; 1 a
+// Dirichlet cell (E = 1, no coupling); 2 a domain-edge cell with the plain
+// couplings (zero across the edge); 3 anything else.
+__global__ void k_cell_classes(Geo g, const float4 *__restrict__ coef, uint8_t *cls, int pitch) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, k = blockIdx.z;
+    if (4 * q >= g.d.nx) return;
+    unsigned byte = 0;
+#pragma unroll
+    for (int d = 0; d < 4; ++d) {
+        const int i = 4 * q + d;
+        const long long c = i + g.sy * j + g.sz * k;
+        const float4 a = coef[c];
+        const float ux = i < g.d.nx - 1 ? coef[c + 1].x : 0.f;
+        const float uy = j < g.d.ny - 1 ? coef[c + g.sy].y : 0.f;
+        const float uz = k < g.d.nz - 1 ? coef[c + g.sz].z : 0.f;
+        const bool plain = a.x == (i > 0 ? g.h2x : 0.f) && ux == (i < g.d.nx - 1 ? g.h2x : 0.f) &&
+                           a.y == (j > 0 ? g.h2y : 0.f) && uy == (j < g.d.ny - 1 ? g.h2y : 0.f) &&
+                           a.z == (k > 0 ? g.h2z : 0.f) && uz == (k < g.d.nz - 1 ? g.h2z : 0.f) && a.w == 0.f;
+        const bool pinned = a.w == 1.f && a.x == 0.f && a.y == 0.f && a.z == 0.f && ux == 0.f && uy == 0.f &&
+                            uz == 0.f;
+        const bool inner = i > 0 && i < g.d.nx - 1 && j > 0 && j < g.d.ny - 1 && k > 0 && k < g.d.nz - 1;
+        const unsigned cl = plain ? (inner ? 0u : 2u) : (pinned ? 1u : 3u);
+        byte |= cl << (2 * d);
+    }
+    cls[q + (long long)pitch * (j + (long long)g.d.ny * k)] = (uint8_t)byte;
+}
+
 // ------------------------------------------------------------ brick flags --
 // A brick is regular when every cell of it, extended by two cells on each
 // side, carries the plain coefficients (h^-2 on interior faces, E = 0).
@@ -902,6 +1304,122 @@ int sweep(const Level &L, const uint8_t *bricks, const float *x_in, float *x_out
     return post("sweep");
 }
 
+// ---- TMA sweep
+bool sweep_tma_ok(const Dims &d) { return d.nx % 4 == 0 && d.nx >= 32; }
+
+static int tma_zchunk(const Dims &d, int sm_count) {
+    // one wave of 3 blocks per SM, at least 4 planes per block
+    long long cols = (long long)((d.nx + tq::TX - 1) / tq::TX) * ((d.ny + tq::TY - 1) / tq::TY);
+    long long want = 3LL * sm_count;
+    int chunks = (int)std::max(1LL, std::min((long long)d.nz, want / cols));
+    int zc = (d.nz + chunks - 1) / chunks;
+    return std::min(std::max(zc, std::min(4, d.nz)), tq::MAXZC);
+}
+
+size_t sweep_tma_blocks(const Dims &d, int sm_count) {
+    int zc = tma_zchunk(d, sm_count);
+    return (size_t)((d.nx + tq::TX - 1) / tq::TX) * ((d.ny + tq::TY - 1) / tq::TY) * ((d.nz + zc - 1) / zc);
+}
+
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+static int encode_planes(CUtensorMap *m, const float *base, const Dims &d, int rows) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    FF_CHECK(enc, FF_E_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    cuuint64_t dims[3] = {(cuuint64_t)d.nx, (cuuint64_t)d.ny, (cuuint64_t)d.nz};
+    cuuint64_t strides[2] = {(cuuint64_t)d.nx * 4, (cuuint64_t)d.nx * d.ny * 4};
+    cuuint32_t box[3] = {(cuuint32_t)tq::RW, (cuuint32_t)rows, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void *)base, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    FF_CHECK(r == CUDA_SUCCESS, FF_E_CUDA, "cuTensorMapEncodeTiled failed (%d) for a %dx%dx%d level", (int)r,
+             d.nx, d.ny, d.nz);
+    return FF_OK;
+}
+
+static int cls_pitch(const Dims &d) { return ((d.nx / 4 + 15) / 16) * 16; }
+
+size_t sweep_tma_cls_bytes(const Dims &d) { return (size_t)cls_pitch(d) * d.ny * d.nz; }
+
+int sweep_tma_maps(const Level &L, const float *x0, const float *x1, uint8_t *cls, SweepMaps &m) {
+    m.ok = false;
+    FF_CHECK(sweep_tma_ok(L.d), FF_E_ARG, "TMA sweep needs nx %% 4 == 0 and nx >= 32");
+    // TMA global addresses must be 16-byte aligned (the allocator gives 256)
+    FF_CHECK(((uintptr_t)x0 | (uintptr_t)x1 | (uintptr_t)L.b | (uintptr_t)cls) % 16 == 0, FF_E_ARG,
+             "TMA operand misaligned");
+    FF_TRY(encode_planes(&m.x[0], x0, L.d, tq::XR));
+    FF_TRY(encode_planes(&m.x[1], x1, L.d, tq::XR));
+    FF_TRY(encode_planes(&m.b, (const float *)L.b, L.d, tq::BR));
+    // class bytes: (nx/4, ny, nz) uint8 with 16-byte row pitch; box (48, TY+2, 1)
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    FF_CHECK(enc, FF_E_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    const int pitch = cls_pitch(L.d);
+    cuuint64_t dims[3] = {(cuuint64_t)(L.d.nx / 4), (cuuint64_t)L.d.ny, (cuuint64_t)L.d.nz};
+    cuuint64_t strides[2] = {(cuuint64_t)pitch, (cuuint64_t)pitch * L.d.ny};
+    cuuint32_t box[3] = {(cuuint32_t)tq::CW, (cuuint32_t)tq::CR, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = enc(&m.cls, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, (void *)cls, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    FF_CHECK(r == CUDA_SUCCESS, FF_E_CUDA, "cuTensorMapEncodeTiled (classes) failed (%d)", (int)r);
+    m.xp[0] = x0;
+    m.xp[1] = x1;
+    m.cls_ptr = cls;
+    m.cls_pitch = pitch;
+    m.ok = true;
+    return FF_OK;
+}
+
+int cell_classes(const Level &L, const SweepMaps &m, cudaStream_t s) {
+    FF_CHECK(m.ok && m.cls_ptr, FF_E_STATE, "cell classes: maps not built");
+    Geo g = make_geo(L);
+    const int nq = L.d.nx / 4;
+    dim3 grid((nq + 127) / 128, L.d.ny, L.d.nz);
+    k_cell_classes<<<grid, 128, 0, s>>>(g, L.coef, m.cls_ptr, m.cls_pitch);
+    return post("cell_classes");
+}
+
+int sweep_tma(const Level &L, const SweepMaps &m, const uint8_t *bricks, int in, int colour_a, float sor,
+              PcgState *st, double *partials, int rz_mode, int sm_count, cudaStream_t s) {
+    FF_CHECK(m.ok, FF_E_STATE, "TMA sweep maps not built");
+    const int out = in == 0 ? 1 : 0;
+    TqArgs a;
+    a.g = make_geo(L);
+    a.x_out = const_cast<float *>(m.xp[out]);
+    a.coef = L.coef;
+    a.bricks = bricks;
+    a.sor = sor;
+    a.rdreg_sor = sor / a.g.dreg;
+    a.colour_a = colour_a;
+    a.zc = tma_zchunk(L.d, sm_count);
+    a.st = st;
+    a.partials = partials;
+    a.rz_mode = rz_mode;
+    dim3 grid((L.d.nx + tq::TX - 1) / tq::TX, (L.d.ny + tq::TY - 1) / tq::TY, (L.d.nz + a.zc - 1) / a.zc);
+    const CUtensorMap &xm = m.x[in < 0 ? out : in];
+    const bool rz = rz_mode != 0;
+    if (in < 0) {
+        if (rz) k_sweep_tma<true, true><<<grid, tq::NT, tq::SMEM, s>>>(a, xm, m.b, m.cls);
+        else k_sweep_tma<true, false><<<grid, tq::NT, tq::SMEM, s>>>(a, xm, m.b, m.cls);
+    } else {
+        if (rz) k_sweep_tma<false, true><<<grid, tq::NT, tq::SMEM, s>>>(a, xm, m.b, m.cls);
+        else k_sweep_tma<false, false><<<grid, tq::NT, tq::SMEM, s>>>(a, xm, m.b, m.cls);
+    }
+    return post("sweep_tma");
+}
+
 int res_restrict(const Level &f, const uint8_t *bricks, const float *x, Level &c, int dims,
                  const PcgState *st, int sm_count, cudaStream_t s) {
     RrArgs a;
@@ -969,6 +1487,10 @@ int fused_configure() {
     FF_CUDA(cudaFuncSetAttribute(k_sweep<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem()));
     FF_CUDA(cudaFuncSetAttribute(k_sweep<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem()));
     FF_CUDA(cudaFuncSetAttribute(k_sweep<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem()));
+    FF_CUDA(cudaFuncSetAttribute(k_sweep_tma<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tq::SMEM));
+    FF_CUDA(cudaFuncSetAttribute(k_sweep_tma<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tq::SMEM));
+    FF_CUDA(cudaFuncSetAttribute(k_sweep_tma<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tq::SMEM));
+    FF_CUDA(cudaFuncSetAttribute(k_sweep_tma<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tq::SMEM));
     FF_CUDA(cudaFuncSetAttribute(k_res_restrict, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rr_smem()));
     FF_CUDA(cudaFuncSetAttribute(k_p_pap, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p_pap_smem()));
     FF_CUDA(cudaFuncSetAttribute(k_x_residual<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,

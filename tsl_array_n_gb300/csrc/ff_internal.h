@@ -1,5 +1,6 @@
 // Internal declarations shared by the libff translation units.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include <stdint.h>
@@ -73,7 +74,8 @@ struct PcgState {
     double alpha, beta, thr, tol, best_rr;
     int stop, iter, stop_iter, first;
     int maxiter, relative, p_cur, x_cur;
-    int launched, bad_cells, growth_stop, pad;
+    int launched, bad_cells, growth_stop;
+    int err;   // nonzero: a kernel gave up on a bounded wait (bit 0: TMA staging)
     unsigned ticket[4];
 };
 
@@ -92,6 +94,21 @@ struct Level {
     float4 *coef = nullptr;                        // fp32 coefficients
     uint2 *coef16 = nullptr;                       // bf16 coefficients (4 x bf16)
     void *x = nullptr, *b = nullptr, *buf = nullptr;  // storage type per mode
+};
+
+// TMA descriptors of one level's sweep operands: the two x buffers (ping-pong)
+// and b, each as a 3D FP32 tensor with the staged box of the TMA sweep.
+// cls: one byte per x-quad, two bits per cell (0 interior with the plain
+// coefficients, 1 Dirichlet, 2 domain edge with the plain coefficients,
+// 3 anything else), rows padded to 16 bytes.
+struct SweepMaps {
+    CUtensorMap x[2];
+    CUtensorMap b;
+    CUtensorMap cls;
+    const float *xp[2] = {nullptr, nullptr};
+    uint8_t *cls_ptr = nullptr;
+    int cls_pitch = 0;
+    bool ok = false;
 };
 
 // --------------------------------------------------------- kernel launchers --
@@ -162,6 +179,15 @@ int brick_flags(const Level &L, uint8_t *bricks, cudaStream_t s);
 int sweep(const Level &L, const uint8_t *bricks, const float *x_in, float *x_out, int colour_a, float sor,
           int first, const Level *coarse, int dims, PcgState *st, double *partials, int rz_mode,
           int sm_count, cudaStream_t s);
+// TMA-staged sweep (levels with nx % 4 == 0 and nx >= 32): x_in is the
+// buffer maps.xp[in] (in < 0: x_in identically zero), x_out the other one
+bool sweep_tma_ok(const Dims &d);
+size_t sweep_tma_cls_bytes(const Dims &d);
+int sweep_tma_maps(const Level &L, const float *x0, const float *x1, uint8_t *cls, SweepMaps &m);
+int cell_classes(const Level &L, const SweepMaps &m, cudaStream_t s);
+int sweep_tma(const Level &L, const SweepMaps &m, const uint8_t *bricks, int in, int colour_a, float sor,
+              PcgState *st, double *partials, int rz_mode, int sm_count, cudaStream_t s);
+size_t sweep_tma_blocks(const Dims &d, int sm_count);
 int res_restrict(const Level &f, const uint8_t *bricks, const float *x, Level &c, int dims,
                  const PcgState *st, int sm_count, cudaStream_t s);
 int fused_p_pap(const Level &L0, const uint8_t *bricks, const float *z, float *p0, float *p1,

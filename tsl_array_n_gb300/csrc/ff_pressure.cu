@@ -53,6 +53,9 @@ struct ff_pressure_s {
     std::vector<float *> x2;
     std::vector<uint8_t *> bricks;
     float *z_final = nullptr;
+    // TMA descriptors per level (levels where the TMA sweep applies)
+    SweepMaps *smaps = nullptr;
+    bool use_tma = true;
 
     // coarsest direct solve
     double *G = nullptr;
@@ -220,6 +223,18 @@ extern "C" int ff_pressure3_create(ff_ctx ctx, const ff_pressure_desc *desc, ff_
                        div_up(g.ny, 256 / (g.nx >= 128 ? 128 : g.nx >= 64 ? 64 : 32)) * g.nz;
     blocks = std::max(blocks, (long long)div_up(n, 1024));
     blocks = std::max(blocks, (long long)ffk::fused_blocks(ps->d, ctx->sm_count));
+    if (ps->fused) {
+        ps->smaps = new SweepMaps[L];
+        for (int l = 0; l < L; ++l) {
+            Level &v = ps->lv[l];
+            if (l == L - 1 || !ffk::sweep_tma_ok(v.d)) continue;
+            uint8_t *cls = nullptr;
+            if ((st = ff_dev_alloc((void **)&cls, ffk::sweep_tma_cls_bytes(v.d), s))) return bail(st);
+            ps->smaps[l].cls_ptr = cls;
+            if ((st = ffk::sweep_tma_maps(v, (const float *)v.x, ps->x2[l], cls, ps->smaps[l]))) return bail(st);
+            blocks = std::max(blocks, (long long)ffk::sweep_tma_blocks(v.d, ctx->sm_count));
+        }
+    }
     if ((st = ff_dev_alloc((void **)&ps->partials, (size_t)blocks * 2 * sizeof(double), s))) return bail(st);
     if (cudaStreamSynchronize(s) != cudaSuccess) return bail(ff_set_error(FF_E_CUDA, "sync after create"));
     *out = ps;
@@ -230,6 +245,9 @@ extern "C" int ff_pressure3_destroy(ff_pressure ps) {
     if (!ps) return FF_OK;
     cudaStreamSynchronize(ps->ctx->stream);
     destroy_graphs(ps);
+    if (ps->smaps)
+        for (size_t l = 0; l < ps->lv.size(); ++l) ff_dev_free(ps->smaps[l].cls_ptr);
+    delete[] ps->smaps;
     ff_field_destroy(ps->pressure);
     ff_field_destroy(ps->bfield);
     ff_field_destroy(ps->maskf);
@@ -320,6 +338,7 @@ extern "C" int ff_pressure3_set(ff_pressure ps, const char *key, double value) {
     else if (k == "relativeTolerance") { ps->desc.relative_tolerance = value != 0; destroy_graphs(ps); }
     else if (k == "checkBadCells") ps->check_bad = value != 0;
     else if (k == "useGraph") { ps->use_graph = value != 0; }
+    else if (k == "useTma") { ps->use_tma = value != 0; destroy_graphs(ps); }
     else if (k == "preconditioner") {
         FF_CHECK(value >= 0 && value <= 2, FF_E_ARG, "unknown preconditioner %g", value);
         ps->desc.preconditioner = (int)value;
@@ -406,9 +425,11 @@ static int prepare(ff_pressure ps, ff_field u, ff_field v, ff_field w) {
         }
         FF_TRY(ffk::build_coef(c, ps->dims, ps->vbf(), s));
         if (ps->bricks[l]) FF_TRY(ffk::brick_flags(c, ps->bricks[l], s));
+        if (ps->smaps && ps->smaps[l].ok) FF_TRY(ffk::cell_classes(c, ps->smaps[l], s));
     }
     FF_TRY(ffk::build_coef(L0, ps->dims, ps->vbf(), s));
     if (ps->bricks[0]) FF_TRY(ffk::brick_flags(L0, ps->bricks[0], s));
+    if (ps->smaps && ps->smaps[0].ok) FF_TRY(ffk::cell_classes(L0, ps->smaps[0], s));
     ps->prepared = true;
     // FP64 direct coarsest solve: refactor when the coarsest operator changed
     if (ps->desc.preconditioner == FF_PRE_MULTIGRID && ps->desc.mg_coarse_mode == FF_COARSE_DIRECT) {
@@ -506,6 +527,25 @@ static int vcycle(ff_pressure ps, int l, const PcgState *st) {
 // `out` receives the buffer holding level l's final x.  rz_mode (level 0
 // only): 0 none, 1 r.z + beta, 2 r.z + seed, fused into the last sweep; the
 // return flag `rz_done` says whether it was.
+// One fused sweep on level l from bufs[cur] (cur < 0: x = 0) into
+// bufs[nxt]: the TMA-staged kernel where the level has descriptors, the
+// cp.async kernel elsewhere.
+static int level_sweep(ff_pressure ps, int l, PcgState *st, float *const bufs[2], int cur, int nxt, int colour_a,
+                       int rz_mode) {
+    Level &v = ps->lv[l];
+    const float sor = (float)ps->desc.mg_sor;
+    if (ps->use_tma && ps->smaps && ps->smaps[l].ok) {
+        // descriptors index the buffers as {level x, second buffer}
+        const int in = cur < 0 ? -1 : (bufs[cur] == ps->smaps[l].xp[0] ? 0 : 1);
+        const int out = in == 0 ? 1 : 0;
+        FF_CHECK(bufs[nxt] == ps->smaps[l].xp[out], FF_E_STATE, "sweep buffers do not match the TMA descriptors");
+        return ffk::sweep_tma(v, ps->smaps[l], ps->bricks[l], in, colour_a, sor, st, ps->partials, rz_mode,
+                              ps->ctx->sm_count, ps->s());
+    }
+    return ffk::sweep(v, ps->bricks[l], cur < 0 ? nullptr : bufs[cur], bufs[nxt], colour_a, sor, cur < 0, nullptr,
+                      ps->dims, st, ps->partials, rz_mode, ps->ctx->sm_count, ps->s());
+}
+
 static int vcycle_fused(ff_pressure ps, int l, PcgState *st, int rz_mode, float **out, bool *rz_done) {
     const int Ln = (int)ps->lv.size();
     Level &v = ps->lv[l];
@@ -523,8 +563,7 @@ static int vcycle_fused(ff_pressure ps, int l, PcgState *st, int rz_mode, float 
         } else {
             for (int it = 0; it < ps->desc.mg_coarsest; ++it) {
                 int nxt = cur < 0 ? 0 : 1 - cur;
-                FF_TRY(ffk::sweep(v, ps->bricks[l], cur < 0 ? nullptr : bufs[cur], bufs[nxt], 0, sor, cur < 0,
-                                  nullptr, ps->dims, st, ps->partials, 0, ps->ctx->sm_count, s));
+                FF_TRY(level_sweep(ps, l, st, bufs, cur, nxt, 0, 0));
                 cur = nxt;
             }
             if (cur == 1) FF_CUDA(cudaMemcpyAsync(v.x, bufs[1], (size_t)v.d.n() * 4, cudaMemcpyDeviceToDevice, s));
@@ -536,8 +575,7 @@ static int vcycle_fused(ff_pressure ps, int l, PcgState *st, int rz_mode, float 
     // pre-smoothing, colour 0 then 1 (relax, multigrid.js:1589-1607)
     for (int it = 0; it < ps->desc.mg_down; ++it) {
         int nxt = cur < 0 ? 0 : 1 - cur;
-        FF_TRY(ffk::sweep(v, ps->bricks[l], cur < 0 ? nullptr : bufs[cur], bufs[nxt], 0, sor, cur < 0, nullptr,
-                          ps->dims, st, ps->partials, 0, ps->ctx->sm_count, s));
+        FF_TRY(level_sweep(ps, l, st, bufs, cur, nxt, 0, 0));
         cur = nxt;
     }
     if (cur < 0) {
@@ -565,8 +603,7 @@ static int vcycle_fused(ff_pressure ps, int l, PcgState *st, int rz_mode, float 
         int nxt = 1 - cur;
         bool last = it == up - 1;
         int rz = (l == 0 && last) ? rz_mode : 0;
-        FF_TRY(ffk::sweep(v, ps->bricks[l], bufs[cur], bufs[nxt], 1, sor, 0, nullptr,
-                          ps->dims, st, ps->partials, rz, ps->ctx->sm_count, s));
+        FF_TRY(level_sweep(ps, l, st, bufs, cur, nxt, 1, rz));
         if (rz) *rz_done = true;
         cur = nxt;
     }
@@ -760,6 +797,9 @@ static int read_diag(ff_pressure ps, ff_diag *diag, int extra_launches) {
     cudaStream_t s = ps->s();
     FF_CUDA(cudaMemcpyAsync(ps->st_host, ps->st, sizeof(PcgState), cudaMemcpyDeviceToHost, s));
     FF_CUDA(cudaStreamSynchronize(s));
+    FF_CHECK(ps->st_host->err == 0, FF_E_CUDA,
+             "a solver kernel gave up waiting for its staged data (error bits 0x%x); the result is invalid",
+             ps->st_host->err);
     if (diag) {
         const PcgState &h = *ps->st_host;
         diag->converged = h.stop == FF_STOP_CONVERGED;
@@ -923,8 +963,10 @@ extern "C" int ff_pressure3_profile(ff_pressure ps, int which, int reps, float *
         case FF_PROF_RELAX:
             // BF16 path: one colour pass; FP32 path: one fused sweep (both colours)
             rc = nf ? ffk::mg_relax(L0, ps->dims, r & 1, (float)ps->desc.mg_sor, 0, 0, 0, vb, ps->st, s)
-                    : ffk::sweep(L0, ps->bricks[0], (float *)L0.x, ps->x2[0], 0, (float)ps->desc.mg_sor, 0, nullptr,
-                                 ps->dims, ps->st, ps->partials, 0, ps->ctx->sm_count, s);
+                    : [&] {
+                          float *const bufs[2] = {(float *)L0.x, ps->x2[0]};
+                          return level_sweep(ps, 0, ps->st, bufs, 0, 1, 0, 0);
+                      }();
             break;
         case FF_PROF_RESIDUAL:
             // fused path: residual + restriction in one kernel
