@@ -182,6 +182,21 @@ typedef struct {
 int ff_collider3_bake(ff_ctx ctx, const ff_shape *shapes, int nshapes, int invert,
                       const int *resolution, const double *grid_spacing, const double *origin,
                       ff_field phi, ff_field wu, ff_field wv, ff_field ww);
+/* ff_collider3_bake without any device allocation (no counterpart in the
+ * reference, which bakes on the CPU).  For hosts that may not allocate device
+ * memory while they run: a process whose device memory is owned by an outside
+ * pool, or a frame loop that cannot take the implicit device-wide
+ * synchronisation of cudaMalloc/cudaFree.  The shape table lives in one
+ * fixed device array of FF_BAKE_NOALLOC_MAX_SHAPES entries per device; more
+ * shapes return FF_E_LIMIT.  The first call on a device looks the array up
+ * (make it before any stream capture).  The array is shared by every caller
+ * on the device: calls that overlap in time (two contexts, two threads) race
+ * on it and must be serialised.  Same arguments, outputs and errors as
+ * ff_collider3_bake; the call returns without synchronising the stream.    */
+#define FF_BAKE_NOALLOC_MAX_SHAPES 64
+int ff_collider3_bake_noalloc(ff_ctx ctx, const ff_shape *shapes, int nshapes, int invert,
+                              const int *resolution, const double *grid_spacing, const double *origin,
+                              ff_field phi, ff_field wu, ff_field wv, ff_field ww);
 
 /* ---- test hooks mirroring the exported multigrid.js / linalg.js pieces -- */
 /* createLaplacianOperator (multigrid.js:457-471): y = A x with the solver's

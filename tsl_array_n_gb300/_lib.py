@@ -78,6 +78,8 @@ PROTOTYPES = {
     "ff_pressure3_prepare": (_I, [_P, _P, _P, _P]),
     "ff_collider3_bake": (_I, [_P, C.POINTER(Shape), _I, _I, _IP, C.POINTER(C.c_double),
                                C.POINTER(C.c_double), _P, _P, _P, _P]),
+    "ff_collider3_bake_noalloc": (_I, [_P, C.POINTER(Shape), _I, _I, _IP, C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double), _P, _P, _P, _P]),
     "ff_laplacian_apply": (_I, [_P, _P, _P]),
     "ff_precondition_apply": (_I, [_P, _P, _P]),
     "ff_mg_restrict": (_I, [_P, _I, _P, _P]),

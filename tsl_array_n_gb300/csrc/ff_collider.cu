@@ -5,6 +5,7 @@
 //   fractionInsideCpu / fractionInsideSdfCpu (src/grid/level_set_utils.js:51-161)
 //   primitiveDistanceCpu                (src/grid/primitive_sdf3.js:169-208)
 #include "ff_internal.h"
+#include <atomic>
 #include <cmath>
 
 namespace {
@@ -205,5 +206,111 @@ extern "C" int ff_collider3_bake(ff_ctx ctx, const ff_shape *shapes, int nshapes
     FF_CUDA(cudaGetLastError());
     FF_CUDA(cudaStreamSynchronize(s));
     cudaFree(dsh);
+    return FF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// ff_collider3_bake_noalloc: the same bake with its shape table in a
+// fixed-size device array instead of a per-call cudaMalloc/cudaFree.
+//
+// Who needs it: a host that bakes colliders inside a loop where a device
+// allocation is not allowed -- a process running under a fixed device-memory
+// budget managed by someone else's pool, or a frame loop where the implicit
+// device-wide synchronisation of cudaMalloc/cudaFree would stall work queued
+// on other streams.  This entry point makes no allocation and no allocating
+// library call; its only device scratch is g_bake_shapes below.
+//
+// Setup: the first call on each device looks up the array's device address
+// (cudaGetSymbolAddress, which may load the module); make that first call
+// before any stream capture.  Later calls only copy the table and launch.
+//
+// Nothing in the table has to start at zero: the kernels read entries
+// 0..nshapes-1 only, and this call writes exactly those before its kernels
+// run (same stream).  There is one table per device, so calls that overlap
+// in time -- from two contexts' streams on the same device, or from two host
+// threads -- race on it; serialise them.
+namespace {
+constexpr int BAKE_NOALLOC_MAX_SHAPES = FF_BAKE_NOALLOC_MAX_SHAPES;
+static __device__ __align__(256) Shape g_bake_shapes[BAKE_NOALLOC_MAX_SHAPES];
+
+constexpr int MAX_DEVICES = 64;
+std::atomic<void *> g_bake_table[MAX_DEVICES] = {};
+
+// device address of g_bake_shapes on `device` (the current device), looked up
+// once per device
+int bake_table(int device, Shape **out) {
+    FF_CHECK(device >= 0 && device < MAX_DEVICES, FF_E_LIMIT, "ff_collider3_bake_noalloc: device %d out of range",
+             device);
+    void *p = g_bake_table[device].load(std::memory_order_acquire);
+    if (!p) {
+        cudaError_t e = cudaGetSymbolAddress(&p, g_bake_shapes);
+        FF_CHECK(e == cudaSuccess && p, FF_E_CUDA, "ff_collider3_bake_noalloc: cudaGetSymbolAddress: %s",
+                 cudaGetErrorString(e));
+        g_bake_table[device].store(p, std::memory_order_release);
+    }
+    *out = static_cast<Shape *>(p);
+    return FF_OK;
+}
+}  // namespace
+
+extern "C" int ff_collider3_bake_noalloc(ff_ctx ctx, const ff_shape *shapes, int nshapes, int invert,
+                                         const int *res, const double *h, const double *origin, ff_field phi,
+                                         ff_field wu, ff_field wv, ff_field ww) {
+    FF_CHECK(ctx && res && h && origin, FF_E_ARG, "ff_collider3_bake_noalloc: NULL argument");
+    FF_CHECK(nshapes >= 0 && nshapes <= BAKE_NOALLOC_MAX_SHAPES, FF_E_LIMIT,
+             "ff_collider3_bake_noalloc: %d shapes exceed the fixed table of %d (use ff_collider3_bake)", nshapes,
+             BAKE_NOALLOC_MAX_SHAPES);
+    FF_CHECK(nshapes == 0 || shapes, FF_E_ARG, "ff_collider3_bake_noalloc: shapes is NULL");
+    const int nx = res[0], ny = res[1], nz = res[2];
+    FF_CHECK(!phi || (phi->count == (long long)nx * ny * nz && phi->dtype == FF_FLOAT), FF_E_ARG, "phi field shape");
+    ff_field ws[3] = {wu, wv, ww};
+    for (int a = 0; a < 3; ++a)
+        FF_CHECK(!ws[a] || (ws[a]->count == (long long)(nx + (a == 0)) * (ny + (a == 1)) * (nz + (a == 2)) &&
+                            ws[a]->dtype == FF_FLOAT),
+                 FF_E_ARG, "face weight field %d shape", a);
+    // shape records as the kernels read them (primitive_sdf3.js:169-200)
+    Shape hs[BAKE_NOALLOC_MAX_SHAPES];
+    for (int q = 0; q < nshapes; ++q) {
+        const ff_shape &src = shapes[q];
+        FF_CHECK(src.type == FF_SHAPE_SPHERE || src.type == FF_SHAPE_BOX, FF_E_ARG,
+                 "primitive_sdf3: unknown shape type '%d'.", src.type);
+        Shape &dst = hs[q];
+        dst.type = src.type == FF_SHAPE_SPHERE ? 0 : 1;
+        dst.has_rotation = src.has_rotation;
+        for (int c = 0; c < 3; ++c) {
+            dst.center[c] = src.center[c];
+            dst.half[c] = src.half_extents[c];
+        }
+        dst.radius = src.radius;
+        const double len = std::sqrt(src.rotation_axis[0] * src.rotation_axis[0] +
+                                     src.rotation_axis[1] * src.rotation_axis[1] +
+                                     src.rotation_axis[2] * src.rotation_axis[2]);
+        for (int c = 0; c < 3; ++c) dst.axis[c] = len > 0 ? src.rotation_axis[c] / len : (c == 2 ? 1.0 : 0.0);
+        dst.angle = src.rotation_angle;
+    }
+    FF_CUDA(cudaSetDevice(ctx->device));
+    Shape *table = nullptr;
+    FF_TRY(bake_table(ctx->device, &table));
+    cudaStream_t s = ctx->stream;
+    // pageable source: the copy has taken the bytes when it returns
+    if (nshapes) FF_CUDA(cudaMemcpyAsync(table, hs, sizeof(Shape) * nshapes, cudaMemcpyHostToDevice, s));
+    const double sign = invert ? -1.0 : 1.0;
+    const dim3 blk(64, 4, 1);
+    if (phi) {
+        dim3 g((nx + 63) / 64, (ny + 3) / 4, nz);
+        k_bake_phi<<<g, blk, 0, s>>>(table, nshapes, sign, nx, ny, nz, origin[0], origin[1], origin[2], h[0], h[1],
+                                     h[2], (float *)phi->d);
+    }
+    for (int a = 0; a < 3; ++a) {
+        if (!ws[a]) continue;
+        const int fx = nx + (a == 0), fy = ny + (a == 1), fz = nz + (a == 2);
+        // dataOriginU/V/W (sdf_collider3.js:226-228)
+        const double o[3] = {origin[0] + (a != 0 ? 0.5 * h[0] : 0.0), origin[1] + (a != 1 ? 0.5 * h[1] : 0.0),
+                             origin[2] + (a != 2 ? 0.5 * h[2] : 0.0)};
+        dim3 g((fx + 63) / 64, (fy + 3) / 4, fz);
+        k_face_weights<<<g, blk, 0, s>>>(table, nshapes, sign, a, fx, fy, fz, o[0], o[1], o[2], h[0], h[1], h[2],
+                                         (float *)ws[a]->d);
+    }
+    FF_CUDA(cudaGetLastError());
     return FF_OK;
 }
