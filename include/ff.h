@@ -198,6 +198,70 @@ int ff_collider3_bake_noalloc(ff_ctx ctx, const ff_shape *shapes, int nshapes, i
                               const int *resolution, const double *grid_spacing, const double *origin,
                               ff_field phi, ff_field wu, ff_field wv, ff_field ww);
 
+/* ---- semi-Lagrangian advection: replaces createSemiLagrangianAdvectionSolver3
+ * (fluxflow src/grid/advection_solver3.js:67-364).  The trace is backTrace
+ * (:20-62): RK2 midpoint substeps of at most one cell (h = min spacing),
+ * at most max_substeps, stopping on the collider SDF with a linear blend.
+ * The final sample is the monotone tricubic of grid_math3.js:137-215.  FP32
+ * with every operation rounded on its own, as the reference's WGSL.       */
+typedef struct ff_advect_s *ff_advect;
+typedef struct {
+    int resolution[3];
+    double grid_spacing[3];
+    double origin[3];
+    double dt;                  /* dt (:67)                            */
+    int max_substeps;           /* maxSubsteps, default 32             */
+    int order;                  /* 1 semi-Lagrangian, 2 MacCormack     */
+} ff_advect_desc;
+int ff_advect3_create(ff_ctx ctx, const ff_advect_desc *desc, ff_advect *out);
+int ff_advect3_destroy(ff_advect a);
+int ff_advect3_set_dt(ff_advect a, double dt);
+/* collider: cell-centred SDF field sampled trilinearly (sdf_collider3.js:33),
+ * or NULL (boundary sample 1 everywhere).  Borrowed.                       */
+int ff_advect3_set_collider(ff_advect a, ff_field phi);
+/* advectFaceCentered3(input, output) (:130-178): every face whose position
+ * samples the collider > 0 gets the cubic sample of `in` at trace(position)
+ * through the velocity (vu, vv, vw); other faces keep the output's value. */
+int ff_advect3_faces(ff_advect a, ff_field vu, ff_field vv, ff_field vw, ff_field in_u, ff_field in_v,
+                     ff_field in_w, ff_field out_u, ff_field out_v, ff_field out_w);
+/* advectScalar3 (:304-360) of a cell-centred scalar */
+int ff_advect3_scalar(ff_advect a, ff_field vu, ff_field vv, ff_field vw, ff_field s_in, ff_field s_out);
+/* trace(start, direction) (:363) of FF_VEC3 points; direction 1 traces
+ * back in time, -1 forward (the FLIP particle advection).                 */
+int ff_advect3_trace(ff_advect a, ff_field vu, ff_field vv, ff_field vw, ff_field p_in, ff_field p_out,
+                     int direction);
+
+/* ---- velocity constraint: replaces createGridBlockedBoundaryConditionSolver3
+ * (fluxflow src/grid/grid_blocked_boundary_condition_solver3.js:48-490).    */
+#define FF_DIRECTION_LEFT 1
+#define FF_DIRECTION_RIGHT 2
+#define FF_DIRECTION_DOWN 4
+#define FF_DIRECTION_UP 8
+#define FF_DIRECTION_BACK 16
+#define FF_DIRECTION_FRONT 32
+#define FF_DIRECTION_ALL_3D 63      /* constant.js:24-38 */
+typedef struct ff_bc_s *ff_bc;
+int ff_bc3_create(ff_ctx ctx, const int *resolution, const double *grid_spacing, const double *origin,
+                  ff_bc *out);
+int ff_bc3_destroy(ff_bc b);
+/* setCollider (:390-404): a static SDF collider (cell field, solid where
+ * phi < 0, friction 0.5) and optionally its face weights (colliderFaceWeights,
+ * :60-62), which then decide the closed faces.  NULL phi removes it.       */
+int ff_bc3_set_collider(ff_bc b, ff_field phi, ff_field wu, ff_field wv, ff_field ww);
+/* closedDomainBoundaryFlag (:102), FF_DIRECTION_* bits, default ALL_3D    */
+int ff_bc3_set_closed(ff_bc b, int flags);
+/* setInflows (:138-146): n inflow SDFs (cell fields, inside where < 0),
+ * velocities (3 per inflow) and modes (0 'set', 1 'add'); n == 0 clears.   */
+int ff_bc3_set_inflows(ff_bc b, int n, const ff_field *phis, const double *velocities, const int *modes);
+/* constrainVelocity(extrapolationDepth = 5) (:445-477), in place          */
+int ff_bc3_constrain(ff_bc b, ff_field u, ff_field v, ff_field w, int depth);
+
+/* ---- explicit viscosity (no counterpart: grid_solver3.js:104 leaves
+ * computeViscosity a no-op): out = in + dt nu lap(in) on the faces strictly
+ * inside each component's own axis range, Neumann at the array ends.       */
+int ff_viscosity3_apply(ff_ctx ctx, const int *resolution, const double *grid_spacing, ff_field u, ff_field v,
+                        ff_field w, double nu, double dt, ff_field u_out, ff_field v_out, ff_field w_out);
+
 /* ---- test hooks mirroring the exported multigrid.js / linalg.js pieces -- */
 /* createLaplacianOperator (multigrid.js:457-471): y = A x with the solver's
  * current level-0 system (call ff_pressure3_prepare first).                 */

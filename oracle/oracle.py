@@ -81,6 +81,12 @@ def _declare(L):
     L.orc_fraction_inside.restype = D
     fp = C.POINTER(C.c_float)
     L.orc_collider_bake.argtypes = [_dp, I, I, I, I, I, D, D, D, D, D, D, fp, fp, fp, fp]
+    ip, F, L64 = C.POINTER(C.c_int), C.c_float, C.c_int64
+    L.orc_trace.argtypes = [ip, fp, fp, fp, fp, fp, fp, F, I, F, L64, fp, fp]
+    L.orc_advect_faces.argtypes = [ip, fp, fp, fp, fp, fp, fp, F, I, I, fp, fp, fp]
+    L.orc_advect_scalar.argtypes = [ip, fp, fp, fp, fp, fp, fp, F, I, I, fp, fp]
+    L.orc_constrain_velocity.argtypes = [ip, fp, fp, fp, fp, fp, fp, fp, fp, fp, I, I, fp, fp, ip, I]
+    L.orc_viscosity.argtypes = [ip, fp, fp, fp, fp, F, F, fp, fp, fp]
 
 
 def _shape_row(s):
@@ -347,3 +353,83 @@ def round_bf16(a):
     lsb = (u >> 16) & 1
     r = ((u + 0x7FFF + lsb) & 0xFFFF0000).astype(np.uint32)
     return r.view(np.float32)
+
+
+# ---------------------------------------------- FP32 grid-velocity kernels --
+# advection_solver3.js, grid_blocked_boundary_condition_solver3.js and the
+# explicit viscosity, restated in C floats (ff_oracle_grid.c).
+def _f32(a):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, dtype=np.float32).ravel()
+    return a
+
+
+def _fptr(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _geom(shape, h, origin):
+    res = (C.c_int * 3)(*shape)
+    hh = (C.c_float * 3)(*[float(x) for x in h])
+    oo = (C.c_float * 3)(*[float(x) for x in origin])
+    return res, hh, oo
+
+
+def trace(shape, h, origin, u, v, w, phi, points, dt, direction=1, max_substeps=32):
+    u, v, w, phi = _f32(u), _f32(v), _f32(w), _f32(phi)
+    p = _f32(points)
+    out = np.empty_like(p)
+    res, hh, oo = _geom(shape, h, origin)
+    lib().orc_trace(res, hh, oo, _fptr(u), _fptr(v), _fptr(w), _fptr(phi), float(dt), int(max_substeps),
+                    float(-1.0 if direction == -1 else 1.0), p.size // 3, _fptr(p), _fptr(out))
+    return out
+
+
+def advect_faces(shape, h, origin, u, v, w, phi, dt, order=1, max_substeps=32, out=None):
+    """advectFaceCentered3 of (u, v, w) through itself; `out` (u, v, w)
+    gives the values kept on faces inside the collider (default: the input)."""
+    u, v, w, phi = _f32(u), _f32(v), _f32(w), _f32(phi)
+    uo, vo, wo = (x.copy() for x in (out if out is not None else (u, v, w)))
+    uo, vo, wo = _f32(uo), _f32(vo), _f32(wo)
+    res, hh, oo = _geom(shape, h, origin)
+    lib().orc_advect_faces(res, hh, oo, _fptr(u), _fptr(v), _fptr(w), _fptr(phi), float(dt), int(max_substeps),
+                           int(order), _fptr(uo), _fptr(vo), _fptr(wo))
+    return uo, vo, wo
+
+
+def advect_scalar(shape, h, origin, u, v, w, phi, s, dt, order=1, max_substeps=32, out=None):
+    u, v, w, phi, s = _f32(u), _f32(v), _f32(w), _f32(phi), _f32(s)
+    so = _f32(out.copy() if out is not None else s.copy())
+    res, hh, oo = _geom(shape, h, origin)
+    lib().orc_advect_scalar(res, hh, oo, _fptr(u), _fptr(v), _fptr(w), _fptr(phi), float(dt), int(max_substeps),
+                            int(order), _fptr(s), _fptr(so))
+    return so
+
+
+def constrain_velocity(shape, h, origin, u, v, w, phi=None, face_weights=None, closed=63, inflows=(), depth=5):
+    """constrainVelocity(depth); inflows: list of (phi, (vx, vy, vz), mode)."""
+    u, v, w = (_f32(x).copy() for x in (u, v, w))
+    phi = _f32(phi)
+    fw = [None, None, None] if face_weights is None else [_f32(x) for x in face_weights]
+    n_in = len(inflows)
+    ncell = shape[0] * shape[1] * shape[2]
+    phis = np.concatenate([_f32(q[0]) for q in inflows]) if n_in else np.zeros(1, np.float32)
+    vel = np.array([c for q in inflows for c in q[1]] or [0.0], np.float32)
+    modes = (C.c_int * max(1, n_in))(*[int(q[2]) for q in inflows])
+    assert phis.size == max(1, n_in * ncell) or n_in == 0
+    res, hh, oo = _geom(shape, h, origin)
+    lib().orc_constrain_velocity(res, hh, oo, _fptr(u), _fptr(v), _fptr(w), _fptr(phi), _fptr(fw[0]),
+                                 _fptr(fw[1]), _fptr(fw[2]), int(closed), n_in, _fptr(phis), _fptr(vel), modes,
+                                 int(depth))
+    return u, v, w
+
+
+def viscosity(shape, h, u, v, w, nu, dt):
+    u, v, w = _f32(u), _f32(v), _f32(w)
+    uo, vo, wo = np.empty_like(u), np.empty_like(v), np.empty_like(w)
+    res = (C.c_int * 3)(*shape)
+    hh = (C.c_float * 3)(*[float(x) for x in h])
+    lib().orc_viscosity(res, hh, _fptr(u), _fptr(v), _fptr(w), float(nu), float(dt), _fptr(uo), _fptr(vo),
+                        _fptr(wo))
+    return uo, vo, wo

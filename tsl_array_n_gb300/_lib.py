@@ -34,6 +34,11 @@ class Shape(C.Structure):
                 ("rotation_axis", C.c_double * 3), ("rotation_angle", C.c_double)]
 
 
+class AdvectDesc(C.Structure):
+    _fields_ = [("resolution", C.c_int * 3), ("grid_spacing", C.c_double * 3), ("origin", C.c_double * 3),
+                ("dt", C.c_double), ("max_substeps", C.c_int), ("order", C.c_int)]
+
+
 class Diag(C.Structure):
     _fields_ = [("converged", C.c_int), ("rejected", C.c_int), ("iterations", C.c_int),
                 ("stopped_by", C.c_int), ("residual", C.c_double), ("b_norm", C.c_double),
@@ -80,6 +85,20 @@ PROTOTYPES = {
                                C.POINTER(C.c_double), _P, _P, _P, _P]),
     "ff_collider3_bake_noalloc": (_I, [_P, C.POINTER(Shape), _I, _I, _IP, C.POINTER(C.c_double),
                                        C.POINTER(C.c_double), _P, _P, _P, _P]),
+    "ff_advect3_create": (_I, [_P, C.POINTER(AdvectDesc), _PP]),
+    "ff_advect3_destroy": (_I, [_P]),
+    "ff_advect3_set_dt": (_I, [_P, _D]),
+    "ff_advect3_set_collider": (_I, [_P, _P]),
+    "ff_advect3_faces": (_I, [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "ff_advect3_scalar": (_I, [_P, _P, _P, _P, _P, _P]),
+    "ff_advect3_trace": (_I, [_P, _P, _P, _P, _P, _P, _I]),
+    "ff_bc3_create": (_I, [_P, _IP, C.POINTER(C.c_double), C.POINTER(C.c_double), _PP]),
+    "ff_bc3_destroy": (_I, [_P]),
+    "ff_bc3_set_collider": (_I, [_P, _P, _P, _P, _P]),
+    "ff_bc3_set_closed": (_I, [_P, _I]),
+    "ff_bc3_set_inflows": (_I, [_P, _I, _PP, C.POINTER(C.c_double), _IP]),
+    "ff_bc3_constrain": (_I, [_P, _P, _P, _P, _I]),
+    "ff_viscosity3_apply": (_I, [_P, _IP, C.POINTER(C.c_double), _P, _P, _P, _D, _D, _P, _P, _P]),
     "ff_laplacian_apply": (_I, [_P, _P, _P]),
     "ff_precondition_apply": (_I, [_P, _P, _P]),
     "ff_mg_restrict": (_I, [_P, _I, _P, _P]),

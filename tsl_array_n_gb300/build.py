@@ -35,14 +35,19 @@ def _headers_mtime():
     return max(os.path.getmtime(h) for h in hs if os.path.exists(h))
 
 
+# per-file extra flags: the grid-velocity kernels round every FP32 operation
+# on its own (no fused multiply-add), as the reference's arithmetic does
+EXTRA = {"ff_grid.cu": ["-fmad=false"]}
+
+
 def _compile(src, verbose):
     obj = os.path.join(BUILD, src + ".o")
     path = os.path.join(CSRC, src)
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(path), _headers_mtime()):
         return obj, ""
-    cmd = [nvcc(), *ARCH, *FLAGS, "-c", path, "-o", obj]
+    cmd = [nvcc(), *ARCH, *FLAGS, *EXTRA.get(src, []), "-c", path, "-o", obj]
     if src.endswith(".cpp"):
-        cmd = [nvcc(), "-x", "cu", *ARCH, *FLAGS, "-c", path, "-o", obj]
+        cmd = [nvcc(), "-x", "cu", *ARCH, *FLAGS, *EXTRA.get(src, []), "-c", path, "-o", obj]
     if verbose:
         cmd += ["-Xptxas", "-v"]
     res = subprocess.run(cmd, capture_output=True, text=True)

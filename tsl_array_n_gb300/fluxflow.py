@@ -8,6 +8,11 @@ Names, option names, defaults and error behaviour follow the reference
   create_sdf_static_collider3     sdf_collider3.js:25-264 (addShapes, computeFaceWeights)
   create_grid_pressure_solver3    grid_pressure_solver3.js:66-574
   create_grid_pressure_solver2    grid_pressure_solver2.js:223-981 (nz == 1)
+  create_semi_lagrangian_advection_solver3  advection_solver3.js:67-364
+  create_sdf_inflow3              sdf_inflow_outflow3.js:15-22
+  create_grid_blocked_boundary_condition_solver3
+                                  grid_blocked_boundary_condition_solver3.js:48-490
+  apply_viscosity3                explicit viscosity (no reference counterpart)
 """
 import ctypes as C
 
@@ -363,3 +368,166 @@ def create_grid_pressure_solver2(resolution, grid_spacing, origin=(0.0, 0.0), **
     solver with nz = 1 (no z axis)."""
     return GridPressureSolver3(tuple(resolution) + (1,), tuple(grid_spacing) + (1.0,),
                                tuple(origin) + (0.0,), **options)
+
+
+# ------------------------------------------------------------- advection --
+class SemiLagrangianAdvectionSolver3:
+    """createSemiLagrangianAdvectionSolver3({velocityGrid, collider, dt,
+    maxSubsteps = 32, order = 1}) (advection_solver3.js:67-364).  Methods
+    return a dispatch function, as the reference returns its batch."""
+
+    def __init__(self, velocity_grid, collider=None, dt=None, max_substeps=32, order=1):
+        if dt is None:
+            raise ValueError("createSemiLagrangianAdvectionSolver3: dt is required.")
+        self.velocity_grid = velocity_grid
+        d = _lib.AdvectDesc()
+        d.resolution[:] = list(velocity_grid.resolution)
+        d.grid_spacing[:] = list(velocity_grid.grid_spacing)
+        d.origin[:] = list(velocity_grid.origin)
+        d.dt = float(dt)
+        d.max_substeps = int(max_substeps)
+        d.order = int(order)
+        self.handle = C.c_void_p()
+        _lib.check(_lib.load().ff_advect3_create(context().handle, C.byref(d), C.byref(self.handle)))
+        self.collider = collider
+        _lib.check(_lib.load().ff_advect3_set_collider(self.handle, collider.phi.handle if collider else None))
+
+    def set_dt(self, dt):
+        _lib.check(_lib.load().ff_advect3_set_dt(self.handle, float(dt)))
+
+    def _vel(self):
+        g = self.velocity_grid
+        return g.data_u.handle, g.data_v.handle, g.data_w.handle
+
+    def advect_face_centered3(self, input_grid, output_grid):
+        def dispatch():
+            _lib.check(_lib.load().ff_advect3_faces(
+                self.handle, *self._vel(), input_grid.data_u.handle, input_grid.data_v.handle,
+                input_grid.data_w.handle, output_grid.data_u.handle, output_grid.data_v.handle,
+                output_grid.data_w.handle))
+        return dispatch
+
+    def advect_scalar3(self, input_field, output_field):
+        def dispatch():
+            _lib.check(_lib.load().ff_advect3_scalar(self.handle, *self._vel(), input_field.handle,
+                                                     output_field.handle))
+        return dispatch
+
+    def trace(self, points_in, points_out, direction=1):
+        """trace(start, direction) of a vec3 field of points."""
+        _lib.check(_lib.load().ff_advect3_trace(self.handle, *self._vel(), points_in.handle,
+                                                points_out.handle, int(direction)))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.load().ff_advect3_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def create_semi_lagrangian_advection_solver3(velocity_grid=None, collider=None, dt=None, max_substeps=32,
+                                             order=1):
+    return SemiLagrangianAdvectionSolver3(velocity_grid, collider, dt, max_substeps, order)
+
+
+# ------------------------------------------------------ boundary conditions --
+DIRECTION_LEFT, DIRECTION_RIGHT, DIRECTION_DOWN, DIRECTION_UP = 1, 2, 4, 8
+DIRECTION_BACK, DIRECTION_FRONT = 16, 32
+DIRECTION_ALL_3D = 63
+
+
+class SDFInflow3(SDFStaticCollider3):
+    """createSDFInflow3(..., {velocity, mode}) (sdf_inflow_outflow3.js:15-22):
+    an SDF region (baked like a static collider) with a velocity that faces
+    inside it take ('set') or gain ('add')."""
+
+    def __init__(self, resolution, grid_spacing, origin=(0.0, 0.0, 0.0), velocity=(0.0, 0.0, 0.0), mode="set"):
+        super().__init__(resolution, grid_spacing, origin)
+        if mode not in ("set", "add"):
+            raise ValueError(f"createSDFInflow3: unknown mode '{mode}'.")
+        self.velocity = tuple(float(v) for v in velocity)
+        self.mode = mode
+
+
+def create_sdf_inflow3(nx, ny, nz, hx, hy, hz, ox=0.0, oy=0.0, oz=0.0, velocity=(0.0, 0.0, 0.0), mode="set"):
+    return SDFInflow3((nx, ny, nz), (hx, hy, hz), (ox, oy, oz), velocity, mode)
+
+
+class GridBlockedBoundaryConditionSolver3:
+    """createGridBlockedBoundaryConditionSolver3(velocity, resolution...,
+    colliderSDF, inflows, colliderFaceWeights)
+    (grid_blocked_boundary_condition_solver3.js:48-490)."""
+
+    def __init__(self, velocity, resolution, grid_spacing, origin=(0.0, 0.0, 0.0), collider=None, inflows=None,
+                 collider_face_weights=None):
+        self.velocity = velocity
+        self.handle = C.c_void_p()
+        _lib.check(_lib.load().ff_bc3_create(context().handle, (C.c_int * 3)(*resolution),
+                                             (C.c_double * 3)(*grid_spacing), (C.c_double * 3)(*origin),
+                                             C.byref(self.handle)))
+        self._closed = DIRECTION_ALL_3D
+        self.set_collider(collider, collider_face_weights)
+        self.set_inflows(inflows)
+
+    @property
+    def closed_domain_boundary_flag(self):
+        return self._closed
+
+    @closed_domain_boundary_flag.setter
+    def closed_domain_boundary_flag(self, flag):
+        _lib.check(_lib.load().ff_bc3_set_closed(self.handle, int(flag)))
+        self._closed = int(flag)
+
+    def set_collider(self, collider, face_weights=None):
+        self.collider, self.face_weights = collider, face_weights
+        w = face_weights or {}
+        _lib.check(_lib.load().ff_bc3_set_collider(
+            self.handle, collider.phi.handle if collider else None,
+            w["u"].handle if "u" in w else None, w["v"].handle if "v" in w else None,
+            w["w"].handle if "w" in w else None))
+
+    def set_inflows(self, inflows):
+        lst = [] if not inflows else (list(inflows) if isinstance(inflows, (list, tuple)) else [inflows])
+        self.inflows = lst
+        n = len(lst)
+        phis = (C.c_void_p * max(1, n))(*[q.phi.handle.value for q in lst])
+        vel = (C.c_double * max(3, 3 * n))(*[c for q in lst for c in q.velocity])
+        modes = (C.c_int * max(1, n))(*[0 if q.mode == "set" else 1 for q in lst])
+        _lib.check(_lib.load().ff_bc3_set_inflows(self.handle, n, phis, vel, modes))
+
+    def constrain_velocity(self, extrapolation_depth=5):
+        g = self.velocity
+        _lib.check(_lib.load().ff_bc3_constrain(self.handle, g.data_u.handle, g.data_v.handle, g.data_w.handle,
+                                                int(extrapolation_depth)))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.load().ff_bc3_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def create_grid_blocked_boundary_condition_solver3(velocity, nx, ny, nz, hx, hy, hz, ox=0.0, oy=0.0, oz=0.0,
+                                                   collider=None, inflows=None, collider_face_weights=None):
+    return GridBlockedBoundaryConditionSolver3(velocity, (nx, ny, nz), (hx, hy, hz), (ox, oy, oz), collider,
+                                               inflows, collider_face_weights)
+
+
+def apply_viscosity3(input_grid, output_grid, nu, dt):
+    """Explicit viscosity u += dt nu lap(u) (no reference counterpart:
+    grid_solver3.js:104 leaves computeViscosity a no-op)."""
+    g = input_grid
+    _lib.check(_lib.load().ff_viscosity3_apply(
+        context().handle, (C.c_int * 3)(*g.resolution), (C.c_double * 3)(*g.grid_spacing), g.data_u.handle,
+        g.data_v.handle, g.data_w.handle, float(nu), float(dt), output_grid.data_u.handle,
+        output_grid.data_v.handle, output_grid.data_w.handle))
