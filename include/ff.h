@@ -262,6 +262,80 @@ int ff_bc3_constrain(ff_bc b, ff_field u, ff_field v, ff_field w, int depth);
 int ff_viscosity3_apply(ff_ctx ctx, const int *resolution, const double *grid_spacing, ff_field u, ff_field v,
                         ff_field w, double nu, double dt, ff_field u_out, ff_field v_out, ff_field w_out);
 
+/* ---- FLIP: replaces createGridFlipSolver3 (fluxflow
+ * src/grid/grid_flip_solver3.js:135-1157) without resampling.  Particles
+ * are FF_VEC3 positions and velocities (AoS, as the reference's vec3
+ * arrays); P2G accumulates round(v w S) and round(w S) in int32 (S =
+ * p2gAtomicScale, :508-530), so the transfer does not depend on the
+ * order particles arrive in.                                               */
+typedef struct ff_flip_s *ff_flip;
+typedef struct {
+    int resolution[3];
+    double grid_spacing[3];
+    double origin[3];
+    int max_particles;             /* maxParticles (required)             */
+    double dt;                     /* dt                                   */
+    double gravity[3];             /* default (0, -9.81, 0)                */
+    int reduced_pressure;          /* reducedPressure, default 1           */
+    double flip_ratio;             /* flipRatio, default 0.97              */
+    double velocity_damping;       /* velocityDamping, default 0.02        */
+    double p2g_atomic_scale;       /* p2gAtomicScale, default 65536        */
+    double weight_epsilon;         /* weightEpsilon, default 1e-4          */
+    int closed_flags;              /* closedDomainBoundaryFlag             */
+    int max_substeps;              /* of the particle trace, default 32    */
+    double collider_push_thresh;   /* colliderPushThresh, default 0        */
+    double collider_push_shift;    /* colliderPushShift, default 0         */
+    int carry_concentration;       /* carryConcentration, default 0        */
+    double mixing, fade;           /* default 0, 0                         */
+    double concentration_atomic_scale;   /* default 4096                   */
+    double ambient_density;        /* > 0 with component_density: the      */
+    double component_density;      /* variable-density coupling (:265-359) */
+    int extrapolation_depth;       /* default 5                            */
+    ff_pressure_desc pressure;     /* the projection's options (`pressure`)*/
+} ff_flip_desc;
+void ff_flip_desc_default(ff_flip_desc *d, const int *resolution, const double *grid_spacing, int max_particles,
+                          double dt);
+/* u, v, w: the velocity grid the solver works on (borrowed)              */
+int ff_flip3_create(ff_ctx ctx, const ff_flip_desc *desc, ff_field u, ff_field v, ff_field w, ff_flip *out);
+int ff_flip3_destroy(ff_flip f);
+/* collider SDF (cell field, borrowed) or NULL                             */
+int ff_flip3_set_collider(ff_flip f, ff_field phi);
+/* number of live particles (<= max_particles); the first n are stepped   */
+int ff_flip3_set_count(ff_flip f, int n);
+/* borrowed handles: positions, velocities (FF_VEC3), concentration (or
+ * NULL), fluidMask (float cells) and the projection's pressure solver    */
+int ff_flip3_fields(ff_flip f, ff_field *positions, ff_field *velocities, ff_field *concentration,
+                    ff_field *fluid_mask, ff_pressure *pressure);
+/* borrowed handles of the grid-side state: cellConcentration and
+ * cellDensity (cells), the beta faces, and the Dirichlet active/target
+ * fields the projection used (any may be NULL when not in use)           */
+int ff_flip3_grid_fields(ff_flip f, ff_field *cell_concentration, ff_field *cell_density, ff_field *beta_u,
+                         ff_field *beta_v, ff_field *beta_w, ff_field *dirichlet_active, ff_field *dirichlet_target);
+/* stages of onAdvanceTimeStep (:1110-1150), for tests and custom steps   */
+#define FF_FLIP_ADVECT_PARTICLES 0        /* advectParticles + pushOutOfCollider */
+#define FF_FLIP_P2G 1                     /* reset, scatter, finalize            */
+#define FF_FLIP_SNAPSHOT 2                /* snapshotOldU/V/W                    */
+#define FF_FLIP_EXTRAPOLATE_WEIGHT 3      /* extrapolateWeightU/V/W              */
+#define FF_FLIP_CONSTRAIN 4               /* boundarySolver.constrainVelocity    */
+#define FF_FLIP_MARK_FLUID 5              /* clear + markFluidCells + adjacency  */
+#define FF_FLIP_CONCENTRATION_GRID 6      /* cell concentration, density, beta   */
+#define FF_FLIP_GRAVITY 7                 /* applyGravity / applyReducedGravity  */
+#define FF_FLIP_PROJECT 8                 /* Dirichlet air cells + projection    */
+#define FF_FLIP_EXTRAPOLATE_PRESSURE 9    /* extrapolatePressureU/V/W            */
+#define FF_FLIP_G2P 10                    /* g2pUpdate                           */
+#define FF_FLIP_CONCENTRATION_PARTICLE 11 /* mixAndFade                          */
+int ff_flip3_stage(ff_flip f, int stage);
+/* onAdvanceTimeStep(): every stage in the reference's order; diag is the
+ * projection's diagnostics                                                */
+int ff_flip3_step(ff_flip f, ff_diag *diag);
+/* computeFlipBoxSeed3 (:70-130): per_axis^3 jittered particles per cell,
+ * mulberry32(seed) (jitter_random.js:29-46), in doubles as JavaScript.
+ * positions NULL: only *count.  FF_E_LIMIT when capacity is too small.    */
+int ff_flip_box_seed3(const double *box_min, const double *box_max, const double *grid_spacing, int per_axis,
+                      double jitter, uint32_t seed, float *positions, int64_t capacity, int64_t *count);
+/* createJitterRandom(seed): the first n values                           */
+int ff_jitter_random(uint32_t seed, int n, double *out);
+
 /* ---- test hooks mirroring the exported multigrid.js / linalg.js pieces -- */
 /* createLaplacianOperator (multigrid.js:457-471): y = A x with the solver's
  * current level-0 system (call ff_pressure3_prepare first).                 */

@@ -87,6 +87,20 @@ def _declare(L):
     L.orc_advect_scalar.argtypes = [ip, fp, fp, fp, fp, fp, fp, F, I, I, fp, fp]
     L.orc_constrain_velocity.argtypes = [ip, fp, fp, fp, fp, fp, fp, fp, fp, fp, I, I, fp, fp, ip, I]
     L.orc_viscosity.argtypes = [ip, fp, fp, fp, fp, F, F, fp, fp, fp]
+    dp, i32p, u8p = C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_uint8)
+    L.orc_jitter_random.argtypes = [C.c_uint32, I, dp]
+    L.orc_flip_box_seed.argtypes = [dp, dp, dp, I, D, C.c_uint32, fp, L64]
+    L.orc_flip_box_seed.restype = L64
+    L.orc_flip_cell_index.argtypes = [ip, fp, fp, L64, fp, C.POINTER(C.c_int64)]
+    L.orc_flip_mark_fluid.argtypes = [ip, fp, fp, L64, fp, fp]
+    L.orc_flip_dirichlet.argtypes = [ip, fp, fp, fp, fp, F, I, u8p, fp]
+    L.orc_flip_p2g.argtypes = [ip, fp, fp, L64, fp, fp, F, F, fp, fp, fp, i32p, i32p, i32p]
+    L.orc_flip_fluid_adjacent.argtypes = [ip, fp, i32p, i32p, i32p]
+    L.orc_flip_g2p.argtypes = [ip, fp, fp, L64, fp, fp, fp, fp, fp, fp, fp, fp, F, F]
+    L.orc_flip_concentration_grid.argtypes = [ip, fp, fp, L64, fp, fp, F, fp, I, F, F, fp, fp, fp, fp, fp]
+    L.orc_flip_reduced_gravity.argtypes = [ip, fp, fp, fp, fp, fp, fp, fp, F, F, fp, fp, fp]
+    L.orc_flip_mix_fade.argtypes = [ip, fp, fp, L64, fp, fp, F, F, fp]
+    L.orc_flip_advect.argtypes = [ip, fp, fp, fp, fp, fp, fp, F, I, L64, fp, fp, F, F]
 
 
 def _shape_row(s):
@@ -433,3 +447,126 @@ def viscosity(shape, h, u, v, w, nu, dt):
     lib().orc_viscosity(res, hh, _fptr(u), _fptr(v), _fptr(w), float(nu), float(dt), _fptr(uo), _fptr(vo),
                         _fptr(wo))
     return uo, vo, wo
+
+
+# ------------------------------------------------------------------- FLIP --
+# grid_flip_solver3.js stages and jitter_random.js, restated in
+# ff_oracle_flip.c (FP32 stages, double-precision seeding).
+def jitter_random(seed, n):
+    out = np.empty(n)
+    lib().orc_jitter_random(int(seed) & 0xFFFFFFFF, n, out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
+
+
+def flip_box_seed(box_min, box_max, h, per_axis=2, jitter=0.2, seed=0x9E3779B9):
+    dd = lambda v: (C.c_double * 3)(*[float(x) for x in v])
+    n = lib().orc_flip_box_seed(dd(box_min), dd(box_max), dd(h), per_axis, float(jitter), seed, None, 0)
+    out = np.empty(3 * n, np.float32)
+    lib().orc_flip_box_seed(dd(box_min), dd(box_max), dd(h), per_axis, float(jitter), seed, _fptr(out), n)
+    return out
+
+
+def _i32(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def flip_cell_index(shape, h, origin, pos):
+    pos = _f32(pos)
+    out = np.empty(pos.size // 3, np.int64)
+    res, hh, oo = _geom(shape, h, origin)
+    lib().orc_flip_cell_index(res, hh, oo, pos.size // 3, _fptr(pos), out.ctypes.data_as(C.POINTER(C.c_int64)))
+    return out
+
+
+def flip_mark_fluid(shape, h, origin, pos):
+    pos = _f32(pos)
+    mask = np.empty(shape[0] * shape[1] * shape[2], np.float32)
+    res, hh, oo = _geom(shape, h, origin)
+    lib().orc_flip_mark_fluid(res, hh, oo, pos.size // 3, _fptr(pos), _fptr(mask))
+    return mask
+
+
+def flip_dirichlet(shape, h, origin, mask, gravity, dt, reduced=True):
+    n = shape[0] * shape[1] * shape[2]
+    active, target = np.empty(n, np.uint8), np.empty(n, np.float32)
+    res, hh, oo = _geom(shape, h, origin)
+    g = (C.c_float * 3)(*[float(x) for x in gravity])
+    lib().orc_flip_dirichlet(res, hh, oo, _fptr(_f32(mask)), g, float(dt), int(reduced),
+                             active.ctypes.data_as(C.POINTER(C.c_uint8)), _fptr(target))
+    return active, target
+
+
+def _face_sizes(shape):
+    nx, ny, nz = shape
+    return (nx + 1) * ny * nz, nx * (ny + 1) * nz, nx * ny * (nz + 1)
+
+
+def flip_p2g(shape, h, origin, pos, vel, scale=65536.0, eps=1e-4):
+    pos, vel = _f32(pos), _f32(vel)
+    su, sv, sw = _face_sizes(shape)
+    u, v, w = np.empty(su, np.float32), np.empty(sv, np.float32), np.empty(sw, np.float32)
+    vu, vv, vw = np.empty(su, np.int32), np.empty(sv, np.int32), np.empty(sw, np.int32)
+    res, hh, oo = _geom(shape, h, origin)
+    lib().orc_flip_p2g(res, hh, oo, pos.size // 3, _fptr(pos), _fptr(vel), float(scale), float(eps), _fptr(u),
+                       _fptr(v), _fptr(w), _i32(vu), _i32(vv), _i32(vw))
+    return (u, v, w), (vu, vv, vw)
+
+
+def flip_fluid_adjacent(shape, mask):
+    su, sv, sw = _face_sizes(shape)
+    au, av, aw = np.empty(su, np.int32), np.empty(sv, np.int32), np.empty(sw, np.int32)
+    lib().orc_flip_fluid_adjacent((C.c_int * 3)(*shape), _fptr(_f32(mask)), _i32(au), _i32(av), _i32(aw))
+    return au, av, aw
+
+
+def flip_g2p(shape, h, origin, pos, vel, new, old, flip_ratio=0.97, damping=0.02):
+    pos, vel = _f32(pos), _f32(vel).copy()
+    new, old = [_f32(x) for x in new], [_f32(x) for x in old]
+    res, hh, oo = _geom(shape, h, origin)
+    lib().orc_flip_g2p(res, hh, oo, pos.size // 3, _fptr(pos), _fptr(vel), *[_fptr(x) for x in new],
+                       *[_fptr(x) for x in old], float(flip_ratio), float(damping))
+    return vel
+
+
+def flip_advect(shape, h, origin, u, v, w, phi, pos, dt, max_substeps=32, push_thresh=0.0, push_shift=0.0):
+    pos = _f32(pos).copy()
+    ext = (C.c_float * 3)(*[float(shape[a] * float(h[a])) for a in range(3)])
+    res, hh, oo = _geom(shape, h, origin)
+    lib().orc_flip_advect(res, hh, oo, _fptr(_f32(u)), _fptr(_f32(v)), _fptr(_f32(w)), _fptr(_f32(phi)),
+                          float(dt), int(max_substeps), pos.size // 3, _fptr(pos), ext, float(push_thresh),
+                          float(push_shift))
+    return pos
+
+
+def flip_concentration_grid(shape, h, origin, pos, conc, mask, cscale=4096.0, density=None):
+    """density: None or (ambient, component); returns cell concentration,
+    cell density and beta faces (None without the density coupling)."""
+    pos, conc = _f32(pos), _f32(conc)
+    n = shape[0] * shape[1] * shape[2]
+    cc, rho = np.empty(n, np.float32), np.empty(n, np.float32)
+    su, sv, sw = _face_sizes(shape)
+    bu, bv, bw = np.empty(su, np.float32), np.empty(sv, np.float32), np.empty(sw, np.float32)
+    res, hh, oo = _geom(shape, h, origin)
+    r0, r1 = density if density else (0.0, 0.0)
+    lib().orc_flip_concentration_grid(res, hh, oo, pos.size // 3, _fptr(pos), _fptr(conc), float(cscale),
+                                      _fptr(_f32(mask)), int(density is not None), float(r0), float(r1), _fptr(cc),
+                                      _fptr(rho), _fptr(bu), _fptr(bv), _fptr(bw))
+    return cc, (rho if density else None), ((bu, bv, bw) if density else None)
+
+
+def flip_reduced_gravity(shape, h, origin, rho, beta, gravity, dt, rref, u, v, w):
+    u, v, w = (_f32(x).copy() for x in (u, v, w))
+    hh = (C.c_float * 3)(*[float(x) for x in h])
+    oo = (C.c_float * 3)(*[float(x) for x in origin])
+    g = (C.c_float * 3)(*[float(x) for x in gravity])
+    lib().orc_flip_reduced_gravity((C.c_int * 3)(*shape), hh, oo, _fptr(_f32(rho)), *[_fptr(_f32(b)) for b in beta],
+                                   g, float(dt), float(rref), _fptr(u), _fptr(v), _fptr(w))
+    return u, v, w
+
+
+def flip_mix_fade(shape, h, origin, pos, cell_conc, conc, mixing, fade):
+    conc = _f32(conc).copy()
+    res, hh, oo = _geom(shape, h, origin)
+    lib().orc_flip_mix_fade(res, hh, oo, _f32(pos).size // 3, _fptr(_f32(pos)), _fptr(_f32(cell_conc)),
+                            float(mixing), float(fade), _fptr(conc))
+    return conc

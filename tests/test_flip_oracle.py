@@ -1,0 +1,113 @@
+"""FLIP seeding and oracle checks that need no GPU: mulberry32 and
+computeFlipBoxSeed3 agree between libff's host code, the C oracle and a
+third restatement written here from jitter_random.js's JavaScript
+semantics; FLIP stage properties of the oracle."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+
+def mulberry32_py(seed, n):
+    """jitter_random.js:29-41 with JavaScript's uint32 semantics."""
+    m = 0xFFFFFFFF
+    state = seed & m
+    out = []
+    for _ in range(n):
+        state = (state + 0x6D2B79F5) & m
+        t = state
+        t = ((t ^ (t >> 15)) * (t | 1)) & m          # Math.imul, then >>> 0
+        t ^= (t + (((t ^ (t >> 7)) * (t | 61)) & m)) & m
+        out.append(((t ^ (t >> 14)) & m) / 4294967296.0)
+    return np.array(out)
+
+
+@pytest.mark.parametrize("seed", [0x9E3779B9, 0, 1, 12345, 0xFFFFFFFF])
+def test_mulberry32_three_ways(oracle, seed):
+    from tsl_array_n_gb300 import _lib
+    ref = mulberry32_py(seed, 257)
+    assert np.array_equal(oracle.jitter_random(seed, 257), ref)
+    out = (C.c_double * 257)()
+    _lib.check(_lib.load().ff_jitter_random(seed, 257, out))
+    assert np.array_equal(np.array(out), ref)
+    assert np.all((ref >= 0) & (ref < 1))
+
+
+def test_box_seed_matches_oracle_and_layout(oracle):
+    from tsl_array_n_gb300 import fluxflow as ff
+    h = (1 / 32, 1 / 16, 1 / 24)
+    box_min, box_max = (0.1, 0.05, 0.2), (0.45, 0.6, 0.55)
+    got = ff.compute_flip_box_seed3(box_min, box_max, *h, particles_per_cell_axis=2, jitter=0.2)
+    ref = oracle.flip_box_seed(box_min, box_max, h, 2, 0.2, 0x9E3779B9)
+    assert got["count"] * 3 == ref.size
+    assert np.array_equal(got["positionsArray"], ref)
+    # every particle stays within its own sub-cell (jitter 0.2 < 0.5)
+    cells = [max(1, int(np.floor((b - a) / hh + 0.5))) for a, b, hh in zip(box_min, box_max, h)]
+    assert got["count"] == cells[0] * cells[1] * cells[2] * 8
+    p = ref.reshape(-1, 3)
+    for a in range(3):
+        assert np.all(p[:, a] > box_min[a]) and np.all(p[:, a] < box_min[a] + cells[a] * h[a])
+
+
+def test_p2g_partition_of_unity_and_order_independence(oracle):
+    """Trilinear weights sum to one, so a uniform particle velocity maps to
+    the same value on every face with weight; the int32 fixed point makes
+    the sum independent of particle order."""
+    sh, h, o = (10, 8, 6), (0.1, 0.125, 1 / 6), (0.0, 0.0, 0.0)
+    pos = oracle.flip_box_seed((0.2, 0.2, 0.2), (0.7, 0.8, 0.8), h, 2, 0.2).reshape(-1, 3)
+    vel = np.tile(np.array([[0.5, -1.25, 2.0]], np.float32), (len(pos), 1))
+    (u, v, w), (vu, vv, vw) = oracle.flip_p2g(sh, h, o, pos, vel)
+    # each term is rounded to 1/S (S = 65536), so faces whose weight comes
+    # from a few small trilinear weights carry a larger relative error
+    for x, valid, want in ((u, vu, 0.5), (v, vv, -1.25), (w, vw, 2.0)):
+        err = np.abs(x[valid == 1] - want) / abs(want)
+        assert np.median(err) < 1e-4 and np.mean(err < 2e-3) > 0.95
+    rng = np.random.default_rng(0)
+    vel2 = rng.standard_normal(pos.shape).astype(np.float32)
+    a = oracle.flip_p2g(sh, h, o, pos, vel2)
+    perm = rng.permutation(len(pos))
+    b = oracle.flip_p2g(sh, h, o, pos[perm], vel2[perm])
+    for x, y in zip(a[0] + a[1], b[0] + b[1]):
+        assert np.array_equal(x, y)
+
+
+def test_mark_fluid_dirichlet_and_adjacency(oracle):
+    sh, h, o = (8, 8, 8), (0.125,) * 3, (0.0, 0.0, 0.0)
+    pos = np.array([[0.3, 0.3, 0.3], [0.9, 0.2, 0.1], [-5.0, 2.0, 0.5]], np.float32)
+    idx = oracle.flip_cell_index(sh, h, o, pos)
+    assert list(idx) == [2 + 8 * (2 + 8 * 2), 7 + 8 * (1 + 8 * 0), 0 + 8 * (7 + 8 * 4)]
+    mask = oracle.flip_mark_fluid(sh, h, o, pos)
+    assert mask.sum() == 3 and all(mask[idx] == 1)
+    active, target = oracle.flip_dirichlet(sh, h, o, mask, (0.0, -9.81, 0.0), 0.01)
+    assert np.array_equal(active, (mask < 0.5).astype(np.uint8))
+    # reduced pressure target -dt g.y y at the cell centre
+    assert np.isclose(target[idx[0]], 0.01 * 9.81 * 0.3125, rtol=1e-6)
+    au, av, aw = oracle.flip_fluid_adjacent(sh, mask)
+    U = au.reshape(8, 8, 9)
+    assert U[2, 2, 2] == 1 and U[2, 2, 3] == 1 and U[2, 2, 4] == 0
+
+
+def test_g2p_pic_limit_and_clamp(oracle):
+    """flipRatio 0 is PIC: the particle takes the sampled new grid velocity
+    (damped); a non-finite result zeroes the particle."""
+    sh, h, o = (6, 6, 6), (1 / 6,) * 3, (0.0, 0.0, 0.0)
+    su, sv, sw = 7 * 36, 6 * 7 * 6, 36 * 7
+    new = [np.full(su, 2.0, np.float32), np.full(sv, -1.0, np.float32), np.zeros(sw, np.float32)]
+    old = [np.zeros(su, np.float32), np.zeros(sv, np.float32), np.zeros(sw, np.float32)]
+    pos = np.array([[0.5, 0.5, 0.5], [0.2, 0.7, 0.3]], np.float32)
+    vel = np.array([[9.0, 9.0, 9.0], [np.nan, 0.0, 0.0]], np.float32)
+    out = oracle.flip_g2p(sh, h, o, pos, vel, new, old, flip_ratio=0.0, damping=0.5).reshape(-1, 3)
+    np.testing.assert_allclose(out[0], [1.0, -0.5, 0.0], rtol=1e-6)
+    assert np.all(out[1] == 0)
+
+
+def test_concentration_density_and_beta(oracle):
+    sh, h, o = (6, 5, 4), (1 / 6, 0.2, 0.25), (0.0, 0.0, 0.0)
+    pos = oracle.flip_box_seed((0.0, 0.0, 0.0), (0.5, 0.6, 0.5), h, 2, 0.2).reshape(-1, 3)
+    conc = (pos[:, 0] > 0.25).astype(np.float32)
+    mask = oracle.flip_mark_fluid(sh, h, o, pos)
+    cc, rho, beta = oracle.flip_concentration_grid(sh, h, o, pos, conc, mask, density=(1.0, 1000.0))
+    assert np.all((cc >= 0) & (cc <= 1))
+    assert np.all((rho >= 1.0) & (rho <= 1000.0))
+    # beta = rho_ref / rho_face: 1 in the heavy phase, 1000 in the light one
+    assert np.isclose(beta[0].max(), 1000.0) and np.isclose(beta[0].min(), 1.0)

@@ -39,6 +39,18 @@ class AdvectDesc(C.Structure):
                 ("dt", C.c_double), ("max_substeps", C.c_int), ("order", C.c_int)]
 
 
+class FlipDesc(C.Structure):
+    _fields_ = [("resolution", C.c_int * 3), ("grid_spacing", C.c_double * 3), ("origin", C.c_double * 3),
+                ("max_particles", C.c_int), ("dt", C.c_double), ("gravity", C.c_double * 3),
+                ("reduced_pressure", C.c_int), ("flip_ratio", C.c_double), ("velocity_damping", C.c_double),
+                ("p2g_atomic_scale", C.c_double), ("weight_epsilon", C.c_double), ("closed_flags", C.c_int),
+                ("max_substeps", C.c_int), ("collider_push_thresh", C.c_double),
+                ("collider_push_shift", C.c_double), ("carry_concentration", C.c_int), ("mixing", C.c_double),
+                ("fade", C.c_double), ("concentration_atomic_scale", C.c_double),
+                ("ambient_density", C.c_double), ("component_density", C.c_double),
+                ("extrapolation_depth", C.c_int), ("pressure", PressureDesc)]
+
+
 class Diag(C.Structure):
     _fields_ = [("converged", C.c_int), ("rejected", C.c_int), ("iterations", C.c_int),
                 ("stopped_by", C.c_int), ("residual", C.c_double), ("b_norm", C.c_double),
@@ -99,6 +111,18 @@ PROTOTYPES = {
     "ff_bc3_set_inflows": (_I, [_P, _I, _PP, C.POINTER(C.c_double), _IP]),
     "ff_bc3_constrain": (_I, [_P, _P, _P, _P, _I]),
     "ff_viscosity3_apply": (_I, [_P, _IP, C.POINTER(C.c_double), _P, _P, _P, _D, _D, _P, _P, _P]),
+    "ff_flip_desc_default": (None, [C.POINTER(FlipDesc), _IP, C.POINTER(C.c_double), _I, _D]),
+    "ff_flip3_create": (_I, [_P, C.POINTER(FlipDesc), _P, _P, _P, _PP]),
+    "ff_flip3_destroy": (_I, [_P]),
+    "ff_flip3_set_collider": (_I, [_P, _P]),
+    "ff_flip3_set_count": (_I, [_P, _I]),
+    "ff_flip3_fields": (_I, [_P, _PP, _PP, _PP, _PP, _PP]),
+    "ff_flip3_grid_fields": (_I, [_P, _PP, _PP, _PP, _PP, _PP, _PP, _PP]),
+    "ff_flip3_stage": (_I, [_P, _I]),
+    "ff_flip3_step": (_I, [_P, C.POINTER(Diag)]),
+    "ff_flip_box_seed3": (_I, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double), _I, _D,
+                               C.c_uint32, _FP, C.c_int64, C.POINTER(C.c_int64)]),
+    "ff_jitter_random": (_I, [C.c_uint32, _I, C.POINTER(C.c_double)]),
     "ff_laplacian_apply": (_I, [_P, _P, _P]),
     "ff_precondition_apply": (_I, [_P, _P, _P]),
     "ff_mg_restrict": (_I, [_P, _I, _P, _P]),

@@ -37,7 +37,7 @@ def _headers_mtime():
 
 # per-file extra flags: the grid-velocity kernels round every FP32 operation
 # on its own (no fused multiply-add), as the reference's arithmetic does
-EXTRA = {"ff_grid.cu": ["-fmad=false"]}
+EXTRA = {"ff_grid.cu": ["-fmad=false"], "ff_flip.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]}
 
 
 def _compile(src, verbose):

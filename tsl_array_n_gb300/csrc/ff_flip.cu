@@ -1,0 +1,695 @@
+// 3D FLIP particle-grid transfer (fluxflow src/grid/grid_flip_solver3.js):
+// particle advection through the grid velocity, fixed-point P2G with int32
+// atomics, fluid marking and the reduced-pressure Dirichlet condition of
+// air cells, the variable-density beta faces and reduced gravity, G2P with
+// the FLIP/PIC blend, and the per-step orchestration (onAdvanceTimeStep).
+//
+// FP32 arithmetic rounds one operation at a time (-fmad=false), in the
+// reference's evaluation order; P2G accumulates round(v w S) and round(w S)
+// as int32 (wrapping like the reference's i32 atomics), so its result does
+// not depend on the order particles arrive in.  Host-side seeding
+// (computeFlipBoxSeed3, mulberry32) is computed in doubles as JavaScript
+// does (-ffp-contract=off on the host compiler).
+#include "ff_grid.cuh"
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace {
+using namespace ffg;
+
+constexpr float MAX_PARTICLE_VELOCITY = 500.0f;   // grid_flip_solver3.js:176 (via the 2D file)
+constexpr float MIN_DENSITY = 1e-4f;              // :182
+constexpr double PRESSURE_BOUND_HEADROOM = 8.0;   // :175
+
+__device__ __forceinline__ bool nonfinite(float v) { return isnan(v) || isinf(v); }
+
+// cellIndexOf (:227-235)
+__device__ __forceinline__ long long cell_of(const G3 &g, const float *p) {
+    const float cx = gclamp((p[0] - g.ox) / g.hx), cy = gclamp((p[1] - g.oy) / g.hy), cz = gclamp((p[2] - g.oz) / g.hz);
+    const int i = iclamp((int)floorf(cx), 0, g.nx - 1), j = iclamp((int)floorf(cy), 0, g.ny - 1),
+              k = iclamp((int)floorf(cz), 0, g.nz - 1);
+    return i + (long long)g.nx * (j + (long long)g.ny * k);
+}
+
+// advectParticles (:925-933) then pushOutOfCollider (:939-951)
+__global__ void k_flip_advect(VelField F, long long n, float *__restrict__ pos, float dt, int max_substeps, F3 mn,
+                              F3 mx, float push_thresh, float push_shift) {
+    const F3 oc = comp_origin(F.g, 3);
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+        const F3 prev{pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]};
+        const F3 tr = back_trace(F, prev, dt, -1.0f, max_substeps);
+        const bool bad = nonfinite(tr.x) || nonfinite(tr.y) || nonfinite(tr.z);
+        F3 q{fminf(fmaxf(bad ? prev.x : tr.x, mn.x), mx.x), fminf(fmaxf(bad ? prev.y : tr.y, mn.y), mx.y),
+             fminf(fmaxf(bad ? prev.z : tr.z, mn.z), mx.z)};
+        if (F.phi) {
+            const float val = trilinear(F.phi, F.g.nx, F.g.ny, F.g.nz, F.g, oc, q);
+            if (val < push_thresh) {
+                const F3 gr = trilinear_gradient(F.phi, F.g, oc, q);
+                const float gl = sqrtf(gr.x * gr.x + gr.y * gr.y + gr.z * gr.z);
+                if (gl > 0.0f) {
+                    const float shift = (push_thresh - val) + push_shift;
+                    q = F3{q.x + gr.x / gl * shift, q.y + gr.y / gl * shift, q.z + gr.z / gl * shift};
+                }
+            }
+        }
+        pos[3 * p] = q.x;
+        pos[3 * p + 1] = q.y;
+        pos[3 * p + 2] = q.z;
+    }
+}
+
+// markFluidCellsKernel (:241-245), after a cleared mask
+__global__ void k_flip_mark(G3 g, long long n, const float *__restrict__ pos, float *__restrict__ mask) {
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x)
+        mask[cell_of(g, pos + 3 * p)] = 1.0f;
+}
+
+// buildScatter (:508-530): each particle adds round(v w S) and round(w S)
+// to the 8 faces around it, per component
+__global__ void k_flip_scatter(G3 g, long long n, const float *__restrict__ pos, const float *__restrict__ vel,
+                               float scale, int *__restrict__ nu, int *__restrict__ du, int *__restrict__ nv,
+                               int *__restrict__ dv, int *__restrict__ nw, int *__restrict__ dw) {
+    int *num[3] = {nu, nv, nw}, *den[3] = {du, dv, dw};
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+        const F3 q{pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            int sx, sy, sz;
+            comp_shape(g, a, sx, sy, sz);
+            const F3 o = comp_origin(g, a);
+            const float value = vel[3 * p + a];
+            const float gx = gclamp((q.x - o.x) / g.hx), gy = gclamp((q.y - o.y) / g.hy), gz = gclamp((q.z - o.z) / g.hz);
+            const int i0 = (int)floorf(gx), j0 = (int)floorf(gy), k0 = (int)floorf(gz);
+            const float fx = gx - (float)i0, fy = gy - (float)j0, fz = gz - (float)k0;
+            const int ic[2] = {iclamp(i0, 0, sx - 1), iclamp(i0 + 1, 0, sx - 1)};
+            const int jc[2] = {iclamp(j0, 0, sy - 1), iclamp(j0 + 1, 0, sy - 1)};
+            const int kc[2] = {iclamp(k0, 0, sz - 1), iclamp(k0 + 1, 0, sz - 1)};
+            const float ux = 1.0f - fx, uy = 1.0f - fy, uz = 1.0f - fz;
+            const float w[8] = {ux * uy * uz, fx * uy * uz, ux * fy * uz, fx * fy * uz,
+                                ux * uy * fz, fx * uy * fz, ux * fy * fz, fx * fy * fz};
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                const long long f = ic[c & 1] + (long long)sx * (jc[(c >> 1) & 1] + (long long)sy * kc[(c >> 2) & 1]);
+                atomicAdd(num[a] + f, __float2int_rn(value * w[c] * scale));
+                atomicAdd(den[a] + f, __float2int_rn(w[c] * scale));
+            }
+        }
+    }
+}
+
+// buildFinalize (:532-550)
+__global__ void k_flip_finalize(long long n, const int *__restrict__ num, const int *__restrict__ den, float scale,
+                                float eps, float *__restrict__ data, int *__restrict__ valid) {
+    for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < n; f += (long long)gridDim.x * blockDim.x) {
+        const float numer = (float)num[f] / scale;
+        const float denom = (float)den[f] / scale;
+        if (denom > eps) {
+            data[f] = numer / denom;
+            valid[f] = 1;
+        } else {
+            data[f] = 0.0f;
+            valid[f] = 0;
+        }
+    }
+}
+
+// computeU/V/WFluidAdjacent (:586-618)
+__global__ void k_flip_adjacent(G3 g, int a, const float *__restrict__ mask, int *__restrict__ adj) {
+    int s[3];
+    comp_shape(g, a, s[0], s[1], s[2]);
+    const long long n = (long long)s[0] * s[1] * s[2];
+    const int nn = a == 0 ? g.nx : (a == 1 ? g.ny : g.nz);
+    for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < n; f += (long long)gridDim.x * blockDim.x) {
+        int idx[3];
+        unflatten(f, s[0], s[1], idx[0], idx[1], idx[2]);
+        int lo[3] = {idx[0], idx[1], idx[2]}, hi[3] = {idx[0], idx[1], idx[2]};
+        lo[a] = iclamp(idx[a] - 1, 0, nn - 1);
+        hi[a] = iclamp(idx[a], 0, nn - 1);
+        const float ml = mask[lo[0] + (long long)g.nx * (lo[1] + (long long)g.ny * lo[2])];
+        const float mh = mask[hi[0] + (long long)g.nx * (hi[1] + (long long)g.ny * hi[2])];
+        adj[f] = (ml > 0.5f || mh > 0.5f) ? 1 : 0;
+    }
+}
+
+// dirichlet(pos) evaluated at the cell centres (:252-259)
+__global__ void k_flip_dirichlet(G3 g, const float *__restrict__ mask, F3 grav, float dt, int reduced,
+                                 uint8_t *__restrict__ active, float *__restrict__ target) {
+    const long long n = (long long)g.nx * g.ny * g.nz;
+    const F3 oc = comp_origin(g, 3);
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        unflatten(c, g.nx, g.ny, i, j, k);
+        const F3 p = index_pos(g, oc, i, j, k);
+        const float m = trilinear(mask, g.nx, g.ny, g.nz, g, oc, p);
+        active[c] = m < 0.5f;
+        target[c] = reduced ? -((grav.x * p.x + grav.y * p.y + grav.z * p.z) * dt) : 0.0f;
+    }
+}
+
+// accumulateConcentration (:999-1004)
+__global__ void k_flip_conc_accum(G3 g, long long n, const float *__restrict__ pos, const float *__restrict__ conc,
+                                  float cscale, int *__restrict__ cnt, int *__restrict__ acc) {
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+        const long long c = cell_of(g, pos + 3 * p);
+        atomicAdd(cnt + c, 1);
+        atomicAdd(acc + c, __float2int_rn(fminf(fmaxf(conc[p], 0.0f), 1.0f) * cscale));
+    }
+}
+
+// resolveCellConcentration (:1006-1015)
+__global__ void k_flip_conc_resolve(long long nc, const int *__restrict__ cnt, const int *__restrict__ acc, float cscale,
+                                    int density, float r0, float r1, float *__restrict__ cell_conc,
+                                    float *__restrict__ cell_rho) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < nc; c += (long long)gridDim.x * blockDim.x) {
+        const float total = (float)cnt[c];
+        const float sum = (float)acc[c] / cscale;
+        const float mean = sum / fmaxf(total, 1.0f);
+        const float cv = total > 0.5f ? fminf(fmaxf(mean, 0.0f), 1.0f) : 0.0f;
+        cell_conc[c] = cv;
+        if (density) cell_rho[c] = r0 + (r1 - r0) * cv;
+    }
+}
+
+// computeBetaU/V/W with faceDensity (:315-345)
+__global__ void k_flip_beta(G3 g, int a, const float *__restrict__ rho, const float *__restrict__ mask, float rref,
+                            float *__restrict__ beta) {
+    int s[3];
+    comp_shape(g, a, s[0], s[1], s[2]);
+    const long long n = (long long)s[0] * s[1] * s[2];
+    const int nn = a == 0 ? g.nx : (a == 1 ? g.ny : g.nz);
+    for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < n; f += (long long)gridDim.x * blockDim.x) {
+        int idx[3];
+        unflatten(f, s[0], s[1], idx[0], idx[1], idx[2]);
+        int A[3] = {idx[0], idx[1], idx[2]}, B[3] = {idx[0], idx[1], idx[2]};
+        A[a] = iclamp(idx[a] - 1, 0, nn - 1);
+        B[a] = iclamp(idx[a], 0, nn - 1);
+        const long long ca = A[0] + (long long)g.nx * (A[1] + (long long)g.ny * A[2]);
+        const long long cb = B[0] + (long long)g.nx * (B[1] + (long long)g.ny * B[2]);
+        const float ra = rho[ca], rb = rho[cb];
+        const bool fa = mask[ca] > 0.5f, fb = mask[cb] > 0.5f;
+        const float rf = (fa && fb) ? (ra + rb) * 0.5f : ((fa || fb) ? (fa ? ra : rb) : rref);
+        beta[f] = rref / fmaxf(rf, MIN_DENSITY);
+    }
+}
+
+// applyReducedGravityU/V/W (:848-884); plain gravity (:821-831) when beta is null
+__global__ void k_flip_gravity(G3 g, int a, const float *__restrict__ rho, const float *__restrict__ beta, F3 grav,
+                               float dt, float rref, float *__restrict__ data) {
+    int s[3];
+    comp_shape(g, a, s[0], s[1], s[2]);
+    const long long n = (long long)s[0] * s[1] * s[2];
+    const int nn = a == 0 ? g.nx : (a == 1 ? g.ny : g.nz);
+    const float ga = a == 0 ? grav.x : (a == 1 ? grav.y : grav.z);
+    const float ha = a == 0 ? g.hx : (a == 1 ? g.hy : g.hz);
+    for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < n; f += (long long)gridDim.x * blockDim.x) {
+        if (!beta) {
+            data[f] = data[f] + ga * dt;
+            continue;
+        }
+        int idx[3];
+        unflatten(f, s[0], s[1], idx[0], idx[1], idx[2]);
+        const float px = g.ox + (a == 0 ? (float)idx[0] * g.hx : ((float)idx[0] + 0.5f) * g.hx);
+        const float py = g.oy + (a == 1 ? (float)idx[1] * g.hy : ((float)idx[1] + 0.5f) * g.hy);
+        const float pz = g.oz + (a == 2 ? (float)idx[2] * g.hz : ((float)idx[2] + 0.5f) * g.hz);
+        int A[3] = {idx[0], idx[1], idx[2]}, B[3] = {idx[0], idx[1], idx[2]};
+        B[a] = iclamp(idx[a], 0, nn - 1);
+        A[a] = iclamp(idx[a] - 1, 0, nn - 1);
+        const float rb = rho[B[0] + (long long)g.nx * (B[1] + (long long)g.ny * B[2])];
+        const float ra = rho[A[0] + (long long)g.nx * (A[1] + (long long)g.ny * A[2])];
+        const float drho = (rb - ra) / ha;
+        const float gp = grav.x * px + grav.y * py + grav.z * pz;
+        const float term = beta[f] * dt / rref * gp * drho;
+        data[f] = data[f] - term;
+    }
+}
+
+// g2pUpdate (:909-922)
+__global__ void k_flip_g2p(G3 g, long long n, const float *__restrict__ pos, float *__restrict__ vel,
+                           const float *__restrict__ u, const float *__restrict__ v, const float *__restrict__ w,
+                           const float *__restrict__ uo, const float *__restrict__ vo, const float *__restrict__ wo,
+                           float ratio, float damp) {
+    const float *nw[3] = {u, v, w}, *od[3] = {uo, vo, wo};
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+        const F3 q{pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]};
+        float out[3];
+        bool bad = false;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            int sx, sy, sz;
+            comp_shape(g, a, sx, sy, sz);
+            const F3 o = comp_origin(g, a);
+            const float nv = trilinear(nw[a], sx, sy, sz, g, o, q);
+            const float ov = trilinear(od[a], sx, sy, sz, g, o, q);
+            const float delta = nv - ov;
+            const float flipv = vel[3 * p + a] + delta;
+            const float blended = flipv * ratio + nv * (1.0f - ratio);
+            out[a] = blended * (1.0f - damp);
+            bad |= nonfinite(out[a]);
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+            vel[3 * p + a] = bad ? 0.0f : fminf(fmaxf(out[a], -MAX_PARTICLE_VELOCITY), MAX_PARTICLE_VELOCITY);
+    }
+}
+
+// mixAndFade (:1022-1029)
+__global__ void k_flip_mix_fade(G3 g, long long n, const float *__restrict__ pos, const float *__restrict__ cell_conc,
+                                float mixing, float fade, float *__restrict__ conc) {
+    const F3 oc = comp_origin(g, 3);
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+        const F3 q{pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]};
+        const float sampled = trilinear(cell_conc, g.nx, g.ny, g.nz, g, oc, q);
+        const float c = fminf(fmaxf(conc[p], 0.0f), 1.0f);
+        const float local = nonfinite(sampled) ? c : sampled;
+        const float blended = c + (local - c) * mixing;
+        conc[p] = fminf(fmaxf(blended * (1.0f - fade), 0.0f), 1.0f);
+    }
+}
+
+int blocks_for(long long n) { return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 152LL * 16)); }
+
+int post(const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return ff_set_error(FF_E_CUDA, "%s launch: %s", what, cudaGetErrorString(e));
+    return FF_OK;
+}
+
+// mulberry32 (jitter_random.js:29-41)
+struct Mulberry32 {
+    uint32_t state;
+    double next() {
+        state = state + 0x6D2B79F5u;
+        uint32_t t = state;
+        t = (t ^ (t >> 15)) * (t | 1u);
+        t ^= t + (t ^ (t >> 7)) * (t | 61u);
+        return (double)(t ^ (t >> 14)) / 4294967296.0;
+    }
+};
+
+}  // namespace
+
+// ------------------------------------------------------------- host side --
+extern "C" int ff_jitter_random(uint32_t seed, int n, double *out) {
+    FF_CHECK(n >= 0 && (n == 0 || out), FF_E_ARG, "ff_jitter_random: bad arguments");
+    Mulberry32 r{seed};
+    for (int q = 0; q < n; ++q) out[q] = r.next();
+    return FF_OK;
+}
+
+extern "C" int ff_flip_box_seed3(const double *bmin, const double *bmax, const double *h, int per_axis, double jitter,
+                                 uint32_t seed, float *positions, int64_t capacity, int64_t *count) {
+    FF_CHECK(bmin && bmax && h && count && per_axis > 0, FF_E_ARG, "computeFlipBoxSeed3: bad arguments");
+    long long cells[3];
+    double sub[3];
+    for (int a = 0; a < 3; ++a) {
+        const double c = std::floor((bmax[a] - bmin[a]) / h[a] + 0.5);   // Math.round
+        cells[a] = c < 1 ? 1 : (long long)c;
+        sub[a] = h[a] / per_axis;
+    }
+    const long long total = cells[0] * cells[1] * cells[2] * per_axis * per_axis * per_axis;
+    *count = total;
+    if (!positions) return FF_OK;
+    FF_CHECK(capacity >= total, FF_E_LIMIT, "computeFlipBoxSeed3: %lld particles exceed the capacity %lld", total,
+             (long long)capacity);
+    Mulberry32 r{seed};
+    long long n = 0;
+    for (long long ck = 0; ck < cells[2]; ++ck)
+        for (long long cj = 0; cj < cells[1]; ++cj)
+            for (long long ci = 0; ci < cells[0]; ++ci)
+                for (int sk = 0; sk < per_axis; ++sk)
+                    for (int sj = 0; sj < per_axis; ++sj)
+                        for (int si = 0; si < per_axis; ++si) {
+                            const double jx = (r.next() * 2 - 1) * jitter * sub[0];
+                            const double jy = (r.next() * 2 - 1) * jitter * sub[1];
+                            const double jz = (r.next() * 2 - 1) * jitter * sub[2];
+                            positions[3 * n] = (float)(bmin[0] + (double)ci * h[0] + (si + 0.5) * sub[0] + jx);
+                            positions[3 * n + 1] = (float)(bmin[1] + (double)cj * h[1] + (sj + 0.5) * sub[1] + jy);
+                            positions[3 * n + 2] = (float)(bmin[2] + (double)ck * h[2] + (sk + 0.5) * sub[2] + jz);
+                            ++n;
+                        }
+    return FF_OK;
+}
+
+extern "C" void ff_flip_desc_default(ff_flip_desc *d, const int *res, const double *h, int max_particles, double dt) {
+    std::memset(d, 0, sizeof *d);
+    for (int a = 0; a < 3; ++a) {
+        d->resolution[a] = res ? res[a] : 1;
+        d->grid_spacing[a] = h ? h[a] : 1.0;
+    }
+    d->max_particles = max_particles;
+    d->dt = dt;
+    d->gravity[1] = -9.81;
+    d->reduced_pressure = 1;
+    d->flip_ratio = 0.97;
+    d->velocity_damping = 0.02;
+    d->p2g_atomic_scale = 65536.0;
+    d->weight_epsilon = 1e-4;
+    d->closed_flags = FF_DIRECTION_ALL_3D;
+    d->max_substeps = 32;
+    d->concentration_atomic_scale = 4096.0;
+    d->extrapolation_depth = 5;
+    ff_pressure_desc_default(&d->pressure, res, h);
+    d->pressure.max_plausible_pressure = 0.0;   // derived from dt, gravity and the domain
+}
+
+struct ff_flip_s {
+    ff_ctx ctx = nullptr;
+    ff_flip_desc desc{};
+    G3 g{};
+    int count = 0;
+    ff_field u = nullptr, v = nullptr, w = nullptr;   // the velocity grid (borrowed)
+    ff_field phi = nullptr;                           // collider (borrowed)
+    ff_field pos = nullptr, vel = nullptr, conc = nullptr, mask = nullptr, active = nullptr, target = nullptr;
+    ff_field cell_conc = nullptr, cell_rho = nullptr, beta[3] = {};
+    float *old[3] = {};
+    int *num[3] = {}, *den[3] = {}, *valid[3] = {}, *adj[3] = {}, *vtmp[2][3] = {};
+    float *scratch[3] = {};
+    int *ccnt = nullptr, *cacc = nullptr;
+    ff_bc bc = nullptr;
+    ff_advect adv = nullptr;
+    ff_pressure ps = nullptr;
+    bool density = false;
+    float r0 = 0, r1 = 0, rref = 1;
+    ff_diag last{};
+};
+
+static long long comp_n(const G3 &g, int a) {
+    if (a == 3) return (long long)g.nx * g.ny * g.nz;
+    int sx, sy, sz;
+    comp_shape(g, a, sx, sy, sz);
+    return (long long)sx * sy * sz;
+}
+
+extern "C" int ff_flip3_destroy(ff_flip f) {
+    if (!f) return FF_OK;
+    cudaStreamSynchronize(f->ctx->stream);
+    ff_pressure3_destroy(f->ps);
+    ff_advect3_destroy(f->adv);
+    ff_bc3_destroy(f->bc);
+    ff_field fs[] = {f->pos, f->vel, f->conc, f->mask, f->active, f->target, f->cell_conc, f->cell_rho,
+                     f->beta[0], f->beta[1], f->beta[2]};
+    for (ff_field x : fs) ff_field_destroy(x);
+    for (int a = 0; a < 3; ++a) {
+        ff_dev_free(f->old[a]);
+        ff_dev_free(f->num[a]);
+        ff_dev_free(f->den[a]);
+        ff_dev_free(f->valid[a]);
+        ff_dev_free(f->adj[a]);
+        ff_dev_free(f->vtmp[0][a]);
+        ff_dev_free(f->vtmp[1][a]);
+        ff_dev_free(f->scratch[a]);
+    }
+    ff_dev_free(f->ccnt);
+    ff_dev_free(f->cacc);
+    delete f;
+    return FF_OK;
+}
+
+extern "C" int ff_flip3_create(ff_ctx ctx, const ff_flip_desc *d, ff_field u, ff_field v, ff_field w, ff_flip *out) {
+    FF_CHECK(ctx && d && out, FF_E_ARG, "ff_flip3_create: NULL argument");
+    FF_CHECK(d->max_particles > 0, FF_E_ARG, "createGridFlipSolver3: options.maxParticles is required.");
+    FF_CHECK(d->max_substeps > 0, FF_E_ARG, "createGridFlipSolver3: maxSubsteps must be positive");
+    const bool density = d->ambient_density != 0.0 || d->component_density != 0.0;
+    FF_CHECK(!density || d->carry_concentration, FF_E_ARG,
+             "createGridFlipSolver3: ambientDensity/componentDensity require carryConcentration: true -- there is no "
+             "concentration field to build a density from otherwise.");
+    FF_CHECK(!density || (d->ambient_density > 0 && d->component_density > 0), FF_E_ARG,
+             "createGridFlipSolver3: ambientDensity and componentDensity must be > 0.");
+    *out = nullptr;
+    cudaSetDevice(ctx->device);
+    ff_flip f = new ff_flip_s();
+    f->ctx = ctx;
+    f->desc = *d;
+    f->g.nx = d->resolution[0];
+    f->g.ny = d->resolution[1];
+    f->g.nz = d->resolution[2];
+    f->g.hx = (float)d->grid_spacing[0];
+    f->g.hy = (float)d->grid_spacing[1];
+    f->g.hz = (float)d->grid_spacing[2];
+    f->g.ox = (float)d->origin[0];
+    f->g.oy = (float)d->origin[1];
+    f->g.oz = (float)d->origin[2];
+    for (int a = 0; a < 3; ++a) {
+        ff_field x = a == 0 ? u : (a == 1 ? v : w);
+        if (!x || x->dtype != FF_FLOAT || x->count != comp_n(f->g, a)) {
+            delete f;
+            return ff_set_error(FF_E_ARG, "createGridFlipSolver3: velocity component %d has the wrong shape", a);
+        }
+    }
+    f->u = u;
+    f->v = v;
+    f->w = w;
+    f->count = d->max_particles;
+    f->density = density;
+    cudaStream_t s = ctx->stream;
+    int st = FF_OK;
+    auto bail = [&](int code) { ff_flip3_destroy(f); return code; };
+    const int np[1] = {d->max_particles};
+    const int cs[3] = {f->g.nx, f->g.ny, f->g.nz};
+    if ((st = ff_field_create(ctx, FF_VEC3, 1, np, &f->pos))) return bail(st);
+    if ((st = ff_field_create(ctx, FF_VEC3, 1, np, &f->vel))) return bail(st);
+    if (d->carry_concentration && (st = ff_field_create(ctx, FF_FLOAT, 1, np, &f->conc))) return bail(st);
+    if ((st = ff_field_create(ctx, FF_FLOAT, 3, cs, &f->mask))) return bail(st);
+    if ((st = ff_field_create(ctx, FF_UINT8, 3, cs, &f->active))) return bail(st);
+    if ((st = ff_field_create(ctx, FF_FLOAT, 3, cs, &f->target))) return bail(st);
+    if (d->carry_concentration) {
+        if ((st = ff_field_create(ctx, FF_FLOAT, 3, cs, &f->cell_conc))) return bail(st);
+        if ((st = ff_field_create(ctx, FF_FLOAT, 3, cs, &f->cell_rho))) return bail(st);
+        if ((st = ff_dev_alloc((void **)&f->ccnt, (size_t)comp_n(f->g, 3) * 4, s))) return bail(st);
+        if ((st = ff_dev_alloc((void **)&f->cacc, (size_t)comp_n(f->g, 3) * 4, s))) return bail(st);
+    }
+    for (int a = 0; a < 3; ++a) {
+        const size_t b = (size_t)comp_n(f->g, a) * 4;
+        if ((st = ff_dev_alloc((void **)&f->old[a], b, s))) return bail(st);
+        if ((st = ff_dev_alloc((void **)&f->num[a], b, s))) return bail(st);
+        if ((st = ff_dev_alloc((void **)&f->den[a], b, s))) return bail(st);
+        if ((st = ff_dev_alloc((void **)&f->valid[a], b, s))) return bail(st);
+        if ((st = ff_dev_alloc((void **)&f->adj[a], b, s))) return bail(st);
+        if ((st = ff_dev_alloc((void **)&f->vtmp[0][a], b, s))) return bail(st);
+        if ((st = ff_dev_alloc((void **)&f->vtmp[1][a], b, s))) return bail(st);
+        if ((st = ff_dev_alloc((void **)&f->scratch[a], b, s))) return bail(st);
+        if (density) {
+            const int fs3[3] = {f->g.nx + (a == 0), f->g.ny + (a == 1), f->g.nz + (a == 2)};
+            if ((st = ff_field_create(ctx, FF_FLOAT, 3, fs3, &f->beta[a]))) return bail(st);
+            if ((st = ff_field_fill(f->beta[a], 1.0f))) return bail(st);
+        }
+    }
+    if (density) {
+        f->r0 = std::max((float)d->ambient_density, MIN_DENSITY);
+        f->r1 = std::max((float)d->component_density, MIN_DENSITY);
+        f->rref = std::max(f->r0, f->r1);
+    }
+    // boundary solver (no collider face weights), advection (trace), pressure
+    if ((st = ff_bc3_create(ctx, d->resolution, d->grid_spacing, d->origin, &f->bc))) return bail(st);
+    if ((st = ff_bc3_set_closed(f->bc, d->closed_flags))) return bail(st);
+    ff_advect_desc ad{};
+    for (int a = 0; a < 3; ++a) {
+        ad.resolution[a] = d->resolution[a];
+        ad.grid_spacing[a] = d->grid_spacing[a];
+        ad.origin[a] = d->origin[a];
+    }
+    ad.dt = d->dt;
+    ad.max_substeps = d->max_substeps;
+    ad.order = 1;
+    if ((st = ff_advect3_create(ctx, &ad, &f->adv))) return bail(st);
+    ff_pressure_desc pd = d->pressure;
+    for (int a = 0; a < 3; ++a) {
+        pd.resolution[a] = d->resolution[a];
+        pd.grid_spacing[a] = d->grid_spacing[a];
+        pd.origin[a] = d->origin[a];
+    }
+    if (!(pd.max_plausible_pressure > 0)) {
+        // derivedMaxPlausiblePressure (:361-366), in doubles as the reference
+        const double gm = std::hypot(std::hypot(d->gravity[0], d->gravity[1]), d->gravity[2]);
+        const double ext = d->resolution[0] * d->grid_spacing[0] + d->resolution[1] * d->grid_spacing[1] +
+                           d->resolution[2] * d->grid_spacing[2];
+        pd.max_plausible_pressure =
+            (d->reduced_pressure && gm > 0) ? PRESSURE_BOUND_HEADROOM * d->dt * gm * ext : 1e6;
+    }
+    if ((st = ff_pressure3_create(ctx, &pd, &f->ps))) return bail(st);
+    if ((st = ff_pressure3_set_dirichlet(f->ps, f->active, f->target))) return bail(st);
+    if (density && (st = ff_pressure3_set_face_weights(f->ps, f->beta[0], f->beta[1], f->beta[2]))) return bail(st);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return bail(ff_set_error(FF_E_CUDA, "flip create sync"));
+    *out = f;
+    return FF_OK;
+}
+
+extern "C" int ff_flip3_set_collider(ff_flip f, ff_field phi) {
+    FF_CHECK(f, FF_E_ARG, "NULL FLIP solver");
+    FF_CHECK(!phi || (phi->dtype == FF_FLOAT && phi->count == comp_n(f->g, 3)), FF_E_ARG,
+             "FLIP collider must be a float cell SDF");
+    f->phi = phi;
+    FF_TRY(ff_bc3_set_collider(f->bc, phi, nullptr, nullptr, nullptr));
+    return ff_advect3_set_collider(f->adv, phi);
+}
+
+extern "C" int ff_flip3_set_count(ff_flip f, int n) {
+    FF_CHECK(f && n >= 0 && n <= f->desc.max_particles, FF_E_ARG, "FLIP particle count out of range");
+    f->count = n;
+    return FF_OK;
+}
+
+extern "C" int ff_flip3_fields(ff_flip f, ff_field *positions, ff_field *velocities, ff_field *concentration,
+                               ff_field *fluid_mask, ff_pressure *pressure) {
+    FF_CHECK(f, FF_E_ARG, "NULL FLIP solver");
+    if (positions) *positions = f->pos;
+    if (velocities) *velocities = f->vel;
+    if (concentration) *concentration = f->conc;
+    if (fluid_mask) *fluid_mask = f->mask;
+    if (pressure) *pressure = f->ps;
+    return FF_OK;
+}
+
+extern "C" int ff_flip3_grid_fields(ff_flip f, ff_field *cell_concentration, ff_field *cell_density, ff_field *beta_u,
+                                    ff_field *beta_v, ff_field *beta_w, ff_field *dirichlet_active,
+                                    ff_field *dirichlet_target) {
+    FF_CHECK(f, FF_E_ARG, "NULL FLIP solver");
+    if (cell_concentration) *cell_concentration = f->cell_conc;
+    if (cell_density) *cell_density = f->density ? f->cell_rho : nullptr;
+    if (beta_u) *beta_u = f->beta[0];
+    if (beta_v) *beta_v = f->beta[1];
+    if (beta_w) *beta_w = f->beta[2];
+    if (dirichlet_active) *dirichlet_active = f->active;
+    if (dirichlet_target) *dirichlet_target = f->target;
+    return FF_OK;
+}
+
+static int extrapolate(ff_flip f, float *data, const int *marker, int a) {
+    cudaStream_t s = f->ctx->stream;
+    int sx, sy, sz;
+    comp_shape(f->g, a, sx, sy, sz);
+    const long long n = comp_n(f->g, a);
+    FF_CUDA(cudaMemcpyAsync(f->vtmp[0][a], marker, n * 4, cudaMemcpyDeviceToDevice, s));
+    float *src = data, *dst = f->scratch[a];
+    int *vs = f->vtmp[0][a], *vd = f->vtmp[1][a];
+    for (int it = 0; it < f->desc.extrapolation_depth; ++it) {
+        k_extrapolate<<<blocks_for(n), 256, 0, s>>>(sx, sy, sz, src, dst, vs, vd);
+        std::swap(src, dst);
+        std::swap(vs, vd);
+    }
+    if (src != data) FF_CUDA(cudaMemcpyAsync(data, src, n * 4, cudaMemcpyDeviceToDevice, s));
+    return post("extrapolate");
+}
+
+// One stage of onAdvanceTimeStep (:1110-1150).
+extern "C" int ff_flip3_stage(ff_flip f, int stage) {
+    FF_CHECK(f, FF_E_ARG, "NULL FLIP solver");
+    cudaSetDevice(f->ctx->device);
+    cudaStream_t s = f->ctx->stream;
+    const ff_flip_desc &d = f->desc;
+    const G3 &g = f->g;
+    const long long n = f->count;
+    float *uvw[3] = {(float *)f->u->d, (float *)f->v->d, (float *)f->w->d};
+    float *pos = (float *)f->pos->d, *vel = (float *)f->vel->d;
+    const F3 grav{(float)d.gravity[0], (float)d.gravity[1], (float)d.gravity[2]};
+    switch (stage) {
+    case FF_FLIP_ADVECT_PARTICLES: {
+        if (n == 0) return FF_OK;
+        VelField F{g, uvw[0], uvw[1], uvw[2], f->phi ? (const float *)f->phi->d : nullptr};
+        // minPos / maxPos (:927-929): the extent in doubles, stored as f32
+        const F3 ext{(float)(d.resolution[0] * d.grid_spacing[0]), (float)(d.resolution[1] * d.grid_spacing[1]),
+                     (float)(d.resolution[2] * d.grid_spacing[2])};
+        const F3 mn{g.ox + 1e-4f, g.oy + 1e-4f, g.oz + 1e-4f};
+        const F3 mx{(g.ox + ext.x) - 1e-4f, (g.oy + ext.y) - 1e-4f, (g.oz + ext.z) - 1e-4f};
+        k_flip_advect<<<blocks_for(n), 256, 0, s>>>(F, n, pos, (float)d.dt, d.max_substeps, mn, mx,
+                                                    (float)d.collider_push_thresh, (float)d.collider_push_shift);
+        return post("advectParticles");
+    }
+    case FF_FLIP_P2G: {
+        for (int a = 0; a < 3; ++a) {
+            FF_CUDA(cudaMemsetAsync(f->num[a], 0, comp_n(g, a) * 4, s));
+            FF_CUDA(cudaMemsetAsync(f->den[a], 0, comp_n(g, a) * 4, s));
+        }
+        const float S = (float)d.p2g_atomic_scale;
+        if (n) k_flip_scatter<<<blocks_for(n), 256, 0, s>>>(g, n, pos, vel, S, f->num[0], f->den[0], f->num[1],
+                                                            f->den[1], f->num[2], f->den[2]);
+        for (int a = 0; a < 3; ++a)
+            k_flip_finalize<<<blocks_for(comp_n(g, a)), 256, 0, s>>>(comp_n(g, a), f->num[a], f->den[a], S,
+                                                                     (float)d.weight_epsilon, uvw[a], f->valid[a]);
+        return post("P2G");
+    }
+    case FF_FLIP_SNAPSHOT:
+        for (int a = 0; a < 3; ++a)
+            FF_CUDA(cudaMemcpyAsync(f->old[a], uvw[a], comp_n(g, a) * 4, cudaMemcpyDeviceToDevice, s));
+        return FF_OK;
+    case FF_FLIP_EXTRAPOLATE_WEIGHT:
+        for (int a = 0; a < 3; ++a) FF_TRY(extrapolate(f, uvw[a], f->valid[a], a));
+        return FF_OK;
+    case FF_FLIP_CONSTRAIN:
+        return ff_bc3_constrain(f->bc, f->u, f->v, f->w, d.extrapolation_depth);
+    case FF_FLIP_MARK_FLUID:
+        FF_CUDA(cudaMemsetAsync(f->mask->d, 0, comp_n(g, 3) * 4, s));
+        if (n) k_flip_mark<<<blocks_for(n), 256, 0, s>>>(g, n, pos, (float *)f->mask->d);
+        for (int a = 0; a < 3; ++a)
+            k_flip_adjacent<<<blocks_for(comp_n(g, a)), 256, 0, s>>>(g, a, (const float *)f->mask->d, f->adj[a]);
+        return post("markFluidCells");
+    case FF_FLIP_CONCENTRATION_GRID: {
+        if (!d.carry_concentration) return FF_OK;
+        const long long nc = comp_n(g, 3);
+        FF_CUDA(cudaMemsetAsync(f->ccnt, 0, nc * 4, s));
+        FF_CUDA(cudaMemsetAsync(f->cacc, 0, nc * 4, s));
+        const float cscale = (float)d.concentration_atomic_scale;
+        if (n) k_flip_conc_accum<<<blocks_for(n), 256, 0, s>>>(g, n, pos, (const float *)f->conc->d, cscale, f->ccnt,
+                                                               f->cacc);
+        k_flip_conc_resolve<<<blocks_for(nc), 256, 0, s>>>(nc, f->ccnt, f->cacc, cscale, f->density, f->r0, f->r1,
+                                                           (float *)f->cell_conc->d, (float *)f->cell_rho->d);
+        if (f->density)
+            for (int a = 0; a < 3; ++a)
+                k_flip_beta<<<blocks_for(comp_n(g, a)), 256, 0, s>>>(g, a, (const float *)f->cell_rho->d,
+                                                                     (const float *)f->mask->d, f->rref,
+                                                                     (float *)f->beta[a]->d);
+        return post("concentration");
+    }
+    case FF_FLIP_GRAVITY:
+        // reduced pressure puts gravity in the air cells' Dirichlet target;
+        // with the density coupling the grid still takes the beta term
+        if (d.reduced_pressure && !f->density) return FF_OK;
+        for (int a = 0; a < 3; ++a)
+            k_flip_gravity<<<blocks_for(comp_n(g, a)), 256, 0, s>>>(
+                g, a, f->density ? (const float *)f->cell_rho->d : nullptr,
+                (d.reduced_pressure && f->density) ? (const float *)f->beta[a]->d : nullptr, grav, (float)d.dt,
+                f->rref, uvw[a]);
+        return post("gravity");
+    case FF_FLIP_PROJECT: {
+        k_flip_dirichlet<<<blocks_for(comp_n(g, 3)), 256, 0, s>>>(g, (const float *)f->mask->d, grav, (float)d.dt,
+                                                                  d.reduced_pressure, (uint8_t *)f->active->d,
+                                                                  (float *)f->target->d);
+        FF_TRY(post("dirichlet"));
+        return ff_pressure3_project(f->ps, f->u, f->v, f->w, f->u, f->v, f->w, &f->last);
+    }
+    case FF_FLIP_EXTRAPOLATE_PRESSURE:
+        for (int a = 0; a < 3; ++a) FF_TRY(extrapolate(f, uvw[a], f->adj[a], a));
+        return FF_OK;
+    case FF_FLIP_G2P:
+        if (n) k_flip_g2p<<<blocks_for(n), 256, 0, s>>>(g, n, pos, vel, uvw[0], uvw[1], uvw[2], f->old[0], f->old[1],
+                                                        f->old[2], (float)d.flip_ratio,
+                                                        std::min(std::max((float)d.velocity_damping, 0.0f), 1.0f));
+        return post("G2P");
+    case FF_FLIP_CONCENTRATION_PARTICLE:
+        if (!d.carry_concentration || !n) return FF_OK;
+        k_flip_mix_fade<<<blocks_for(n), 256, 0, s>>>(g, n, pos, (const float *)f->cell_conc->d,
+                                                      std::min(std::max((float)d.mixing, 0.0f), 1.0f),
+                                                      std::min(std::max((float)d.fade, 0.0f), 1.0f),
+                                                      (float *)f->conc->d);
+        return post("mixAndFade");
+    default:
+        return ff_set_error(FF_E_ARG, "ff_flip3_stage: unknown stage %d", stage);
+    }
+}
+
+// onAdvanceTimeStep (:1137-1144): pre-P2G, P2G and grid stages, the
+// projection, then the post-projection stages.  Resampling (:621-820) is
+// not part of this step.
+extern "C" int ff_flip3_step(ff_flip f, ff_diag *diag) {
+    FF_CHECK(f, FF_E_ARG, "NULL FLIP solver");
+    static const int order[] = {FF_FLIP_ADVECT_PARTICLES, FF_FLIP_P2G,         FF_FLIP_SNAPSHOT,
+                                FF_FLIP_EXTRAPOLATE_WEIGHT, FF_FLIP_CONSTRAIN,   FF_FLIP_MARK_FLUID,
+                                FF_FLIP_CONCENTRATION_GRID, FF_FLIP_GRAVITY,     FF_FLIP_CONSTRAIN,
+                                FF_FLIP_PROJECT,            FF_FLIP_CONSTRAIN,   FF_FLIP_EXTRAPOLATE_PRESSURE,
+                                FF_FLIP_G2P,                FF_FLIP_CONCENTRATION_PARTICLE};
+    for (int st : order) FF_TRY(ff_flip3_stage(f, st));
+    if (diag) *diag = f->last;
+    return FF_OK;
+}

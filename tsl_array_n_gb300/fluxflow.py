@@ -13,6 +13,9 @@ Names, option names, defaults and error behaviour follow the reference
   create_grid_blocked_boundary_condition_solver3
                                   grid_blocked_boundary_condition_solver3.js:48-490
   apply_viscosity3                explicit viscosity (no reference counterpart)
+  create_grid_flip_solver3        grid_flip_solver3.js:135-1157 (no resampling)
+  compute_flip_box_seed3          grid_flip_solver3.js:70-130
+  create_jitter_random            jitter_random.js:29-46
 """
 import ctypes as C
 
@@ -531,3 +534,158 @@ def apply_viscosity3(input_grid, output_grid, nu, dt):
         context().handle, (C.c_int * 3)(*g.resolution), (C.c_double * 3)(*g.grid_spacing), g.data_u.handle,
         g.data_v.handle, g.data_w.handle, float(nu), float(dt), output_grid.data_u.handle,
         output_grid.data_v.handle, output_grid.data_w.handle))
+
+
+# -------------------------------------------------------------------- FLIP --
+DEFAULT_JITTER_SEED = 0x9E3779B9   # jitter_random.js:46
+
+
+def create_jitter_random(seed):
+    """createJitterRandom(seed): a function returning the next value in [0, 1)."""
+    state = {"seed": int(seed) & 0xFFFFFFFF, "i": 0, "buf": []}
+
+    def random():
+        if state["i"] >= len(state["buf"]):
+            n = 1024 + state["i"]
+            out = (C.c_double * n)()
+            _lib.check(_lib.load().ff_jitter_random(state["seed"], n, out))
+            state["buf"] = list(out)
+        v = state["buf"][state["i"]]
+        state["i"] += 1
+        return v
+    return random
+
+
+def compute_flip_box_seed3(box_min, box_max, grid_spacing_x, grid_spacing_y, grid_spacing_z, particles_per_cell_axis=2,
+                           jitter=0.2, random_seed=DEFAULT_JITTER_SEED):
+    """computeFlipBoxSeed3({boxMin, boxMax, gridSpacingX/Y/Z,
+    particlesPerCellAxis, jitter, randomSeed}) -> {count, positionsArray,
+    velocitiesArray}."""
+    dd = lambda v: (C.c_double * 3)(*[float(x) for x in v])
+    h = dd((grid_spacing_x, grid_spacing_y, grid_spacing_z))
+    lib = _lib.load()
+    count = C.c_int64()
+    _lib.check(lib.ff_flip_box_seed3(dd(box_min), dd(box_max), h, int(particles_per_cell_axis), float(jitter),
+                                     int(random_seed) & 0xFFFFFFFF, None, 0, C.byref(count)))
+    pos = np.empty(3 * count.value, np.float32)
+    _lib.check(lib.ff_flip_box_seed3(dd(box_min), dd(box_max), h, int(particles_per_cell_axis), float(jitter),
+                                     int(random_seed) & 0xFFFFFFFF, pos.ctypes.data_as(C.POINTER(C.c_float)),
+                                     count.value, C.byref(count)))
+    return {"count": count.value, "positionsArray": pos, "velocitiesArray": np.zeros_like(pos)}
+
+
+class GridFlipSolver3:
+    """createGridFlipSolver3({velocityGrid, gridSpacing, origin, maxParticles,
+    dt, gravity, reducedPressure, flipRatio, velocityDamping, p2gAtomicScale,
+    weightEpsilon, closedDomainBoundaryFlag, collider, colliderPushThresh,
+    colliderPushShift, carryConcentration, mixing, fade,
+    concentrationAtomicScale, ambientDensity, componentDensity, pressure})
+    (grid_flip_solver3.js:135-1157), without particle resampling."""
+
+    STAGES = {"advectParticles": 0, "p2g": 1, "snapshotOld": 2, "extrapolateWeight": 3, "constrainVelocity": 4,
+              "markFluidCells": 5, "concentrationGrid": 6, "gravity": 7, "project": 8, "extrapolatePressure": 9,
+              "g2p": 10, "concentrationParticle": 11}
+
+    def __init__(self, velocity_grid=None, max_particles=None, dt=None, gravity=(0.0, -9.81, 0.0),
+                 reduced_pressure=True, flip_ratio=0.97, velocity_damping=0.02, p2g_atomic_scale=65536.0,
+                 weight_epsilon=1e-4, closed_domain_boundary_flag=None, collider=None, collider_push_thresh=0.0,
+                 collider_push_shift=0.0, carry_concentration=False, mixing=0.0, fade=0.0,
+                 concentration_atomic_scale=4096.0, ambient_density=None, component_density=None, pressure=None,
+                 max_substeps=32, extrapolation_depth=5):
+        if velocity_grid is None:
+            raise ValueError("createGridFlipSolver3: options.velocityGrid is required.")
+        if not max_particles:
+            raise ValueError("createGridFlipSolver3: options.maxParticles is required.")
+        g = velocity_grid
+        self.velocity_grid = g
+        lib = _lib.load()
+        d = _lib.FlipDesc()
+        lib.ff_flip_desc_default(C.byref(d), (C.c_int * 3)(*g.resolution), (C.c_double * 3)(*g.grid_spacing),
+                                 int(max_particles), float(dt))
+        d.origin[:] = list(g.origin)
+        d.gravity[:] = [float(x) for x in gravity]
+        d.reduced_pressure = int(bool(reduced_pressure))
+        d.flip_ratio, d.velocity_damping = float(flip_ratio), float(velocity_damping)
+        d.p2g_atomic_scale, d.weight_epsilon = float(p2g_atomic_scale), float(weight_epsilon)
+        if closed_domain_boundary_flag is not None:
+            d.closed_flags = int(closed_domain_boundary_flag)
+        d.max_substeps = int(max_substeps)
+        d.collider_push_thresh, d.collider_push_shift = float(collider_push_thresh), float(collider_push_shift)
+        d.carry_concentration = int(bool(carry_concentration))
+        d.mixing, d.fade = float(mixing), float(fade)
+        d.concentration_atomic_scale = float(concentration_atomic_scale)
+        if (ambient_density is None) != (component_density is None):
+            raise ValueError("createGridFlipSolver3: give both ambientDensity and componentDensity or neither.")
+        if ambient_density is not None:
+            d.ambient_density, d.component_density = float(ambient_density), float(component_density)
+        d.extrapolation_depth = int(extrapolation_depth)
+        p = pressure or {}
+        mg = p.get("multigrid", {})
+        pd = d.pressure
+        pd.preconditioner = PRECONDITIONERS[p.get("preconditioner", "multigrid")]
+        pd.tolerance = float(p.get("tolerance", pd.tolerance))
+        pd.mg_levels = int(mg.get("numberOfLevels", pd.mg_levels))
+        pd.mg_down = int(mg.get("numberOfSmoothingIterationsDown", pd.mg_down))
+        pd.mg_up = int(mg.get("numberOfSmoothingIterationsUp", pd.mg_up))
+        pd.mg_coarsest = int(mg.get("numberOfCoarsestIterations", pd.mg_coarsest))
+        pd.mg_coarse_mode = 1 if mg.get("coarseSolve", "sweeps") == "direct" else 0
+        if "maxPlausiblePressure" in p:
+            pd.max_plausible_pressure = float(p["maxPlausiblePressure"])
+        if p.get("precision", "fp32") != "fp32":
+            pd.iterate = 1
+        self.desc = d
+        self.handle = C.c_void_p()
+        _lib.check(lib.ff_flip3_create(context().handle, C.byref(d), g.data_u.handle, g.data_v.handle,
+                                       g.data_w.handle, C.byref(self.handle)))
+        self.collider = collider
+        if collider is not None:
+            _lib.check(lib.ff_flip3_set_collider(self.handle, collider.phi.handle))
+        hs = [C.c_void_p() for _ in range(5)]
+        _lib.check(lib.ff_flip3_fields(self.handle, *[C.byref(x) for x in hs]))
+        ctx = context()
+        self.positions = BorrowedField(hs[0], ctx)
+        self.velocities = BorrowedField(hs[1], ctx)
+        self.concentration = BorrowedField(hs[2], ctx) if hs[2].value else None
+        self.fluid_mask = BorrowedField(hs[3], ctx)
+        self.diagnostics = {}
+
+    def grid_fields(self):
+        """cellConcentration, cellDensity, (betaU, betaV, betaW) and the
+        Dirichlet active/target fields of the last projection (None when
+        not in use)."""
+        hs = [C.c_void_p() for _ in range(7)]
+        _lib.check(_lib.load().ff_flip3_grid_fields(self.handle, *[C.byref(x) for x in hs]))
+        ctx = context()
+        f = [BorrowedField(h, ctx) if h.value else None for h in hs]
+        return {"cellConcentration": f[0], "cellDensity": f[1], "beta": tuple(f[2:5]), "dirichletActive": f[5],
+                "dirichletTarget": f[6]}
+
+    def set_particle_count(self, n):
+        _lib.check(_lib.load().ff_flip3_set_count(self.handle, int(n)))
+
+    def stage(self, name):
+        _lib.check(_lib.load().ff_flip3_stage(self.handle, self.STAGES[name]))
+
+    def on_advance_time_step(self):
+        """onAdvanceTimeStep(): returns the projection's diagnostics."""
+        d = _lib.Diag()
+        _lib.check(_lib.load().ff_flip3_step(self.handle, C.byref(d)))
+        self.diagnostics = {"converged": bool(d.converged), "rejected": bool(d.rejected),
+                            "iterations": d.iterations, "stoppedBy": STOP_REASONS.get(d.stopped_by, "none"),
+                            "residual": d.residual}
+        return self.diagnostics
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.load().ff_flip3_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def create_grid_flip_solver3(**options):
+    return GridFlipSolver3(**options)
