@@ -126,6 +126,7 @@ typedef struct {
     int bad_cells;              /* non-finite or |p| > maxPlausiblePressure    */
     int max_iterations;         /* the cap that applied                        */
     int kernel_launches;        /* libff kernels launched by the call          */
+    int warm_start;             /* -1 none, 0 previous pressure kept, 1 network guess used */
 } ff_diag;
 
 #define FF_STOP_NONE 0
@@ -335,6 +336,38 @@ int ff_flip_box_seed3(const double *box_min, const double *box_max, const double
                       double jitter, uint32_t seed, float *positions, int64_t capacity, int64_t *count);
 /* createJitterRandom(seed): the first n values                           */
 int ff_jitter_random(uint32_t seed, int n, double *out);
+
+/* ---- learned warm start (no reference counterpart): a 3-level 3D U-Net
+ * (16/32/64 channels, 3x3x3 convolutions, GELU, 2x average pooling, nearest
+ * upsampling with skip concatenation, a 1x1 output) mapping (divergence b,
+ * solid mask, previous pressure) to a pressure guess.  BF16 weights and
+ * activations, FP32 accumulation, FP32 master weights and Adam.  Inputs are
+ * normalised by rms(b) and rms(p_prev) (or rms(b) L^2 / 4 pi^2 when p_prev
+ * is zero); the output is in pressure units.  Resolutions must be multiples
+ * of 4.  Parameters are one FP32 vector: per convolution W[27][cin][cout]
+ * (tap = (dz+1) 9 + (dy+1) 3 + (dx+1)) then bias[cout], in network order,
+ * then the output layer's 16 weights and bias.                            */
+typedef struct ff_unet_s *ff_unet;
+int ff_unet_create(ff_ctx ctx, uint32_t seed, ff_unet *out);
+int ff_unet_destroy(ff_unet u);
+int ff_unet_param_count(ff_unet u, int64_t *n);
+int ff_unet_get_params(ff_unet u, float *host, int64_t n);
+int ff_unet_set_params(ff_unet u, const float *host, int64_t n);   /* resets Adam */
+int ff_unet_get_grads(ff_unet u, float *host, int64_t n);
+/* p_prev and mask may be NULL; out: float cell field                     */
+int ff_unet_forward(ff_unet u, const int *resolution, double grid_spacing, ff_field b, ff_field mask,
+                    ff_field p_prev, ff_field out);
+/* forward, MSE against target (normalised units), backward into the
+ * gradient buffer (overwritten), loss in *loss                            */
+int ff_unet_loss_backward(ff_unet u, const int *resolution, double grid_spacing, ff_field b, ff_field mask,
+                          ff_field p_prev, ff_field target, double *loss);
+int ff_unet_adam_step(ff_unet u, double lr, double beta1, double beta2, double eps);
+/* Use `net` (borrowed; NULL to stop) for the initial guess of every later
+ * project()/solve(): after the system is built, the network predicts p0
+ * from (b, Dirichlet mask, current pressure); p0 replaces the current
+ * pressure only when ||b - A p0|| < ||b - A p_prev||, and Dirichlet cells
+ * keep their targets.  ff_diag.warm_start reports the choice.             */
+int ff_pressure3_set_warm_start(ff_pressure ps, ff_unet net);
 
 /* ---- test hooks mirroring the exported multigrid.js / linalg.js pieces -- */
 /* createLaplacianOperator (multigrid.js:457-471): y = A x with the solver's

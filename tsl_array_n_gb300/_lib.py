@@ -54,7 +54,8 @@ class FlipDesc(C.Structure):
 class Diag(C.Structure):
     _fields_ = [("converged", C.c_int), ("rejected", C.c_int), ("iterations", C.c_int),
                 ("stopped_by", C.c_int), ("residual", C.c_double), ("b_norm", C.c_double),
-                ("bad_cells", C.c_int), ("max_iterations", C.c_int), ("kernel_launches", C.c_int)]
+                ("bad_cells", C.c_int), ("max_iterations", C.c_int), ("kernel_launches", C.c_int),
+                ("warm_start", C.c_int)]
 
 
 # every symbol include/ff.h declares, with (restype, argtypes)
@@ -123,6 +124,16 @@ PROTOTYPES = {
     "ff_flip_box_seed3": (_I, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double), _I, _D,
                                C.c_uint32, _FP, C.c_int64, C.POINTER(C.c_int64)]),
     "ff_jitter_random": (_I, [C.c_uint32, _I, C.POINTER(C.c_double)]),
+    "ff_unet_create": (_I, [_P, C.c_uint32, _PP]),
+    "ff_unet_destroy": (_I, [_P]),
+    "ff_unet_param_count": (_I, [_P, C.POINTER(C.c_int64)]),
+    "ff_unet_get_params": (_I, [_P, _FP, C.c_int64]),
+    "ff_unet_set_params": (_I, [_P, _FP, C.c_int64]),
+    "ff_unet_get_grads": (_I, [_P, _FP, C.c_int64]),
+    "ff_unet_forward": (_I, [_P, _IP, _D, _P, _P, _P, _P]),
+    "ff_unet_loss_backward": (_I, [_P, _IP, _D, _P, _P, _P, _P, C.POINTER(C.c_double)]),
+    "ff_unet_adam_step": (_I, [_P, _D, _D, _D, _D]),
+    "ff_pressure3_set_warm_start": (_I, [_P, _P]),
     "ff_laplacian_apply": (_I, [_P, _P, _P]),
     "ff_precondition_apply": (_I, [_P, _P, _P]),
     "ff_mg_restrict": (_I, [_P, _I, _P, _P]),

@@ -56,6 +56,10 @@ struct ff_pressure_s {
     // TMA descriptors per level (levels where the TMA sweep applies)
     SweepMaps *smaps = nullptr;
     bool use_tma = true;
+    // learned warm start (borrowed network), its guess field, last choice
+    ff_unet net = nullptr;
+    ff_field guess = nullptr;
+    int warm_used = -1;
 
     // coarsest direct solve
     double *G = nullptr;
@@ -245,6 +249,7 @@ extern "C" int ff_pressure3_destroy(ff_pressure ps) {
     if (!ps) return FF_OK;
     cudaStreamSynchronize(ps->ctx->stream);
     destroy_graphs(ps);
+    ff_field_destroy(ps->guess);
     if (ps->smaps)
         for (size_t l = 0; l < ps->lv.size(); ++l) ff_dev_free(ps->smaps[l].cls_ptr);
     delete[] ps->smaps;
@@ -739,6 +744,82 @@ static int run_solve(ff_pressure ps) {
 static int read_diag(ff_pressure ps, ff_diag *diag, int extra_launches);
 static int prepare_launches(ff_pressure ps, bool build);
 
+namespace {
+// sum over cells of (b - Ax)^2 into FP64 block partials
+__global__ void k_res_sumsq(long long n, const float *__restrict__ b, const float *__restrict__ ax,
+                            double *__restrict__ partial) {
+    __shared__ double sred[256];
+    double acc = 0.0;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        const double r = (double)b[c] - (double)ax[c];
+        acc += r * r;
+    }
+    sred[threadIdx.x] = acc;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st) sred[threadIdx.x] += sred[threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sred[0];
+}
+// the iterate becomes the guess; Dirichlet cells keep their targets
+__global__ void k_apply_guess(long long n, const float *__restrict__ guess, const uint8_t *__restrict__ mask,
+                              const float *__restrict__ tgt, float *__restrict__ hi, float *__restrict__ lo) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        hi[c] = mask[c] ? tgt[c] : guess[c];
+        if (lo) lo[c] = 0.0f;
+    }
+}
+}  // namespace
+
+extern "C" int ff_pressure3_set_warm_start(ff_pressure ps, ff_unet net) {
+    FF_CHECK(ps, FF_E_ARG, "NULL pressure solver");
+    ps->net = net;
+    if (net && !ps->guess) {
+        int shape[3] = {ps->d.nx, ps->d.ny, ps->d.nz};
+        FF_TRY(ff_field_create(ps->ctx, FF_FLOAT, 3, shape, &ps->guess));
+    }
+    return FF_OK;
+}
+
+// ||b - A x||^2 with the level-0 operator (x in `ax` scratch afterwards)
+static int residual_sq(ff_pressure ps, const float *x, float *ax, double *out) {
+    cudaStream_t s = ps->s();
+    const long long n = ps->d.n();
+    FF_TRY(ffk::laplacian_apply(ps->d, ps->lv[0].coef, x, ax, s));
+    const int nb = 256;
+    k_res_sumsq<<<nb, 256, 0, s>>>(n, (const float *)ps->bfield->d, ax, ps->partials);
+    FF_CUDA(cudaGetLastError());
+    std::vector<double> hp(nb);
+    FF_CUDA(cudaMemcpyAsync(hp.data(), ps->partials, sizeof(double) * nb, cudaMemcpyDeviceToHost, s));
+    FF_CUDA(cudaStreamSynchronize(s));
+    double t = 0;
+    for (double x2 : hp) t += x2;
+    *out = t;
+    return FF_OK;
+}
+
+// learned warm start: predict, compare residuals, keep the better start
+static int warm_start(ff_pressure ps) {
+    ps->warm_used = -1;
+    if (!ps->net) return FF_OK;
+    cudaStream_t s = ps->s();
+    int res[3] = {ps->d.nx, ps->d.ny, ps->d.nz};
+    FF_TRY(ff_unet_forward(ps->net, res, (double)ps->hx, ps->bfield, ps->maskf, ps->pressure, ps->guess));
+    double r_prev, r_net;
+    FF_TRY(residual_sq(ps, ps->xh0(), ps->r, &r_prev));
+    FF_TRY(residual_sq(ps, (const float *)ps->guess->d, ps->p0, &r_net));
+    ps->warm_used = 0;
+    if (r_net < r_prev) {
+        const long long n = ps->d.n();
+        k_apply_guess<<<256, 256, 0, s>>>(n, (const float *)ps->guess->d, (const uint8_t *)ps->maskf->d, ps->tgt,
+                                          ps->xh0(), ps->x_lo0);
+        FF_CUDA(cudaGetLastError());
+        ps->warm_used = 1;
+    }
+    return FF_OK;
+}
+
 extern "C" int ff_pressure3_project(ff_pressure ps, ff_field u_in, ff_field v_in, ff_field w_in,
                                     ff_field u_out, ff_field v_out, ff_field w_out, ff_diag *diag) {
     FF_CHECK(ps && u_in && v_in && u_out && v_out, FF_E_ARG, "project: NULL field");
@@ -752,6 +833,7 @@ extern "C" int ff_pressure3_project(ff_pressure ps, ff_field u_in, ff_field v_in
     cudaSetDevice(ps->ctx->device);
     cudaStream_t s = ps->s();
     FF_TRY(prepare(ps, u_in, v_in, w_in));
+    FF_TRY(warm_start(ps));
     FF_TRY(run_solve(ps));
     // circuit breaker + snapshot (:289-336, :547-554), then the correction
     FF_TRY(ffk::count_bad_and_commit(d, ps->xh0(), ps->x_lo0, ps->x_hi1, ps->x_lo1, ps->snap_hi,
@@ -813,6 +895,7 @@ static int read_diag(ff_pressure ps, ff_diag *diag, int extra_launches) {
         diag->bad_cells = h.bad_cells;
         diag->rejected = ps->check_bad && h.bad_cells > 0;
         diag->max_iterations = ps->maxiter;
+        diag->warm_start = ps->warm_used;
         // setup: state init, residual, preconditioner, r.z; then each loop
         // body the device ran: p/pAp, x/residual, preconditioner, r.z, control
         int per_iter = 4 + precond_launches(ps);
@@ -830,6 +913,7 @@ extern "C" int ff_pressure3_solve(ff_pressure ps, ff_field b, ff_diag *diag) {
     cudaStream_t s = ps->s();
     FF_TRY(prepare(ps, nullptr, nullptr, nullptr));
     FF_CUDA(cudaMemcpyAsync(ps->bfield->d, b->d, b->bytes, cudaMemcpyDeviceToDevice, s));
+    FF_TRY(warm_start(ps));
     FF_TRY(run_solve(ps));
     FF_TRY(ffk::count_bad_and_commit(ps->d, ps->xh0(), ps->x_lo0, ps->x_hi1, ps->x_lo1, ps->snap_hi,
                                      ps->snap_lo, ps->st,

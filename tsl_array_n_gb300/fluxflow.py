@@ -282,7 +282,7 @@ class GridPressureSolver3:
                 iterations=int(diag.iterations), stoppedBy=STOP_REASONS[diag.stopped_by],
                 residual=float(diag.residual), bNorm=float(diag.b_norm),
                 badCells=int(diag.bad_cells), maxIterations=int(diag.max_iterations),
-                kernelLaunches=int(diag.kernel_launches))
+                kernelLaunches=int(diag.kernel_launches), warmStart=int(diag.warm_start))
             return self.diagnostics
 
         return dispatch
@@ -295,7 +295,8 @@ class GridPressureSolver3:
             converged=bool(diag.converged), rejected=bool(diag.rejected),
             iterations=int(diag.iterations), stoppedBy=STOP_REASONS[diag.stopped_by],
             residual=float(diag.residual), bNorm=float(diag.b_norm),
-            badCells=int(diag.bad_cells), maxIterations=int(diag.max_iterations))
+            badCells=int(diag.bad_cells), maxIterations=int(diag.max_iterations),
+            warmStart=int(diag.warm_start))
         return dict(self.diagnostics)
 
     # -- test hooks -----------------------------------------------------------
