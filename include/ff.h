@@ -73,6 +73,8 @@ int ff_field_download(ff_field f, void *host, size_t bytes);
 int ff_field_upload_async(ff_field f, const void *host, size_t bytes);
 int ff_field_download_async(ff_field f, void *host, size_t bytes);
 int ff_field_fill(ff_field f, float value);
+/* device-to-device copy between fields of one type and size              */
+int ff_field_copy(ff_field dst, ff_field src);
 int ff_field_info(ff_field f, int *dtype, int *ndim, int *shape3, int64_t *count);
 void *ff_field_device_ptr(ff_field f);
 
@@ -256,6 +258,12 @@ int ff_bc3_set_closed(ff_bc b, int flags);
 int ff_bc3_set_inflows(ff_bc b, int n, const ff_field *phis, const double *velocities, const int *modes);
 /* constrainVelocity(extrapolationDepth = 5) (:445-477), in place          */
 int ff_bc3_constrain(ff_bc b, ff_field u, ff_field v, ff_field w, int depth);
+
+/* ---- external force: createExternalForceSolver3 (fluxflow
+ * src/grid/external_force_solver3.js:7-29) for a uniform force; every face
+ * of each component gains force.x * dt (.y, .z).                           */
+int ff_velocity3_add_force(ff_ctx ctx, const int *resolution, ff_field u, ff_field v, ff_field w, double fx,
+                           double fy, double fz, double dt);
 
 /* ---- explicit viscosity (no counterpart: grid_solver3.js:104 leaves
  * computeViscosity a no-op): out = in + dt nu lap(in) on the faces strictly

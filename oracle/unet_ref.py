@@ -1,8 +1,8 @@
 """Oracle (test infrastructure only): the warm-start U-Net in PyTorch on the
 CPU in FP32, rounding to BF16 at the points where the GPU stores BF16 (the
-normalised input, each convolution's weights and GELU output, pooled and
-upsampled activations, and the gradient of every convolution's
-pre-activation).  Used to check the GPU forward pass, the loss gradients and
+normalised input, each convolution's weights and GELU output except the
+last one, which feeds the FP32 head directly, pooled and upsampled
+activations, and the gradient of every convolution's pre-activation).  Used to check the GPU forward pass, the loss gradients and
 the Adam update (Kingma & Ba 2015).
 
 Parameter vector layout (shared with libff): per convolution W[27][cin][cout]
@@ -81,18 +81,20 @@ def forward(params, b, mask, p_prev, h, shape, requires_grad=False):
         tw.append((w, bb))
     head = head.clone().requires_grad_(requires_grad)
 
-    def conv(i, inp):
+    def conv(i, inp, store_bf16=True):
         w, bb = tw[i]
         wt = bf16(w).permute(4, 3, 0, 1, 2)   # [co][ci][dz][dy][dx]
         z = F.conv3d(inp, wt, padding=1) + bb.view(1, -1, 1, 1, 1)
         z = _RoundGrad.apply(z)
-        return bf16(F.gelu(z))
+        y = F.gelu(z)
+        return bf16(y) if store_bf16 else y
 
     e0 = conv(1, conv(0, x))
     e1 = conv(3, conv(2, bf16(F.avg_pool3d(e0, 2))))
     bt = conv(5, conv(4, bf16(F.avg_pool3d(e1, 2))))
     d1 = conv(7, conv(6, torch.cat([F.interpolate(bt, scale_factor=2, mode="nearest"), e1], 1)))
-    d0 = conv(9, conv(8, torch.cat([F.interpolate(d1, scale_factor=2, mode="nearest"), e0], 1)))
+    # the last convolution's output feeds the FP32 head without BF16 rounding
+    d0 = conv(9, conv(8, torch.cat([F.interpolate(d1, scale_factor=2, mode="nearest"), e0], 1)), store_bf16=False)
     raw = (d0 * head[:16].view(1, -1, 1, 1, 1)).sum(1)[0] + head[16]
     return raw, (sb, sp), tw, head
 

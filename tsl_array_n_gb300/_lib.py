@@ -81,6 +81,7 @@ PROTOTYPES = {
     "ff_field_upload_async": (_I, [_P, _P, _S]),
     "ff_field_download_async": (_I, [_P, _P, _S]),
     "ff_field_fill": (_I, [_P, C.c_float]),
+    "ff_field_copy": (_I, [_P, _P]),
     "ff_field_info": (_I, [_P, _IP, _IP, _IP, C.POINTER(C.c_int64)]),
     "ff_field_device_ptr": (_P, [_P]),
     "ff_pressure_desc_default": (None, [C.POINTER(PressureDesc), _IP, C.POINTER(C.c_double)]),
@@ -112,6 +113,7 @@ PROTOTYPES = {
     "ff_bc3_set_inflows": (_I, [_P, _I, _PP, C.POINTER(C.c_double), _IP]),
     "ff_bc3_constrain": (_I, [_P, _P, _P, _P, _I]),
     "ff_viscosity3_apply": (_I, [_P, _IP, C.POINTER(C.c_double), _P, _P, _P, _D, _D, _P, _P, _P]),
+    "ff_velocity3_add_force": (_I, [_P, _IP, _P, _P, _P, _D, _D, _D, _D]),
     "ff_flip_desc_default": (None, [C.POINTER(FlipDesc), _IP, C.POINTER(C.c_double), _I, _D]),
     "ff_flip3_create": (_I, [_P, C.POINTER(FlipDesc), _P, _P, _P, _PP]),
     "ff_flip3_destroy": (_I, [_P]),

@@ -176,6 +176,14 @@ extern "C" int ff_field_download_async(ff_field f, void *host, size_t bytes) {
     return FF_OK;
 }
 
+extern "C" int ff_field_copy(ff_field dst, ff_field src) {
+    FF_CHECK(dst && src, FF_E_ARG, "ff_field_copy: NULL field");
+    FF_CHECK(dst->bytes == src->bytes && dst->dtype == src->dtype, FF_E_ARG,
+             "ff_field_copy: fields differ in type or size");
+    FF_CUDA(cudaMemcpyAsync(dst->d, src->d, dst->bytes, cudaMemcpyDeviceToDevice, dst->ctx->stream));
+    return FF_OK;
+}
+
 extern "C" int ff_field_fill(ff_field f, float value) {
     FF_CHECK(f, FF_E_ARG, "ff_field_fill: NULL field");
     if (f->dtype == FF_FLOAT || f->dtype == FF_VEC3) {

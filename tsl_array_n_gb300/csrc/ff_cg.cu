@@ -120,6 +120,11 @@ __global__ void k_setup_residual(Dims d, const float4 *__restrict__ coef,
             st->bb = tot[1];
             double nb = sqrt(fabs(tot[1]));
             st->thr = st->relative ? fmax(st->tol * nb, st->tol) : st->tol;
+            // the start already meets the tolerance (linalg.js:1695-1699)
+            if (sqrt(fabs(tot[0])) < st->thr) {
+                st->stop = FF_STOP_CONVERGED;
+                st->stop_iter = 0;
+            }
         }
     }
 }
@@ -254,9 +259,11 @@ __global__ void k_rz_beta(Dims d, const float *__restrict__ r, const ZT *__restr
                 // seedScalarsKernel (linalg.js:1259-1267)
                 st->rz_old = rz;
                 st->pap_baseline = fmax(fabs(st->rr), PAP_BASELINE_FLOOR);
-                st->stop = 0;
+                if (st->stop != FF_STOP_CONVERGED) {
+                    st->stop = 0;
+                    st->stop_iter = 0;
+                }
                 st->iter = 0;
-                st->stop_iter = 0;
                 st->first = 1;
                 st->best_rr = -1.0;
             } else {

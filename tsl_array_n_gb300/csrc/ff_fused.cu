@@ -303,9 +303,11 @@ __global__ void __launch_bounds__(NT, 4) k_sweep(SweepArgs a) {
                     // seedScalarsKernel (linalg.js:1259-1267)
                     st->rz_old = rz;
                     st->pap_baseline = fmax(fabs(st->rr), PAP_BASELINE_FLOOR);
-                    st->stop = 0;
+                    if (st->stop != FF_STOP_CONVERGED) {
+                        st->stop = 0;
+                        st->stop_iter = 0;
+                    }
                     st->iter = 0;
-                    st->stop_iter = 0;
                     st->first = 1;
                     st->best_rr = -1.0;
                 } else {
@@ -674,9 +676,11 @@ __global__ void __launch_bounds__(tq::NT, 3)
                     // seedScalarsKernel (linalg.js:1259-1267)
                     st->rz_old = rz;
                     st->pap_baseline = fmax(fabs(st->rr), PAP_BASELINE_FLOOR);
-                    st->stop = 0;
+                    if (st->stop != FF_STOP_CONVERGED) {
+                        st->stop = 0;
+                        st->stop_iter = 0;
+                    }
                     st->iter = 0;
-                    st->stop_iter = 0;
                     st->first = 1;
                     st->best_rr = -1.0;
                 } else {
@@ -992,6 +996,11 @@ __global__ void __launch_bounds__(NT, 3) k_x_residual(CgArgs a) {
                 st->bb = tot[1];
                 double nb = sqrt(fabs(tot[1]));
                 st->thr = st->relative ? fmax(st->tol * nb, st->tol) : st->tol;
+                // the start already meets the tolerance (linalg.js:1695-1699)
+                if (sqrt(fabs(tot[0])) < st->thr) {
+                    st->stop = FF_STOP_CONVERGED;
+                    st->stop_iter = 0;
+                }
             }
         }
     } else {
@@ -1168,6 +1177,69 @@ __global__ void __launch_bounds__(NT, 4) k_res_restrict(RrArgs a) {
     cp_wait<0>();
 }
 
+// ------------------------------------------------------------ prolongation --
+// buildCorrectKernel (multigrid.js:990-1040) on FP32 levels with nx % 4 == 0:
+// x_f += P x_c, skipped on fine Dirichlet cells.  A thread owns an x-quad
+// of fine cells; along x the quad's four cells take (1/4, 3/4), (3/4, 1/4),
+// (1/4, 3/4), (3/4, 1/4) of the coarse cells 2q-1 .. 2q+2 (clamped), along
+// y and z the correctionTapsForAxis pair of its row and plane.
+__device__ __forceinline__ void ptaps2(int f, int nc, int *idx, float *w) {
+    const int ci = f >> 1;
+    if ((f & 1) == 0) {
+        idx[0] = ci > 0 ? ci - 1 : ci; w[0] = 0.25f;
+        idx[1] = ci; w[1] = 0.75f;
+    } else {
+        idx[0] = ci; w[0] = 0.75f;
+        idx[1] = ci < nc - 1 ? ci + 1 : ci; w[1] = 0.25f;
+    }
+}
+
+__global__ void k_prolong4(Dims fd, Dims cd, int dims, const float *__restrict__ coarse,
+                           const uint8_t *__restrict__ fmask, float *__restrict__ fine, const PcgState *st) {
+    if (st && st->stop) return;
+    const int nq = fd.nx >> 2;
+    const long long n = (long long)nq * fd.ny * fd.nz;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int qx = (int)(q % nq);
+        const long long r = q / nq;
+        const int j = (int)(r % fd.ny), k = (int)(r / fd.ny);
+        const int c1 = 2 * qx, c2 = 2 * qx + 1;
+        const int c0 = c1 > 0 ? c1 - 1 : c1, c3 = c2 < cd.nx - 1 ? c2 + 1 : c2;
+        int jj[2], kk[2];
+        float wj[2], wk[2];
+        ptaps2(j, cd.ny, jj, wj);
+        int nk = 2;
+        if (dims == 3) ptaps2(k, cd.nz, kk, wk);
+        else { kk[0] = 0; wk[0] = 1.f; nk = 1; }
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+        for (int b = 0; b < 2; ++b)
+            for (int g = 0; g < nk; ++g) {
+                const float *row = coarse + (long long)cd.nx * (jj[b] + (long long)cd.ny * kk[g]);
+                const float w = wj[b] * wk[g];
+                const float v0 = __ldg(row + c0), v1 = __ldg(row + c1), v2 = __ldg(row + c2), v3 = __ldg(row + c3);
+                a0 += (0.25f * v0 + 0.75f * v1) * w;
+                a1 += (0.75f * v1 + 0.25f * v2) * w;
+                a2 += (0.25f * v1 + 0.75f * v2) * w;
+                a3 += (0.75f * v2 + 0.25f * v3) * w;
+            }
+        const long long f0 = 4LL * q;   // fine cell index of the quad's first cell
+        float4 x = *reinterpret_cast<const float4 *>(fine + f0);
+        if (fmask) {
+            const uchar4 m = *reinterpret_cast<const uchar4 *>(fmask + f0);
+            if (!m.x) x.x += a0;
+            if (!m.y) x.y += a1;
+            if (!m.z) x.z += a2;
+            if (!m.w) x.w += a3;
+        } else {
+            x.x += a0;
+            x.y += a1;
+            x.z += a2;
+            x.w += a3;
+        }
+        *reinterpret_cast<float4 *>(fine + f0) = x;
+    }
+}
+
 // ----------------------------------------------------------- cell classes --
 // Two bits per cell, one byte per x-quad (rows `pitch` bytes apart): 0 an
 // interior cell whose six couplings are the plain h^-2 and E = 0; 1 a
@@ -1302,6 +1374,14 @@ int sweep(const Level &L, const uint8_t *bricks, const float *x_in, float *x_out
         else k_sweep<false, false><<<grid, block, smem, s>>>(a);
     }
     return post("sweep");
+}
+
+int prolong4(const Level &c, const Level &f, int dims, float *fine_x, const PcgState *st, cudaStream_t s) {
+    FF_CHECK(f.d.nx % 4 == 0, FF_E_ARG, "prolong4 needs nx %% 4 == 0");
+    const long long n = (long long)(f.d.nx / 4) * f.d.ny * f.d.nz;
+    const int nb = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
+    k_prolong4<<<nb, 256, 0, s>>>(f.d, c.d, dims, (const float *)c.x, f.mask, fine_x, st);
+    return post("prolong4");
 }
 
 // ---- TMA sweep

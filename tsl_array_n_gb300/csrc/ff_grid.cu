@@ -546,6 +546,32 @@ extern "C" int ff_bc3_constrain(ff_bc b, ff_field u, ff_field v, ff_field w, int
     return post("constrainVelocity");
 }
 
+// ------------------------------------------------------------ forces --
+namespace {
+__global__ void k_add_const(long long n, float *__restrict__ d, float fdt) {
+    for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < n; f += (long long)gridDim.x * blockDim.x)
+        d[f] = d[f] + fdt;
+}
+}  // namespace
+
+// createExternalForceSolver3 (external_force_solver3.js:7-29) with a
+// uniform force: u += f.x dt on every face of each component
+extern "C" int ff_velocity3_add_force(ff_ctx ctx, const int *res, ff_field u, ff_field v, ff_field w, double fx,
+                                      double fy, double fz, double dt) {
+    FF_CHECK(ctx && res, FF_E_ARG, "ff_velocity3_add_force: NULL argument");
+    const double unit[3] = {1.0, 1.0, 1.0};   // spacing does not enter
+    const G3 g = geom_of(res, unit, nullptr);
+    ff_field fs[3] = {u, v, w};
+    const float fdt[3] = {(float)fx * (float)dt, (float)fy * (float)dt, (float)fz * (float)dt};
+    cudaSetDevice(ctx->device);
+    for (int a = 0; a < 3; ++a) {
+        FF_CHECK(field_is(fs[a], comp_count(g, a)), FF_E_ARG, "add_force: component %d shape", a);
+        k_add_const<<<launch_blocks(comp_count(g, a)), 256, 0, ctx->stream>>>(comp_count(g, a), (float *)fs[a]->d,
+                                                                             fdt[a]);
+    }
+    return post("add_force");
+}
+
 // -------------------------------------------------------------- viscosity --
 extern "C" int ff_viscosity3_apply(ff_ctx ctx, const int *res, const double *h, ff_field u, ff_field v, ff_field w,
                                    double nu, double dt, ff_field uo, ff_field vo, ff_field wo) {

@@ -181,6 +181,8 @@ int sweep(const Level &L, const uint8_t *bricks, const float *x_in, float *x_out
           int sm_count, cudaStream_t s);
 // TMA-staged sweep (levels with nx % 4 == 0 and nx >= 32): x_in is the
 // buffer maps.xp[in] (in < 0: x_in identically zero), x_out the other one
+// x_f += P x_c on an FP32 level with nx % 4 == 0 (one thread per x-quad)
+int prolong4(const Level &c, const Level &f, int dims, float *fine_x, const PcgState *st, cudaStream_t s);
 bool sweep_tma_ok(const Dims &d);
 size_t sweep_tma_cls_bytes(const Dims &d);
 int sweep_tma_maps(const Level &L, const float *x0, const float *x1, uint8_t *cls, SweepMaps &m);

@@ -602,7 +602,7 @@ static int vcycle_fused(ff_pressure ps, int l, PcgState *st, int rz_mode, float 
         // x += P e (buildCorrectKernel, multigrid.js:990-1040)
         Level tmp = v;
         tmp.x = bufs[cur];
-        FF_TRY(ffk::mg_prolong(coarse, tmp, ps->dims, 0, 0, st, s));
+        FF_TRY(ffk::prolong4(coarse, tmp, ps->dims, bufs[cur], st, s));
     }
     for (int it = 0; it < up; ++it) {
         int nxt = 1 - cur;
@@ -1063,7 +1063,9 @@ extern "C" int ff_pressure3_profile(ff_pressure ps, int which, int reps, float *
             rc = ps->lv.size() > 1 ? ffk::mg_restrict(L0, ps->lv[1], ps->dims, vb, vb, 0, ps->st, s) : FF_OK;
             break;
         case FF_PROF_PROLONG:
-            rc = ps->lv.size() > 1 ? ffk::mg_prolong(ps->lv[1], L0, ps->dims, vb, 0, ps->st, s) : FF_OK;
+            if (ps->lv.size() > 1)
+                rc = nf ? ffk::mg_prolong(ps->lv[1], L0, ps->dims, vb, 0, ps->st, s)
+                        : ffk::prolong4(ps->lv[1], L0, ps->dims, (float *)L0.x, ps->st, s);
             break;
         case FF_PROF_RZ:
             rc = ffk::cg_rz_beta(d, ps->r, ps->z, 0, ps->st, ps->partials, 0, s);

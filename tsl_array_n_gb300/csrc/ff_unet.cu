@@ -322,12 +322,14 @@ __global__ void k_input(long long n, const float *__restrict__ b, const uint8_t 
     }
 }
 
-// 1x1x1 output layer (16 -> 1) in FP32: out = sp (w . y + b)
-__global__ void k_head(long long n, const bf16 *__restrict__ Yin, const float *__restrict__ w,
+// 1x1x1 output layer (16 -> 1) in FP32 on the last convolution's FP32
+// pre-activations (no BF16 rounding reaches the guess, whose grid-scale
+// noise the Laplacian would amplify): out = sp (w . gelu(z) + b)
+__global__ void k_head(long long n, const float *__restrict__ Zin, const float *__restrict__ w,
                        const float *__restrict__ scales, float *__restrict__ out, float *__restrict__ raw) {
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
         float s = w[16];
-        for (int c = 0; c < 16; ++c) s += __bfloat162float(Yin[v * 16 + c]) * w[c];
+        for (int c = 0; c < 16; ++c) s += gelu(Zin[v * 16 + c]) * w[c];
         if (raw) raw[v] = s;
         if (out) out[v] = s * scales[1];
     }
@@ -353,7 +355,7 @@ __global__ void k_loss(long long n, const float *__restrict__ raw, const float *
     if (threadIdx.x == 0) partial[blockIdx.x] = sred[0] / (double)n;
 }
 // head backward: dY[v, c] = draw[v] w[c]; dw[c] += sum draw y; db += sum draw
-__global__ void k_head_grad(long long n, const bf16 *__restrict__ Yin, const float *__restrict__ w,
+__global__ void k_head_grad(long long n, const float *__restrict__ Zin, const float *__restrict__ w,
                             const float *__restrict__ draw, float *__restrict__ dY, float *__restrict__ dw) {
     __shared__ float sw[17];
     if (threadIdx.x < 17) sw[threadIdx.x] = 0.f;
@@ -363,7 +365,7 @@ __global__ void k_head_grad(long long n, const bf16 *__restrict__ Yin, const flo
         const float g = draw[v];
         for (int c = 0; c < 16; ++c) {
             dY[v * 16 + c] = g * w[c];
-            lw[c] += g * __bfloat162float(Yin[v * 16 + c]);
+            lw[c] += g * gelu(Zin[v * 16 + c]);
         }
         lw[16] += g;
     }
@@ -689,7 +691,7 @@ static int forward(ff_unet u, const float *b, const uint8_t *mask, const float *
     k_up_concat<<<gblocks(n0 * 48), 256, 0, s>>>(level_vol(u, 0), 32, 16, u->act[11], u->act[2], u->act[12]);
     FF_TRY(conv(8));
     FF_TRY(conv(9));
-    k_head<<<gblocks(n0), 256, 0, s>>>(n0, u->act[14], u->w + u->head_off, u->scales, out, u->raw);
+    k_head<<<gblocks(n0), 256, 0, s>>>(n0, u->pre[9], u->w + u->head_off, u->scales, out, u->raw);
     return post("unet forward");
 }
 
@@ -727,7 +729,7 @@ static int conv_backward(ff_unet u, int l, bool accumulate_input) {
 static int backward(ff_unet u) {
     cudaStream_t s = u->ctx->stream;
     const long long n0 = u->vol.n();
-    k_head_grad<<<std::min(gblocks(n0), 1024), 256, 0, s>>>(n0, u->act[14], u->w + u->head_off, u->draw, u->grad[14],
+    k_head_grad<<<std::min(gblocks(n0), 1024), 256, 0, s>>>(n0, u->pre[9], u->w + u->head_off, u->draw, u->grad[14],
                                                              u->g + u->head_off);
     FF_TRY(post("head grad"));
     FF_TRY(conv_backward(u, 9, false));   // grad[13]

@@ -13,6 +13,7 @@ Names, option names, defaults and error behaviour follow the reference
   create_grid_blocked_boundary_condition_solver3
                                   grid_blocked_boundary_condition_solver3.js:48-490
   apply_viscosity3                explicit viscosity (no reference counterpart)
+  create_grid_solver3             grid_solver3.js:24-149 (forces, viscosity, projection, advection)
   create_grid_flip_solver3        grid_flip_solver3.js:135-1157 (no resampling)
   compute_flip_box_seed3          grid_flip_solver3.js:70-130
   create_jitter_random            jitter_random.js:29-46
@@ -690,3 +691,68 @@ class GridFlipSolver3:
 
 def create_grid_flip_solver3(**options):
     return GridFlipSolver3(**options)
+
+
+# ---------------------------------------------------------------- solver --
+class GridSolver3:
+    """createGridSolver3({velocityGrid, gridSpacing, origin, force, dirichlet,
+    collider, inflows, closedDomainBoundaryFlag, dt, advection, pressure})
+    (grid_solver3.js:24-149) with a uniform force vector and an explicit
+    viscosity `nu` (the reference's computeViscosity is a no-op, :104; nu = 0
+    keeps it so).  onAdvanceTimeStep runs external forces, viscosity, the
+    projection and the advection, each followed by constrainVelocity, as
+    the reference's default stages do (:112-140)."""
+
+    def __init__(self, velocity_grid=None, force=None, dirichlet=None, collider=None, inflows=None,
+                 closed_domain_boundary_flag=None, dt=None, advection=None, pressure=None, nu=0.0):
+        if velocity_grid is None:
+            raise ValueError("createGridSolver3: options.velocityGrid is required.")
+        g = velocity_grid
+        self.velocity_grid, self.dt, self.nu = g, dt, float(nu)
+        self.force = tuple(float(x) for x in force) if force is not None else None
+        pressure = dict(pressure or {})
+        cw = pressure.pop("collider_weights", None)
+        if collider is not None and cw is None:
+            cw = collider.compute_face_weights(g.resolution, g.grid_spacing, g.origin)
+        self.collider_face_weights = cw
+        self.boundary_solver = GridBlockedBoundaryConditionSolver3(g, g.resolution, g.grid_spacing, g.origin,
+                                                                   collider, inflows, cw)
+        if closed_domain_boundary_flag is not None:
+            self.boundary_solver.closed_domain_boundary_flag = closed_domain_boundary_flag
+        self.velocity_prev = FaceCenteredGrid3(g.resolution, g.grid_spacing, g.origin)
+        self._scratch = FaceCenteredGrid3(g.resolution, g.grid_spacing, g.origin)
+        self.pressure_solver = create_grid_pressure_solver3(g.resolution, g.grid_spacing, g.origin,
+                                                            dirichlet=dirichlet, collider_weights=cw, **pressure)
+        self._project = self.pressure_solver.project(g, g)
+        adv = dict(advection or {})
+        self.advection_solver = SemiLagrangianAdvectionSolver3(self.velocity_prev, collider, dt, **adv)
+        self._advect = self.advection_solver.advect_face_centered3(self.velocity_prev, g)
+        self.pressure = self.pressure_solver.pressure
+
+    def _copy(self, dst, src):
+        lib = _lib.load()
+        for a, b in ((dst.data_u, src.data_u), (dst.data_v, src.data_v), (dst.data_w, src.data_w)):
+            _lib.check(lib.ff_field_copy(a.handle, b.handle))
+
+    def on_advance_time_step(self, time_step_in_seconds=None):
+        dt = float(self.dt if time_step_in_seconds is None else time_step_in_seconds)
+        g = self.velocity_grid
+        lib = _lib.load()
+        if self.force is not None:
+            _lib.check(lib.ff_velocity3_add_force(context().handle, (C.c_int * 3)(*g.resolution), g.data_u.handle,
+                                                  g.data_v.handle, g.data_w.handle, *self.force, dt))
+            self.boundary_solver.constrain_velocity()
+        if self.nu > 0:
+            apply_viscosity3(g, self._scratch, self.nu, dt)
+            self._copy(g, self._scratch)
+        diag = self._project()
+        self.boundary_solver.constrain_velocity()
+        self._copy(self.velocity_prev, g)
+        self.advection_solver.set_dt(dt)
+        self._advect()
+        self.boundary_solver.constrain_velocity()
+        return diag
+
+
+def create_grid_solver3(**options):
+    return GridSolver3(**options)
