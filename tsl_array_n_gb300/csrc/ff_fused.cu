@@ -1177,6 +1177,124 @@ __global__ void __launch_bounds__(NT, 4) k_res_restrict(RrArgs a) {
     cp_wait<0>();
 }
 
+// --------------------------------------------- residual and restriction --
+// buildResidualKernel (multigrid.js:741-749) + buildRestrictKernel
+// (:866-914) as two streaming passes on levels with cell classes:
+//  k_resid_rx: r = b - A x per cell (class dispatch as the sweep; zero on a
+//   Dirichlet cell), then the x-direction restriction taps (1/8, 3/8, 3/8,
+//   1/8 at fine 2I-1 .. 2I+2, clamped) into rx (nx/2 x ny x nz);
+//  k_restrict_yz: the y and z taps of rx into the coarse b, zero on coarse
+//   Dirichlet cells.
+__device__ __forceinline__ float resid_cls(const Geo &g, const float4 *coef, unsigned cls, int i, int j, int k,
+                                           float bval, float vc, float xm, float xp, float ym, float yp, float zm,
+                                           float zp) {
+    if (cls == 0) return bval - apply_reg(g, vc, xm, xp, ym, yp, zm, zp);
+    if (cls == 1) return 0.0f;   // Dirichlet cell (the fine-mask zero)
+    const long long c = i + g.sy * j + g.sz * k;
+    Coef q = coef_at(g, coef, cls == 2, i, j, k, c);
+    return bval - apply_q(q, vc, xm, xp, ym, yp, zm, zp);
+}
+
+// residual of the fine cell i of row `row` with scalar loads (used for the
+// cells next to a quad that another warp owns)
+__device__ __forceinline__ float resid_scalar(const Geo &g, const float *__restrict__ x, const float *__restrict__ b,
+                                              const float4 *__restrict__ coef, const uint8_t *crow, long long row,
+                                              long long rym, long long ryp, long long rzm, long long rzp, int i, int j,
+                                              int k) {
+    const unsigned cb = (crow[i >> 2] >> (2 * (i & 3))) & 3u;
+    const float xm = __ldg(x + row + (i > 0 ? i - 1 : i));
+    const float xp = __ldg(x + row + (i < g.d.nx - 1 ? i + 1 : i));
+    return resid_cls(g, coef, cb, i, j, k, __ldg(b + row + i), __ldg(x + row + i), xm, xp, __ldg(x + rym + i),
+                     __ldg(x + ryp + i), __ldg(x + rzm + i), __ldg(x + rzp + i));
+}
+
+// One thread per fine x-quad: float4 loads of the quad's row, its y and z
+// neighbours and b; the residual at the cells just outside the quad comes
+// from the neighbouring lanes (same row), computed directly at warp edges.
+__global__ void __launch_bounds__(256) k_resid_rx(Geo g, const float *__restrict__ x, const float *__restrict__ b,
+                                                  const float4 *__restrict__ coef, const uint8_t *__restrict__ cls,
+                                                  int cpitch, float *__restrict__ rx, const PcgState *st) {
+    if (st && st->stop) return;
+    const int nq = g.d.nx >> 2, cnx = g.d.nx >> 1;
+    const long long n = (long long)nq * g.d.ny * g.d.nz;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const bool valid = t < n;
+    const long long tt = valid ? t : n - 1;
+    const int qx = (int)(tt % nq);
+    const long long rr = tt / nq;
+    const int j = (int)(rr % g.d.ny), k = (int)(rr / g.d.ny);
+    const int i0 = 4 * qx;
+    const long long row = g.sy * j + g.sz * k;
+    const long long rym = row + (j > 0 ? -g.sy : 0), ryp = row + (j < g.d.ny - 1 ? g.sy : 0);
+    const long long rzm = row + (k > 0 ? -g.sz : 0), rzp = row + (k < g.d.nz - 1 ? g.sz : 0);
+    const uint8_t *crow = cls + (long long)cpitch * (j + (long long)g.d.ny * k);
+    const float4 c = __ldg(reinterpret_cast<const float4 *>(x + row + i0));
+    const float xl = i0 > 0 ? __ldg(x + row + i0 - 1) : c.x;
+    const float xr = i0 + 4 < g.d.nx ? __ldg(x + row + i0 + 4) : c.w;
+    const float4 ym = __ldg(reinterpret_cast<const float4 *>(x + rym + i0));
+    const float4 yp = __ldg(reinterpret_cast<const float4 *>(x + ryp + i0));
+    const float4 zm = __ldg(reinterpret_cast<const float4 *>(x + rzm + i0));
+    const float4 zp = __ldg(reinterpret_cast<const float4 *>(x + rzp + i0));
+    const float4 bq = __ldg(reinterpret_cast<const float4 *>(b + row + i0));
+    const unsigned cq = crow[qx];
+    float r0, r1, r2, r3;
+    if (cq == 0) {
+        r0 = bq.x - apply_reg(g, c.x, xl, c.y, ym.x, yp.x, zm.x, zp.x);
+        r1 = bq.y - apply_reg(g, c.y, c.x, c.z, ym.y, yp.y, zm.y, zp.y);
+        r2 = bq.z - apply_reg(g, c.z, c.y, c.w, ym.z, yp.z, zm.z, zp.z);
+        r3 = bq.w - apply_reg(g, c.w, c.z, xr, ym.w, yp.w, zm.w, zp.w);
+    } else {
+        r0 = resid_cls(g, coef, cq & 3u, i0, j, k, bq.x, c.x, xl, c.y, ym.x, yp.x, zm.x, zp.x);
+        r1 = resid_cls(g, coef, (cq >> 2) & 3u, i0 + 1, j, k, bq.y, c.y, c.x, c.z, ym.y, yp.y, zm.y, zp.y);
+        r2 = resid_cls(g, coef, (cq >> 4) & 3u, i0 + 2, j, k, bq.z, c.z, c.y, c.w, ym.z, yp.z, zm.z, zp.z);
+        r3 = resid_cls(g, coef, (cq >> 6) & 3u, i0 + 3, j, k, bq.w, c.w, c.z, xr, ym.w, yp.w, zm.w, zp.w);
+    }
+    // r at i0-1 (left neighbour's r3) and i0+4 (right neighbour's r0)
+    const int lane = threadIdx.x & 31;
+    float rl = __shfl_up_sync(0xffffffffu, r3, 1);
+    float rh = __shfl_down_sync(0xffffffffu, r0, 1);
+    if (!valid) return;
+    if (qx == 0) rl = r0;                                   // fine 2I-1 clamps to 2I at I = 0
+    else if (lane == 0) rl = resid_scalar(g, x, b, coef, crow, row, rym, ryp, rzm, rzp, i0 - 1, j, k);
+    if (2 * qx + 1 >= cnx - 1) rh = r3;                     // fine 2I+2 clamps to 2I+1 at the end
+    else if (lane == 31) rh = resid_scalar(g, x, b, coef, crow, row, rym, ryp, rzm, rzp, i0 + 4, j, k);
+    float2 out;
+    out.x = 0.125f * rl + 0.375f * r0 + 0.375f * r1 + 0.125f * r2;
+    out.y = 0.125f * r1 + 0.375f * r2 + 0.375f * r3 + 0.125f * rh;
+    *reinterpret_cast<float2 *>(rx + (long long)cnx * (j + (long long)g.d.ny * k) + 2 * qx) = out;
+}
+
+__global__ void k_restrict_yz(Dims fd, Dims cd, int dims, const float *__restrict__ rx,
+                              const uint8_t *__restrict__ cmask, float *__restrict__ cb, const PcgState *st) {
+    if (st && st->stop) return;
+    const long long n = cd.n();
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        const int I = (int)(c % cd.nx);
+        const long long rr = c / cd.nx;
+        const int J = (int)(rr % cd.ny), K = (int)(rr / cd.ny);
+        if (cmask && cmask[c]) {
+            cb[c] = 0.0f;
+            continue;
+        }
+        int jy[4], kz[4];
+        rtap4(J, cd.ny, jy);
+        const float w4[4] = {0.125f, 0.375f, 0.375f, 0.125f};
+        int nzt = 4;
+        if (dims == 3) rtap4(K, cd.nz, kz);
+        else { kz[0] = K; nzt = 1; }
+        float s = 0.0f;
+        for (int q = 0; q < nzt; ++q) {
+            const float wz = dims == 3 ? w4[q] : 1.0f;
+            float part = 0.0f;
+#pragma unroll
+            for (int p = 0; p < 4; ++p)
+                part += __ldg(rx + I + (long long)cd.nx * (jy[p] + (long long)fd.ny * kz[q])) * w4[p];
+            s += part * wz;
+        }
+        cb[c] = s;
+    }
+}
+
 // ------------------------------------------------------------ prolongation --
 // buildCorrectKernel (multigrid.js:990-1040) on FP32 levels with nx % 4 == 0:
 // x_f += P x_c, skipped on fine Dirichlet cells.  A thread owns an x-quad
@@ -1374,6 +1492,19 @@ int sweep(const Level &L, const uint8_t *bricks, const float *x_in, float *x_out
         else k_sweep<false, false><<<grid, block, smem, s>>>(a);
     }
     return post("sweep");
+}
+
+int res_restrict2(const Level &f, const SweepMaps &m, const float *x, float *rx, Level &c, int dims,
+                  const PcgState *st, cudaStream_t s) {
+    FF_CHECK(m.ok && m.cls_ptr && f.d.nx % 4 == 0, FF_E_STATE, "res_restrict2 needs cell classes and nx %% 4 == 0");
+    Geo g = make_geo(f);
+    const long long nq = (long long)(f.d.nx / 4) * f.d.ny * f.d.nz;
+    k_resid_rx<<<(int)((nq + 255) / 256), 256, 0, s>>>(g, x, (const float *)f.b, f.coef, m.cls_ptr, m.cls_pitch, rx,
+                                                         st);
+    const long long nc = c.d.n();
+    k_restrict_yz<<<(int)std::min<long long>((nc + 255) / 256, 152LL * 16), 256, 0, s>>>(f.d, c.d, dims, rx, c.mask,
+                                                                                          (float *)c.b, st);
+    return post("res_restrict2");
 }
 
 int prolong4(const Level &c, const Level &f, int dims, float *fine_x, const PcgState *st, cudaStream_t s) {

@@ -181,6 +181,10 @@ int sweep(const Level &L, const uint8_t *bricks, const float *x_in, float *x_out
           int sm_count, cudaStream_t s);
 // TMA-staged sweep (levels with nx % 4 == 0 and nx >= 32): x_in is the
 // buffer maps.xp[in] (in < 0: x_in identically zero), x_out the other one
+// residual r = b - A x and its restriction into the coarse b in two
+// streaming passes through rx (nx/2 x ny x nz floats); needs cell classes
+int res_restrict2(const Level &f, const SweepMaps &m, const float *x, float *rx, Level &c, int dims,
+                  const PcgState *st, cudaStream_t s);
 // x_f += P x_c on an FP32 level with nx % 4 == 0 (one thread per x-quad)
 int prolong4(const Level &c, const Level &f, int dims, float *fine_x, const PcgState *st, cudaStream_t s);
 bool sweep_tma_ok(const Dims &d);

@@ -589,7 +589,10 @@ static int vcycle_fused(ff_pressure ps, int l, PcgState *st, int rz_mode, float 
     }
     // residual and restriction into the coarse b, fused (the fine residual
     // never reaches memory)
-    FF_TRY(ffk::res_restrict(v, ps->bricks[l], bufs[cur], c, ps->dims, st, ps->ctx->sm_count, s));
+    if (ps->use_tma && ps->smaps && ps->smaps[l].ok && v.buf)
+        FF_TRY(ffk::res_restrict2(v, ps->smaps[l], bufs[cur], (float *)v.buf, c, ps->dims, st, s));
+    else
+        FF_TRY(ffk::res_restrict(v, ps->bricks[l], bufs[cur], c, ps->dims, st, ps->ctx->sm_count, s));
     float *coarse_x = nullptr;
     bool dummy;
     FF_TRY(vcycle_fused(ps, l + 1, st, 0, &coarse_x, &dummy));
@@ -1055,6 +1058,9 @@ extern "C" int ff_pressure3_profile(ff_pressure ps, int which, int reps, float *
         case FF_PROF_RESIDUAL:
             // fused path: residual + restriction in one kernel
             if (nf) rc = ffk::mg_residual(L0, ps->dims, 0, 0, vb, vb, ps->st, s);
+            else if (ps->lv.size() > 1 && ps->use_tma && ps->smaps && ps->smaps[0].ok && L0.buf)
+                rc = ffk::res_restrict2(L0, ps->smaps[0], (const float *)L0.x, (float *)L0.buf, ps->lv[1], ps->dims,
+                                        ps->st, s);
             else if (ps->lv.size() > 1)
                 rc = ffk::res_restrict(L0, ps->bricks[0], (const float *)L0.x, ps->lv[1], ps->dims, ps->st,
                                        ps->ctx->sm_count, s);
