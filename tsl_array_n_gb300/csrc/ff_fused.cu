@@ -339,7 +339,11 @@ __global__ void __launch_bounds__(NT, 4) k_sweep(SweepArgs a) {
 // columns i0-4 .. i0+67, come into shared-memory rings through
 // cp.async.bulk.tensor copies issued by one thread, completing on one
 // mbarrier per stage; the tensor map zero-fills everything outside the
-// domain.  Each thread owns an x-quad; a warp holds two rows of the same
+// domain.  Each thread owns an x-quad and keeps it in registers for planes
+// m-1..m+3 as the wavefront marches in z: z-neighbours come from registers,
+// x-neighbours from the next lane by shuffle (the tile's edge columns from
+// shared memory), y-neighbours from shared memory, where each thread leaves
+// its quad after the first colour.  A warp holds two rows of the same
 // parity, so the colour offset inside a quad is uniform across the warp.
 // Waits are bounded in time: a block that gives up records bit 0 of
 // PcgState::err and stops (the host then reports the solve as failed).
@@ -348,7 +352,7 @@ constexpr int TX = 64, TY = 16, QX = TX / 4, NT = QX * TY;   // 16 x 16 threads
 constexpr int RW = TX + 8;                  // staged columns i0-4 .. i0+TX+3
 constexpr int XR = TY + 4, BR = TY + 2;     // staged rows of x and of b
 constexpr int SD = 3;                       // stages in flight
-constexpr int XS = SD + 4, BS = SD + 2;     // ring slots: x planes m-1..m+3+SD-1, b planes m..m+2+SD-1
+constexpr int XS = SD + 3, BS = SD;         // ring slots: x planes m..m+3+SD-1, b planes m+2..m+2+SD-1
 constexpr int XPL = XR * RW;                // 1440 floats, 45 x 128 B
 constexpr int BPL = ((BR * RW * 4 + 127) / 128) * 32;   // b slot padded to 128 B (1312 floats)
 constexpr unsigned XBYTES = XR * RW * 4, BBYTES = BR * RW * 4;
@@ -357,8 +361,8 @@ constexpr int CW = 48, CR = TY + 2;         // staged class bytes: quads i0/4-16
 constexpr int CPL = ((CW * CR + 127) / 128) * 128;      // class slot padded to 128 B (896)
 constexpr unsigned CBYTES = CW * CR;
 constexpr int MAXZC = 256;                  // planes per block
-constexpr size_t SMEM = 128 + sizeof(float) * ((size_t)XS * XPL + (size_t)BS * BPL) + (size_t)BS * CPL + 8 * SD;
-static_assert(RING <= NT, "one ring cell per thread");
+constexpr int CS = SD + 1;                  // class slots: plane k0-1, then planes m+3..m+3+SD-1
+constexpr size_t SMEM = 128 + sizeof(float) * ((size_t)XS * XPL + (size_t)BS * BPL) + (size_t)CS * CPL + 8 * SD;
 static_assert((XPL * 4) % 128 == 0 && (BPL * 4) % 128 == 0, "TMA destinations stay 128-byte aligned");
 }  // namespace tq
 
@@ -367,7 +371,8 @@ struct TqArgs {
     float *x_out;
     const float4 *coef;
     const uint8_t *bricks;
-    float sor, rdreg_sor;
+    const float4 *gco;             // class-3 upper couplings and 1 / diagonal
+    float sor, rdreg_sor, omsor;   // sor, sor / dreg, 1 - sor
     int colour_a, zc;
     PcgState *st;
     double *partials;
@@ -417,76 +422,106 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-// One relaxation with coefficients from memory (cells next to a solid, a
-// Dirichlet cell or the domain edge).
-__device__ __forceinline__ float relax_general(const float4 *coef, float h2x, float h2y, float h2z, int nx, int ny,
-                                            int nz, long long sy, long long sz, bool reg, float sor, int i, int j,
-                                            int k, float vc, float xm, float xp, float ym, float yp, float zm,
-                                            float zp, float bval) {
-    Geo g;
-    g.d = Dims{nx, ny, nz};
-    g.h2x = h2x;
-    g.h2y = h2y;
-    g.h2z = h2z;
-    g.sy = sy;
-    g.sz = sz;
-    const long long c = i + sy * j + sz * k;
-    Coef q = coef_at(g, coef, reg, i, j, k, c);
-    return vc + ((bval - apply_q(q, vc, xm, xp, ym, yp, zm, zp)) / diag_q(q)) * sor;
+// One relaxation of a cell with the plain couplings (class 0 or 2).  With
+// S the h^-2-weighted sum of the six neighbours (the tensor maps zero-fill
+// those across the domain edge, which drops the absent faces from S) and
+// d = dreg + corr the cell's diagonal (corr = h^-2 summed over the absent
+// faces), the row is (A v) = S + d v and the relaxation
+// v + sor (b - A v) / d = (1 - sor) v + (b - S) rd, rd = sor / d.
+__device__ __forceinline__ float relax_plain(const Geo &g, float omsor, float vc, float xm, float xp, float ym,
+                                             float yp, float zm, float zp, float bval, float rd) {
+    const float s = __fmaf_rn(g.h2z, zm + zp, __fmaf_rn(g.h2y, ym + yp, g.h2x * (xm + xp)));
+    return __fmaf_rn(bval - s, rd, omsor * vc);
 }
 
-// One relaxation by cell class (see SweepMaps): the short formula for an
-// interior cell with the plain coefficients, the closed form of a Dirichlet
-// row (A x = -x), or the coefficient form (plain values at the domain edge,
-// stored coefficients elsewhere).
-__device__ __forceinline__ float relax_cls(const Geo &g, const TqArgs &a, unsigned cls, int i, int j, int k,
-                                           float vc, float xm, float xp, float ym, float yp, float zm, float zp,
-                                           float bval) {
-    if (cls == 0) return __fmaf_rn(bval - apply_reg(g, vc, xm, xp, ym, yp, zm, zp), a.rdreg_sor, vc);
-    if (cls == 1) return vc - (bval + vc) * a.sor;
-    return relax_general(a.coef, g.h2x, g.h2y, g.h2z, g.d.nx, g.d.ny, g.d.nz, g.sy, g.sz, cls == 2, a.sor, i, j, k,
-                         vc, xm, xp, ym, yp, zm, zp, bval);
+// One relaxation by cell class (see SweepMaps), all in the form
+// (1 - sor) v + (b - S) rd with S the coupling-weighted neighbour sum:
+// classes 0 and 2 with the plain couplings (rd given), class 1 (a Dirichlet
+// row, A x = -x) with no coupling and rd = -sor, class 3 with its stored
+// couplings (lower faces from coef, upper faces and 1 / diagonal from gco).
+// Neighbours across the domain edge are zero-filled, so the lower-face
+// couplings need no masking there.
+__device__ __forceinline__ float relax_any(const Geo &g, const TqArgs &a, unsigned cls, long long c, float vc,
+                                           float xm, float xp, float ym, float yp, float zm, float zp, float bval,
+                                           float rd) {
+    float kx = g.h2x, ux = g.h2x, ky = g.h2y, uy = g.h2y, kz = g.h2z, uz = g.h2z;
+    if (cls == 1u) {
+        kx = ux = ky = uy = kz = uz = 0.f;
+        rd = -a.sor;
+    } else if (cls == 3u) {
+        const float4 lo = __ldg(a.coef + c), hi = __ldg(a.gco + c);
+        kx = lo.x;
+        ky = lo.y;
+        kz = lo.z;
+        ux = hi.x;
+        uy = hi.y;
+        uz = hi.z;
+        rd = a.sor * hi.w;
+    }
+    float s = kx * xm;
+    s = __fmaf_rn(ux, xp, s);
+    s = __fmaf_rn(ky, ym, s);
+    s = __fmaf_rn(uy, yp, s);
+    s = __fmaf_rn(kz, zm, s);
+    s = __fmaf_rn(uz, zp, s);
+    return __fmaf_rn(bval - s, rd, a.omsor * vc);
 }
 
-// Relax the two cells of colour offset P (cells P and P+2) of the quad whose
-// first cell sits at offset o of plane X; Xm/Xp are the planes below and
-// above, B the b plane (offset bo), cq the quad's class byte.  Writes the
-// quad back and returns it.
+// sor over the diagonal of a plain cell whose absent faces sum to corr
+__device__ __forceinline__ float plain_scale(const Geo &g, const TqArgs &a, float corr) {
+    return corr == 0.f ? a.rdreg_sor : a.sor / (g.dreg + corr);
+}
+
+// Scales of a quad's plain cells on one plane: cells 0, 1-2 and 3 differ
+// only in the x faces.
+struct QuadScale {
+    float r0, r12, r3;
+};
+__device__ __forceinline__ QuadScale quad_scale(const Geo &g, const TqArgs &a, float cy, float cx0, float cx3,
+                                                float cz) {
+    QuadScale q;
+    q.r0 = plain_scale(g, a, cy + cx0 + cz);
+    q.r12 = plain_scale(g, a, cy + cz);
+    q.r3 = plain_scale(g, a, cy + cx3 + cz);
+    return q;
+}
+
+// Relax the two cells of colour offset P (cells P and P+2) of quad q in
+// registers: s is the x-neighbour outside the quad (cell -1 for P = 0, cell
+// 4 for P = 1), ym/yp/zm/zp the neighbouring quads, bq the right-hand side,
+// cq the class byte.
 template <int P>
-__device__ __forceinline__ float4 relax_quad(const Geo &g, const TqArgs &a, float *X, const float *Xm,
-                                             const float *Xp, const float *B, int o, int bo, unsigned cq, int gi,
-                                             int gj, int k, float4 &bq) {
-    float4 c = *reinterpret_cast<const float4 *>(X + o);
-    const float s = X[o + (P ? 4 : -1)];
-    const float4 ym = *reinterpret_cast<const float4 *>(X + o - tq::RW);
-    const float4 yp = *reinterpret_cast<const float4 *>(X + o + tq::RW);
-    const float4 zm = *reinterpret_cast<const float4 *>(Xm + o);
-    const float4 zp = *reinterpret_cast<const float4 *>(Xp + o);
-    bq = *reinterpret_cast<const float4 *>(B + bo);
-    const float v0 = P ? c.y : c.x, l0 = P ? c.x : s, r0 = P ? c.z : c.y;
-    const float v1 = P ? c.w : c.z, l1 = P ? c.z : c.y, r1 = P ? s : c.w;
+__device__ __forceinline__ void relax_pair(const Geo &g, const TqArgs &a, float4 &q, float s, const float4 &ym,
+                                           const float4 &yp, const float4 &zm, const float4 &zp, const float4 &bq,
+                                           unsigned cq, const QuadScale &e, int gi, int gj, int k) {
+    const float v0 = P ? q.y : q.x, l0 = P ? q.x : s, r0 = P ? q.z : q.y;
+    const float v1 = P ? q.w : q.z, l1 = P ? q.z : q.y, r1 = P ? s : q.w;
     const float ym0 = P ? ym.y : ym.x, ym1 = P ? ym.w : ym.z, yp0 = P ? yp.y : yp.x, yp1 = P ? yp.w : yp.z;
     const float zm0 = P ? zm.y : zm.x, zm1 = P ? zm.w : zm.z, zp0 = P ? zp.y : zp.x, zp1 = P ? zp.w : zp.z;
     const float b0 = P ? bq.y : bq.x, b1 = P ? bq.w : bq.z;
-    const unsigned c0 = (cq >> (2 * P)) & 3u, c1 = (cq >> (2 * P + 4)) & 3u;
+    const float ra = P ? e.r12 : e.r0, rb = P ? e.r3 : e.r12;
     float n0, n1;
-    if ((c0 | c1) == 0) {
-        n0 = __fmaf_rn(b0 - apply_reg(g, v0, l0, r0, ym0, yp0, zm0, zp0), a.rdreg_sor, v0);
-        n1 = __fmaf_rn(b1 - apply_reg(g, v1, l1, r1, ym1, yp1, zm1, zp1), a.rdreg_sor, v1);
+    if (!(cq & (0x11u << (2 * P)))) {
+        n0 = relax_plain(g, a.omsor, v0, l0, r0, ym0, yp0, zm0, zp0, b0, ra);
+        n1 = relax_plain(g, a.omsor, v1, l1, r1, ym1, yp1, zm1, zp1, b1, rb);
     } else {
-        n0 = relax_cls(g, a, c0, gi + P, gj, k, v0, l0, r0, ym0, yp0, zm0, zp0, b0);
-        n1 = relax_cls(g, a, c1, gi + P + 2, gj, k, v1, l1, r1, ym1, yp1, zm1, zp1, b1);
+        const long long c = gi + P + g.sy * gj + g.sz * k;
+        n0 = relax_any(g, a, (cq >> (2 * P)) & 3u, c, v0, l0, r0, ym0, yp0, zm0, zp0, b0, ra);
+        n1 = relax_any(g, a, (cq >> (2 * P + 4)) & 3u, c + 2, v1, l1, r1, ym1, yp1, zm1, zp1, b1, rb);
     }
     if (P) {
-        c.y = n0;
-        c.w = n1;
+        q.y = n0;
+        q.w = n1;
     } else {
-        c.x = n0;
-        c.z = n1;
+        q.x = n0;
+        q.z = n1;
     }
-    *reinterpret_cast<float4 *>(X + o) = c;
-    return c;
 }
+
+__device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+// any cell of class 3 among the four 2-bit fields of a class byte
+__device__ __forceinline__ bool any_general(unsigned c) { return (c & (c >> 1) & 0x55u) != 0; }
 
 template <bool FIRST, bool RZ>
 __global__ void __launch_bounds__(tq::NT, 3)
@@ -494,8 +529,9 @@ __global__ void __launch_bounds__(tq::NT, 3)
                 const __grid_constant__ CUtensorMap cmap) {
     constexpr int TX = tq::TX, TY = tq::TY, QX = tq::QX, RW = tq::RW, SD = tq::SD, XS = tq::XS, BS = tq::BS;
     constexpr int XPL = tq::XPL, BPL = tq::BPL, RING = tq::RING;
-    constexpr unsigned XBYTES = tq::XBYTES, BBYTES = tq::BBYTES + tq::CBYTES;
-    constexpr int CW = tq::CW, CPL = tq::CPL;
+    constexpr unsigned XBYTES = tq::XBYTES, BBYTES = tq::BBYTES, CBYTES = tq::CBYTES;
+    constexpr int CW = tq::CW, CPL = tq::CPL, CS = tq::CS;
+    constexpr unsigned FULL = 0xffffffffu;
     if (a.st && a.rz_mode != 2 && (a.st->stop || a.st->err)) return;
     extern __shared__ __align__(16) unsigned char dyn_raw[];
     // 128-byte alignment by pointer arithmetic on the shared array (keeps the
@@ -503,17 +539,18 @@ __global__ void __launch_bounds__(tq::NT, 3)
     float *xs = reinterpret_cast<float *>(dyn_raw + ((128u - (smem_u32(dyn_raw) & 127u)) & 127u));
     float *bs = xs + XS * XPL;
     uint8_t *cs = reinterpret_cast<uint8_t *>(bs + BS * BPL);
-    const unsigned bar0 = smem_u32(cs + BS * CPL);
+    const unsigned bar0 = smem_u32(cs + CS * CPL);
     const Geo &g = a.g;
     // warp w holds rows r and r+2 (same colour parity), r = 4(w/2) + w%2
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int qx = lane & (QX - 1), ty = 4 * (warp >> 1) + (warp & 1) + 2 * (lane >> 4);
-    // the TMA issuer is a thread of the last warp, which has no ring cells
-    constexpr int ISSUER = tq::NT - 32;
-    static_assert(ISSUER >= RING, "issuer warp carries no ring cell");
+    // the TMA issuer is the last thread, which has no ring cell
+    constexpr int ISSUER = tq::NT - 1;
+    static_assert(ISSUER >= RING, "issuer carries no ring cell");
     const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
     const int k0 = blockIdx.z * a.zc, k1 = min(k0 + a.zc, g.d.nz);
-    // steps k0-3 .. k1-1; step m's stage brings x(m+3) and b(m+2)
+    // steps k0-3 .. k1-1; step m's stage brings x(m+3), b(m+2) and the
+    // class bytes of plane m+3
     const int mstart = k0 - 3;
     // x planes are read at z = -64 (entirely outside: zero fill) when the
     // input is identically zero
@@ -524,46 +561,46 @@ __global__ void __launch_bounds__(tq::NT, 3)
         asm volatile("prefetch.tensormap [%0];" ::"l"(&cmap) : "memory");
         for (int q = 0; q < SD; ++q) mbar_init(bar0 + 8 * q, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        // x plane p lives in slot (p - k0 + 3) mod XS, b plane p in (p - k0 + 1) mod BS.
-        // Stage of step mstart: x(k0-2), x(k0-1), x(k0), b(k0-1);
-        // stage of step mstart+q: x(k0+q), b(k0-1+q).
-        mbar_expect_tx(bar0, 3 * XBYTES + BBYTES);
+        // x plane p lives in slot (p - k0 + 3) mod XS, b plane p in slot
+        // (p - k0 + 1) mod BS, class plane p >= k0 in slot 1 + (p - k0) mod
+        // SD (slot 0 holds class plane k0-1).  Stage of step mstart: x(k0-2),
+        // x(k0-1), x(k0), b(k0-1), class(k0-1), class(k0); stage of step
+        // mstart+q: x(k0+q), b(k0-1+q), class(k0+q).
+        mbar_expect_tx(bar0, 3 * XBYTES + BBYTES + 2 * CBYTES);
         for (int q = 0; q < 3; ++q) tma_load_3d(smem_u32(xs + (1 + q) * XPL), &xmap, i0 - 4, j0 - 2, xz(k0 - 2 + q), bar0);
         tma_load_3d(smem_u32(bs), &bmap, i0 - 4, j0 - 1, k0 - 1, bar0);
         tma_load_3d(smem_u32(cs), &cmap, i0 / 4 - 16, j0 - 1, k0 - 1, bar0);
+        tma_load_3d(smem_u32(cs + CPL), &cmap, i0 / 4 - 16, j0 - 1, k0, bar0);
         for (int q = 1; q < SD && mstart + q < k1; ++q) {
-            mbar_expect_tx(bar0 + 8 * q, XBYTES + BBYTES);
+            mbar_expect_tx(bar0 + 8 * q, XBYTES + BBYTES + CBYTES);
             tma_load_3d(smem_u32(xs + (3 + q) * XPL), &xmap, i0 - 4, j0 - 2, xz(k0 + q), bar0 + 8 * q);
             tma_load_3d(smem_u32(bs + q * BPL), &bmap, i0 - 4, j0 - 1, k0 - 1 + q, bar0 + 8 * q);
-            tma_load_3d(smem_u32(cs + q * CPL), &cmap, i0 / 4 - 16, j0 - 1, k0 - 1 + q, bar0 + 8 * q);
+            tma_load_3d(smem_u32(cs + (1 + q) * CPL), &cmap, i0 / 4 - 16, j0 - 1, k0 + q, bar0 + 8 * q);
         }
     }
     __syncthreads();
 
-    // slot indices of x planes m-1..m+3 and b planes m..m+2 at step m = mstart
-    int sxm1 = XS - 1, sx0 = 0, sxp1 = 1, sxp2 = 2, sxp3 = 3;
-    int sb0 = BS - 2, sbp1 = BS - 1, sbp2 = 0;
-    int bi = 0;
+    // slot of x plane m (planes m+1..m+3 follow, mod XS) and of b plane m+2;
+    // the class plane m+3 sits in slot 1 + bi
+    int sx = 0, sb = 0, bi = 0;
     unsigned ph = 0;
     const int ca = a.colour_a, cb = 1 - ca;
     const int lx = 4 * qx, gi = i0 + lx, gj = j0 + ty;
     const bool quad_in = gi < g.d.nx && gj < g.d.ny;
     const int o = (ty + 2) * RW + 4 + lx, bo = (ty + 1) * RW + 4 + lx;
-    float *outp = a.x_out + (gi + g.sy * gj) + g.sz * k0;
     const int co = (ty + 1) * CW + 16 + qx;   // this quad's class byte in a class plane
-    // Coefficient lines of quads in irregular bricks are prefetched into L2
-    // one plane ahead of their first use (the first colour on plane m+3 runs
-    // in step m+1): regular-brick flags of this thread's brick column for
-    // brick planes bz0.. of planes k0-1..k1+2, as a bitmask (bit = bz - bz0).
-    const long long bplane = (long long)g.bnx * g.bny;
-    const int bz0 = max(0, (k0 - 1) >> 3), bz1 = min((g.d.nz + 7) / 8 - 1, (k1 + 2) >> 3);
-    unsigned long long qmask = ~0ull;
-    if (a.bricks && quad_in) {
-        const uint8_t *col = a.bricks + (gi >> 5) + (long long)g.bnx * (gj >> 4);
-        qmask = 0;
-        for (int bz = bz0; bz <= bz1; ++bz) qmask |= (unsigned long long)(col[bplane * bz] != 0) << (bz - bz0);
-    }
-    const float4 *qcoef = a.coef + (gi + g.sy * gj);
+    float *outp = a.x_out + (gi + g.sy * gj) + g.sz * k0;
+    const long long qoff = gi + g.sy * gj;
+    // h^-2 of the absent faces in y and in x (cells 0 and 3); planes strictly
+    // inside in z use `inner`, the first and last plane add h^-2 in z (a
+    // block-uniform branch)
+    const float cy = g.h2y * (float)((gj == 0) + (gj == g.d.ny - 1));
+    const float cx0 = gi == 0 ? g.h2x : 0.f, cx3 = gi + 3 == g.d.nx - 1 ? g.h2x : 0.f;
+    const QuadScale inner = quad_scale(g, a, cy, cx0, cx3, 0.f);
+    auto scale_at = [&](int k) {
+        const float cz = g.h2z * (float)((k == 0) + (k == g.d.nz - 1));
+        return cz == 0.f ? inner : quad_scale(g, a, cy, cx0, cx3, cz);
+    };
     // this thread's ring cell (tid < RING): rows above and below the tile
     // step along x, columns left and right step along y; the first-colour
     // cell of each pair sits at offset (c + j0 + k + rpar) & 1
@@ -582,58 +619,118 @@ __global__ void __launch_bounds__(tq::NT, 3)
             rlx = TX; rly = 2 * t; rpar = TX;
         }
     }
+    // The thread's quad on planes m-1 .. m+2: q0 (plane m) and q1 carry the
+    // first colour relaxed, q2 the values as staged; b of planes m and m+1;
+    // the class bytes of planes m .. m+3 (bits 0-7 .. 24-31).
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 qm1 = zero4, q0 = zero4, q1 = zero4, q2 = zero4, bb0 = zero4, bb1 = zero4;
+    unsigned cpipe = 0;
+    unsigned rcls = 0;   // class of this thread's ring cell on plane m+2
     Acc acc;
     bool failed = false;
     for (int m = mstart; m < k1; ++m) {
         const bool got = mbar_wait_bounded(bar0 + 8 * bi, ph);
-        float *Xm1 = xs + sxm1 * XPL, *X0 = xs + sx0 * XPL, *Xp1 = xs + sxp1 * XPL, *Xp2 = xs + sxp2 * XPL,
-              *Xp3 = xs + sxp3 * XPL;
-        const float *B0 = bs + sb0 * BPL, *Bp2 = bs + sbp2 * BPL;
-        const uint8_t *C0 = cs + sb0 * CPL, *Cp2 = cs + sbp2 * CPL;
-        if (got && m >= k0) {
-            if (quad_in) {
-                // second colour on plane m, then plane m is final
-                const unsigned cq = C0[co];
-                float4 bq, v;
-                if ((cb ^ gj ^ m) & 1) v = relax_quad<1>(g, a, X0, Xm1, Xp1, B0, o, bo, cq, gi, gj, m, bq);
-                else v = relax_quad<0>(g, a, X0, Xm1, Xp1, B0, o, bo, cq, gi, gj, m, bq);
-                *reinterpret_cast<float4 *>(outp) = v;
-                if (RZ) {
-                    acc.add(bq.x * v.x);
-                    acc.add(bq.y * v.y);
-                    acc.add(bq.z * v.z);
-                    acc.add(bq.w * v.w);
-                }
+        const int s1 = sx + 1 == XS ? 0 : sx + 1, s2 = s1 + 1 == XS ? 0 : s1 + 1, s3 = s2 + 1 == XS ? 0 : s2 + 1;
+        float *X0 = xs + sx * XPL, *X1 = xs + s1 * XPL, *X2 = xs + s2 * XPL, *X3 = xs + s3 * XPL;
+        const float *Bn = bs + sb * BPL;
+        const uint8_t *C3 = cs + (1 + bi) * CPL;
+        if (got) {
+            if (m == mstart) {
+                q1 = lds4(X1 + o);
+                q2 = lds4(X2 + o);
+                cpipe = (unsigned)cs[co] << 16;
             }
-            outp += g.sz;
-        }
-        const int kp = m + 3;
-        if (quad_in && kp >= k0 - 1 && kp <= k1 && kp < g.d.nz && !((qmask >> ((kp >> 3) - bz0)) & 1ull))
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(qcoef + g.sz * kp));
-        const int ka = m + 2;
-        if (got && ka >= 0 && ka <= k1 && ka < g.d.nz) {
-            // first colour on plane m+2: this thread's quad, then its ring cell
-            if (quad_in) {
-                const unsigned cq = Cp2[co];
-                float4 bq;
-                if ((ca ^ gj ^ ka) & 1) relax_quad<1>(g, a, Xp2, Xp1, Xp3, Bp2, o, bo, cq, gi, gj, ka, bq);
-                else relax_quad<0>(g, a, Xp2, Xp1, Xp3, Bp2, o, bo, cq, gi, gj, ka, bq);
+            const float4 q3 = lds4(X3 + o);
+            const float4 bb2 = lds4(Bn + bo);
+            const unsigned c3 = C3[co];
+            cpipe |= c3 << 24;
+            // coefficient lines of this quad's class-3 cells on plane m+3 go
+            // to L1 ahead of their first use in step m+1
+            const int kp = m + 3;
+            if (quad_in && any_general(c3) && kp < g.d.nz) {
+                const long long off = qoff + g.sz * kp;
+                prefetch_l1(a.coef + off);
+                prefetch_l1(a.gco + off);
+            }
+            const int ka = m + 2;
+            if (ka >= 0 && ka <= k1 && ka < g.d.nz) {
+                // first colour on plane m+2 (its neighbours carry the second
+                // colour: values as staged)
+                const float4 ym = lds4(X2 + o - RW), yp = lds4(X2 + o + RW);
+                const QuadScale e = scale_at(ka);
+                const unsigned c2 = (cpipe >> 16) & 0xffu;
+                if ((ca ^ gj ^ ka) & 1) {
+                    float s = __shfl_down_sync(FULL, q2.x, 1);
+                    if (qx == QX - 1) s = X2[o + 4];
+                    if (quad_in) relax_pair<1>(g, a, q2, s, ym, yp, q1, q3, bb2, c2, e, gi, gj, ka);
+                } else {
+                    float s = __shfl_up_sync(FULL, q2.w, 1);
+                    if (qx == 0) s = X2[o - 1];
+                    if (quad_in) relax_pair<0>(g, a, q2, s, ym, yp, q1, q3, bb2, c2, e, gi, gj, ka);
+                }
+                if (quad_in) *reinterpret_cast<float4 *>(X2 + o) = q2;
             }
             if (tid < RING) {
-                const int sh = (ca + j0 + ka + rpar) & 1;
-                const int lxr = rlx + (rrow ? sh : 0), lyr = rly + (rrow ? 0 : sh);
-                const int ri = i0 + lxr, rj = j0 + lyr;
-                if (ri >= 0 && ri < g.d.nx && rj >= 0 && rj < g.d.ny) {
-                    const int ro = (lyr + 2) * RW + lxr + 4;
-                    const float xc = Xp2[ro];
-                    const float bval = Bp2[(lyr + 1) * RW + lxr + 4];
-                    const unsigned rc = (Cp2[(lyr + 1) * CW + 16 + (lxr >> 2)] >> (2 * (lxr & 3))) & 3u;
-                    Xp2[ro] = relax_cls(g, a, rc, ri, rj, ka, xc, Xp2[ro - 1], Xp2[ro + 1], Xp2[ro - RW], Xp2[ro + RW],
-                                        Xp1[ro], Xp3[ro], bval);
+                // the ring cell's class on plane m+3 (kept for the next step;
+                // its class-3 coefficient lines go to L1), then the ring cell
+                // on plane m+2
+                const int lxr0 = rlx + (rrow ? ((ca + j0 + ka + rpar) & 1) : 0);
+                const int lyr0 = rly + (rrow ? 0 : ((ca + j0 + ka + rpar) & 1));
+                const int lxr1 = rlx + (rrow ? ((ca + j0 + kp + rpar) & 1) : 0);
+                const int lyr1 = rly + (rrow ? 0 : ((ca + j0 + kp + rpar) & 1));
+                if (m == mstart) rcls = (cs[(lyr0 + 1) * CW + 16 + (lxr0 >> 2)] >> (2 * (lxr0 & 3))) & 3u;
+                const unsigned rnext = (C3[(lyr1 + 1) * CW + 16 + (lxr1 >> 2)] >> (2 * (lxr1 & 3))) & 3u;
+                const int pi = i0 + lxr1, pj = j0 + lyr1;
+                if (rnext == 3u && pi >= 0 && pi < g.d.nx && pj >= 0 && pj < g.d.ny && kp < g.d.nz) {
+                    const long long off = pi + g.sy * pj + g.sz * kp;
+                    prefetch_l1(a.coef + off);
+                    prefetch_l1(a.gco + off);
                 }
+                const int ri = i0 + lxr0, rj = j0 + lyr0;
+                if (ka >= 0 && ka <= k1 && ka < g.d.nz && ri >= 0 && ri < g.d.nx && rj >= 0 && rj < g.d.ny) {
+                    const int ro = (lyr0 + 2) * RW + lxr0 + 4;
+                    const float xc = X2[ro];
+                    const float bval = Bn[(lyr0 + 1) * RW + lxr0 + 4];
+                    const float corr = g.h2x * (float)((ri == 0) + (ri == g.d.nx - 1)) +
+                                       g.h2y * (float)((rj == 0) + (rj == g.d.ny - 1)) +
+                                       g.h2z * (float)((ka == 0) + (ka == g.d.nz - 1));
+                    X2[ro] = relax_any(g, a, rcls, ri + g.sy * rj + g.sz * ka, xc, X2[ro - 1], X2[ro + 1],
+                                       X2[ro - RW], X2[ro + RW], X1[ro], X3[ro], bval, plain_scale(g, a, corr));
+                }
+                rcls = rnext;
             }
+            if (m >= k0) {
+                // second colour on plane m (its neighbours carry the first
+                // colour: relaxed in steps m-3..m-1), then plane m is final
+                const float4 ym = lds4(X0 + o - RW), yp = lds4(X0 + o + RW);
+                const QuadScale e = scale_at(m);
+                const unsigned c0 = cpipe & 0xffu;
+                if ((cb ^ gj ^ m) & 1) {
+                    float s = __shfl_down_sync(FULL, q0.x, 1);
+                    if (qx == QX - 1) s = X0[o + 4];
+                    if (quad_in) relax_pair<1>(g, a, q0, s, ym, yp, qm1, q1, bb0, c0, e, gi, gj, m);
+                } else {
+                    float s = __shfl_up_sync(FULL, q0.w, 1);
+                    if (qx == 0) s = X0[o - 1];
+                    if (quad_in) relax_pair<0>(g, a, q0, s, ym, yp, qm1, q1, bb0, c0, e, gi, gj, m);
+                }
+                if (quad_in) {
+                    *reinterpret_cast<float4 *>(outp) = q0;
+                    if (RZ) {
+                        acc.add(bb0.x * q0.x);
+                        acc.add(bb0.y * q0.y);
+                        acc.add(bb0.z * q0.z);
+                        acc.add(bb0.w * q0.w);
+                    }
+                }
+                outp += g.sz;
+            }
+            qm1 = q0; q0 = q1; q1 = q2; q2 = q3;
+            bb0 = bb1; bb1 = bb2;
+            cpipe >>= 8;
         }
-        // x plane m-1 and b plane m are dead: refill them with step m+SD's data
+        // x plane m, b plane m+2 and class plane m+3 are dead: refill them
+        // with step m+SD's data
         fence_proxy_async_smem();
         if (__syncthreads_or(!got)) {
             failed = true;
@@ -641,13 +738,13 @@ __global__ void __launch_bounds__(tq::NT, 3)
         }
         if (tid == ISSUER && m + SD < k1) {
             const int mn = m + SD;
-            mbar_expect_tx(bar0 + 8 * bi, XBYTES + BBYTES);
-            tma_load_3d(smem_u32(Xm1), &xmap, i0 - 4, j0 - 2, xz(mn + 3), bar0 + 8 * bi);
-            tma_load_3d(smem_u32(bs + sb0 * BPL), &bmap, i0 - 4, j0 - 1, mn + 2, bar0 + 8 * bi);
-            tma_load_3d(smem_u32(cs + sb0 * CPL), &cmap, i0 / 4 - 16, j0 - 1, mn + 2, bar0 + 8 * bi);
+            mbar_expect_tx(bar0 + 8 * bi, XBYTES + BBYTES + CBYTES);
+            tma_load_3d(smem_u32(X0), &xmap, i0 - 4, j0 - 2, xz(mn + 3), bar0 + 8 * bi);
+            tma_load_3d(smem_u32(bs + sb * BPL), &bmap, i0 - 4, j0 - 1, mn + 2, bar0 + 8 * bi);
+            tma_load_3d(smem_u32(C3), &cmap, i0 / 4 - 16, j0 - 1, mn + 3, bar0 + 8 * bi);
         }
-        sxm1 = sx0; sx0 = sxp1; sxp1 = sxp2; sxp2 = sxp3; sxp3 = sxp3 + 1 == XS ? 0 : sxp3 + 1;
-        sb0 = sbp1; sbp1 = sbp2; sbp2 = sbp2 + 1 == BS ? 0 : sbp2 + 1;
+        sx = s1;
+        sb = sb + 1 == BS ? 0 : sb + 1;
         if (++bi == SD) { bi = 0; ph ^= 1; }
     }
     if (failed) {
@@ -1363,7 +1460,7 @@ __global__ void k_prolong4(Dims fd, Dims cd, int dims, const float *__restrict__
 // interior cell whose six couplings are the plain h^-2 and E = 0; 1 a
 // Dirichlet cell (E = 1, no coupling); 2 a domain-edge cell with the plain
 // couplings (zero across the edge); 3 anything else.
-__global__ void k_cell_classes(Geo g, const float4 *__restrict__ coef, uint8_t *cls, int pitch) {
+__global__ void k_cell_classes(Geo g, const float4 *__restrict__ coef, uint8_t *cls, int pitch, float4 *gco) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y, k = blockIdx.z;
     if (4 * q >= g.d.nx) return;
@@ -1384,6 +1481,13 @@ __global__ void k_cell_classes(Geo g, const float4 *__restrict__ coef, uint8_t *
         const bool inner = i > 0 && i < g.d.nx - 1 && j > 0 && j < g.d.ny - 1 && k > 0 && k < g.d.nz - 1;
         const unsigned cl = plain ? (inner ? 0u : 2u) : (pinned ? 1u : 3u);
         byte |= cl << (2 * d);
+        if (cl == 3u) {
+            // the row's diagonal as the relaxation divides by it (absent
+            // faces at the domain edge carry no coupling)
+            const float kx = i > 0 ? a.x : 0.f, ky = j > 0 ? a.y : 0.f, kz = k > 0 ? a.z : 0.f;
+            const float diag = -(a.w + kx + ux + ky + uy + kz + uz);
+            gco[c] = make_float4(ux, uy, uz, 1.f / diag);
+        }
     }
     cls[q + (long long)pitch * (j + (long long)g.d.ny * k)] = (uint8_t)byte;
 }
@@ -1598,7 +1702,8 @@ int cell_classes(const Level &L, const SweepMaps &m, cudaStream_t s) {
     Geo g = make_geo(L);
     const int nq = L.d.nx / 4;
     dim3 grid((nq + 127) / 128, L.d.ny, L.d.nz);
-    k_cell_classes<<<grid, 128, 0, s>>>(g, L.coef, m.cls_ptr, m.cls_pitch);
+    FF_CHECK(m.gco, FF_E_STATE, "cell classes: coefficient array not allocated");
+    k_cell_classes<<<grid, 128, 0, s>>>(g, L.coef, m.cls_ptr, m.cls_pitch, m.gco);
     return post("cell_classes");
 }
 
@@ -1613,6 +1718,8 @@ int sweep_tma(const Level &L, const SweepMaps &m, const uint8_t *bricks, int in,
     a.bricks = bricks;
     a.sor = sor;
     a.rdreg_sor = sor / a.g.dreg;
+    a.omsor = 1.f - sor;
+    a.gco = m.gco;
     a.colour_a = colour_a;
     a.zc = tma_zchunk(L.d, sm_count);
     a.st = st;

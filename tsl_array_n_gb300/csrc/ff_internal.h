@@ -108,6 +108,9 @@ struct SweepMaps {
     const float *xp[2] = {nullptr, nullptr};
     uint8_t *cls_ptr = nullptr;
     int cls_pitch = 0;
+    // per cell of class 3: couplings across the upper x, y, z faces and the
+    // reciprocal of the diagonal (other cells' entries are not written)
+    float4 *gco = nullptr;
     bool ok = false;
 };
 

@@ -235,6 +235,9 @@ extern "C" int ff_pressure3_create(ff_ctx ctx, const ff_pressure_desc *desc, ff_
             uint8_t *cls = nullptr;
             if ((st = ff_dev_alloc((void **)&cls, ffk::sweep_tma_cls_bytes(v.d), s))) return bail(st);
             ps->smaps[l].cls_ptr = cls;
+            float4 *gco = nullptr;
+            if ((st = ff_dev_alloc((void **)&gco, (size_t)v.d.n() * sizeof(float4), s))) return bail(st);
+            ps->smaps[l].gco = gco;
             if ((st = ffk::sweep_tma_maps(v, (const float *)v.x, ps->x2[l], cls, ps->smaps[l]))) return bail(st);
             blocks = std::max(blocks, (long long)ffk::sweep_tma_blocks(v.d, ctx->sm_count));
         }
@@ -251,7 +254,10 @@ extern "C" int ff_pressure3_destroy(ff_pressure ps) {
     destroy_graphs(ps);
     ff_field_destroy(ps->guess);
     if (ps->smaps)
-        for (size_t l = 0; l < ps->lv.size(); ++l) ff_dev_free(ps->smaps[l].cls_ptr);
+        for (size_t l = 0; l < ps->lv.size(); ++l) {
+            ff_dev_free(ps->smaps[l].cls_ptr);
+            ff_dev_free(ps->smaps[l].gco);
+        }
     delete[] ps->smaps;
     ff_field_destroy(ps->pressure);
     ff_field_destroy(ps->bfield);
