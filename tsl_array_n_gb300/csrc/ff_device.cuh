@@ -97,14 +97,17 @@ __device__ __forceinline__ double warp_sum(double v) {
 
 template <int NV>
 __device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *partials, unsigned *ticket,
-                                            double (&tot)[NV]) {
+                                            double (&tot)[NV], int slot = -1) {
     __shared__ double sred[NV][32];
     __shared__ bool last;
     const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
     const int nthr = blockDim.x * blockDim.y * blockDim.z;
     const int lane = tid & 31, warp = tid >> 5, nwarp = (nthr + 31) >> 5;
     const unsigned nblocks = gridDim.x * gridDim.y * gridDim.z;
-    const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    // the block's partial goes to `slot` when given (a work-item index), else
+    // to its linear block index
+    const unsigned bid =
+        slot >= 0 ? (unsigned)slot : blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
 #pragma unroll
     for (int q = 0; q < NV; ++q) {
         double w = warp_sum(v[q]);

@@ -372,6 +372,8 @@ struct TqArgs {
     const float4 *coef;
     const uint8_t *bricks;
     const float4 *gco;             // class-3 upper couplings and 1 / diagonal
+    const int *order;              // work item of each block (tile column + z-chunk)
+    int gx, gy;                    // tiles along x and y
     float sor, rdreg_sor, omsor;   // sor, sor / dreg, 1 - sor
     int colour_a, zc;
     PcgState *st;
@@ -547,8 +549,11 @@ __global__ void __launch_bounds__(tq::NT, 3)
     // the TMA issuer is the last thread, which has no ring cell
     constexpr int ISSUER = tq::NT - 1;
     static_assert(ISSUER >= RING, "issuer carries no ring cell");
-    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
-    const int k0 = blockIdx.z * a.zc, k1 = min(k0 + a.zc, g.d.nz);
+    // one block per work item (a tile column and a z-chunk of it), in the
+    // order the work list gives
+    const int item = a.order ? a.order[blockIdx.x] : (int)blockIdx.x;
+    const int i0 = (item % a.gx) * TX, j0 = ((item / a.gx) % a.gy) * TY;
+    const int k0 = (item / (a.gx * a.gy)) * a.zc, k1 = min(k0 + a.zc, g.d.nz);
     // steps k0-3 .. k1-1; step m's stage brings x(m+3), b(m+2) and the
     // class bytes of plane m+3
     const int mstart = k0 - 3;
@@ -764,7 +769,7 @@ __global__ void __launch_bounds__(tq::NT, 3)
     if (RZ) {
         double v[1] = {acc.value()};
         double tot[1];
-        if (grid_reduce<1>(v, a.partials, &a.st->ticket[3], tot)) {
+        if (grid_reduce<1>(v, a.partials, &a.st->ticket[3], tot, item)) {
             if (tid == 0) {
                 PcgState *st = a.st;
                 double rz = tot[0];
@@ -1492,6 +1497,68 @@ __global__ void k_cell_classes(Geo g, const float4 *__restrict__ coef, uint8_t *
     cls[q + (long long)pitch * (j + (long long)g.d.ny * k)] = (uint8_t)byte;
 }
 
+// ------------------------------------------------------- sweep work order --
+// The TMA sweep's work items (tile columns x z-chunks) in launch order: the
+// items whose bricks hold a non-plain cell (solid faces, Dirichlet cells)
+// first, then the rest, each group by item index (a stable partition, so
+// the order is deterministic).  One block of 1024 threads; each thread
+// takes a contiguous run of at most 32 items.
+__global__ void __launch_bounds__(1024) k_sweep_order(Geo g, const uint8_t *__restrict__ bricks, int gx, int gy,
+                                                      int gz, int zc, int *order) {
+    __shared__ int wsum[32];
+    __shared__ int total;
+    const int n = gx * gy * gz;
+    const int per = (n + (int)blockDim.x - 1) / (int)blockDim.x;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int lo = min(n, t * per), hi = min(n, lo + per);
+    unsigned mask = 0;
+    int cnt = 0;
+    for (int it = lo; it < hi; ++it) {
+        bool heavy = false;
+        if (bricks) {
+            const int tx = it % gx, ty = (it / gx) % gy, tz = it / (gx * gy);
+            const int k0 = tz * zc, k1 = min(k0 + zc, g.d.nz);
+            const int bz0 = max(0, k0 - 1) / BZ, bz1 = min(g.d.nz - 1, k1) / BZ;
+            const int bx1 = min(2 * tx + 2, g.bnx);
+            for (int bz = bz0; bz <= bz1 && !heavy; ++bz)
+                for (int bx = 2 * tx; bx < bx1 && !heavy; ++bx)
+                    heavy = bricks[bx + (long long)g.bnx * (ty + (long long)g.bny * bz)] == 0;
+        }
+        if (heavy) {
+            mask |= 1u << (it - lo);
+            ++cnt;
+        }
+    }
+    // exclusive scan of the heavy counts over the threads
+    int inc = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += v;
+    }
+    if (lane == 31) wsum[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = (int)blockDim.x >> 5;
+        int w = lane < nw ? wsum[lane] : 0;
+        int wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += v;
+        }
+        if (lane < nw) wsum[lane] = wi - w;
+        if (lane == 31) total = wi;
+    }
+    __syncthreads();
+    int hpos = wsum[warp] + inc - cnt;       // heavy items before this thread's run
+    int lpos = total + (lo - hpos);          // light items go after all heavy ones
+    for (int it = lo; it < hi; ++it) {
+        if ((mask >> (it - lo)) & 1u) order[hpos++] = it;
+        else order[lpos++] = it;
+    }
+}
+
 // ------------------------------------------------------------ brick flags --
 // A brick is regular when every cell of it, extended by two cells on each
 // side, carries the plain coefficients (h^-2 on interior faces, E = 0).
@@ -1623,11 +1690,17 @@ int prolong4(const Level &c, const Level &f, int dims, float *fine_x, const PcgS
 bool sweep_tma_ok(const Dims &d) { return d.nx % 4 == 0 && d.nx >= 32; }
 
 static int tma_zchunk(const Dims &d, int sm_count) {
-    // one wave of 3 blocks per SM, at least 4 planes per block
+    // About two waves of 3 blocks per SM when the z-chunks stay at 12 planes
+    // or more (the work order then starts the expensive items first and the
+    // cheap ones fill in behind them), else one wave; at least 4 planes.
     long long cols = (long long)((d.nx + tq::TX - 1) / tq::TX) * ((d.ny + tq::TY - 1) / tq::TY);
-    long long want = 3LL * sm_count;
-    int chunks = (int)std::max(1LL, std::min((long long)d.nz, want / cols));
-    int zc = (d.nz + chunks - 1) / chunks;
+    long long wave = 3LL * sm_count;
+    int c2 = (int)std::max(1LL, std::min((long long)d.nz, 2 * wave / cols));
+    int zc = (d.nz + c2 - 1) / c2;
+    if (zc < 12) {
+        int c1 = (int)std::max(1LL, std::min((long long)d.nz, wave / cols));
+        zc = (d.nz + c1 - 1) / c1;
+    }
     return std::min(std::max(zc, std::min(4, d.nz)), tq::MAXZC);
 }
 
@@ -1697,14 +1770,23 @@ int sweep_tma_maps(const Level &L, const float *x0, const float *x1, uint8_t *cl
     return FF_OK;
 }
 
-int cell_classes(const Level &L, const SweepMaps &m, cudaStream_t s) {
+int cell_classes(const Level &L, const SweepMaps &m, const uint8_t *bricks, int sm_count, cudaStream_t s) {
     FF_CHECK(m.ok && m.cls_ptr, FF_E_STATE, "cell classes: maps not built");
     Geo g = make_geo(L);
     const int nq = L.d.nx / 4;
     dim3 grid((nq + 127) / 128, L.d.ny, L.d.nz);
     FF_CHECK(m.gco, FF_E_STATE, "cell classes: coefficient array not allocated");
     k_cell_classes<<<grid, 128, 0, s>>>(g, L.coef, m.cls_ptr, m.cls_pitch, m.gco);
-    return post("cell_classes");
+    FF_TRY(post("cell_classes"));
+    if (m.order) {
+        const int zc = tma_zchunk(L.d, sm_count);
+        const int gx = (L.d.nx + tq::TX - 1) / tq::TX, gy = (L.d.ny + tq::TY - 1) / tq::TY;
+        const int gz = (L.d.nz + zc - 1) / zc;
+        FF_CHECK((long long)gx * gy * gz <= 1024LL * 32, FF_E_ARG, "sweep work order: too many items");
+        k_sweep_order<<<1, 1024, 0, s>>>(g, bricks, gx, gy, gz, zc, m.order);
+        FF_TRY(post("sweep_order"));
+    }
+    return FF_OK;
 }
 
 int sweep_tma(const Level &L, const SweepMaps &m, const uint8_t *bricks, int in, int colour_a, float sor,
@@ -1720,12 +1802,15 @@ int sweep_tma(const Level &L, const SweepMaps &m, const uint8_t *bricks, int in,
     a.rdreg_sor = sor / a.g.dreg;
     a.omsor = 1.f - sor;
     a.gco = m.gco;
+    a.order = m.order;
     a.colour_a = colour_a;
     a.zc = tma_zchunk(L.d, sm_count);
     a.st = st;
     a.partials = partials;
     a.rz_mode = rz_mode;
-    dim3 grid((L.d.nx + tq::TX - 1) / tq::TX, (L.d.ny + tq::TY - 1) / tq::TY, (L.d.nz + a.zc - 1) / a.zc);
+    a.gx = (L.d.nx + tq::TX - 1) / tq::TX;
+    a.gy = (L.d.ny + tq::TY - 1) / tq::TY;
+    dim3 grid(a.gx * a.gy * ((L.d.nz + a.zc - 1) / a.zc));
     const CUtensorMap &xm = m.x[in < 0 ? out : in];
     const bool rz = rz_mode != 0;
     if (in < 0) {

@@ -111,6 +111,9 @@ struct SweepMaps {
     // per cell of class 3: couplings across the upper x, y, z faces and the
     // reciprocal of the diagonal (other cells' entries are not written)
     float4 *gco = nullptr;
+    // work order of the sweep's blocks (tile columns x z-chunks, those with
+    // non-plain cells first)
+    int *order = nullptr;
     bool ok = false;
 };
 
@@ -193,7 +196,7 @@ int prolong4(const Level &c, const Level &f, int dims, float *fine_x, const PcgS
 bool sweep_tma_ok(const Dims &d);
 size_t sweep_tma_cls_bytes(const Dims &d);
 int sweep_tma_maps(const Level &L, const float *x0, const float *x1, uint8_t *cls, SweepMaps &m);
-int cell_classes(const Level &L, const SweepMaps &m, cudaStream_t s);
+int cell_classes(const Level &L, const SweepMaps &m, const uint8_t *bricks, int sm_count, cudaStream_t s);
 int sweep_tma(const Level &L, const SweepMaps &m, const uint8_t *bricks, int in, int colour_a, float sor,
               PcgState *st, double *partials, int rz_mode, int sm_count, cudaStream_t s);
 size_t sweep_tma_blocks(const Dims &d, int sm_count);

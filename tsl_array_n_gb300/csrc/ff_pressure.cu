@@ -238,6 +238,10 @@ extern "C" int ff_pressure3_create(ff_ctx ctx, const ff_pressure_desc *desc, ff_
             float4 *gco = nullptr;
             if ((st = ff_dev_alloc((void **)&gco, (size_t)v.d.n() * sizeof(float4), s))) return bail(st);
             ps->smaps[l].gco = gco;
+            int *order = nullptr;
+            if ((st = ff_dev_alloc((void **)&order, ffk::sweep_tma_blocks(v.d, ctx->sm_count) * sizeof(int), s)))
+                return bail(st);
+            ps->smaps[l].order = order;
             if ((st = ffk::sweep_tma_maps(v, (const float *)v.x, ps->x2[l], cls, ps->smaps[l]))) return bail(st);
             blocks = std::max(blocks, (long long)ffk::sweep_tma_blocks(v.d, ctx->sm_count));
         }
@@ -257,6 +261,7 @@ extern "C" int ff_pressure3_destroy(ff_pressure ps) {
         for (size_t l = 0; l < ps->lv.size(); ++l) {
             ff_dev_free(ps->smaps[l].cls_ptr);
             ff_dev_free(ps->smaps[l].gco);
+            ff_dev_free(ps->smaps[l].order);
         }
     delete[] ps->smaps;
     ff_field_destroy(ps->pressure);
@@ -436,11 +441,13 @@ static int prepare(ff_pressure ps, ff_field u, ff_field v, ff_field w) {
         }
         FF_TRY(ffk::build_coef(c, ps->dims, ps->vbf(), s));
         if (ps->bricks[l]) FF_TRY(ffk::brick_flags(c, ps->bricks[l], s));
-        if (ps->smaps && ps->smaps[l].ok) FF_TRY(ffk::cell_classes(c, ps->smaps[l], s));
+        if (ps->smaps && ps->smaps[l].ok)
+            FF_TRY(ffk::cell_classes(c, ps->smaps[l], ps->bricks[l], ps->ctx->sm_count, s));
     }
     FF_TRY(ffk::build_coef(L0, ps->dims, ps->vbf(), s));
     if (ps->bricks[0]) FF_TRY(ffk::brick_flags(L0, ps->bricks[0], s));
-    if (ps->smaps && ps->smaps[0].ok) FF_TRY(ffk::cell_classes(L0, ps->smaps[0], s));
+    if (ps->smaps && ps->smaps[0].ok)
+        FF_TRY(ffk::cell_classes(L0, ps->smaps[0], ps->bricks[0], ps->ctx->sm_count, s));
     ps->prepared = true;
     // FP64 direct coarsest solve: refactor when the coarsest operator changed
     if (ps->desc.preconditioner == FF_PRE_MULTIGRID && ps->desc.mg_coarse_mode == FF_COARSE_DIRECT) {
