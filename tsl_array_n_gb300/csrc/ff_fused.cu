@@ -801,6 +801,580 @@ __global__ void __launch_bounds__(tq::NT, 3)
     }
 }
 
+// ------------------------------------------------------ CG on TMA levels --
+// The two CG kernels of level 0 in the layout of the TMA sweep: 64 x 16
+// tiles in the sweep's work order, one x-quad per thread, a z-march with
+// one barrier per plane.  Step k brings plane k+1 of the operands (rows
+// j0-1 .. j0+16, columns i0-4 .. i0+67) through cp.async.bulk.tensor, forms
+// the operand there (p = z + beta p, or x + alpha p in double-single) for
+// the thread's quad, the halo rows and the halo columns, keeps the quad in
+// registers and leaves the plane in shared memory, then applies A to plane
+// k: z-neighbours from registers, x-neighbours by shuffle, y-neighbours from
+// the shared plane.  Cells by class: the plain second differences (class 0),
+// plus h^-2 v for each face across the domain edge (class 2, whose
+// zero-filled neighbour entered as 0 - v), -v for a Dirichlet row (class 1),
+// the stored couplings otherwise (class 3).
+namespace tcg {
+constexpr int TX = 64, TY = 16, QX = TX / 4, NT = QX * TY;
+constexpr int RW = TX + 8, PR = TY + 2;   // staged columns i0-4 .. i0+TX+3, rows j0-1 .. j0+TY
+constexpr int PPL = ((PR * RW * 4 + 127) / 128) * 32;   // plane slot (1312 floats)
+constexpr int BPL = TY * RW;                            // b: rows j0 .. j0+TY-1 (1152 floats)
+constexpr unsigned PBYTES = PR * RW * 4, BBYTES = TY * RW * 4;
+constexpr int CW = 48, CPL = 896;
+constexpr unsigned CBYTES = CW * PR;
+constexpr int PSD = 3, XSD = 3;           // stages in flight
+constexpr size_t PAP_SMEM = 128 + 4 * ((size_t)PSD * 2 * PPL + 2 * PPL) + (size_t)PSD * CPL + 8 * PSD;
+constexpr size_t XR_SMEM =
+    128 + 4 * ((size_t)XSD * (3 * PPL + BPL) + 4 * PPL) + (size_t)XSD * CPL + 8 * XSD;
+static_assert((BPL * 4) % 128 == 0, "TMA destinations stay 128-byte aligned");
+}  // namespace tcg
+
+struct TcgArgs {
+    Geo g;
+    const float4 *coef, *gco;
+    const int *order;
+    int gx, gy, zc;
+    float *p0, *p1;
+    float *xh0, *xl0, *xh1, *xl1, *r;
+    PcgState *st;
+    double *partials;
+};
+
+__device__ __forceinline__ float4 fma4(float s, const float4 &a, const float4 &b) {
+    return make_float4(__fmaf_rn(s, a.x, b.x), __fmaf_rn(s, a.y, b.y), __fmaf_rn(s, a.z, b.z),
+                       __fmaf_rn(s, a.w, b.w));
+}
+__device__ __forceinline__ void st4(float *p, const float4 &v) { *reinterpret_cast<float4 *>(p) = v; }
+
+// (A v)_c of one cell by class; ci its index, corr = h^-2 summed over its
+// faces across the domain edge.
+__device__ __forceinline__ float ap_cell(const Geo &g, const float4 *coef, const float4 *gco, unsigned c, int i,
+                                         int j, int k, long long ci, float vc, float xm, float xp, float ym, float yp,
+                                         float zm, float zp, float corr) {
+    const float ar = apply_reg(g, vc, xm, xp, ym, yp, zm, zp);
+    if (c == 0u) return ar;
+    if (c == 2u) return __fmaf_rn(corr, vc, ar);
+    if (c == 1u) return -vc;
+    const float4 lo = __ldg(coef + ci), hi = __ldg(gco + ci);
+    Coef q;
+    q.kx = i > 0 ? lo.x : 0.f;
+    q.ky = j > 0 ? lo.y : 0.f;
+    q.kz = k > 0 ? lo.z : 0.f;
+    q.e = lo.w;
+    q.ux = hi.x;
+    q.uy = hi.y;
+    q.uz = hi.z;
+    return apply_q(q, vc, xm, xp, ym, yp, zm, zp);
+}
+
+// h^-2 summed over the faces across the domain edge of a quad's cells 0..3
+__device__ __forceinline__ float4 quad_edge(const Geo &g, int gi, int gj, int k) {
+    const float c = g.h2y * (float)((gj == 0) + (gj == g.d.ny - 1)) + g.h2z * (float)((k == 0) + (k == g.d.nz - 1));
+    return make_float4(c + (gi == 0 ? g.h2x : 0.f), c, c, c + (gi + 3 == g.d.nx - 1 ? g.h2x : 0.f));
+}
+
+__global__ void __launch_bounds__(tcg::NT, 4)
+    k_p_pap_tma(TcgArgs a, const __grid_constant__ CUtensorMap zmap, const __grid_constant__ CUtensorMap p0map,
+                const __grid_constant__ CUtensorMap p1map, const __grid_constant__ CUtensorMap cmap) {
+    constexpr int TX = tcg::TX, TY = tcg::TY, QX = tcg::QX, RW = tcg::RW, PPL = tcg::PPL, CW = tcg::CW;
+    constexpr int CPL = tcg::CPL, SD = tcg::PSD;
+    constexpr unsigned PBYTES = tcg::PBYTES, CBYTES = tcg::CBYTES, FULL = 0xffffffffu;
+    PcgState *st = a.st;
+    if (st->stop || st->err) return;
+    extern __shared__ __align__(16) unsigned char dyn_raw[];
+    float *zs = reinterpret_cast<float *>(dyn_raw + ((128u - (smem_u32(dyn_raw) & 127u)) & 127u));
+    float *pos = zs + SD * PPL;   // old p, one plane per stage
+    float *pn = pos + SD * PPL;   // new p of plane k in slot k & 1
+    uint8_t *cs = reinterpret_cast<uint8_t *>(pn + 2 * PPL);
+    const unsigned bar0 = smem_u32(cs + SD * CPL);
+    const Geo &g = a.g;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int qx = lane & (QX - 1), ty = 4 * (warp >> 1) + (warp & 1) + 2 * (lane >> 4);
+    constexpr int ISSUER = tcg::NT - 1;
+    const int pc = st->p_cur;
+    const bool first = st->first != 0;
+    const float beta = (float)st->beta;
+    const CUtensorMap *pm = pc ? &p1map : &p0map;
+    float *pnew = pc ? a.p0 : a.p1;
+    const int item = a.order ? a.order[blockIdx.x] : (int)blockIdx.x;
+    const int i0 = (item % a.gx) * TX, j0 = ((item / a.gx) % a.gy) * TY;
+    const int k0 = (item / (a.gx * a.gy)) * a.zc, k1 = min(k0 + a.zc, g.d.nz);
+    // steps k0-2 .. k1-1: step k brings plane k+1 of z, the old p and the
+    // classes, forms the new p there and applies A to plane k
+    const int mstart = k0 - 2;
+    const unsigned stage_bytes = (first ? 1u : 2u) * PBYTES + CBYTES;
+    if (tid == ISSUER) {
+        asm volatile("prefetch.tensormap [%0];" ::"l"(&zmap) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(pm) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(&cmap) : "memory");
+        for (int q = 0; q < SD; ++q) mbar_init(bar0 + 8 * q, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        for (int q = 0; q < SD && mstart + q < k1; ++q) {
+            const int pl = mstart + q + 1;
+            mbar_expect_tx(bar0 + 8 * q, stage_bytes);
+            tma_load_3d(smem_u32(zs + q * PPL), &zmap, i0 - 4, j0 - 1, pl, bar0 + 8 * q);
+            if (!first) tma_load_3d(smem_u32(pos + q * PPL), pm, i0 - 4, j0 - 1, pl, bar0 + 8 * q);
+            tma_load_3d(smem_u32(cs + q * CPL), &cmap, i0 / 4 - 16, j0 - 1, pl, bar0 + 8 * q);
+        }
+    }
+    __syncthreads();
+    const int lx = 4 * qx, gi = i0 + lx, gj = j0 + ty;
+    const bool quad_in = gi < g.d.nx && gj < g.d.ny;
+    const int o = (ty + 1) * RW + 4 + lx;
+    const int co = (ty + 1) * CW + 16 + qx;
+    const long long qoff = gi + g.sy * gj;
+    // halo quads of the new p: rows j0-1 and j0+TY, one on each of lanes 0..3
+    const int hq = warp * 4 + lane;
+    const int ho = (hq < QX ? 0 : tcg::PR - 1) * RW + 4 + 4 * (hq & (QX - 1));
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 pm1 = zero4, p0 = zero4;   // new p on planes k-1 and k
+    unsigned ck = 0;                  // class byte of plane k
+    Acc acc;
+    int bi = 0;
+    unsigned ph = 0;
+    bool failed = false;
+    for (int k = mstart; k < k1; ++k) {
+        const bool got = mbar_wait_bounded(bar0 + 8 * bi, ph);
+        const float *Z = zs + bi * PPL, *Po = pos + bi * PPL;
+        float *N1 = pn + ((k + 1) & 1) * PPL;
+        const float *N0 = pn + (k & 1) * PPL;
+        float4 p1 = zero4;
+        unsigned cnext = 0;
+        if (got) {
+            // the new p on plane k+1: this quad, the halo rows, the halo columns
+            const int kn = k + 1;
+            const float4 zq = lds4(Z + o);
+            p1 = first ? zq : fma4(beta, lds4(Po + o), zq);
+            st4(N1 + o, p1);
+            if (lane < 4) {
+                const float4 zh = lds4(Z + ho);
+                st4(N1 + ho, first ? zh : fma4(beta, lds4(Po + ho), zh));
+            }
+            if (qx == 0) N1[o - 1] = first ? Z[o - 1] : __fmaf_rn(beta, Po[o - 1], Z[o - 1]);
+            if (qx == QX - 1) N1[o + 4] = first ? Z[o + 4] : __fmaf_rn(beta, Po[o + 4], Z[o + 4]);
+            if (quad_in && kn >= k0 && kn < k1) st4(pnew + qoff + g.sz * kn, p1);
+            cnext = cs[bi * CPL + co];
+            if (quad_in && any_general(cnext) && kn < g.d.nz) {
+                prefetch_l1(a.coef + qoff + g.sz * kn);
+                prefetch_l1(a.gco + qoff + g.sz * kn);
+            }
+            if (k >= k0) {
+                // A on plane k
+                const float4 ym = lds4(N0 + o - RW), yp = lds4(N0 + o + RW);
+                float xl = __shfl_up_sync(FULL, p0.w, 1), xr = __shfl_down_sync(FULL, p0.x, 1);
+                if (qx == 0) xl = N0[o - 1];
+                if (qx == QX - 1) xr = N0[o + 4];
+                if (quad_in) {
+                    float a0, a1, a2, a3;
+                    if (ck == 0u) {
+                        a0 = apply_reg(g, p0.x, xl, p0.y, ym.x, yp.x, pm1.x, p1.x);
+                        a1 = apply_reg(g, p0.y, p0.x, p0.z, ym.y, yp.y, pm1.y, p1.y);
+                        a2 = apply_reg(g, p0.z, p0.y, p0.w, ym.z, yp.z, pm1.z, p1.z);
+                        a3 = apply_reg(g, p0.w, p0.z, xr, ym.w, yp.w, pm1.w, p1.w);
+                    } else {
+                        const float4 e = quad_edge(g, gi, gj, k);
+                        const long long ci = qoff + g.sz * k;
+                        a0 = ap_cell(g, a.coef, a.gco, ck & 3u, gi, gj, k, ci, p0.x, xl, p0.y, ym.x, yp.x, pm1.x,
+                                     p1.x, e.x);
+                        a1 = ap_cell(g, a.coef, a.gco, (ck >> 2) & 3u, gi + 1, gj, k, ci + 1, p0.y, p0.x, p0.z,
+                                     ym.y, yp.y, pm1.y, p1.y, e.y);
+                        a2 = ap_cell(g, a.coef, a.gco, (ck >> 4) & 3u, gi + 2, gj, k, ci + 2, p0.z, p0.y, p0.w,
+                                     ym.z, yp.z, pm1.z, p1.z, e.z);
+                        a3 = ap_cell(g, a.coef, a.gco, ck >> 6, gi + 3, gj, k, ci + 3, p0.w, p0.z, xr, ym.w, yp.w,
+                                     pm1.w, p1.w, e.w);
+                    }
+                    acc.add(p0.x * a0);
+                    acc.add(p0.y * a1);
+                    acc.add(p0.z * a2);
+                    acc.add(p0.w * a3);
+                }
+            }
+        }
+        pm1 = p0;
+        p0 = p1;
+        ck = cnext;
+        // plane k+1's stage is consumed: refill it with plane k+1+SD
+        fence_proxy_async_smem();
+        if (__syncthreads_or(!got)) {
+            failed = true;
+            break;
+        }
+        if (tid == ISSUER && k + SD < k1) {
+            const int pl = k + SD + 1;
+            mbar_expect_tx(bar0 + 8 * bi, stage_bytes);
+            tma_load_3d(smem_u32(zs + bi * PPL), &zmap, i0 - 4, j0 - 1, pl, bar0 + 8 * bi);
+            if (!first) tma_load_3d(smem_u32(pos + bi * PPL), pm, i0 - 4, j0 - 1, pl, bar0 + 8 * bi);
+            tma_load_3d(smem_u32(cs + bi * CPL), &cmap, i0 / 4 - 16, j0 - 1, pl, bar0 + 8 * bi);
+        }
+        if (++bi == SD) { bi = 0; ph ^= 1; }
+    }
+    if (failed) {
+        if (tid == ISSUER) {
+            atomicOr(&st->err, 1);
+            for (int q = 0; q < SD; ++q) mbar_wait_bounded(bar0 + 8 * ((bi + q) % SD), ph ^ (unsigned)((bi + q) / SD));
+        }
+        __syncthreads();
+        return;
+    }
+    double v[1] = {acc.value()};
+    double tot[1];
+    if (grid_reduce<1>(v, a.partials, &st->ticket[1], tot, item)) {
+        if (tid == 0) {
+            // alphaKernel (linalg.js:1147-1199)
+            double pAp = tot[0];
+            double value = st->rz_old / pAp;
+            int code = 0;
+            if (nonfinite_d(pAp) || pAp == 0.0) code = FF_STOP_DEGENERATE_PAP;
+            else if (fabs(pAp) > st->pap_baseline * MAX_PAP_GROWTH_FACTOR) code = FF_STOP_PAP_GROWTH;
+            else if (nonfinite_or_above(value, MAX_ALPHA_MAGNITUDE)) code = FF_STOP_ALPHA_MAGNITUDE;
+            st->pAp = pAp;
+            st->alpha = (st->stop != 0 || code != 0) ? 0.0 : value;
+            if (st->stop == 0) st->stop = code;
+            st->p_cur = pc ^ 1;
+            st->first = 0;
+        }
+    }
+}
+
+// r = b - A x in double-single for one cell of class 1 or 3: each coupling
+// term K (x_n - x_c) formed from (hi, lo) with an error-free difference and
+// product, summed with TwoSum (the general path of the cp.async kernel).
+__device__ __forceinline__ float resid_ds_general(const Coef &q, float bc, float chv, float clv, float xmh,
+                                                  float xml, float xph, float xpl, float ymh, float yml, float yph,
+                                                  float ypl, float zmh, float zml, float zph, float zpl) {
+    float S = 0.f, Se = 0.f;
+    auto term = [&](float K, float hn, float ln) {
+        float dh, de;
+        two_sum(hn, -chv, dh, de);
+        de = __fadd_rn(de, __fsub_rn(ln, clv));
+        float pr, pe;
+        two_prod(K, dh, pr, pe);
+        pe = __fmaf_rn(K, de, pe);
+        float s2, e2;
+        two_sum(S, pr, s2, e2);
+        S = s2;
+        Se = __fadd_rn(Se, __fadd_rn(e2, pe));
+    };
+    term(q.kx, xmh, xml);
+    term(q.ux, xph, xpl);
+    term(q.ky, ymh, yml);
+    term(q.uy, yph, ypl);
+    term(q.kz, zmh, zml);
+    term(q.uz, zph, zpl);
+    {
+        float pr, pe;
+        two_prod(-q.e, chv, pr, pe);
+        pe = __fmaf_rn(-q.e, clv, pe);
+        float s2, e2;
+        two_sum(S, pr, s2, e2);
+        S = s2;
+        Se = __fadd_rn(Se, __fadd_rn(e2, pe));
+    }
+    float r0, e0;
+    two_sum(bc, -S, r0, e0);
+    return __fadd_rn(r0, __fsub_rn(e0, Se));
+}
+
+// One cell's residual by class (hi/lo of the cell and its six neighbours).
+template <bool DS>
+__device__ __forceinline__ float resid_cell(const Geo &g, const float4 *coef, const float4 *gco, unsigned c, int i,
+                                            int j, int k, long long ci, float bc, float ch, float cl, float xmh,
+                                            float xml, float xph, float xpl, float ymh, float yml, float yph,
+                                            float ypl, float zmh, float zml, float zph, float zpl, float corr) {
+    if (!(c & 1u)) {
+        float ax = apply_reg(g, ch, xmh, xph, ymh, yph, zmh, zph);
+        if (c == 2u) ax = __fmaf_rn(corr, ch, ax);
+        if (DS) {
+            float al = apply_reg(g, cl, xml, xpl, yml, ypl, zml, zpl);
+            if (c == 2u) al = __fmaf_rn(corr, cl, al);
+            ax += al;
+        }
+        return bc - ax;
+    }
+    Coef q;
+    if (c == 1u) {
+        q.kx = q.ky = q.kz = q.ux = q.uy = q.uz = 0.f;
+        q.e = 1.f;
+    } else {
+        const float4 lo = __ldg(coef + ci), hi = __ldg(gco + ci);
+        q.kx = i > 0 ? lo.x : 0.f;
+        q.ky = j > 0 ? lo.y : 0.f;
+        q.kz = k > 0 ? lo.z : 0.f;
+        q.e = lo.w;
+        q.ux = hi.x;
+        q.uy = hi.y;
+        q.uz = hi.z;
+    }
+    if (DS)
+        return resid_ds_general(q, bc, ch, cl, xmh, xml, xph, xpl, ymh, yml, yph, ypl, zmh, zml, zph, zpl);
+    return bc - apply_q(q, ch, xmh, xph, ymh, yph, zmh, zph);
+}
+
+template <bool SETUP, bool DS>
+__global__ void __launch_bounds__(tcg::NT, 2)
+    k_x_residual_tma(TcgArgs a, const __grid_constant__ CUtensorMap h0map, const __grid_constant__ CUtensorMap h1map,
+                     const __grid_constant__ CUtensorMap l0map, const __grid_constant__ CUtensorMap l1map,
+                     const __grid_constant__ CUtensorMap p0map, const __grid_constant__ CUtensorMap p1map,
+                     const __grid_constant__ CUtensorMap bmap, const __grid_constant__ CUtensorMap cmap) {
+    constexpr int TX = tcg::TX, TY = tcg::TY, QX = tcg::QX, RW = tcg::RW, PPL = tcg::PPL, BPL = tcg::BPL;
+    constexpr int CW = tcg::CW, CPL = tcg::CPL, SD = tcg::XSD;
+    constexpr unsigned PBYTES = tcg::PBYTES, BBYTES = tcg::BBYTES, CBYTES = tcg::CBYTES, FULL = 0xffffffffu;
+    PcgState *st = a.st;
+    if (!SETUP && (st->stop || st->err)) return;
+    extern __shared__ __align__(16) unsigned char dyn_raw[];
+    float *hs = reinterpret_cast<float *>(dyn_raw + ((128u - (smem_u32(dyn_raw) & 127u)) & 127u));
+    float *ls = hs + SD * PPL;    // x lo per stage
+    float *qs = ls + SD * PPL;    // p per stage
+    float *bs = qs + SD * PPL;    // b per stage
+    float *nh = bs + SD * BPL;    // new x hi of plane k in slot k & 1
+    float *nl = nh + 2 * PPL;     // new x lo
+    uint8_t *cs = reinterpret_cast<uint8_t *>(nl + 2 * PPL);
+    const unsigned bar0 = smem_u32(cs + SD * CPL);
+    const Geo &g = a.g;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int qx = lane & (QX - 1), ty = 4 * (warp >> 1) + (warp & 1) + 2 * (lane >> 4);
+    constexpr int ISSUER = tcg::NT - 1;
+    const int xc = SETUP ? 0 : st->x_cur;
+    const CUtensorMap *hm = xc ? &h1map : &h0map, *lm = xc ? &l1map : &l0map;
+    const CUtensorMap *qm = st->p_cur ? &p1map : &p0map;
+    float *oh = xc ? a.xh0 : a.xh1, *ol = xc ? a.xl0 : a.xl1;
+    const double alpha = SETUP ? 0.0 : st->alpha;
+    const float ahi = (float)alpha, alo = (float)(alpha - (double)ahi);
+    const int item = a.order ? a.order[blockIdx.x] : (int)blockIdx.x;
+    const int i0 = (item % a.gx) * TX, j0 = ((item / a.gx) % a.gy) * TY;
+    const int k0 = (item / (a.gx * a.gy)) * a.zc, k1 = min(k0 + a.zc, g.d.nz);
+    // steps k0-2 .. k1-1: step k brings plane k+1 of x (hi, lo), p, b and
+    // the classes, forms x + alpha p there and forms r on plane k
+    const int mstart = k0 - 2;
+    constexpr unsigned stage_bytes = (1u + (DS ? 1u : 0u) + (SETUP ? 0u : 1u)) * PBYTES + BBYTES + CBYTES;
+    if (tid == ISSUER) {
+        for (int q = 0; q < SD; ++q) mbar_init(bar0 + 8 * q, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        for (int q = 0; q < SD && mstart + q < k1; ++q) {
+            const int pl = mstart + q + 1;
+            const unsigned bar = bar0 + 8 * q;
+            mbar_expect_tx(bar, stage_bytes);
+            tma_load_3d(smem_u32(hs + q * PPL), hm, i0 - 4, j0 - 1, pl, bar);
+            if (DS) tma_load_3d(smem_u32(ls + q * PPL), lm, i0 - 4, j0 - 1, pl, bar);
+            if (!SETUP) tma_load_3d(smem_u32(qs + q * PPL), qm, i0 - 4, j0 - 1, pl, bar);
+            tma_load_3d(smem_u32(bs + q * BPL), &bmap, i0 - 4, j0, pl, bar);
+            tma_load_3d(smem_u32(cs + q * CPL), &cmap, i0 / 4 - 16, j0 - 1, pl, bar);
+        }
+    }
+    __syncthreads();
+    const int lx = 4 * qx, gi = i0 + lx, gj = j0 + ty;
+    const bool quad_in = gi < g.d.nx && gj < g.d.ny;
+    const int o = (ty + 1) * RW + 4 + lx, bo = ty * RW + 4 + lx;
+    const int co = (ty + 1) * CW + 16 + qx;
+    const long long qoff = gi + g.sy * gj;
+    const int hq = warp * 4 + lane;
+    const int ho = (hq < QX ? 0 : tcg::PR - 1) * RW + 4 + 4 * (hq & (QX - 1));
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    // x (hi, lo) on planes k-1 and k, b on plane k
+    float4 hm1 = zero4, lm1 = zero4, h0 = zero4, l0 = zero4, b0 = zero4;
+    unsigned ck = 0;
+    Acc acc_rr, acc_bb;
+    int bi = 0;
+    unsigned ph = 0;
+    bool failed = false;
+    // x + alpha p of one staged value
+    auto form1 = [&](const float *H, const float *L, const float *Q, int off, float &oh1, float &ol1) {
+        const float hv = H[off], lv = DS ? L[off] : 0.f;
+        if (SETUP) {
+            oh1 = hv;
+            ol1 = lv;
+        } else if (DS) {
+            ds_axpy(hv, lv, ahi, alo, Q[off], oh1, ol1);
+        } else {
+            oh1 = __fmaf_rn(ahi, Q[off], hv);
+            ol1 = 0.f;
+        }
+    };
+    auto form4 = [&](const float *H, const float *L, const float *Q, int off, float4 &oh4, float4 &ol4) {
+        const float4 hv = lds4(H + off), lv = DS ? lds4(L + off) : zero4;
+        if (SETUP) {
+            oh4 = hv;
+            ol4 = lv;
+        } else {
+            const float4 qv = lds4(Q + off);
+            if (DS) {
+                ds_axpy(hv.x, lv.x, ahi, alo, qv.x, oh4.x, ol4.x);
+                ds_axpy(hv.y, lv.y, ahi, alo, qv.y, oh4.y, ol4.y);
+                ds_axpy(hv.z, lv.z, ahi, alo, qv.z, oh4.z, ol4.z);
+                ds_axpy(hv.w, lv.w, ahi, alo, qv.w, oh4.w, ol4.w);
+            } else {
+                oh4 = fma4(ahi, qv, hv);
+                ol4 = zero4;
+            }
+        }
+    };
+    for (int k = mstart; k < k1; ++k) {
+        const bool got = mbar_wait_bounded(bar0 + 8 * bi, ph);
+        const float *H = hs + bi * PPL, *L = ls + bi * PPL, *Q = qs + bi * PPL, *B = bs + bi * BPL;
+        float *NH1 = nh + ((k + 1) & 1) * PPL, *NL1 = nl + ((k + 1) & 1) * PPL;
+        const float *NH0 = nh + (k & 1) * PPL, *NL0 = nl + (k & 1) * PPL;
+        float4 h1 = zero4, l1 = zero4, b1 = zero4;
+        unsigned cnext = 0;
+        if (got) {
+            const int kn = k + 1;
+            // x + alpha p on plane k+1: this quad, the halo rows, the halo columns
+            form4(H, L, Q, o, h1, l1);
+            st4(NH1 + o, h1);
+            if (DS) st4(NL1 + o, l1);
+            if (lane < 4) {
+                float4 hh, hl;
+                form4(H, L, Q, ho, hh, hl);
+                st4(NH1 + ho, hh);
+                if (DS) st4(NL1 + ho, hl);
+            }
+            if (qx == 0 || qx == QX - 1) {
+                const int eo = qx == 0 ? o - 1 : o + 4;
+                float eh, el;
+                form1(H, L, Q, eo, eh, el);
+                NH1[eo] = eh;
+                if (DS) NL1[eo] = el;
+            }
+            if (!SETUP && quad_in && kn >= k0 && kn < k1) {
+                st4(oh + qoff + g.sz * kn, h1);
+                if (DS) st4(ol + qoff + g.sz * kn, l1);
+            }
+            b1 = lds4(B + bo);
+            cnext = cs[bi * CPL + co];
+            if (quad_in && any_general(cnext) && kn < g.d.nz) {
+                prefetch_l1(a.coef + qoff + g.sz * kn);
+                prefetch_l1(a.gco + qoff + g.sz * kn);
+            }
+            if (k >= k0) {
+                // r = b - A x on plane k
+                const float4 ymh = lds4(NH0 + o - RW), yph = lds4(NH0 + o + RW);
+                const float4 yml = DS ? lds4(NL0 + o - RW) : zero4, ypl = DS ? lds4(NL0 + o + RW) : zero4;
+                float xlh = __shfl_up_sync(FULL, h0.w, 1), xrh = __shfl_down_sync(FULL, h0.x, 1);
+                float xll = DS ? __shfl_up_sync(FULL, l0.w, 1) : 0.f, xrl = DS ? __shfl_down_sync(FULL, l0.x, 1) : 0.f;
+                if (qx == 0) {
+                    xlh = NH0[o - 1];
+                    if (DS) xll = NL0[o - 1];
+                }
+                if (qx == QX - 1) {
+                    xrh = NH0[o + 4];
+                    if (DS) xrl = NL0[o + 4];
+                }
+                if (quad_in) {
+                    float4 rq;
+                    if (ck == 0u) {
+                        float ax0 = apply_reg(g, h0.x, xlh, h0.y, ymh.x, yph.x, hm1.x, h1.x);
+                        float ax1 = apply_reg(g, h0.y, h0.x, h0.z, ymh.y, yph.y, hm1.y, h1.y);
+                        float ax2 = apply_reg(g, h0.z, h0.y, h0.w, ymh.z, yph.z, hm1.z, h1.z);
+                        float ax3 = apply_reg(g, h0.w, h0.z, xrh, ymh.w, yph.w, hm1.w, h1.w);
+                        if (DS) {
+                            ax0 += apply_reg(g, l0.x, xll, l0.y, yml.x, ypl.x, lm1.x, l1.x);
+                            ax1 += apply_reg(g, l0.y, l0.x, l0.z, yml.y, ypl.y, lm1.y, l1.y);
+                            ax2 += apply_reg(g, l0.z, l0.y, l0.w, yml.z, ypl.z, lm1.z, l1.z);
+                            ax3 += apply_reg(g, l0.w, l0.z, xrl, yml.w, ypl.w, lm1.w, l1.w);
+                        }
+                        rq = make_float4(b0.x - ax0, b0.y - ax1, b0.z - ax2, b0.w - ax3);
+                    } else {
+                        const float4 e = quad_edge(g, gi, gj, k);
+                        const long long ci = qoff + g.sz * k;
+                        rq.x = resid_cell<DS>(g, a.coef, a.gco, ck & 3u, gi, gj, k, ci, b0.x, h0.x, l0.x, xlh, xll,
+                                              h0.y, l0.y, ymh.x, yml.x, yph.x, ypl.x, hm1.x, lm1.x, h1.x, l1.x, e.x);
+                        rq.y = resid_cell<DS>(g, a.coef, a.gco, (ck >> 2) & 3u, gi + 1, gj, k, ci + 1, b0.y, h0.y,
+                                              l0.y, h0.x, l0.x, h0.z, l0.z, ymh.y, yml.y, yph.y, ypl.y, hm1.y, lm1.y,
+                                              h1.y, l1.y, e.y);
+                        rq.z = resid_cell<DS>(g, a.coef, a.gco, (ck >> 4) & 3u, gi + 2, gj, k, ci + 2, b0.z, h0.z,
+                                              l0.z, h0.y, l0.y, h0.w, l0.w, ymh.z, yml.z, yph.z, ypl.z, hm1.z, lm1.z,
+                                              h1.z, l1.z, e.z);
+                        rq.w = resid_cell<DS>(g, a.coef, a.gco, ck >> 6, gi + 3, gj, k, ci + 3, b0.w, h0.w, l0.w,
+                                              h0.z, l0.z, xrh, xrl, ymh.w, yml.w, yph.w, ypl.w, hm1.w, lm1.w, h1.w,
+                                              l1.w, e.w);
+                    }
+                    st4(a.r + qoff + g.sz * k, rq);
+                    acc_rr.add(rq.x * rq.x);
+                    acc_rr.add(rq.y * rq.y);
+                    acc_rr.add(rq.z * rq.z);
+                    acc_rr.add(rq.w * rq.w);
+                    if (SETUP) {
+                        acc_bb.add(b0.x * b0.x);
+                        acc_bb.add(b0.y * b0.y);
+                        acc_bb.add(b0.z * b0.z);
+                        acc_bb.add(b0.w * b0.w);
+                    }
+                }
+            }
+        }
+        hm1 = h0;
+        lm1 = l0;
+        h0 = h1;
+        l0 = l1;
+        b0 = b1;
+        ck = cnext;
+        fence_proxy_async_smem();
+        if (__syncthreads_or(!got)) {
+            failed = true;
+            break;
+        }
+        if (tid == ISSUER && k + SD < k1) {
+            const int pl = k + SD + 1;
+            const unsigned bar = bar0 + 8 * bi;
+            mbar_expect_tx(bar, stage_bytes);
+            tma_load_3d(smem_u32(hs + bi * PPL), hm, i0 - 4, j0 - 1, pl, bar);
+            if (DS) tma_load_3d(smem_u32(ls + bi * PPL), lm, i0 - 4, j0 - 1, pl, bar);
+            if (!SETUP) tma_load_3d(smem_u32(qs + bi * PPL), qm, i0 - 4, j0 - 1, pl, bar);
+            tma_load_3d(smem_u32(bs + bi * BPL), &bmap, i0 - 4, j0, pl, bar);
+            tma_load_3d(smem_u32(cs + bi * CPL), &cmap, i0 / 4 - 16, j0 - 1, pl, bar);
+        }
+        if (++bi == SD) { bi = 0; ph ^= 1; }
+    }
+    if (failed) {
+        if (tid == ISSUER) {
+            atomicOr(&st->err, 1);
+            for (int q = 0; q < SD; ++q) mbar_wait_bounded(bar0 + 8 * ((bi + q) % SD), ph ^ (unsigned)((bi + q) / SD));
+        }
+        __syncthreads();
+        return;
+    }
+    if (SETUP) {
+        double v[2] = {acc_rr.value(), acc_bb.value()};
+        double tot[2];
+        if (grid_reduce<2>(v, a.partials, &st->ticket[0], tot, item)) {
+            if (tid == 0) {
+                st->rr = tot[0];
+                st->bb = tot[1];
+                double nb = sqrt(fabs(tot[1]));
+                st->thr = st->relative ? fmax(st->tol * nb, st->tol) : st->tol;
+                // the start already meets the tolerance (linalg.js:1695-1699)
+                if (sqrt(fabs(tot[0])) < st->thr) {
+                    st->stop = FF_STOP_CONVERGED;
+                    st->stop_iter = 0;
+                }
+            }
+        }
+    } else {
+        double v[1] = {acc_rr.value()};
+        double tot[1];
+        if (grid_reduce<1>(v, a.partials, &st->ticket[2], tot, item)) {
+            if (tid == 0) {
+                double rr = tot[0];
+                st->rr = rr;
+                st->x_cur = xc ^ 1;
+                st->iter += 1;
+                if (!nonfinite_d(rr)) {
+                    if (st->best_rr < 0.0 || fabs(rr) < st->best_rr) st->best_rr = fabs(rr);
+                    else if (st->best_rr > 0.0 && fabs(rr) > st->best_rr * MAX_RESIDUAL_GROWTH && st->stop == 0)
+                        st->growth_stop = 1;
+                }
+                double res = sqrt(fabs(rr));
+                bool conv = !nonfinite_or_above(res, st->thr);
+                if (conv && st->stop == 0) {
+                    st->stop = FF_STOP_CONVERGED;
+                    st->stop_iter = st->iter;
+                } else if (st->growth_stop && st->stop == 0) {
+                    st->stop = FF_STOP_RESIDUAL_GROWING;
+                }
+            }
+        }
+    }
+}
+
 // ------------------------------------------------------------------ CG ----
 struct CgArgs {
     Geo g;
@@ -1896,6 +2470,15 @@ int fused_configure() {
     FF_CUDA(cudaFuncSetAttribute(k_sweep_tma<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tq::SMEM));
     FF_CUDA(cudaFuncSetAttribute(k_res_restrict, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rr_smem()));
     FF_CUDA(cudaFuncSetAttribute(k_p_pap, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p_pap_smem()));
+    FF_CUDA(cudaFuncSetAttribute(k_p_pap_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcg::PAP_SMEM));
+    FF_CUDA(cudaFuncSetAttribute(k_x_residual_tma<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tcg::XR_SMEM));
+    FF_CUDA(cudaFuncSetAttribute(k_x_residual_tma<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tcg::XR_SMEM));
+    FF_CUDA(cudaFuncSetAttribute(k_x_residual_tma<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tcg::XR_SMEM));
+    FF_CUDA(cudaFuncSetAttribute(k_x_residual_tma<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tcg::XR_SMEM));
     FF_CUDA(cudaFuncSetAttribute(k_x_residual<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)xres_smem<true, true>()));
     FF_CUDA(cudaFuncSetAttribute(k_x_residual<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1918,6 +2501,87 @@ int fused_x_residual(const Level &L0, const uint8_t *bricks, const float *p0, co
     else rc = ds ? launch_xres<false, true>(a, grid, block, s) : launch_xres<false, false>(a, grid, block, s);
     FF_TRY(rc);
     return post("x_residual");
+}
+
+
+int cg_tma_maps(const Level &L0, const float *z0, const float *z1, const float *p0, const float *p1,
+                const float *xh0, const float *xl0, const float *xh1, const float *xl1, const float *b, bool ds,
+                CgMaps &m) {
+    m.ok = false;
+    FF_CHECK(sweep_tma_ok(L0.d), FF_E_ARG, "TMA CG kernels need nx %% 4 == 0 and nx >= 32");
+    uintptr_t any = (uintptr_t)z0 | (uintptr_t)z1 | (uintptr_t)p0 | (uintptr_t)p1 | (uintptr_t)xh0 |
+                    (uintptr_t)xh1 | (uintptr_t)b;
+    if (ds) any |= (uintptr_t)xl0 | (uintptr_t)xl1;
+    FF_CHECK(any % 16 == 0, FF_E_ARG, "TMA operand misaligned");
+    FF_TRY(encode_planes(&m.z[0], z0, L0.d, tcg::PR));
+    FF_TRY(encode_planes(&m.z[1], z1, L0.d, tcg::PR));
+    FF_TRY(encode_planes(&m.p[0], p0, L0.d, tcg::PR));
+    FF_TRY(encode_planes(&m.p[1], p1, L0.d, tcg::PR));
+    FF_TRY(encode_planes(&m.xh[0], xh0, L0.d, tcg::PR));
+    FF_TRY(encode_planes(&m.xh[1], xh1, L0.d, tcg::PR));
+    if (ds) {
+        FF_TRY(encode_planes(&m.xl[0], xl0, L0.d, tcg::PR));
+        FF_TRY(encode_planes(&m.xl[1], xl1, L0.d, tcg::PR));
+    } else {
+        m.xl[0] = m.xh[0];
+        m.xl[1] = m.xh[1];
+    }
+    FF_TRY(encode_planes(&m.b, b, L0.d, tcg::TY));
+    m.zp[0] = z0;
+    m.zp[1] = z1;
+    m.ds = ds;
+    m.ok = true;
+    return FF_OK;
+}
+
+static TcgArgs tcg_args(const Level &L0, const SweepMaps &sm, int sm_count) {
+    TcgArgs a;
+    a.g = make_geo(L0);
+    a.coef = L0.coef;
+    a.gco = sm.gco;
+    a.order = sm.order;
+    a.gx = (L0.d.nx + tcg::TX - 1) / tcg::TX;
+    a.gy = (L0.d.ny + tcg::TY - 1) / tcg::TY;
+    a.zc = tma_zchunk(L0.d, sm_count);
+    return a;
+}
+
+int p_pap_tma(const Level &L0, const SweepMaps &sm, const CgMaps &m, const float *z, float *p0, float *p1,
+              PcgState *st, double *partials, int sm_count, cudaStream_t s) {
+    FF_CHECK(sm.ok && m.ok, FF_E_STATE, "TMA CG maps not built");
+    const int zi = z == m.zp[0] ? 0 : z == m.zp[1] ? 1 : -1;
+    FF_CHECK(zi >= 0, FF_E_STATE, "p.Ap: z is in neither sweep buffer");
+    TcgArgs a = tcg_args(L0, sm, sm_count);
+    a.p0 = p0;
+    a.p1 = p1;
+    a.st = st;
+    a.partials = partials;
+    dim3 grid(a.gx * a.gy * ((L0.d.nz + a.zc - 1) / a.zc));
+    k_p_pap_tma<<<grid, tcg::NT, tcg::PAP_SMEM, s>>>(a, m.z[zi], m.p[0], m.p[1], sm.cls);
+    return post("p_pap_tma");
+}
+
+int x_residual_tma(const Level &L0, const SweepMaps &sm, const CgMaps &m, float *xh0, float *xl0, float *xh1,
+                   float *xl1, float *r, PcgState *st, double *partials, int setup, int sm_count, cudaStream_t s) {
+    FF_CHECK(sm.ok && m.ok, FF_E_STATE, "TMA CG maps not built");
+    TcgArgs a = tcg_args(L0, sm, sm_count);
+    a.xh0 = xh0;
+    a.xl0 = xl0;
+    a.xh1 = xh1;
+    a.xl1 = xl1;
+    a.r = r;
+    a.st = st;
+    a.partials = partials;
+    dim3 grid(a.gx * a.gy * ((L0.d.nz + a.zc - 1) / a.zc));
+    const size_t sh = tcg::XR_SMEM;
+    if (setup) {
+        if (m.ds) k_x_residual_tma<true, true><<<grid, tcg::NT, sh, s>>>(a, m.xh[0], m.xh[1], m.xl[0], m.xl[1], m.p[0], m.p[1], m.b, sm.cls);
+        else k_x_residual_tma<true, false><<<grid, tcg::NT, sh, s>>>(a, m.xh[0], m.xh[1], m.xl[0], m.xl[1], m.p[0], m.p[1], m.b, sm.cls);
+    } else {
+        if (m.ds) k_x_residual_tma<false, true><<<grid, tcg::NT, sh, s>>>(a, m.xh[0], m.xh[1], m.xl[0], m.xl[1], m.p[0], m.p[1], m.b, sm.cls);
+        else k_x_residual_tma<false, false><<<grid, tcg::NT, sh, s>>>(a, m.xh[0], m.xh[1], m.xl[0], m.xl[1], m.p[0], m.p[1], m.b, sm.cls);
+    }
+    return post("x_residual_tma");
 }
 
 }  // namespace ffk

@@ -117,6 +117,18 @@ struct SweepMaps {
     bool ok = false;
 };
 
+// Tensor maps of the level-0 CG operands for the TMA CG kernels: plane
+// regions of 18 rows (16 for b) and 72 columns.
+struct CgMaps {
+    CUtensorMap z[2];          // preconditioned residual, in either sweep buffer
+    CUtensorMap p[2];          // search directions (ping-pong)
+    CUtensorMap xh[2], xl[2];  // iterate, high and low words (ping-pong)
+    CUtensorMap b;             // right-hand side of the solve
+    const float *zp[2] = {nullptr, nullptr};
+    bool ds = false;
+    bool ok = false;
+};
+
 // --------------------------------------------------------- kernel launchers --
 namespace ffk {
 // generic
@@ -197,6 +209,13 @@ bool sweep_tma_ok(const Dims &d);
 size_t sweep_tma_cls_bytes(const Dims &d);
 int sweep_tma_maps(const Level &L, const float *x0, const float *x1, uint8_t *cls, SweepMaps &m);
 int cell_classes(const Level &L, const SweepMaps &m, const uint8_t *bricks, int sm_count, cudaStream_t s);
+int cg_tma_maps(const Level &L0, const float *z0, const float *z1, const float *p0, const float *p1,
+                const float *xh0, const float *xl0, const float *xh1, const float *xl1, const float *b, bool ds,
+                CgMaps &m);
+int p_pap_tma(const Level &L0, const SweepMaps &sm, const CgMaps &m, const float *z, float *p0, float *p1,
+              PcgState *st, double *partials, int sm_count, cudaStream_t s);
+int x_residual_tma(const Level &L0, const SweepMaps &sm, const CgMaps &m, float *xh0, float *xl0, float *xh1,
+                   float *xl1, float *r, PcgState *st, double *partials, int setup, int sm_count, cudaStream_t s);
 int sweep_tma(const Level &L, const SweepMaps &m, const uint8_t *bricks, int in, int colour_a, float sor,
               PcgState *st, double *partials, int rz_mode, int sm_count, cudaStream_t s);
 size_t sweep_tma_blocks(const Dims &d, int sm_count);

@@ -55,6 +55,7 @@ struct ff_pressure_s {
     float *z_final = nullptr;
     // TMA descriptors per level (levels where the TMA sweep applies)
     SweepMaps *smaps = nullptr;
+    CgMaps cgm;              // level-0 CG operands for the TMA CG kernels
     bool use_tma = true;
     // learned warm start (borrowed network), its guess field, last choice
     ff_unet net = nullptr;
@@ -247,6 +248,10 @@ extern "C" int ff_pressure3_create(ff_ctx ctx, const ff_pressure_desc *desc, ff_
         }
     }
     if ((st = ff_dev_alloc((void **)&ps->partials, (size_t)blocks * 2 * sizeof(double), s))) return bail(st);
+    if (ps->smaps && ps->smaps[0].ok &&
+        (st = ffk::cg_tma_maps(ps->lv[0], (const float *)ps->z, ps->x2[0], ps->p0, ps->p1, ps->xh0(), ps->x_lo0,
+                               ps->x_hi1, ps->x_lo1, (const float *)ps->bfield->d, ps->ds(), ps->cgm)))
+        return bail(st);
     if (cudaStreamSynchronize(s) != cudaSuccess) return bail(ff_set_error(FF_E_CUDA, "sync after create"));
     *out = ps;
     return FF_OK;
@@ -658,6 +663,9 @@ static int precondition(ff_pressure ps, PcgState *st) {
 }
 
 // ------------------------------------------------------------------ solve --
+// the level-0 CG kernels run in the TMA layout when the sweep does
+static bool cg_tma(const ff_pressure ps) { return ps->use_tma && ps->cgm.ok && ps->smaps && ps->smaps[0].ok; }
+
 static int enqueue_setup(ff_pressure ps) {
     const Dims &d = ps->d;
     cudaStream_t s = ps->s();
@@ -666,9 +674,13 @@ static int enqueue_setup(ff_pressure ps) {
         FF_TRY(ffk::cg_setup_residual(d, ps->lv[0].coef, (const float *)ps->bfield->d, ps->xh0(),
                                       ps->x_lo0, ps->r, ps->st, ps->partials, ps->ds(), s));
     } else {
-        FF_TRY(ffk::fused_x_residual(ps->lv[0], ps->bricks[0], ps->p0, ps->p1, (const float *)ps->bfield->d,
-                                     ps->xh0(), ps->x_lo0, ps->x_hi1, ps->x_lo1, ps->r, ps->st, ps->partials,
-                                     ps->ds(), 1, ps->ctx->sm_count, s));
+        if (cg_tma(ps))
+            FF_TRY(ffk::x_residual_tma(ps->lv[0], ps->smaps[0], ps->cgm, ps->xh0(), ps->x_lo0, ps->x_hi1, ps->x_lo1,
+                                       ps->r, ps->st, ps->partials, 1, ps->ctx->sm_count, s));
+        else
+            FF_TRY(ffk::fused_x_residual(ps->lv[0], ps->bricks[0], ps->p0, ps->p1, (const float *)ps->bfield->d,
+                                         ps->xh0(), ps->x_lo0, ps->x_hi1, ps->x_lo1, ps->r, ps->st, ps->partials,
+                                         ps->ds(), 1, ps->ctx->sm_count, s));
     }
     bool rz_done;
     FF_TRY(precondition_rz(ps, ps->st, 2, &rz_done));
@@ -687,11 +699,19 @@ static int enqueue_iteration(ff_pressure ps, unsigned long long handle, int use_
                                          ps->st, ps->partials, ps->ds(), s));
     } else {
         // z_final is static for a configuration: the setup's V-cycle left it
-        FF_TRY(ffk::fused_p_pap(ps->lv[0], ps->bricks[0], ps->z_final ? ps->z_final : (float *)ps->z, ps->p0,
-                                ps->p1, ps->st, ps->partials, ps->ctx->sm_count, s));
-        FF_TRY(ffk::fused_x_residual(ps->lv[0], ps->bricks[0], ps->p0, ps->p1, (const float *)ps->bfield->d,
-                                     ps->xh0(), ps->x_lo0, ps->x_hi1, ps->x_lo1, ps->r, ps->st, ps->partials,
-                                     ps->ds(), 0, ps->ctx->sm_count, s));
+        const float *zf = ps->z_final ? ps->z_final : (const float *)ps->z;
+        if (cg_tma(ps)) {
+            FF_TRY(ffk::p_pap_tma(ps->lv[0], ps->smaps[0], ps->cgm, zf, ps->p0, ps->p1, ps->st, ps->partials,
+                                  ps->ctx->sm_count, s));
+            FF_TRY(ffk::x_residual_tma(ps->lv[0], ps->smaps[0], ps->cgm, ps->xh0(), ps->x_lo0, ps->x_hi1, ps->x_lo1,
+                                       ps->r, ps->st, ps->partials, 0, ps->ctx->sm_count, s));
+        } else {
+            FF_TRY(ffk::fused_p_pap(ps->lv[0], ps->bricks[0], zf, ps->p0, ps->p1, ps->st, ps->partials,
+                                    ps->ctx->sm_count, s));
+            FF_TRY(ffk::fused_x_residual(ps->lv[0], ps->bricks[0], ps->p0, ps->p1, (const float *)ps->bfield->d,
+                                         ps->xh0(), ps->x_lo0, ps->x_hi1, ps->x_lo1, ps->r, ps->st, ps->partials,
+                                         ps->ds(), 0, ps->ctx->sm_count, s));
+        }
     }
     bool rz_done;
     FF_TRY(precondition_rz(ps, ps->st, 1, &rz_done));
@@ -1049,6 +1069,8 @@ extern "C" int ff_pressure3_profile(ff_pressure ps, int which, int reps, float *
         switch (which) {
         case FF_PROF_P_PAP:
             rc = nf ? ffk::cg_update_p_pap(d, L0.coef, ps->z, 0, ps->p0, ps->p1, ps->st, ps->partials, s)
+                 : cg_tma(ps) ? ffk::p_pap_tma(L0, ps->smaps[0], ps->cgm, (const float *)ps->z, ps->p0, ps->p1,
+                                               ps->st, ps->partials, ps->ctx->sm_count, s)
                     : ffk::fused_p_pap(L0, ps->bricks[0], (float *)ps->z, ps->p0, ps->p1, ps->st, ps->partials,
                                        ps->ctx->sm_count, s);
             break;
@@ -1056,6 +1078,8 @@ extern "C" int ff_pressure3_profile(ff_pressure ps, int which, int reps, float *
             rc = nf ? ffk::cg_update_x_residual(d, L0.coef, (const float *)ps->bfield->d, ps->p0, ps->p1, ps->xh0(),
                                                 ps->x_lo0, ps->x_hi1, ps->x_lo1, ps->r, ps->st, ps->partials,
                                                 ps->ds(), s)
+                 : cg_tma(ps) ? ffk::x_residual_tma(L0, ps->smaps[0], ps->cgm, ps->xh0(), ps->x_lo0, ps->x_hi1,
+                                                    ps->x_lo1, ps->r, ps->st, ps->partials, 0, ps->ctx->sm_count, s)
                     : ffk::fused_x_residual(L0, ps->bricks[0], ps->p0, ps->p1, (const float *)ps->bfield->d,
                                             ps->xh0(), ps->x_lo0, ps->x_hi1, ps->x_lo1, ps->r, ps->st,
                                             ps->partials, ps->ds(), 0, ps->ctx->sm_count, s);
