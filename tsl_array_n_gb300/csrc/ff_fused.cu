@@ -2034,6 +2034,347 @@ __global__ void k_prolong4(Dims fd, Dims cd, int dims, const float *__restrict__
     }
 }
 
+// ------------------------------------------------- coarse-level V-cycle --
+// The V-cycle below a level (its pre-smoothing, residual and restriction,
+// every coarser level, the direct coarsest solve, the prolongations and the
+// post-smoothing) in one cooperative launch: phases over all cells of one
+// level separated by grid-wide barriers.  The coarse levels are too small
+// to fill the GPU, so one launch per sweep would cost more in launch and
+// pipeline latency than in work.  Colour passes run in place (a colour
+// reads only the other colour); the first pass on a level writes every cell,
+// the level starting from x = 0.  Values written inside the launch are read
+// through L2 (ld.global.cg), never from a possibly stale L1 line.  Per cell the arithmetic is that of the
+// level kernels: the TMA sweep's relaxation by class, k_resid_rx's residual
+// and x-taps followed by k_restrict_yz's y and z taps, k_coarse_direct's
+// row products, k_prolong4's correction.
+constexpr int TAIL_MAXL = 8;
+constexpr int TAIL_NT = 1024;
+struct TailLevel {
+    Geo g;
+    float *x, *b, *r;              // r: residual scratch of the level
+    const float4 *coef, *gco;
+    const uint8_t *cls, *mask;     // class bytes (cpitch bytes per row), Dirichlet mask (may be null)
+    int cpitch;
+    float rdreg_sor;               // sor / dreg
+};
+struct TailArgs {
+    TailLevel lv[TAIL_MAXL];
+    int nl;                        // levels, the last one the coarsest
+    int down, up, dims;
+    float sor, omsor;
+    const double *G;               // coarsest inverse, nG x nG, row-major (direct mode)
+    int nG;
+    int coarse_sweeps;             // > 0: that many sweeps on the coarsest level instead of G b
+    PcgState *st;                  // may be null
+    unsigned *bar;                 // grid barrier: arrivals, generation, abort
+};
+
+// Grid-wide barrier of the cooperative launch over three words: a count of
+// arrivals that only grows within a launch (barrier k completes when it
+// reaches k x blocks), the number of blocks done with the launch (the last
+// one clears both counts, once no block polls them), and an abort flag.  A
+// block that waits more than 0.5 s raises the abort flag, which releases
+// every waiting block; all then return false.
+__device__ bool tail_sync(unsigned *bar, unsigned &passed) {
+    __shared__ int ok_s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        volatile unsigned *vb = bar;
+        if (vb[2]) {
+            ok = 0;
+        } else {
+            const unsigned target = (passed + 1) * gridDim.x;
+            __threadfence();
+            atomicAdd(&bar[0], 1u);
+            const unsigned long long t0 = globaltimer_ns();
+            while (vb[0] < target) {
+                if (vb[2]) { ok = 0; break; }
+                if (globaltimer_ns() - t0 > 500000000ull) {
+                    atomicExch(&bar[2], 1u);
+                    ok = 0;
+                    break;
+                }
+            }
+            __threadfence();
+        }
+        ok_s = ok;
+    }
+    __syncthreads();
+    ++passed;
+    return ok_s != 0;
+}
+
+// after a block's last barrier: the last block to get here clears the counts
+__device__ void tail_done(unsigned *bar) {
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&bar[1], 1u) == gridDim.x - 1) {
+            atomicExch(&bar[0], 0u);
+            atomicExch(&bar[1], 0u);
+        }
+    }
+}
+
+__device__ __forceinline__ unsigned tail_class(const TailLevel &L, int i, int j, int k) {
+    return (__ldg(L.cls + (long long)L.cpitch * (j + (long long)L.g.d.ny * k) + (i >> 2)) >> (2 * (i & 3))) & 3u;
+}
+
+// the relaxation of one cell by class (the TMA sweep's arithmetic)
+__device__ __forceinline__ float tail_relax(const TailArgs &a, const TailLevel &L, unsigned cl, long long c, int i,
+                                           int j, int k, float vc, float xm, float xp, float ym, float yp, float zm,
+                                           float zp, float bval) {
+    const Geo &g = L.g;
+    if (!(cl & 1u)) {
+        const float corr = g.h2x * (float)((i == 0) + (i == g.d.nx - 1)) +
+                           g.h2y * (float)((j == 0) + (j == g.d.ny - 1)) +
+                           g.h2z * (float)((k == 0) + (k == g.d.nz - 1));
+        const float rd = corr == 0.f ? L.rdreg_sor : a.sor / (g.dreg + corr);
+        return relax_plain(g, a.omsor, vc, xm, xp, ym, yp, zm, zp, bval, rd);
+    }
+    if (cl == 1u) return __fmaf_rn(bval, -a.sor, a.omsor * vc);
+    const float4 lo = __ldg(L.coef + c), hi = __ldg(L.gco + c);
+    float s = lo.x * xm;
+    s = __fmaf_rn(hi.x, xp, s);
+    s = __fmaf_rn(lo.y, ym, s);
+    s = __fmaf_rn(hi.y, yp, s);
+    s = __fmaf_rn(lo.z, zm, s);
+    s = __fmaf_rn(hi.z, zp, s);
+    return __fmaf_rn(bval - s, a.sor * hi.w, a.omsor * vc);
+}
+
+// one colour pass (colour col = (i + j + k) & 1) in place, one thread per
+// cell of the colour (nx is even: nx / 2 of them per row); `first`: x is 0
+// on entry and the thread also writes 0 to the row neighbour of the other
+// colour
+__device__ void tail_colour(const TailArgs &a, const TailLevel &L, int col, bool first, long long t0,
+                            long long stride) {
+    const Geo &g = L.g;
+    const int nx = g.d.nx, ny = g.d.ny, nz = g.d.nz, hx = nx >> 1;
+    const long long n = (long long)hx * ny * nz;
+    float *x = L.x;
+    for (long long t = t0; t < n; t += stride) {
+        const int m = (int)(t % hx);
+        const long long rr = t / hx;
+        const int j = (int)(rr % ny), k = (int)(rr / ny);
+        const int par = (j + k + col) & 1;
+        const int i = 2 * m + par;
+        const long long c = i + g.sy * j + g.sz * k;
+        float vc = 0.f, xm = 0.f, xp = 0.f, ym = 0.f, yp = 0.f, zm = 0.f, zp = 0.f;
+        if (first) {
+            x[c + (par ? -1 : 1)] = 0.f;
+        } else {
+            vc = __ldcg(x + c);
+            if (i > 0) xm = __ldcg(x + c - 1);
+            if (i < nx - 1) xp = __ldcg(x + c + 1);
+            if (j > 0) ym = __ldcg(x + c - g.sy);
+            if (j < ny - 1) yp = __ldcg(x + c + g.sy);
+            if (k > 0) zm = __ldcg(x + c - g.sz);
+            if (k < nz - 1) zp = __ldcg(x + c + g.sz);
+        }
+        x[c] = tail_relax(a, L, tail_class(L, i, j, k), c, i, j, k, vc, xm, xp, ym, yp, zm, zp, __ldcg(L.b + c));
+    }
+}
+
+// r = b - A x (0 on Dirichlet cells); xzero: x is taken as 0 and cleared
+__device__ void tail_residual(const TailLevel &L, bool xzero, long long t0, long long stride) {
+    const Geo &g = L.g;
+    const int nx = g.d.nx, ny = g.d.ny, nz = g.d.nz;
+    const long long n = (long long)nx * ny * nz;
+    const float *x = L.x;
+    for (long long c = t0; c < n; c += stride) {
+        const int i = (int)(c % nx);
+        const long long rr = c / nx;
+        const int j = (int)(rr % ny), k = (int)(rr / ny);
+        const unsigned cl = tail_class(L, i, j, k);
+        if (xzero) {
+            L.r[c] = cl == 1u ? 0.f : __ldcg(L.b + c);
+            L.x[c] = 0.f;
+            continue;
+        }
+        const float vc = __ldcg(x + c);
+        const float xm = i > 0 ? __ldcg(x + c - 1) : vc, xp = i < nx - 1 ? __ldcg(x + c + 1) : vc;
+        const float ym = j > 0 ? __ldcg(x + c - g.sy) : vc, yp = j < ny - 1 ? __ldcg(x + c + g.sy) : vc;
+        const float zm = k > 0 ? __ldcg(x + c - g.sz) : vc, zp = k < nz - 1 ? __ldcg(x + c + g.sz) : vc;
+        L.r[c] = resid_cls(g, L.coef, cl, i, j, k, __ldcg(L.b + c), vc, xm, xp, ym, yp, zm, zp);
+    }
+}
+
+// coarse b = R r (the 1/8, 3/8, 3/8, 1/8 taps per axis), 0 on coarse
+// Dirichlet cells; relax0: also the coarse level's first colour-0 pass
+// (from x = 0 a cell needs only its own b; colour-1 cells get 0)
+__device__ void tail_restrict(const TailArgs &a, const TailLevel &F, const TailLevel &C, bool relax0, long long t0,
+                              long long stride) {
+    const Dims fd = F.g.d, cd = C.g.d;
+    const long long n = (long long)cd.nx * cd.ny * cd.nz;
+    const float w4[4] = {0.125f, 0.375f, 0.375f, 0.125f};
+    for (long long c = t0; c < n; c += stride) {
+        const int I = (int)(c % cd.nx);
+        const long long rr = c / cd.nx;
+        const int J = (int)(rr % cd.ny), K = (int)(rr / cd.ny);
+        if (C.mask && __ldg(C.mask + c)) {
+            C.b[c] = 0.f;
+            if (relax0)
+                C.x[c] = ((I + J + K) & 1) ? 0.f
+                                           : tail_relax(a, C, tail_class(C, I, J, K), c, I, J, K, 0.f, 0.f, 0.f, 0.f,
+                                                        0.f, 0.f, 0.f, 0.f);
+            continue;
+        }
+        int ix[4], jy[4], kz[4];
+        rtap4(I, cd.nx, ix);
+        rtap4(J, cd.ny, jy);
+        int nzt = 4;
+        if (a.dims == 3) rtap4(K, cd.nz, kz);
+        else { kz[0] = K; nzt = 1; }
+        float s = 0.f;
+        for (int q = 0; q < nzt; ++q) {
+            const float wz = a.dims == 3 ? w4[q] : 1.0f;
+            float part = 0.f;
+#pragma unroll
+            for (int p = 0; p < 4; ++p) {
+                const float *row = F.r + (long long)fd.nx * (jy[p] + (long long)fd.ny * kz[q]);
+                const float rx = 0.125f * __ldcg(row + ix[0]) + 0.375f * __ldcg(row + ix[1]) +
+                                 0.375f * __ldcg(row + ix[2]) + 0.125f * __ldcg(row + ix[3]);
+                part += rx * w4[p];
+            }
+            s += part * wz;
+        }
+        C.b[c] = s;
+        if (relax0)
+            C.x[c] = ((I + J + K) & 1) ? 0.f
+                                       : tail_relax(a, C, tail_class(C, I, J, K), c, I, J, K, 0.f, 0.f, 0.f, 0.f, 0.f,
+                                                    0.f, 0.f, s);
+    }
+}
+
+// coarsest x = G b, one warp per row (FP64)
+__device__ void tail_direct(const TailArgs &a, const TailLevel &C) {
+    const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    for (long long row = warp; row < a.nG; row += nwarps) {
+        const double *gr = a.G + row * a.nG;
+        double s = 0.0;
+        for (int j = lane; j < a.nG; j += 32) s += __ldg(gr + j) * (double)__ldcg(C.b + j);
+        s = warp_sum(s);
+        if (lane == 0) C.x[row] = (float)s;
+    }
+}
+
+// fine x += P coarse x, skipped on fine Dirichlet cells
+__device__ void tail_prolong(const TailArgs &a, const TailLevel &C, const TailLevel &F, long long t0,
+                             long long stride) {
+    const Dims fd = F.g.d, cd = C.g.d;
+    const long long n = (long long)fd.nx * fd.ny * fd.nz;
+    for (long long c = t0; c < n; c += stride) {
+        if (F.mask && __ldg(F.mask + c)) continue;
+        const int i = (int)(c % fd.nx);
+        const long long rr = c / fd.nx;
+        const int j = (int)(rr % fd.ny), k = (int)(rr / fd.ny);
+        int ii[2], jj[2], kk[2];
+        float wi[2], wj[2], wk[2];
+        ptaps2(i, cd.nx, ii, wi);
+        ptaps2(j, cd.ny, jj, wj);
+        int nk = 2;
+        if (a.dims == 3) ptaps2(k, cd.nz, kk, wk);
+        else { kk[0] = 0; wk[0] = 1.f; nk = 1; }
+        float acc = 0.f;
+        for (int b = 0; b < 2; ++b)
+            for (int q = 0; q < nk; ++q) {
+                const float *row = C.x + (long long)cd.nx * (jj[b] + (long long)cd.ny * kk[q]);
+                const float w = wj[b] * wk[q];
+                acc += (wi[0] * __ldcg(row + ii[0]) + wi[1] * __ldcg(row + ii[1])) * w;
+            }
+        F.x[c] = __ldcg(F.x + c) + acc;
+    }
+}
+
+// one colour pass on the coarsest level from the stored coefficients
+// (k_coarse_sweeps' arithmetic: x += sor (b - A x) / diag)
+__device__ void tail_coarse_colour(const TailArgs &a, const TailLevel &C, int col, long long t0, long long stride) {
+    const Dims d = C.g.d;
+    const long long sy = d.nx, sz = (long long)d.nx * d.ny, n = d.n();
+    float *x = C.x;
+    for (long long c = t0; c < n; c += stride) {
+        const int i = (int)(c % d.nx);
+        const long long rr = c / d.nx;
+        const int j = (int)(rr % d.ny), k = (int)(rr / d.ny);
+        if (((i + j + k) & 1) != col) continue;
+        const float xc = __ldcg(x + c);
+        const float4 kc = __ldg(C.coef + c);
+        float s = -kc.w * xc;
+        float D = -(kc.w + kc.x + kc.y + kc.z);
+        if (i > 0) s += kc.x * (__ldcg(x + c - 1) - xc);
+        if (i < d.nx - 1) { const float k1 = __ldg(&C.coef[c + 1].x); s += k1 * (__ldcg(x + c + 1) - xc); D -= k1; }
+        if (j > 0) s += kc.y * (__ldcg(x + c - sy) - xc);
+        if (j < d.ny - 1) { const float k1 = __ldg(&C.coef[c + sy].y); s += k1 * (__ldcg(x + c + sy) - xc); D -= k1; }
+        if (k > 0) s += kc.z * (__ldcg(x + c - sz) - xc);
+        if (k < d.nz - 1) { const float k1 = __ldg(&C.coef[c + sz].z); s += k1 * (__ldcg(x + c + sz) - xc); D -= k1; }
+        x[c] = xc + ((__ldcg(C.b + c) - s) / D) * a.sor;
+    }
+}
+
+__global__ void __launch_bounds__(TAIL_NT, 1) k_vcycle_tail(TailArgs a) {
+    PcgState *st = a.st;
+    if (st && (st->stop || st->err)) return;
+    unsigned *bar = a.bar;
+    unsigned passed = 0;
+    const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    bool ok = true;
+    // the coarse level's first colour-0 pass rides on the restriction into it
+    // (not into the coarsest level, which is solved directly or swept)
+    for (int l = 0; l < a.nl - 1 && ok; ++l) {
+        const TailLevel &L = a.lv[l];
+        const bool fused0 = l > 0 && a.down > 0;
+        for (int it = 0; it < a.down && ok; ++it) {
+            if (!(fused0 && it == 0)) {
+                tail_colour(a, L, 0, it == 0, t0, stride);
+                ok = tail_sync(bar, passed);
+                if (!ok) break;
+            }
+            tail_colour(a, L, 1, false, t0, stride);
+            ok = tail_sync(bar, passed);
+        }
+        if (!ok) break;
+        tail_residual(L, a.down == 0, t0, stride);
+        ok = tail_sync(bar, passed);
+        if (!ok) break;
+        tail_restrict(a, L, a.lv[l + 1], l + 1 < a.nl - 1 && a.down > 0, t0, stride);
+        ok = tail_sync(bar, passed);
+    }
+    if (ok) {
+        const TailLevel &C = a.lv[a.nl - 1];
+        if (a.coarse_sweeps > 0) {
+            for (long long c = t0; c < C.g.d.n(); c += stride) C.x[c] = 0.f;
+            ok = tail_sync(bar, passed);
+            for (int it = 0; it < a.coarse_sweeps && ok; ++it)
+                for (int col = 0; col < 2 && ok; ++col) {
+                    tail_coarse_colour(a, C, col, t0, stride);
+                    ok = tail_sync(bar, passed);
+                }
+        } else {
+            tail_direct(a, C);
+            ok = tail_sync(bar, passed);
+        }
+    }
+    for (int l = a.nl - 2; l >= 0 && ok; --l) {
+        const TailLevel &L = a.lv[l];
+        tail_prolong(a, a.lv[l + 1], L, t0, stride);
+        ok = tail_sync(bar, passed);
+        for (int it = 0; it < a.up && ok; ++it) {
+            tail_colour(a, L, 1, false, t0, stride);
+            ok = tail_sync(bar, passed);
+            if (!ok) break;
+            tail_colour(a, L, 0, false, t0, stride);
+            // the kernel's end orders the last pass before the next launch
+            if (!(l == 0 && it == a.up - 1)) ok = tail_sync(bar, passed);
+        }
+    }
+    if (ok) tail_done(bar);
+    else if (threadIdx.x == 0 && st) atomicOr(&st->err, 2);
+}
+
 // ----------------------------------------------------------- cell classes --
 // Two bits per cell, one byte per x-quad (rows `pitch` bytes apart): 0 an
 // interior cell whose six couplings are the plain h^-2 and E = 0; 1 a
@@ -2345,7 +2686,7 @@ int sweep_tma_maps(const Level &L, const float *x0, const float *x1, uint8_t *cl
 }
 
 int cell_classes(const Level &L, const SweepMaps &m, const uint8_t *bricks, int sm_count, cudaStream_t s) {
-    FF_CHECK(m.ok && m.cls_ptr, FF_E_STATE, "cell classes: maps not built");
+    FF_CHECK(m.cls_ptr && m.cls_pitch > 0, FF_E_STATE, "cell classes: class array not allocated");
     Geo g = make_geo(L);
     const int nq = L.d.nx / 4;
     dim3 grid((nq + 127) / 128, L.d.ny, L.d.nz);
@@ -2582,6 +2923,65 @@ int x_residual_tma(const Level &L0, const SweepMaps &sm, const CgMaps &m, float 
         else k_x_residual_tma<false, false><<<grid, tcg::NT, sh, s>>>(a, m.xh[0], m.xh[1], m.xl[0], m.xl[1], m.p[0], m.p[1], m.b, sm.cls);
     }
     return post("x_residual_tma");
+}
+
+
+size_t cls_row_pitch(const Dims &d) { return (size_t)cls_pitch(d); }
+
+int vcycle_tail(const Level *lv, const SweepMaps *sm, int nl, int dims, int down, int up, float sor,
+                const double *G, int nG, int coarse_sweeps, PcgState *st, unsigned *bar, int sm_count,
+                cudaStream_t s) {
+    FF_CHECK(nl >= 2 && nl <= TAIL_MAXL, FF_E_ARG, "coarse V-cycle: %d levels (2..%d)", nl, TAIL_MAXL);
+    FF_CHECK(bar, FF_E_ARG, "coarse V-cycle: no barrier words");
+    FF_CHECK(coarse_sweeps > 0 || (G && nG == lv[nl - 1].d.n()), FF_E_STATE, "coarse V-cycle: no coarsest inverse");
+    TailArgs a;
+    for (int l = 0; l < nl; ++l) {
+        TailLevel &t = a.lv[l];
+        const Level &L = lv[l];
+        t.g = make_geo(L);
+        t.x = (float *)L.x;
+        t.b = (float *)L.b;
+        t.r = (float *)L.buf;
+        t.coef = L.coef;
+        t.mask = L.mask;
+        t.rdreg_sor = sor / t.g.dreg;
+        if (l < nl - 1) {
+            FF_CHECK(sm[l].cls_ptr && sm[l].gco && L.buf, FF_E_STATE, "coarse V-cycle: level %d lacks classes", l);
+            t.cls = sm[l].cls_ptr;
+            t.cpitch = sm[l].cls_pitch;
+            t.gco = sm[l].gco;
+        } else {
+            t.cls = nullptr;
+            t.cpitch = 0;
+            t.gco = nullptr;
+        }
+    }
+    a.nl = nl;
+    a.down = down;
+    a.up = up;
+    a.dims = dims;
+    a.sor = sor;
+    a.omsor = 1.f - sor;
+    a.G = G;
+    a.nG = nG;
+    a.coarse_sweeps = coarse_sweeps;
+    a.st = st;
+    a.bar = bar;
+    static int per_sm = -1;
+    if (per_sm < 0) FF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vcycle_tail, TAIL_NT, 0));
+    FF_CHECK(per_sm >= 1, FF_E_CUDA, "coarse V-cycle kernel does not fit an SM");
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)sm_count);
+    cfg.blockDim = dim3(TAIL_NT);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    FF_CUDA(cudaLaunchKernelEx(&cfg, k_vcycle_tail, a));
+    return post("vcycle_tail");
 }
 
 }  // namespace ffk

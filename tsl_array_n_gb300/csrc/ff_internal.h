@@ -75,7 +75,7 @@ struct PcgState {
     int stop, iter, stop_iter, first;
     int maxiter, relative, p_cur, x_cur;
     int launched, bad_cells, growth_stop;
-    int err;   // nonzero: a kernel gave up on a bounded wait (bit 0: TMA staging)
+    int err;   // nonzero: a kernel gave up on a bounded wait (bit 0: TMA staging, bit 1: grid barrier)
     unsigned ticket[4];
 };
 
@@ -209,6 +209,14 @@ bool sweep_tma_ok(const Dims &d);
 size_t sweep_tma_cls_bytes(const Dims &d);
 int sweep_tma_maps(const Level &L, const float *x0, const float *x1, uint8_t *cls, SweepMaps &m);
 int cell_classes(const Level &L, const SweepMaps &m, const uint8_t *bricks, int sm_count, cudaStream_t s);
+size_t cls_row_pitch(const Dims &d);
+// the V-cycle from level lv[0] down to the coarsest lv[nl-1] and back, one
+// cooperative launch (coarse_sweeps > 0: sweeps instead of G b at the bottom)
+// bar: three words (arrivals, generation, abort), zero before the first
+// launch and after a failed one; st may be null (no stop or error flags)
+int vcycle_tail(const Level *lv, const SweepMaps *sm, int nl, int dims, int down, int up, float sor,
+                const double *G, int nG, int coarse_sweeps, PcgState *st, unsigned *bar, int sm_count,
+                cudaStream_t s);
 int cg_tma_maps(const Level &L0, const float *z0, const float *z1, const float *p0, const float *p1,
                 const float *xh0, const float *xl0, const float *xh1, const float *xl1, const float *b, bool ds,
                 CgMaps &m);

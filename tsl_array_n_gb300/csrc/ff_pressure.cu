@@ -57,6 +57,10 @@ struct ff_pressure_s {
     SweepMaps *smaps = nullptr;
     CgMaps cgm;              // level-0 CG operands for the TMA CG kernels
     bool use_tma = true;
+    // first level of the coarse V-cycle run as one cooperative launch (-1: none)
+    int tail_l = -1;
+    bool use_tail = true;
+    unsigned *tail_bar = nullptr;   // its grid barrier: arrivals, generation, abort
     // learned warm start (borrowed network), its guess field, last choice
     ff_unet net = nullptr;
     ff_field guess = nullptr;
@@ -246,6 +250,23 @@ extern "C" int ff_pressure3_create(ff_ctx ctx, const ff_pressure_desc *desc, ff_
             if ((st = ffk::sweep_tma_maps(v, (const float *)v.x, ps->x2[l], cls, ps->smaps[l]))) return bail(st);
             blocks = std::max(blocks, (long long)ffk::sweep_tma_blocks(v.d, ctx->sm_count));
         }
+        // the coarse V-cycle in one launch: from the first level of at most
+        // 64^3 cells (below level 0) whose levels down to the last but one
+        // all have nx % 4 == 0 (class bytes per x-quad) and a residual buffer
+        for (int l = 1; l < L - 1 && ps->tail_l < 0; ++l) {
+            if (ps->lv[l].d.n() > (1LL << 18)) continue;
+            bool ok = true;
+            for (int q = l; q < L - 1; ++q) ok = ok && ps->lv[q].d.nx % 4 == 0 && ps->lv[q].buf;
+            if (ok) ps->tail_l = l;
+        }
+        if (ps->tail_l >= 0 && (st = ff_dev_alloc((void **)&ps->tail_bar, 4 * sizeof(unsigned), s))) return bail(st);
+        for (int l = ps->tail_l; l >= 0 && l < L - 1; ++l) {
+            SweepMaps &m = ps->smaps[l];
+            if (m.cls_ptr) continue;
+            if ((st = ff_dev_alloc((void **)&m.cls_ptr, ffk::sweep_tma_cls_bytes(ps->lv[l].d), s))) return bail(st);
+            if ((st = ff_dev_alloc((void **)&m.gco, (size_t)ps->lv[l].d.n() * sizeof(float4), s))) return bail(st);
+            m.cls_pitch = (int)ffk::cls_row_pitch(ps->lv[l].d);
+        }
     }
     if ((st = ff_dev_alloc((void **)&ps->partials, (size_t)blocks * 2 * sizeof(double), s))) return bail(st);
     if (ps->smaps && ps->smaps[0].ok &&
@@ -269,6 +290,7 @@ extern "C" int ff_pressure3_destroy(ff_pressure ps) {
             ff_dev_free(ps->smaps[l].order);
         }
     delete[] ps->smaps;
+    ff_dev_free(ps->tail_bar);
     ff_field_destroy(ps->pressure);
     ff_field_destroy(ps->bfield);
     ff_field_destroy(ps->maskf);
@@ -360,6 +382,7 @@ extern "C" int ff_pressure3_set(ff_pressure ps, const char *key, double value) {
     else if (k == "checkBadCells") ps->check_bad = value != 0;
     else if (k == "useGraph") { ps->use_graph = value != 0; }
     else if (k == "useTma") { ps->use_tma = value != 0; destroy_graphs(ps); }
+    else if (k == "coarseTail") { ps->use_tail = value != 0; destroy_graphs(ps); }
     else if (k == "preconditioner") {
         FF_CHECK(value >= 0 && value <= 2, FF_E_ARG, "unknown preconditioner %g", value);
         ps->desc.preconditioner = (int)value;
@@ -446,12 +469,12 @@ static int prepare(ff_pressure ps, ff_field u, ff_field v, ff_field w) {
         }
         FF_TRY(ffk::build_coef(c, ps->dims, ps->vbf(), s));
         if (ps->bricks[l]) FF_TRY(ffk::brick_flags(c, ps->bricks[l], s));
-        if (ps->smaps && ps->smaps[l].ok)
+        if (ps->smaps && ps->smaps[l].cls_ptr)
             FF_TRY(ffk::cell_classes(c, ps->smaps[l], ps->bricks[l], ps->ctx->sm_count, s));
     }
     FF_TRY(ffk::build_coef(L0, ps->dims, ps->vbf(), s));
     if (ps->bricks[0]) FF_TRY(ffk::brick_flags(L0, ps->bricks[0], s));
-    if (ps->smaps && ps->smaps[0].ok)
+    if (ps->smaps && ps->smaps[0].cls_ptr)
         FF_TRY(ffk::cell_classes(L0, ps->smaps[0], ps->bricks[0], ps->ctx->sm_count, s));
     ps->prepared = true;
     // FP64 direct coarsest solve: refactor when the coarsest operator changed
@@ -577,6 +600,16 @@ static int vcycle_fused(ff_pressure ps, int l, PcgState *st, int rz_mode, float 
     float *bufs[2] = {(float *)v.x, ps->x2[l]};
     int cur = -1;   // -1: x is identically zero
     *rz_done = false;
+    const bool direct = ps->desc.mg_coarse_mode == FF_COARSE_DIRECT;
+    if (l == ps->tail_l && ps->use_tail && l > 0 && ps->tail_bar &&
+        (direct ? ps->G != nullptr : ps->desc.mg_coarsest > 0)) {
+        // this level and every coarser one in one cooperative launch
+        FF_TRY(ffk::vcycle_tail(&ps->lv[l], &ps->smaps[l], Ln - l, ps->dims, ps->desc.mg_down, ps->desc.mg_up, sor,
+                                direct ? ps->G : nullptr, direct ? ps->nG : 0, direct ? 0 : ps->desc.mg_coarsest, st,
+                                ps->tail_bar, ps->ctx->sm_count, s));
+        *out = (float *)v.x;
+        return FF_OK;
+    }
     if (l == Ln - 1) {
         if (ps->desc.mg_coarse_mode == FF_COARSE_DIRECT) {
             FF_TRY(ffk::mg_coarse_direct(v, ps->G, ps->nG, 0, 0, st, s));
@@ -663,6 +696,13 @@ static int precondition(ff_pressure ps, PcgState *st) {
 }
 
 // ------------------------------------------------------------------ solve --
+// clears the coarse V-cycle's barrier words (after a launch that gave up
+// they keep its arrivals and abort flag)
+static int reset_tail_bar(ff_pressure ps) {
+    if (ps->tail_bar) FF_CUDA(cudaMemsetAsync(ps->tail_bar, 0, 4 * sizeof(unsigned), ps->s()));
+    return FF_OK;
+}
+
 // the level-0 CG kernels run in the TMA layout when the sweep does
 static bool cg_tma(const ff_pressure ps) { return ps->use_tma && ps->cgm.ok && ps->smaps && ps->smaps[0].ok; }
 
@@ -670,6 +710,7 @@ static int enqueue_setup(ff_pressure ps) {
     const Dims &d = ps->d;
     cudaStream_t s = ps->s();
     FF_TRY(ffk::state_init(ps->st, ps->desc.tolerance, ps->maxiter, ps->desc.relative_tolerance, s));
+    FF_TRY(reset_tail_bar(ps));
     if (!ps->fused) {
         FF_TRY(ffk::cg_setup_residual(d, ps->lv[0].coef, (const float *)ps->bfield->d, ps->xh0(),
                                       ps->x_lo0, ps->r, ps->st, ps->partials, ps->ds(), s));
@@ -981,10 +1022,17 @@ extern "C" int ff_precondition_apply(ff_pressure ps, ff_field r, ff_field z) {
     FF_CHECK(r->count == ps->d.n() && z->count == ps->d.n(), FF_E_ARG, "field size mismatch");
     cudaStream_t s = ps->s();
     FF_CUDA(cudaMemcpyAsync(ps->r, r->d, r->bytes, cudaMemcpyDeviceToDevice, s));
+    FF_TRY(reset_tail_bar(ps));
     FF_TRY(precondition(ps, nullptr));
     long long n = ps->d.n();
     FF_CUDA(cudaMemcpyAsync(z->d, ps->z_final ? ps->z_final : ps->z, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
     FF_CUDA(cudaStreamSynchronize(s));
+    if (ps->tail_bar) {
+        // the coarse V-cycle's abort flag (this path has no solver state)
+        unsigned abort_flag = 0;
+        FF_CUDA(cudaMemcpy(&abort_flag, ps->tail_bar + 2, sizeof(unsigned), cudaMemcpyDeviceToHost));
+        FF_CHECK(abort_flag == 0, FF_E_CUDA, "coarse V-cycle: a grid barrier timed out");
+    }
     return FF_OK;
 }
 
@@ -1061,6 +1109,7 @@ extern "C" int ff_pressure3_profile(ff_pressure ps, int which, int reps, float *
     const int vb = ps->vbf();
     const bool nf = !ps->fused;   // profile the per-colour kernels when not fused
     // an NVTX range lets a profiler select exactly these launches
+    FF_TRY(reset_tail_bar(ps));
     nvtxRangePushA("ff_profile");
     for (int r = 0; r < reps; ++r) {
         FF_CUDA(cudaMemsetAsync(&ps->st->stop, 0, sizeof(int), s));

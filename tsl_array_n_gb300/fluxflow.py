@@ -349,7 +349,7 @@ class _Settings:
     """The runtime ``settings`` object (grid_pressure_solver3.js:135)."""
 
     _KEYS = {"tolerance", "maxIterations", "relativeTolerance", "checkBadCells", "useGraph",
-             "useTma", "preconditioner", "sorFactor"}
+             "useTma", "coarseTail", "preconditioner", "sorFactor"}
 
     def __init__(self, solver):
         object.__setattr__(self, "_s", solver)
