@@ -38,12 +38,15 @@ def kernel_bytes_per_cell(precision):
         return {"p_pAp": 4 + 4 + 16 + 4, "x_residual": xb + 4 + 4 + 16 + xb + 4,
                 "relax": 4 + 4 + 8 + 2, "residual": 4 + 4 + 8 + 2, "restrict": 2 + 0.25,
                 "prolong": 0.25 + 8, "rz": 8}
-    # fused path: regular bricks read no coefficients
+    # fused path: plain cells read no coefficients; the TMA kernels read one
+    # class byte per four cells
     return {
         "p_pAp": 4 + 4 + 4,                 # z, p -> p
         "x_residual": xb + 4 + 4 + xb + 4,  # x, p, b -> x, r
-        "relax": 4 + 4 + 4,                 # one full red-black sweep: x, b -> x
-        "residual": 4 + 4 + 0.5,            # fused residual+restriction: x, b -> coarse b
+        "relax": 4 + 4 + 4 + 0.25,          # one full red-black sweep: x, b, classes -> x
+        # residual with the x restriction taps (x, b, classes -> half-size
+        # rx), then the y/z taps (rx -> coarse b)
+        "residual": 4 + 4 + 0.25 + 2 + 2 + 0.5,
         "restrict": 4 + 0.5,
         "prolong": 0.5 + 8,
         "rz": 8,
