@@ -1887,23 +1887,24 @@ __device__ __forceinline__ float resid_scalar(const Geo &g, const float *__restr
 // One thread per fine x-quad: float4 loads of the quad's row, its y and z
 // neighbours and b; the residual at the cells just outside the quad comes
 // from the neighbouring lanes (same row), computed directly at warp edges.
-__global__ void __launch_bounds__(256) k_resid_rx(Geo g, const float *__restrict__ x, const float *__restrict__ b,
+// Block (32, 8): a warp holds 32 consecutive quads of one row; grid (quads
+// / 32, rows / 8, planes) so no index needs a division.
+__global__ void __launch_bounds__(256, 4) k_resid_rx(Geo g, const float *__restrict__ x, const float *__restrict__ b,
                                                   const float4 *__restrict__ coef, const uint8_t *__restrict__ cls,
                                                   int cpitch, float *__restrict__ rx, const PcgState *st) {
     if (st && st->stop) return;
     const int nq = g.d.nx >> 2, cnx = g.d.nx >> 1;
-    const long long n = (long long)nq * g.d.ny * g.d.nz;
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const bool valid = t < n;
-    const long long tt = valid ? t : n - 1;
-    const int qx = (int)(tt % nq);
-    const long long rr = tt / nq;
-    const int j = (int)(rr % g.d.ny), k = (int)(rr / g.d.ny);
+    const int j = blockIdx.y * 8 + threadIdx.y, k = blockIdx.z;
+    if (j >= g.d.ny) return;   // whole warps (a warp is one row segment)
+    const int qraw = blockIdx.x * 32 + threadIdx.x;
+    const bool valid = qraw < nq;
+    const int qx = valid ? qraw : nq - 1;
     const int i0 = 4 * qx;
     const long long row = g.sy * j + g.sz * k;
     const long long rym = row + (j > 0 ? -g.sy : 0), ryp = row + (j < g.d.ny - 1 ? g.sy : 0);
     const long long rzm = row + (k > 0 ? -g.sz : 0), rzp = row + (k < g.d.nz - 1 ? g.sz : 0);
     const uint8_t *crow = cls + (long long)cpitch * (j + (long long)g.d.ny * k);
+    const int lane = threadIdx.x;
     const float4 c = __ldg(reinterpret_cast<const float4 *>(x + row + i0));
     const float xl = i0 > 0 ? __ldg(x + row + i0 - 1) : c.x;
     const float xr = i0 + 4 < g.d.nx ? __ldg(x + row + i0 + 4) : c.w;
@@ -1926,7 +1927,6 @@ __global__ void __launch_bounds__(256) k_resid_rx(Geo g, const float *__restrict
         r3 = resid_cls(g, coef, (cq >> 6) & 3u, i0 + 3, j, k, bq.w, c.w, c.z, xr, ym.w, yp.w, zm.w, zp.w);
     }
     // r at i0-1 (left neighbour's r3) and i0+4 (right neighbour's r0)
-    const int lane = threadIdx.x & 31;
     float rl = __shfl_up_sync(0xffffffffu, r3, 1);
     float rh = __shfl_down_sync(0xffffffffu, r0, 1);
     if (!valid) return;
@@ -1971,6 +1971,50 @@ __global__ void k_restrict_yz(Dims fd, Dims cd, int dims, const float *__restric
     }
 }
 
+// The y and z taps for four consecutive coarse cells per thread (float4 rows
+// of rx and of the coarse b; needs the coarse nx % 4 == 0).  Block (32, 8),
+// grid (coarse nx / 128, coarse ny / 8, coarse nz).
+__global__ void __launch_bounds__(256) k_restrict_yz4(Dims fd, Dims cd, int dims, const float *__restrict__ rx,
+                                                      const uint8_t *__restrict__ cmask, float *__restrict__ cb,
+                                                      const PcgState *st) {
+    if (st && st->stop) return;
+    const int I = 4 * (blockIdx.x * 32 + threadIdx.x), J = blockIdx.y * 8 + threadIdx.y, K = blockIdx.z;
+    if (I >= cd.nx || J >= cd.ny) return;
+    int jy[4], kz[4];
+    rtap4(J, cd.ny, jy);
+    const float w4[4] = {0.125f, 0.375f, 0.375f, 0.125f};
+    int nzt = 4;
+    if (dims == 3) rtap4(K, cd.nz, kz);
+    else { kz[0] = K; nzt = 1; }
+    float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int q = 0; q < nzt; ++q) {
+        const float wz = dims == 3 ? w4[q] : 1.0f;
+        float4 part = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+            const float4 v =
+                __ldg(reinterpret_cast<const float4 *>(rx + I + (long long)cd.nx * (jy[p] + (long long)fd.ny * kz[q])));
+            part.x += v.x * w4[p];
+            part.y += v.y * w4[p];
+            part.z += v.z * w4[p];
+            part.w += v.w * w4[p];
+        }
+        s.x += part.x * wz;
+        s.y += part.y * wz;
+        s.z += part.z * wz;
+        s.w += part.w * wz;
+    }
+    const long long c = I + (long long)cd.nx * (J + (long long)cd.ny * K);
+    if (cmask) {
+        const uchar4 m = *reinterpret_cast<const uchar4 *>(cmask + c);
+        if (m.x) s.x = 0.f;
+        if (m.y) s.y = 0.f;
+        if (m.z) s.z = 0.f;
+        if (m.w) s.w = 0.f;
+    }
+    *reinterpret_cast<float4 *>(cb + c) = s;
+}
+
 // ------------------------------------------------------------ prolongation --
 // buildCorrectKernel (multigrid.js:990-1040) on FP32 levels with nx % 4 == 0:
 // x_f += P x_c, skipped on fine Dirichlet cells.  A thread owns an x-quad
@@ -1988,15 +2032,16 @@ __device__ __forceinline__ void ptaps2(int f, int nc, int *idx, float *w) {
     }
 }
 
-__global__ void k_prolong4(Dims fd, Dims cd, int dims, const float *__restrict__ coarse,
-                           const uint8_t *__restrict__ fmask, float *__restrict__ fine, const PcgState *st) {
+// Block (32, 8), grid (quads / 32, rows / 8, planes): one quad per thread.
+__global__ void __launch_bounds__(256) k_prolong4(Dims fd, Dims cd, int dims, const float *__restrict__ coarse,
+                                                  const uint8_t *__restrict__ fmask, float *__restrict__ fine,
+                                                  const PcgState *st) {
     if (st && st->stop) return;
     const int nq = fd.nx >> 2;
-    const long long n = (long long)nq * fd.ny * fd.nz;
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        const int qx = (int)(q % nq);
-        const long long r = q / nq;
-        const int j = (int)(r % fd.ny), k = (int)(r / fd.ny);
+    {
+        const int qx = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y, k = blockIdx.z;
+        if (qx >= nq || j >= fd.ny) return;
+        const long long q = qx + (long long)nq * (j + (long long)fd.ny * k);
         const int c1 = 2 * qx, c2 = 2 * qx + 1;
         const int c0 = c1 > 0 ? c1 - 1 : c1, c3 = c2 < cd.nx - 1 ? c2 + 1 : c2;
         int jj[2], kk[2];
@@ -2585,19 +2630,24 @@ int res_restrict2(const Level &f, const SweepMaps &m, const float *x, float *rx,
     FF_CHECK(m.ok && m.cls_ptr && f.d.nx % 4 == 0, FF_E_STATE, "res_restrict2 needs cell classes and nx %% 4 == 0");
     Geo g = make_geo(f);
     const long long nq = (long long)(f.d.nx / 4) * f.d.ny * f.d.nz;
-    k_resid_rx<<<(int)((nq + 255) / 256), 256, 0, s>>>(g, x, (const float *)f.b, f.coef, m.cls_ptr, m.cls_pitch, rx,
+    (void)nq;
+    k_resid_rx<<<dim3((f.d.nx / 4 + 31) / 32, (f.d.ny + 7) / 8, f.d.nz), dim3(32, 8), 0, s>>>(
+        g, x, (const float *)f.b, f.coef, m.cls_ptr, m.cls_pitch, rx,
                                                          st);
     const long long nc = c.d.n();
-    k_restrict_yz<<<(int)std::min<long long>((nc + 255) / 256, 152LL * 16), 256, 0, s>>>(f.d, c.d, dims, rx, c.mask,
-                                                                                          (float *)c.b, st);
+    if (c.d.nx % 4 == 0 && c.d.nx == f.d.nx / 2)
+        k_restrict_yz4<<<dim3((c.d.nx / 4 + 31) / 32, (c.d.ny + 7) / 8, c.d.nz), dim3(32, 8), 0, s>>>(
+            f.d, c.d, dims, rx, c.mask, (float *)c.b, st);
+    else
+        k_restrict_yz<<<(int)std::min<long long>((nc + 255) / 256, 152LL * 16), 256, 0, s>>>(f.d, c.d, dims, rx,
+                                                                                              c.mask, (float *)c.b, st);
     return post("res_restrict2");
 }
 
 int prolong4(const Level &c, const Level &f, int dims, float *fine_x, const PcgState *st, cudaStream_t s) {
     FF_CHECK(f.d.nx % 4 == 0, FF_E_ARG, "prolong4 needs nx %% 4 == 0");
-    const long long n = (long long)(f.d.nx / 4) * f.d.ny * f.d.nz;
-    const int nb = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
-    k_prolong4<<<nb, 256, 0, s>>>(f.d, c.d, dims, (const float *)c.x, f.mask, fine_x, st);
+    k_prolong4<<<dim3((f.d.nx / 4 + 31) / 32, (f.d.ny + 7) / 8, f.d.nz), dim3(32, 8), 0, s>>>(
+        f.d, c.d, dims, (const float *)c.x, f.mask, fine_x, st);
     return post("prolong4");
 }
 
