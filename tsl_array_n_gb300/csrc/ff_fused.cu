@@ -530,7 +530,7 @@ __global__ void __launch_bounds__(tq::NT, 3)
     k_sweep_tma(TqArgs a, const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap bmap,
                 const __grid_constant__ CUtensorMap cmap) {
     constexpr int TX = tq::TX, TY = tq::TY, QX = tq::QX, RW = tq::RW, SD = tq::SD, XS = tq::XS, BS = tq::BS;
-    constexpr int XPL = tq::XPL, BPL = tq::BPL, RING = tq::RING;
+    constexpr int XPL = tq::XPL, BPL = tq::BPL;
     constexpr unsigned XBYTES = tq::XBYTES, BBYTES = tq::BBYTES, CBYTES = tq::CBYTES;
     constexpr int CW = tq::CW, CPL = tq::CPL, CS = tq::CS;
     constexpr unsigned FULL = 0xffffffffu;
@@ -548,7 +548,7 @@ __global__ void __launch_bounds__(tq::NT, 3)
     const int qx = lane & (QX - 1), ty = 4 * (warp >> 1) + (warp & 1) + 2 * (lane >> 4);
     // the TMA issuer is the last thread, which has no ring cell
     constexpr int ISSUER = tq::NT - 1;
-    static_assert(ISSUER >= RING, "issuer carries no ring cell");
+    static_assert(ISSUER / 32 >= 3, "issuer carries no ring cell");
     // one block per work item (a tile column and a z-chunk of it), in the
     // order the work list gives
     const int item = a.order ? a.order[blockIdx.x] : (int)blockIdx.x;
@@ -560,6 +560,12 @@ __global__ void __launch_bounds__(tq::NT, 3)
     // x planes are read at z = -64 (entirely outside: zero fill) when the
     // input is identically zero
     auto xz = [&](int p) { return FIRST ? -64 : p; };
+    __shared__ float rdt[27];
+    if (tid < 27) {
+        const int mx = tid % 3, myy = (tid / 3) % 3, mz = tid / 9;
+        const float corr = g.h2x * (float)mx + g.h2y * (float)myy + g.h2z * (float)mz;
+        rdt[tid] = corr == 0.f ? a.rdreg_sor : a.sor / (g.dreg + corr);
+    }
     if (tid == ISSUER) {
         asm volatile("prefetch.tensormap [%0];" ::"l"(&xmap) : "memory");
         asm volatile("prefetch.tensormap [%0];" ::"l"(&bmap) : "memory");
@@ -599,38 +605,43 @@ __global__ void __launch_bounds__(tq::NT, 3)
     // h^-2 of the absent faces in y and in x (cells 0 and 3); planes strictly
     // inside in z use `inner`, the first and last plane add h^-2 in z (a
     // block-uniform branch)
-    const float cy = g.h2y * (float)((gj == 0) + (gj == g.d.ny - 1));
-    const float cx0 = gi == 0 ? g.h2x : 0.f, cx3 = gi + 3 == g.d.nx - 1 ? g.h2x : 0.f;
-    const QuadScale inner = quad_scale(g, a, cy, cx0, cx3, 0.f);
-    auto scale_at = [&](int k) {
-        const float cz = g.h2z * (float)((k == 0) + (k == g.d.nz - 1));
-        return cz == 0.f ? inner : quad_scale(g, a, cy, cx0, cx3, cz);
-    };
-    // this thread's ring cell (tid < RING): rows above and below the tile
-    // step along x, columns left and right step along y; the first-colour
-    // cell of each pair sits at offset (c + j0 + k + rpar) & 1
-    int rlx = 0, rly = 0, rpar = 0;
-    bool rrow = false;
-    if (tid < RING) {
-        int t = tid;
-        if (t < TX / 2 + 1) {
-            rly = -1; rlx = -1 + 2 * t; rpar = 0; rrow = true;
-        } else if ((t -= TX / 2 + 1) < TX / 2 + 1) {
-            rly = TY; rlx = -1 + 2 * t; rpar = TY + 1; rrow = true;
-        } else if ((t -= TX / 2 + 1) < TY / 2) {
-            rlx = -1; rly = 2 * t; rpar = 1;
-        } else {
-            t -= TY / 2;
-            rlx = TX; rly = 2 * t; rpar = TX;
-        }
-    }
+    // rdt[mx + 3 my + 9 mz] (written before the first barrier): sor over the
+    // diagonal of a plain cell with mx, my, mz faces across the domain edge
+    const int my = (gj == 0) + (gj == g.d.ny - 1);
+    const int mx0 = gi == 0, mx3 = gi + 3 == g.d.nx - 1;
+    const int mze = g.d.nz == 1 ? 2 : 1;   // faces across the edge on the first and last plane
+    QuadScale inner, zedge;
+    // the scales, from the table written before the first barrier
+    inner.r0 = rdt[mx0 + 3 * my];
+    inner.r12 = rdt[3 * my];
+    inner.r3 = rdt[mx3 + 3 * my];
+    zedge.r0 = rdt[mx0 + 3 * my + 9 * mze];
+    zedge.r12 = rdt[3 * my + 9 * mze];
+    zedge.r3 = rdt[mx3 + 3 * my + 9 * mze];
+    // the block-uniform choice of the first and last plane
+    auto scale_at = [&](int k) { return (k == 0 || k == g.d.nz - 1) ? zedge : inner; };
+    // The tile's halo ring on plane m+2 (its first colour, which the second
+    // colour on that plane reads two steps later): lanes 0..15 of warp 0 the
+    // row above the tile and of warp 1 the row below, as quads; lanes 0..15
+    // of warp 2 the cells left (lanes 0..7) and right (8..15) of the tile,
+    // one pair of rows each.
+    const int rrole = (lane < 16 && warp < 3) ? warp : -1;   // 0, 1 rows; 2 columns
+    const int rlrow = rrole == 0 ? -1 : TY;                    // ring rows: staged-row offset
+    const int rgi = i0 + 4 * lane, rgj = j0 + rlrow;
+    const bool rquad_in = rrole >= 0 && rrole < 2 && rgj >= 0 && rgj < g.d.ny && rgi < g.d.nx;
+    const int ro4 = (rlrow + 2) * RW + 4 + 4 * lane, rbo = (rlrow + 1) * RW + 4 + 4 * lane;
+    const int rco = (rlrow + 1) * CW + 16 + lane;
+    const int rmy = (rgj == 0) + (rgj == g.d.ny - 1), rmx0 = rgi == 0, rmx3 = rgi + 3 == g.d.nx - 1;
+    const int clx = (lane & 8) ? TX : -1, crow = 2 * (lane & 7);   // ring columns
+    const int cgi = i0 + clx;
+    const int cmx = (cgi == 0) + (cgi == g.d.nx - 1);
     // The thread's quad on planes m-1 .. m+2: q0 (plane m) and q1 carry the
     // first colour relaxed, q2 the values as staged; b of planes m and m+1;
     // the class bytes of planes m .. m+3 (bits 0-7 .. 24-31).
     const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
     float4 qm1 = zero4, q0 = zero4, q1 = zero4, q2 = zero4, bb0 = zero4, bb1 = zero4;
     unsigned cpipe = 0;
-    unsigned rcls = 0;   // class of this thread's ring cell on plane m+2
+    unsigned rcls = 0;   // class byte of this thread's ring quad or cell on plane m+2
     Acc acc;
     bool failed = false;
     for (int m = mstart; m < k1; ++m) {
@@ -675,32 +686,59 @@ __global__ void __launch_bounds__(tq::NT, 3)
                 }
                 if (quad_in) *reinterpret_cast<float4 *>(X2 + o) = q2;
             }
-            if (tid < RING) {
-                // the ring cell's class on plane m+3 (kept for the next step;
-                // its class-3 coefficient lines go to L1), then the ring cell
+            if (rrole == 0 || rrole == 1) {
+                // ring row quad: its class byte on plane m+3 (kept for the
+                // next step; class-3 lines go to L1), then the first colour
                 // on plane m+2
-                const int lxr0 = rlx + (rrow ? ((ca + j0 + ka + rpar) & 1) : 0);
-                const int lyr0 = rly + (rrow ? 0 : ((ca + j0 + ka + rpar) & 1));
-                const int lxr1 = rlx + (rrow ? ((ca + j0 + kp + rpar) & 1) : 0);
-                const int lyr1 = rly + (rrow ? 0 : ((ca + j0 + kp + rpar) & 1));
-                if (m == mstart) rcls = (cs[(lyr0 + 1) * CW + 16 + (lxr0 >> 2)] >> (2 * (lxr0 & 3))) & 3u;
-                const unsigned rnext = (C3[(lyr1 + 1) * CW + 16 + (lxr1 >> 2)] >> (2 * (lxr1 & 3))) & 3u;
-                const int pi = i0 + lxr1, pj = j0 + lyr1;
-                if (rnext == 3u && pi >= 0 && pi < g.d.nx && pj >= 0 && pj < g.d.ny && kp < g.d.nz) {
-                    const long long off = pi + g.sy * pj + g.sz * kp;
+                if (m == mstart) rcls = cs[rco];
+                const unsigned rnext = C3[rco];
+                if (rquad_in && any_general(rnext) && kp < g.d.nz) {
+                    const long long off = rgi + g.sy * rgj + g.sz * kp;
                     prefetch_l1(a.coef + off);
                     prefetch_l1(a.gco + off);
                 }
-                const int ri = i0 + lxr0, rj = j0 + lyr0;
-                if (ka >= 0 && ka <= k1 && ka < g.d.nz && ri >= 0 && ri < g.d.nx && rj >= 0 && rj < g.d.ny) {
-                    const int ro = (lyr0 + 2) * RW + lxr0 + 4;
-                    const float xc = X2[ro];
-                    const float bval = Bn[(lyr0 + 1) * RW + lxr0 + 4];
-                    const float corr = g.h2x * (float)((ri == 0) + (ri == g.d.nx - 1)) +
-                                       g.h2y * (float)((rj == 0) + (rj == g.d.ny - 1)) +
-                                       g.h2z * (float)((ka == 0) + (ka == g.d.nz - 1));
-                    X2[ro] = relax_any(g, a, rcls, ri + g.sy * rj + g.sz * ka, xc, X2[ro - 1], X2[ro + 1],
-                                       X2[ro - RW], X2[ro + RW], X1[ro], X3[ro], bval, plain_scale(g, a, corr));
+                if (ka >= 0 && ka <= k1 && ka < g.d.nz && rgj >= 0 && rgj < g.d.ny) {
+                    float4 rq = lds4(X2 + ro4);
+                    const float4 rym = lds4(X2 + ro4 - RW), ryp = lds4(X2 + ro4 + RW);
+                    const float4 rzm = lds4(X1 + ro4), rzp = lds4(X3 + ro4), rbq = lds4(Bn + rbo);
+                    const int mz = (ka == 0 || ka == g.d.nz - 1) ? 9 * mze : 0;
+                    QuadScale re;
+                    re.r0 = rdt[rmx0 + 3 * rmy + mz];
+                    re.r12 = rdt[3 * rmy + mz];
+                    re.r3 = rdt[rmx3 + 3 * rmy + mz];
+                    constexpr unsigned HALF = 0x0000ffffu;
+                    if ((ca ^ rgj ^ ka) & 1) {
+                        float sv = __shfl_down_sync(HALF, rq.x, 1);
+                        if (lane == QX - 1) sv = X2[ro4 + 4];
+                        if (rquad_in) relax_pair<1>(g, a, rq, sv, rym, ryp, rzm, rzp, rbq, rcls, re, rgi, rgj, ka);
+                    } else {
+                        float sv = __shfl_up_sync(HALF, rq.w, 1);
+                        if (lane == 0) sv = X2[ro4 - 1];
+                        if (rquad_in) relax_pair<0>(g, a, rq, sv, rym, ryp, rzm, rzp, rbq, rcls, re, rgi, rgj, ka);
+                    }
+                    if (rquad_in) *reinterpret_cast<float4 *>(X2 + ro4) = rq;
+                }
+                rcls = rnext;
+            } else if (rrole == 2) {
+                // ring column cell: rows crow, crow+1, the first colour's one
+                const int sh0 = (ca + j0 + ka + clx + crow) & 1, sh1 = (ca + j0 + kp + clx + crow) & 1;
+                const int ly0 = crow + sh0, ly1 = crow + sh1;
+                const int byt = (clx >> 2) + 16, bit = 2 * (clx & 3);
+                if (m == mstart) rcls = (cs[(ly0 + 1) * CW + byt] >> bit) & 3u;
+                const unsigned rnext = (C3[(ly1 + 1) * CW + byt] >> bit) & 3u;
+                const bool col_in = cgi >= 0 && cgi < g.d.nx;
+                if (rnext == 3u && col_in && j0 + ly1 < g.d.ny && kp < g.d.nz) {
+                    const long long off = cgi + g.sy * (j0 + ly1) + g.sz * kp;
+                    prefetch_l1(a.coef + off);
+                    prefetch_l1(a.gco + off);
+                }
+                const int rj = j0 + ly0;
+                if (ka >= 0 && ka <= k1 && ka < g.d.nz && col_in && rj < g.d.ny) {
+                    const int ro = (ly0 + 2) * RW + clx + 4;
+                    const int mz = (ka == 0 || ka == g.d.nz - 1) ? 9 * mze : 0;
+                    const float rd = rdt[cmx + 3 * ((rj == 0) + (rj == g.d.ny - 1)) + mz];
+                    X2[ro] = relax_any(g, a, rcls, cgi + g.sy * rj + g.sz * ka, X2[ro], X2[ro - 1], X2[ro + 1],
+                                       X2[ro - RW], X2[ro + RW], X1[ro], X3[ro], Bn[(ly0 + 1) * RW + clx + 4], rd);
                 }
                 rcls = rnext;
             }
@@ -923,9 +961,9 @@ __global__ void __launch_bounds__(tcg::NT, 4)
     const int o = (ty + 1) * RW + 4 + lx;
     const int co = (ty + 1) * CW + 16 + qx;
     const long long qoff = gi + g.sy * gj;
-    // halo quads of the new p: rows j0-1 and j0+TY, one on each of lanes 0..3
-    const int hq = warp * 4 + lane;
-    const int ho = (hq < QX ? 0 : tcg::PR - 1) * RW + 4 + 4 * (hq & (QX - 1));
+    // halo quads of the new p: rows j0-1 and j0+TY on lanes 0..15 of warps 0 and 1
+    const bool halo = warp < 2 && lane < QX;   // warp 0: row j0-1, warp 1: row j0+TY (16 quads each)
+    const int ho = (warp == 0 ? 0 : tcg::PR - 1) * RW + 4 + 4 * (lane & (QX - 1));
     const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
     float4 pm1 = zero4, p0 = zero4;   // new p on planes k-1 and k
     unsigned ck = 0;                  // class byte of plane k
@@ -946,7 +984,7 @@ __global__ void __launch_bounds__(tcg::NT, 4)
             const float4 zq = lds4(Z + o);
             p1 = first ? zq : fma4(beta, lds4(Po + o), zq);
             st4(N1 + o, p1);
-            if (lane < 4) {
+            if (halo) {
                 const float4 zh = lds4(Z + ho);
                 st4(N1 + ho, first ? zh : fma4(beta, lds4(Po + ho), zh));
             }
@@ -1167,8 +1205,8 @@ __global__ void __launch_bounds__(tcg::NT, 2)
     const int o = (ty + 1) * RW + 4 + lx, bo = ty * RW + 4 + lx;
     const int co = (ty + 1) * CW + 16 + qx;
     const long long qoff = gi + g.sy * gj;
-    const int hq = warp * 4 + lane;
-    const int ho = (hq < QX ? 0 : tcg::PR - 1) * RW + 4 + 4 * (hq & (QX - 1));
+    const bool halo = warp < 2 && lane < QX;   // warp 0: row j0-1, warp 1: row j0+TY (16 quads each)
+    const int ho = (warp == 0 ? 0 : tcg::PR - 1) * RW + 4 + 4 * (lane & (QX - 1));
     const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
     // x (hi, lo) on planes k-1 and k, b on plane k
     float4 hm1 = zero4, lm1 = zero4, h0 = zero4, l0 = zero4, b0 = zero4;
@@ -1221,7 +1259,7 @@ __global__ void __launch_bounds__(tcg::NT, 2)
             form4(H, L, Q, o, h1, l1);
             st4(NH1 + o, h1);
             if (DS) st4(NL1 + o, l1);
-            if (lane < 4) {
+            if (halo) {
                 float4 hh, hl;
                 form4(H, L, Q, ho, hh, hl);
                 st4(NH1 + ho, hh);
