@@ -366,8 +366,10 @@ __global__ void k_system_weights(long long n, const float *fw, const float *cw, 
 }
 
 // dispatchBuildSystem (:350-453)
-__global__ void k_build_system(Dims d, float hx, float hy, float hz, const float *u,
-                               const float *v, const float *w, const float *cwu,
+// ihx, ihy, ihz: (float)(1 / (double)h^2) per axis, formed once on the host
+// (FP64 arithmetic per cell would dominate the kernel on this part)
+__global__ void k_build_system(Dims d, float hx, float hy, float hz, float ihx, float ihy, float ihz,
+                               const float *u, const float *v, const float *w, const float *cwu,
                                const float *cwv, const float *cww, const float *swu,
                                const float *swv, const float *sww, const uint8_t *mask,
                                const float *tgt, float *b, float *xh, float *xl) {
@@ -401,8 +403,6 @@ __global__ void k_build_system(Dims d, float hx, float hy, float hz, const float
         if (xl) xl[q.c] = 0.f;
         return;
     }
-    const float ihx = (float)(1.0 / ((double)hx * hx)), ihy = (float)(1.0 / ((double)hy * hy)),
-                ihz = (float)(1.0 / ((double)hz * hz));
     float acc = 0.f;
     if (q.i > 0 && mask[q.c - 1]) acc += (swu ? swu[fu] : 1.f) * tgt[q.c - 1] * ihx;
     if (q.i < d.nx - 1 && mask[q.c + 1]) acc += (swu ? swu[fu + 1] : 1.f) * tgt[q.c + 1] * ihx;
@@ -518,7 +518,9 @@ int build_system(Dims d, float hx, float hy, float hz, const float *u, const flo
                  cudaStream_t s) {
     (void)fw;
     auto L = launch3(d.nx, d.ny, d.nz);
-    k_build_system<<<L.grid, L.block, 0, s>>>(d, hx, hy, hz, u, v, w, cw[0], cw[1], cw[2],
+    const float ihx = (float)(1.0 / ((double)hx * hx)), ihy = (float)(1.0 / ((double)hy * hy)),
+                ihz = (float)(1.0 / ((double)hz * hz));
+    k_build_system<<<L.grid, L.block, 0, s>>>(d, hx, hy, hz, ihx, ihy, ihz, u, v, w, cw[0], cw[1], cw[2],
                                               sw[0], sw[1], sw[2], mask, tgt, b, x_hi, x_lo);
     return post("build_system");
 }
