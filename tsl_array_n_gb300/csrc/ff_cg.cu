@@ -450,28 +450,46 @@ __global__ void k_commit(long long n, float *xh0, float *xl0, const float *xh1,
 
 // dispatchCorrectU/V/W (:457-494): interior faces only, gated by the
 // collider weight, scaled by the face weight (beta).
-__global__ void k_correct_axis(Dims d, int axis, float h, const float *xh, const float *xl,
-                               const float *fw, const float *cw, const float *in, float *out) {
-    int fx = d.nx + (axis == 0), fy = d.ny + (axis == 1);
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y * blockDim.y + threadIdx.y;
-    int k = blockIdx.z;
-    if (i >= fx || j >= fy) return;
-    int m = axis == 0 ? i : axis == 1 ? j : k;
-    int nm = axis == 0 ? d.nx : axis == 1 ? d.ny : d.nz;
-    long long f = i + (long long)fx * (j + (long long)fy * k);
-    if (m <= 0 || m >= nm) {
-        if (in != out) out[f] = in[f];
-        return;
+// All axes of the correction in one pass: thread (i, j, k) over
+// [0, nx] x [0, ny] x [0, nz] takes the u, v and w faces indexed (i, j, k)
+// that exist (p difference over h, times the face weight, zero where the
+// collider weight is zero; boundary faces copied); the pressure at cell
+// (i, j, k) is read once for the three.
+__global__ void k_correct3(Dims d, int naxes, float hx, float hy, float hz, const float *xh, const float *xl,
+                           const float *fwu, const float *fwv, const float *fww, const float *cwu,
+                           const float *cwv, const float *cww, const float *uin, const float *vin,
+                           const float *win, float *uout, float *vout, float *wout) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i > d.nx || j > d.ny) return;
+    const bool cell_in = i < d.nx && j < d.ny && k < d.nz;
+    const long long c = i + (long long)d.nx * (j + (long long)d.ny * k);
+    float pc = 0.f;
+    if (cell_in) {
+        pc = xh[c];
     }
-    long long c = i + (long long)d.nx * (j + (long long)d.ny * k);
-    long long off = axis == 0 ? 1 : axis == 1 ? d.nx : (long long)d.nx * d.ny;
-    float dp = xh[c] - xh[c - off];
-    if (xl) dp += xl[c] - xl[c - off];
-    float g = dp / h;
-    if (fw) g = g * fw[f];
-    if (cw) g = g * (cw[f] > 0.f ? 1.f : 0.f);
-    out[f] = in[f] - g;
+    const float pcl = (cell_in && xl) ? xl[c] : 0.f;
+    // one face: m its index along the axis, nm the cells along it
+    auto face = [&](int m, int nm, long long f, long long off, float h, const float *fw, const float *cw,
+                    const float *in, float *out) {
+        if (m <= 0 || m >= nm) {
+            if (in != out) out[f] = in[f];
+            return;
+        }
+        float dp = pc - xh[c - off];
+        if (xl) dp += pcl - xl[c - off];
+        float g = dp / h;
+        if (fw) g = g * fw[f];
+        if (cw) g = g * (cw[f] > 0.f ? 1.f : 0.f);
+        out[f] = in[f] - g;
+    };
+    if (j < d.ny && k < d.nz)
+        face(i, d.nx, i + (long long)(d.nx + 1) * (j + (long long)d.ny * k), 1, hx, fwu, cwu, uin, uout);
+    if (i < d.nx && k < d.nz)
+        face(j, d.ny, i + (long long)d.nx * (j + (long long)(d.ny + 1) * k), d.nx, hy, fwv, cwv, vin, vout);
+    if (naxes == 3 && i < d.nx && j < d.ny)
+        face(k, d.nz, c, (long long)d.nx * d.ny, hz, fww, cww, win, wout);
 }
 
 }  // namespace
@@ -540,14 +558,12 @@ int count_bad_and_commit(Dims d, float *x_hi0, float *x_lo0, float *x_hi1, float
 int correct(Dims d, float hx, float hy, float hz, const float *x_hi, const float *x_lo,
             const float *fw[3], const float *cw[3], const float *uin, const float *vin,
             const float *win, float *uout, float *vout, float *wout, cudaStream_t s) {
-    const float hs[3] = {hx, hy, hz};
     const float *ins[3] = {uin, vin, win};
     float *outs[3] = {uout, vout, wout};
-    int naxes = d.nz > 1 ? 3 : 2;
-    for (int a = 0; a < naxes; ++a) {
-        auto L = launch3(d.nx + (a == 0), d.ny + (a == 1), d.nz + (a == 2));
-        k_correct_axis<<<L.grid, L.block, 0, s>>>(d, a, hs[a], x_hi, x_lo, fw[a], cw[a], ins[a], outs[a]);
-    }
+    const int naxes = d.nz > 1 ? 3 : 2;
+    auto L = launch3(d.nx + 1, d.ny + 1, d.nz + (naxes == 3 ? 1 : 0));
+    k_correct3<<<L.grid, L.block, 0, s>>>(d, naxes, hx, hy, hz, x_hi, x_lo, fw[0], fw[1], fw[2], cw[0], cw[1],
+                                          cw[2], ins[0], ins[1], ins[2], outs[0], outs[1], outs[2]);
     return post("correct");
 }
 

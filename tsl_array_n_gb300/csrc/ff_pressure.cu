@@ -428,8 +428,13 @@ static int prepare(ff_pressure ps, ff_field u, ff_field v, ff_field w) {
     ps->has_w = fw[0] || cw[0];
     float *sw[3] = {nullptr, nullptr, nullptr};
     if (ps->has_w) {
-        for (int a = 0; a < ps->dims; ++a) sw[a] = ps->sw[a];
-        FF_TRY(ffk::system_weights(d, fw, cw, sw, s));
+        if (fw[0] && cw[0]) {
+            for (int a = 0; a < ps->dims; ++a) sw[a] = ps->sw[a];
+            FF_TRY(ffk::system_weights(d, fw, cw, sw, s));
+        } else {
+            // one factor only: the system weights are those arrays themselves
+            for (int a = 0; a < ps->dims; ++a) sw[a] = (float *)(fw[0] ? fw[a] : cw[a]);
+        }
     }
     // dispatchBuildSystem (:429-453); pins p at Dirichlet cells
     if (u) {
