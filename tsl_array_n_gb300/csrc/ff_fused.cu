@@ -2692,12 +2692,13 @@ int prolong4(const Level &c, const Level &f, int dims, float *fine_x, const PcgS
 // ---- TMA sweep
 bool sweep_tma_ok(const Dims &d) { return d.nx % 4 == 0 && d.nx >= 32; }
 
-static int tma_zchunk(const Dims &d, int sm_count) {
-    // About two waves of 3 blocks per SM when the z-chunks stay at 12 planes
-    // or more (the work order then starts the expensive items first and the
-    // cheap ones fill in behind them), else one wave; at least 4 planes.
+static int tma_zchunk_bps(const Dims &d, int sm_count, int bps) {
+    // About two waves of resident blocks (bps per SM) when the z-chunks stay
+    // at 12 planes or more (the work order then starts the expensive items
+    // first and the cheap ones fill in behind them), else one wave; at
+    // least 4 planes.
     long long cols = (long long)((d.nx + tq::TX - 1) / tq::TX) * ((d.ny + tq::TY - 1) / tq::TY);
-    long long wave = 3LL * sm_count;
+    long long wave = (long long)bps * sm_count;
     int c2 = (int)std::max(1LL, std::min((long long)d.nz, 2 * wave / cols));
     int zc = (d.nz + c2 - 1) / c2;
     if (zc < 12) {
@@ -2705,6 +2706,15 @@ static int tma_zchunk(const Dims &d, int sm_count) {
         zc = (d.nz + c1 - 1) / c1;
     }
     return std::min(std::max(zc, std::min(4, d.nz)), tq::MAXZC);
+}
+// the sweep: three blocks per SM
+static int tma_zchunk(const Dims &d, int sm_count) { return tma_zchunk_bps(d, sm_count, 3); }
+// the CG kernels: p.Ap four blocks per SM, x + alpha p with b - A x two
+static int cg_bps(int which) { return which == 0 ? 4 : 2; }
+
+size_t cg_tma_items(const Dims &d, int sm_count, int which) {
+    const int zc = tma_zchunk_bps(d, sm_count, cg_bps(which));
+    return (size_t)((d.nx + tq::TX - 1) / tq::TX) * ((d.ny + tq::TY - 1) / tq::TY) * ((d.nz + zc - 1) / zc);
 }
 
 size_t sweep_tma_blocks(const Dims &d, int sm_count) {
@@ -2781,12 +2791,16 @@ int cell_classes(const Level &L, const SweepMaps &m, const uint8_t *bricks, int 
     FF_CHECK(m.gco, FF_E_STATE, "cell classes: coefficient array not allocated");
     k_cell_classes<<<grid, 128, 0, s>>>(g, L.coef, m.cls_ptr, m.cls_pitch, m.gco);
     FF_TRY(post("cell_classes"));
-    if (m.order) {
-        const int zc = tma_zchunk(L.d, sm_count);
+    // work orders: the sweep's, and on level 0 those of the two CG kernels
+    // (their own z-chunks for their own blocks per SM)
+    for (int w = 0; w < 3; ++w) {
+        int *order = w == 0 ? m.order : w == 1 ? m.order_pap : m.order_xr;
+        if (!order) continue;
+        const int zc = w == 0 ? tma_zchunk(L.d, sm_count) : tma_zchunk_bps(L.d, sm_count, cg_bps(w - 1));
         const int gx = (L.d.nx + tq::TX - 1) / tq::TX, gy = (L.d.ny + tq::TY - 1) / tq::TY;
         const int gz = (L.d.nz + zc - 1) / zc;
         FF_CHECK((long long)gx * gy * gz <= 1024LL * 32, FF_E_ARG, "sweep work order: too many items");
-        k_sweep_order<<<1, 1024, 0, s>>>(g, bricks, gx, gy, gz, zc, m.order);
+        k_sweep_order<<<1, 1024, 0, s>>>(g, bricks, gx, gy, gz, zc, order);
         FF_TRY(post("sweep_order"));
     }
     return FF_OK;
@@ -2963,15 +2977,16 @@ int cg_tma_maps(const Level &L0, const float *z0, const float *z1, const float *
     return FF_OK;
 }
 
-static TcgArgs tcg_args(const Level &L0, const SweepMaps &sm, int sm_count) {
+// which: 0 p.Ap, 1 x + alpha p with b - A x
+static TcgArgs tcg_args(const Level &L0, const SweepMaps &sm, int sm_count, int which) {
     TcgArgs a;
     a.g = make_geo(L0);
     a.coef = L0.coef;
     a.gco = sm.gco;
-    a.order = sm.order;
+    a.order = which == 0 ? sm.order_pap : sm.order_xr;
     a.gx = (L0.d.nx + tcg::TX - 1) / tcg::TX;
     a.gy = (L0.d.ny + tcg::TY - 1) / tcg::TY;
-    a.zc = tma_zchunk(L0.d, sm_count);
+    a.zc = tma_zchunk_bps(L0.d, sm_count, cg_bps(which));
     return a;
 }
 
@@ -2980,7 +2995,7 @@ int p_pap_tma(const Level &L0, const SweepMaps &sm, const CgMaps &m, const float
     FF_CHECK(sm.ok && m.ok, FF_E_STATE, "TMA CG maps not built");
     const int zi = z == m.zp[0] ? 0 : z == m.zp[1] ? 1 : -1;
     FF_CHECK(zi >= 0, FF_E_STATE, "p.Ap: z is in neither sweep buffer");
-    TcgArgs a = tcg_args(L0, sm, sm_count);
+    TcgArgs a = tcg_args(L0, sm, sm_count, 0);
     a.p0 = p0;
     a.p1 = p1;
     a.st = st;
@@ -2993,7 +3008,7 @@ int p_pap_tma(const Level &L0, const SweepMaps &sm, const CgMaps &m, const float
 int x_residual_tma(const Level &L0, const SweepMaps &sm, const CgMaps &m, float *xh0, float *xl0, float *xh1,
                    float *xl1, float *r, PcgState *st, double *partials, int setup, int sm_count, cudaStream_t s) {
     FF_CHECK(sm.ok && m.ok, FF_E_STATE, "TMA CG maps not built");
-    TcgArgs a = tcg_args(L0, sm, sm_count);
+    TcgArgs a = tcg_args(L0, sm, sm_count, 1);
     a.xh0 = xh0;
     a.xl0 = xl0;
     a.xh1 = xh1;

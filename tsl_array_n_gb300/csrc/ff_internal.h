@@ -114,6 +114,8 @@ struct SweepMaps {
     // work order of the sweep's blocks (tile columns x z-chunks, those with
     // non-plain cells first)
     int *order = nullptr;
+    // level 0: the work orders of the two TMA CG kernels
+    int *order_pap = nullptr, *order_xr = nullptr;
     bool ok = false;
 };
 
@@ -227,6 +229,8 @@ int x_residual_tma(const Level &L0, const SweepMaps &sm, const CgMaps &m, float 
 int sweep_tma(const Level &L, const SweepMaps &m, const uint8_t *bricks, int in, int colour_a, float sor,
               PcgState *st, double *partials, int rz_mode, int sm_count, cudaStream_t s);
 size_t sweep_tma_blocks(const Dims &d, int sm_count);
+// work items of the level-0 TMA CG kernels (which: 0 p.Ap, 1 x + alpha p)
+size_t cg_tma_items(const Dims &d, int sm_count, int which);
 int res_restrict(const Level &f, const uint8_t *bricks, const float *x, Level &c, int dims,
                  const PcgState *st, int sm_count, cudaStream_t s);
 int fused_p_pap(const Level &L0, const uint8_t *bricks, const float *z, float *p0, float *p1,

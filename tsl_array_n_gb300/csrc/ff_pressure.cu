@@ -247,6 +247,14 @@ extern "C" int ff_pressure3_create(ff_ctx ctx, const ff_pressure_desc *desc, ff_
             if ((st = ff_dev_alloc((void **)&order, ffk::sweep_tma_blocks(v.d, ctx->sm_count) * sizeof(int), s)))
                 return bail(st);
             ps->smaps[l].order = order;
+            if (l == 0) {
+                for (int w = 0; w < 2; ++w) {
+                    const size_t items = ffk::cg_tma_items(v.d, ctx->sm_count, w);
+                    if ((st = ff_dev_alloc((void **)&order, items * sizeof(int), s))) return bail(st);
+                    (w == 0 ? ps->smaps[l].order_pap : ps->smaps[l].order_xr) = order;
+                    blocks = std::max(blocks, (long long)items);
+                }
+            }
             if ((st = ffk::sweep_tma_maps(v, (const float *)v.x, ps->x2[l], cls, ps->smaps[l]))) return bail(st);
             blocks = std::max(blocks, (long long)ffk::sweep_tma_blocks(v.d, ctx->sm_count));
         }
@@ -288,6 +296,8 @@ extern "C" int ff_pressure3_destroy(ff_pressure ps) {
             ff_dev_free(ps->smaps[l].cls_ptr);
             ff_dev_free(ps->smaps[l].gco);
             ff_dev_free(ps->smaps[l].order);
+            ff_dev_free(ps->smaps[l].order_pap);
+            ff_dev_free(ps->smaps[l].order_xr);
         }
     delete[] ps->smaps;
     ff_dev_free(ps->tail_bar);
