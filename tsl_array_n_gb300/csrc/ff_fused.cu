@@ -2465,8 +2465,8 @@ __global__ void __launch_bounds__(TAIL_NT, 1) k_vcycle_tail(TailArgs a) {
 // couplings (zero across the edge); 3 anything else.
 __global__ void k_cell_classes(Geo g, const float4 *__restrict__ coef, uint8_t *cls, int pitch, float4 *gco) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y, k = blockIdx.z;
-    if (4 * q >= g.d.nx) return;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    if (4 * q >= g.d.nx || j >= g.d.ny) return;
     unsigned byte = 0;
 #pragma unroll
     for (int d = 0; d < 4; ++d) {
@@ -2787,9 +2787,11 @@ int cell_classes(const Level &L, const SweepMaps &m, const uint8_t *bricks, int 
     FF_CHECK(m.cls_ptr && m.cls_pitch > 0, FF_E_STATE, "cell classes: class array not allocated");
     Geo g = make_geo(L);
     const int nq = L.d.nx / 4;
-    dim3 grid((nq + 127) / 128, L.d.ny, L.d.nz);
+    // blocks of (quads of a row rounded up to a warp, at most 128) x rows
+    const int bx = std::min(128, (nq + 31) / 32 * 32), by = 256 / bx;
+    dim3 grid((nq + bx - 1) / bx, (L.d.ny + by - 1) / by, L.d.nz);
     FF_CHECK(m.gco, FF_E_STATE, "cell classes: coefficient array not allocated");
-    k_cell_classes<<<grid, 128, 0, s>>>(g, L.coef, m.cls_ptr, m.cls_pitch, m.gco);
+    k_cell_classes<<<grid, dim3(bx, by), 0, s>>>(g, L.coef, m.cls_ptr, m.cls_pitch, m.gco);
     FF_TRY(post("cell_classes"));
     // work orders: the sweep's, and on level 0 those of the two CG kernels
     // (their own z-chunks for their own blocks per SM)
