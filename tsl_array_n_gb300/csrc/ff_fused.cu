@@ -382,6 +382,11 @@ struct TqArgs {
 };
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+// Kernels launched with programmatic stream serialization may start while
+// the previous kernel drains; this waits until it has completed and its
+// writes are visible (a no-op for an ordinary launch).  Every such kernel
+// calls it before its first global-memory access.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
     unsigned long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -534,6 +539,7 @@ __global__ void __launch_bounds__(tq::NT, 3)
     constexpr unsigned XBYTES = tq::XBYTES, BBYTES = tq::BBYTES, CBYTES = tq::CBYTES;
     constexpr int CW = tq::CW, CPL = tq::CPL, CS = tq::CS;
     constexpr unsigned FULL = 0xffffffffu;
+    pdl_wait();
     if (a.st && a.rz_mode != 2 && (a.st->stop || a.st->err)) return;
     extern __shared__ __align__(16) unsigned char dyn_raw[];
     // 128-byte alignment by pointer arithmetic on the shared array (keeps the
@@ -917,6 +923,7 @@ __global__ void __launch_bounds__(tcg::NT, 4)
     constexpr int TX = tcg::TX, TY = tcg::TY, QX = tcg::QX, RW = tcg::RW, PPL = tcg::PPL, CW = tcg::CW;
     constexpr int CPL = tcg::CPL, SD = tcg::PSD;
     constexpr unsigned PBYTES = tcg::PBYTES, CBYTES = tcg::CBYTES, FULL = 0xffffffffu;
+    pdl_wait();
     PcgState *st = a.st;
     if (st->stop || st->err) return;
     extern __shared__ __align__(16) unsigned char dyn_raw[];
@@ -1157,6 +1164,7 @@ __global__ void __launch_bounds__(tcg::NT, 2)
     constexpr int TX = tcg::TX, TY = tcg::TY, QX = tcg::QX, RW = tcg::RW, PPL = tcg::PPL, BPL = tcg::BPL;
     constexpr int CW = tcg::CW, CPL = tcg::CPL, SD = tcg::XSD;
     constexpr unsigned PBYTES = tcg::PBYTES, BBYTES = tcg::BBYTES, CBYTES = tcg::CBYTES, FULL = 0xffffffffu;
+    pdl_wait();
     PcgState *st = a.st;
     if (!SETUP && (st->stop || st->err)) return;
     extern __shared__ __align__(16) unsigned char dyn_raw[];
@@ -1930,6 +1938,7 @@ __device__ __forceinline__ float resid_scalar(const Geo &g, const float *__restr
 __global__ void __launch_bounds__(256, 4) k_resid_rx(Geo g, const float *__restrict__ x, const float *__restrict__ b,
                                                   const float4 *__restrict__ coef, const uint8_t *__restrict__ cls,
                                                   int cpitch, float *__restrict__ rx, const PcgState *st) {
+    pdl_wait();
     if (st && st->stop) return;
     const int nq = g.d.nx >> 2, cnx = g.d.nx >> 1;
     const int j = blockIdx.y * 8 + threadIdx.y, k = blockIdx.z;
@@ -2015,6 +2024,7 @@ __global__ void k_restrict_yz(Dims fd, Dims cd, int dims, const float *__restric
 __global__ void __launch_bounds__(256) k_restrict_yz4(Dims fd, Dims cd, int dims, const float *__restrict__ rx,
                                                       const uint8_t *__restrict__ cmask, float *__restrict__ cb,
                                                       const PcgState *st) {
+    pdl_wait();
     if (st && st->stop) return;
     const int I = 4 * (blockIdx.x * 32 + threadIdx.x), J = blockIdx.y * 8 + threadIdx.y, K = blockIdx.z;
     if (I >= cd.nx || J >= cd.ny) return;
@@ -2074,6 +2084,7 @@ __device__ __forceinline__ void ptaps2(int f, int nc, int *idx, float *w) {
 __global__ void __launch_bounds__(256) k_prolong4(Dims fd, Dims cd, int dims, const float *__restrict__ coarse,
                                                   const uint8_t *__restrict__ fmask, float *__restrict__ fine,
                                                   const PcgState *st) {
+    pdl_wait();
     if (st && st->stop) return;
     const int nq = fd.nx >> 2;
     {
@@ -2663,19 +2674,38 @@ int sweep(const Level &L, const uint8_t *bricks, const float *x_in, float *x_out
     return post("sweep");
 }
 
+// launch with programmatic stream serialization (the kernel calls pdl_wait
+// before touching memory)
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
+
 int res_restrict2(const Level &f, const SweepMaps &m, const float *x, float *rx, Level &c, int dims,
                   const PcgState *st, cudaStream_t s) {
     FF_CHECK(m.ok && m.cls_ptr && f.d.nx % 4 == 0, FF_E_STATE, "res_restrict2 needs cell classes and nx %% 4 == 0");
     Geo g = make_geo(f);
     const long long nq = (long long)(f.d.nx / 4) * f.d.ny * f.d.nz;
     (void)nq;
-    k_resid_rx<<<dim3((f.d.nx / 4 + 31) / 32, (f.d.ny + 7) / 8, f.d.nz), dim3(32, 8), 0, s>>>(
-        g, x, (const float *)f.b, f.coef, m.cls_ptr, m.cls_pitch, rx,
-                                                         st);
+    FF_CUDA(launch_pdl(k_resid_rx, dim3((f.d.nx / 4 + 31) / 32, (f.d.ny + 7) / 8, f.d.nz), dim3(32, 8), 0, s,
+                       g, x, (const float *)f.b, f.coef, m.cls_ptr, m.cls_pitch, rx,
+                                                         st));
     const long long nc = c.d.n();
     if (c.d.nx % 4 == 0 && c.d.nx == f.d.nx / 2)
-        k_restrict_yz4<<<dim3((c.d.nx / 4 + 31) / 32, (c.d.ny + 7) / 8, c.d.nz), dim3(32, 8), 0, s>>>(
-            f.d, c.d, dims, rx, c.mask, (float *)c.b, st);
+        FF_CUDA(launch_pdl(k_restrict_yz4, dim3((c.d.nx / 4 + 31) / 32, (c.d.ny + 7) / 8, c.d.nz), dim3(32, 8), 0,
+                           s, f.d, c.d, dims, (const float *)rx, (const uint8_t *)c.mask, (float *)c.b,
+                           (const PcgState *)st));
     else
         k_restrict_yz<<<(int)std::min<long long>((nc + 255) / 256, 152LL * 16), 256, 0, s>>>(f.d, c.d, dims, rx,
                                                                                               c.mask, (float *)c.b, st);
@@ -2684,8 +2714,8 @@ int res_restrict2(const Level &f, const SweepMaps &m, const float *x, float *rx,
 
 int prolong4(const Level &c, const Level &f, int dims, float *fine_x, const PcgState *st, cudaStream_t s) {
     FF_CHECK(f.d.nx % 4 == 0, FF_E_ARG, "prolong4 needs nx %% 4 == 0");
-    k_prolong4<<<dim3((f.d.nx / 4 + 31) / 32, (f.d.ny + 7) / 8, f.d.nz), dim3(32, 8), 0, s>>>(
-        f.d, c.d, dims, (const float *)c.x, f.mask, fine_x, st);
+    FF_CUDA(launch_pdl(k_prolong4, dim3((f.d.nx / 4 + 31) / 32, (f.d.ny + 7) / 8, f.d.nz), dim3(32, 8), 0, s,
+                       f.d, c.d, dims, (const float *)c.x, (const uint8_t *)f.mask, fine_x, st));
     return post("prolong4");
 }
 
@@ -2833,11 +2863,11 @@ int sweep_tma(const Level &L, const SweepMaps &m, const uint8_t *bricks, int in,
     const CUtensorMap &xm = m.x[in < 0 ? out : in];
     const bool rz = rz_mode != 0;
     if (in < 0) {
-        if (rz) k_sweep_tma<true, true><<<grid, tq::NT, tq::SMEM, s>>>(a, xm, m.b, m.cls);
-        else k_sweep_tma<true, false><<<grid, tq::NT, tq::SMEM, s>>>(a, xm, m.b, m.cls);
+        if (rz) FF_CUDA(launch_pdl(k_sweep_tma<true, true>, grid, dim3(tq::NT), tq::SMEM, s, a, xm, m.b, m.cls));
+        else FF_CUDA(launch_pdl(k_sweep_tma<true, false>, grid, dim3(tq::NT), tq::SMEM, s, a, xm, m.b, m.cls));
     } else {
-        if (rz) k_sweep_tma<false, true><<<grid, tq::NT, tq::SMEM, s>>>(a, xm, m.b, m.cls);
-        else k_sweep_tma<false, false><<<grid, tq::NT, tq::SMEM, s>>>(a, xm, m.b, m.cls);
+        if (rz) FF_CUDA(launch_pdl(k_sweep_tma<false, true>, grid, dim3(tq::NT), tq::SMEM, s, a, xm, m.b, m.cls));
+        else FF_CUDA(launch_pdl(k_sweep_tma<false, false>, grid, dim3(tq::NT), tq::SMEM, s, a, xm, m.b, m.cls));
     }
     return post("sweep_tma");
 }
@@ -3003,7 +3033,7 @@ int p_pap_tma(const Level &L0, const SweepMaps &sm, const CgMaps &m, const float
     a.st = st;
     a.partials = partials;
     dim3 grid(a.gx * a.gy * ((L0.d.nz + a.zc - 1) / a.zc));
-    k_p_pap_tma<<<grid, tcg::NT, tcg::PAP_SMEM, s>>>(a, m.z[zi], m.p[0], m.p[1], sm.cls);
+    FF_CUDA(launch_pdl(k_p_pap_tma, grid, dim3(tcg::NT), tcg::PAP_SMEM, s, a, m.z[zi], m.p[0], m.p[1], sm.cls));
     return post("p_pap_tma");
 }
 
@@ -3021,11 +3051,11 @@ int x_residual_tma(const Level &L0, const SweepMaps &sm, const CgMaps &m, float 
     dim3 grid(a.gx * a.gy * ((L0.d.nz + a.zc - 1) / a.zc));
     const size_t sh = tcg::XR_SMEM;
     if (setup) {
-        if (m.ds) k_x_residual_tma<true, true><<<grid, tcg::NT, sh, s>>>(a, m.xh[0], m.xh[1], m.xl[0], m.xl[1], m.p[0], m.p[1], m.b, sm.cls);
-        else k_x_residual_tma<true, false><<<grid, tcg::NT, sh, s>>>(a, m.xh[0], m.xh[1], m.xl[0], m.xl[1], m.p[0], m.p[1], m.b, sm.cls);
+        if (m.ds) FF_CUDA(launch_pdl(k_x_residual_tma<true, true>, grid, dim3(tcg::NT), sh, s, a, m.xh[0], m.xh[1], m.xl[0], m.xl[1], m.p[0], m.p[1], m.b, sm.cls));
+        else FF_CUDA(launch_pdl(k_x_residual_tma<true, false>, grid, dim3(tcg::NT), sh, s, a, m.xh[0], m.xh[1], m.xl[0], m.xl[1], m.p[0], m.p[1], m.b, sm.cls));
     } else {
-        if (m.ds) k_x_residual_tma<false, true><<<grid, tcg::NT, sh, s>>>(a, m.xh[0], m.xh[1], m.xl[0], m.xl[1], m.p[0], m.p[1], m.b, sm.cls);
-        else k_x_residual_tma<false, false><<<grid, tcg::NT, sh, s>>>(a, m.xh[0], m.xh[1], m.xl[0], m.xl[1], m.p[0], m.p[1], m.b, sm.cls);
+        if (m.ds) FF_CUDA(launch_pdl(k_x_residual_tma<false, true>, grid, dim3(tcg::NT), sh, s, a, m.xh[0], m.xh[1], m.xl[0], m.xl[1], m.p[0], m.p[1], m.b, sm.cls));
+        else FF_CUDA(launch_pdl(k_x_residual_tma<false, false>, grid, dim3(tcg::NT), sh, s, a, m.xh[0], m.xh[1], m.xl[0], m.xl[1], m.p[0], m.p[1], m.b, sm.cls));
     }
     return post("x_residual_tma");
 }
