@@ -606,7 +606,6 @@ __global__ void __launch_bounds__(tq::NT, 3)
     const bool quad_in = gi < g.d.nx && gj < g.d.ny;
     const int o = (ty + 2) * RW + 4 + lx, bo = (ty + 1) * RW + 4 + lx;
     const int co = (ty + 1) * CW + 16 + qx;   // this quad's class byte in a class plane
-    float *outp = a.x_out + (gi + g.sy * gj) + g.sz * k0;
     const long long qoff = gi + g.sy * gj;
     // h^-2 of the absent faces in y and in x (cells 0 and 3); planes strictly
     // inside in z use `inner`, the first and last plane add h^-2 in z (a
@@ -616,31 +615,30 @@ __global__ void __launch_bounds__(tq::NT, 3)
     const int my = (gj == 0) + (gj == g.d.ny - 1);
     const int mx0 = gi == 0, mx3 = gi + 3 == g.d.nx - 1;
     const int mze = g.d.nz == 1 ? 2 : 1;   // faces across the edge on the first and last plane
-    QuadScale inner, zedge;
-    // the scales, from the table written before the first barrier
+    QuadScale inner;
+    // the scales, from the table written before the first barrier; the first
+    // and last plane (a block-uniform branch) read theirs when they come
     inner.r0 = rdt[mx0 + 3 * my];
     inner.r12 = rdt[3 * my];
     inner.r3 = rdt[mx3 + 3 * my];
-    zedge.r0 = rdt[mx0 + 3 * my + 9 * mze];
-    zedge.r12 = rdt[3 * my + 9 * mze];
-    zedge.r3 = rdt[mx3 + 3 * my + 9 * mze];
-    // the block-uniform choice of the first and last plane
-    auto scale_at = [&](int k) { return (k == 0 || k == g.d.nz - 1) ? zedge : inner; };
+    const int tix = mx0 | (my << 1) | (mx3 << 3);   // table indices, packed
+    auto scale_at = [&](int k) {
+        if (k != 0 && k != g.d.nz - 1) return inner;
+        const int m0 = tix & 1, myy = (tix >> 1) & 3, m3 = tix >> 3, mz = 9 * mze;
+        QuadScale e;
+        e.r0 = rdt[m0 + 3 * myy + mz];
+        e.r12 = rdt[3 * myy + mz];
+        e.r3 = rdt[m3 + 3 * myy + mz];
+        return e;
+    };
     // The tile's halo ring on plane m+2 (its first colour, which the second
     // colour on that plane reads two steps later): lanes 0..15 of warp 0 the
     // row above the tile and of warp 1 the row below, as quads; lanes 0..15
     // of warp 2 the cells left (lanes 0..7) and right (8..15) of the tile,
     // one pair of rows each.
+    // (the ring's per-thread positions are recomputed inside its branches,
+    // so they take no registers across the z-march)
     const int rrole = (lane < 16 && warp < 3) ? warp : -1;   // 0, 1 rows; 2 columns
-    const int rlrow = rrole == 0 ? -1 : TY;                    // ring rows: staged-row offset
-    const int rgi = i0 + 4 * lane, rgj = j0 + rlrow;
-    const bool rquad_in = rrole >= 0 && rrole < 2 && rgj >= 0 && rgj < g.d.ny && rgi < g.d.nx;
-    const int ro4 = (rlrow + 2) * RW + 4 + 4 * lane, rbo = (rlrow + 1) * RW + 4 + 4 * lane;
-    const int rco = (rlrow + 1) * CW + 16 + lane;
-    const int rmy = (rgj == 0) + (rgj == g.d.ny - 1), rmx0 = rgi == 0, rmx3 = rgi + 3 == g.d.nx - 1;
-    const int clx = (lane & 8) ? TX : -1, crow = 2 * (lane & 7);   // ring columns
-    const int cgi = i0 + clx;
-    const int cmx = (cgi == 0) + (cgi == g.d.nx - 1);
     // The thread's quad on planes m-1 .. m+2: q0 (plane m) and q1 carry the
     // first colour relaxed, q2 the values as staged; b of planes m and m+1;
     // the class bytes of planes m .. m+3 (bits 0-7 .. 24-31).
@@ -692,62 +690,6 @@ __global__ void __launch_bounds__(tq::NT, 3)
                 }
                 if (quad_in) *reinterpret_cast<float4 *>(X2 + o) = q2;
             }
-            if (rrole == 0 || rrole == 1) {
-                // ring row quad: its class byte on plane m+3 (kept for the
-                // next step; class-3 lines go to L1), then the first colour
-                // on plane m+2
-                if (m == mstart) rcls = cs[rco];
-                const unsigned rnext = C3[rco];
-                if (rquad_in && any_general(rnext) && kp < g.d.nz) {
-                    const long long off = rgi + g.sy * rgj + g.sz * kp;
-                    prefetch_l1(a.coef + off);
-                    prefetch_l1(a.gco + off);
-                }
-                if (ka >= 0 && ka <= k1 && ka < g.d.nz && rgj >= 0 && rgj < g.d.ny) {
-                    float4 rq = lds4(X2 + ro4);
-                    const float4 rym = lds4(X2 + ro4 - RW), ryp = lds4(X2 + ro4 + RW);
-                    const float4 rzm = lds4(X1 + ro4), rzp = lds4(X3 + ro4), rbq = lds4(Bn + rbo);
-                    const int mz = (ka == 0 || ka == g.d.nz - 1) ? 9 * mze : 0;
-                    QuadScale re;
-                    re.r0 = rdt[rmx0 + 3 * rmy + mz];
-                    re.r12 = rdt[3 * rmy + mz];
-                    re.r3 = rdt[rmx3 + 3 * rmy + mz];
-                    constexpr unsigned HALF = 0x0000ffffu;
-                    if ((ca ^ rgj ^ ka) & 1) {
-                        float sv = __shfl_down_sync(HALF, rq.x, 1);
-                        if (lane == QX - 1) sv = X2[ro4 + 4];
-                        if (rquad_in) relax_pair<1>(g, a, rq, sv, rym, ryp, rzm, rzp, rbq, rcls, re, rgi, rgj, ka);
-                    } else {
-                        float sv = __shfl_up_sync(HALF, rq.w, 1);
-                        if (lane == 0) sv = X2[ro4 - 1];
-                        if (rquad_in) relax_pair<0>(g, a, rq, sv, rym, ryp, rzm, rzp, rbq, rcls, re, rgi, rgj, ka);
-                    }
-                    if (rquad_in) *reinterpret_cast<float4 *>(X2 + ro4) = rq;
-                }
-                rcls = rnext;
-            } else if (rrole == 2) {
-                // ring column cell: rows crow, crow+1, the first colour's one
-                const int sh0 = (ca + j0 + ka + clx + crow) & 1, sh1 = (ca + j0 + kp + clx + crow) & 1;
-                const int ly0 = crow + sh0, ly1 = crow + sh1;
-                const int byt = (clx >> 2) + 16, bit = 2 * (clx & 3);
-                if (m == mstart) rcls = (cs[(ly0 + 1) * CW + byt] >> bit) & 3u;
-                const unsigned rnext = (C3[(ly1 + 1) * CW + byt] >> bit) & 3u;
-                const bool col_in = cgi >= 0 && cgi < g.d.nx;
-                if (rnext == 3u && col_in && j0 + ly1 < g.d.ny && kp < g.d.nz) {
-                    const long long off = cgi + g.sy * (j0 + ly1) + g.sz * kp;
-                    prefetch_l1(a.coef + off);
-                    prefetch_l1(a.gco + off);
-                }
-                const int rj = j0 + ly0;
-                if (ka >= 0 && ka <= k1 && ka < g.d.nz && col_in && rj < g.d.ny) {
-                    const int ro = (ly0 + 2) * RW + clx + 4;
-                    const int mz = (ka == 0 || ka == g.d.nz - 1) ? 9 * mze : 0;
-                    const float rd = rdt[cmx + 3 * ((rj == 0) + (rj == g.d.ny - 1)) + mz];
-                    X2[ro] = relax_any(g, a, rcls, cgi + g.sy * rj + g.sz * ka, X2[ro], X2[ro - 1], X2[ro + 1],
-                                       X2[ro - RW], X2[ro + RW], X1[ro], X3[ro], Bn[(ly0 + 1) * RW + clx + 4], rd);
-                }
-                rcls = rnext;
-            }
             if (m >= k0) {
                 // second colour on plane m (its neighbours carry the first
                 // colour: relaxed in steps m-3..m-1), then plane m is final
@@ -764,7 +706,7 @@ __global__ void __launch_bounds__(tq::NT, 3)
                     if (quad_in) relax_pair<0>(g, a, q0, s, ym, yp, qm1, q1, bb0, c0, e, gi, gj, m);
                 }
                 if (quad_in) {
-                    *reinterpret_cast<float4 *>(outp) = q0;
+                    *reinterpret_cast<float4 *>(a.x_out + qoff + g.sz * m) = q0;
                     if (RZ) {
                         acc.add(bb0.x * q0.x);
                         acc.add(bb0.y * q0.y);
@@ -772,11 +714,75 @@ __global__ void __launch_bounds__(tq::NT, 3)
                         acc.add(bb0.w * q0.w);
                     }
                 }
-                outp += g.sz;
             }
             qm1 = q0; q0 = q1; q1 = q2; q2 = q3;
             bb0 = bb1; bb1 = bb2;
             cpipe >>= 8;
+            // the halo ring on plane m+2 last: the quads' transients are dead
+            if (rrole == 0 || rrole == 1) {
+                // ring row quad: its class byte on plane m+3 (kept for the
+                // next step; class-3 lines go to L1), then the first colour
+                // on plane m+2
+                const int rlrow = rrole == 0 ? -1 : TY;   // staged-row offset
+                const int rgi = i0 + 4 * lane, rgj = j0 + rlrow;
+                const bool rquad_in = rgj >= 0 && rgj < g.d.ny && rgi < g.d.nx;
+                const int ro4 = (rlrow + 2) * RW + 4 + 4 * lane, rbo = (rlrow + 1) * RW + 4 + 4 * lane;
+                const int rco = (rlrow + 1) * CW + 16 + lane;
+                if (m == mstart) rcls = cs[rco];
+                const unsigned rnext = C3[rco];
+                if (rquad_in && any_general(rnext) && kp < g.d.nz) {
+                    const long long off = rgi + g.sy * rgj + g.sz * kp;
+                    prefetch_l1(a.coef + off);
+                    prefetch_l1(a.gco + off);
+                }
+                if (ka >= 0 && ka <= k1 && ka < g.d.nz && rgj >= 0 && rgj < g.d.ny) {
+                    float4 rq = lds4(X2 + ro4);
+                    const float4 rym = lds4(X2 + ro4 - RW), ryp = lds4(X2 + ro4 + RW);
+                    const float4 rzm = lds4(X1 + ro4), rzp = lds4(X3 + ro4), rbq = lds4(Bn + rbo);
+                    const int mz = (ka == 0 || ka == g.d.nz - 1) ? 9 * mze : 0;
+                    const int rmy = (rgj == 0) + (rgj == g.d.ny - 1);
+                    QuadScale re;
+                    re.r0 = rdt[(rgi == 0) + 3 * rmy + mz];
+                    re.r12 = rdt[3 * rmy + mz];
+                    re.r3 = rdt[(rgi + 3 == g.d.nx - 1) + 3 * rmy + mz];
+                    constexpr unsigned HALF = 0x0000ffffu;
+                    if ((ca ^ rgj ^ ka) & 1) {
+                        float sv = __shfl_down_sync(HALF, rq.x, 1);
+                        if (lane == QX - 1) sv = X2[ro4 + 4];
+                        if (rquad_in) relax_pair<1>(g, a, rq, sv, rym, ryp, rzm, rzp, rbq, rcls, re, rgi, rgj, ka);
+                    } else {
+                        float sv = __shfl_up_sync(HALF, rq.w, 1);
+                        if (lane == 0) sv = X2[ro4 - 1];
+                        if (rquad_in) relax_pair<0>(g, a, rq, sv, rym, ryp, rzm, rzp, rbq, rcls, re, rgi, rgj, ka);
+                    }
+                    if (rquad_in) *reinterpret_cast<float4 *>(X2 + ro4) = rq;
+                }
+                rcls = rnext;
+            } else if (rrole == 2) {
+                // ring column cell: rows crow, crow+1, the first colour's one
+                const int clx = (lane & 8) ? TX : -1, crow = 2 * (lane & 7);
+                const int cgi = i0 + clx;
+                const int sh0 = (ca + j0 + ka + clx + crow) & 1, sh1 = (ca + j0 + kp + clx + crow) & 1;
+                const int ly0 = crow + sh0, ly1 = crow + sh1;
+                const int byt = (clx >> 2) + 16, bit = 2 * (clx & 3);
+                if (m == mstart) rcls = (cs[(ly0 + 1) * CW + byt] >> bit) & 3u;
+                const unsigned rnext = (C3[(ly1 + 1) * CW + byt] >> bit) & 3u;
+                const bool col_in = cgi >= 0 && cgi < g.d.nx;
+                if (rnext == 3u && col_in && j0 + ly1 < g.d.ny && kp < g.d.nz) {
+                    const long long off = cgi + g.sy * (j0 + ly1) + g.sz * kp;
+                    prefetch_l1(a.coef + off);
+                    prefetch_l1(a.gco + off);
+                }
+                const int rj = j0 + ly0;
+                if (ka >= 0 && ka <= k1 && ka < g.d.nz && col_in && rj < g.d.ny) {
+                    const int ro = (ly0 + 2) * RW + clx + 4;
+                    const int mz = (ka == 0 || ka == g.d.nz - 1) ? 9 * mze : 0;
+                    const float rd = rdt[(cgi == 0) + (cgi == g.d.nx - 1) + 3 * ((rj == 0) + (rj == g.d.ny - 1)) + mz];
+                    X2[ro] = relax_any(g, a, rcls, cgi + g.sy * rj + g.sz * ka, X2[ro], X2[ro - 1], X2[ro + 1],
+                                       X2[ro - RW], X2[ro + RW], X1[ro], X3[ro], Bn[(ly0 + 1) * RW + clx + 4], rd);
+                }
+                rcls = rnext;
+            }
         }
         // x plane m, b plane m+2 and class plane m+3 are dead: refill them
         // with step m+SD's data
