@@ -272,7 +272,7 @@ int ff_viscosity3_apply(ff_ctx ctx, const int *resolution, const double *grid_sp
                         ff_field w, double nu, double dt, ff_field u_out, ff_field v_out, ff_field w_out);
 
 /* ---- FLIP: replaces createGridFlipSolver3 (fluxflow
- * src/grid/grid_flip_solver3.js:135-1157) without resampling.  Particles
+ * src/grid/grid_flip_solver3.js:135-1157), resampling included.  Particles
  * are FF_VEC3 positions and velocities (AoS, as the reference's vec3
  * arrays); P2G accumulates round(v w S) and round(w S) in int32 (S =
  * p2gAtomicScale, :508-530), so the transfer does not depend on the
@@ -301,6 +301,9 @@ typedef struct {
     double component_density;      /* variable-density coupling (:265-359) */
     int extrapolation_depth;       /* default 5                            */
     ff_pressure_desc pressure;     /* the projection's options (`pressure`)*/
+    int resample_enabled;          /* resample.enabled, default 1 (:178)   */
+    int min_particles_per_cell;    /* resample.minParticlesPerCell, 4      */
+    int max_particles_per_cell;    /* resample.maxParticlesPerCell, 8      */
 } ff_flip_desc;
 void ff_flip_desc_default(ff_flip_desc *d, const int *resolution, const double *grid_spacing, int max_particles,
                           double dt);
@@ -333,7 +336,12 @@ int ff_flip3_grid_fields(ff_flip f, ff_field *cell_concentration, ff_field *cell
 #define FF_FLIP_EXTRAPOLATE_PRESSURE 9    /* extrapolatePressureU/V/W            */
 #define FF_FLIP_G2P 10                    /* g2pUpdate                           */
 #define FF_FLIP_CONCENTRATION_PARTICLE 11 /* mixAndFade                          */
+#define FF_FLIP_RESAMPLE 12               /* resamplePass, then markFluidCells   */
 int ff_flip3_stage(ff_flip f, int stage);
+/* the last resamplePass (:621-820): donors = particles in cells above
+ * max_particles_per_cell, requested = the slots under-full cells asked
+ * for; min(donors, requested) particles moved.  Synchronises the stream. */
+int ff_flip3_resample_stats(ff_flip f, int64_t *donors, int64_t *requested);
 /* onAdvanceTimeStep(): every stage in the reference's order; diag is the
  * projection's diagnostics                                                */
 int ff_flip3_step(ff_flip f, ff_diag *diag);

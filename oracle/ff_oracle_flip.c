@@ -14,6 +14,7 @@
  *                                   :265-359, :848-884, :960-1049
  *   G2P                             :909-922
  *   advectParticles, pushOutOfCollider :925-957
+ *   resamplePass                    :621-820
  */
 #include <math.h>
 #include <stdint.h>
@@ -442,4 +443,67 @@ void orc_flip_advect(const int *res, const float *h, const float *o, const float
         float shift = (push_thresh - val) + push_shift;
         for (int a = 0; a < 3; ++a) q[a] = q[a] + gr[a] / gl * shift;
     }
+}
+
+/* resamplePass (:621-820): particles in cells holding more than max_pc are
+ * donors, ranked in particle order; cells holding fewer than min_pc with
+ * at least 3 of their 6 clamped face neighbours at min_pc or more ask for
+ * min_pc - count, and claim donor slots in flat cell order (i fastest).  A
+ * claimed donor moves to the claiming cell's centre, cellCenterOrigin +
+ * (i, j, k) h, and takes the face-centred velocity sampled there
+ * (faceCenteredValueAtPosition3).  The pass then rebuilds the fluid mask
+ * (markFluidCells, run again by the caller).  Returns the number of
+ * particles moved. */
+int64_t orc_flip_resample(const int *res, const float *h, const float *o, int64_t n, float *pos, float *vel,
+                          const float *u, const float *v, const float *w, int min_pc, int max_pc) {
+    fg g = make_fg(res, h, o);
+    const int64_t nc = (int64_t)g.nx * g.ny * g.nz;
+    int32_t *cnt = (int32_t *)calloc((size_t)nc, sizeof(int32_t));
+    int64_t *pool = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n > 0 ? n : 1));
+    int64_t *cell = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n > 0 ? n : 1));
+    for (int64_t p = 0; p < n; ++p) {
+        cell[p] = cell_index(&g, pos + 3 * p);
+        cnt[cell[p]] += 1;
+    }
+    int64_t donors = 0;
+    for (int64_t p = 0; p < n; ++p)
+        if (cnt[cell[p]] > max_pc) pool[donors++] = p;
+    const float *comp[3] = {u, v, w};
+    const float cc[3] = {g.ox + g.hx * 0.5f, g.oy + g.hy * 0.5f, g.oz + g.hz * 0.5f};
+    int64_t base = 0, moved = 0;
+    for (int k = 0; k < g.nz; ++k)
+        for (int j = 0; j < g.ny; ++j)
+            for (int i = 0; i < g.nx; ++i) {
+                const int64_t c = i + (int64_t)g.nx * (j + (int64_t)g.ny * k);
+                const int32_t count = cnt[c];
+#define ORC_CNT(ii, jj, kk) cnt[(ii) + (int64_t)g.nx * ((jj) + (int64_t)g.ny * (kk))]
+                const int nb = (ORC_CNT(i > 0 ? i - 1 : 0, j, k) >= min_pc) +
+                               (ORC_CNT(i < g.nx - 1 ? i + 1 : g.nx - 1, j, k) >= min_pc) +
+                               (ORC_CNT(i, j > 0 ? j - 1 : 0, k) >= min_pc) +
+                               (ORC_CNT(i, j < g.ny - 1 ? j + 1 : g.ny - 1, k) >= min_pc) +
+                               (ORC_CNT(i, j, k > 0 ? k - 1 : 0) >= min_pc) +
+                               (ORC_CNT(i, j, k < g.nz - 1 ? k + 1 : g.nz - 1) >= min_pc);
+#undef ORC_CNT
+                const int need = (count < min_pc && nb >= 3) ? min_pc - count : 0;
+                for (int q = 0; q < need; ++q) {
+                    const int64_t slot = base + q;
+                    if (slot >= donors) break;
+                    const int64_t d = pool[slot];
+                    float np[3] = {cc[0] + (float)i * g.hx, cc[1] + (float)j * g.hy, cc[2] + (float)k * g.hz};
+                    for (int a = 0; a < 3; ++a) {
+                        int s[3];
+                        float oa[3];
+                        shape_of(&g, a, s);
+                        origin_of(&g, a, oa);
+                        vel[3 * d + a] = tri_sample(comp[a], &g, s, oa, np);
+                    }
+                    for (int a = 0; a < 3; ++a) pos[3 * d + a] = np[a];
+                    ++moved;
+                }
+                base += need;
+            }
+    free(cnt);
+    free(pool);
+    free(cell);
+    return moved;
 }

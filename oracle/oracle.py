@@ -101,6 +101,8 @@ def _declare(L):
     L.orc_flip_reduced_gravity.argtypes = [ip, fp, fp, fp, fp, fp, fp, fp, F, F, fp, fp, fp]
     L.orc_flip_mix_fade.argtypes = [ip, fp, fp, L64, fp, fp, F, F, fp]
     L.orc_flip_advect.argtypes = [ip, fp, fp, fp, fp, fp, fp, F, I, L64, fp, fp, F, F]
+    L.orc_flip_resample.argtypes = [ip, fp, fp, L64, fp, fp, fp, fp, fp, I, I]
+    L.orc_flip_resample.restype = L64
 
 
 def _shape_row(s):
@@ -570,3 +572,12 @@ def flip_mix_fade(shape, h, origin, pos, cell_conc, conc, mixing, fade):
     lib().orc_flip_mix_fade(res, hh, oo, _f32(pos).size // 3, _fptr(_f32(pos)), _fptr(_f32(cell_conc)),
                             float(mixing), float(fade), _fptr(conc))
     return conc
+
+
+def flip_resample(shape, h, origin, pos, vel, u, v, w, min_pc=4, max_pc=8):
+    """resamplePass: returns (positions, velocities, particles moved)."""
+    pos, vel = _f32(pos).copy(), _f32(vel).copy()
+    res, hh, oo = _geom(shape, h, origin)
+    moved = lib().orc_flip_resample(res, hh, oo, pos.size // 3, _fptr(pos), _fptr(vel), _fptr(_f32(u)),
+                                    _fptr(_f32(v)), _fptr(_f32(w)), int(min_pc), int(max_pc))
+    return pos, vel, int(moved)

@@ -133,3 +133,40 @@ def test_dam_break_steps(gpu, oracle):
     assert p[:, 1].mean() < y0 - 1e-3
     vel = solver.velocities.to_array()
     assert np.all(np.isfinite(vel)) and np.abs(vel).max() <= 500
+
+
+@pytest.mark.parametrize("shape,n,mm", [(SH, 24000, (4, 8)), ((40, 36, 33), 160000, (3, 6))])
+def test_resample_bit_exact(gpu, oracle, shape, n, mm):
+    """resamplePass on the GPU: the same donors move to the same cells with
+    the same sampled velocities as the oracle (ranks are prefix sums in
+    index order), and the fluid mask is rebuilt from the new positions."""
+    from tsl_array_n_gb300 import fluxflow as ff
+    h = tuple(1.0 / s for s in shape)
+    grid = ff.FaceCenteredGrid3(shape, h, O)
+    rng = np.random.default_rng(11)
+    pos = (rng.random((n, 3)) * np.array([0.6, 0.5, 0.7])).astype(np.float32)
+    vel = rng.standard_normal((n, 3)).astype(np.float32)
+    nx, ny, nz = shape
+    u, v, w = (rng.standard_normal(s).astype(np.float32)
+               for s in ((nx + 1) * ny * nz, nx * (ny + 1) * nz, nx * ny * (nz + 1)))
+    grid.set(u, v, w)
+    solver = ff.create_grid_flip_solver3(velocity_grid=grid, max_particles=n, dt=0.01,
+                                         resample={"minParticlesPerCell": mm[0], "maxParticlesPerCell": mm[1]})
+    solver.positions.from_array(pos)
+    solver.velocities.from_array(vel)
+    solver.stage("resample")
+    rp, rv, moved = oracle.flip_resample(shape, h, O, pos, vel, u, v, w, *mm)
+    assert moved > 0
+    st = solver.resample_stats()
+    assert st["moved"] == moved
+    same(solver.positions.to_array(), rp)
+    same(solver.velocities.to_array(), rv)
+    same(solver.fluid_mask.to_array(), oracle.flip_mark_fluid(shape, h, O, rp))
+
+
+def test_resample_disabled_is_a_no_op(gpu):
+    grid, solver, pos, n = make(resample={"enabled": False})
+    solver.positions.from_array(np.zeros((n, 3), np.float32) + 0.01)   # all in one cell
+    solver.stage("resample")
+    assert np.all(solver.positions.to_array() == np.float32(0.01))
+    assert solver.resample_stats() == {"donors": 0, "requested": 0, "moved": 0}

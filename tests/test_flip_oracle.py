@@ -111,3 +111,72 @@ def test_concentration_density_and_beta(oracle):
     assert np.all((rho >= 1.0) & (rho <= 1000.0))
     # beta = rho_ref / rho_face: 1 in the heavy phase, 1000 in the light one
     assert np.isclose(beta[0].max(), 1000.0) and np.isclose(beta[0].min(), 1.0)
+
+
+def resample_numpy(oracle, sh, h, o, pos, vel, u, v, w, min_pc, max_pc):
+    """resamplePass (grid_flip_solver3.js:621-820) a second way, vectorised:
+    donors ranked by particle index, needs scanned in flat cell order,
+    velocities through the oracle's G2P in its PIC limit (ratio 0, no
+    damping: the interpolated grid velocity itself)."""
+    nx, ny, nz = sh
+    pos = np.asarray(pos, np.float32).reshape(-1, 3).copy()
+    vel = np.asarray(vel, np.float32).reshape(-1, 3).copy()
+    cell = oracle.flip_cell_index(sh, h, o, pos)
+    cnt = np.bincount(cell, minlength=nx * ny * nz).reshape(nz, ny, nx)
+    donors = np.nonzero(cnt.ravel()[cell] > max_pc)[0]
+    ok = (cnt >= min_pc).astype(np.int64)
+    nb = np.zeros_like(ok)
+    for ax in range(3):
+        lo = np.concatenate([np.take(ok, [0], axis=ax), np.take(ok, np.arange(ok.shape[ax] - 1), axis=ax)], axis=ax)
+        hi = np.concatenate([np.take(ok, np.arange(1, ok.shape[ax]), axis=ax), np.take(ok, [-1], axis=ax)], axis=ax)
+        nb += lo + hi
+    need = np.where((cnt < min_pc) & (nb >= 3), min_pc - cnt, 0).ravel()
+    cells = np.repeat(np.arange(need.size), need)[:donors.size]
+    movers = donors[:cells.size]
+    i, j, k = cells % nx, (cells // nx) % ny, cells // (nx * ny)
+    f32 = np.float32
+    for a, idx in enumerate((i, j, k)):
+        cc = f32(o[a]) + f32(h[a]) * f32(0.5)
+        pos[movers, a] = cc + idx.astype(f32) * f32(h[a])
+    if movers.size:
+        z = np.zeros((movers.size, 3), np.float32)
+        vel[movers] = oracle.flip_g2p(sh, h, o, pos[movers], z, (u, v, w), (u, v, w), 0.0, 0.0).reshape(-1, 3)
+    return pos.ravel(), vel.ravel(), int(movers.size), int(donors.size), int(need.sum())
+
+
+def random_fluid(sh, h, n, seed, frac=(0.6, 0.5, 0.7)):
+    rng = np.random.default_rng(seed)
+    hi = np.array([sh[a] * h[a] * frac[a] for a in range(3)])
+    return (rng.random((n, 3)) * hi).astype(np.float32)
+
+
+@pytest.mark.parametrize("min_pc,max_pc", [(4, 8), (3, 5), (6, 7)])
+def test_resample_matches_vectorised_restatement(oracle, min_pc, max_pc):
+    sh, h, o = (12, 10, 9), (1 / 12, 0.1, 1 / 9), (0.0, -0.5, 0.25)
+    n = 5 * int(12 * 0.6 * 10 * 0.5 * 9 * 0.7)
+    pos = random_fluid(sh, h, n, 7)
+    pos[:, 1] += -0.5
+    pos[:, 2] += 0.25
+    rng = np.random.default_rng(8)
+    vel = rng.standard_normal((n, 3)).astype(np.float32)
+    su, sv, sw = (13, 10, 9), (12, 11, 9), (12, 10, 10)
+    u, v, w = (rng.standard_normal(np.prod(s)).astype(np.float32) for s in (su, sv, sw))
+    p1, v1, moved = oracle.flip_resample(sh, h, o, pos, vel, u, v, w, min_pc, max_pc)
+    p2, v2, moved2, donors, need = resample_numpy(oracle, sh, h, o, pos, vel, u, v, w, min_pc, max_pc)
+    assert moved > 0 and moved == moved2 == min(donors, need)
+    assert np.array_equal(p1, p2) and np.array_equal(v1, v2)
+    changed = np.any(p1.reshape(-1, 3) != pos, axis=1)
+    assert changed.sum() <= moved
+
+
+def test_resample_no_donors_or_no_need(oracle):
+    sh, h, o = (6, 6, 6), (1 / 6,) * 3, (0.0, 0.0, 0.0)
+    u, v, w = (np.zeros(s, np.float32) for s in (7 * 36, 7 * 36, 7 * 36))
+    # eight particles in every cell: nothing above max, nothing below min
+    seed = oracle.flip_box_seed((0, 0, 0), (1, 1, 1), (1 / 6,) * 3, 2, 0.2, 0x9E3779B9)
+    vel = np.ones(seed.size, np.float32)
+    p, vv, moved = oracle.flip_resample(sh, h, o, seed, vel, u, v, w)
+    assert moved == 0 and np.array_equal(p, seed) and np.array_equal(vv, vel)
+    # an empty particle set
+    p, vv, moved = oracle.flip_resample(sh, h, o, np.zeros(0, np.float32), np.zeros(0, np.float32), u, v, w)
+    assert moved == 0 and p.size == 0

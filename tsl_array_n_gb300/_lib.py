@@ -48,7 +48,8 @@ class FlipDesc(C.Structure):
                 ("collider_push_shift", C.c_double), ("carry_concentration", C.c_int), ("mixing", C.c_double),
                 ("fade", C.c_double), ("concentration_atomic_scale", C.c_double),
                 ("ambient_density", C.c_double), ("component_density", C.c_double),
-                ("extrapolation_depth", C.c_int), ("pressure", PressureDesc)]
+                ("extrapolation_depth", C.c_int), ("pressure", PressureDesc), ("resample_enabled", C.c_int),
+                ("min_particles_per_cell", C.c_int), ("max_particles_per_cell", C.c_int)]
 
 
 class Diag(C.Structure):
@@ -123,6 +124,7 @@ PROTOTYPES = {
     "ff_flip3_grid_fields": (_I, [_P, _PP, _PP, _PP, _PP, _PP, _PP, _PP]),
     "ff_flip3_stage": (_I, [_P, _I]),
     "ff_flip3_step": (_I, [_P, C.POINTER(Diag)]),
+    "ff_flip3_resample_stats": (_I, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "ff_flip_box_seed3": (_I, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double), _I, _D,
                                C.c_uint32, _FP, C.c_int64, C.POINTER(C.c_int64)]),
     "ff_jitter_random": (_I, [C.c_uint32, _I, C.POINTER(C.c_double)]),

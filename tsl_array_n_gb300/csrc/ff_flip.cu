@@ -268,6 +268,209 @@ __global__ void k_flip_mix_fade(G3 g, long long n, const float *__restrict__ pos
     }
 }
 
+// ---- resamplePass (:621-820) ------------------------------------------
+// Donor ranks and claim slots are prefix sums in index order -- particle
+// order for donors, flat cell order (i fastest) for claims -- so which
+// particle lands where does not depend on scheduling.  A block owns
+// RS_CHUNK consecutive items, each warp RS_WARP_ITEMS of them in rounds of
+// 32 (coalesced); a warp ranks its items by ballot (donors) or a shuffle
+// scan (needs), and the scanned block totals place the blocks.
+constexpr int RS_ROUNDS = 16, RS_WARP_ITEMS = RS_ROUNDS * 32, RS_CHUNK = 8 * RS_WARP_ITEMS;
+
+// markDonorsKernel (:686-693): every particle of a cell above max_pc
+__device__ __forceinline__ bool rs_donor(const G3 &g, const float *__restrict__ pos, long long p,
+                                         const int *__restrict__ cnt, int max_pc) {
+    return cnt[cell_of(g, pos + 3 * p)] > max_pc;
+}
+
+// markNeedKernel (:716-724) with neighborFluidCount (:700-713): min_pc -
+// count for a cell below min_pc with at least 3 of its 6 face neighbours
+// (indices clamped to the grid) at min_pc or more
+__device__ __forceinline__ int rs_need(const G3 &g, const int *__restrict__ cnt, long long c, int min_pc) {
+    const int count = cnt[c];
+    if (count >= min_pc) return 0;
+    const long long plane = (long long)g.nx * g.ny;
+    const int k = (int)(c / plane), rem = (int)(c - k * plane), j = rem / g.nx, i = rem - j * g.nx;
+    const int nb = (cnt[i > 0 ? c - 1 : c] >= min_pc) + (cnt[i < g.nx - 1 ? c + 1 : c] >= min_pc) +
+                   (cnt[j > 0 ? c - g.nx : c] >= min_pc) + (cnt[j < g.ny - 1 ? c + g.nx : c] >= min_pc) +
+                   (cnt[k > 0 ? c - plane : c] >= min_pc) + (cnt[k < g.nz - 1 ? c + plane : c] >= min_pc);
+    return nb >= 3 ? min_pc - count : 0;
+}
+
+__device__ __forceinline__ long long rs_warp_sum(long long v) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// the exclusive offset of this warp's total inside the block (every lane
+// passes the same warp total); *total: the block's sum
+__device__ __forceinline__ long long rs_warp_offset(long long mine, long long *total) {
+    __shared__ long long wsum[8];
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) wsum[w] = mine;
+    __syncthreads();
+    long long off = 0, tot = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        off += q < w ? wsum[q] : 0;
+        tot += wsum[q];
+    }
+    *total = tot;
+    return off;
+}
+
+// countPerCellKernel (:674-679)
+__global__ void k_rs_count(G3 g, long long n, const float *__restrict__ pos, int *__restrict__ cnt) {
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x)
+        atomicAdd(cnt + cell_of(g, pos + 3 * p), 1);
+}
+
+// per-block donor totals (blocks [0, nbp)) and need totals (the rest)
+__global__ void __launch_bounds__(256) k_rs_sums(G3 g, long long n, const float *__restrict__ pos,
+                                                 const int *__restrict__ cnt, int min_pc, int max_pc, int nbp,
+                                                 long long *__restrict__ bsum_p, long long *__restrict__ bsum_c) {
+    const bool parts = (int)blockIdx.x < nbp;
+    const long long b = parts ? blockIdx.x : blockIdx.x - nbp;
+    const long long first = b * RS_CHUNK + (threadIdx.x >> 5) * RS_WARP_ITEMS + (threadIdx.x & 31);
+    const long long nc = (long long)g.nx * g.ny * g.nz;
+    long long mine = 0;
+#pragma unroll 4
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        const long long x = first + 32 * r;
+        if (parts)
+            mine += (x < n && rs_donor(g, pos, x, cnt, max_pc)) ? 1 : 0;
+        else
+            mine += x < nc ? rs_need(g, cnt, x, min_pc) : 0;
+    }
+    long long total;
+    rs_warp_offset(rs_warp_sum(mine), &total);
+    if (threadIdx.x == 0) (parts ? bsum_p : bsum_c)[b] = total;
+}
+
+// the inclusive scans of donorFlag and cellNeed (:650-651) at block
+// granularity: both block-total arrays become exclusive offsets in place;
+// tot[0] = donors (donorScan's last entry), tot[1] = cells' total need
+__global__ void __launch_bounds__(1024) k_rs_scan(long long *__restrict__ a, int na, long long *__restrict__ c, int nc,
+                                                  long long *__restrict__ tot) {
+    __shared__ long long ws[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int which = 0; which < 2; ++which) {
+        long long *x = which ? c : a;
+        const int m = which ? nc : na;
+        long long carry = 0;
+        for (int base = 0; base < m; base += 1024) {
+            const int i = base + threadIdx.x;
+            const long long v = i < m ? x[i] : 0;
+            long long s = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const long long t = __shfl_up_sync(0xffffffffu, s, o);
+                if (lane >= o) s += t;
+            }
+            if (lane == 31) ws[w] = s;
+            __syncthreads();
+            if (w == 0) {
+                long long t = ws[lane];
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const long long u = __shfl_up_sync(0xffffffffu, t, o);
+                    if (lane >= o) t += u;
+                }
+                ws[lane] = t;
+            }
+            __syncthreads();
+            if (i < m) x[i] = carry + (w ? ws[w - 1] : 0) + s - v;
+            carry += ws[31];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) tot[which] = carry;
+    }
+}
+
+// scatterDonorsKernel (:697-704): donorPool[rank] = p, rank = the number
+// of donors before p in particle order
+__global__ void __launch_bounds__(256) k_rs_scatter(G3 g, long long n, const float *__restrict__ pos,
+                                                    const int *__restrict__ cnt, int max_pc,
+                                                    const long long *__restrict__ bsum_p, int *__restrict__ pool) {
+    const int lane = threadIdx.x & 31;
+    const long long first = blockIdx.x * (long long)RS_CHUNK + (threadIdx.x >> 5) * RS_WARP_ITEMS;
+    unsigned bal[RS_ROUNDS];
+    long long mine = 0;
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        const long long x = first + 32 * r + lane;
+        bal[r] = __ballot_sync(0xffffffffu, x < n && rs_donor(g, pos, x, cnt, max_pc));
+        mine += __popc(bal[r]);
+    }
+    long long total;
+    long long run = bsum_p[blockIdx.x] + rs_warp_offset(mine, &total);
+    const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        if ((bal[r] >> lane) & 1u) pool[run + __popc(bal[r] & below)] = (int)(first + 32 * r + lane);
+        run += __popc(bal[r]);
+    }
+}
+
+// claimDonorsKernel (:726-790): the cell's slots start at the need of the
+// cells before it; while a slot is below the donor total, that donor moves
+// to the cell centre with the face-centred velocity sampled there
+__global__ void __launch_bounds__(256) k_rs_claim(G3 g, const int *__restrict__ cnt, int min_pc,
+                                                  const long long *__restrict__ bsum_c,
+                                                  const long long *__restrict__ tot, const int *__restrict__ pool,
+                                                  const float *__restrict__ u, const float *__restrict__ v,
+                                                  const float *__restrict__ w, float *__restrict__ pos,
+                                                  float *__restrict__ vel) {
+    const int lane = threadIdx.x & 31;
+    const long long nc = (long long)g.nx * g.ny * g.nz;
+    const long long first = blockIdx.x * (long long)RS_CHUNK + (threadIdx.x >> 5) * RS_WARP_ITEMS + lane;
+    int need[RS_ROUNDS];
+    long long mine = 0;
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        const long long x = first + 32 * r;
+        need[r] = x < nc ? rs_need(g, cnt, x, min_pc) : 0;
+        mine += need[r];
+    }
+    long long total;
+    long long run = bsum_c[blockIdx.x] + rs_warp_offset(rs_warp_sum(mine), &total);
+    if (total == 0) return;
+    const long long donors = tot[0];
+    const float *comp[3] = {u, v, w};
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        long long s = need[r];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long t = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += t;
+        }
+        const long long slot0 = run + s - need[r];
+        run += __shfl_sync(0xffffffffu, s, 31);
+        if (need[r] > 0 && slot0 < donors) {
+            const long long c = first + 32 * r, plane = (long long)g.nx * g.ny;
+            const int k = (int)(c / plane), rem = (int)(c - k * plane), j = rem / g.nx, i = rem - j * g.nx;
+            const F3 q = index_pos(g, comp_origin(g, 3), i, j, k);
+            float vq[3];
+            for (int a = 0; a < 3; ++a) {
+                int sx, sy, sz;
+                comp_shape(g, a, sx, sy, sz);
+                vq[a] = trilinear(comp[a], sx, sy, sz, g, comp_origin(g, a), q);
+            }
+            for (int m = 0; m < need[r] && slot0 + m < donors; ++m) {
+                const long long d = pool[slot0 + m];
+                pos[3 * d] = q.x;
+                pos[3 * d + 1] = q.y;
+                pos[3 * d + 2] = q.z;
+                vel[3 * d] = vq[0];
+                vel[3 * d + 1] = vq[1];
+                vel[3 * d + 2] = vq[2];
+            }
+        }
+    }
+}
+
 int blocks_for(long long n) { return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 152LL * 16)); }
 
 int post(const char *what) {
@@ -350,6 +553,9 @@ extern "C" void ff_flip_desc_default(ff_flip_desc *d, const int *res, const doub
     d->max_substeps = 32;
     d->concentration_atomic_scale = 4096.0;
     d->extrapolation_depth = 5;
+    d->resample_enabled = 1;   // resample defaults (:178-180)
+    d->min_particles_per_cell = 4;
+    d->max_particles_per_cell = 8;
     ff_pressure_desc_default(&d->pressure, res, h);
     d->pressure.max_plausible_pressure = 0.0;   // derived from dt, gravity and the domain
 }
@@ -367,6 +573,11 @@ struct ff_flip_s {
     int *num[3] = {}, *den[3] = {}, *valid[3] = {}, *adj[3] = {}, *vtmp[2][3] = {};
     float *scratch[3] = {};
     int *ccnt = nullptr, *cacc = nullptr;
+    // resampling: per-cell counts, the donor pool, block totals (particle
+    // blocks then cell blocks) and the two totals
+    int *rs_cnt = nullptr, *rs_pool = nullptr;
+    long long *rs_bsum = nullptr, *rs_tot = nullptr;
+    int rs_nbp = 0;
     ff_bc bc = nullptr;
     ff_advect adv = nullptr;
     ff_pressure ps = nullptr;
@@ -403,6 +614,10 @@ extern "C" int ff_flip3_destroy(ff_flip f) {
     }
     ff_dev_free(f->ccnt);
     ff_dev_free(f->cacc);
+    ff_dev_free(f->rs_cnt);
+    ff_dev_free(f->rs_pool);
+    ff_dev_free(f->rs_bsum);
+    ff_dev_free(f->rs_tot);
     delete f;
     return FF_OK;
 }
@@ -475,6 +690,16 @@ extern "C" int ff_flip3_create(ff_ctx ctx, const ff_flip_desc *d, ff_field u, ff
             if ((st = ff_field_create(ctx, FF_FLOAT, 3, fs3, &f->beta[a]))) return bail(st);
             if ((st = ff_field_fill(f->beta[a], 1.0f))) return bail(st);
         }
+    }
+    if (d->resample_enabled) {
+        const long long nc = comp_n(f->g, 3);
+        f->rs_nbp = (int)(((long long)d->max_particles + RS_CHUNK - 1) / RS_CHUNK);
+        const long long nb = f->rs_nbp + (nc + RS_CHUNK - 1) / RS_CHUNK;
+        if ((st = ff_dev_alloc((void **)&f->rs_cnt, (size_t)nc * 4, s))) return bail(st);
+        if ((st = ff_dev_alloc((void **)&f->rs_pool, (size_t)d->max_particles * 4, s))) return bail(st);
+        if ((st = ff_dev_alloc((void **)&f->rs_bsum, (size_t)nb * 8, s))) return bail(st);
+        if ((st = ff_dev_alloc((void **)&f->rs_tot, 16, s))) return bail(st);
+        if (cudaMemsetAsync(f->rs_tot, 0, 16, s) != cudaSuccess) return bail(ff_set_error(FF_E_CUDA, "flip create"));
     }
     if (density) {
         f->r0 = std::max((float)d->ambient_density, MIN_DENSITY);
@@ -674,22 +899,55 @@ extern "C" int ff_flip3_stage(ff_flip f, int stage) {
                                                       std::min(std::max((float)d.fade, 0.0f), 1.0f),
                                                       (float *)f->conc->d);
         return post("mixAndFade");
+    case FF_FLIP_RESAMPLE: {
+        // resamplePass (:813-816): counts, donors, needs, claims, then the
+        // fluid mask and face adjacency again (:806-810)
+        if (!d.resample_enabled) return FF_OK;
+        const long long nc = comp_n(g, 3);
+        const int nbp = (int)((n + RS_CHUNK - 1) / RS_CHUNK), nbc = (int)((nc + RS_CHUNK - 1) / RS_CHUNK);
+        long long *bsum_c = f->rs_bsum + f->rs_nbp;
+        FF_CUDA(cudaMemsetAsync(f->rs_cnt, 0, nc * 4, s));
+        if (n) k_rs_count<<<blocks_for(n), 256, 0, s>>>(g, n, pos, f->rs_cnt);
+        k_rs_sums<<<nbp + nbc, 256, 0, s>>>(g, n, pos, f->rs_cnt, d.min_particles_per_cell,
+                                            d.max_particles_per_cell, nbp, f->rs_bsum, bsum_c);
+        k_rs_scan<<<1, 1024, 0, s>>>(f->rs_bsum, nbp, bsum_c, nbc, f->rs_tot);
+        if (nbp) k_rs_scatter<<<nbp, 256, 0, s>>>(g, n, pos, f->rs_cnt, d.max_particles_per_cell, f->rs_bsum,
+                                                  f->rs_pool);
+        k_rs_claim<<<nbc, 256, 0, s>>>(g, f->rs_cnt, d.min_particles_per_cell, bsum_c, f->rs_tot, f->rs_pool,
+                                       uvw[0], uvw[1], uvw[2], pos, vel);
+        FF_TRY(post("resample"));
+        return ff_flip3_stage(f, FF_FLIP_MARK_FLUID);
+    }
     default:
         return ff_set_error(FF_E_ARG, "ff_flip3_stage: unknown stage %d", stage);
     }
 }
 
-// onAdvanceTimeStep (:1137-1144): pre-P2G, P2G and grid stages, the
-// projection, then the post-projection stages.  Resampling (:621-820) is
-// not part of this step.
+// onAdvanceTimeStep (:1137-1144): pre-P2G, P2G and grid stages (resampling
+// after the fluid mask, :1087-1093), the projection, then the
+// post-projection stages.
 extern "C" int ff_flip3_step(ff_flip f, ff_diag *diag) {
     FF_CHECK(f, FF_E_ARG, "NULL FLIP solver");
     static const int order[] = {FF_FLIP_ADVECT_PARTICLES, FF_FLIP_P2G,         FF_FLIP_SNAPSHOT,
                                 FF_FLIP_EXTRAPOLATE_WEIGHT, FF_FLIP_CONSTRAIN,   FF_FLIP_MARK_FLUID,
-                                FF_FLIP_CONCENTRATION_GRID, FF_FLIP_GRAVITY,     FF_FLIP_CONSTRAIN,
+                                FF_FLIP_RESAMPLE,           FF_FLIP_CONCENTRATION_GRID, FF_FLIP_GRAVITY,
+                                FF_FLIP_CONSTRAIN,
                                 FF_FLIP_PROJECT,            FF_FLIP_CONSTRAIN,   FF_FLIP_EXTRAPOLATE_PRESSURE,
                                 FF_FLIP_G2P,                FF_FLIP_CONCENTRATION_PARTICLE};
     for (int st : order) FF_TRY(ff_flip3_stage(f, st));
     if (diag) *diag = f->last;
+    return FF_OK;
+}
+
+extern "C" int ff_flip3_resample_stats(ff_flip f, int64_t *donors, int64_t *requested) {
+    FF_CHECK(f, FF_E_ARG, "NULL FLIP solver");
+    long long t[2] = {0, 0};
+    if (f->rs_tot) {
+        cudaSetDevice(f->ctx->device);
+        FF_CUDA(cudaMemcpyAsync(t, f->rs_tot, sizeof t, cudaMemcpyDeviceToHost, f->ctx->stream));
+        FF_CUDA(cudaStreamSynchronize(f->ctx->stream));
+    }
+    if (donors) *donors = t[0];
+    if (requested) *requested = t[1];
     return FF_OK;
 }

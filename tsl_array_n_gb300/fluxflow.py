@@ -581,19 +581,22 @@ class GridFlipSolver3:
     dt, gravity, reducedPressure, flipRatio, velocityDamping, p2gAtomicScale,
     weightEpsilon, closedDomainBoundaryFlag, collider, colliderPushThresh,
     colliderPushShift, carryConcentration, mixing, fade,
-    concentrationAtomicScale, ambientDensity, componentDensity, pressure})
-    (grid_flip_solver3.js:135-1157), without particle resampling."""
+    concentrationAtomicScale, ambientDensity, componentDensity, pressure,
+    resample}) (grid_flip_solver3.js:135-1157).  resample = {enabled=True,
+    minParticlesPerCell=4, maxParticlesPerCell=8} (:178-180) moves particles
+    from over-full cells to under-full cells beside the fluid each step
+    (:621-820)."""
 
     STAGES = {"advectParticles": 0, "p2g": 1, "snapshotOld": 2, "extrapolateWeight": 3, "constrainVelocity": 4,
               "markFluidCells": 5, "concentrationGrid": 6, "gravity": 7, "project": 8, "extrapolatePressure": 9,
-              "g2p": 10, "concentrationParticle": 11}
+              "g2p": 10, "concentrationParticle": 11, "resample": 12}
 
     def __init__(self, velocity_grid=None, max_particles=None, dt=None, gravity=(0.0, -9.81, 0.0),
                  reduced_pressure=True, flip_ratio=0.97, velocity_damping=0.02, p2g_atomic_scale=65536.0,
                  weight_epsilon=1e-4, closed_domain_boundary_flag=None, collider=None, collider_push_thresh=0.0,
                  collider_push_shift=0.0, carry_concentration=False, mixing=0.0, fade=0.0,
                  concentration_atomic_scale=4096.0, ambient_density=None, component_density=None, pressure=None,
-                 max_substeps=32, extrapolation_depth=5):
+                 max_substeps=32, extrapolation_depth=5, resample=None):
         if velocity_grid is None:
             raise ValueError("createGridFlipSolver3: options.velocityGrid is required.")
         if not max_particles:
@@ -621,6 +624,10 @@ class GridFlipSolver3:
         if ambient_density is not None:
             d.ambient_density, d.component_density = float(ambient_density), float(component_density)
         d.extrapolation_depth = int(extrapolation_depth)
+        rs = resample or {}
+        d.resample_enabled = int(bool(rs.get("enabled", True)))
+        d.min_particles_per_cell = int(rs.get("minParticlesPerCell", 4))
+        d.max_particles_per_cell = int(rs.get("maxParticlesPerCell", 8))
         p = pressure or {}
         mg = p.get("multigrid", {})
         pd = d.pressure
@@ -667,6 +674,12 @@ class GridFlipSolver3:
 
     def stage(self, name):
         _lib.check(_lib.load().ff_flip3_stage(self.handle, self.STAGES[name]))
+
+    def resample_stats(self):
+        """The last resampling pass: {"donors", "requested", "moved"}."""
+        dn, rq = C.c_int64(), C.c_int64()
+        _lib.check(_lib.load().ff_flip3_resample_stats(self.handle, C.byref(dn), C.byref(rq)))
+        return {"donors": dn.value, "requested": rq.value, "moved": min(dn.value, rq.value)}
 
     def on_advance_time_step(self):
         """onAdvanceTimeStep(): returns the projection's diagnostics."""
