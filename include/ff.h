@@ -271,6 +271,34 @@ int ff_velocity3_add_force(ff_ctx ctx, const int *resolution, ff_field u, ff_fie
 int ff_viscosity3_apply(ff_ctx ctx, const int *resolution, const double *grid_spacing, ff_field u, ff_field v,
                         ff_field w, double nu, double dt, ff_field u_out, ff_field v_out, ff_field w_out);
 
+/* ---- outflow: replaces createGridOutflowSolver3 (fluxflow
+ * src/grid/grid_outflow_solver3.js:79-210) with createSDFOutflow3
+ * (sdf_inflow_outflow3.js:25-29, an SDF baked like a static collider).
+ * Each outflow is a float cell SDF (borrowed) on its own grid:
+ * phi_resolution / phi_spacing / phi_origin hold 3 entries per outflow
+ * (phi_origin may be NULL: zeros).  At most 64 outflows.                  */
+typedef struct ff_outflow_s *ff_outflow;
+int ff_outflow3_create(ff_ctx ctx, const int *resolution, const double *grid_spacing, const double *origin, int n,
+                       const ff_field *phis, const int *phi_resolution, const double *phi_spacing,
+                       const double *phi_origin, double dt, int apply_velocity_bc, ff_outflow *out);
+int ff_outflow3_destroy(ff_outflow o);
+int ff_outflow3_set_dt(ff_outflow o, double dt);
+/* applyOutflowVelocityBC (:153-170): per outflow, u then v then w, faces
+ * inside relax toward the velocity one spacing upstream by the Courant
+ * number of the outward bulk speed (convective condition, :98-133); a
+ * no-op when created with apply_velocity_bc = 0                           */
+int ff_outflow3_apply_velocity_bc(ff_outflow o, ff_field u, ff_field v, ff_field w);
+/* clearOutflowScalarField(scalarGrid)() (:174-196): cells of a
+ * cell-centred scalar grid (its own geometry) inside an outflow become 0  */
+int ff_outflow3_clear_scalar(ff_outflow o, ff_field scalar, const int *resolution, const double *grid_spacing,
+                             const double *origin);
+/* the `dirichlet` closure (createOutflowPressureDirichlet3, :44-64)
+ * evaluated at the cell centres of a pressure grid: active (uint8) = 1
+ * where an outflow holds the centre, target (float) = target everywhere;
+ * pass both to ff_pressure3_set_dirichlet                                 */
+int ff_outflow3_dirichlet(ff_outflow o, const int *resolution, const double *grid_spacing, const double *origin,
+                          double target, ff_field active, ff_field target_field);
+
 /* ---- FLIP: replaces createGridFlipSolver3 (fluxflow
  * src/grid/grid_flip_solver3.js:135-1157), resampling included.  Particles
  * are FF_VEC3 positions and velocities (AoS, as the reference's vec3

@@ -13,6 +13,9 @@
  *   constrainVelocity grid_blocked_boundary_condition_solver3.js:30-477,
  *                     array_utils3.js:88-228 (Jacobi extrapolation),
  *                     level_set_utils.js:5-40 (fractionInsideSdf)
+ *   outflow           grid_outflow_solver3.js:79-210 (convective velocity
+ *                     condition, scalar clearing), sdf_inflow_outflow3.js:44-64
+ *                     (pressure Dirichlet of the outflow cells)
  *   explicit viscosity (no reference counterpart: grid_solver3.js:104 is a
  *                     no-op) u += dt nu lap(u) on interior faces, Neumann
  *                     at the array ends.
@@ -614,4 +617,118 @@ void orc_viscosity(const int *res, const float *h, const float *u, const float *
                     out[a][f] = x + c * lap;
                 }
     }
+}
+
+/* ---- outflow (grid_outflow_solver3.js:79-210) --------------------------
+ * Each outflow is a cell-centred SDF on its own grid (geometry pres/ph/po,
+ * three entries per outflow; the SDFs concatenated in phi_all); inside is
+ * phi < 0 (level_set_utils.js:5-9), sampled trilinearly (sdf_collider3.js:33-45). */
+static og_geom outflow_geom(const int *pres, const float *ph, const float *po, int q) {
+    og_geom G = {pres[3 * q], pres[3 * q + 1], pres[3 * q + 2], ph[3 * q],     ph[3 * q + 1],
+                 ph[3 * q + 2], po[3 * q], po[3 * q + 1], po[3 * q + 2]};
+    return G;
+}
+static const float *outflow_phi(const float *phi_all, const int *pres, int q) {
+    const float *p = phi_all;
+    for (int r = 0; r < q; ++r) p += (int64_t)pres[3 * r] * pres[3 * r + 1] * pres[3 * r + 2];
+    return p;
+}
+static float outflow_sample(const float *phi, const og_geom *G, f3 pt) {
+    return trilinear(phi, G->nx, G->ny, G->nz, G, comp_origin(G, 3), pt);
+}
+
+/* applyOutflowVelocityBC (:98-170): per outflow, per component (u, v, w in
+ * turn, each written back before the next is computed), a face inside the
+ * outflow with a non-zero SDF gradient relaxes toward the velocity sampled
+ * one spacing upstream, pt + n h, n = grad / |grad|, by the Courant number
+ * clamp(max(0, U . -n) dt / h, 0, 1) of the bulk velocity U at the face,
+ * then clamps to +-1e3; a face with a zero gradient keeps its value. */
+void orc_outflow_velocity(const int *res, const float *h, const float *o, float *u, float *v, float *w, float dt,
+                          int n_out, const float *phi_all, const int *pres, const float *ph, const float *po) {
+    og_field F = make_field(res, h, o, u, v, w, NULL);
+    float *data[3] = {u, v, w};
+    const float hs[3] = {h[0], h[1], h[2]};
+    for (int q = 0; q < n_out; ++q) {
+        og_geom G = outflow_geom(pres, ph, po, q);
+        const float *phi = outflow_phi(phi_all, pres, q);
+        for (int a = 0; a < 3; ++a) {
+            int sx, sy, sz;
+            comp_shape(&F.g, a, &sx, &sy, &sz);
+            const int64_t n = (int64_t)sx * sy * sz;
+            float *dst = (float *)malloc(sizeof(float) * (size_t)n);
+            unsigned char *in = (unsigned char *)calloc((size_t)n, 1);
+            const f3 oa = comp_origin(&F.g, a);
+            for (int k = 0; k < sz; ++k)
+                for (int j = 0; j < sy; ++j)
+                    for (int i = 0; i < sx; ++i) {
+                        const int64_t c = i + (int64_t)sx * (j + (int64_t)sy * k);
+                        const f3 pt = index_pos(&F.g, oa, i, j, k);
+                        if (!(outflow_sample(phi, &G, pt) < 0.0f)) continue;
+                        in[c] = 1;
+                        const float cur = data[a][c];
+                        const f3 gr = trilinear_gradient(phi, &G, comp_origin(&G, 3), pt);
+                        const float gl = sqrtf(gr.x * gr.x + gr.y * gr.y + gr.z * gr.z);
+                        if (!(gl > 0.0f)) {
+                            dst[c] = cur;
+                            continue;
+                        }
+                        const f3 nn = {gr.x / gl, gr.y / gl, gr.z / gl};
+                        const f3 up = {pt.x + nn.x * hs[a], pt.y + nn.y * hs[a], pt.z + nn.z * hs[a]};
+                        const f3 bulk = sample_vel(&F, pt);
+                        float dot = bulk.x * -nn.x;
+                        dot = dot + bulk.y * -nn.y;
+                        dot = dot + bulk.z * -nn.z;
+                        const float speed = fmaxf(0.0f, dot);
+                        const float courant = fminf(fmaxf(speed * dt / hs[a], 0.0f), 1.0f);
+                        const f3 uv = sample_vel(&F, up);
+                        const float upc = a == 0 ? uv.x : (a == 1 ? uv.y : uv.z);
+                        const float relaxed = cur + (upc - cur) * courant;
+                        dst[c] = fminf(fmaxf(relaxed, -1.0e3f), 1.0e3f);
+                    }
+            for (int64_t c = 0; c < n; ++c)
+                if (in[c]) data[a][c] = dst[c];
+            free(dst);
+            free(in);
+        }
+    }
+}
+
+/* clearOutflowScalarField (:174-196): cells of a cell-centred scalar grid
+ * (geometry sres/sh/so) inside any outflow become 0 */
+void orc_outflow_clear_scalar(const int *sres, const float *sh, const float *so, float *data, int n_out,
+                              const float *phi_all, const int *pres, const float *ph, const float *po) {
+    og_geom S = {sres[0], sres[1], sres[2], sh[0], sh[1], sh[2], so[0], so[1], so[2]};
+    const f3 oc = comp_origin(&S, 3);
+    for (int q = 0; q < n_out; ++q) {
+        og_geom G = outflow_geom(pres, ph, po, q);
+        const float *phi = outflow_phi(phi_all, pres, q);
+        for (int k = 0; k < S.nz; ++k)
+            for (int j = 0; j < S.ny; ++j)
+                for (int i = 0; i < S.nx; ++i)
+                    if (outflow_sample(phi, &G, index_pos(&S, oc, i, j, k)) < 0.0f)
+                        data[i + (int64_t)S.nx * (j + (int64_t)S.ny * k)] = 0.0f;
+    }
+}
+
+/* createOutflowPressureDirichlet3 (sdf_inflow_outflow3.js:44-64) at the
+ * cell centres of the pressure grid (geometry sres/sh/so): active where any
+ * outflow holds the centre, target everywhere */
+void orc_outflow_dirichlet(const int *sres, const float *sh, const float *so, float target, int n_out,
+                           const float *phi_all, const int *pres, const float *ph, const float *po,
+                           uint8_t *active, float *tgt) {
+    og_geom S = {sres[0], sres[1], sres[2], sh[0], sh[1], sh[2], so[0], so[1], so[2]};
+    const f3 oc = comp_origin(&S, 3);
+    for (int k = 0; k < S.nz; ++k)
+        for (int j = 0; j < S.ny; ++j)
+            for (int i = 0; i < S.nx; ++i) {
+                const int64_t c = i + (int64_t)S.nx * (j + (int64_t)S.ny * k);
+                const f3 pt = index_pos(&S, oc, i, j, k);
+                int in = 0;
+                for (int q = 0; q < n_out; ++q) {
+                    og_geom G = outflow_geom(pres, ph, po, q);
+                    in |= outflow_sample(outflow_phi(phi_all, pres, q), &G, pt) < 0.0f;
+                }
+                active[c] = (uint8_t)in;
+                tgt[c] = target;
+            }
 }

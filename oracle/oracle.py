@@ -88,6 +88,9 @@ def _declare(L):
     L.orc_constrain_velocity.argtypes = [ip, fp, fp, fp, fp, fp, fp, fp, fp, fp, I, I, fp, fp, ip, I]
     L.orc_viscosity.argtypes = [ip, fp, fp, fp, fp, F, F, fp, fp, fp]
     dp, i32p, u8p = C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_uint8)
+    L.orc_outflow_velocity.argtypes = [ip, fp, fp, fp, fp, fp, F, I, fp, ip, fp, fp]
+    L.orc_outflow_clear_scalar.argtypes = [ip, fp, fp, fp, I, fp, ip, fp, fp]
+    L.orc_outflow_dirichlet.argtypes = [ip, fp, fp, F, I, fp, ip, fp, fp, u8p, fp]
     L.orc_jitter_random.argtypes = [C.c_uint32, I, dp]
     L.orc_flip_box_seed.argtypes = [dp, dp, dp, I, D, C.c_uint32, fp, L64]
     L.orc_flip_box_seed.restype = L64
@@ -449,6 +452,43 @@ def viscosity(shape, h, u, v, w, nu, dt):
     lib().orc_viscosity(res, hh, _fptr(u), _fptr(v), _fptr(w), float(nu), float(dt), _fptr(uo), _fptr(vo),
                         _fptr(wo))
     return uo, vo, wo
+
+
+def _outflows(outflows):
+    """outflows: list of (phi, resolution, spacing, origin) -> C arguments"""
+    n = len(outflows)
+    phi = np.concatenate([_f32(q[0]) for q in outflows]) if n else np.zeros(1, np.float32)
+    pres = (C.c_int * max(3, 3 * n))(*[int(x) for q in outflows for x in q[1]])
+    ph = (C.c_float * max(3, 3 * n))(*[float(x) for q in outflows for x in q[2]])
+    po = (C.c_float * max(3, 3 * n))(*[float(x) for q in outflows for x in q[3]])
+    return n, phi, pres, ph, po
+
+
+def outflow_velocity(shape, h, origin, u, v, w, dt, outflows):
+    """applyOutflowVelocityBC (grid_outflow_solver3.js:98-170)"""
+    u, v, w = (_f32(x).copy() for x in (u, v, w))
+    res, hh, oo = _geom(shape, h, origin)
+    n, phi, pres, ph, po = _outflows(outflows)
+    lib().orc_outflow_velocity(res, hh, oo, _fptr(u), _fptr(v), _fptr(w), float(dt), n, _fptr(phi), pres, ph, po)
+    return u, v, w
+
+
+def outflow_clear_scalar(shape, h, origin, data, outflows):
+    data = _f32(data).copy()
+    res, hh, oo = _geom(shape, h, origin)
+    n, phi, pres, ph, po = _outflows(outflows)
+    lib().orc_outflow_clear_scalar(res, hh, oo, _fptr(data), n, _fptr(phi), pres, ph, po)
+    return data
+
+
+def outflow_dirichlet(shape, h, origin, outflows, target=0.0):
+    res, hh, oo = _geom(shape, h, origin)
+    n, phi, pres, ph, po = _outflows(outflows)
+    nc = int(np.prod(shape))
+    active, tgt = np.empty(nc, np.uint8), np.empty(nc, np.float32)
+    lib().orc_outflow_dirichlet(res, hh, oo, float(target), n, _fptr(phi), pres, ph, po,
+                                active.ctypes.data_as(C.POINTER(C.c_uint8)), _fptr(tgt))
+    return active, tgt
 
 
 # ------------------------------------------------------------------- FLIP --

@@ -138,3 +138,93 @@ def test_viscosity_bit_exact(gpu, oracle):
     ref = oracle.viscosity(SH, H, u, v, w, 0.002, 0.01)
     for g, r in zip(b.get(), ref):
         same(g, r)
+
+
+def outflows():
+    """Two outflows: a box slab at the high-x end on the velocity grid, and
+    a sphere near the low-x end baked on a coarser grid of its own."""
+    from tsl_array_n_gb300 import fluxflow as ff
+    a = ff.create_sdf_outflow3(*SH, *H)
+    a.add_shapes([{"type": "box", "center": [1.2, 0.5, 0.5], "halfExtents": [0.35, 2.0, 2.0]}])
+    coarse, hc = (14, 10, 12), (1 / 14, 1 / 10, 1 / 12)
+    b = ff.create_sdf_outflow3(*coarse, *hc)
+    b.add_shapes([{"type": "sphere", "center": [0.05, 0.4, 0.6], "radius": 0.25}])
+    return [a, b]
+
+
+def orc_outflows(qs):
+    return [(q.phi.to_array(), q.resolution, q.grid_spacing, q.origin) for q in qs]
+
+
+@pytest.mark.parametrize("dt", [0.01, 0.2])
+def test_outflow_velocity_bc_bit_exact(gpu, oracle, dt):
+    from tsl_array_n_gb300 import fluxflow as ff
+    u, v, w = velocity(5, amp=2.0)
+    u = u + np.float32(1.0)
+    vel = grid(u, v, w)
+    qs = outflows()
+    of = ff.create_grid_outflow_solver3(velocity_grid=vel, outflows=qs, dt=dt)
+    of.apply_outflow_velocity_bc()
+    ref = oracle.outflow_velocity(SH, H, O, u, v, w, dt, orc_outflows(qs))
+    changed = 0
+    for g, r, x in zip(vel.get(), ref, (u, v, w)):
+        same(g, r)
+        changed += int((r != x).sum())
+    assert changed > 0
+    # applyVelocityBC: false leaves the velocity alone
+    vel2 = grid(u, v, w)
+    ff.create_grid_outflow_solver3(velocity_grid=vel2, outflows=qs, dt=dt,
+                                   apply_velocity_bc=False).apply_outflow_velocity_bc()
+    for g, x in zip(vel2.get(), (u, v, w)):
+        same(g, x)
+
+
+def test_outflow_clear_scalar_and_dirichlet_bit_exact(gpu, oracle):
+    from tsl_array_n_gb300 import fluxflow as ff
+    from tsl_array_n_gb300.tsl_array_n import Field
+    u, v, w = velocity(6)
+    vel = grid(u, v, w)
+    qs = outflows()
+    of = ff.create_grid_outflow_solver3(velocity_grid=vel, outflows=qs, dt=0.01)
+    rng = np.random.default_rng(9)
+    s = rng.random(SH[0] * SH[1] * SH[2]).astype(np.float32) + 0.5
+    f = Field("float", SH).from_array(s)
+    of.clear_outflow_scalar_field(f)()
+    ref = oracle.outflow_clear_scalar(SH, H, O, s, orc_outflows(qs))
+    same(f.to_array(), ref)
+    assert (ref == 0).any()
+    a, t = of.dirichlet.fields(SH, H, O)
+    ra, rt = oracle.outflow_dirichlet(SH, H, O, orc_outflows(qs))
+    assert np.array_equal(a.to_array(), ra)
+    same(t.to_array(), rt)
+    # the standalone factory with a target
+    a2, t2 = ff.create_outflow_pressure_dirichlet3(qs, target=0.5).fields(SH, H, O)
+    assert np.array_equal(a2.to_array(), ra) and np.all(t2.to_array() == np.float32(0.5))
+
+
+def test_projection_with_outflow_dirichlet(gpu):
+    """A channel with a uniform inflow at low x and an outflow slab at high
+    x: the projection pins the outflow cells to p = 0 and converges, and the
+    velocity leaving the fluid region is divergence-free."""
+    from tsl_array_n_gb300 import fluxflow as ff
+    u, v, w = velocity(7, amp=0.5)
+    u = u + np.float32(1.0)
+    vel = grid(u, v, w)
+    out = grid(u, v, w)
+    of = ff.create_grid_outflow_solver3(velocity_grid=vel, outflows=outflows()[:1], dt=0.01)
+    ps = ff.create_grid_pressure_solver3(SH, H, O, dirichlet=of.dirichlet, tolerance=1e-6)
+    ps.project(vel, out)()
+    d = ps.diagnostics
+    assert d["converged"] and not d["rejected"], d
+    a, _ = of.dirichlet.fields(SH, H, O)
+    pinned = a.to_array().astype(bool)
+    p = ps.pressure.to_array()
+    assert pinned.any() and np.all(p[pinned] == 0)
+    # combined with a host-side condition: b wins where both are active
+    left = lambda x, y, z: (x < 0.1, np.full_like(x, 2.0))
+    comb = ff.combine_dirichlet3(of.dirichlet, left)
+    ca, ct = comb.fields(SH, H, O)
+    ca, ct = ca.to_array().astype(bool), ct.to_array()
+    x = ff.cell_positions(SH, H, O)[0]
+    assert np.array_equal(ca, pinned | (x < 0.1))
+    assert np.all(ct[x < 0.1] == 2.0) and np.all(ct[pinned & ~(x < 0.1)] == 0.0)

@@ -128,3 +128,93 @@ def test_viscosity_constant_and_quadratic(oracle):
     U, U0 = uo.reshape(nz, ny, nx + 1), u.reshape(nz, ny, nx + 1)
     inner = (slice(None), slice(1, ny - 1), slice(1, nx))
     np.testing.assert_allclose(U[inner] - U0[inner], 0.002, rtol=2e-3)
+
+
+# ---- outflow (grid_outflow_solver3.js) ------------------------------------
+def slab_phi(sh, h, o, x0):
+    """The padded outflow slab x > x0 of the reference's examples: phi =
+    x0 - x at the cell centres, so the SDF gradient is (-1, 0, 0), pointing
+    back into the fluid."""
+    nx, ny, nz = sh
+    x = o[0] + (np.arange(nx) + 0.5) * h[0]
+    return np.broadcast_to((x0 - x).astype(np.float32), (nz, ny, nx)).ravel().copy()
+
+
+def face_x(sh, h, o, a):
+    nx, ny, nz = sh
+    s = [(nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1)][a]
+    off = 0.0 if a == 0 else 0.5
+    return np.broadcast_to(o[0] + (np.arange(s[0]) + off) * h[0], s[::-1]).ravel()
+
+
+def test_outflow_courant_one_is_an_upwind_copy(oracle):
+    """A slab with a bulk velocity U dt / h >= 1: every face inside takes
+    the value one spacing upstream (toward the fluid) as it was before the
+    pass -- a component's relaxed values are written back only after the
+    whole component is computed."""
+    sh, h, o = SH, H, O
+    x0 = 10 / 12
+    phi = slab_phi(sh, h, o, x0)
+    su, sv, sw = sizes(sh)
+    rng = np.random.default_rng(3)
+    u = (2.0 + 0.1 * rng.standard_normal(su)).astype(np.float32)   # outward everywhere
+    v = rng.standard_normal(sv).astype(np.float32)
+    w = rng.standard_normal(sw).astype(np.float32)
+    dt = 1.0   # U dt / h >> 1: courant 1
+    uo, vo, wo = oracle.outflow_velocity(sh, h, o, u, v, w, dt, [(phi, sh, h, o)])
+    nx, ny, nz = sh
+    U, Uo = u.reshape(nz, ny, nx + 1), uo.reshape(nz, ny, nx + 1)
+    xu = face_x(sh, h, o, 0).reshape(nz, ny, nx + 1)
+    inside = xu > x0 + 1e-6
+    # outside the slab nothing changes
+    assert np.array_equal(Uo[~inside], U[~inside])
+    # inside: the u face one spacing toward the fluid (the upstream sample
+    # lands on that face up to the rounding of pt - h)
+    ii = np.nonzero(inside[0, 0])[0]
+    np.testing.assert_allclose(Uo[:, :, ii], U[:, :, ii - 1], rtol=1e-5, atol=1e-6)
+
+
+def test_outflow_inflow_faces_and_convexity(oracle):
+    sh, h, o = SH, H, O
+    phi = slab_phi(sh, h, o, 9 / 12)
+    su, sv, sw = sizes(sh)
+    rng = np.random.default_rng(4)
+    v = rng.standard_normal(sv).astype(np.float32)
+    w = rng.standard_normal(sw).astype(np.float32)
+    # flow back in through the outflow: courant 0, the u faces keep their values
+    u_in = np.full(su, -1.5, np.float32) + (0.01 * rng.standard_normal(su)).astype(np.float32)
+    uo, _, _ = oracle.outflow_velocity(sh, h, o, u_in, v, w, 0.01, [(phi, sh, h, o)])
+    assert np.array_equal(uo, u_in)
+    # partial courant: each relaxed u face lies between its old value and the upstream one
+    u = (1.0 + rng.random(su)).astype(np.float32)
+    uo, _, _ = oracle.outflow_velocity(sh, h, o, u, v, w, 0.02, [(phi, sh, h, o)])
+    nx, ny, nz = sh
+    U, Uo = u.reshape(nz, ny, nx + 1), uo.reshape(nz, ny, nx + 1)
+    changed = Uo != U
+    assert changed.any()
+    kk, jj, ii = np.nonzero(changed)
+    lo = np.minimum(U[kk, jj, ii], U[kk, jj, ii - 1]) - 1e-5
+    hi = np.maximum(U[kk, jj, ii], U[kk, jj, ii - 1]) + 1e-5
+    assert np.all((Uo[kk, jj, ii] >= lo) & (Uo[kk, jj, ii] <= hi))
+
+
+def test_outflow_clear_scalar_and_dirichlet(oracle):
+    sh, h, o = SH, H, O
+    x0 = 9 / 12
+    phi = slab_phi(sh, h, o, x0)
+    rng = np.random.default_rng(5)
+    s = rng.random(np.prod(sh)).astype(np.float32) + 0.5
+    out = oracle.outflow_clear_scalar(sh, h, o, s, [(phi, sh, h, o)])
+    inside = phi < 0
+    assert np.all(out[inside] == 0) and np.array_equal(out[~inside], s[~inside])
+    active, target = oracle.outflow_dirichlet(sh, h, o, [(phi, sh, h, o)], target=0.25)
+    assert np.array_equal(active.astype(bool), inside) and np.all(target == np.float32(0.25))
+    # a second outflow on a coarser grid ORs in
+    sh2, h2 = (6, 5, 4), (1 / 6, 1 / 5, 1 / 4)
+    nx2, ny2, nz2 = sh2   # the low-x end: phi = x - 2/6
+    phi2 = np.broadcast_to(((o[0] + (np.arange(nx2) + 0.5) * h2[0]) - 2 / 6).astype(np.float32),
+                           (nz2, ny2, nx2)).ravel().copy()
+    active2, _ = oracle.outflow_dirichlet(sh, h, o, [(phi, sh, h, o), (phi2, sh2, h2, o)])
+    nx, ny, nz = sh
+    xc = np.broadcast_to(o[0] + (np.arange(nx) + 0.5) * h[0], (nz, ny, nx)).ravel()
+    assert np.array_equal(active2.astype(bool), (xc > x0) | (xc < 2 / 6))

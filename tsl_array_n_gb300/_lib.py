@@ -116,6 +116,13 @@ PROTOTYPES = {
     "ff_viscosity3_apply": (_I, [_P, _IP, C.POINTER(C.c_double), _P, _P, _P, _D, _D, _P, _P, _P]),
     "ff_velocity3_add_force": (_I, [_P, _IP, _P, _P, _P, _D, _D, _D, _D]),
     "ff_flip_desc_default": (None, [C.POINTER(FlipDesc), _IP, C.POINTER(C.c_double), _I, _D]),
+    "ff_outflow3_create": (_I, [_P, _IP, C.POINTER(C.c_double), C.POINTER(C.c_double), _I, _PP, _IP,
+                                C.POINTER(C.c_double), C.POINTER(C.c_double), _D, _I, _PP]),
+    "ff_outflow3_destroy": (_I, [_P]),
+    "ff_outflow3_set_dt": (_I, [_P, _D]),
+    "ff_outflow3_apply_velocity_bc": (_I, [_P, _P, _P, _P]),
+    "ff_outflow3_clear_scalar": (_I, [_P, _P, _IP, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "ff_outflow3_dirichlet": (_I, [_P, _IP, C.POINTER(C.c_double), C.POINTER(C.c_double), _D, _P, _P]),
     "ff_flip3_create": (_I, [_P, C.POINTER(FlipDesc), _P, _P, _P, _PP]),
     "ff_flip3_destroy": (_I, [_P]),
     "ff_flip3_set_collider": (_I, [_P, _P]),

@@ -592,3 +592,211 @@ extern "C" int ff_viscosity3_apply(ff_ctx ctx, const int *res, const double *h, 
     }
     return post("viscosity");
 }
+
+// ---------------------------------------------------------------- outflow --
+// createGridOutflowSolver3 (src/grid/grid_outflow_solver3.js:79-210).  Each
+// outflow is a cell-centred SDF on its own grid, inside where phi < 0
+// (level_set_utils.js:5-9), sampled trilinearly (sdf_collider3.js:33-45).
+namespace {
+
+// extrapolate kernel of applyOutflowVelocityBC (:98-133) for one outflow and
+// one component: faces inside the outflow relax toward the velocity one
+// spacing upstream (pt + n h, n the unit SDF gradient) by the Courant number
+// of the outward bulk speed, clamped to +-1e3; a zero gradient keeps the
+// face.  Faces outside are not written (the copy kernel skips them too).
+__global__ void k_outflow_relax(VelField F, int a, G3 pg, const float *__restrict__ phi, float dt,
+                                float *__restrict__ dst) {
+    int sx, sy, sz;
+    comp_shape(F.g, a, sx, sy, sz);
+    const long long n = (long long)sx * sy * sz;
+    const F3 o = comp_origin(F.g, a), po = comp_origin(pg, 3);
+    const float h = a == 0 ? F.g.hx : (a == 1 ? F.g.hy : F.g.hz);
+    const float *cur_d = a == 0 ? F.u : (a == 1 ? F.v : F.w);
+    for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < n; f += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        unflatten(f, sx, sy, i, j, k);
+        const F3 pt = index_pos(F.g, o, i, j, k);
+        if (!(trilinear(phi, pg.nx, pg.ny, pg.nz, pg, po, pt) < 0.0f)) continue;
+        const float cur = cur_d[f];
+        const F3 gr = trilinear_gradient(phi, pg, po, pt);
+        const float gl = sqrtf(gr.x * gr.x + gr.y * gr.y + gr.z * gr.z);
+        if (!(gl > 0.0f)) {
+            dst[f] = cur;
+            continue;
+        }
+        const F3 nn{gr.x / gl, gr.y / gl, gr.z / gl};
+        const F3 up{pt.x + nn.x * h, pt.y + nn.y * h, pt.z + nn.z * h};
+        const F3 bulk = sample_vel(F, pt);
+        float dot = bulk.x * -nn.x;
+        dot = dot + bulk.y * -nn.y;
+        dot = dot + bulk.z * -nn.z;
+        const float courant = fminf(fmaxf(fmaxf(0.0f, dot) * dt / h, 0.0f), 1.0f);
+        const F3 uv = sample_vel(F, up);
+        const float upc = a == 0 ? uv.x : (a == 1 ? uv.y : uv.z);
+        const float relaxed = cur + (upc - cur) * courant;
+        dst[f] = fminf(fmaxf(relaxed, -1.0e3f), 1.0e3f);
+    }
+}
+
+// copy kernel (:137-150): faces inside the outflow take the relaxed value;
+// also clearOutflowScalarField (:174-196) with src == nullptr (a = 3, the
+// cells of a scalar grid, set to 0)
+__global__ void k_outflow_copy(G3 g, int a, G3 pg, const float *__restrict__ phi, const float *__restrict__ src,
+                               float *__restrict__ data) {
+    int sx, sy, sz;
+    if (a == 3) {
+        sx = g.nx;
+        sy = g.ny;
+        sz = g.nz;
+    } else {
+        comp_shape(g, a, sx, sy, sz);
+    }
+    const long long n = (long long)sx * sy * sz;
+    const F3 o = comp_origin(g, a), po = comp_origin(pg, 3);
+    for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < n; f += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        unflatten(f, sx, sy, i, j, k);
+        if (trilinear(phi, pg.nx, pg.ny, pg.nz, pg, po, index_pos(g, o, i, j, k)) < 0.0f)
+            data[f] = src ? src[f] : 0.0f;
+    }
+}
+
+// createOutflowPressureDirichlet3 (sdf_inflow_outflow3.js:44-64) at the cell
+// centres of grid g (dataPosition, grid_data3.js:10-18): active where any
+// outflow holds the centre; the target everywhere
+__global__ void k_outflow_dirichlet(G3 g, int n_out, const float *const *__restrict__ phis,
+                                    const G3 *__restrict__ pgs, float target, uint8_t *__restrict__ active,
+                                    float *__restrict__ tgt) {
+    const long long n = (long long)g.nx * g.ny * g.nz;
+    const F3 o = comp_origin(g, 3);
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        unflatten(c, g.nx, g.ny, i, j, k);
+        const F3 pt = index_pos(g, o, i, j, k);
+        bool in = false;
+        for (int q = 0; q < n_out; ++q) {
+            const G3 pg = pgs[q];
+            in |= trilinear(phis[q], pg.nx, pg.ny, pg.nz, pg, comp_origin(pg, 3), pt) < 0.0f;
+        }
+        active[c] = in ? 1 : 0;
+        tgt[c] = target;
+    }
+}
+
+}  // namespace
+
+struct ff_outflow_s {
+    ff_ctx ctx = nullptr;
+    G3 g{};
+    float dt = 0.0f;
+    int apply = 1;
+    std::vector<ff_field> phi;   // borrowed
+    std::vector<G3> pg;
+    float *dst[3] = {};
+    const float **d_phi = nullptr;   // device copies for the Dirichlet kernel
+    G3 *d_pg = nullptr;
+};
+
+extern "C" int ff_outflow3_destroy(ff_outflow o) {
+    if (!o) return FF_OK;
+    cudaStreamSynchronize(o->ctx->stream);
+    for (int a = 0; a < 3; ++a) ff_dev_free(o->dst[a]);
+    ff_dev_free((void *)o->d_phi);
+    ff_dev_free(o->d_pg);
+    delete o;
+    return FF_OK;
+}
+
+extern "C" int ff_outflow3_create(ff_ctx ctx, const int *res, const double *h, const double *origin, int n,
+                                  const ff_field *phis, const int *phi_res, const double *phi_h,
+                                  const double *phi_origin, double dt, int apply_velocity_bc, ff_outflow *out) {
+    FF_CHECK(ctx && res && h && out && n >= 0 && (n == 0 || (phis && phi_res && phi_h)), FF_E_ARG,
+             "ff_outflow3_create: bad arguments");
+    FF_CHECK(res[0] > 0 && res[1] > 0 && res[2] > 0, FF_E_ARG, "createGridOutflowSolver3: bad resolution");
+    FF_CHECK(n <= 64, FF_E_LIMIT, "createGridOutflowSolver3: at most 64 outflows");
+    *out = nullptr;
+    std::vector<G3> pg(n);
+    for (int q = 0; q < n; ++q) {
+        pg[q] = geom_of(phi_res + 3 * q, phi_h + 3 * q, phi_origin ? phi_origin + 3 * q : nullptr);
+        FF_CHECK(pg[q].nx > 0 && pg[q].ny > 0 && pg[q].nz > 0 && field_is(phis[q], comp_count(pg[q], 3)), FF_E_ARG,
+                 "createGridOutflowSolver3: outflow %d must be a float cell SDF of its grid's shape", q);
+    }
+    cudaSetDevice(ctx->device);
+    ff_outflow o = new ff_outflow_s();
+    o->ctx = ctx;
+    o->g = geom_of(res, h, origin);
+    o->dt = (float)dt;
+    o->apply = apply_velocity_bc != 0;
+    o->phi.assign(phis, phis + n);
+    o->pg = pg;
+    int st = FF_OK;
+    for (int a = 0; a < 3 && st == FF_OK; ++a)
+        st = ff_dev_alloc((void **)&o->dst[a], (size_t)comp_count(o->g, a) * 4, ctx->stream);
+    if (st == FF_OK) st = ff_dev_alloc((void **)&o->d_phi, sizeof(float *) * std::max(1, n), ctx->stream);
+    if (st == FF_OK) st = ff_dev_alloc((void **)&o->d_pg, sizeof(G3) * std::max(1, n), ctx->stream);
+    if (st == FF_OK && n) {
+        std::vector<const float *> hp(n);
+        for (int q = 0; q < n; ++q) hp[q] = (const float *)phis[q]->d;
+        if (cudaMemcpy(o->d_phi, hp.data(), sizeof(float *) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(o->d_pg, pg.data(), sizeof(G3) * n, cudaMemcpyHostToDevice) != cudaSuccess)
+            st = ff_set_error(FF_E_CUDA, "createGridOutflowSolver3: upload");
+    }
+    if (st != FF_OK) {
+        ff_outflow3_destroy(o);
+        return st;
+    }
+    *out = o;
+    return FF_OK;
+}
+
+extern "C" int ff_outflow3_set_dt(ff_outflow o, double dt) {
+    FF_CHECK(o, FF_E_ARG, "NULL outflow solver");
+    o->dt = (float)dt;
+    return FF_OK;
+}
+
+extern "C" int ff_outflow3_apply_velocity_bc(ff_outflow o, ff_field u, ff_field v, ff_field w) {
+    FF_CHECK(o, FF_E_ARG, "NULL outflow solver");
+    ff_field fs[3] = {u, v, w};
+    for (int a = 0; a < 3; ++a)
+        FF_CHECK(field_is(fs[a], comp_count(o->g, a)), FF_E_ARG, "applyOutflowVelocityBC: component %d shape", a);
+    if (!o->apply) return FF_OK;
+    cudaSetDevice(o->ctx->device);
+    cudaStream_t s = o->ctx->stream;
+    VelField F{o->g, (const float *)u->d, (const float *)v->d, (const float *)w->d, nullptr};
+    for (size_t q = 0; q < o->phi.size(); ++q)
+        for (int a = 0; a < 3; ++a) {
+            const long long n = comp_count(o->g, a);
+            const float *phi = (const float *)o->phi[q]->d;
+            k_outflow_relax<<<launch_blocks(n), 256, 0, s>>>(F, a, o->pg[q], phi, o->dt, o->dst[a]);
+            k_outflow_copy<<<launch_blocks(n), 256, 0, s>>>(o->g, a, o->pg[q], phi, o->dst[a], (float *)fs[a]->d);
+        }
+    return post("applyOutflowVelocityBC");
+}
+
+extern "C" int ff_outflow3_clear_scalar(ff_outflow o, ff_field scalar, const int *res, const double *h,
+                                        const double *origin) {
+    FF_CHECK(o && res && h, FF_E_ARG, "clearOutflowScalarField: NULL argument");
+    const G3 sg = geom_of(res, h, origin);
+    FF_CHECK(field_is(scalar, comp_count(sg, 3)), FF_E_ARG, "clearOutflowScalarField: float cell field expected");
+    cudaSetDevice(o->ctx->device);
+    const long long n = comp_count(sg, 3);
+    for (size_t q = 0; q < o->phi.size(); ++q)
+        k_outflow_copy<<<launch_blocks(n), 256, 0, o->ctx->stream>>>(sg, 3, o->pg[q], (const float *)o->phi[q]->d,
+                                                                    nullptr, (float *)scalar->d);
+    return post("clearOutflowScalarField");
+}
+
+extern "C" int ff_outflow3_dirichlet(ff_outflow o, const int *res, const double *h, const double *origin,
+                                     double target, ff_field active, ff_field target_field) {
+    FF_CHECK(o && res && h, FF_E_ARG, "outflow dirichlet: NULL argument");
+    const G3 cg = geom_of(res, h, origin);
+    const long long n = comp_count(cg, 3);
+    FF_CHECK(active && active->dtype == FF_UINT8 && active->count == n && field_is(target_field, n), FF_E_ARG,
+             "outflow dirichlet: active must be a uint8 and target a float cell field");
+    cudaSetDevice(o->ctx->device);
+    k_outflow_dirichlet<<<launch_blocks(n), 256, 0, o->ctx->stream>>>(cg, (int)o->phi.size(), o->d_phi, o->d_pg,
+                                                                      (float)target, (uint8_t *)active->d,
+                                                                      (float *)target_field->d);
+    return post("outflow dirichlet");
+}

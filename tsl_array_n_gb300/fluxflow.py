@@ -247,6 +247,12 @@ class GridPressureSolver3:
         if dl is None:
             _lib.check(_lib.load().ff_pressure3_set_dirichlet(self.handle, None, None))
             return
+        if hasattr(dl, "fields"):
+            # evaluated on the device (outflow Dirichlet, combinations)
+            a, t = dl.fields(self.resolution, self.grid_spacing, self.origin)
+            self._keep["dirichlet"] = (a, t)
+            _lib.check(_lib.load().ff_pressure3_set_dirichlet(self.handle, a.handle, t.handle))
+            return
         if callable(dl):
             x, y, z = cell_positions(self.resolution, self.grid_spacing, self.origin)
             active, target = dl(x, y, z)
@@ -526,6 +532,148 @@ def create_grid_blocked_boundary_condition_solver3(velocity, nx, ny, nz, hx, hy,
                                                    collider=None, inflows=None, collider_face_weights=None):
     return GridBlockedBoundaryConditionSolver3(velocity, (nx, ny, nz), (hx, hy, hz), (ox, oy, oz), collider,
                                                inflows, collider_face_weights)
+
+
+class SDFOutflow3(SDFStaticCollider3):
+    """createSDFOutflow3 (sdf_inflow_outflow3.js:25-29): an outflow region,
+    baked like a static collider (solid = inside the outflow)."""
+
+
+def create_sdf_outflow3(nx, ny, nz, hx, hy, hz, ox=0.0, oy=0.0, oz=0.0):
+    return SDFOutflow3((nx, ny, nz), (hx, hy, hz), (ox, oy, oz))
+
+
+def _outflow_handle(res, spacing, origin, outflows, dt, apply_velocity_bc):
+    n = len(outflows)
+    h = C.c_void_p()
+    _lib.check(_lib.load().ff_outflow3_create(
+        context().handle, (C.c_int * 3)(*res), (C.c_double * 3)(*spacing), (C.c_double * 3)(*origin), n,
+        (C.c_void_p * max(1, n))(*[q.phi.handle.value for q in outflows]),
+        (C.c_int * max(3, 3 * n))(*[int(x) for q in outflows for x in q.resolution]),
+        (C.c_double * max(3, 3 * n))(*[float(x) for q in outflows for x in q.grid_spacing]),
+        (C.c_double * max(3, 3 * n))(*[float(x) for q in outflows for x in q.origin]),
+        float(dt), int(bool(apply_velocity_bc)), C.byref(h)))
+    return h
+
+
+class OutflowPressureDirichlet3:
+    """createOutflowPressureDirichlet3(outflows, {target = 0})
+    (sdf_inflow_outflow3.js:44-64): Dirichlet wherever an outflow holds a
+    cell centre.  GridPressureSolver3 evaluates it on the device at its own
+    cell centres (``fields``)."""
+
+    def __init__(self, outflows, target=0.0, _handle=None, _owner=None):
+        self.outflows = list(outflows) if isinstance(outflows, (list, tuple)) else [outflows]
+        self.target = float(target)
+        self._owner = _owner
+        self._own = _handle is None
+        self.handle = _handle if _handle is not None else _outflow_handle((1, 1, 1), (1.0,) * 3, (0.0,) * 3,
+                                                                           self.outflows, 0.0, False)
+
+    def fields(self, resolution, grid_spacing, origin=(0.0, 0.0, 0.0)):
+        a, t = Field("uint8", tuple(resolution)), Field("float", tuple(resolution))
+        _lib.check(_lib.load().ff_outflow3_dirichlet(self.handle, (C.c_int * 3)(*resolution),
+                                                     (C.c_double * 3)(*grid_spacing), (C.c_double * 3)(*origin),
+                                                     self.target, a.handle, t.handle))
+        return a, t
+
+    def close(self):
+        if self._own and getattr(self, "handle", None):
+            _lib.load().ff_outflow3_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def create_outflow_pressure_dirichlet3(outflows, target=0.0):
+    return OutflowPressureDirichlet3(outflows, target)
+
+
+def _dirichlet_arrays(d, resolution, grid_spacing, origin):
+    n = int(np.prod(resolution))
+    if hasattr(d, "fields"):
+        a, t = d.fields(resolution, grid_spacing, origin)
+        return a.to_array().astype(bool), t.to_array()
+    active, target = d(*cell_positions(resolution, grid_spacing, origin)) if callable(d) else d
+    return (np.broadcast_to(np.asarray(active, bool), (n,)),
+            np.broadcast_to(np.asarray(target, np.float32), (n,)))
+
+
+class _CombinedDirichlet3:
+    def __init__(self, a, b):
+        self.a, self.b = a, b
+
+    def fields(self, resolution, grid_spacing, origin=(0.0, 0.0, 0.0)):
+        aa, at = _dirichlet_arrays(self.a, resolution, grid_spacing, origin)
+        ba, bt = _dirichlet_arrays(self.b, resolution, grid_spacing, origin)
+        return (Field("uint8", tuple(resolution)).from_array((aa | ba).astype(np.uint8)),
+                Field("float", tuple(resolution)).from_array(np.where(ba, bt, at).astype(np.float32)))
+
+
+def combine_dirichlet3(a, b):
+    """combineDirichlet3 (sdf_inflow_outflow3.js:77-94): active where
+    either is, b's target where b is active (b wins on overlap)."""
+    if not a:
+        return b
+    if not b:
+        return a
+    return _CombinedDirichlet3(a, b)
+
+
+class GridOutflowSolver3:
+    """createGridOutflowSolver3({velocityGrid, velocityPrev, outflows, dt,
+    applyVelocityBC}) (grid_outflow_solver3.js:79-210): the pressure
+    Dirichlet of the outflow cells (``dirichlet``), the convective velocity
+    condition (``apply_outflow_velocity_bc``) and scalar clearing
+    (``clear_outflow_scalar_field``).  velocityPrev is accepted and unused,
+    as in the reference."""
+
+    def __init__(self, velocity_grid, outflows, dt, apply_velocity_bc=True, velocity_prev=None):
+        g = velocity_grid
+        self.velocity_grid = g
+        self.outflows = list(outflows) if isinstance(outflows, (list, tuple)) else [outflows]
+        self.handle = _outflow_handle(g.resolution, g.grid_spacing, g.origin, self.outflows, dt, apply_velocity_bc)
+        self.dirichlet = OutflowPressureDirichlet3(self.outflows, 0.0, _handle=self.handle, _owner=self)
+
+    def set_dt(self, dt):
+        _lib.check(_lib.load().ff_outflow3_set_dt(self.handle, float(dt)))
+
+    def apply_outflow_velocity_bc(self):
+        g = self.velocity_grid
+        _lib.check(_lib.load().ff_outflow3_apply_velocity_bc(self.handle, g.data_u.handle, g.data_v.handle,
+                                                             g.data_w.handle))
+
+    def clear_outflow_scalar_field(self, scalar, resolution=None, grid_spacing=None, origin=None):
+        """Returns clear(): zero the cells of ``scalar`` (a float cell Field;
+        geometry defaults to the velocity grid's) inside any outflow."""
+        g = self.velocity_grid
+        res = (C.c_int * 3)(*(resolution or g.resolution))
+        h = (C.c_double * 3)(*(grid_spacing or g.grid_spacing))
+        o = (C.c_double * 3)(*(origin or g.origin))
+
+        def clear():
+            _lib.check(_lib.load().ff_outflow3_clear_scalar(self.handle, scalar.handle, res, h, o))
+        return clear
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.load().ff_outflow3_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def create_grid_outflow_solver3(velocity_grid=None, outflows=None, dt=None, apply_velocity_bc=True,
+                                velocity_prev=None):
+    return GridOutflowSolver3(velocity_grid, outflows, dt, apply_velocity_bc, velocity_prev)
 
 
 def apply_viscosity3(input_grid, output_grid, nu, dt):
