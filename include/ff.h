@@ -373,6 +373,72 @@ int ff_flip3_resample_stats(ff_flip f, int64_t *donors, int64_t *requested);
 /* onAdvanceTimeStep(): every stage in the reference's order; diag is the
  * projection's diagnostics                                                */
 int ff_flip3_step(ff_flip f, ff_diag *diag);
+/* ---- 2D two-phase FLIP: replaces createGridTwoPhaseFlipSolver2 (fluxflow
+ * src/grid/grid_two_phase_flip_solver2.js:479-1622), run on a
+ * one-cell-thick grid (u, v: the 2D face arrays; particles on the plane
+ * through the cell centres).  Every cell is fluid; density and beta faces
+ * follow the particles' concentration; the pressure is pinned to 0 at
+ * pin_cell (pressurePin; {-1, -1} = null).                                 */
+typedef struct ff_twophase_s *ff_twophase;
+typedef struct {
+    int resolution[2];
+    double grid_spacing[2];
+    double origin[2];
+    int max_particles;             /* maxParticles (required)             */
+    double dt;
+    double gravity[2];             /* default (0, -9.81)                   */
+    double ambient_density;        /* gasDensity / ambientDensity, 0.01    */
+    double component_density;      /* liquidDensity / componentDensity, 1  */
+    double mixing, fade;           /* default 0, 0                         */
+    double concentration_atomic_scale;   /* default 4096                   */
+    double flip_ratio;             /* default 0.97                         */
+    double gas_flip_ratio;         /* default 0.90                         */
+    double velocity_damping;       /* default 0.02                         */
+    double p2g_atomic_scale;       /* default 65536                        */
+    double weight_epsilon;         /* default 1e-4                         */
+    int closed_flags;              /* closedDomainBoundaryFlag, default 15 */
+    int max_substeps;              /* of the particle trace, default 32    */
+    double collider_push_thresh, collider_push_shift;
+    int pin_cell[2];               /* default topCenter (nx/2, ny-1)       */
+    int resample_enabled;          /* resample.enabled, default 1          */
+    int min_particles_per_cell;    /* default 3                            */
+    int max_particles_per_cell;    /* default 8                            */
+    int extrapolation_depth;       /* default 5                            */
+    ff_pressure_desc pressure;     /* multigrid levels default: deepest of
+                                      up to 4 the resolution divides into  */
+} ff_twophase_desc;
+void ff_twophase_desc_default(ff_twophase_desc *d, const int *resolution, const double *grid_spacing,
+                              int max_particles, double dt);
+int ff_twophase2_create(ff_ctx ctx, const ff_twophase_desc *desc, ff_field u, ff_field v, ff_twophase *out);
+int ff_twophase2_destroy(ff_twophase t);
+int ff_twophase2_set_collider(ff_twophase t, ff_field phi);
+int ff_twophase2_set_count(ff_twophase t, int n);
+/* positions / velocities as 2D pairs (x, y), phase (concentration) per
+ * particle; NULL leaves that array alone                                  */
+int ff_twophase2_set_particles(ff_twophase t, int n, const float *xy, const float *vxy, const float *phase);
+int ff_twophase2_get_particles(ff_twophase t, int n, float *xy, float *vxy, float *phase);
+/* borrowed handles: phase (= concentration), liquidFraction, density
+ * (cells), betaU, betaV (faces), and the pressure solver                   */
+int ff_twophase2_fields(ff_twophase t, ff_field *phase, ff_field *liquid_fraction, ff_field *density,
+                        ff_field *beta_u, ff_field *beta_v, ff_pressure *pressure);
+#define FF_TP_ADVECT 0             /* advectParticles + pushOutOfCollider  */
+#define FF_TP_DENSITY 1            /* countPhases, density, betaU/V        */
+#define FF_TP_P2G 2                /* scatter + finalize U/V               */
+#define FF_TP_SNAPSHOT 3           /* snapshotOldU/V                       */
+#define FF_TP_EXTRAPOLATE_WEIGHT 4 /* extrapolateWeightU/V                 */
+#define FF_TP_CONSTRAIN 5          /* boundarySolver.constrainVelocity     */
+#define FF_TP_GRAVITY 6            /* applyGravityU/V                      */
+#define FF_TP_PROJECT 7            /* the variable-density projection      */
+#define FF_TP_G2P 8                /* g2pUpdate (per-phase blend)          */
+#define FF_TP_MIX 9                /* mixConcentration (mixing / fade)     */
+#define FF_TP_RESAMPLE 10          /* per-phase resamplePass               */
+int ff_twophase2_stage(ff_twophase t, int stage);
+/* onAdvanceTimeStep(): every stage in the reference's order               */
+int ff_twophase2_step(ff_twophase t, ff_diag *diag);
+/* the last resampling pass: {liquid donors, liquid cells' need, gas
+ * donors, gas cells' need}.  Synchronises the stream.                      */
+int ff_twophase2_resample_stats(ff_twophase t, int64_t *out4);
+
 /* computeFlipBoxSeed3 (:70-130): per_axis^3 jittered particles per cell,
  * mulberry32(seed) (jitter_random.js:29-46), in doubles as JavaScript.
  * positions NULL: only *count.  FF_E_LIMIT when capacity is too small.    */

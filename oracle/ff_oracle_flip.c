@@ -15,6 +15,11 @@
  *   G2P                             :909-922
  *   advectParticles, pushOutOfCollider :925-957
  *   resamplePass                    :621-820
+ * and of the 2D two-phase solver (grid_two_phase_flip_solver2.js):
+ *   countPhases / density / beta    :646-762
+ *   g2pUpdate (per-phase blend)     :966-992
+ *   mixConcentration                :1055-1073
+ *   per-phase resamplePass          :1226-1494
  */
 #include <math.h>
 #include <stdint.h>
@@ -505,5 +510,189 @@ int64_t orc_flip_resample(const int *res, const float *h, const float *o, int64_
     free(cnt);
     free(pool);
     free(cell);
+    return moved;
+}
+
+/* ==== 2D two-phase FLIP (grid_two_phase_flip_solver2.js) =================
+ * Written in 2D with (x, y) pairs, independently of the one-cell-thick 3D
+ * layout the device runs it on. */
+typedef struct {
+    int nx, ny;
+    float hx, hy, ox, oy;
+} fg2;
+
+/* cellIndexOf (:608-614) */
+static int64_t cell2(const fg2 *g, const float *p) {
+    float cx = gclamp((p[0] - g->ox) / g->hx), cy = gclamp((p[1] - g->oy) / g->hy);
+    int i = iclamp((int)floorf(cx), 0, g->nx - 1), j = iclamp((int)floorf(cy), 0, g->ny - 1);
+    return i + (int64_t)g->nx * j;
+}
+/* collocatedValueAtPosition2 (grid_math.js:35-73) */
+static float bilinear2(const float *d, int sx, int sy, float ox, float oy, float hx, float hy, float x, float y) {
+    float gx = gclamp((x - ox) / hx), gy = gclamp((y - oy) / hy);
+    int i0 = (int)floorf(gx), j0 = (int)floorf(gy);
+    float fx = gx - (float)i0, fy = gy - (float)j0;
+    int i0c = iclamp(i0, 0, sx - 1), i1c = iclamp(i0 + 1, 0, sx - 1);
+    int j0c = iclamp(j0, 0, sy - 1), j1c = iclamp(j0 + 1, 0, sy - 1);
+    float ux = 1.0f - fx, uy = 1.0f - fy;
+    float s = d[i0c + (int64_t)sx * j0c] * (ux * uy);
+    s = s + d[i1c + (int64_t)sx * j0c] * (fx * uy);
+    s = s + d[i0c + (int64_t)sx * j1c] * (ux * fy);
+    s = s + d[i1c + (int64_t)sx * j1c] * (fx * fy);
+    return s;
+}
+/* faceCenteredValueAtPosition2 (grid_math.js:75-90) */
+static void face2(const fg2 *g, const float *u, const float *v, float x, float y, float *out) {
+    out[0] = bilinear2(u, g->nx + 1, g->ny, g->ox, g->oy + g->hy * 0.5f, g->hx, g->hy, x, y);
+    out[1] = bilinear2(v, g->nx, g->ny + 1, g->ox + g->hx * 0.5f, g->oy, g->hx, g->hy, x, y);
+}
+
+/* countPhasesKernel, computeDensityKernel, computeBetaU/V (:646-762) */
+void orc_tp_density(const int *res, const float *h, const float *o, int64_t n, const float *pos, const float *phase,
+                    float cscale, float rho0, float rho1, int32_t *cnt, int32_t *acc, float *frac, float *rho,
+                    float *bu, float *bv) {
+    fg2 g = {res[0], res[1], h[0], h[1], o[0], o[1]};
+    const int nx = g.nx, ny = g.ny;
+    const int64_t nc = (int64_t)nx * ny;
+    memset(cnt, 0, 4 * (size_t)nc);
+    memset(acc, 0, 4 * (size_t)nc);
+    for (int64_t p = 0; p < n; ++p) {
+        int64_t c = cell2(&g, pos + 2 * p);
+        cnt[c] = (int32_t)((uint32_t)cnt[c] + 1u);
+        acc[c] = (int32_t)((uint32_t)acc[c] + (uint32_t)sat_i32(rintf(fminf(fmaxf(phase[p], 0.0f), 1.0f) * cscale)));
+    }
+    const float r0 = fmaxf(rho0, 1e-4f), r1 = fmaxf(rho1, 1e-4f), rref = fmaxf(r0, r1);
+    for (int64_t c = 0; c < nc; ++c) {
+        float total = (float)cnt[c], sum = (float)acc[c] / cscale;
+        float mean = sum / fmaxf(total, 1.0f);
+        float f = total > 0.5f ? fminf(fmaxf(mean, 0.0f), 1.0f) : 0.0f;
+        frac[c] = f;
+        rho[c] = r0 + (r1 - r0) * f;
+    }
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i <= nx; ++i)
+            bu[i + (int64_t)(nx + 1) * j] =
+                rref / fmaxf((rho[iclamp(i - 1, 0, nx - 1) + (int64_t)nx * j] + rho[iclamp(i, 0, nx - 1) + (int64_t)nx * j]) *
+                                 0.5f, 1e-4f);
+    for (int j = 0; j <= ny; ++j)
+        for (int i = 0; i < nx; ++i)
+            bv[i + (int64_t)nx * j] =
+                rref / fmaxf((rho[i + (int64_t)nx * iclamp(j - 1, 0, ny - 1)] + rho[i + (int64_t)nx * iclamp(j, 0, ny - 1)]) *
+                                 0.5f, 1e-4f);
+}
+
+/* g2pUpdate (:966-992): the FLIP/PIC blend ratio runs from gas_ratio at
+ * concentration 0 to flip_ratio at 1 */
+void orc_tp_g2p(const int *res, const float *h, const float *o, int64_t n, const float *pos, float *vel,
+                const float *phase, const float *u, const float *v, const float *uo, const float *vo, float flip_ratio,
+                float gas_ratio, float damping) {
+    fg2 g = {res[0], res[1], h[0], h[1], o[0], o[1]};
+    const float fr = fminf(fmaxf(flip_ratio, 0.0f), 1.0f), gr = fminf(fmaxf(gas_ratio, 0.0f), 1.0f);
+    const float damp = fminf(fmaxf(damping, 0.0f), 1.0f);
+    for (int64_t p = 0; p < n; ++p) {
+        float nv[2], ov[2], out[2];
+        face2(&g, u, v, pos[2 * p], pos[2 * p + 1], nv);
+        face2(&g, uo, vo, pos[2 * p], pos[2 * p + 1], ov);
+        const float c = fminf(fmaxf(phase[p], 0.0f), 1.0f);
+        const float ratio = gr + (fr - gr) * c;
+        int bad = 0;
+        for (int a = 0; a < 2; ++a) {
+            float delta = nv[a] - ov[a];
+            float flipv = vel[2 * p + a] + delta;
+            float blended = flipv * ratio + nv[a] * (1.0f - ratio);
+            out[a] = blended * (1.0f - damp);
+            bad |= nonfinite(out[a]);
+        }
+        for (int a = 0; a < 2; ++a) vel[2 * p + a] = bad ? 0.0f : fminf(fmaxf(out[a], -500.0f), 500.0f);
+    }
+}
+
+/* mixConcentration (:1055-1073) */
+void orc_tp_mix(const int *res, const float *h, const float *o, int64_t n, const float *pos, const float *frac,
+                float mixing, float fade, float *phase) {
+    fg2 g = {res[0], res[1], h[0], h[1], o[0], o[1]};
+    const float mx = fminf(fmaxf(mixing, 0.0f), 1.0f), fd = fminf(fmaxf(fade, 0.0f), 1.0f);
+    for (int64_t p = 0; p < n; ++p) {
+        float sampled = bilinear2(frac, g.nx, g.ny, g.ox + g.hx * 0.5f, g.oy + g.hy * 0.5f, g.hx, g.hy, pos[2 * p],
+                                  pos[2 * p + 1]);
+        float c = fminf(fmaxf(phase[p], 0.0f), 1.0f);
+        float local = nonfinite(sampled) ? c : sampled;
+        float blended = c + (local - c) * mx;
+        phase[p] = fminf(fmaxf(blended * (1.0f - fd), 0.0f), 1.0f);
+    }
+}
+
+/* resamplePassNow (:1226-1494) on the counts (cnt, acc) of orc_tp_density:
+ * recipients' signed need, liquid / gas donor ranks in particle order in a
+ * pool filled from both ends (each half capped at max(1, maxParticles/2)),
+ * claims in flat cell order.  stats: liquid donors, liquid need, gas
+ * donors, gas need.  Returns the number of particles moved. */
+int64_t orc_tp_resample(const int *res, const float *h, const float *o, int64_t n, int max_particles, float *pos,
+                        float *vel, const float *phase, const float *u, const float *v, const int32_t *cnt,
+                        const int32_t *acc, float cscale, int min_pc, int max_pc, int64_t *stats) {
+    fg2 g = {res[0], res[1], h[0], h[1], o[0], o[1]};
+    const int nx = g.nx, ny = g.ny;
+    const int64_t nc = (int64_t)nx * ny;
+    int32_t *need = (int32_t *)malloc(4 * (size_t)nc);
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+            const int64_t c = i + (int64_t)nx * j;
+            const int64_t l = i > 0 ? c - 1 : c, r = i < nx - 1 ? c + 1 : c, d = j > 0 ? c - nx : c,
+                          up = j < ny - 1 ? c + nx : c;
+            const int count = cnt[c];
+            const int nb = (cnt[l] >= min_pc) + (cnt[r] >= min_pc) + (cnt[d] >= min_pc) + (cnt[up] >= min_pc);
+            const float total = (float)count, sum = (float)acc[c] / cscale;
+            const float ntot = (float)(int32_t)((uint32_t)cnt[l] + (uint32_t)cnt[r] + (uint32_t)cnt[d] + (uint32_t)cnt[up]);
+            const float nsum =
+                (float)(int32_t)((uint32_t)acc[l] + (uint32_t)acc[r] + (uint32_t)acc[d] + (uint32_t)acc[up]) / cscale;
+            const float own = sum / fmaxf(total, 1.0f), around = nsum / fmaxf(ntot, 1.0f);
+            const int liquid = total > 0.5f ? own > 0.5f : around > 0.5f;
+            const int needed = min_pc - count;
+            need[c] = (count < min_pc && nb >= 2) ? (liquid ? needed : -needed) : 0;
+        }
+    const int64_t half = max_particles / 2 > 1 ? max_particles / 2 : 1, top = max_particles - 1;
+    int *pool = (int *)malloc(sizeof(int) * (size_t)(max_particles > 0 ? max_particles : 1));
+    int64_t nl = 0, ng = 0;
+    for (int64_t p = 0; p < n; ++p) {
+        if (!(cnt[cell2(&g, pos + 2 * p)] > max_pc)) continue;
+        if (phase[p] > 0.5f) {
+            if (nl < half) pool[nl] = (int)p;
+            ++nl;
+        } else {
+            if (ng < half) pool[top - ng] = (int)p;
+            ++ng;
+        }
+    }
+    const int64_t avl = nl < half ? nl : half, avg = ng < half ? ng : half;
+    int64_t bl = 0, bg = 0, moved = 0;
+    const float ccx = g.ox + g.hx * 0.5f, ccy = g.oy + g.hy * 0.5f;
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+            const int q = need[i + (int64_t)nx * j];
+            if (q == 0) continue;
+            const int liquid = q > 0;
+            const int64_t needed = liquid ? q : -q, base = liquid ? bl : bg, avail = liquid ? avl : avg;
+            if (liquid) bl += needed;
+            else bg += needed;
+            for (int64_t m = 0; m < needed && base + m < avail; ++m) {
+                const int64_t dnr = pool[liquid ? base + m : top - (base + m)];
+                const float x = ccx + (float)i * g.hx, y = ccy + (float)j * g.hy;
+                float vv[2];
+                face2(&g, u, v, x, y, vv);
+                pos[2 * dnr] = x;
+                pos[2 * dnr + 1] = y;
+                vel[2 * dnr] = vv[0];
+                vel[2 * dnr + 1] = vv[1];
+                ++moved;
+            }
+        }
+    if (stats) {
+        stats[0] = nl;
+        stats[1] = bl;
+        stats[2] = ng;
+        stats[3] = bg;
+    }
+    free(need);
+    free(pool);
     return moved;
 }

@@ -104,6 +104,12 @@ def _declare(L):
     L.orc_flip_reduced_gravity.argtypes = [ip, fp, fp, fp, fp, fp, fp, fp, F, F, fp, fp, fp]
     L.orc_flip_mix_fade.argtypes = [ip, fp, fp, L64, fp, fp, F, F, fp]
     L.orc_flip_advect.argtypes = [ip, fp, fp, fp, fp, fp, fp, F, I, L64, fp, fp, F, F]
+    L.orc_tp_density.argtypes = [ip, fp, fp, L64, fp, fp, F, F, F, i32p, i32p, fp, fp, fp, fp]
+    L.orc_tp_g2p.argtypes = [ip, fp, fp, L64, fp, fp, fp, fp, fp, fp, fp, F, F, F]
+    L.orc_tp_mix.argtypes = [ip, fp, fp, L64, fp, fp, F, F, fp]
+    L.orc_tp_resample.argtypes = [ip, fp, fp, L64, I, fp, fp, fp, fp, fp, i32p, i32p, F, I, I,
+                                  C.POINTER(C.c_int64)]
+    L.orc_tp_resample.restype = L64
     L.orc_flip_resample.argtypes = [ip, fp, fp, L64, fp, fp, fp, fp, fp, I, I]
     L.orc_flip_resample.restype = L64
 
@@ -621,3 +627,54 @@ def flip_resample(shape, h, origin, pos, vel, u, v, w, min_pc=4, max_pc=8):
     moved = lib().orc_flip_resample(res, hh, oo, pos.size // 3, _fptr(pos), _fptr(vel), _fptr(_f32(u)),
                                     _fptr(_f32(v)), _fptr(_f32(w)), int(min_pc), int(max_pc))
     return pos, vel, int(moved)
+
+
+# ------------------------------------------------------- two-phase FLIP 2D --
+# grid_two_phase_flip_solver2.js, restated in 2D in ff_oracle_flip.c.
+def _geom2(shape, h, origin):
+    return ((C.c_int * 2)(*shape), (C.c_float * 2)(*[float(x) for x in h]),
+            (C.c_float * 2)(*[float(x) for x in origin]))
+
+
+def tp_density(shape, h, origin, pos, phase, rho0, rho1, cscale=4096.0):
+    """returns cnt, acc (int32 cells), liquidFraction, density, betaU, betaV"""
+    nx, ny = shape
+    pos, phase = _f32(pos), _f32(phase)
+    cnt, acc = np.empty(nx * ny, np.int32), np.empty(nx * ny, np.int32)
+    frac, rho = np.empty(nx * ny, np.float32), np.empty(nx * ny, np.float32)
+    bu, bv = np.empty((nx + 1) * ny, np.float32), np.empty(nx * (ny + 1), np.float32)
+    res, hh, oo = _geom2(shape, h, origin)
+    lib().orc_tp_density(res, hh, oo, pos.size // 2, _fptr(pos), _fptr(phase), float(cscale), float(rho0),
+                         float(rho1), _i32(cnt), _i32(acc), _fptr(frac), _fptr(rho), _fptr(bu), _fptr(bv))
+    return cnt, acc, frac, rho, bu, bv
+
+
+def tp_g2p(shape, h, origin, pos, vel, phase, new, old, flip_ratio=0.97, gas_ratio=0.9, damping=0.02):
+    vel = _f32(vel).copy()
+    res, hh, oo = _geom2(shape, h, origin)
+    lib().orc_tp_g2p(res, hh, oo, _f32(pos).size // 2, _fptr(_f32(pos)), _fptr(vel), _fptr(_f32(phase)),
+                     _fptr(_f32(new[0])), _fptr(_f32(new[1])), _fptr(_f32(old[0])), _fptr(_f32(old[1])),
+                     float(flip_ratio), float(gas_ratio), float(damping))
+    return vel
+
+
+def tp_mix(shape, h, origin, pos, frac, phase, mixing, fade):
+    phase = _f32(phase).copy()
+    res, hh, oo = _geom2(shape, h, origin)
+    lib().orc_tp_mix(res, hh, oo, _f32(pos).size // 2, _fptr(_f32(pos)), _fptr(_f32(frac)), float(mixing),
+                     float(fade), _fptr(phase))
+    return phase
+
+
+def tp_resample(shape, h, origin, pos, vel, phase, u, v, cnt, acc, max_particles, min_pc=3, max_pc=8,
+                cscale=4096.0):
+    """returns positions, velocities, moved, stats (liquid donors, liquid
+    need, gas donors, gas need)"""
+    pos, vel = _f32(pos).copy(), _f32(vel).copy()
+    stats = np.zeros(4, np.int64)
+    res, hh, oo = _geom2(shape, h, origin)
+    moved = lib().orc_tp_resample(res, hh, oo, pos.size // 2, int(max_particles), _fptr(pos), _fptr(vel),
+                                  _fptr(_f32(phase)), _fptr(_f32(u)), _fptr(_f32(v)),
+                                  _i32(np.ascontiguousarray(cnt, np.int32)), _i32(np.ascontiguousarray(acc, np.int32)),
+                                  float(cscale), int(min_pc), int(max_pc), stats.ctypes.data_as(C.POINTER(C.c_int64)))
+    return pos, vel, int(moved), stats

@@ -180,3 +180,97 @@ def test_resample_no_donors_or_no_need(oracle):
     # an empty particle set
     p, vv, moved = oracle.flip_resample(sh, h, o, np.zeros(0, np.float32), np.zeros(0, np.float32), u, v, w)
     assert moved == 0 and p.size == 0
+
+
+# ---- 2D two-phase (grid_two_phase_flip_solver2.js) -------------------------
+def test_two_phase_box_seed():
+    from tsl_array_n_gb300 import fluxflow as ff
+    seed = ff.compute_two_phase_box_seed((0.0, 0.0), (1.0, 0.5), 0.125, 0.125, is_liquid=lambda p: p[1] < 0.25)
+    assert seed["count"] == 8 * 4 * 4
+    pos = seed["positionsArray"].reshape(-1, 2)
+    assert np.array_equal(seed["phasesArray"] > 0.5, pos[:, 1] < 0.25)
+    assert seed["liquidCount"] + seed["gasCount"] == seed["count"]
+    # the first particle from mulberry32's first two values (jitter_random.js)
+    r = mulberry32_py(0x9E3779B9, 2)
+    sub = 0.125 / 2
+    x = 0.0 + 0 * 0.125 + 0.5 * sub + (r[0] * 2 - 1) * 0.2 * sub
+    y = 0.0 + 0 * 0.125 + 0.5 * sub + (r[1] * 2 - 1) * 0.2 * sub
+    assert pos[0, 0] == np.float32(x) and pos[0, 1] == np.float32(y)
+    c = ff.compute_two_phase_box_seed((0.0, 0.0), (0.5, 0.5), 0.25, 0.25, concentration_at=lambda p: 3 * p[0] - 0.5)
+    assert c["phasesArray"].min() >= 0 and c["phasesArray"].max() <= 1 and 0 < c["meanConcentration"] < 1
+
+
+def test_two_phase_density_and_beta(oracle):
+    sh, h, o = (10, 8), (0.1, 0.125), (0.0, 0.0)
+    rng = np.random.default_rng(1)
+    n = 400
+    pos = (rng.random((n, 2)) * [1.0, 1.0]).astype(np.float32)
+    phase = (pos[:, 1] < 0.5).astype(np.float32)
+    cnt, acc, frac, rho, bu, bv = oracle.tp_density(sh, h, o, pos, phase, 0.01, 1.0)
+    assert cnt.sum() == n and np.all((frac >= 0) & (frac <= 1))
+    empty = cnt == 0
+    assert np.all(frac[empty] == 0)
+    np.testing.assert_allclose(rho, 0.01 + (1.0 - 0.01) * frac, rtol=1e-6)
+    R = rho.reshape(8, 10)
+    BU = bu.reshape(8, 11)
+    np.testing.assert_allclose(BU[:, 1:-1], 1.0 / ((R[:, :-1] + R[:, 1:]) * 0.5), rtol=1e-6)
+    np.testing.assert_allclose(BU[:, 0], 1.0 / R[:, 0], rtol=1e-6)
+    # the reference density is the heavier component: beta >= 1 everywhere,
+    # and exactly 1 between two all-liquid cells
+    c1, _, _, _, bu1, bv1 = oracle.tp_density(sh, h, o, pos, np.ones(n, np.float32), 0.01, 1.0)
+    assert np.all(bu1 >= 1.0) and np.all(bv1 >= 1.0)
+    occ = c1.reshape(8, 10) > 0
+    assert np.all(bu1.reshape(8, 11)[:, 1:-1][occ[:, :-1] & occ[:, 1:]] == 1.0)
+
+
+def tp_resample_numpy(sh, h, o, pos, vel, phase, u, v, cnt, acc, max_particles, min_pc, max_pc, cscale=4096.0):
+    """The per-phase resampling a second way, vectorised."""
+    nx, ny = sh
+    f32 = np.float32
+    pos = pos.reshape(-1, 2).copy()
+    vel = vel.reshape(-1, 2).copy()
+    C = cnt.reshape(ny, nx).astype(np.int64)
+    A = acc.reshape(ny, nx).astype(np.int64)
+    pad = lambda X: (np.concatenate([X[:, :1], X[:, :-1]], 1), np.concatenate([X[:, 1:], X[:, -1:]], 1),
+                     np.concatenate([X[:1], X[:-1]], 0), np.concatenate([X[1:], X[-1:]], 0))
+    nb = sum((q >= min_pc).astype(int) for q in pad(C))
+    ntot = sum(pad(C)).astype(f32)
+    nsum = sum(pad(A)).astype(f32) / f32(cscale)
+    own = (A.astype(f32) / f32(cscale)) / np.maximum(C.astype(f32), f32(1))
+    around = nsum / np.maximum(ntot, f32(1))
+    liquid = np.where(C > 0, own > 0.5, around > 0.5)
+    needed = min_pc - C
+    need = np.where((C < min_pc) & (nb >= 2), np.where(liquid, needed, -needed), 0).ravel()
+    cell = np.clip(np.floor((pos - np.array(o, f32)) / np.array(h, f32)).astype(int), 0, [nx - 1, ny - 1])
+    over = cnt[cell[:, 0] + nx * cell[:, 1]] > max_pc
+    half, top = max(1, max_particles // 2), max_particles - 1
+    lq = np.nonzero(over & (phase > 0.5))[0]
+    gs = np.nonzero(over & ~(phase > 0.5))[0]
+    moved = 0
+    for sign, donors in ((1, lq), (-1, gs)):
+        want = np.where(sign * need > 0, sign * need, 0)
+        cells = np.repeat(np.arange(need.size), want)[:min(donors.size, half)]
+        movers = donors[:cells.size]
+        i, j = cells % nx, cells // nx
+        pos[movers, 0] = (f32(o[0]) + f32(h[0]) * f32(0.5)) + i.astype(f32) * f32(h[0])
+        pos[movers, 1] = (f32(o[1]) + f32(h[1]) * f32(0.5)) + j.astype(f32) * f32(h[1])
+        moved += movers.size
+    return pos.ravel(), moved
+
+
+@pytest.mark.parametrize("mm", [(3, 8), (4, 6)])
+def test_two_phase_resample_matches_vectorised_restatement(oracle, mm):
+    sh, h, o = (16, 12), (1 / 16, 1 / 12), (0.0, 0.0)
+    rng = np.random.default_rng(6)
+    n = 5 * 16 * 12
+    pos = (rng.random((n, 2)) ** 1.7).astype(np.float32)   # crowded near the origin, sparse far from it
+    vel = rng.standard_normal((n, 2)).astype(np.float32)
+    phase = (rng.random(n) < 0.6).astype(np.float32)
+    u = rng.standard_normal(17 * 12).astype(np.float32)
+    v = rng.standard_normal(16 * 13).astype(np.float32)
+    cnt, acc, *_ = oracle.tp_density(sh, h, o, pos, phase, 0.01, 1.0)
+    p1, v1, moved, stats = oracle.tp_resample(sh, h, o, pos, vel, phase, u, v, cnt, acc, n, *mm)
+    p2, moved2 = tp_resample_numpy(sh, h, o, pos, vel, phase, u, v, cnt, acc, n, *mm)
+    assert moved > 0 and moved == moved2
+    assert np.array_equal(p1, p2)
+    assert stats[1] > 0 and stats[3] > 0   # both phases asked for particles

@@ -52,6 +52,18 @@ class FlipDesc(C.Structure):
                 ("min_particles_per_cell", C.c_int), ("max_particles_per_cell", C.c_int)]
 
 
+class TwoPhaseDesc(C.Structure):
+    _fields_ = [("resolution", C.c_int * 2), ("grid_spacing", C.c_double * 2), ("origin", C.c_double * 2),
+                ("max_particles", C.c_int), ("dt", C.c_double), ("gravity", C.c_double * 2),
+                ("ambient_density", C.c_double), ("component_density", C.c_double), ("mixing", C.c_double),
+                ("fade", C.c_double), ("concentration_atomic_scale", C.c_double), ("flip_ratio", C.c_double),
+                ("gas_flip_ratio", C.c_double), ("velocity_damping", C.c_double), ("p2g_atomic_scale", C.c_double),
+                ("weight_epsilon", C.c_double), ("closed_flags", C.c_int), ("max_substeps", C.c_int),
+                ("collider_push_thresh", C.c_double), ("collider_push_shift", C.c_double),
+                ("pin_cell", C.c_int * 2), ("resample_enabled", C.c_int), ("min_particles_per_cell", C.c_int),
+                ("max_particles_per_cell", C.c_int), ("extrapolation_depth", C.c_int), ("pressure", PressureDesc)]
+
+
 class Diag(C.Structure):
     _fields_ = [("converged", C.c_int), ("rejected", C.c_int), ("iterations", C.c_int),
                 ("stopped_by", C.c_int), ("residual", C.c_double), ("b_norm", C.c_double),
@@ -131,6 +143,17 @@ PROTOTYPES = {
     "ff_flip3_grid_fields": (_I, [_P, _PP, _PP, _PP, _PP, _PP, _PP, _PP]),
     "ff_flip3_stage": (_I, [_P, _I]),
     "ff_flip3_step": (_I, [_P, C.POINTER(Diag)]),
+    "ff_twophase_desc_default": (None, [C.POINTER(TwoPhaseDesc), _IP, C.POINTER(C.c_double), _I, _D]),
+    "ff_twophase2_create": (_I, [_P, C.POINTER(TwoPhaseDesc), _P, _P, _PP]),
+    "ff_twophase2_destroy": (_I, [_P]),
+    "ff_twophase2_set_collider": (_I, [_P, _P]),
+    "ff_twophase2_set_count": (_I, [_P, _I]),
+    "ff_twophase2_set_particles": (_I, [_P, _I, _FP, _FP, _FP]),
+    "ff_twophase2_get_particles": (_I, [_P, _I, _FP, _FP, _FP]),
+    "ff_twophase2_fields": (_I, [_P, _PP, _PP, _PP, _PP, _PP, _PP]),
+    "ff_twophase2_stage": (_I, [_P, _I]),
+    "ff_twophase2_step": (_I, [_P, C.POINTER(Diag)]),
+    "ff_twophase2_resample_stats": (_I, [_P, C.POINTER(C.c_int64)]),
     "ff_flip3_resample_stats": (_I, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "ff_flip_box_seed3": (_I, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double), _I, _D,
                                C.c_uint32, _FP, C.c_int64, C.POINTER(C.c_int64)]),

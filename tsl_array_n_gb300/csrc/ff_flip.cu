@@ -33,9 +33,12 @@ __device__ __forceinline__ long long cell_of(const G3 &g, const float *p) {
     return i + (long long)g.nx * (j + (long long)g.ny * k);
 }
 
-// advectParticles (:925-933) then pushOutOfCollider (:939-951)
+// advectParticles (:925-933) then pushOutOfCollider (:939-951).  keep_z:
+// particles of a one-cell-thick grid standing in for a 2D one stay on their
+// plane (the trace leaves z alone there anyway, except for the rounding of
+// the collider-crossing blend)
 __global__ void k_flip_advect(VelField F, long long n, float *__restrict__ pos, float dt, int max_substeps, F3 mn,
-                              F3 mx, float push_thresh, float push_shift) {
+                              F3 mx, float push_thresh, float push_shift, int keep_z) {
     const F3 oc = comp_origin(F.g, 3);
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
         const F3 prev{pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]};
@@ -56,7 +59,7 @@ __global__ void k_flip_advect(VelField F, long long n, float *__restrict__ pos, 
         }
         pos[3 * p] = q.x;
         pos[3 * p + 1] = q.y;
-        pos[3 * p + 2] = q.z;
+        pos[3 * p + 2] = keep_z ? prev.z : q.z;
     }
 }
 
@@ -67,15 +70,16 @@ __global__ void k_flip_mark(G3 g, long long n, const float *__restrict__ pos, fl
 }
 
 // buildScatter (:508-530): each particle adds round(v w S) and round(w S)
-// to the 8 faces around it, per component
+// to the 8 faces around it, per component (the first ncomp components)
 __global__ void k_flip_scatter(G3 g, long long n, const float *__restrict__ pos, const float *__restrict__ vel,
                                float scale, int *__restrict__ nu, int *__restrict__ du, int *__restrict__ nv,
-                               int *__restrict__ dv, int *__restrict__ nw, int *__restrict__ dw) {
+                               int *__restrict__ dv, int *__restrict__ nw, int *__restrict__ dw, int ncomp) {
     int *num[3] = {nu, nv, nw}, *den[3] = {du, dv, dw};
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
         const F3 q{pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]};
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
+            if (a >= ncomp) break;
             int sx, sy, sz;
             comp_shape(g, a, sx, sy, sz);
             const F3 o = comp_origin(g, a);
@@ -172,7 +176,9 @@ __global__ void k_flip_conc_resolve(long long nc, const int *__restrict__ cnt, c
     }
 }
 
-// computeBetaU/V/W with faceDensity (:315-345)
+// computeBetaU/V/W with faceDensity (:315-345); mask == nullptr: every
+// cell is fluid, the face density is the mean of its two cells
+// (grid_two_phase_flip_solver2.js:750-762)
 __global__ void k_flip_beta(G3 g, int a, const float *__restrict__ rho, const float *__restrict__ mask, float rref,
                             float *__restrict__ beta) {
     int s[3];
@@ -188,7 +194,7 @@ __global__ void k_flip_beta(G3 g, int a, const float *__restrict__ rho, const fl
         const long long ca = A[0] + (long long)g.nx * (A[1] + (long long)g.ny * A[2]);
         const long long cb = B[0] + (long long)g.nx * (B[1] + (long long)g.ny * B[2]);
         const float ra = rho[ca], rb = rho[cb];
-        const bool fa = mask[ca] > 0.5f, fb = mask[cb] > 0.5f;
+        const bool fa = !mask || mask[ca] > 0.5f, fb = !mask || mask[cb] > 0.5f;
         const float rf = (fa && fb) ? (ra + rb) * 0.5f : ((fa || fb) ? (fa ? ra : rb) : rref);
         beta[f] = rref / fmaxf(rf, MIN_DENSITY);
     }
@@ -225,14 +231,18 @@ __global__ void k_flip_gravity(G3 g, int a, const float *__restrict__ rho, const
     }
 }
 
-// g2pUpdate (:909-922)
+// g2pUpdate (:909-922).  conc != nullptr: the per-particle blend of the
+// two-phase solver, gas_ratio + (ratio - gas_ratio) clamp(c, 0, 1)
+// (grid_two_phase_flip_solver2.js:966-992)
 __global__ void k_flip_g2p(G3 g, long long n, const float *__restrict__ pos, float *__restrict__ vel,
                            const float *__restrict__ u, const float *__restrict__ v, const float *__restrict__ w,
                            const float *__restrict__ uo, const float *__restrict__ vo, const float *__restrict__ wo,
-                           float ratio, float damp) {
+                           float flip_ratio, float damp, const float *__restrict__ conc, float gas_ratio) {
     const float *nw[3] = {u, v, w}, *od[3] = {uo, vo, wo};
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
         const F3 q{pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]};
+        const float ratio =
+            conc ? gas_ratio + (flip_ratio - gas_ratio) * fminf(fmaxf(conc[p], 0.0f), 1.0f) : flip_ratio;
         float out[3];
         bool bad = false;
 #pragma unroll
@@ -467,6 +477,210 @@ __global__ void __launch_bounds__(256) k_rs_claim(G3 g, const int *__restrict__ 
                 vel[3 * d + 1] = vq[1];
                 vel[3 * d + 2] = vq[2];
             }
+        }
+    }
+}
+
+// ---- per-phase resampling of the 2D two-phase solver
+// (grid_two_phase_flip_solver2.js:1226-1500) on the one-cell-thick grid.
+// Two donor pools share one buffer: liquid donors (phase > 0.5) rank
+// upward from 0, gas donors downward from the top, each capped at
+// pool_half; a cell's need is signed (+ liquid, - gas) and each phase's
+// cells claim from that phase's pool in flat cell order.
+
+// computeRecipientNeedKernel (:1298-1310): eligible below min_pc with at
+// least 2 of the 4 clamped neighbours at min_pc or more; the phase is the
+// cell's own majority, or its neighbours' when it is empty
+// (recipientWantsLiquid, :1270-1296)
+__global__ void k_tp_need(G3 g, const int *__restrict__ cnt, const int *__restrict__ acc, float cscale, int min_pc,
+                          int *__restrict__ need) {
+    const long long nc = (long long)g.nx * g.ny;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < nc; c += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(c / g.nx), i = (int)(c - (long long)j * g.nx);
+        const long long l = i > 0 ? c - 1 : c, r = i < g.nx - 1 ? c + 1 : c;
+        const long long d = j > 0 ? c - g.nx : c, u = j < g.ny - 1 ? c + g.nx : c;
+        const int count = cnt[c];
+        const int nb = (cnt[l] >= min_pc) + (cnt[r] >= min_pc) + (cnt[d] >= min_pc) + (cnt[u] >= min_pc);
+        const bool eligible = count < min_pc && nb >= 2;
+        const float total = (float)count, sum = (float)acc[c] / cscale;
+        const float ntot = (float)(cnt[l] + cnt[r] + cnt[d] + cnt[u]);
+        const float nsum = (float)(acc[l] + acc[r] + acc[d] + acc[u]) / cscale;
+        const float own = sum / fmaxf(total, 1.0f), around = nsum / fmaxf(ntot, 1.0f);
+        const bool liquid = total > 0.5f ? own > 0.5f : around > 0.5f;
+        const int needed = min_pc - count;
+        need[c] = eligible ? (liquid ? needed : -needed) : 0;
+    }
+}
+
+// offsets of this warp's two totals inside the block, and the block's sums
+__device__ __forceinline__ void rs_warp_offset2(long long a, long long b, long long &oa, long long &ob, long long &ta,
+                                                long long &tb) {
+    __shared__ long long ws[2][8];
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        ws[0][w] = a;
+        ws[1][w] = b;
+    }
+    __syncthreads();
+    oa = ob = ta = tb = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        oa += q < w ? ws[0][q] : 0;
+        ob += q < w ? ws[1][q] : 0;
+        ta += ws[0][q];
+        tb += ws[1][q];
+    }
+}
+
+__device__ __forceinline__ bool tp_over(const G3 &g, const float *__restrict__ pos, long long p,
+                                        const int *__restrict__ cnt, int max_pc) {
+    return cnt[cell_of(g, pos + 3 * p)] > max_pc;
+}
+
+// per-block totals: particle blocks count liquid and gas donors
+// (markDonorsKernel, :1316-1327), cell blocks sum the split needs
+// (splitNeedKernel, :1359-1368)
+__global__ void __launch_bounds__(256) k_tp_sums(G3 g, long long n, const float *__restrict__ pos,
+                                                 const float *__restrict__ phase, const int *__restrict__ cnt,
+                                                 const int *__restrict__ need, int max_pc, int nbp,
+                                                 long long *__restrict__ pl, long long *__restrict__ pg,
+                                                 long long *__restrict__ cl, long long *__restrict__ cg) {
+    const bool parts = (int)blockIdx.x < nbp;
+    const long long b = parts ? blockIdx.x : blockIdx.x - nbp;
+    const long long first = b * RS_CHUNK + (threadIdx.x >> 5) * RS_WARP_ITEMS + (threadIdx.x & 31);
+    const long long nc = (long long)g.nx * g.ny;
+    long long ml = 0, mg = 0;
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        const long long x = first + 32 * r;
+        if (parts) {
+            if (x < n && tp_over(g, pos, x, cnt, max_pc)) {
+                if (phase[x] > 0.5f) ++ml;
+                else ++mg;
+            }
+        } else if (x < nc) {
+            const int q = need[x];
+            ml += q > 0 ? q : 0;
+            mg += q < 0 ? -q : 0;
+        }
+    }
+    long long oa, ob, ta, tb;
+    rs_warp_offset2(rs_warp_sum(ml), rs_warp_sum(mg), oa, ob, ta, tb);
+    if (threadIdx.x == 0) {
+        (parts ? pl : cl)[b] = ta;
+        (parts ? pg : cg)[b] = tb;
+    }
+}
+
+// scatterDonorsKernel (:1331-1355): liquid rank r -> pool[r], gas rank r ->
+// pool[top - r], ranks at or past pool_half dropped
+__global__ void __launch_bounds__(256) k_tp_scatter(G3 g, long long n, const float *__restrict__ pos,
+                                                    const float *__restrict__ phase, const int *__restrict__ cnt,
+                                                    int max_pc, const long long *__restrict__ pl,
+                                                    const long long *__restrict__ pg, long long pool_half,
+                                                    long long top, int *__restrict__ pool) {
+    const int lane = threadIdx.x & 31;
+    const long long first = blockIdx.x * (long long)RS_CHUNK + (threadIdx.x >> 5) * RS_WARP_ITEMS;
+    unsigned bl[RS_ROUNDS], bg[RS_ROUNDS];
+    long long ml = 0, mg = 0;
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        const long long x = first + 32 * r + lane;
+        const bool over = x < n && tp_over(g, pos, x, cnt, max_pc);
+        const bool liq = over && phase[x] > 0.5f;
+        bl[r] = __ballot_sync(0xffffffffu, liq);
+        bg[r] = __ballot_sync(0xffffffffu, over && !liq);
+        ml += __popc(bl[r]);
+        mg += __popc(bg[r]);
+    }
+    long long oa, ob, ta, tb;
+    rs_warp_offset2(ml, mg, oa, ob, ta, tb);
+    long long rl = pl[blockIdx.x] + oa, rg = pg[blockIdx.x] + ob;
+    const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        const int p = (int)(first + 32 * r + lane);
+        if ((bl[r] >> lane) & 1u) {
+            const long long k = rl + __popc(bl[r] & below);
+            if (k < pool_half) pool[k] = p;
+        }
+        if ((bg[r] >> lane) & 1u) {
+            const long long k = rg + __popc(bg[r] & below);
+            if (k < pool_half) pool[top - k] = p;
+        }
+        rl += __popc(bl[r]);
+        rg += __popc(bg[r]);
+    }
+}
+
+__device__ __forceinline__ long long warp_excl_scan(long long v, long long &total) {
+    const int lane = threadIdx.x & 31;
+    long long s = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long t = __shfl_up_sync(0xffffffffu, s, o);
+        if (lane >= o) s += t;
+    }
+    total = __shfl_sync(0xffffffffu, s, 31);
+    return s - v;
+}
+
+// claimDonorsKernel (:1453-1478) with buildClaimLoop (:1403-1451): a cell's
+// slots in its phase's pool start at that phase's need before it; slots
+// below min(donors, pool_half) move the donor to the cell centre with the
+// face-centred velocity there
+__global__ void __launch_bounds__(256) k_tp_claim(G3 g, const int *__restrict__ need,
+                                                  const long long *__restrict__ cl, const long long *__restrict__ cg,
+                                                  const long long *__restrict__ tot, long long pool_half, long long top,
+                                                  const int *__restrict__ pool, const float *__restrict__ u,
+                                                  const float *__restrict__ v, const float *__restrict__ w,
+                                                  float *__restrict__ pos, float *__restrict__ vel) {
+    const int lane = threadIdx.x & 31;
+    const long long nc = (long long)g.nx * g.ny;
+    const long long first = blockIdx.x * (long long)RS_CHUNK + (threadIdx.x >> 5) * RS_WARP_ITEMS + lane;
+    int q[RS_ROUNDS];
+    long long ml = 0, mg = 0;
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        const long long x = first + 32 * r;
+        q[r] = x < nc ? need[x] : 0;
+        ml += q[r] > 0 ? q[r] : 0;
+        mg += q[r] < 0 ? -q[r] : 0;
+    }
+    long long oa, ob, ta, tb;
+    rs_warp_offset2(rs_warp_sum(ml), rs_warp_sum(mg), oa, ob, ta, tb);
+    if (ta == 0 && tb == 0) return;
+    long long rl = cl[blockIdx.x] + oa, rg = cg[blockIdx.x] + ob;
+    const long long avail_l = tot[0] < pool_half ? tot[0] : pool_half;
+    const long long avail_g = tot[2] < pool_half ? tot[2] : pool_half;
+    const float *comp[3] = {u, v, w};
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        const long long nl = q[r] > 0 ? q[r] : 0, ng = q[r] < 0 ? -q[r] : 0;
+        long long tl, tg;
+        const long long sl = rl + warp_excl_scan(nl, tl), sg = rg + warp_excl_scan(ng, tg);
+        rl += tl;
+        rg += tg;
+        if (q[r] == 0) continue;
+        const bool liquid = q[r] > 0;
+        const long long needed = liquid ? nl : ng, slot0 = liquid ? sl : sg, avail = liquid ? avail_l : avail_g;
+        if (slot0 >= avail) continue;
+        const long long c = first + 32 * r;
+        const int j = (int)(c / g.nx), i = (int)(c - (long long)j * g.nx);
+        F3 qp = index_pos(g, comp_origin(g, 3), i, j, 0);
+        float vq[3];
+        for (int a = 0; a < 3; ++a) {
+            int sx, sy, sz;
+            comp_shape(g, a, sx, sy, sz);
+            vq[a] = trilinear(comp[a], sx, sy, sz, g, comp_origin(g, a), qp);
+        }
+        for (long long m = 0; m < needed && slot0 + m < avail; ++m) {
+            const long long d = pool[liquid ? slot0 + m : top - (slot0 + m)];
+            pos[3 * d] = qp.x;
+            pos[3 * d + 1] = qp.y;
+            pos[3 * d + 2] = qp.z;
+            vel[3 * d] = vq[0];
+            vel[3 * d + 1] = vq[1];
+            vel[3 * d + 2] = vq[2];
         }
     }
 }
@@ -819,7 +1033,7 @@ extern "C" int ff_flip3_stage(ff_flip f, int stage) {
         const F3 mn{g.ox + 1e-4f, g.oy + 1e-4f, g.oz + 1e-4f};
         const F3 mx{(g.ox + ext.x) - 1e-4f, (g.oy + ext.y) - 1e-4f, (g.oz + ext.z) - 1e-4f};
         k_flip_advect<<<blocks_for(n), 256, 0, s>>>(F, n, pos, (float)d.dt, d.max_substeps, mn, mx,
-                                                    (float)d.collider_push_thresh, (float)d.collider_push_shift);
+                                                    (float)d.collider_push_thresh, (float)d.collider_push_shift, 0);
         return post("advectParticles");
     }
     case FF_FLIP_P2G: {
@@ -829,7 +1043,7 @@ extern "C" int ff_flip3_stage(ff_flip f, int stage) {
         }
         const float S = (float)d.p2g_atomic_scale;
         if (n) k_flip_scatter<<<blocks_for(n), 256, 0, s>>>(g, n, pos, vel, S, f->num[0], f->den[0], f->num[1],
-                                                            f->den[1], f->num[2], f->den[2]);
+                                                            f->den[1], f->num[2], f->den[2], 3);
         for (int a = 0; a < 3; ++a)
             k_flip_finalize<<<blocks_for(comp_n(g, a)), 256, 0, s>>>(comp_n(g, a), f->num[a], f->den[a], S,
                                                                      (float)d.weight_epsilon, uvw[a], f->valid[a]);
@@ -890,7 +1104,8 @@ extern "C" int ff_flip3_stage(ff_flip f, int stage) {
     case FF_FLIP_G2P:
         if (n) k_flip_g2p<<<blocks_for(n), 256, 0, s>>>(g, n, pos, vel, uvw[0], uvw[1], uvw[2], f->old[0], f->old[1],
                                                         f->old[2], (float)d.flip_ratio,
-                                                        std::min(std::max((float)d.velocity_damping, 0.0f), 1.0f));
+                                                        std::min(std::max((float)d.velocity_damping, 0.0f), 1.0f),
+                                                        nullptr, 0.0f);
         return post("G2P");
     case FF_FLIP_CONCENTRATION_PARTICLE:
         if (!d.carry_concentration || !n) return FF_OK;
@@ -949,5 +1164,435 @@ extern "C" int ff_flip3_resample_stats(ff_flip f, int64_t *donors, int64_t *requ
     }
     if (donors) *donors = t[0];
     if (requested) *requested = t[1];
+    return FF_OK;
+}
+
+// ----------------------------------------------------------- two-phase 2D --
+// createGridTwoPhaseFlipSolver2 (src/grid/grid_two_phase_flip_solver2.js:
+// 479-1622) on a one-cell-thick 3D grid: the 2D u and v arrays are the
+// k = 0 planes of (nx+1, ny, 1) and (nx, ny+1, 1) face arrays, particles
+// sit on the plane z = hz/2 through the cell centres, and the z velocity is
+// an internal zero field.  With those, every z term of the 3D kernels is an
+// exact +0 or x1 and they compute the 2D expressions operation for
+// operation (bilinear = trilinear at fz = 0; hz = max(hx, hy) keeps the
+// trace's min spacing).  Every cell is fluid; the pressure is pinned to 0
+// at one cell (pressurePin, :767-797); beta = rho_max / face density
+// (:750-762); gravity is uniform (:932-944); the FLIP/PIC blend follows the
+// particle's concentration (:966-992); resampling keeps two pools by phase.
+extern "C" void ff_twophase_desc_default(ff_twophase_desc *d, const int *res, const double *h, int max_particles,
+                                         double dt) {
+    std::memset(d, 0, sizeof *d);
+    for (int a = 0; a < 2; ++a) {
+        d->resolution[a] = res ? res[a] : 1;
+        d->grid_spacing[a] = h ? h[a] : 1.0;
+    }
+    d->max_particles = max_particles;
+    d->dt = dt;
+    d->gravity[1] = -9.81;
+    d->ambient_density = 0.01;   // gasDensity (:496)
+    d->component_density = 1.0;  // liquidDensity (:495)
+    d->concentration_atomic_scale = 4096.0;
+    d->flip_ratio = 0.97;
+    d->gas_flip_ratio = 0.90;
+    d->velocity_damping = 0.02;
+    d->p2g_atomic_scale = 65536.0;
+    d->weight_epsilon = 1e-4;
+    d->closed_flags = 15;   // DIRECTION_ALL in 2D
+    d->max_substeps = 32;
+    d->pin_cell[0] = d->resolution[0] / 2;   // 'topCenter' (:770-772)
+    d->pin_cell[1] = d->resolution[1] - 1;
+    d->resample_enabled = 1;   // resample defaults (:535-539)
+    d->min_particles_per_cell = 3;
+    d->max_particles_per_cell = 8;
+    d->extrapolation_depth = 5;
+    const int r3[3] = {d->resolution[0], d->resolution[1], 1};
+    const double h3[3] = {d->grid_spacing[0], d->grid_spacing[1], std::max(d->grid_spacing[0], d->grid_spacing[1])};
+    ff_pressure_desc_default(&d->pressure, r3, h3);
+    // defaultMultigridLevels (:372-384): deepest of up to 4 levels that
+    // every axis divides into
+    int levels = 1;
+    while (levels < 4 && d->resolution[0] % (1 << levels) == 0 && d->resolution[1] % (1 << levels) == 0) ++levels;
+    d->pressure.mg_levels = levels;
+}
+
+struct ff_twophase_s {
+    ff_ctx ctx = nullptr;
+    ff_twophase_desc desc{};
+    G3 g{};
+    int count = 0;
+    ff_field u = nullptr, v = nullptr, phi = nullptr;   // borrowed
+    ff_field w = nullptr;                               // internal zero z velocity
+    ff_field pos = nullptr, vel = nullptr, phase = nullptr, frac = nullptr, rho = nullptr, beta[3] = {};
+    ff_field active = nullptr, target = nullptr;
+    float *old[2] = {};
+    int *num[2] = {}, *den[2] = {}, *valid[2] = {}, *vtmp[2][2] = {};
+    float *scratch[2] = {};
+    int *ccnt = nullptr, *cacc = nullptr;
+    int *rs_need = nullptr, *rs_pool = nullptr;
+    long long *rs_bsum = nullptr, *rs_tot = nullptr;
+    int rs_nbp = 0, rs_nbc = 0;
+    ff_bc bc = nullptr;
+    ff_pressure ps = nullptr;
+    float r0 = 0, r1 = 0, rref = 1;
+    ff_diag last{};
+};
+
+extern "C" int ff_twophase2_destroy(ff_twophase t) {
+    if (!t) return FF_OK;
+    cudaStreamSynchronize(t->ctx->stream);
+    ff_pressure3_destroy(t->ps);
+    ff_bc3_destroy(t->bc);
+    ff_field fs[] = {t->w, t->pos, t->vel, t->phase, t->frac, t->rho, t->beta[0], t->beta[1], t->beta[2],
+                     t->active, t->target};
+    for (ff_field x : fs) ff_field_destroy(x);
+    for (int a = 0; a < 2; ++a) {
+        ff_dev_free(t->old[a]);
+        ff_dev_free(t->num[a]);
+        ff_dev_free(t->den[a]);
+        ff_dev_free(t->valid[a]);
+        ff_dev_free(t->vtmp[0][a]);
+        ff_dev_free(t->vtmp[1][a]);
+        ff_dev_free(t->scratch[a]);
+    }
+    void *ps[] = {t->ccnt, t->cacc, t->rs_need, t->rs_pool, t->rs_bsum, t->rs_tot};
+    for (void *p : ps) ff_dev_free(p);
+    delete t;
+    return FF_OK;
+}
+
+extern "C" int ff_twophase2_create(ff_ctx ctx, const ff_twophase_desc *d, ff_field u, ff_field v, ff_twophase *out) {
+    FF_CHECK(ctx && d && out, FF_E_ARG, "ff_twophase2_create: NULL argument");
+    FF_CHECK(d->max_particles > 0, FF_E_ARG, "createGridTwoPhaseFlipSolver2: options.maxParticles is required.");
+    FF_CHECK(d->resolution[0] > 0 && d->resolution[1] > 0, FF_E_ARG, "createGridTwoPhaseFlipSolver2: bad resolution");
+    FF_CHECK(d->component_density > 0, FF_E_ARG,
+             "createGridTwoPhaseFlipSolver2: the concentration-1 density (liquidDensity / componentDensity) must be "
+             "> 0, got %g.", d->component_density);
+    FF_CHECK(d->ambient_density > 0, FF_E_ARG,
+             "createGridTwoPhaseFlipSolver2: the concentration-0 density (gasDensity / ambientDensity) must be > 0, "
+             "got %g.", d->ambient_density);
+    FF_CHECK(d->pin_cell[0] < 0 || (d->pin_cell[0] < d->resolution[0] && d->pin_cell[1] >= 0 &&
+                                    d->pin_cell[1] < d->resolution[1]),
+             FF_E_ARG, "createGridTwoPhaseFlipSolver2: pressurePin cell outside the grid");
+    FF_CHECK(d->max_substeps > 0, FF_E_ARG, "createGridTwoPhaseFlipSolver2: maxSubsteps must be positive");
+    *out = nullptr;
+    cudaSetDevice(ctx->device);
+    ff_twophase t = new ff_twophase_s();
+    t->ctx = ctx;
+    t->desc = *d;
+    const int nx = d->resolution[0], ny = d->resolution[1];
+    t->g.nx = nx;
+    t->g.ny = ny;
+    t->g.nz = 1;
+    t->g.hx = (float)d->grid_spacing[0];
+    t->g.hy = (float)d->grid_spacing[1];
+    t->g.hz = (float)std::max(d->grid_spacing[0], d->grid_spacing[1]);
+    t->g.ox = (float)d->origin[0];
+    t->g.oy = (float)d->origin[1];
+    t->g.oz = 0.0f;
+    if (!u || !v || u->dtype != FF_FLOAT || v->dtype != FF_FLOAT || u->count != (long long)(nx + 1) * ny ||
+        v->count != (long long)nx * (ny + 1)) {
+        delete t;
+        return ff_set_error(FF_E_ARG, "createGridTwoPhaseFlipSolver2: velocity grid has the wrong shape");
+    }
+    t->u = u;
+    t->v = v;
+    t->count = d->max_particles;
+    t->r0 = std::max((float)d->ambient_density, MIN_DENSITY);
+    t->r1 = std::max((float)d->component_density, MIN_DENSITY);
+    t->rref = std::max(t->r0, t->r1);
+    cudaStream_t s = ctx->stream;
+    int st = FF_OK;
+    auto bail = [&](int code) { ff_twophase2_destroy(t); return code; };
+    const int np[1] = {d->max_particles};
+    const int cs[3] = {nx, ny, 1}, ws[3] = {nx, ny, 2};
+    const long long nc = (long long)nx * ny;
+    if ((st = ff_field_create(ctx, FF_FLOAT, 3, ws, &t->w))) return bail(st);
+    if ((st = ff_field_create(ctx, FF_VEC3, 1, np, &t->pos))) return bail(st);
+    if ((st = ff_field_create(ctx, FF_VEC3, 1, np, &t->vel))) return bail(st);
+    if ((st = ff_field_create(ctx, FF_FLOAT, 1, np, &t->phase))) return bail(st);
+    if ((st = ff_field_create(ctx, FF_FLOAT, 3, cs, &t->frac))) return bail(st);
+    if ((st = ff_field_create(ctx, FF_FLOAT, 3, cs, &t->rho))) return bail(st);
+    if ((st = ff_field_create(ctx, FF_UINT8, 3, cs, &t->active))) return bail(st);
+    if ((st = ff_field_create(ctx, FF_FLOAT, 3, cs, &t->target))) return bail(st);
+    if ((st = ff_field_fill(t->rho, (float)d->component_density))) return bail(st);
+    // particles start at rest at (0, 0) on the centre plane, all gas until
+    // seeded (:599-606)
+    {
+        std::vector<float> p3((size_t)3 * d->max_particles, 0.0f);
+        for (size_t p = 0; p < (size_t)d->max_particles; ++p) p3[3 * p + 2] = t->g.oz + t->g.hz * 0.5f;
+        if ((st = ff_field_upload(t->pos, p3.data(), p3.size() * 4))) return bail(st);
+        if (cudaMemsetAsync(t->vel->d, 0, t->vel->bytes, s) != cudaSuccess ||
+            cudaMemsetAsync(t->phase->d, 0, t->phase->bytes, s) != cudaSuccess)
+            return bail(ff_set_error(FF_E_CUDA, "twophase"));
+    }
+    for (int a = 0; a < 3; ++a) {
+        const int fs3[3] = {nx + (a == 0), ny + (a == 1), 1 + (a == 2)};
+        if ((st = ff_field_create(ctx, FF_FLOAT, 3, fs3, &t->beta[a]))) return bail(st);
+        if ((st = ff_field_fill(t->beta[a], 1.0f))) return bail(st);
+    }
+    for (int a = 0; a < 2; ++a) {
+        const size_t b = (size_t)comp_n(t->g, a) * 4;
+        if ((st = ff_dev_alloc((void **)&t->old[a], b, s))) return bail(st);
+        if ((st = ff_dev_alloc((void **)&t->num[a], b, s))) return bail(st);
+        if ((st = ff_dev_alloc((void **)&t->den[a], b, s))) return bail(st);
+        if ((st = ff_dev_alloc((void **)&t->valid[a], b, s))) return bail(st);
+        if ((st = ff_dev_alloc((void **)&t->vtmp[0][a], b, s))) return bail(st);
+        if ((st = ff_dev_alloc((void **)&t->vtmp[1][a], b, s))) return bail(st);
+        if ((st = ff_dev_alloc((void **)&t->scratch[a], b, s))) return bail(st);
+    }
+    if ((st = ff_dev_alloc((void **)&t->ccnt, (size_t)nc * 4, s))) return bail(st);
+    if ((st = ff_dev_alloc((void **)&t->cacc, (size_t)nc * 4, s))) return bail(st);
+    if (d->resample_enabled) {
+        t->rs_nbp = (int)(((long long)d->max_particles + RS_CHUNK - 1) / RS_CHUNK);
+        t->rs_nbc = (int)((nc + RS_CHUNK - 1) / RS_CHUNK);
+        if ((st = ff_dev_alloc((void **)&t->rs_need, (size_t)nc * 4, s))) return bail(st);
+        if ((st = ff_dev_alloc((void **)&t->rs_pool, (size_t)d->max_particles * 4, s))) return bail(st);
+        if ((st = ff_dev_alloc((void **)&t->rs_bsum, (size_t)2 * (t->rs_nbp + t->rs_nbc) * 8, s))) return bail(st);
+        if ((st = ff_dev_alloc((void **)&t->rs_tot, 32, s))) return bail(st);
+        if (cudaMemsetAsync(t->rs_tot, 0, 32, s) != cudaSuccess) return bail(ff_set_error(FF_E_CUDA, "twophase"));
+    }
+    // the pressure pin as a Dirichlet cell at 0 (dirichletAt, :786-795)
+    {
+        std::vector<uint8_t> act((size_t)nc, 0);
+        if (d->pin_cell[0] >= 0) act[(size_t)d->pin_cell[0] + (size_t)nx * d->pin_cell[1]] = 1;
+        if ((st = ff_field_upload(t->active, act.data(), act.size()))) return bail(st);
+        if (cudaMemsetAsync(t->target->d, 0, (size_t)nc * 4, s) != cudaSuccess)
+            return bail(ff_set_error(FF_E_CUDA, "twophase"));
+    }
+    const int r3[3] = {nx, ny, 1};
+    const double h3[3] = {d->grid_spacing[0], d->grid_spacing[1], (double)t->g.hz};
+    const double o3[3] = {d->origin[0], d->origin[1], 0.0};
+    if ((st = ff_bc3_create(ctx, r3, h3, o3, &t->bc))) return bail(st);
+    if ((st = ff_bc3_set_closed(t->bc, (d->closed_flags & 15) | 48))) return bail(st);
+    ff_pressure_desc pd = d->pressure;
+    for (int a = 0; a < 3; ++a) {
+        pd.resolution[a] = r3[a];
+        pd.grid_spacing[a] = h3[a];
+        pd.origin[a] = o3[a];
+    }
+    if ((st = ff_pressure3_create(ctx, &pd, &t->ps))) return bail(st);
+    if ((st = ff_pressure3_set_dirichlet(t->ps, t->active, t->target))) return bail(st);
+    if ((st = ff_pressure3_set_face_weights(t->ps, t->beta[0], t->beta[1], t->beta[2]))) return bail(st);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return bail(ff_set_error(FF_E_CUDA, "two-phase create sync"));
+    *out = t;
+    return FF_OK;
+}
+
+extern "C" int ff_twophase2_set_collider(ff_twophase t, ff_field phi) {
+    FF_CHECK(t, FF_E_ARG, "NULL two-phase solver");
+    FF_CHECK(!phi || (phi->dtype == FF_FLOAT && phi->count == (long long)t->g.nx * t->g.ny), FF_E_ARG,
+             "two-phase collider must be a float cell SDF");
+    t->phi = phi;
+    return ff_bc3_set_collider(t->bc, phi, nullptr, nullptr, nullptr);
+}
+
+extern "C" int ff_twophase2_set_count(ff_twophase t, int n) {
+    FF_CHECK(t && n >= 0 && n <= t->desc.max_particles, FF_E_ARG, "two-phase particle count out of range");
+    t->count = n;
+    return FF_OK;
+}
+
+extern "C" int ff_twophase2_set_particles(ff_twophase t, int n, const float *xy, const float *vxy,
+                                          const float *phase) {
+    FF_CHECK(t && n >= 0 && n <= t->desc.max_particles, FF_E_ARG, "two-phase particle upload: bad count");
+    cudaSetDevice(t->ctx->device);
+    const float zc = t->g.oz + t->g.hz * 0.5f;
+    std::vector<float> p3((size_t)3 * n), v3((size_t)3 * n);
+    for (size_t p = 0; p < (size_t)n; ++p) {
+        if (xy) {
+            p3[3 * p] = xy[2 * p];
+            p3[3 * p + 1] = xy[2 * p + 1];
+            p3[3 * p + 2] = zc;
+        }
+        if (vxy) {
+            v3[3 * p] = vxy[2 * p];
+            v3[3 * p + 1] = vxy[2 * p + 1];
+            v3[3 * p + 2] = 0.0f;
+        }
+    }
+    cudaStream_t s = t->ctx->stream;
+    if (n && xy) FF_CUDA(cudaMemcpyAsync(t->pos->d, p3.data(), p3.size() * 4, cudaMemcpyHostToDevice, s));
+    if (n && vxy) FF_CUDA(cudaMemcpyAsync(t->vel->d, v3.data(), v3.size() * 4, cudaMemcpyHostToDevice, s));
+    if (n && phase) FF_CUDA(cudaMemcpyAsync(t->phase->d, phase, (size_t)n * 4, cudaMemcpyHostToDevice, s));
+    FF_CUDA(cudaStreamSynchronize(s));
+    return FF_OK;
+}
+
+extern "C" int ff_twophase2_get_particles(ff_twophase t, int n, float *xy, float *vxy, float *phase) {
+    FF_CHECK(t && n >= 0 && n <= t->desc.max_particles, FF_E_ARG, "two-phase particle download: bad count");
+    cudaSetDevice(t->ctx->device);
+    cudaStream_t s = t->ctx->stream;
+    std::vector<float> p3((size_t)3 * n), v3((size_t)3 * n);
+    if (n && xy) FF_CUDA(cudaMemcpyAsync(p3.data(), t->pos->d, p3.size() * 4, cudaMemcpyDeviceToHost, s));
+    if (n && vxy) FF_CUDA(cudaMemcpyAsync(v3.data(), t->vel->d, v3.size() * 4, cudaMemcpyDeviceToHost, s));
+    if (n && phase) FF_CUDA(cudaMemcpyAsync(phase, t->phase->d, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+    FF_CUDA(cudaStreamSynchronize(s));
+    for (int p = 0; p < n; ++p)
+        for (int a = 0; a < 2; ++a) {
+            if (xy) xy[2 * (size_t)p + a] = p3[3 * (size_t)p + a];
+            if (vxy) vxy[2 * (size_t)p + a] = v3[3 * (size_t)p + a];
+        }
+    return FF_OK;
+}
+
+extern "C" int ff_twophase2_fields(ff_twophase t, ff_field *phase, ff_field *liquid_fraction, ff_field *density,
+                                   ff_field *beta_u, ff_field *beta_v, ff_pressure *pressure) {
+    FF_CHECK(t, FF_E_ARG, "NULL two-phase solver");
+    if (phase) *phase = t->phase;
+    if (liquid_fraction) *liquid_fraction = t->frac;
+    if (density) *density = t->rho;
+    if (beta_u) *beta_u = t->beta[0];
+    if (beta_v) *beta_v = t->beta[1];
+    if (pressure) *pressure = t->ps;
+    return FF_OK;
+}
+
+static int tp_extrapolate(ff_twophase t, float *data, const int *marker, int a) {
+    cudaStream_t s = t->ctx->stream;
+    int sx, sy, sz;
+    comp_shape(t->g, a, sx, sy, sz);
+    const long long n = comp_n(t->g, a);
+    FF_CUDA(cudaMemcpyAsync(t->vtmp[0][a], marker, n * 4, cudaMemcpyDeviceToDevice, s));
+    float *src = data, *dst = t->scratch[a];
+    int *vs = t->vtmp[0][a], *vd = t->vtmp[1][a];
+    for (int it = 0; it < t->desc.extrapolation_depth; ++it) {
+        k_extrapolate<<<blocks_for(n), 256, 0, s>>>(sx, sy, sz, src, dst, vs, vd);
+        std::swap(src, dst);
+        std::swap(vs, vd);
+    }
+    if (src != data) FF_CUDA(cudaMemcpyAsync(data, src, n * 4, cudaMemcpyDeviceToDevice, s));
+    return post("extrapolate");
+}
+
+// One stage of onAdvanceTimeStep (:1505-1592).
+extern "C" int ff_twophase2_stage(ff_twophase t, int stage) {
+    FF_CHECK(t, FF_E_ARG, "NULL two-phase solver");
+    cudaSetDevice(t->ctx->device);
+    cudaStream_t s = t->ctx->stream;
+    const ff_twophase_desc &d = t->desc;
+    const G3 &g = t->g;
+    const long long n = t->count, nc = (long long)g.nx * g.ny;
+    float *uv[2] = {(float *)t->u->d, (float *)t->v->d};
+    float *w = (float *)t->w->d;
+    float *pos = (float *)t->pos->d, *vel = (float *)t->vel->d, *ph = (float *)t->phase->d;
+    const float cscale = (float)d.concentration_atomic_scale;
+    switch (stage) {
+    case FF_TP_ADVECT: {
+        // advectParticles + pushOutOfCollider (:1098-1124)
+        FF_CUDA(cudaMemsetAsync(w, 0, comp_n(g, 2) * 4, s));
+        if (n == 0) return FF_OK;
+        VelField F{g, uv[0], uv[1], w, t->phi ? (const float *)t->phi->d : nullptr};
+        const F3 mn{g.ox + 1e-4f, g.oy + 1e-4f, g.oz + 1e-4f};
+        const F3 mx{(g.ox + (float)(d.resolution[0] * d.grid_spacing[0])) - 1e-4f,
+                    (g.oy + (float)(d.resolution[1] * d.grid_spacing[1])) - 1e-4f, (g.oz + g.hz) - 1e-4f};
+        k_flip_advect<<<blocks_for(n), 256, 0, s>>>(F, n, pos, (float)d.dt, d.max_substeps, mn, mx,
+                                                    (float)d.collider_push_thresh, (float)d.collider_push_shift, 1);
+        return post("advectParticles");
+    }
+    case FF_TP_DENSITY:
+        // countPhasesKernel, computeDensityKernel, computeBetaU/V (:646-762)
+        FF_CUDA(cudaMemsetAsync(t->ccnt, 0, nc * 4, s));
+        FF_CUDA(cudaMemsetAsync(t->cacc, 0, nc * 4, s));
+        if (n) k_flip_conc_accum<<<blocks_for(n), 256, 0, s>>>(g, n, pos, ph, cscale, t->ccnt, t->cacc);
+        k_flip_conc_resolve<<<blocks_for(nc), 256, 0, s>>>(nc, t->ccnt, t->cacc, cscale, 1, t->r0, t->r1,
+                                                           (float *)t->frac->d, (float *)t->rho->d);
+        for (int a = 0; a < 2; ++a)
+            k_flip_beta<<<blocks_for(comp_n(g, a)), 256, 0, s>>>(g, a, (const float *)t->rho->d, nullptr, t->rref,
+                                                                 (float *)t->beta[a]->d);
+        return post("density");
+    case FF_TP_P2G: {
+        // scatterU/V, finalizeU/V (:850-930)
+        const float S = (float)d.p2g_atomic_scale;
+        for (int a = 0; a < 2; ++a) {
+            FF_CUDA(cudaMemsetAsync(t->num[a], 0, comp_n(g, a) * 4, s));
+            FF_CUDA(cudaMemsetAsync(t->den[a], 0, comp_n(g, a) * 4, s));
+        }
+        if (n) k_flip_scatter<<<blocks_for(n), 256, 0, s>>>(g, n, pos, vel, S, t->num[0], t->den[0], t->num[1],
+                                                            t->den[1], nullptr, nullptr, 2);
+        for (int a = 0; a < 2; ++a)
+            k_flip_finalize<<<blocks_for(comp_n(g, a)), 256, 0, s>>>(comp_n(g, a), t->num[a], t->den[a], S,
+                                                                     (float)d.weight_epsilon, uv[a], t->valid[a]);
+        return post("P2G");
+    }
+    case FF_TP_SNAPSHOT:
+        for (int a = 0; a < 2; ++a)
+            FF_CUDA(cudaMemcpyAsync(t->old[a], uv[a], comp_n(g, a) * 4, cudaMemcpyDeviceToDevice, s));
+        return FF_OK;
+    case FF_TP_EXTRAPOLATE_WEIGHT:
+        for (int a = 0; a < 2; ++a) FF_TRY(tp_extrapolate(t, uv[a], t->valid[a], a));
+        return FF_OK;
+    case FF_TP_CONSTRAIN:
+        // the 2D grid's u and v are the 3D arrays' k = 0 planes
+        return ff_bc3_constrain(t->bc, t->u, t->v, t->w, d.extrapolation_depth);
+    case FF_TP_GRAVITY: {
+        const F3 grav{(float)d.gravity[0], (float)d.gravity[1], 0.0f};
+        for (int a = 0; a < 2; ++a)
+            k_flip_gravity<<<blocks_for(comp_n(g, a)), 256, 0, s>>>(g, a, nullptr, nullptr, grav, (float)d.dt, 1.0f,
+                                                                    uv[a]);
+        return post("gravity");
+    }
+    case FF_TP_PROJECT:
+        return ff_pressure3_project(t->ps, t->u, t->v, t->w, t->u, t->v, t->w, &t->last);
+    case FF_TP_G2P: {
+        FF_CUDA(cudaMemsetAsync(w, 0, comp_n(g, 2) * 4, s));
+        if (!n) return FF_OK;
+        const float clamp01[3] = {std::min(std::max((float)d.flip_ratio, 0.0f), 1.0f),
+                                  std::min(std::max((float)d.gas_flip_ratio, 0.0f), 1.0f),
+                                  std::min(std::max((float)d.velocity_damping, 0.0f), 1.0f)};
+        k_flip_g2p<<<blocks_for(n), 256, 0, s>>>(g, n, pos, vel, uv[0], uv[1], w, t->old[0], t->old[1], w, clamp01[0],
+                                                 clamp01[2], ph, clamp01[1]);
+        return post("G2P");
+    }
+    case FF_TP_MIX:
+        // mixConcentration (:1055-1073), skipped when both controls are 0
+        if (!n || (d.mixing == 0.0 && d.fade == 0.0)) return FF_OK;
+        k_flip_mix_fade<<<blocks_for(n), 256, 0, s>>>(g, n, pos, (const float *)t->frac->d,
+                                                      std::min(std::max((float)d.mixing, 0.0f), 1.0f),
+                                                      std::min(std::max((float)d.fade, 0.0f), 1.0f), ph);
+        return post("mixConcentration");
+    case FF_TP_RESAMPLE: {
+        // resamplePassNow (:1480-1494) on the counts of this frame's DENSITY stage
+        if (!d.resample_enabled) return FF_OK;
+        const int nbp = (int)((n + RS_CHUNK - 1) / RS_CHUNK), nbc = t->rs_nbc;
+        long long *pl = t->rs_bsum, *pg = pl + t->rs_nbp, *cl = pg + t->rs_nbp, *cg = cl + nbc;
+        const long long half = std::max(1, d.max_particles / 2), top = d.max_particles - 1;
+        k_tp_need<<<blocks_for(nc), 256, 0, s>>>(g, t->ccnt, t->cacc, cscale, d.min_particles_per_cell, t->rs_need);
+        k_tp_sums<<<nbp + nbc, 256, 0, s>>>(g, n, pos, ph, t->ccnt, t->rs_need, d.max_particles_per_cell, nbp, pl, pg,
+                                            cl, cg);
+        k_rs_scan<<<1, 1024, 0, s>>>(pl, nbp, cl, nbc, t->rs_tot);
+        k_rs_scan<<<1, 1024, 0, s>>>(pg, nbp, cg, nbc, t->rs_tot + 2);
+        if (nbp)
+            k_tp_scatter<<<nbp, 256, 0, s>>>(g, n, pos, ph, t->ccnt, d.max_particles_per_cell, pl, pg, half, top,
+                                             t->rs_pool);
+        k_tp_claim<<<nbc, 256, 0, s>>>(g, t->rs_need, cl, cg, t->rs_tot, half, top, t->rs_pool, uv[0], uv[1], w, pos,
+                                       vel);
+        return post("resample");
+    }
+    default:
+        return ff_set_error(FF_E_ARG, "ff_twophase2_stage: unknown stage %d", stage);
+    }
+}
+
+// onAdvanceTimeStep (:1505-1592)
+extern "C" int ff_twophase2_step(ff_twophase t, ff_diag *diag) {
+    FF_CHECK(t, FF_E_ARG, "NULL two-phase solver");
+    static const int order[] = {FF_TP_ADVECT,    FF_TP_DENSITY, FF_TP_P2G,       FF_TP_SNAPSHOT,
+                                FF_TP_EXTRAPOLATE_WEIGHT,       FF_TP_CONSTRAIN, FF_TP_GRAVITY,
+                                FF_TP_CONSTRAIN, FF_TP_PROJECT, FF_TP_CONSTRAIN, FF_TP_G2P,
+                                FF_TP_MIX,       FF_TP_RESAMPLE};
+    for (int st : order) FF_TRY(ff_twophase2_stage(t, st));
+    if (diag) *diag = t->last;
+    return FF_OK;
+}
+
+extern "C" int ff_twophase2_resample_stats(ff_twophase t, int64_t *out4) {
+    FF_CHECK(t && out4, FF_E_ARG, "NULL argument");
+    long long v[4] = {0, 0, 0, 0};
+    if (t->rs_tot) {
+        cudaSetDevice(t->ctx->device);
+        FF_CUDA(cudaMemcpyAsync(v, t->rs_tot, sizeof v, cudaMemcpyDeviceToHost, t->ctx->stream));
+        FF_CUDA(cudaStreamSynchronize(t->ctx->stream));
+    }
+    for (int q = 0; q < 4; ++q) out4[q] = v[q];
     return FF_OK;
 }

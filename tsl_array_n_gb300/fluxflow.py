@@ -19,6 +19,7 @@ Names, option names, defaults and error behaviour follow the reference
   create_jitter_random            jitter_random.js:29-46
 """
 import ctypes as C
+import math
 
 import numpy as np
 
@@ -855,6 +856,248 @@ def create_grid_flip_solver3(**options):
 
 
 # ---------------------------------------------------------------- solver --
+class FaceCenteredGrid2:
+    """createFaceCenteredGrid2 (grid_data2.js): u (nx+1, ny), v (nx, ny+1),
+    staggered origins; the same memory as a one-cell-thick 3D grid's u and
+    v."""
+
+    def __init__(self, resolution, grid_spacing=(1.0, 1.0), origin=(0.0, 0.0)):
+        nx, ny = resolution
+        self.resolution = (nx, ny)
+        self.grid_spacing = tuple(float(h) for h in grid_spacing)
+        self.origin = tuple(float(o) for o in origin)
+        self.data_size_u = (nx + 1, ny)
+        self.data_size_v = (nx, ny + 1)
+        self.data_u = Field("float", self.data_size_u)
+        self.data_v = Field("float", self.data_size_v)
+        hx, hy = self.grid_spacing
+        ox, oy = self.origin
+        self.data_origin_u = (ox, oy + 0.5 * hy)
+        self.data_origin_v = (ox + 0.5 * hx, oy)
+
+    def set(self, u, v):
+        self.data_u.from_array(u)
+        self.data_v.from_array(v)
+        return self
+
+    def get(self):
+        return self.data_u.to_array(), self.data_v.to_array()
+
+
+def create_face_centered_grid2(nx, ny, hx=1.0, hy=1.0, ox=0.0, oy=0.0):
+    return FaceCenteredGrid2((nx, ny), (hx, hy), (ox, oy))
+
+
+PHASE_GAS, PHASE_LIQUID = 0, 1
+
+
+def compute_two_phase_box_seed(box_min, box_max, grid_spacing_x, grid_spacing_y, particles_per_cell_axis=2,
+                               jitter=0.2, random_seed=DEFAULT_JITTER_SEED, is_liquid=None, concentration_at=None):
+    """computeTwoPhaseBoxSeed (grid_two_phase_flip_solver2.js:397-477): a
+    jittered box of particles, each tagged with a phase (or a concentration
+    from ``concentration_at``), computed in doubles as JavaScript does."""
+    min_x, min_y = (float(x) for x in box_min)
+    max_x, max_y = (float(x) for x in box_max)
+    jsround = lambda x: math.floor(x + 0.5)
+    cells_x = max(1, jsround((max_x - min_x) / grid_spacing_x))
+    cells_y = max(1, jsround((max_y - min_y) / grid_spacing_y))
+    k = int(particles_per_cell_axis)
+    sub_x, sub_y = grid_spacing_x / k, grid_spacing_y / k
+    rnd = create_jitter_random(random_seed)
+    pos, phases = [], []
+    for cj in range(cells_y):
+        for ci in range(cells_x):
+            for sj in range(k):
+                for si in range(k):
+                    jx = (rnd() * 2 - 1) * jitter * sub_x
+                    jy = (rnd() * 2 - 1) * jitter * sub_y
+                    x = min_x + ci * grid_spacing_x + (si + 0.5) * sub_x + jx
+                    y = min_y + cj * grid_spacing_y + (sj + 0.5) * sub_y + jy
+                    pos += [x, y]
+                    if concentration_at is not None:
+                        phases.append(min(1.0, max(0.0, float(concentration_at([x, y])))))
+                    else:
+                        phases.append(PHASE_LIQUID if (is_liquid is None or is_liquid([x, y])) else PHASE_GAS)
+    ph = np.array(phases, np.float32)
+    n = len(phases)
+    return {"count": n, "positionsArray": np.array(pos, np.float32), "velocitiesArray": np.zeros(2 * n, np.float32),
+            "phasesArray": ph, "liquidCount": int((ph > 0.5).sum()), "gasCount": int(n - (ph > 0.5).sum()),
+            "meanConcentration": float(np.sum(ph.astype(np.float64))) / n if n else 0.0}
+
+
+class _TwoPhaseParticles:
+    """positions / velocities of the two-phase solver as (x, y) pairs."""
+
+    def __init__(self, solver, which):
+        self._s, self._w = solver, which
+
+    def from_array(self, values):
+        a = np.ascontiguousarray(values, np.float32).ravel()
+        n = a.size // 2
+        fp = a.ctypes.data_as(C.POINTER(C.c_float))
+        args = (fp, None, None) if self._w == 0 else (None, fp, None)
+        _lib.check(_lib.load().ff_twophase2_set_particles(self._s.handle, n, *args))
+        return self
+
+    def to_array(self):
+        n = self._s.max_particles
+        out = np.empty(2 * n, np.float32)
+        fp = out.ctypes.data_as(C.POINTER(C.c_float))
+        args = (fp, None, None) if self._w == 0 else (None, fp, None)
+        _lib.check(_lib.load().ff_twophase2_get_particles(self._s.handle, n, *args))
+        return out
+
+
+class GridTwoPhaseFlipSolver2:
+    """createGridTwoPhaseFlipSolver2({velocityGrid, gridSpacing, origin,
+    maxParticles, dt, gravity, liquidDensity, gasDensity, ambientDensity,
+    componentDensity, mixing, fade, concentrationAtomicScale, flipRatio,
+    gasFlipRatio, velocityDamping, p2gAtomicScale, weightEpsilon,
+    closedDomainBoundaryFlag, collider, colliderPushThresh,
+    colliderPushShift, pressurePin, resample, pressure})
+    (grid_two_phase_flip_solver2.js:479-1622)."""
+
+    STAGES = {"advectParticles": 0, "density": 1, "p2g": 2, "snapshotOld": 3, "extrapolateWeight": 4,
+              "constrainVelocity": 5, "gravity": 6, "project": 7, "g2p": 8, "mixConcentration": 9, "resample": 10}
+
+    def __init__(self, velocity_grid=None, grid_spacing=None, origin=None, max_particles=None, dt=None,
+                 gravity=(0.0, -9.81), liquid_density=1.0, gas_density=0.01, ambient_density=None,
+                 component_density=None, mixing=0.0, fade=0.0, concentration_atomic_scale=4096.0, flip_ratio=0.97,
+                 gas_flip_ratio=0.90, velocity_damping=0.02, p2g_atomic_scale=65536.0, weight_epsilon=1e-4,
+                 closed_domain_boundary_flag=None, collider=None, collider_push_thresh=0.0, collider_push_shift=0.0,
+                 pressure_pin="topCenter", resample=None, pressure=None, max_substeps=32):
+        vocabulary = ambient_density is None and component_density is None
+        if ambient_density is not None:
+            gas_density = ambient_density
+        if component_density is not None:
+            liquid_density = component_density
+        if velocity_grid is None:
+            raise ValueError("createGridTwoPhaseFlipSolver2: options.velocityGrid is required.")
+        if not max_particles:
+            raise ValueError("createGridTwoPhaseFlipSolver2: options.maxParticles is required.")
+        if not liquid_density > 0:
+            raise ValueError("createGridTwoPhaseFlipSolver2: the concentration-1 density (liquidDensity / "
+                             f"componentDensity) must be > 0, got {liquid_density}.")
+        if not gas_density > 0:
+            raise ValueError("createGridTwoPhaseFlipSolver2: the concentration-0 density (gasDensity / "
+                             f"ambientDensity) must be > 0, got {gas_density}.")
+        if vocabulary and gas_density > liquid_density:
+            raise ValueError(f"createGridTwoPhaseFlipSolver2: gasDensity ({gas_density}) must not exceed "
+                             f"liquidDensity ({liquid_density}) -- the two phase tags would then be named "
+                             "backwards. Use ambientDensity/componentDensity for a lighter concentration-1 "
+                             "component.")
+        g = velocity_grid
+        res = tuple(g.resolution)[:2]
+        spacing = tuple(grid_spacing or g.grid_spacing)[:2]
+        org = tuple(origin or g.origin)[:2]
+        if pressure_pin == "topCenter":
+            pin = (res[0] // 2, res[1] - 1)
+        elif pressure_pin is None:
+            pin = (-1, -1)
+        elif isinstance(pressure_pin, (list, tuple)) and len(pressure_pin) == 2:
+            pin = (int(pressure_pin[0]), int(pressure_pin[1]))
+        else:
+            raise ValueError("createGridTwoPhaseFlipSolver2: pressurePin must be 'topCenter', null, or an [i, j] "
+                             f"cell index, got {pressure_pin!r}.")
+        self.pin_cell = None if pin[0] < 0 else list(pin)
+        lib = _lib.load()
+        d = _lib.TwoPhaseDesc()
+        lib.ff_twophase_desc_default(C.byref(d), (C.c_int * 2)(*res), (C.c_double * 2)(*spacing),
+                                     int(max_particles), float(dt))
+        d.origin[:] = [float(x) for x in org]
+        d.gravity[:] = [float(x) for x in gravity]
+        d.ambient_density, d.component_density = float(gas_density), float(liquid_density)
+        d.mixing, d.fade = float(mixing), float(fade)
+        d.concentration_atomic_scale = float(concentration_atomic_scale)
+        d.flip_ratio, d.gas_flip_ratio = float(flip_ratio), float(gas_flip_ratio)
+        d.velocity_damping = float(velocity_damping)
+        d.p2g_atomic_scale, d.weight_epsilon = float(p2g_atomic_scale), float(weight_epsilon)
+        if closed_domain_boundary_flag is not None:
+            d.closed_flags = int(closed_domain_boundary_flag)
+        d.collider_push_thresh, d.collider_push_shift = float(collider_push_thresh), float(collider_push_shift)
+        d.pin_cell[:] = list(pin)
+        d.max_substeps = int(max_substeps)
+        rs = resample or {}
+        d.resample_enabled = int(bool(rs.get("enabled", True)))
+        d.min_particles_per_cell = int(rs.get("minParticlesPerCell", 3))
+        d.max_particles_per_cell = int(rs.get("maxParticlesPerCell", 8))
+        p = pressure or {}
+        mg = p.get("multigrid", {})
+        pd = d.pressure
+        pd.preconditioner = PRECONDITIONERS[p.get("preconditioner", "multigrid")]
+        pd.tolerance = float(p.get("tolerance", pd.tolerance))
+        pd.mg_levels = int(mg.get("numberOfLevels", pd.mg_levels))
+        pd.mg_down = int(mg.get("numberOfSmoothingIterationsDown", pd.mg_down))
+        pd.mg_up = int(mg.get("numberOfSmoothingIterationsUp", pd.mg_up))
+        pd.mg_coarsest = int(mg.get("numberOfCoarsestIterations", pd.mg_coarsest))
+        pd.mg_coarse_mode = 1 if mg.get("coarseSolve", "sweeps") == "direct" else 0
+        if "maxIterations" in p:
+            pd.max_iterations = int(p["maxIterations"])
+        if "maxPlausiblePressure" in p:
+            pd.max_plausible_pressure = float(p["maxPlausiblePressure"])
+        if p.get("precision", "fp32") != "fp32":
+            pd.iterate = 1
+        self.desc = d
+        self.max_particles = int(max_particles)
+        self.velocity_grid = g
+        self.handle = C.c_void_p()
+        _lib.check(lib.ff_twophase2_create(context().handle, C.byref(d), g.data_u.handle, g.data_v.handle,
+                                           C.byref(self.handle)))
+        self.collider = collider
+        if collider is not None:
+            _lib.check(lib.ff_twophase2_set_collider(self.handle, collider.phi.handle))
+        hs = [C.c_void_p() for _ in range(6)]
+        _lib.check(lib.ff_twophase2_fields(self.handle, *[C.byref(x) for x in hs]))
+        ctx = context()
+        self.positions = _TwoPhaseParticles(self, 0)
+        self.velocities = _TwoPhaseParticles(self, 1)
+        self.phase = BorrowedField(hs[0], ctx)
+        self.concentration = self.phase
+        self.liquid_fraction = BorrowedField(hs[1], ctx)
+        self.density = BorrowedField(hs[2], ctx)
+        self.beta_u = BorrowedField(hs[3], ctx)
+        self.beta_v = BorrowedField(hs[4], ctx)
+        pf = [C.c_void_p() for _ in range(4)]
+        _lib.check(lib.ff_pressure3_fields(hs[5], *[C.byref(x) for x in pf]))
+        self.pressure = BorrowedField(pf[0], ctx)
+        self.diagnostics = {}
+
+    def set_particle_count(self, n):
+        _lib.check(_lib.load().ff_twophase2_set_count(self.handle, int(n)))
+
+    def stage(self, name):
+        _lib.check(_lib.load().ff_twophase2_stage(self.handle, self.STAGES[name]))
+
+    def resample_stats(self):
+        v = (C.c_int64 * 4)()
+        _lib.check(_lib.load().ff_twophase2_resample_stats(self.handle, v))
+        return {"liquidDonors": v[0], "liquidRequested": v[1], "gasDonors": v[2], "gasRequested": v[3]}
+
+    def on_advance_time_step(self):
+        """onAdvanceTimeStep(): returns the projection's diagnostics."""
+        d = _lib.Diag()
+        _lib.check(_lib.load().ff_twophase2_step(self.handle, C.byref(d)))
+        self.diagnostics = {"converged": bool(d.converged), "rejected": bool(d.rejected),
+                            "iterations": d.iterations, "stoppedBy": STOP_REASONS.get(d.stopped_by, "none"),
+                            "residual": d.residual}
+        return self.diagnostics
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.load().ff_twophase2_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def create_grid_two_phase_flip_solver2(**options):
+    return GridTwoPhaseFlipSolver2(**options)
+
+
 class GridSolver3:
     """createGridSolver3({velocityGrid, gridSpacing, origin, force, dirichlet,
     collider, inflows, closedDomainBoundaryFlag, dt, advection, pressure})
