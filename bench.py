@@ -14,6 +14,7 @@ reference is JavaScript + WebGPU and cannot run on this machine) on the
 host cores, on a bounded sample of the same workload.
 """
 import argparse
+import datetime
 import json
 import os
 import subprocess
@@ -66,43 +67,68 @@ def peaks():
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling every 20 ms, started before the solver is built so
+    that it is running when the timed region opens.  mark() and stop() record the
+    wall-clock bracket of the timed region; the summary keeps the rows whose
+    nvidia-smi timestamp falls inside it (the nearest rows when none do)."""
+
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self):
         self.proc = None
         self.path = os.path.join(ROOT, "gpurun_out", "clocks.csv")
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
-                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-lms", "200", "-i", str(os.environ.get("LOCAL_RANK", 0))],
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits", "-lms", "20", "-i",
+                 str(os.environ.get("LOCAL_RANK", 0))],
                 stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
 
+    def mark(self):
+        """the timed region opens"""
+        self.t0 = datetime.datetime.now()
+
     def stop(self):
         if not self.proc:
             return None
+        self.t1 = datetime.datetime.now()
+        time.sleep(0.05)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
         self.f.close()
-        rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        rows = [[c.strip() for c in r.split(",")] for r in open(self.path).read().strip().splitlines()
+                if r.count(",") >= 9]
         if not rows:
             return None
-        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
-        mx = max(float(r[2]) for r in rows)
+        stamp = []
+        for r in rows:
+            try:
+                stamp.append(datetime.datetime.strptime(r[0], "%Y/%m/%d %H:%M:%S.%f"))
+            except ValueError:
+                stamp.append(None)
+        inside = [r for r, t in zip(rows, stamp) if t is not None and self.t0 <= t <= self.t1]
+        if not inside and all(t is not None for t in stamp):
+            # the sample closest to the middle of the region
+            mid = self.t0 + (self.t1 - self.t0) / 2
+            inside = [min(zip(rows, stamp), key=lambda rt: abs((rt[1] - mid).total_seconds()))[0]]
+        rows = inside or rows
+        sm = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        mx = max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip() == "Active"})
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[6 + i] == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": reasons,
-                "samples": len(rows)}
+                "samples": len(inside), "interval_ms": 20}
 
 
 def dist_setup(n_gpus):
@@ -150,6 +176,9 @@ def run_gb300(args):
     grid = ff.FaceCenteredGrid3(shape, h).set(sc["u"], sc["v"], sc["w"])
     out = ff.FaceCenteredGrid3(shape, h)
     levels = max(1, int(np.log2(n)) - 2)          # 256 -> 6 levels, 8^3 coarsest
+    clocks = Clocks()   # sampling from here on: running well before the timed region
+    if not args.profile_only:
+        clocks.start()
     solver = ff.create_grid_pressure_solver3(
         shape, h, collider_weights=cw, dirichlet=(sc["active"], sc["target"]),
         multigrid={"numberOfLevels": levels, "coarseSolve": args.coarse},
@@ -174,10 +203,9 @@ def run_gb300(args):
         return
 
     # device-resident timing
-    clocks = Clocks()
     barrier(dist)
     ctx.synchronize()
-    clocks.start()
+    clocks.mark()
     _lib.check(lib.ff_ctx_event_record(ctx.handle, 0))
     launches = 0
     diags = []
