@@ -463,21 +463,19 @@ __global__ void k_correct3(Dims d, int naxes, float hx, float hy, float hz, cons
                            const float *fwu, const float *fwv, const float *fww, const float *cwu,
                            const float *cwv, const float *cww, const float *uin, const float *vin,
                            const float *win, float *uout, float *vout, float *wout) {
+    // one thread per cell: its lower face on each axis, and the upper
+    // domain-edge face when the cell is the last along that axis
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
-    if (i > d.nx || j > d.ny) return;
-    const bool cell_in = i < d.nx && j < d.ny && k < d.nz;
+    if (i >= d.nx || j >= d.ny) return;
     const long long c = i + (long long)d.nx * (j + (long long)d.ny * k);
-    float pc = 0.f;
-    if (cell_in) {
-        pc = xh[c];
-    }
-    const float pcl = (cell_in && xl) ? xl[c] : 0.f;
-    // one face: m its index along the axis, nm the cells along it
-    auto face = [&](int m, int nm, long long f, long long off, float h, const float *fw, const float *cw,
-                    const float *in, float *out) {
-        if (m <= 0 || m >= nm) {
+    const float pc = xh[c];
+    const float pcl = xl ? xl[c] : 0.f;
+    // a face strictly inside the domain along its axis (m > 0)
+    auto face = [&](int m, long long f, long long off, float h, const float *fw, const float *cw, const float *in,
+                    float *out) {
+        if (m == 0) {
             if (in != out) out[f] = in[f];
             return;
         }
@@ -488,12 +486,17 @@ __global__ void k_correct3(Dims d, int naxes, float hx, float hy, float hz, cons
         if (cw) g = g * (cw[f] > 0.f ? 1.f : 0.f);
         out[f] = in[f] - g;
     };
-    if (j < d.ny && k < d.nz)
-        face(i, d.nx, i + (long long)(d.nx + 1) * (j + (long long)d.ny * k), 1, hx, fwu, cwu, uin, uout);
-    if (i < d.nx && k < d.nz)
-        face(j, d.ny, i + (long long)d.nx * (j + (long long)(d.ny + 1) * k), d.nx, hy, fwv, cwv, vin, vout);
-    if (naxes == 3 && i < d.nx && j < d.ny)
-        face(k, d.nz, c, (long long)d.nx * d.ny, hz, fww, cww, win, wout);
+    const long long fu = i + (long long)(d.nx + 1) * (j + (long long)d.ny * k);
+    face(i, fu, 1, hx, fwu, cwu, uin, uout);
+    if (i == d.nx - 1 && uin != uout) uout[fu + 1] = uin[fu + 1];
+    const long long fv = i + (long long)d.nx * (j + (long long)(d.ny + 1) * k);
+    face(j, fv, d.nx, hy, fwv, cwv, vin, vout);
+    if (j == d.ny - 1 && vin != vout) vout[fv + d.nx] = vin[fv + d.nx];
+    if (naxes == 3) {
+        const long long plane = (long long)d.nx * d.ny;
+        face(k, c, plane, hz, fww, cww, win, wout);
+        if (k == d.nz - 1 && win != wout) wout[c + plane] = win[c + plane];
+    }
 }
 
 }  // namespace
@@ -570,7 +573,7 @@ int correct(Dims d, float hx, float hy, float hz, const float *x_hi, const float
     const float *ins[3] = {uin, vin, win};
     float *outs[3] = {uout, vout, wout};
     const int naxes = d.nz > 1 ? 3 : 2;
-    auto L = launch3(d.nx + 1, d.ny + 1, d.nz + (naxes == 3 ? 1 : 0));
+    auto L = launch3(d.nx, d.ny, d.nz);
     k_correct3<<<L.grid, L.block, 0, s>>>(d, naxes, hx, hy, hz, x_hi, x_lo, fw[0], fw[1], fw[2], cw[0], cw[1],
                                           cw[2], ins[0], ins[1], ins[2], outs[0], outs[1], outs[2]);
     return post("correct");

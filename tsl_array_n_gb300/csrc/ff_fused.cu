@@ -2138,7 +2138,8 @@ __global__ void __launch_bounds__(256) k_prolong4(Dims fd, Dims cd, int dims, co
 // The V-cycle below a level (its pre-smoothing, residual and restriction,
 // every coarser level, the direct coarsest solve, the prolongations and the
 // post-smoothing) in one cooperative launch: phases over all cells of one
-// level separated by grid-wide barriers.  The coarse levels are too small
+// level separated by grid-wide barriers.  Tail levels hold at most 2^18
+// cells (the host picks them so), so cell indices are 32-bit.  The coarse levels are too small
 // to fill the GPU, so one launch per sweep would cost more in launch and
 // pipeline latency than in work.  Colour passes run in place (a colour
 // reads only the other colour); the first pass on a level writes every cell,
@@ -2217,7 +2218,7 @@ __device__ void tail_done(unsigned *bar) {
 }
 
 __device__ __forceinline__ unsigned tail_class(const TailLevel &L, int i, int j, int k) {
-    return (__ldg(L.cls + (long long)L.cpitch * (j + (long long)L.g.d.ny * k) + (i >> 2)) >> (2 * (i & 3))) & 3u;
+    return (__ldg(L.cls + L.cpitch * (j + L.g.d.ny * k) + (i >> 2)) >> (2 * (i & 3))) & 3u;
 }
 
 // the relaxation of one cell by class (the TMA sweep's arithmetic)
@@ -2251,15 +2252,15 @@ __device__ void tail_colour(const TailArgs &a, const TailLevel &L, int col, bool
                             long long stride) {
     const Geo &g = L.g;
     const int nx = g.d.nx, ny = g.d.ny, nz = g.d.nz, hx = nx >> 1;
-    const long long n = (long long)hx * ny * nz;
+    const int n = hx * ny * nz;
     float *x = L.x;
-    for (long long t = t0; t < n; t += stride) {
-        const int m = (int)(t % hx);
-        const long long rr = t / hx;
-        const int j = (int)(rr % ny), k = (int)(rr / ny);
+    for (int t = (int)t0; t < n; t += (int)stride) {
+        const int m = t % hx;
+        const int rr = t / hx;
+        const int j = rr % ny, k = rr / ny;
         const int par = (j + k + col) & 1;
         const int i = 2 * m + par;
-        const long long c = i + g.sy * j + g.sz * k;
+        const int c = i + (int)g.sy * j + (int)g.sz * k;
         float vc = 0.f, xm = 0.f, xp = 0.f, ym = 0.f, yp = 0.f, zm = 0.f, zp = 0.f;
         if (first) {
             x[c + (par ? -1 : 1)] = 0.f;
@@ -2280,12 +2281,12 @@ __device__ void tail_colour(const TailArgs &a, const TailLevel &L, int col, bool
 __device__ void tail_residual(const TailLevel &L, bool xzero, long long t0, long long stride) {
     const Geo &g = L.g;
     const int nx = g.d.nx, ny = g.d.ny, nz = g.d.nz;
-    const long long n = (long long)nx * ny * nz;
+    const int n = nx * ny * nz;
     const float *x = L.x;
-    for (long long c = t0; c < n; c += stride) {
-        const int i = (int)(c % nx);
-        const long long rr = c / nx;
-        const int j = (int)(rr % ny), k = (int)(rr / ny);
+    for (int c = (int)t0; c < n; c += (int)stride) {
+        const int i = c % nx;
+        const int rr = c / nx;
+        const int j = rr % ny, k = rr / ny;
         const unsigned cl = tail_class(L, i, j, k);
         if (xzero) {
             L.r[c] = cl == 1u ? 0.f : __ldcg(L.b + c);
@@ -2306,12 +2307,12 @@ __device__ void tail_residual(const TailLevel &L, bool xzero, long long t0, long
 __device__ void tail_restrict(const TailArgs &a, const TailLevel &F, const TailLevel &C, bool relax0, long long t0,
                               long long stride) {
     const Dims fd = F.g.d, cd = C.g.d;
-    const long long n = (long long)cd.nx * cd.ny * cd.nz;
+    const int n = cd.nx * cd.ny * cd.nz;
     const float w4[4] = {0.125f, 0.375f, 0.375f, 0.125f};
-    for (long long c = t0; c < n; c += stride) {
-        const int I = (int)(c % cd.nx);
-        const long long rr = c / cd.nx;
-        const int J = (int)(rr % cd.ny), K = (int)(rr / cd.ny);
+    for (int c = (int)t0; c < n; c += (int)stride) {
+        const int I = c % cd.nx;
+        const int rr = c / cd.nx;
+        const int J = rr % cd.ny, K = rr / cd.ny;
         if (C.mask && __ldg(C.mask + c)) {
             C.b[c] = 0.f;
             if (relax0)
@@ -2332,7 +2333,7 @@ __device__ void tail_restrict(const TailArgs &a, const TailLevel &F, const TailL
             float part = 0.f;
 #pragma unroll
             for (int p = 0; p < 4; ++p) {
-                const float *row = F.r + (long long)fd.nx * (jy[p] + (long long)fd.ny * kz[q]);
+                const float *row = F.r + fd.nx * (jy[p] + fd.ny * kz[q]);
                 const float rx = 0.125f * __ldcg(row + ix[0]) + 0.375f * __ldcg(row + ix[1]) +
                                  0.375f * __ldcg(row + ix[2]) + 0.125f * __ldcg(row + ix[3]);
                 part += rx * w4[p];
@@ -2365,12 +2366,12 @@ __device__ void tail_direct(const TailArgs &a, const TailLevel &C) {
 __device__ void tail_prolong(const TailArgs &a, const TailLevel &C, const TailLevel &F, long long t0,
                              long long stride) {
     const Dims fd = F.g.d, cd = C.g.d;
-    const long long n = (long long)fd.nx * fd.ny * fd.nz;
-    for (long long c = t0; c < n; c += stride) {
+    const int n = fd.nx * fd.ny * fd.nz;
+    for (int c = (int)t0; c < n; c += (int)stride) {
         if (F.mask && __ldg(F.mask + c)) continue;
-        const int i = (int)(c % fd.nx);
-        const long long rr = c / fd.nx;
-        const int j = (int)(rr % fd.ny), k = (int)(rr / fd.ny);
+        const int i = c % fd.nx;
+        const int rr = c / fd.nx;
+        const int j = rr % fd.ny, k = rr / fd.ny;
         int ii[2], jj[2], kk[2];
         float wi[2], wj[2], wk[2];
         ptaps2(i, cd.nx, ii, wi);
@@ -2381,7 +2382,7 @@ __device__ void tail_prolong(const TailArgs &a, const TailLevel &C, const TailLe
         float acc = 0.f;
         for (int b = 0; b < 2; ++b)
             for (int q = 0; q < nk; ++q) {
-                const float *row = C.x + (long long)cd.nx * (jj[b] + (long long)cd.ny * kk[q]);
+                const float *row = C.x + cd.nx * (jj[b] + cd.ny * kk[q]);
                 const float w = wj[b] * wk[q];
                 acc += (wi[0] * __ldcg(row + ii[0]) + wi[1] * __ldcg(row + ii[1])) * w;
             }
@@ -2393,12 +2394,12 @@ __device__ void tail_prolong(const TailArgs &a, const TailLevel &C, const TailLe
 // (k_coarse_sweeps' arithmetic: x += sor (b - A x) / diag)
 __device__ void tail_coarse_colour(const TailArgs &a, const TailLevel &C, int col, long long t0, long long stride) {
     const Dims d = C.g.d;
-    const long long sy = d.nx, sz = (long long)d.nx * d.ny, n = d.n();
+    const int sy = d.nx, sz = d.nx * d.ny, n = (int)d.n();
     float *x = C.x;
-    for (long long c = t0; c < n; c += stride) {
-        const int i = (int)(c % d.nx);
-        const long long rr = c / d.nx;
-        const int j = (int)(rr % d.ny), k = (int)(rr / d.ny);
+    for (int c = (int)t0; c < n; c += (int)stride) {
+        const int i = c % d.nx;
+        const int rr = c / d.nx;
+        const int j = rr % d.ny, k = rr / d.ny;
         if (((i + j + k) & 1) != col) continue;
         const float xc = __ldcg(x + c);
         const float4 kc = __ldg(C.coef + c);
