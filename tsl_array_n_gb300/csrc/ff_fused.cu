@@ -2480,37 +2480,85 @@ __global__ void __launch_bounds__(TAIL_NT, 1) k_vcycle_tail(TailArgs a) {
 // Two bits per cell, one byte per x-quad (rows `pitch` bytes apart): 0 an
 // interior cell whose six couplings are the plain h^-2 and E = 0; 1 a
 // Dirichlet cell (E = 1, no coupling); 2 a domain-edge cell with the plain
-// couplings (zero across the edge); 3 anything else.
-__global__ void k_cell_classes(Geo g, const float4 *__restrict__ coef, uint8_t *cls, int pitch, float4 *gco) {
+// couplings (zero across the edge); 3 anything else, which also stores gco =
+// (upper x, y, z couplings, 1 / diagonal).
+//
+// The level's coefficients (k_build_coef's formulas, from the weights and
+// the Dirichlet mask) and its classes in one pass: the upper couplings a
+// class needs are the lower couplings of the next cells, computed here from
+// the same faces instead of read back from the coefficient array.
+__global__ void k_coef_classes(Geo g, int dims, const float *__restrict__ wu, const float *__restrict__ wv,
+                               const float *__restrict__ ww, const uint8_t *__restrict__ mask, float hx2, float hy2,
+                               float hz2, float4 *__restrict__ coef, uint2 *__restrict__ coef16,
+                               uint8_t *__restrict__ cls, int pitch, float4 *__restrict__ gco) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
-    if (4 * q >= g.d.nx || j >= g.d.ny) return;
+    const Dims d = g.d;
+    if (4 * q >= d.nx || j >= d.ny) return;
+    auto W = [](const float *w, long long f) { return w ? w[f] : 1.f; };
+    auto P = [&](long long n) { return mask ? mask[n] != 0 : false; };
     unsigned byte = 0;
 #pragma unroll
-    for (int d = 0; d < 4; ++d) {
-        const int i = 4 * q + d;
+    for (int dd = 0; dd < 4; ++dd) {
+        const int i = 4 * q + dd;
         const long long c = i + g.sy * j + g.sz * k;
-        const float4 a = coef[c];
-        const float ux = i < g.d.nx - 1 ? coef[c + 1].x : 0.f;
-        const float uy = j < g.d.ny - 1 ? coef[c + g.sy].y : 0.f;
-        const float uz = k < g.d.nz - 1 ? coef[c + g.sz].z : 0.f;
-        const bool plain = a.x == (i > 0 ? g.h2x : 0.f) && ux == (i < g.d.nx - 1 ? g.h2x : 0.f) &&
-                           a.y == (j > 0 ? g.h2y : 0.f) && uy == (j < g.d.ny - 1 ? g.h2y : 0.f) &&
-                           a.z == (k > 0 ? g.h2z : 0.f) && uz == (k < g.d.nz - 1 ? g.h2z : 0.f) && a.w == 0.f;
-        const bool pinned = a.w == 1.f && a.x == 0.f && a.y == 0.f && a.z == 0.f && ux == 0.f && uy == 0.f &&
-                            uz == 0.f;
-        const bool inner = i > 0 && i < g.d.nx - 1 && j > 0 && j < g.d.ny - 1 && k > 0 && k < g.d.nz - 1;
+        const long long fu = i + (long long)(d.nx + 1) * (j + (long long)d.ny * k);
+        const long long fv = i + (long long)d.nx * (j + (long long)(d.ny + 1) * k);
+        const bool pc = P(c);
+        float kx = 0.f, ky = 0.f, kz = 0.f, e = 0.f;
+        if (i > 0) { if (!pc && !P(c - 1)) kx = W(wu, fu) * hx2; else if (!pc) e += W(wu, fu) * hx2; }
+        if (i < d.nx - 1 && !pc && P(c + 1)) e += W(wu, fu + 1) * hx2;
+        if (j > 0) { if (!pc && !P(c - g.sy)) ky = W(wv, fv) * hy2; else if (!pc) e += W(wv, fv) * hy2; }
+        if (j < d.ny - 1 && !pc && P(c + g.sy)) e += W(wv, fv + d.nx) * hy2;
+        if (dims == 3) {
+            if (k > 0) { if (!pc && !P(c - g.sz)) kz = W(ww, c) * hz2; else if (!pc) e += W(ww, c) * hz2; }
+            if (k < d.nz - 1 && !pc && P(c + g.sz)) e += W(ww, c + g.sz) * hz2;
+        }
+        if (pc) e = 1.f;
+        coef[c] = make_float4(kx, ky, kz, e);
+        if (coef16) {
+            auto b16 = [](float v) { return (unsigned)__bfloat16_as_ushort(__float2bfloat16_rn(v)); };
+            coef16[c] = make_uint2(b16(kx) | (b16(ky) << 16), b16(kz) | (b16(e) << 16));
+        }
+        // the next cells' lower couplings (their k_build_coef x, y, z)
+        const float ux = (i < d.nx - 1 && !P(c + 1) && !pc) ? W(wu, fu + 1) * hx2 : 0.f;
+        const float uy = (j < d.ny - 1 && !P(c + g.sy) && !pc) ? W(wv, fv + d.nx) * hy2 : 0.f;
+        const float uz = (dims == 3 && k < d.nz - 1 && !P(c + g.sz) && !pc) ? W(ww, c + g.sz) * hz2 : 0.f;
+        const bool plain = kx == (i > 0 ? g.h2x : 0.f) && ux == (i < d.nx - 1 ? g.h2x : 0.f) &&
+                           ky == (j > 0 ? g.h2y : 0.f) && uy == (j < d.ny - 1 ? g.h2y : 0.f) &&
+                           kz == (k > 0 ? g.h2z : 0.f) && uz == (k < d.nz - 1 ? g.h2z : 0.f) && e == 0.f;
+        const bool pinned = e == 1.f && kx == 0.f && ky == 0.f && kz == 0.f && ux == 0.f && uy == 0.f && uz == 0.f;
+        const bool inner = i > 0 && i < d.nx - 1 && j > 0 && j < d.ny - 1 && k > 0 && k < d.nz - 1;
         const unsigned cl = plain ? (inner ? 0u : 2u) : (pinned ? 1u : 3u);
-        byte |= cl << (2 * d);
+        byte |= cl << (2 * dd);
         if (cl == 3u) {
-            // the row's diagonal as the relaxation divides by it (absent
-            // faces at the domain edge carry no coupling)
-            const float kx = i > 0 ? a.x : 0.f, ky = j > 0 ? a.y : 0.f, kz = k > 0 ? a.z : 0.f;
-            const float diag = -(a.w + kx + ux + ky + uy + kz + uz);
+            const float diag = -(e + kx + ux + ky + uy + kz + uz);
             gco[c] = make_float4(ux, uy, uz, 1.f / diag);
         }
     }
-    cls[q + (long long)pitch * (j + (long long)g.d.ny * k)] = (uint8_t)byte;
+    cls[q + (long long)pitch * (j + (long long)d.ny * k)] = (uint8_t)byte;
+}
+
+// Brick flags from the classes: a brick is regular when every cell of it,
+// extended by two cells on each side, is of class 0 or 2.  A plain class
+// also checks the cell's upper couplings, so this marks a subset of the
+// bricks the coefficient test (k_brick_flags) marks: every brick flagged
+// regular here is regular by that test too.
+__global__ void k_brick_flags_cls(Geo g, const uint8_t *__restrict__ cls, int pitch, uint8_t *bricks) {
+    const int bx = blockIdx.x, by = blockIdx.y, bz = blockIdx.z;
+    const int ia = max(0, bx * TX - 2), ib = min(g.d.nx, bx * TX + TX + 2);
+    const int ja = max(0, by * TY - 2), jb = min(g.d.ny, by * TY + TY + 2);
+    const int ka = max(0, bz * BZ - 2), kb = min(g.d.nz, bz * BZ + BZ + 2);
+    const int w = ib - ia, hgt = jb - ja, dep = kb - ka;
+    const int total = w * hgt * dep;
+    int ok = 1;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int i = ia + t % w, r = t / w, j = ja + r % hgt, k = ka + r / hgt;
+        const unsigned cl = (cls[(long long)pitch * (j + (long long)g.d.ny * k) + (i >> 2)] >> (2 * (i & 3))) & 3u;
+        if (cl & 1u) ok = 0;
+    }
+    ok = __syncthreads_and(ok);
+    if (threadIdx.x == 0) bricks[bx + (long long)g.bnx * (by + (long long)g.bny * bz)] = (uint8_t)ok;
 }
 
 // ------------------------------------------------------- sweep work order --
@@ -2820,16 +2868,29 @@ int sweep_tma_maps(const Level &L, const float *x0, const float *x1, uint8_t *cl
     return FF_OK;
 }
 
-int cell_classes(const Level &L, const SweepMaps &m, const uint8_t *bricks, int sm_count, cudaStream_t s) {
-    FF_CHECK(m.cls_ptr && m.cls_pitch > 0, FF_E_STATE, "cell classes: class array not allocated");
+static int work_orders(const Level &L, const SweepMaps &m, const uint8_t *bricks, int sm_count, cudaStream_t s);
+
+int coef_classes(const Level &L, const SweepMaps &m, uint8_t *bricks, int dims, int want16, int sm_count,
+                 cudaStream_t s) {
+    FF_CHECK(m.cls_ptr && m.cls_pitch > 0 && m.gco, FF_E_STATE, "cell classes: class arrays not allocated");
     Geo g = make_geo(L);
     const int nq = L.d.nx / 4;
-    // blocks of (quads of a row rounded up to a warp, at most 128) x rows
     const int bx = std::min(128, (nq + 31) / 32 * 32), by = 256 / bx;
     dim3 grid((nq + bx - 1) / bx, (L.d.ny + by - 1) / by, L.d.nz);
-    FF_CHECK(m.gco, FF_E_STATE, "cell classes: coefficient array not allocated");
-    k_cell_classes<<<grid, dim3(bx, by), 0, s>>>(g, L.coef, m.cls_ptr, m.cls_pitch, m.gco);
-    FF_TRY(post("cell_classes"));
+    k_coef_classes<<<grid, dim3(bx, by), 0, s>>>(g, dims, L.w[0], L.w[1], L.w[2], L.mask, L.h2inv[0], L.h2inv[1],
+                                                  L.h2inv[2], L.coef, want16 ? L.coef16 : nullptr, m.cls_ptr,
+                                                  m.cls_pitch, m.gco);
+    FF_TRY(post("coef_classes"));
+    if (bricks) {
+        dim3 bg(g.bnx, g.bny, (L.d.nz + BZ - 1) / BZ);
+        k_brick_flags_cls<<<bg, 256, 0, s>>>(g, m.cls_ptr, m.cls_pitch, bricks);
+        FF_TRY(post("brick_flags_cls"));
+    }
+    return work_orders(L, m, bricks, sm_count, s);
+}
+
+static int work_orders(const Level &L, const SweepMaps &m, const uint8_t *bricks, int sm_count, cudaStream_t s) {
+    Geo g = make_geo(L);
     // work orders: the sweep's, and on level 0 those of the two CG kernels
     // (their own z-chunks for their own blocks per SM)
     for (int w = 0; w < 3; ++w) {

@@ -210,7 +210,11 @@ int prolong4(const Level &c, const Level &f, int dims, float *fine_x, const PcgS
 bool sweep_tma_ok(const Dims &d);
 size_t sweep_tma_cls_bytes(const Dims &d);
 int sweep_tma_maps(const Level &L, const float *x0, const float *x1, uint8_t *cls, SweepMaps &m);
-int cell_classes(const Level &L, const SweepMaps &m, const uint8_t *bricks, int sm_count, cudaStream_t s);
+// the level's coefficients (as build_coef), classes, brick flags from the
+// classes (when bricks is non-null) and work orders in one pass over the
+// weights and mask
+int coef_classes(const Level &L, const SweepMaps &m, uint8_t *bricks, int dims, int want16, int sm_count,
+                 cudaStream_t s);
 size_t cls_row_pitch(const Dims &d);
 // the V-cycle from level lv[0] down to the coarsest lv[nl-1] and back, one
 // cooperative launch (coarse_sweeps > 0: sweeps instead of G b at the bottom)

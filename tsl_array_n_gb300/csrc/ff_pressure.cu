@@ -415,6 +415,17 @@ extern "C" int ff_pressure3_fields(ff_pressure ps, ff_field *pressure, ff_field 
 // --------------------------------------------------------------- prepare --
 static const float *fptr(ff_field f) { return f ? (const float *)f->d : nullptr; }
 
+// a level's coefficients, brick flags, classes and work orders: one fused
+// pass where the level keeps classes, else the coefficient kernels
+static int build_level(ff_pressure ps, int l, cudaStream_t s) {
+    Level &L = ps->lv[l];
+    if (ps->smaps && ps->smaps[l].cls_ptr)
+        return ffk::coef_classes(L, ps->smaps[l], ps->bricks[l], ps->dims, ps->vbf(), ps->ctx->sm_count, s);
+    FF_TRY(ffk::build_coef(L, ps->dims, ps->vbf(), s));
+    if (ps->bricks[l]) FF_TRY(ffk::brick_flags(L, ps->bricks[l], s));
+    return FF_OK;
+}
+
 static int prepare(ff_pressure ps, ff_field u, ff_field v, ff_field w) {
     cudaStream_t s = ps->s();
     const Dims &d = ps->d;
@@ -482,15 +493,9 @@ static int prepare(ff_pressure ps, ff_field u, ff_field v, ff_field w) {
         } else {
             FF_CUDA(cudaMemsetAsync(c.mask, 0, (size_t)c.d.n(), s));
         }
-        FF_TRY(ffk::build_coef(c, ps->dims, ps->vbf(), s));
-        if (ps->bricks[l]) FF_TRY(ffk::brick_flags(c, ps->bricks[l], s));
-        if (ps->smaps && ps->smaps[l].cls_ptr)
-            FF_TRY(ffk::cell_classes(c, ps->smaps[l], ps->bricks[l], ps->ctx->sm_count, s));
+        FF_TRY(build_level(ps, l, s));
     }
-    FF_TRY(ffk::build_coef(L0, ps->dims, ps->vbf(), s));
-    if (ps->bricks[0]) FF_TRY(ffk::brick_flags(L0, ps->bricks[0], s));
-    if (ps->smaps && ps->smaps[0].cls_ptr)
-        FF_TRY(ffk::cell_classes(L0, ps->smaps[0], ps->bricks[0], ps->ctx->sm_count, s));
+    FF_TRY(build_level(ps, 0, s));
     ps->prepared = true;
     // FP64 direct coarsest solve: refactor when the coarsest operator changed
     if (ps->desc.preconditioner == FF_PRE_MULTIGRID && ps->desc.mg_coarse_mode == FF_COARSE_DIRECT) {
