@@ -1993,6 +1993,62 @@ __global__ void __launch_bounds__(256, 4) k_resid_rx(Geo g, const float *__restr
     *reinterpret_cast<float2 *>(rx + (long long)cnx * (j + (long long)g.d.ny * k) + 2 * qx) = out;
 }
 
+// k_resid_rx with whole rows of quads in the block (blockDim.x = nx / 4,
+// which divides 256): the residuals at i0 - 1 and i0 + 4 are the row
+// neighbours' r3 and r0, exchanged through shared memory, so no lane
+// recomputes a residual at a warp's edge
+__global__ void __launch_bounds__(256, 4) k_resid_rx_rows(Geo g, const float *__restrict__ x,
+                                                       const float *__restrict__ b, const float4 *__restrict__ coef,
+                                                       const uint8_t *__restrict__ cls, int cpitch,
+                                                       float *__restrict__ rx, const PcgState *st) {
+    __shared__ float s_r0[256], s_r3[256];
+    pdl_wait();
+    if (st && st->stop) return;
+    const int nq = g.d.nx >> 2, cnx = g.d.nx >> 1;
+    const int qx = threadIdx.x;
+    const int jr = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    const bool valid = jr < g.d.ny;
+    const int j = valid ? jr : g.d.ny - 1;   // rows past the end compute a copy of the last and store nothing
+    const int i0 = 4 * qx;
+    const long long row = g.sy * j + g.sz * k;
+    const long long rym = row + (j > 0 ? -g.sy : 0), ryp = row + (j < g.d.ny - 1 ? g.sy : 0);
+    const long long rzm = row + (k > 0 ? -g.sz : 0), rzp = row + (k < g.d.nz - 1 ? g.sz : 0);
+    const uint8_t *crow = cls + (long long)cpitch * (j + (long long)g.d.ny * k);
+    const float4 c = __ldg(reinterpret_cast<const float4 *>(x + row + i0));
+    const float xl = i0 > 0 ? __ldg(x + row + i0 - 1) : c.x;
+    const float xr = i0 + 4 < g.d.nx ? __ldg(x + row + i0 + 4) : c.w;
+    const float4 ym = __ldg(reinterpret_cast<const float4 *>(x + rym + i0));
+    const float4 yp = __ldg(reinterpret_cast<const float4 *>(x + ryp + i0));
+    const float4 zm = __ldg(reinterpret_cast<const float4 *>(x + rzm + i0));
+    const float4 zp = __ldg(reinterpret_cast<const float4 *>(x + rzp + i0));
+    const float4 bq = __ldg(reinterpret_cast<const float4 *>(b + row + i0));
+    const unsigned cq = crow[qx];
+    float r0, r1, r2, r3;
+    if (cq == 0) {
+        r0 = bq.x - apply_reg(g, c.x, xl, c.y, ym.x, yp.x, zm.x, zp.x);
+        r1 = bq.y - apply_reg(g, c.y, c.x, c.z, ym.y, yp.y, zm.y, zp.y);
+        r2 = bq.z - apply_reg(g, c.z, c.y, c.w, ym.z, yp.z, zm.z, zp.z);
+        r3 = bq.w - apply_reg(g, c.w, c.z, xr, ym.w, yp.w, zm.w, zp.w);
+    } else {
+        r0 = resid_cls(g, coef, cq & 3u, i0, j, k, bq.x, c.x, xl, c.y, ym.x, yp.x, zm.x, zp.x);
+        r1 = resid_cls(g, coef, (cq >> 2) & 3u, i0 + 1, j, k, bq.y, c.y, c.x, c.z, ym.y, yp.y, zm.y, zp.y);
+        r2 = resid_cls(g, coef, (cq >> 4) & 3u, i0 + 2, j, k, bq.z, c.z, c.y, c.w, ym.z, yp.z, zm.z, zp.z);
+        r3 = resid_cls(g, coef, (cq >> 6) & 3u, i0 + 3, j, k, bq.w, c.w, c.z, xr, ym.w, yp.w, zm.w, zp.w);
+    }
+    const int t = threadIdx.y * blockDim.x + qx;
+    s_r0[t] = r0;
+    s_r3[t] = r3;
+    __syncthreads();
+    // fine 2I-1 clamps to 2I at I = 0, fine 2I+2 to 2I+1 at the row's end
+    const float rl = qx == 0 ? r0 : s_r3[t - 1];
+    const float rh = qx == nq - 1 ? r3 : s_r0[t + 1];
+    if (!valid) return;
+    float2 out;
+    out.x = 0.125f * rl + 0.375f * r0 + 0.375f * r1 + 0.125f * r2;
+    out.y = 0.125f * r1 + 0.375f * r2 + 0.375f * r3 + 0.125f * rh;
+    *reinterpret_cast<float2 *>(rx + (long long)cnx * (j + (long long)g.d.ny * k) + 2 * qx) = out;
+}
+
 __global__ void k_restrict_yz(Dims fd, Dims cd, int dims, const float *__restrict__ rx,
                               const uint8_t *__restrict__ cmask, float *__restrict__ cb, const PcgState *st) {
     if (st && st->stop) return;
@@ -2753,9 +2809,14 @@ int res_restrict2(const Level &f, const SweepMaps &m, const float *x, float *rx,
     Geo g = make_geo(f);
     const long long nq = (long long)(f.d.nx / 4) * f.d.ny * f.d.nz;
     (void)nq;
-    FF_CUDA(launch_pdl(k_resid_rx, dim3((f.d.nx / 4 + 31) / 32, (f.d.ny + 7) / 8, f.d.nz), dim3(32, 8), 0, s,
-                       g, x, (const float *)f.b, f.coef, m.cls_ptr, m.cls_pitch, rx,
-                                                         st));
+    const int nqr = f.d.nx / 4;
+    if (nqr <= 256 && 256 % nqr == 0)
+        FF_CUDA(launch_pdl(k_resid_rx_rows, dim3(1, (f.d.ny + 256 / nqr - 1) / (256 / nqr), f.d.nz),
+                           dim3(nqr, 256 / nqr), 0, s, g, x, (const float *)f.b, f.coef, m.cls_ptr, m.cls_pitch, rx,
+                           st));
+    else
+        FF_CUDA(launch_pdl(k_resid_rx, dim3((f.d.nx / 4 + 31) / 32, (f.d.ny + 7) / 8, f.d.nz), dim3(32, 8), 0, s,
+                           g, x, (const float *)f.b, f.coef, m.cls_ptr, m.cls_pitch, rx, st));
     const long long nc = c.d.n();
     if (c.d.nx % 4 == 0 && c.d.nx == f.d.nx / 2)
         FF_CUDA(launch_pdl(k_restrict_yz4, dim3((c.d.nx / 4 + 31) / 32, (c.d.ny + 7) / 8, c.d.nz), dim3(32, 8), 0,
