@@ -1997,7 +1997,7 @@ __global__ void __launch_bounds__(256, 4) k_resid_rx(Geo g, const float *__restr
 // which divides 256): the residuals at i0 - 1 and i0 + 4 are the row
 // neighbours' r3 and r0, exchanged through shared memory, so no lane
 // recomputes a residual at a warp's edge
-__global__ void __launch_bounds__(256, 4) k_resid_rx_rows(Geo g, const float *__restrict__ x,
+__global__ void __launch_bounds__(256, 5) k_resid_rx_rows(Geo g, const float *__restrict__ x,
                                                        const float *__restrict__ b, const float4 *__restrict__ coef,
                                                        const uint8_t *__restrict__ cls, int cpitch,
                                                        float *__restrict__ rx, const PcgState *st) {
