@@ -2547,52 +2547,54 @@ __global__ void k_coef_classes(Geo g, int dims, const float *__restrict__ wu, co
                                const float *__restrict__ ww, const uint8_t *__restrict__ mask, float hx2, float hy2,
                                float hz2, float4 *__restrict__ coef, uint2 *__restrict__ coef16,
                                uint8_t *__restrict__ cls, int pitch, float4 *__restrict__ gco) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    // one thread per cell (coalesced coefficient stores); the four lanes of
+    // an x-quad (nx % 4 == 0, blockDim.x a multiple of 32) merge their
+    // classes into the quad's byte with shuffles
     const Dims d = g.d;
-    if (4 * q >= d.nx || j >= d.ny) return;
+    const int ir = blockIdx.x * blockDim.x + threadIdx.x;
+    const int jr = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    const bool in = ir < d.nx && jr < d.ny;   // whole quads are in or out
+    const int i = in ? ir : 0, j = in ? jr : 0;
     auto W = [](const float *w, long long f) { return w ? w[f] : 1.f; };
     auto P = [&](long long n) { return mask ? mask[n] != 0 : false; };
-    unsigned byte = 0;
-#pragma unroll
-    for (int dd = 0; dd < 4; ++dd) {
-        const int i = 4 * q + dd;
-        const long long c = i + g.sy * j + g.sz * k;
-        const long long fu = i + (long long)(d.nx + 1) * (j + (long long)d.ny * k);
-        const long long fv = i + (long long)d.nx * (j + (long long)(d.ny + 1) * k);
-        const bool pc = P(c);
-        float kx = 0.f, ky = 0.f, kz = 0.f, e = 0.f;
-        if (i > 0) { if (!pc && !P(c - 1)) kx = W(wu, fu) * hx2; else if (!pc) e += W(wu, fu) * hx2; }
-        if (i < d.nx - 1 && !pc && P(c + 1)) e += W(wu, fu + 1) * hx2;
-        if (j > 0) { if (!pc && !P(c - g.sy)) ky = W(wv, fv) * hy2; else if (!pc) e += W(wv, fv) * hy2; }
-        if (j < d.ny - 1 && !pc && P(c + g.sy)) e += W(wv, fv + d.nx) * hy2;
-        if (dims == 3) {
-            if (k > 0) { if (!pc && !P(c - g.sz)) kz = W(ww, c) * hz2; else if (!pc) e += W(ww, c) * hz2; }
-            if (k < d.nz - 1 && !pc && P(c + g.sz)) e += W(ww, c + g.sz) * hz2;
-        }
-        if (pc) e = 1.f;
-        coef[c] = make_float4(kx, ky, kz, e);
-        if (coef16) {
-            auto b16 = [](float v) { return (unsigned)__bfloat16_as_ushort(__float2bfloat16_rn(v)); };
-            coef16[c] = make_uint2(b16(kx) | (b16(ky) << 16), b16(kz) | (b16(e) << 16));
-        }
-        // the next cells' lower couplings (their k_build_coef x, y, z)
-        const float ux = (i < d.nx - 1 && !P(c + 1) && !pc) ? W(wu, fu + 1) * hx2 : 0.f;
-        const float uy = (j < d.ny - 1 && !P(c + g.sy) && !pc) ? W(wv, fv + d.nx) * hy2 : 0.f;
-        const float uz = (dims == 3 && k < d.nz - 1 && !P(c + g.sz) && !pc) ? W(ww, c + g.sz) * hz2 : 0.f;
-        const bool plain = kx == (i > 0 ? g.h2x : 0.f) && ux == (i < d.nx - 1 ? g.h2x : 0.f) &&
-                           ky == (j > 0 ? g.h2y : 0.f) && uy == (j < d.ny - 1 ? g.h2y : 0.f) &&
-                           kz == (k > 0 ? g.h2z : 0.f) && uz == (k < d.nz - 1 ? g.h2z : 0.f) && e == 0.f;
-        const bool pinned = e == 1.f && kx == 0.f && ky == 0.f && kz == 0.f && ux == 0.f && uy == 0.f && uz == 0.f;
-        const bool inner = i > 0 && i < d.nx - 1 && j > 0 && j < d.ny - 1 && k > 0 && k < d.nz - 1;
-        const unsigned cl = plain ? (inner ? 0u : 2u) : (pinned ? 1u : 3u);
-        byte |= cl << (2 * dd);
-        if (cl == 3u) {
-            const float diag = -(e + kx + ux + ky + uy + kz + uz);
-            gco[c] = make_float4(ux, uy, uz, 1.f / diag);
-        }
+    const long long c = i + g.sy * j + g.sz * k;
+    const long long fu = i + (long long)(d.nx + 1) * (j + (long long)d.ny * k);
+    const long long fv = i + (long long)d.nx * (j + (long long)(d.ny + 1) * k);
+    const bool pc = P(c);
+    float kx = 0.f, ky = 0.f, kz = 0.f, e = 0.f;
+    if (i > 0) { if (!pc && !P(c - 1)) kx = W(wu, fu) * hx2; else if (!pc) e += W(wu, fu) * hx2; }
+    if (i < d.nx - 1 && !pc && P(c + 1)) e += W(wu, fu + 1) * hx2;
+    if (j > 0) { if (!pc && !P(c - g.sy)) ky = W(wv, fv) * hy2; else if (!pc) e += W(wv, fv) * hy2; }
+    if (j < d.ny - 1 && !pc && P(c + g.sy)) e += W(wv, fv + d.nx) * hy2;
+    if (dims == 3) {
+        if (k > 0) { if (!pc && !P(c - g.sz)) kz = W(ww, c) * hz2; else if (!pc) e += W(ww, c) * hz2; }
+        if (k < d.nz - 1 && !pc && P(c + g.sz)) e += W(ww, c + g.sz) * hz2;
     }
-    cls[q + (long long)pitch * (j + (long long)d.ny * k)] = (uint8_t)byte;
+    if (pc) e = 1.f;
+    // the next cells' lower couplings (their k_build_coef x, y, z)
+    const float ux = (i < d.nx - 1 && !P(c + 1) && !pc) ? W(wu, fu + 1) * hx2 : 0.f;
+    const float uy = (j < d.ny - 1 && !P(c + g.sy) && !pc) ? W(wv, fv + d.nx) * hy2 : 0.f;
+    const float uz = (dims == 3 && k < d.nz - 1 && !P(c + g.sz) && !pc) ? W(ww, c + g.sz) * hz2 : 0.f;
+    const bool plain = kx == (i > 0 ? g.h2x : 0.f) && ux == (i < d.nx - 1 ? g.h2x : 0.f) &&
+                       ky == (j > 0 ? g.h2y : 0.f) && uy == (j < d.ny - 1 ? g.h2y : 0.f) &&
+                       kz == (k > 0 ? g.h2z : 0.f) && uz == (k < d.nz - 1 ? g.h2z : 0.f) && e == 0.f;
+    const bool pinned = e == 1.f && kx == 0.f && ky == 0.f && kz == 0.f && ux == 0.f && uy == 0.f && uz == 0.f;
+    const bool inner = i > 0 && i < d.nx - 1 && j > 0 && j < d.ny - 1 && k > 0 && k < d.nz - 1;
+    const unsigned cl = plain ? (inner ? 0u : 2u) : (pinned ? 1u : 3u);
+    unsigned byte = cl << (2 * (ir & 3));
+    byte |= __shfl_xor_sync(0xffffffffu, byte, 1);
+    byte |= __shfl_xor_sync(0xffffffffu, byte, 2);
+    if (!in) return;
+    coef[c] = make_float4(kx, ky, kz, e);
+    if (coef16) {
+        auto b16 = [](float v) { return (unsigned)__bfloat16_as_ushort(__float2bfloat16_rn(v)); };
+        coef16[c] = make_uint2(b16(kx) | (b16(ky) << 16), b16(kz) | (b16(e) << 16));
+    }
+    if (cl == 3u) {
+        const float diag = -(e + kx + ux + ky + uy + kz + uz);
+        gco[c] = make_float4(ux, uy, uz, 1.f / diag);
+    }
+    if ((i & 3) == 0) cls[(i >> 2) + (long long)pitch * (j + (long long)d.ny * k)] = (uint8_t)byte;
 }
 
 // Brick flags from the classes: a brick is regular when every cell of it,
@@ -2605,13 +2607,20 @@ __global__ void k_brick_flags_cls(Geo g, const uint8_t *__restrict__ cls, int pi
     const int ia = max(0, bx * TX - 2), ib = min(g.d.nx, bx * TX + TX + 2);
     const int ja = max(0, by * TY - 2), jb = min(g.d.ny, by * TY + TY + 2);
     const int ka = max(0, bz * BZ - 2), kb = min(g.d.nz, bz * BZ + BZ + 2);
-    const int w = ib - ia, hgt = jb - ja, dep = kb - ka;
-    const int total = w * hgt * dep;
+    // whole class bytes (x-quads) covering [ia, ib), cells outside masked off
+    const int qa = ia >> 2, qb = (ib - 1) >> 2;
+    const int wq = qb - qa + 1, hgt = jb - ja, dep = kb - ka;
+    const int total = wq * hgt * dep;
     int ok = 1;
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const int i = ia + t % w, r = t / w, j = ja + r % hgt, k = ka + r / hgt;
-        const unsigned cl = (cls[(long long)pitch * (j + (long long)g.d.ny * k) + (i >> 2)] >> (2 * (i & 3))) & 3u;
-        if (cl & 1u) ok = 0;
+    for (int t = threadIdx.x; t < total && ok; t += blockDim.x) {
+        const int q = qa + t % wq, r = t / wq, j = ja + r % hgt, k = ka + r / hgt;
+        unsigned m = 0;
+#pragma unroll
+        for (int dd = 0; dd < 4; ++dd) {
+            const int i = 4 * q + dd;
+            if (i >= ia && i < ib) m |= 1u << (2 * dd);   // the odd classes (1, 3) have the low bit set
+        }
+        if (cls[(long long)pitch * (j + (long long)g.d.ny * k) + q] & m) ok = 0;
     }
     ok = __syncthreads_and(ok);
     if (threadIdx.x == 0) bricks[bx + (long long)g.bnx * (by + (long long)g.bny * bz)] = (uint8_t)ok;
@@ -2935,9 +2944,11 @@ int coef_classes(const Level &L, const SweepMaps &m, uint8_t *bricks, int dims, 
                  cudaStream_t s) {
     FF_CHECK(m.cls_ptr && m.cls_pitch > 0 && m.gco, FF_E_STATE, "cell classes: class arrays not allocated");
     Geo g = make_geo(L);
-    const int nq = L.d.nx / 4;
-    const int bx = std::min(128, (nq + 31) / 32 * 32), by = 256 / bx;
-    dim3 grid((nq + bx - 1) / bx, (L.d.ny + by - 1) / by, L.d.nz);
+    // one thread per cell, blocks of (a row rounded up to a warp, at most
+    // 128 cells) x rows
+    const int bx = std::min(128, (L.d.nx + 31) / 32 * 32), by = 256 / bx;
+    dim3 grid((L.d.nx + bx - 1) / bx, (L.d.ny + by - 1) / by, L.d.nz);
+    FF_CHECK(L.d.nx % 4 == 0, FF_E_STATE, "cell classes need nx %% 4 == 0");
     k_coef_classes<<<grid, dim3(bx, by), 0, s>>>(g, dims, L.w[0], L.w[1], L.w[2], L.mask, L.h2inv[0], L.h2inv[1],
                                                   L.h2inv[2], L.coef, want16 ? L.coef16 : nullptr, m.cls_ptr,
                                                   m.cls_pitch, m.gco);
