@@ -4,8 +4,10 @@
 // reference counterpart: fluxflow has no network.
 //
 // Activations are stored channels-last (z, y, x, c) in BF16; convolutions
-// are implicit GEMMs (M = voxels, K = 27 taps x Cin, N = Cout) on the
-// tensor cores with BF16 operands and FP32 accumulation; pre-activations
+// are implicit GEMMs (M = voxels, K = 27 taps x Cin, N = Cout) with BF16
+// operands and FP32 accumulation, on tcgen05 (accumulators in TMEM) for the
+// forward and input-gradient convolutions and on WMMA for the weight
+// gradients; pre-activations
 // are kept in FP32 for the backward pass; master weights, gradients and the
 // Adam moments are FP32, with a BF16 copy of the weights for the GEMMs.
 // The input-gradient convolution reuses the forward kernel with the taps
@@ -23,7 +25,6 @@ typedef __nv_bfloat16 bf16;
 
 namespace {
 
-constexpr int MT = 64;   // voxels per conv block (4 warps x 16)
 
 __device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
 __device__ __forceinline__ float gelu_grad(float x) {
@@ -44,70 +45,212 @@ __device__ __forceinline__ void tap_offset(int t, int &dx, int &dy, int &dz) {
     dx = t % 3 - 1;
 }
 
-// 3x3x3 convolution, zero padding 1: Y[v, co] = act(sum_{t, ci} X[v + off(t), ci] W[t, ci, co] + bias[co]).
-// X has CIN channels (a multiple of 16), W is [27][CIN][COUT] BF16.  Writes
-// the FP32 pre-activation Z (if given) and the BF16 output Y (if given).
-template <int COUT>
-__global__ void __launch_bounds__(128) k_conv3(Vol v, const bf16 *__restrict__ X, int cin, const bf16 *__restrict__ W,
-                                              const float *__restrict__ bias, int act, float *__restrict__ Z,
-                                              bf16 *__restrict__ Y) {
-    constexpr int LDA = 16 + 8, LDB = COUT + 8, LDC = COUT + 4;
-    __shared__ __align__(32) bf16 As[MT * LDA];
-    __shared__ __align__(32) bf16 Bs[16 * LDB];
-    __shared__ __align__(32) float Cs[MT * LDC];
-    const int tid = threadIdx.x, warp = tid >> 5;
-    const long long v0 = (long long)blockIdx.x * MT;
-    const long long nvox = v.n();
-    // this thread's A rows: row r = tid / 2, 8 channels at half (tid & 1)
-    const int ar = tid >> 1, ah = tid & 1;
-    const long long av = v0 + ar;
-    int ax = 0, ay = 0, az = 0;
-    if (av < nvox) {
-        ax = (int)(av % v.nx);
-        ay = (int)((av / v.nx) % v.ny);
-        az = (int)(av / ((long long)v.nx * v.ny));
+// ---- tcgen05 convolution ------------------------------------------------
+// 3x3x3 convolution, zero padding 1: Y[v, co] = act(sum_{t, ci} X[v + off(t),
+// ci] W[t, ci, co] + bias[co]), X with Cin channels (a multiple of 16, at
+// most 96), writing the FP32 pre-activation Z and/or the BF16 output Y.
+// An implicit GEMM on the 5th-generation tensor cores: one CTA owns
+// 128 voxels (M = 128, one TMEM lane per voxel) and all Cout columns
+// (N = Cout, FP32 accumulators in TMEM); K runs over the 27 taps, one tap
+// (K = Cin) per stage.  Both operands sit in shared memory in the canonical
+// no-swizzle K-major layout: 8-row x 16-byte core matrices, core matrices
+// adjacent along K 128 bytes apart (LBO) and 8-row groups Cin / 8 x 128
+// bytes apart (SBO).  The A tile (128 voxel rows of the tap's shifted
+// input, zeros outside the volume) is gathered by the 128 threads, one row
+// each; the B tile (the tap's Cout x Cin weights) is a contiguous copy of
+// weights packed in that layout beforehand.  One elected thread issues the
+// MMAs and commits them to the stage's mbarrier; two stages alternate, so
+// the gather of tap t+1 overlaps the MMAs of tap t.  Waits are bounded
+// (0.5 s of globaltimer), after which the CTA flags the error, frees its
+// TMEM and returns.
+constexpr int TC_M = 128;
+
+__device__ __forceinline__ unsigned long long tc_timer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+// shared-memory matrix descriptor: start, leading (K) and stride (M/N)
+// byte offsets >> 4, descriptor version 1 (bits 46-47), no swizzle
+__device__ __forceinline__ uint64_t tc_sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo & 0x3FFFFu) >> 4) << 16) |
+           ((uint64_t)((sbo & 0x3FFFFu) >> 4) << 32) | (1ull << 46);
+}
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N >> 3 at bit 17, M >> 4 at bit 24
+__host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+// true once the phase of the given parity completed; false after 0.5 s
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    const unsigned long long t0 = tc_timer();
+    while (true) {
+        uint32_t done;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     " selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done)
+                     : "r"(bar), "r"(parity)
+                     : "memory");
+        if (done) return true;
+        if (tc_timer() - t0 > 500000000ull) return false;
     }
-    wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc[COUT / 16];
+}
+__device__ __forceinline__ void tc_mma(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, int acc) {
+    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+                 "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+// 16 consecutive FP32 accumulator columns of this thread's TMEM lane
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                 "%13, %14, %15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                   "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int j = 0; j < COUT / 16; ++j) wmma::fill_fragment(acc[j], 0.0f);
+    for (int q = 0; q < 16; ++q) v[q] = __uint_as_float(r[q]);
+}
+
+// the B operand of every tap in the canonical K-major layout: from W
+// [27][cin][cout] (N contiguous) to P[t][(n / 8) (cin / 8) + k / 8][n % 8][k % 8]
+__global__ void k_pack_b(int cin, int cout, const bf16 *__restrict__ W, bf16 *__restrict__ P) {
+    const long long n_all = 27LL * cin * cout;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n_all;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int t = (int)(e / ((long long)cin * cout));
+        const int rem = (int)(e - (long long)t * cin * cout);
+        const int k = rem / cout, n = rem % cout;
+        const long long dst = (long long)t * cin * cout +
+                              ((long long)((n >> 3) * (cin >> 3) + (k >> 3)) << 6) + ((n & 7) << 3) + (k & 7);
+        P[dst] = W[e];
+    }
+}
+
+template <int COUT>
+__global__ void __launch_bounds__(128) k_conv3_tc(Vol v, const bf16 *__restrict__ X, int cin,
+                                                 const bf16 *__restrict__ P, const float *__restrict__ bias, int act,
+                                                 float *__restrict__ Z, bf16 *__restrict__ Y, int *__restrict__ err) {
+    constexpr int TCOLS = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : 128);   // TMEM columns (a power of 2, >= 32)
+    extern __shared__ unsigned char tc_smem[];
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ uint32_t tmem_slot;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int a_bytes = TC_M * cin * 2, b_bytes = COUT * cin * 2;
+    const int stage_bytes = (a_bytes + b_bytes + 1023) & ~1023;
+    // stages start on a 1024-byte boundary of the shared window
+    const uint32_t raw = smem_u32(tc_smem);
+    unsigned char *stages = tc_smem + (((raw + 1023u) & ~1023u) - raw);
+    const uint32_t bar0 = smem_u32(&bars[0]), bar1 = smem_u32(&bars[1]);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(TCOLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+    }
+    if (tid == 0) {
+        mbar_init(bar0, 1);
+        mbar_init(bar1, 1);
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_slot;
+    const long long nvox = v.n();
+    const long long vox = (long long)blockIdx.x * TC_M + tid;
+    int ax = 0, ay = 0, az = 0;
+    if (vox < nvox) {
+        ax = (int)(vox % v.nx);
+        ay = (int)((vox / v.nx) % v.ny);
+        az = (int)(vox / ((long long)v.nx * v.ny));
+    }
+    const uint32_t idesc = tc_idesc(TC_M, COUT);
+    const uint32_t sbo = (uint32_t)(cin >> 3) * 128u;
+    const int groups = cin >> 3;
+    bool ok = true;
+    int last = -1;   // the last tap whose MMAs were committed
     for (int t = 0; t < 27; ++t) {
+        const int st = t & 1;
+        unsigned char *stg = stages + st * stage_bytes;
+        // the stage's previous MMAs (tap t - 2) must be done before it is overwritten
+        if (t >= 2) ok = mbar_wait(st ? bar1 : bar0, (uint32_t)(((t >> 1) - 1) & 1));
+        if (!__syncthreads_and(ok)) {
+            ok = false;
+            break;
+        }
         int dx, dy, dz;
         tap_offset(t, dx, dy, dz);
         const int sx = ax + dx, sy = ay + dy, sz = az + dz;
-        const bool in = av < nvox && sx >= 0 && sx < v.nx && sy >= 0 && sy < v.ny && sz >= 0 && sz < v.nz;
-        const long long src = in ? (sx + (long long)v.nx * (sy + (long long)v.ny * sz)) : 0;
-        for (int c0 = 0; c0 < cin; c0 += 16) {
-            uint4 a = make_uint4(0, 0, 0, 0);
-            if (in) a = *reinterpret_cast<const uint4 *>(X + src * cin + c0 + 8 * ah);
-            *reinterpret_cast<uint4 *>(As + ar * LDA + 8 * ah) = a;
-            for (int q = tid; q < 16 * COUT / 8; q += 128) {
-                const int k = q / (COUT / 8), n8 = q % (COUT / 8);
-                *reinterpret_cast<uint4 *>(Bs + k * LDB + 8 * n8) =
-                    *reinterpret_cast<const uint4 *>(W + ((long long)(t * cin + c0 + k)) * COUT + 8 * n8);
-            }
-            __syncthreads();
-            wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::row_major> fa;
-            wmma::load_matrix_sync(fa, As + warp * 16 * LDA, LDA);
-#pragma unroll
-            for (int j = 0; j < COUT / 16; ++j) {
-                wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> fb;
-                wmma::load_matrix_sync(fb, Bs + 16 * j, LDB);
-                wmma::mma_sync(acc[j], fa, fb, acc[j]);
-            }
-            __syncthreads();
+        const bool in = vox < nvox && sx >= 0 && sx < v.nx && sy >= 0 && sy < v.ny && sz >= 0 && sz < v.nz;
+        const uint4 *src = reinterpret_cast<const uint4 *>(X + (in ? (sx + (long long)v.nx * (sy + (long long)v.ny * sz)) : 0) * cin);
+        uint4 *arow = reinterpret_cast<uint4 *>(stg) + ((tid >> 3) * groups) * 8 + (tid & 7);
+        for (int g = 0; g < groups; ++g) arow[g * 8] = in ? __ldg(src + g) : make_uint4(0, 0, 0, 0);
+        const uint4 *pt = reinterpret_cast<const uint4 *>(P + (long long)t * cin * COUT);
+        uint4 *bt = reinterpret_cast<uint4 *>(stg + a_bytes);
+        for (int q = tid; q < (COUT * cin) >> 3; q += TC_M) bt[q] = __ldg(pt + q);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint32_t a0 = smem_u32(stg), b0 = a0 + (uint32_t)a_bytes;
+            for (int kc = 0; kc < (cin >> 4); ++kc)
+                tc_mma(tmem, tc_sdesc(a0 + 256u * kc, 128u, sbo), tc_sdesc(b0 + 256u * kc, 128u, sbo), idesc,
+                       (t > 0 || kc > 0) ? 1 : 0);
+            tc_commit(st ? bar1 : bar0);
         }
+        last = t;
     }
+    // every MMA committed so far is done once the last commit's phase is
+    if (last >= 0) {
+        const bool done = mbar_wait((last & 1) ? bar1 : bar0, (uint32_t)((last >> 1) & 1));
+        ok = ok && done;
+    }
+    ok = __syncthreads_and(ok);
+    if (ok) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
 #pragma unroll
-    for (int j = 0; j < COUT / 16; ++j)
-        wmma::store_matrix_sync(Cs + warp * 16 * LDC + 16 * j, acc[j], LDC, wmma::mem_row_major);
+        for (int c0 = 0; c0 < COUT; c0 += 16) {
+            float acc[16];
+            tc_ld16(lane_addr + (uint32_t)c0, acc);
+            if (vox < nvox) {
+                float z[16];
+#pragma unroll
+                for (int q = 0; q < 16; ++q) z[q] = acc[q] + (bias ? __ldg(bias + c0 + q) : 0.0f);
+                if (Z) {
+                    float4 *zr = reinterpret_cast<float4 *>(Z + vox * COUT + c0);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) zr[q] = make_float4(z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
+                }
+                if (Y) {
+                    __align__(16) bf16 yb[16];
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) yb[q] = __float2bfloat16_rn(act ? gelu(z[q]) : z[q]);
+                    uint4 *yr = reinterpret_cast<uint4 *>(Y + vox * COUT + c0);
+                    yr[0] = reinterpret_cast<const uint4 *>(yb)[0];
+                    yr[1] = reinterpret_cast<const uint4 *>(yb)[1];
+                }
+            }
+        }
+    } else if (tid == 0) {
+        atomicExch(err, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
-    for (int q = tid; q < MT * COUT; q += 128) {
-        const int r = q / COUT, c = q % COUT;
-        const long long vv = v0 + r;
-        if (vv >= nvox) continue;
-        float z = Cs[r * LDC + c] + (bias ? bias[c] : 0.0f);
-        if (Z) Z[vv * COUT + c] = z;
-        if (Y) Y[vv * COUT + c] = __float2bfloat16_rn(act ? gelu(z) : z);
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TCOLS));
     }
 }
 
@@ -410,18 +553,36 @@ int post(const char *what) {
     return FF_OK;
 }
 
+template <int COUT>
+int launch_conv_tc(Vol v, const bf16 *X, int cin, const bf16 *pk, const float *bias, int act, float *Z, bf16 *Y,
+                   int *err, cudaStream_t s) {
+    // two stages of (128 x cin A + COUT x cin B) BF16, 1 KB aligned, + alignment slack
+    const int stage = (TC_M * cin * 2 + COUT * cin * 2 + 1023) & ~1023;
+    const int smem = 2 * stage + 1024;
+    static int configured = 0;
+    if (smem > configured) {
+        FF_CUDA(cudaFuncSetAttribute(k_conv3_tc<COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        configured = smem;
+    }
+    const unsigned nb = (unsigned)((v.n() + TC_M - 1) / TC_M);
+    k_conv3_tc<COUT><<<nb, TC_M, smem, s>>>(v, X, cin, pk, bias, act, Z, Y, err);
+    return post("conv3 tcgen05");
+}
+
+// W: [27][cin][cout] BF16; pk: scratch for the packed copy (27 cin cout)
 int launch_conv(int cout, Vol v, const bf16 *X, int cin, const bf16 *W, const float *bias, int act, float *Z, bf16 *Y,
-                cudaStream_t s) {
-    const int nb = (int)((v.n() + MT - 1) / MT);
+                bf16 *pk, int *err, cudaStream_t s) {
+    if (cin % 16 || cin > 96) return ff_set_error(FF_E_ARG, "unet: conv input channels %d (multiples of 16 to 96)", cin);
+    k_pack_b<<<gblocks(27LL * cin * cout), 256, 0, s>>>(cin, cout, W, pk);
+    FF_TRY(post("pack weights"));
     switch (cout) {
-    case 16: k_conv3<16><<<nb, 128, 0, s>>>(v, X, cin, W, bias, act, Z, Y); break;
-    case 32: k_conv3<32><<<nb, 128, 0, s>>>(v, X, cin, W, bias, act, Z, Y); break;
-    case 48: k_conv3<48><<<nb, 128, 0, s>>>(v, X, cin, W, bias, act, Z, Y); break;
-    case 64: k_conv3<64><<<nb, 128, 0, s>>>(v, X, cin, W, bias, act, Z, Y); break;
-    case 96: k_conv3<96><<<nb, 128, 0, s>>>(v, X, cin, W, bias, act, Z, Y); break;
+    case 16: return launch_conv_tc<16>(v, X, cin, pk, bias, act, Z, Y, err, s);
+    case 32: return launch_conv_tc<32>(v, X, cin, pk, bias, act, Z, Y, err, s);
+    case 48: return launch_conv_tc<48>(v, X, cin, pk, bias, act, Z, Y, err, s);
+    case 64: return launch_conv_tc<64>(v, X, cin, pk, bias, act, Z, Y, err, s);
+    case 96: return launch_conv_tc<96>(v, X, cin, pk, bias, act, Z, Y, err, s);
     default: return ff_set_error(FF_E_ARG, "unet: no conv kernel for %d output channels", cout);
     }
-    return post("conv3");
 }
 
 int launch_wgrad(int cin, int cout, Vol v, const bf16 *X, const bf16 *G, float *dW, cudaStream_t s) {
@@ -461,6 +622,8 @@ struct ff_unet_s {
     float *w = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;   // master params, grads, Adam moments
     bf16 *wb = nullptr;             // BF16 weights (per conv, padded cin)
     bf16 *wt = nullptr;             // flipped/transposed BF16 weights (largest layer)
+    bf16 *wpk = nullptr;            // one layer's weights packed for the tcgen05 B operand
+    int *tc_err = nullptr;          // set by a tcgen05 conv whose wait ran out
     float *g0 = nullptr;            // first layer's weight gradient over the padded 16 inputs
     std::vector<long long> wb_off;
     long long adam_t = 0;
@@ -564,6 +727,8 @@ extern "C" int ff_unet_create(ff_ctx ctx, uint32_t seed, ff_unet *out) {
         (st = ff_dev_alloc((void **)&u->m, off * 4, s)) || (st = ff_dev_alloc((void **)&u->v, off * 4, s)) ||
         (st = ff_dev_alloc((void **)&u->wb, woff * sizeof(bf16), s)) ||
         (st = ff_dev_alloc((void **)&u->wt, 27LL * 96 * 64 * sizeof(bf16), s)) ||
+        (st = ff_dev_alloc((void **)&u->wpk, 27LL * 96 * 64 * sizeof(bf16), s)) ||
+        (st = ff_dev_alloc((void **)&u->tc_err, sizeof(int), s)) ||
         (st = ff_dev_alloc((void **)&u->g0, 27LL * 16 * 16 * sizeof(float), s)))
         return bail(st);
     // He-normal weights (std sqrt(2 / fan_in)), zero biases; head 0.1 / sqrt(16)
@@ -589,6 +754,8 @@ extern "C" int ff_unet_destroy(ff_unet u) {
     ff_dev_free(u->v);
     ff_dev_free(u->wb);
     ff_dev_free(u->wt);
+    ff_dev_free(u->wpk);
+    ff_dev_free(u->tc_err);
     ff_dev_free(u->g0);
     delete u;
     return FF_OK;
@@ -675,7 +842,7 @@ static int forward(ff_unet u, const float *b, const uint8_t *mask, const float *
         const ConvLayer &c = u->convs[l];
         const int si = CONV_IN[l], so = CONV_OUT[l];
         return launch_conv(c.cout, level_vol(u, SLOT_LEVEL[so]), u->act[si], c.cin, u->wb + u->wb_off[l],
-                           u->w + c.b_off, c.act, u->pre[l], u->act[so], s);
+                           u->w + c.b_off, c.act, u->pre[l], u->act[so], u->wpk, u->tc_err, s);
     };
     FF_TRY(conv(0));
     FF_TRY(conv(1));
@@ -722,7 +889,7 @@ static int conv_backward(ff_unet u, int l, bool accumulate_input) {
     // through the pre-activation output of the conv kernel
     float *dst = u->grad[si];
     if (accumulate_input) return ff_set_error(FF_E_STATE, "unet: accumulate not supported");
-    FF_TRY(launch_conv(c.cin, v, u->gbuf, c.cout, u->wt, nullptr, 0, dst, nullptr, s));
+    FF_TRY(launch_conv(c.cin, v, u->gbuf, c.cout, u->wt, nullptr, 0, dst, nullptr, u->wpk, u->tc_err, s));
     return FF_OK;
 }
 
@@ -755,6 +922,19 @@ static int backward(ff_unet u) {
 
 static int field_ok(ff_field f, long long n, int dtype) { return f && f->count == n && f->dtype == dtype; }
 
+// a tcgen05 convolution whose bounded wait ran out leaves the error word
+// set: report it (once) after the stream drains
+static int tc_status(ff_unet u) {
+    int e = 0;
+    FF_CUDA(cudaMemcpyAsync(&e, u->tc_err, sizeof(int), cudaMemcpyDeviceToHost, u->ctx->stream));
+    FF_CUDA(cudaStreamSynchronize(u->ctx->stream));
+    if (e) {
+        FF_CUDA(cudaMemsetAsync(u->tc_err, 0, sizeof(int), u->ctx->stream));
+        return ff_set_error(FF_E_CUDA, "unet: a tensor-core convolution timed out waiting for its MMAs");
+    }
+    return FF_OK;
+}
+
 extern "C" int ff_unet_forward(ff_unet u, const int *res, double h, ff_field b, ff_field mask, ff_field p_prev,
                                ff_field out) {
     FF_CHECK(u && res, FF_E_ARG, "NULL argument");
@@ -764,8 +944,9 @@ extern "C" int ff_unet_forward(ff_unet u, const int *res, double h, ff_field b, 
     FF_CHECK(field_ok(b, n, FF_FLOAT) && field_ok(out, n, FF_FLOAT) && (!p_prev || field_ok(p_prev, n, FF_FLOAT)) &&
                  (!mask || field_ok(mask, n, FF_UINT8)),
              FF_E_ARG, "unet forward: fields must be cell fields of the resolution (mask uint8)");
-    return forward(u, (const float *)b->d, mask ? (const uint8_t *)mask->d : nullptr,
-                   p_prev ? (const float *)p_prev->d : nullptr, h, (float *)out->d);
+    FF_TRY(forward(u, (const float *)b->d, mask ? (const uint8_t *)mask->d : nullptr,
+                   p_prev ? (const float *)p_prev->d : nullptr, h, (float *)out->d));
+    return tc_status(u);
 }
 
 // forward + MSE loss against `target` + backward: leaves dL/dparams in the
@@ -793,7 +974,7 @@ extern "C" int ff_unet_loss_backward(ff_unet u, const int *res, double h, ff_fie
     double tot = 0;
     for (double x : hp) tot += x;
     if (loss) *loss = tot;
-    return FF_OK;
+    return tc_status(u);
 }
 
 extern "C" int ff_unet_adam_step(ff_unet u, double lr, double beta1, double beta2, double eps) {
