@@ -5,22 +5,20 @@
 //
 // Activations are stored channels-last (z, y, x, c) in BF16; convolutions
 // are implicit GEMMs (M = voxels, K = 27 taps x Cin, N = Cout) with BF16
-// operands and FP32 accumulation, on tcgen05 (accumulators in TMEM) for the
-// forward and input-gradient convolutions and on WMMA for the weight
-// gradients; pre-activations
+// operands and FP32 accumulation on tcgen05 (accumulators in TMEM):
+// forward, input-gradient and weight-gradient convolutions; pre-activations
 // are kept in FP32 for the backward pass; master weights, gradients and the
 // Adam moments are FP32, with a BF16 copy of the weights for the GEMMs.
 // The input-gradient convolution reuses the forward kernel with the taps
 // flipped and the weight matrix transposed; weight gradients accumulate
 // per-tap [Cin x Cout] tiles over voxel chunks with FP32 atomics.
 #include "ff_internal.h"
-#include <mma.h>
+#include <cuda_bf16.h>
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
 
-using namespace nvcuda;
 typedef __nv_bfloat16 bf16;
 
 namespace {
@@ -79,10 +77,11 @@ __device__ __forceinline__ uint64_t tc_sdesc(uint32_t addr, uint32_t lbo, uint32
     return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo & 0x3FFFFu) >> 4) << 16) |
            ((uint64_t)((sbo & 0x3FFFFu) >> 4) << 32) | (1ull << 46);
 }
-// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
-// K-major, N >> 3 at bit 17, M >> 4 at bit 24
-__host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, K-major
+// (or, mn_major, both MN-major: bits 15 and 16), N >> 3 at bit 17, M >> 4 at bit 24
+__host__ __device__ constexpr uint32_t tc_idesc(int m, int n, bool mn_major = false) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | (mn_major ? (3u << 15) : 0u) | ((uint32_t)(n >> 3) << 17) |
+           ((uint32_t)(m >> 4) << 24);
 }
 __device__ __forceinline__ void mbar_init(uint32_t bar, unsigned count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
@@ -254,72 +253,155 @@ __global__ void __launch_bounds__(128) k_conv3_tc(Vol v, const bf16 *__restrict_
     }
 }
 
-// weight gradient: dW[t, ci, co] += sum_v X[v + off(t), ci] G[v, co] over a
-// chunk of 256 voxels; block = (chunk, tap)
-template <int CIN, int COUT>
-__global__ void __launch_bounds__(128) k_conv3_wgrad(Vol v, const bf16 *__restrict__ X, const bf16 *__restrict__ G,
-                                                    float *__restrict__ dW) {
-    constexpr int LDX = CIN + 8, LDG = COUT + 8, NT = (CIN / 16) * (COUT / 16), PER = (NT + 3) / 4;
-    __shared__ __align__(32) bf16 Xs[16 * LDX];
-    __shared__ __align__(32) bf16 Gs[16 * LDG];
-    __shared__ __align__(32) float Cs[4][16 * 16];
+// weight gradient on tcgen05: dW[t, ci, co] += sum_v X[v + off(t), ci] G[v, co]
+// over a chunk of WG_VC voxels; block = (chunk, tap).  The GEMM runs
+// transposed, D[co][ci] = sum_v G[v][co] X[v + off(t)][ci]: M = Cout padded
+// to 128 (columns past Cout stay zero), N = Cin, K = the chunk's voxels in
+// stages of 64.  Both operands are MN-major in the canonical no-swizzle
+// layout: a core matrix is 8 K-rows (voxels) of 16 bytes (8 consecutive
+// channels), i.e. channels-last rows copied as they are; core matrices 128
+// bytes apart along K (LBO) and 1 KB apart along M / N (SBO).  The
+// accumulators are added to dW with FP32 atomics (order-dependent in the
+// last bits).
+constexpr int WG_KC = 64, WG_VC = 1024, WG_MAXQ = 10;   // rows per thread: 64 (Cin + Cout) / 8 / 128
+
+__global__ void __launch_bounds__(128) k_conv3_wgrad_tc(Vol v, const bf16 *__restrict__ X, int cin,
+                                                       const bf16 *__restrict__ G, int cout, float *__restrict__ dW,
+                                                       int *__restrict__ err) {
+    extern __shared__ unsigned char tc_smem[];
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ uint32_t tmem_slot;
+    const int tcols = cin <= 32 ? 32 : (cin <= 64 ? 64 : 128);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int a_bytes = TC_M * WG_KC * 2, b_bytes = cin * WG_KC * 2;
+    const int stage_bytes = (a_bytes + b_bytes + 1023) & ~1023;
+    const uint32_t raw = smem_u32(tc_smem);
+    unsigned char *stages = tc_smem + (((raw + 1023u) & ~1023u) - raw);
+    const uint32_t bar0 = smem_u32(&bars[0]), bar1 = smem_u32(&bars[1]);
+    // A rows at or past Cout are never written below: zero both stages' A once
+    for (int q = tid; q < a_bytes / 16; q += TC_M) {
+        reinterpret_cast<uint4 *>(stages)[q] = make_uint4(0, 0, 0, 0);
+        reinterpret_cast<uint4 *>(stages + stage_bytes)[q] = make_uint4(0, 0, 0, 0);
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(tcols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+    }
+    if (tid == 0) {
+        mbar_init(bar0, 1);
+        mbar_init(bar1, 1);
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_slot;
     const int t = blockIdx.y;
     int dx, dy, dz;
     tap_offset(t, dx, dy, dz);
     const long long nvox = v.n();
-    wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc[PER];
+    const long long vbeg = (long long)blockIdx.x * WG_VC;
+    const int nst = (int)std::min<long long>(WG_VC / WG_KC, (nvox - vbeg + WG_KC - 1) / WG_KC);
+    const uint32_t idesc = tc_idesc(TC_M, cin, true);
+    constexpr uint32_t SBO = (WG_KC / 8) * 128;   // 8-channel groups along M or N
+    const int gco = cout >> 3, gci = cin >> 3;
+    // a stage is 64 (Cout / 8) A rows then 64 (Cin / 8) B rows of 16 bytes;
+    // thread tid moves rows tid + 128 j (the A/B boundary is a multiple of
+    // 128, so row j is A or B for the whole block).  The next stage's rows
+    // are loaded into registers while the current stage's MMAs run.
+    const int na = WG_KC * gco, nrows = WG_KC * (gco + gci), nq = nrows / TC_M;
+    uint4 pre[WG_MAXQ];
+    auto fetch = [&](int sidx) {
+        const long long k0 = vbeg + (long long)sidx * WG_KC;
 #pragma unroll
-    for (int p = 0; p < PER; ++p) wmma::fill_fragment(acc[p], 0.0f);
-    const long long vbeg = (long long)blockIdx.x * 256;
-    for (long long k0 = vbeg; k0 < vbeg + 256; k0 += 16) {
-        // stage 16 voxels of shifted X and of G
-        for (int q = tid; q < 16 * (CIN / 8); q += 128) {
-            const int r = q / (CIN / 8), c8 = q % (CIN / 8);
+        for (int j = 0; j < WG_MAXQ; ++j) {
+            if (j >= nq) break;
+            const int q = tid + TC_M * j;
+            const bool isa = q < na;
+            const int qq = isa ? q : q - na;
+            const int r = qq % WG_KC, cg = qq / WG_KC;
             const long long vv = k0 + r;
             uint4 val = make_uint4(0, 0, 0, 0);
             if (vv < nvox) {
-                const int x = (int)(vv % v.nx), y = (int)((vv / v.nx) % v.ny), z = (int)(vv / ((long long)v.nx * v.ny));
-                const int sx = x + dx, sy = y + dy, sz = z + dz;
-                if (sx >= 0 && sx < v.nx && sy >= 0 && sy < v.ny && sz >= 0 && sz < v.nz)
-                    val = *reinterpret_cast<const uint4 *>(X + (sx + (long long)v.nx * (sy + (long long)v.ny * sz)) * CIN + 8 * c8);
+                if (isa) {
+                    val = __ldg(reinterpret_cast<const uint4 *>(G + vv * cout) + cg);
+                } else {
+                    const int x = (int)(vv % v.nx), y = (int)((vv / v.nx) % v.ny),
+                              z = (int)(vv / ((long long)v.nx * v.ny));
+                    const int sx = x + dx, sy = y + dy, sz = z + dz;
+                    if (sx >= 0 && sx < v.nx && sy >= 0 && sy < v.ny && sz >= 0 && sz < v.nz)
+                        val = __ldg(reinterpret_cast<const uint4 *>(
+                                        X + (sx + (long long)v.nx * (sy + (long long)v.ny * sz)) * cin) + cg);
+                }
             }
-            *reinterpret_cast<uint4 *>(Xs + r * LDX + 8 * c8) = val;
+            pre[j] = val;
         }
-        for (int q = tid; q < 16 * (COUT / 8); q += 128) {
-            const int r = q / (COUT / 8), c8 = q % (COUT / 8);
-            const long long vv = k0 + r;
-            uint4 val = make_uint4(0, 0, 0, 0);
-            if (vv < nvox) val = *reinterpret_cast<const uint4 *>(G + vv * COUT + 8 * c8);
-            *reinterpret_cast<uint4 *>(Gs + r * LDG + 8 * c8) = val;
-        }
-        __syncthreads();
+    };
+    // row (cg, r) of A or B: one 16-byte row of core matrix (cg, r / 8)
+    auto put = [&](unsigned char *stg) {
+        uint4 *A = reinterpret_cast<uint4 *>(stg), *B = reinterpret_cast<uint4 *>(stg + a_bytes);
 #pragma unroll
-        for (int p = 0; p < PER; ++p) {
-            const int tile = warp + 4 * p;
-            if (tile < NT) {
-                const int ci = tile / (COUT / 16), co = tile % (COUT / 16);
-                wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::col_major> fa;   // X^T: [ci x v]
-                wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> fb;   // G: [v x co]
-                wmma::load_matrix_sync(fa, Xs + 16 * ci, LDX);
-                wmma::load_matrix_sync(fb, Gs + 16 * co, LDG);
-                wmma::mma_sync(acc[p], fa, fb, acc[p]);
-            }
+        for (int j = 0; j < WG_MAXQ; ++j) {
+            if (j >= nq) break;
+            const int q = tid + TC_M * j;
+            const bool isa = q < na;
+            const int qq = isa ? q : q - na;
+            const int r = qq % WG_KC, cg = qq / WG_KC;
+            (isa ? A : B)[(cg * (WG_KC / 8) + (r >> 3)) * 8 + (r & 7)] = pre[j];
         }
+    };
+    bool ok = true;
+    int last = -1;
+    fetch(0);
+    for (int sidx = 0; sidx < nst; ++sidx) {
+        const int st = sidx & 1;
+        unsigned char *stg = stages + st * stage_bytes;
+        // the stage's previous MMAs (stage sidx - 2) must be done before it is overwritten
+        if (sidx >= 2) ok = mbar_wait(st ? bar1 : bar0, (uint32_t)(((sidx >> 1) - 1) & 1));
+        if (!__syncthreads_and(ok)) {
+            ok = false;
+            break;
+        }
+        put(stg);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint32_t a0 = smem_u32(stg), b0 = a0 + (uint32_t)a_bytes;
+#pragma unroll
+            for (int kc = 0; kc < WG_KC / 16; ++kc)
+                tc_mma(tmem, tc_sdesc(a0 + 256u * kc, 128u, SBO), tc_sdesc(b0 + 256u * kc, 128u, SBO), idesc,
+                       (sidx > 0 || kc > 0) ? 1 : 0);
+            tc_commit(st ? bar1 : bar0);
+        }
+        last = sidx;
+        if (sidx + 1 < nst) fetch(sidx + 1);
     }
+    if (last >= 0) {
+        const bool done = mbar_wait((last & 1) ? bar1 : bar0, (uint32_t)((last >> 1) & 1));
+        ok = ok && done;
+    }
+    ok = __syncthreads_and(ok);
+    if (ok && last >= 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const int co = warp * 32 + lane;
+        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+        for (int c0 = 0; c0 < cin; c0 += 16) {
+            float acc[16];
+            tc_ld16(lane_addr + (uint32_t)c0, acc);
+            if (co < cout) {
 #pragma unroll
-    for (int p = 0; p < PER; ++p) {
-        const int tile = warp + 4 * p;
-        if (tile >= NT) continue;
-        const int ci = tile / (COUT / 16), co = tile % (COUT / 16);
-        wmma::store_matrix_sync(Cs[warp], acc[p], 16, wmma::mem_row_major);
-        __syncwarp();
-        for (int e = lane; e < 256; e += 32) {
-            const int r = e / 16, c = e % 16;
-            atomicAdd(dW + ((long long)t * CIN + 16 * ci + r) * COUT + 16 * co + c, Cs[warp][e]);
+                for (int q = 0; q < 16; ++q) atomicAdd(dW + ((long long)t * cin + c0 + q) * cout + co, acc[q]);
+            }
         }
-        __syncwarp();
+    } else if (!ok && tid == 0) {
+        atomicExch(err, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tcols));
     }
 }
 
@@ -585,13 +667,20 @@ int launch_conv(int cout, Vol v, const bf16 *X, int cin, const bf16 *W, const fl
     }
 }
 
-int launch_wgrad(int cin, int cout, Vol v, const bf16 *X, const bf16 *G, float *dW, cudaStream_t s) {
-    dim3 grid((unsigned)((v.n() + 255) / 256), 27);
-#define WG(A, B) \
-    if (cin == A && cout == B) { k_conv3_wgrad<A, B><<<grid, 128, 0, s>>>(v, X, G, dW); return post("conv3 wgrad"); }
-    WG(16, 16) WG(16, 32) WG(32, 32) WG(32, 64) WG(64, 64) WG(96, 32) WG(48, 16)
-#undef WG
-    return ff_set_error(FF_E_ARG, "unet: no weight-gradient kernel for %d -> %d", cin, cout);
+int launch_wgrad(int cin, int cout, Vol v, const bf16 *X, const bf16 *G, float *dW, int *err, cudaStream_t s) {
+    if (cin % 16 || cin > 96 || cout % 16 || cout > TC_M || WG_KC * (cin + cout) / 8 > TC_M * WG_MAXQ)
+        return ff_set_error(FF_E_ARG, "unet: no weight-gradient kernel for %d -> %d", cin, cout);
+    // two stages of (128 x 64 A + cin x 64 B) BF16, 1 KB aligned, + alignment slack
+    const int stage = (TC_M * WG_KC * 2 + cin * WG_KC * 2 + 1023) & ~1023;
+    const int smem = 2 * stage + 1024;
+    static int configured = 0;
+    if (smem > configured) {
+        FF_CUDA(cudaFuncSetAttribute(k_conv3_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        configured = smem;
+    }
+    dim3 grid((unsigned)((v.n() + WG_VC - 1) / WG_VC), 27);
+    k_conv3_wgrad_tc<<<grid, TC_M, smem, s>>>(v, X, cin, G, cout, dW, err);
+    return post("conv3 wgrad tcgen05");
 }
 
 // deterministic Gaussian initialisation: mulberry32 + Box-Muller
@@ -873,11 +962,11 @@ static int conv_backward(ff_unet u, int l, bool accumulate_input) {
     k_act_grad<<<gblocks(nout), 256, 0, s>>>(nout, u->grad[so], u->pre[l], c.act, u->gbuf);
     FF_TRY(post("act grad"));
     if (c.cin == c.cin_real) {
-        FF_TRY(launch_wgrad(c.cin, c.cout, v, u->act[si], u->gbuf, u->g + c.w_off, s));
+        FF_TRY(launch_wgrad(c.cin, c.cout, v, u->act[si], u->gbuf, u->g + c.w_off, u->tc_err, s));
     } else {
         // padded input channels: accumulate over all 16, keep the real ones
         FF_CUDA(cudaMemsetAsync(u->g0, 0, 27LL * c.cin * c.cout * 4, s));
-        FF_TRY(launch_wgrad(c.cin, c.cout, v, u->act[si], u->gbuf, u->g0, s));
+        FF_TRY(launch_wgrad(c.cin, c.cout, v, u->act[si], u->gbuf, u->g0, u->tc_err, s));
         k_gather_rows<<<gblocks(27LL * c.cin_real * c.cout), 256, 0, s>>>(c.cin_real, c.cin, c.cout, u->g0,
                                                                           u->g + c.w_off);
     }
