@@ -47,21 +47,19 @@ __device__ __forceinline__ void tap_offset(int t, int &dx, int &dy, int &dz) {
 // 3x3x3 convolution, zero padding 1: Y[v, co] = act(sum_{t, ci} X[v + off(t),
 // ci] W[t, ci, co] + bias[co]), X with Cin channels (a multiple of 16, at
 // most 96), writing the FP32 pre-activation Z and/or the BF16 output Y.
-// An implicit GEMM on the 5th-generation tensor cores: one CTA owns
-// 128 voxels (M = 128, one TMEM lane per voxel) and all Cout columns
-// (N = Cout, FP32 accumulators in TMEM); K runs over the 27 taps, one tap
-// (K = Cin) per stage.  Both operands sit in shared memory in the canonical
-// no-swizzle K-major layout: 8-row x 16-byte core matrices, core matrices
-// adjacent along K 128 bytes apart (LBO) and 8-row groups Cin / 8 x 128
-// bytes apart (SBO).  The A tile (128 voxel rows of the tap's shifted
-// input, zeros outside the volume) is gathered by the 128 threads, one row
-// each; the B tile (the tap's Cout x Cin weights) is a contiguous copy of
-// weights packed in that layout beforehand.  One elected thread issues the
-// MMAs and commits them to the stage's mbarrier; two stages alternate, so
-// the gather of tap t+1 overlaps the MMAs of tap t.  Waits are bounded
-// (0.5 s of globaltimer), after which the CTA flags the error, frees its
-// TMEM and returns.
+// An implicit GEMM on the 5th-generation tensor cores: one CTA owns 128
+// output voxels (M = 128, one TMEM lane each) and all Cout columns (N =
+// Cout, FP32 accumulators in TMEM); K runs over the 27 taps x Cin.  The
+// operands sit in shared memory in the canonical no-swizzle K-major layout
+// (8-row x 16-byte core matrices): the input halo of the CTA's tile staged
+// once (k_conv3_tch), and the weights, packed beforehand by k_pack_b, in
+// stages of several taps.  One elected thread issues the MMAs and commits
+// them to the stage's mbarrier; two weight stages alternate.  Waits are
+// bounded (0.5 s of globaltimer), after which the CTA flags the error,
+// frees its TMEM and returns.
 constexpr int TC_M = 128;
+// stride between 8-row groups of the packed weights (Cin / 8 core matrices each)
+__device__ __forceinline__ uint32_t sbo_b(int cin) { return (uint32_t)(cin >> 3) * 128u; }
 
 __device__ __forceinline__ unsigned long long tc_timer() {
     unsigned long long t;
@@ -138,20 +136,35 @@ __global__ void k_pack_b(int cin, int cout, const bf16 *__restrict__ W, bf16 *__
     }
 }
 
+// The convolution over tiles of 8 x 16 x 1 output voxels (row m of
+// the tile: x0 + m % 8, y0 + m / 8): the input halo of the tile (x0-1 ..
+// x0+8, y0-1 .. y0+16, z0-1 .. z0+1, zero outside the volume) is staged
+// once, as lines of 10 voxels x 16 bytes per (z, y, channel group), so that
+// each tap's A operand is a view of it: the tap's first core matrix at line
+// (z0+dz, y0+dy, group 0) + (dx + 1) x 16 bytes, core matrices 160 bytes
+// apart along K (the next channel group) and Cin / 8 x 160 bytes apart
+// along M (the next row of the tile).  Per tap only the weights move.
+constexpr int HX = 10, HY = 18, HZ = 3, HLINE = HX * 16;
+
+// rtap: taps whose weights one stage holds (27, 9, 3 or 1; the host picks
+// the largest that fits shared memory beside the halo)
 template <int COUT>
-__global__ void __launch_bounds__(128) k_conv3_tc(Vol v, const bf16 *__restrict__ X, int cin,
-                                                 const bf16 *__restrict__ P, const float *__restrict__ bias, int act,
-                                                 float *__restrict__ Z, bf16 *__restrict__ Y, int *__restrict__ err) {
-    constexpr int TCOLS = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : 128);   // TMEM columns (a power of 2, >= 32)
+__global__ void __launch_bounds__(128) k_conv3_tch(Vol v, const bf16 *__restrict__ X, int cin,
+                                                  const bf16 *__restrict__ P, const float *__restrict__ bias, int act,
+                                                  float *__restrict__ Z, bf16 *__restrict__ Y, int rtap,
+                                                  int *__restrict__ err) {
+    constexpr int TCOLS = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : 128);
     extern __shared__ unsigned char tc_smem[];
     __shared__ __align__(8) uint64_t bars[2];
     __shared__ uint32_t tmem_slot;
     const int tid = threadIdx.x, warp = tid >> 5;
-    const int a_bytes = TC_M * cin * 2, b_bytes = COUT * cin * 2;
-    const int stage_bytes = (a_bytes + b_bytes + 1023) & ~1023;
-    // stages start on a 1024-byte boundary of the shared window
+    const int groups = cin >> 3;
+    const int halo_bytes = HZ * HY * groups * HLINE;
+    const int b_bytes = COUT * cin * 2;   // one tap's packed weights
+    const int b_stage = (rtap * b_bytes + 1023) & ~1023;
     const uint32_t raw = smem_u32(tc_smem);
-    unsigned char *stages = tc_smem + (((raw + 1023u) & ~1023u) - raw);
+    unsigned char *halo = tc_smem + (((raw + 1023u) & ~1023u) - raw);
+    unsigned char *bst = halo + ((halo_bytes + 1023) & ~1023);
     const uint32_t bar0 = smem_u32(&bars[0]), bar1 = smem_u32(&bars[1]);
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
@@ -163,54 +176,59 @@ __global__ void __launch_bounds__(128) k_conv3_tc(Vol v, const bf16 *__restrict_
         mbar_init(bar0, 1);
         mbar_init(bar1, 1);
     }
+    const int tiles_x = (v.nx + 7) >> 3, tiles_y = (v.ny + 15) >> 4;
+    const int bx = blockIdx.x % tiles_x, by = (blockIdx.x / tiles_x) % tiles_y;
+    const int x0 = 8 * bx, y0 = 16 * by, z0 = blockIdx.x / (tiles_x * tiles_y);
+    // the halo: 540 positions x Cin / 8 groups, consecutive threads on
+    // consecutive groups of a voxel
+    for (int q = tid; q < HZ * HY * HX * groups; q += TC_M) {
+        const int g = q % groups, pos = q / groups;
+        const int xc = pos % HX, yr = (pos / HX) % HY, zp = pos / (HX * HY);
+        const int sx = x0 - 1 + xc, sy = y0 - 1 + yr, sz = z0 - 1 + zp;
+        uint4 val = make_uint4(0, 0, 0, 0);
+        if (sx >= 0 && sx < v.nx && sy >= 0 && sy < v.ny && sz >= 0 && sz < v.nz)
+            val = __ldg(reinterpret_cast<const uint4 *>(X + (sx + (long long)v.nx * (sy + (long long)v.ny * sz)) * cin) + g);
+        *reinterpret_cast<uint4 *>(halo + ((zp * HY + yr) * groups + g) * HLINE + xc * 16) = val;
+    }
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_slot;
-    const long long nvox = v.n();
-    const long long vox = (long long)blockIdx.x * TC_M + tid;
-    int ax = 0, ay = 0, az = 0;
-    if (vox < nvox) {
-        ax = (int)(vox % v.nx);
-        ay = (int)((vox / v.nx) % v.ny);
-        az = (int)(vox / ((long long)v.nx * v.ny));
-    }
     const uint32_t idesc = tc_idesc(TC_M, COUT);
-    const uint32_t sbo = (uint32_t)(cin >> 3) * 128u;
-    const int groups = cin >> 3;
+    const uint32_t hbase = smem_u32(halo), sbo = (uint32_t)groups * HLINE;
+    const uint32_t nb16 = (uint32_t)(rtap * b_bytes) >> 4;   // 16-byte rows of a stage
+    const int rounds = 27 / rtap;
     bool ok = true;
-    int last = -1;   // the last tap whose MMAs were committed
-    for (int t = 0; t < 27; ++t) {
-        const int st = t & 1;
-        unsigned char *stg = stages + st * stage_bytes;
-        // the stage's previous MMAs (tap t - 2) must be done before it is overwritten
-        if (t >= 2) ok = mbar_wait(st ? bar1 : bar0, (uint32_t)(((t >> 1) - 1) & 1));
+    int last = -1;
+    for (int rr = 0; rr < rounds; ++rr) {
+        const int st = rr & 1;
+        unsigned char *bt = bst + st * b_stage;
+        // the stage's previous MMAs (round rr - 2) must be done before it is overwritten
+        if (rr >= 2) ok = mbar_wait(st ? bar1 : bar0, (uint32_t)(((rr >> 1) - 1) & 1));
         if (!__syncthreads_and(ok)) {
             ok = false;
             break;
         }
-        int dx, dy, dz;
-        tap_offset(t, dx, dy, dz);
-        const int sx = ax + dx, sy = ay + dy, sz = az + dz;
-        const bool in = vox < nvox && sx >= 0 && sx < v.nx && sy >= 0 && sy < v.ny && sz >= 0 && sz < v.nz;
-        const uint4 *src = reinterpret_cast<const uint4 *>(X + (in ? (sx + (long long)v.nx * (sy + (long long)v.ny * sz)) : 0) * cin);
-        uint4 *arow = reinterpret_cast<uint4 *>(stg) + ((tid >> 3) * groups) * 8 + (tid & 7);
-        for (int g = 0; g < groups; ++g) arow[g * 8] = in ? __ldg(src + g) : make_uint4(0, 0, 0, 0);
-        const uint4 *pt = reinterpret_cast<const uint4 *>(P + (long long)t * cin * COUT);
-        uint4 *bt = reinterpret_cast<uint4 *>(stg + a_bytes);
-        for (int q = tid; q < (COUT * cin) >> 3; q += TC_M) bt[q] = __ldg(pt + q);
+        // taps rr rtap .. rr rtap + rtap - 1 are contiguous in the packed weights
+        const uint4 *pt = reinterpret_cast<const uint4 *>(P + (long long)rr * rtap * cin * COUT);
+        for (uint32_t q = tid; q < nb16; q += TC_M) reinterpret_cast<uint4 *>(bt)[q] = __ldg(pt + q);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;");
-            const uint32_t a0 = smem_u32(stg), b0 = a0 + (uint32_t)a_bytes;
-            for (int kc = 0; kc < (cin >> 4); ++kc)
-                tc_mma(tmem, tc_sdesc(a0 + 256u * kc, 128u, sbo), tc_sdesc(b0 + 256u * kc, 128u, sbo), idesc,
-                       (t > 0 || kc > 0) ? 1 : 0);
+            for (int u = 0; u < rtap; ++u) {
+                const int t = rr * rtap + u;
+                int dx, dy, dz;
+                tap_offset(t, dx, dy, dz);
+                const uint32_t a0 = hbase + (uint32_t)(((dz + 1) * HY + (dy + 1)) * groups * HLINE + (dx + 1) * 16);
+                const uint32_t b0 = smem_u32(bt) + (uint32_t)(u * b_bytes);
+                for (int kc = 0; kc < (cin >> 4); ++kc)
+                    tc_mma(tmem, tc_sdesc(a0 + 2u * HLINE * kc, HLINE, sbo),
+                           tc_sdesc(b0 + 256u * kc, 128u, sbo_b(cin)), idesc, (t > 0 || kc > 0) ? 1 : 0);
+            }
             tc_commit(st ? bar1 : bar0);
         }
-        last = t;
+        last = rr;
     }
-    // every MMA committed so far is done once the last commit's phase is
     if (last >= 0) {
         const bool done = mbar_wait((last & 1) ? bar1 : bar0, (uint32_t)((last >> 1) & 1));
         ok = ok && done;
@@ -219,11 +237,14 @@ __global__ void __launch_bounds__(128) k_conv3_tc(Vol v, const bf16 *__restrict_
     if (ok) {
         asm volatile("tcgen05.fence::after_thread_sync;");
         const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+        const int x = x0 + (tid & 7), y = y0 + (tid >> 3);
+        const bool in = x < v.nx && y < v.ny;
+        const long long vox = x + (long long)v.nx * (y + (long long)v.ny * z0);
 #pragma unroll
         for (int c0 = 0; c0 < COUT; c0 += 16) {
             float acc[16];
             tc_ld16(lane_addr + (uint32_t)c0, acc);
-            if (vox < nvox) {
+            if (in) {
                 float z[16];
 #pragma unroll
                 for (int q = 0; q < 16; ++q) z[q] = acc[q] + (bias ? __ldg(bias + c0 + q) : 0.0f);
@@ -636,19 +657,26 @@ int post(const char *what) {
 }
 
 template <int COUT>
-int launch_conv_tc(Vol v, const bf16 *X, int cin, const bf16 *pk, const float *bias, int act, float *Z, bf16 *Y,
-                   int *err, cudaStream_t s) {
-    // two stages of (128 x cin A + COUT x cin B) BF16, 1 KB aligned, + alignment slack
-    const int stage = (TC_M * cin * 2 + COUT * cin * 2 + 1023) & ~1023;
-    const int smem = 2 * stage + 1024;
+int launch_conv_tch(Vol v, const bf16 *X, int cin, const bf16 *pk, const float *bias, int act, float *Z, bf16 *Y,
+                    int *err, cudaStream_t s) {
+    // the halo (3 x 18 x cin / 8 lines of 160 bytes) and two weight stages
+    // of rtap taps, each 1 KB aligned, + alignment slack; rtap the largest
+    // of 27, 9, 3, 1 within 120 KB
+    const int halo = (HZ * HY * (cin / 8) * HLINE + 1023) & ~1023;
+    int rtap = 27, bstage = 0, smem = 0;
+    for (; rtap >= 1; rtap /= 3) {
+        bstage = (rtap * COUT * cin * 2 + 1023) & ~1023;
+        smem = halo + 2 * bstage + 1024;
+        if (smem <= 120 * 1024 || rtap == 1) break;
+    }
     static int configured = 0;
     if (smem > configured) {
-        FF_CUDA(cudaFuncSetAttribute(k_conv3_tc<COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        FF_CUDA(cudaFuncSetAttribute(k_conv3_tch<COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         configured = smem;
     }
-    const unsigned nb = (unsigned)((v.n() + TC_M - 1) / TC_M);
-    k_conv3_tc<COUT><<<nb, TC_M, smem, s>>>(v, X, cin, pk, bias, act, Z, Y, err);
-    return post("conv3 tcgen05");
+    const long long nb = (long long)((v.nx + 7) / 8) * ((v.ny + 15) / 16) * v.nz;
+    k_conv3_tch<COUT><<<(unsigned)nb, TC_M, smem, s>>>(v, X, cin, pk, bias, act, Z, Y, rtap, err);
+    return post("conv3 tcgen05 halo");
 }
 
 // W: [27][cin][cout] BF16; pk: scratch for the packed copy (27 cin cout)
@@ -658,11 +686,11 @@ int launch_conv(int cout, Vol v, const bf16 *X, int cin, const bf16 *W, const fl
     k_pack_b<<<gblocks(27LL * cin * cout), 256, 0, s>>>(cin, cout, W, pk);
     FF_TRY(post("pack weights"));
     switch (cout) {
-    case 16: return launch_conv_tc<16>(v, X, cin, pk, bias, act, Z, Y, err, s);
-    case 32: return launch_conv_tc<32>(v, X, cin, pk, bias, act, Z, Y, err, s);
-    case 48: return launch_conv_tc<48>(v, X, cin, pk, bias, act, Z, Y, err, s);
-    case 64: return launch_conv_tc<64>(v, X, cin, pk, bias, act, Z, Y, err, s);
-    case 96: return launch_conv_tc<96>(v, X, cin, pk, bias, act, Z, Y, err, s);
+    case 16: return launch_conv_tch<16>(v, X, cin, pk, bias, act, Z, Y, err, s);
+    case 32: return launch_conv_tch<32>(v, X, cin, pk, bias, act, Z, Y, err, s);
+    case 48: return launch_conv_tch<48>(v, X, cin, pk, bias, act, Z, Y, err, s);
+    case 64: return launch_conv_tch<64>(v, X, cin, pk, bias, act, Z, Y, err, s);
+    case 96: return launch_conv_tch<96>(v, X, cin, pk, bias, act, Z, Y, err, s);
     default: return ff_set_error(FF_E_ARG, "unet: no conv kernel for %d output channels", cout);
     }
 }
