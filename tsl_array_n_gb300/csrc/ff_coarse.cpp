@@ -10,69 +10,89 @@
 // marks a null direction; its D^+ entry is set to 0.  G = -L^-T D^+ L^-1 is a
 // symmetric generalised inverse (A G A = A), so the V-cycle stays symmetric.
 // G is formed explicitly so the device applies it as one dense FP64 matvec.
+// The matrix is banded (bandwidth nx ny in lexicographic order) and its
+// factor keeps that band, so the factorisation and the column solves run
+// over the band only.
 #include "ff_internal.h"
+#include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <thread>
 
 int ff_coarse_inverse(int nx, int ny, int nz, const float4 *coef, std::vector<double> &G) {
     const int n = nx * ny * nz;
     const long long sy = nx, sz = (long long)nx * ny;
-    std::vector<double> B((size_t)n * n, 0.0);
+    // lexicographic order: every coupling lies within `band` of the diagonal,
+    // and so does every nonzero of L (no fill outside the band)
+    const int band = nz > 1 ? (int)sz : (ny > 1 ? (int)sy : 1);
+    const int W = band + 1;   // Lb[r * W + d] = B[r][r - d] (d = 0: the diagonal), then L[r][r - d]
+    std::vector<double> Lb((size_t)n * W, 0.0);
+    auto at = [&](long long r, long long c) -> double & { return Lb[(size_t)r * W + (r - c)]; };
     for (int k = 0; k < nz; ++k)
         for (int j = 0; j < ny; ++j)
             for (int i = 0; i < nx; ++i) {
                 long long c = i + sy * (j + (long long)ny * k);
                 float4 kc = coef[c];
                 double diag = (double)kc.w + kc.x + kc.y + kc.z;
-                auto couple = [&](long long m, double K) {
-                    B[(size_t)c * n + m] -= K;   // B = -A, off-diagonal -K
-                };
-                if (i > 0) couple(c - 1, kc.x);
-                if (j > 0) couple(c - sy, kc.y);
-                if (k > 0) couple(c - sz, kc.z);
-                if (i < nx - 1) { double K = coef[c + 1].x; diag += K; couple(c + 1, K); }
-                if (j < ny - 1) { double K = coef[c + sy].y; diag += K; couple(c + sy, K); }
-                if (k < nz - 1) { double K = coef[c + sz].z; diag += K; couple(c + sz, K); }
-                B[(size_t)c * n + c] += diag;
+                // B = -A: off-diagonal -K (the lower couplings; B is symmetric)
+                if (i > 0) at(c, c - 1) -= kc.x;
+                if (j > 0) at(c, c - sy) -= kc.y;
+                if (k > 0) at(c, c - sz) -= kc.z;
+                if (i < nx - 1) diag += coef[c + 1].x;
+                if (j < ny - 1) diag += coef[c + sy].y;
+                if (k < nz - 1) diag += coef[c + sz].z;
+                at(c, c) += diag;
             }
     std::vector<double> orig(n), D(n);
-    for (int j = 0; j < n; ++j) orig[j] = B[(size_t)j * n + j];
-    // in-place L D L^T in the lower triangle (unit L below the diagonal)
+    for (int j = 0; j < n; ++j) orig[j] = at(j, j);
+    // in-place L D L^T (unit L below the diagonal) over the band; the terms
+    // outside it are exact zeros, so this equals the dense factorisation
     std::vector<double> tmp(n);
     for (int j = 0; j < n; ++j) {
-        double *rj = &B[(size_t)j * n];
-        for (int k = 0; k < j; ++k) tmp[k] = rj[k] * D[k];
-        double d = rj[j];
-        for (int k = 0; k < j; ++k) d -= rj[k] * tmp[k];
+        const int lo = std::max(0, j - band);
+        for (int k = lo; k < j; ++k) tmp[k] = at(j, k) * D[k];
+        double d = at(j, j);
+        for (int k = lo; k < j; ++k) d -= at(j, k) * tmp[k];
         bool zero = !(d > 1e-10 * std::fabs(orig[j])) || orig[j] == 0.0;
         D[j] = zero ? 0.0 : d;
-        for (int i = j + 1; i < n; ++i) {
-            double *ri = &B[(size_t)i * n];
-            if (zero) { ri[j] = 0.0; continue; }
-            double s = ri[j];
-            for (int k = 0; k < j; ++k) s -= ri[k] * tmp[k];
-            ri[j] = s / d;
+        const int hi = std::min(n - 1, j + band);
+        for (int i = j + 1; i <= hi; ++i) {
+            if (zero) { at(i, j) = 0.0; continue; }
+            double s = at(i, j);
+            for (int k = std::max(lo, i - band); k < j; ++k) s -= at(i, k) * tmp[k];
+            at(i, j) = s / d;
         }
     }
-    // G = -L^-T D^+ L^-1, column by column
+    // G = -L^-T D^+ L^-1, column by column (independent: spread over the
+    // host's cores), each solve within the band
     G.assign((size_t)n * n, 0.0);
-    std::vector<double> y(n);
-    for (int col = 0; col < n; ++col) {
-        std::fill(y.begin(), y.end(), 0.0);
-        y[col] = 1.0;
-        for (int i = col + 1; i < n; ++i) {   // forward: L y = e_col
-            const double *ri = &B[(size_t)i * n];
-            double s = 0.0;
-            for (int k = col; k < i; ++k) s += ri[k] * y[k];
-            y[i] = -s;
+    auto columns = [&](int c0, int c1) {
+        std::vector<double> y(n);
+        for (int col = c0; col < c1; ++col) {
+            std::fill(y.begin(), y.end(), 0.0);
+            y[col] = 1.0;
+            for (int i = col + 1; i < n; ++i) {   // forward: L y = e_col
+                double s = 0.0;
+                for (int k = std::max(col, i - band); k < i; ++k) s += at(i, k) * y[k];
+                y[i] = -s;
+            }
+            for (int i = 0; i < n; ++i) y[i] = D[i] > 0.0 ? y[i] / D[i] : 0.0;
+            for (int i = n - 1; i >= 0; --i) {   // backward: L^T x = y
+                double s = y[i];
+                const int kh = std::min(n - 1, i + band);
+                for (int k = i + 1; k <= kh; ++k) s -= at(k, i) * y[k];
+                y[i] = s;
+            }
+            for (int i = 0; i < n; ++i) G[(size_t)i * n + col] = -y[i];
         }
-        for (int i = 0; i < n; ++i) y[i] = D[i] > 0.0 ? y[i] / D[i] : 0.0;
-        for (int i = n - 1; i >= 0; --i) {   // backward: L^T x = y
-            double s = y[i];
-            for (int k = i + 1; k < n; ++k) s -= B[(size_t)k * n + i] * y[k];
-            y[i] = s;
-        }
-        for (int i = 0; i < n; ++i) G[(size_t)i * n + col] = -y[i];
+    };
+    const int nt = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    if (nt == 1 || n < 256) {
+        columns(0, n);
+    } else {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nt; ++t) pool.emplace_back(columns, (int)((long long)n * t / nt), (int)((long long)n * (t + 1) / nt));
+        for (std::thread &th : pool) th.join();
     }
     // exact symmetry in FP64 (the column solves agree with the rows to rounding)
     for (int i = 0; i < n; ++i)
