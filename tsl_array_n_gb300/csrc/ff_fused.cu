@@ -2206,6 +2206,11 @@ __global__ void __launch_bounds__(256) k_prolong4(Dims fd, Dims cd, int dims, co
 // row products, k_prolong4's correction.
 constexpr int TAIL_MAXL = 8;
 constexpr int TAIL_NT = 1024;
+// Levels up to this many cells run in one block (measured: a 64 x 64 level
+// gains, a 16^3 level, with its 64-tap restriction and 7-point colours,
+// loses against the grid barriers it saves).
+constexpr int TAIL_ONE_BLOCK_2D = 8192;
+constexpr int TAIL_ONE_BLOCK_3D = 512;
 struct TailLevel {
     Geo g;
     float *x, *b, *r;              // r: residual scratch of the level
@@ -2478,54 +2483,73 @@ __global__ void __launch_bounds__(TAIL_NT, 1) k_vcycle_tail(TailArgs a) {
     unsigned passed = 0;
     const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long stride = (long long)gridDim.x * blockDim.x;
+    // A phase over a level of at most one_block cells runs in block 0
+    // alone, with a block barrier after it; a phase over a larger level runs
+    // on every block with a grid barrier after it, and one more grid barrier
+    // first when block-0 phases precede it.  Every block takes the same
+    // sequence of grid barriers (the choice depends only on level sizes).
+    bool solo_prev = false;
+    const int one_block = a.dims == 3 ? TAIL_ONE_BLOCK_3D : TAIL_ONE_BLOCK_2D;
+    auto small = [&](int l) { return a.lv[l].g.d.n() <= one_block; };
+    auto phase = [&](bool solo, bool sync_after, auto &&work) -> bool {
+        if (solo) {
+            if (blockIdx.x == 0) {
+                work((long long)threadIdx.x, (long long)blockDim.x);
+                __syncthreads();
+            }
+            solo_prev = true;
+            return true;
+        }
+        if (solo_prev) {
+            solo_prev = false;
+            if (!tail_sync(bar, passed)) return false;
+        }
+        work(t0, stride);
+        return sync_after ? tail_sync(bar, passed) : true;
+    };
     bool ok = true;
     // the coarse level's first colour-0 pass rides on the restriction into it
     // (not into the coarsest level, which is solved directly or swept)
     for (int l = 0; l < a.nl - 1 && ok; ++l) {
         const TailLevel &L = a.lv[l];
-        const bool fused0 = l > 0 && a.down > 0;
+        const bool fused0 = l > 0 && a.down > 0, sl = small(l);
         for (int it = 0; it < a.down && ok; ++it) {
-            if (!(fused0 && it == 0)) {
-                tail_colour(a, L, 0, it == 0, t0, stride);
-                ok = tail_sync(bar, passed);
-                if (!ok) break;
-            }
-            tail_colour(a, L, 1, false, t0, stride);
-            ok = tail_sync(bar, passed);
+            if (!(fused0 && it == 0))
+                ok = phase(sl, true, [&](long long q0, long long qs) { tail_colour(a, L, 0, it == 0, q0, qs); });
+            if (ok) ok = phase(sl, true, [&](long long q0, long long qs) { tail_colour(a, L, 1, false, q0, qs); });
         }
         if (!ok) break;
-        tail_residual(L, a.down == 0, t0, stride);
-        ok = tail_sync(bar, passed);
+        ok = phase(sl, true, [&](long long q0, long long qs) { tail_residual(L, a.down == 0, q0, qs); });
         if (!ok) break;
-        tail_restrict(a, L, a.lv[l + 1], l + 1 < a.nl - 1 && a.down > 0, t0, stride);
-        ok = tail_sync(bar, passed);
+        // the restriction runs over the coarse level's cells
+        ok = phase(small(l + 1), true, [&](long long q0, long long qs) {
+            tail_restrict(a, L, a.lv[l + 1], l + 1 < a.nl - 1 && a.down > 0, q0, qs);
+        });
     }
     if (ok) {
         const TailLevel &C = a.lv[a.nl - 1];
         if (a.coarse_sweeps > 0) {
-            for (long long c = t0; c < C.g.d.n(); c += stride) C.x[c] = 0.f;
-            ok = tail_sync(bar, passed);
+            const bool sc = small(a.nl - 1);
+            ok = phase(sc, true, [&](long long q0, long long qs) {
+                for (long long c = q0; c < C.g.d.n(); c += qs) C.x[c] = 0.f;
+            });
             for (int it = 0; it < a.coarse_sweeps && ok; ++it)
-                for (int col = 0; col < 2 && ok; ++col) {
-                    tail_coarse_colour(a, C, col, t0, stride);
-                    ok = tail_sync(bar, passed);
-                }
+                for (int col = 0; col < 2 && ok; ++col)
+                    ok = phase(sc, true, [&](long long q0, long long qs) { tail_coarse_colour(a, C, col, q0, qs); });
         } else {
-            tail_direct(a, C);
-            ok = tail_sync(bar, passed);
+            // G b as one FP64 matvec over every block's warps
+            ok = phase(false, true, [&](long long, long long) { tail_direct(a, C); });
         }
     }
     for (int l = a.nl - 2; l >= 0 && ok; --l) {
         const TailLevel &L = a.lv[l];
-        tail_prolong(a, a.lv[l + 1], L, t0, stride);
-        ok = tail_sync(bar, passed);
+        const bool sl = small(l);
+        ok = phase(sl, true, [&](long long q0, long long qs) { tail_prolong(a, a.lv[l + 1], L, q0, qs); });
         for (int it = 0; it < a.up && ok; ++it) {
-            tail_colour(a, L, 1, false, t0, stride);
-            ok = tail_sync(bar, passed);
-            if (!ok) break;
-            tail_colour(a, L, 0, false, t0, stride);
+            ok = phase(sl, true, [&](long long q0, long long qs) { tail_colour(a, L, 1, false, q0, qs); });
             // the kernel's end orders the last pass before the next launch
-            if (!(l == 0 && it == a.up - 1)) ok = tail_sync(bar, passed);
+            if (ok) ok = phase(sl, !(l == 0 && it == a.up - 1),
+                               [&](long long q0, long long qs) { tail_colour(a, L, 0, false, q0, qs); });
         }
     }
     if (ok) tail_done(bar);
