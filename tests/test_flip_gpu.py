@@ -133,6 +133,17 @@ def test_dam_break_steps(gpu, oracle):
     assert p[:, 1].mean() < y0 - 1e-3
     vel = solver.velocities.to_array()
     assert np.all(np.isfinite(vel)) and np.abs(vel).max() <= 500
+    # the projection's own solver (pressureSolver): its pressure is the
+    # solver's, its Dirichlet cells are the air cells of the last step
+    from tsl_array_n_gb300 import tsl_array_n
+    ps = solver.pressure_solver
+    assert ps.level_shape(0) == SH
+    air = ps.dirichlet_mask.to_array() != 0
+    assert 0 < air.sum() < air.size
+    assert np.array_equal(solver.pressure.to_array(), ps.pressure.to_array())
+    y = tsl_array_n.Field("float", SH)
+    ps.apply_laplacian(solver.pressure, y)
+    assert np.all(np.isfinite(y.to_array()))
 
 
 @pytest.mark.parametrize("shape,n,mm", [(SH, 24000, (4, 8)), ((40, 36, 33), 160000, (3, 6))])

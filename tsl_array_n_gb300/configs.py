@@ -1,0 +1,209 @@
+"""Timings of the configurations besides the 256^3 sphere solve (which
+bench.py measures): one JSON line per configuration on cuda:0.
+
+    python -m tsl_array_n_gb300.configs [c1] [c2[:steps]] [c4] [c5[:steps]]
+
+- c1: 2D 128^2 cylinder, 4-level MGPCG to 1e-6 (double-single and plain
+  FP32 iterate): ms per solve, iterations, residual.
+- c2: 2D 1024 x 256 channel past a cylinder of radius 16 cells at x = 128
+  cells, u = 1 inflow, Re = U D / nu = 200, CFL 0.5, outflow column
+  Dirichlet p = 0: ms per step over 100 steps, then the run continued to
+  2000 steps with the transverse velocity sampled at four probes on the
+  cylinder's centre line (1, 2, 3.3 and 5 diameters behind it), from which
+  the Strouhal number follows by the crossing count of the reference's
+  karman_shedding.mjs:94-114 (opening 30% discarded, crossings of the mean
+  with a 0.25 sigma dead band, period = 2 span / crossings).
+- c4: the U-Net warm start's forward at 128^3 and 256^3 and its loss and
+  backward at 128^3.
+- c5: 3D FLIP dam break, 256 x 128 x 128, 2^3 particles per cell in a
+  liquid column of 40% of the domain, 500 steps: ms per step.
+
+All inputs are synthetic and seeded; every timing is taken with the device
+synchronised on both sides.
+"""
+import json
+import math
+import sys
+import time
+
+import numpy as np
+
+from . import fluxflow as ff, scenes, tsl_array_n
+from .tsl_array_n import Field
+
+
+def _now(ctx):
+    ctx.synchronize()
+    return time.perf_counter()
+
+
+def c1(ctx):
+    sc = scenes.cylinder_scene_2d()
+    n = 128
+    shape, h = sc["shape"], sc["h"]
+    cw = {"u": Field("float", (n + 1, n, 1)).from_array(sc["wu"]), "v": Field("float", (n, n + 1, 1)).from_array(sc["wv"]),
+          "w": Field("float", (n, n, 2)).from_array(np.ones(2 * n * n, np.float32))}
+    out = {"config": "C1 2D 128^2 cylinder, 4-level MGPCG, tolerance 1e-6"}
+    for prec in ("mixed", "fp32"):
+        s = ff.create_grid_pressure_solver2((n, n), h[:2], collider_weights=cw, dirichlet=(sc["active"], sc["target"]),
+                                            multigrid={"numberOfLevels": 4}, precision=prec, tolerance=1e-6)
+        grid = ff.FaceCenteredGrid3(shape, h).set(sc["u"], sc["v"], sc["w"])
+        o = ff.FaceCenteredGrid3(shape, h)
+        disp = s.project(grid, o)
+        for _ in range(3):
+            s.pressure.fill(0.0)
+            d = disp()
+        t0 = _now(ctx)
+        for _ in range(20):
+            s.pressure.fill(0.0)
+            d = disp()
+        out[prec] = {"ms_per_solve": round((_now(ctx) - t0) / 20 * 1e3, 3), "iterations": d["iterations"],
+                     "converged": d["converged"], "residual": d["residual"]}
+    return out
+
+
+def strouhal(series, every, dt, diameter, speed):
+    """The crossing-count estimate of karman_shedding.mjs:94-114 for one
+    probe's samples (one every `every` steps of length dt): None when the
+    signal crosses its mean fewer than twice."""
+    raw = np.asarray(series[int(math.floor(len(series) * 0.3)):], np.float64)
+    if raw.size < 20:
+        return None, 0
+    dev = raw - raw.mean()
+    std = float(np.sqrt(np.mean(dev * dev)))
+    crossings, last = 0, 0
+    for d in dev:
+        s = 1 if d > 0.25 * std else (-1 if d < -0.25 * std else 0)
+        if s != 0 and last != 0 and s != last:
+            crossings += 1
+        if s != 0:
+            last = s
+    if crossings < 2:
+        return None, crossings
+    period_steps = 2.0 * raw.size * every / crossings
+    return (diameter / speed) / (period_steps * dt), crossings
+
+
+def c2(ctx, steps=2000, timed=100, every=2):
+    nx, ny = 1024, 256
+    h = 1.0 / ny
+    # one cell layer with hz = h: the sphere below cuts it in a disc of
+    # radius 16 cells (the w faces are closed walls, so hz enters nothing else)
+    res, hh = (nx, ny, 1), (h, h, h)
+    radius, cx, cy = 16, 128, ny // 2
+    grid = ff.FaceCenteredGrid3(res, hh)
+    grid.set(np.ones(ny * (nx + 1), np.float32), np.zeros(nx * (ny + 1), np.float32), np.zeros(2 * nx * ny, np.float32))
+    col = ff.create_sdf_static_collider3(*res, *hh)
+    col.add_shapes([{"type": "sphere", "center": [cx * h, cy * h, 0.5 * h], "radius": radius * h}])
+    inflow = ff.create_sdf_inflow3(*res, *hh, velocity=(1.0, 0.0, 0.0), mode="set")
+    inflow.add_shapes([{"type": "box", "center": [0.0, 0.5, 0.5 * h], "halfExtents": [1.5 * h, 1.0, 1.0]}])
+    active = np.zeros((ny, nx), np.uint8)
+    active[:, nx - 1] = 1
+    dt, speed, diameter = 0.5 * h, 1.0, 2 * radius * h
+    solver = ff.create_grid_solver3(velocity_grid=grid, collider=col, inflows=[inflow], dt=dt, nu=speed * diameter / 200.0,
+                                    closed_domain_boundary_flag=ff.DIRECTION_DOWN | ff.DIRECTION_UP |
+                                    ff.DIRECTION_BACK | ff.DIRECTION_FRONT,
+                                    dirichlet=(active.ravel(), np.zeros(nx * ny, np.float32)),
+                                    pressure={"multigrid": {"numberOfLevels": 5}, "precision": "mixed", "tolerance": 1e-6})
+    for _ in range(5):
+        solver.on_advance_time_step()
+    its = []
+    t0 = _now(ctx)
+    for _ in range(timed):
+        its.append(solver.on_advance_time_step()["iterations"])
+    ms = (_now(ctx) - t0) / timed * 1e3
+    # v at the probes (cell columns radius * (2, 4, 6.6, 10) behind the centre)
+    probes = [cx + int(round(f * 2 * radius)) for f in (1.0, 2.0, 3.3, 5.0)]
+    series, sym_break = [], None
+    done = 5 + timed
+    for step in range(done, steps):
+        solver.on_advance_time_step()
+        if (step - done) % every == 0:
+            v = grid.data_v.to_array()
+            row = [float(v[i + nx * cy]) for i in probes]
+            series.append(row)
+            if sym_break is None and max(abs(x) for x in row) > 0.01 * speed:
+                sym_break = step + 1
+    st = []
+    for p in range(len(probes)):
+        s, crossings = strouhal([r[p] for r in series], every, dt, diameter, speed)
+        st.append({"probe_cells_behind": probes[p] - cx, "strouhal": None if s is None else round(s, 4),
+                   "crossings": crossings})
+    return {"config": "C2 2D 1024x256 channel past a cylinder r = 16 cells, Re 200, CFL 0.5",
+            "ms_per_step": round(ms, 3), "mean_iterations": float(np.mean(its)), "timed_steps": timed,
+            "steps": steps, "symmetry_break_step": sym_break, "probes": st}
+
+
+def c4(ctx):
+    from .warmstart import UNetWarmStart
+    out = {"config": "C4 U-Net warm start (3 levels, 16/32/64 channels)"}
+    for n in (128, 256):
+        shp = (n, n, n)
+        rng = np.random.default_rng(0)
+        b = Field("float", shp).from_array(rng.standard_normal(n ** 3).astype(np.float32))
+        m = Field("uint8", shp).from_array(np.zeros(n ** 3, np.uint8))
+        p = Field("float", shp).from_array(rng.standard_normal(n ** 3).astype(np.float32))
+        o = Field("float", shp)
+        net = UNetWarmStart(seed=1)
+        for _ in range(3):
+            net.forward(shp, 1.0 / n, b, m, p, o)
+        t0 = _now(ctx)
+        for _ in range(10):
+            net.forward(shp, 1.0 / n, b, m, p, o)
+        r = {"forward_ms": round((_now(ctx) - t0) / 10 * 1e3, 3)}
+        if n == 128:
+            t = Field("float", shp).from_array(rng.standard_normal(n ** 3).astype(np.float32))
+            for _ in range(2):
+                net.loss_backward(shp, 1.0 / n, b, m, p, t)
+            t0 = _now(ctx)
+            for _ in range(5):
+                net.loss_backward(shp, 1.0 / n, b, m, p, t)
+            r["loss_backward_ms"] = round((_now(ctx) - t0) / 5 * 1e3, 3)
+        out[f"{n}^3"] = r
+        del b, m, p, o, net
+    return out
+
+
+def c5(ctx, steps=500):
+    shp, hh = (256, 128, 128), (1.0 / 128,) * 3
+    grid = ff.FaceCenteredGrid3(shp, hh)
+    # the liquid column: 0.8 x 0.5 x 1 of the 2 x 1 x 1 domain (40%)
+    seed = ff.compute_flip_box_seed3((0.0, 0.0, 0.0), (1.6, 0.5, 1.0), *hh)
+    npart = seed["count"]
+    # the coarsest level (16 x 8 x 8) swept, as the reference does: its
+    # Dirichlet cells move every step, and a direct inverse would be
+    # refactored every step
+    s = ff.create_grid_flip_solver3(velocity_grid=grid, max_particles=npart, dt=0.002, flip_ratio=0.95,
+                                    pressure={"multigrid": {"numberOfLevels": 5, "coarseSolve": "sweeps"},
+                                              "tolerance": 1e-6, "precision": "mixed"})
+    s.positions.from_array(seed["positionsArray"])
+    s.velocities.from_array(np.zeros(3 * npart, np.float32))
+    for _ in range(3):
+        s.on_advance_time_step()
+    its, worst = [], 0.0
+    t0 = _now(ctx)
+    for _ in range(steps):
+        a = time.perf_counter()
+        its.append(s.on_advance_time_step()["iterations"])
+        worst = max(worst, time.perf_counter() - a)
+    ms = (_now(ctx) - t0) / steps * 1e3
+    return {"config": "C5 3D FLIP dam break 256x128x128, 8 particles per cell, column 40%", "particles": npart,
+            "steps": steps, "ms_per_step": round(ms, 3), "mean_iterations": float(np.mean(its)),
+            "max_iterations": int(max(its)), "slowest_step_host_ms": round(worst * 1e3, 3)}
+
+
+def main(argv):
+    """Arguments: configuration names, each optionally with a step count
+    (``c2:6000`` runs the channel 6000 steps, ``c5:200`` the dam break 200)."""
+    runs = []
+    for a in argv:
+        name, _, steps = a.partition(":")
+        if name in ("c1", "c2", "c4", "c5"):
+            runs.append((name, {"steps": int(steps)} if steps else {}))
+    ctx = tsl_array_n.init(0)
+    for name, kw in runs or [(n, {}) for n in ("c1", "c2", "c4", "c5")]:
+        print(json.dumps(globals()[name](ctx, **kw)), flush=True)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

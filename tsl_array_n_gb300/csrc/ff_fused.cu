@@ -2211,6 +2211,8 @@ constexpr int TAIL_NT = 1024;
 // loses against the grid barriers it saves).
 constexpr int TAIL_ONE_BLOCK_2D = 8192;
 constexpr int TAIL_ONE_BLOCK_3D = 512;
+// the coarsest level's sweeps (7-point colours, no restriction) in 2D and 3D
+constexpr int TAIL_ONE_BLOCK_COARSE = 8192;
 struct TailLevel {
     Geo g;
     float *x, *b, *r;              // r: residual scratch of the level
@@ -2529,7 +2531,7 @@ __global__ void __launch_bounds__(TAIL_NT, 1) k_vcycle_tail(TailArgs a) {
     if (ok) {
         const TailLevel &C = a.lv[a.nl - 1];
         if (a.coarse_sweeps > 0) {
-            const bool sc = small(a.nl - 1);
+            const bool sc = a.lv[a.nl - 1].g.d.n() <= TAIL_ONE_BLOCK_COARSE;
             ok = phase(sc, true, [&](long long q0, long long qs) {
                 for (long long c = q0; c < C.g.d.n(); c += qs) C.x[c] = 0.f;
             });

@@ -208,8 +208,17 @@ class GridPressureSolver3:
         h = C.c_void_p()
         _lib.check(lib.ff_pressure3_create(context().handle, C.byref(d), C.byref(h)))
         self.handle = h
+        self._bind(dirichlet)
+        if face_weights is not None:
+            self.set_face_weights(face_weights)
+        if collider_weights is not None:
+            self.set_collider_weights(collider_weights)
+        if dirichlet is not None:
+            self.update_dirichlet()
+
+    def _bind(self, dirichlet):
         p, b, m, v = C.c_void_p(), C.c_void_p(), C.c_void_p(), C.c_void_p()
-        _lib.check(lib.ff_pressure3_fields(h, C.byref(p), C.byref(b), C.byref(m), C.byref(v)))
+        _lib.check(_lib.load().ff_pressure3_fields(self.handle, C.byref(p), C.byref(b), C.byref(m), C.byref(v)))
         ctx = context()
         self.pressure = BorrowedField(p, ctx)
         self.b = BorrowedField(b, ctx)
@@ -219,12 +228,21 @@ class GridPressureSolver3:
                             "stoppedBy": None}
         self._keep = {}
         self._dirichlet = dirichlet
-        if face_weights is not None:
-            self.set_face_weights(face_weights)
-        if collider_weights is not None:
-            self.set_collider_weights(collider_weights)
-        if dirichlet is not None:
-            self.update_dirichlet()
+
+    @classmethod
+    def borrowed(cls, handle, owner, resolution, grid_spacing, origin=(0.0, 0.0, 0.0)):
+        """The pressure solver another solver owns (the FLIP solver's
+        ``pressureSolver``, grid_flip_solver3.js:1144-1155): the same
+        methods on its handle, which ``close`` leaves to the owner."""
+        self = cls.__new__(cls)
+        self.resolution = tuple(int(n) for n in resolution)
+        self.grid_spacing = tuple(float(h) for h in grid_spacing)
+        self.origin = tuple(float(o) for o in origin)
+        self.desc = None
+        self.handle = C.c_void_p(handle)
+        self._owner = owner
+        self._bind(None)
+        return self
 
     # -- inputs ------------------------------------------------------------
     def set_face_weights(self, fw):
@@ -341,6 +359,9 @@ class GridPressureSolver3:
         _lib.check(_lib.load().ff_mg_prolong_add(self.handle, fine_level, coarse.handle, fine.handle))
 
     def close(self):
+        if getattr(self, "_owner", None) is not None:
+            self.handle = None      # the owner destroys it
+            return
         if getattr(self, "handle", None):
             _lib.load().ff_pressure3_destroy(self.handle)
             self.handle = None
@@ -805,6 +826,8 @@ class GridFlipSolver3:
         self.velocities = BorrowedField(hs[1], ctx)
         self.concentration = BorrowedField(hs[2], ctx) if hs[2].value else None
         self.fluid_mask = BorrowedField(hs[3], ctx)
+        self.pressure_solver = GridPressureSolver3.borrowed(hs[4].value, self, g.resolution, g.grid_spacing, g.origin)
+        self.pressure = self.pressure_solver.pressure
         self.diagnostics = {}
 
     def grid_fields(self):
