@@ -16,7 +16,8 @@ bench.py measures): one JSON line per configuration on cuda:0.
 - c4: the U-Net warm start's forward at 128^3 and 256^3 and its loss and
   backward at 128^3.
 - c5: 3D FLIP dam break, 256 x 128 x 128, 2^3 particles per cell in a
-  liquid column of 40% of the domain, 500 steps: ms per step.
+  liquid column of 40% of the domain, 500 steps: ms per step; c5dump and
+  c5solve save one of its pressure systems and solve it standalone.
 
 All inputs are synthetic and seeded; every timing is taken with the device
 synchronised on both sides.
@@ -164,7 +165,7 @@ def c4(ctx):
     return out
 
 
-def c5(ctx, steps=500):
+def _dam_break():
     shp, hh = (256, 128, 128), (1.0 / 128,) * 3
     grid = ff.FaceCenteredGrid3(shp, hh)
     # the liquid column: 0.8 x 0.5 x 1 of the 2 x 1 x 1 domain (40%)
@@ -174,10 +175,18 @@ def c5(ctx, steps=500):
     # Dirichlet cells move every step, and a direct inverse would be
     # refactored every step
     s = ff.create_grid_flip_solver3(velocity_grid=grid, max_particles=npart, dt=0.002, flip_ratio=0.95,
-                                    pressure={"multigrid": {"numberOfLevels": 5, "coarseSolve": "sweeps"},
-                                              "tolerance": 1e-6, "precision": "mixed"})
+                                    pressure=dict(DAM_BREAK_PRESSURE))
     s.positions.from_array(seed["positionsArray"])
     s.velocities.from_array(np.zeros(3 * npart, np.float32))
+    return grid, s, npart
+
+
+DAM_BREAK_PRESSURE = {"multigrid": {"numberOfLevels": 5, "coarseSolve": "sweeps"}, "tolerance": 1e-6,
+                      "precision": "mixed"}
+
+
+def c5(ctx, steps=500):
+    grid, s, npart = _dam_break()
     for _ in range(3):
         s.on_advance_time_step()
     its, worst = [], 0.0
@@ -192,14 +201,59 @@ def c5(ctx, steps=500):
             "max_iterations": int(max(its)), "slowest_step_host_ms": round(worst * 1e3, 3)}
 
 
+def c5dump(ctx, steps, path):
+    """Run the dam break `steps` steps and save the last projection's
+    system (Dirichlet active/target cells and b) to `path` (.npz)."""
+    grid, s, npart = _dam_break()
+    for _ in range(steps):
+        d = s.on_advance_time_step()
+    gf = s.grid_fields()
+    np.savez(path, active=gf["dirichletActive"].to_array(), target=gf["dirichletTarget"].to_array(),
+             b=s.pressure_solver.b.to_array(), iterations=d["iterations"])
+    return {"config": f"C5 pressure system after {steps} steps", "path": path, "iterations": d["iterations"]}
+
+
+def c5solve(ctx, path, reps=1):
+    """Solve a saved dam-break system with a standalone solver of the same
+    options (CUDA graphs off, so a profiler sees each kernel) and report
+    the per-kernel times of ff_pressure3_profile."""
+    import ctypes as C
+    from . import _lib
+    z = np.load(path)
+    shp, hh = (256, 128, 128), (1.0 / 128,) * 3
+    opts = dict(DAM_BREAK_PRESSURE)
+    ps = ff.create_grid_pressure_solver3(shp, hh, dirichlet=(z["active"], z["target"]), multigrid=opts["multigrid"],
+                                         tolerance=opts["tolerance"], precision=opts["precision"])
+    ps.settings.useGraph = False
+    b = Field("float", shp).from_array(z["b"])
+    for _ in range(reps):
+        ps.pressure.fill(0.0)
+        d = ps.solve(b)
+    out = {"config": "C5 pressure system, standalone solve", "iterations": d["iterations"],
+           "converged": d["converged"], "air_fraction": round(float(np.mean(z["active"] != 0)), 4)}
+    for name, kid in (("p_pAp", 0), ("x_residual", 1), ("sweep", 2), ("residual_restrict", 3), ("prolong", 5),
+                      ("vcycle", 7)):
+        avg = C.c_float()
+        _lib.check(_lib.load().ff_pressure3_profile(ps.handle, kid, 5, C.byref(avg)))
+        out[name + "_ms"] = round(avg.value, 4)
+    return out
+
+
 def main(argv):
     """Arguments: configuration names, each optionally with a step count
-    (``c2:6000`` runs the channel 6000 steps, ``c5:200`` the dam break 200)."""
+    (``c2:6000`` runs the channel 6000 steps, ``c5:200`` the dam break 200);
+    ``c5dump:300:sys.npz`` saves the dam break's system after 300 steps and
+    ``c5solve:sys.npz`` solves and profiles it standalone."""
     runs = []
     for a in argv:
-        name, _, steps = a.partition(":")
+        name, _, rest = a.partition(":")
         if name in ("c1", "c2", "c4", "c5"):
-            runs.append((name, {"steps": int(steps)} if steps else {}))
+            runs.append((name, {"steps": int(rest)} if rest else {}))
+        elif name == "c5dump":
+            steps, _, path = rest.partition(":")
+            runs.append((name, {"steps": int(steps), "path": path}))
+        elif name == "c5solve":
+            runs.append((name, {"path": rest}))
     ctx = tsl_array_n.init(0)
     for name, kw in runs or [(n, {}) for n in ("c1", "c2", "c4", "c5")]:
         print(json.dumps(globals()[name](ctx, **kw)), flush=True)
