@@ -18,6 +18,7 @@ import datetime
 import json
 import os
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -78,7 +79,9 @@ class Clocks:
 
     def __init__(self):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks.csv")
+        # the raw samples: FF_CLOCKS_CSV if set, else a temporary file
+        self.path = os.environ.get("FF_CLOCKS_CSV") or os.path.join(tempfile.gettempdir(),
+                                                                     f"ff_clocks_{os.getpid()}.csv")
         self.t0 = self.t1 = None
 
     def start(self):

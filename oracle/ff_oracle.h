@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product library (libff.so) links,
  * loads or calls this code.  Only tests/, __graft_entry__.smoke() and the CPU
- * baseline arm of bench.py use it, and only as the checker.
+ * baseline arm of bench.py use it, and only to check or time against it.
  *
  * Every function restates one piece of the reference (bertJcW/tsl_array_n,
  * package fluxflow) and cites the file:line it follows.  Layout everywhere is

@@ -1,7 +1,7 @@
 """ctypes front end of the FP64 CPU oracle (test infrastructure only).
 
 Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline arm of bench.py
-import this module, and only as the checker.  The product library never
+import this module, and only to check or time against it.  The product library never
 loads it.  Arrays are numpy, i-fastest (Fortran order of (nx, ny, nz)),
 flattened: cell (i,j,k) -> i + nx*(j + ny*k).
 """

@@ -1,7 +1,7 @@
 """Regenerates the golden fixtures in this folder from the reference checkout.
 
-Run in a checkout that has the reference at REFERENCE (default
-/root/reference); the GPU machine never runs this.  Writes:
+Run where the reference sources are present, at REFERENCE (default
+/root/reference); the tests read only the committed fixtures.  Writes:
 
   stalled_frame110.npz, stalled_frame112.npz
       The frozen 48x24x24 pressure systems that the reference ships under
