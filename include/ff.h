@@ -192,10 +192,14 @@ int ff_collider3_bake(ff_ctx ctx, const ff_shape *shapes, int nshapes, int inver
  * synchronisation of cudaMalloc/cudaFree.  The shape table lives in one
  * fixed device array of FF_BAKE_NOALLOC_MAX_SHAPES entries per device; more
  * shapes return FF_E_LIMIT.  The first call on a device looks the array up
- * (make it before any stream capture).  The array is shared by every caller
- * on the device: calls that overlap in time (two contexts, two threads) race
- * on it and must be serialised.  Same arguments, outputs and errors as
- * ff_collider3_bake; the call returns without synchronising the stream.    */
+ * (make it before any stream capture).  The table reaches the device as a
+ * kernel parameter, so the call copies nothing from host memory and returns
+ * without waiting for its kernels.  The array is shared by every caller on
+ * the device, so calls must be ordered on the GPU: issue them on the same
+ * stream, or make the next caller wait for the previous call's stream (an
+ * event or a synchronize) first; unordered calls (two contexts' streams, two
+ * threads) race on it.  The caller's current device is restored on return.
+ * Same arguments, outputs and errors as ff_collider3_bake.                */
 #define FF_BAKE_NOALLOC_MAX_SHAPES 64
 int ff_collider3_bake_noalloc(ff_ctx ctx, const ff_shape *shapes, int nshapes, int invert,
                               const int *resolution, const double *grid_spacing, const double *origin,

@@ -1,7 +1,8 @@
 """Regenerates the golden fixtures in this folder from the reference checkout.
 
-Run where the reference sources are present, at REFERENCE (default
-/root/reference); the tests read only the committed fixtures.  Writes:
+Run where the reference sources are present, with the checkout's root as
+the one argument (`python make_golden.py <reference checkout>`); the tests
+read only the committed fixtures.  Writes:
 
   stalled_frame110.npz, stalled_frame112.npz
       The frozen 48x24x24 pressure systems that the reference ships under
@@ -15,13 +16,14 @@ import sys
 
 import numpy as np
 
-REFERENCE = os.environ.get("REFERENCE", "/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
 NAMES = ["b", "pressure", "dirichletMask", "ventMask", "weightU", "weightV", "weightW"]
 
 
 def main():
-    base = os.path.join(REFERENCE, "packages/fluxflow/sandbox/stalled-system/data")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python make_golden.py <reference checkout>")
+    base = os.path.join(sys.argv[1], "packages/fluxflow/sandbox/stalled-system/data")
     for frame in ("frame-110", "frame-112"):
         d = os.path.join(base, frame)
         meta = json.load(open(os.path.join(d, "meta.json")))

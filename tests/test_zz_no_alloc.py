@@ -1,8 +1,9 @@
 """ff_collider3_bake_noalloc through the C ABI: the fixed-table variant of
 the collider bake gives the same fields as ff_collider3_bake, on two
 different shape sets baked back to back (the second call must not see the
-first call's table), and rejects more shapes than its table holds.  Named
-to be collected last; it also passes on its own."""
+first call's table), leaves the device's free memory unchanged once warm,
+and rejects more shapes than its table holds.  Named to be collected last;
+it also passes on its own."""
 import ctypes as C
 
 import numpy as np
@@ -55,6 +56,39 @@ def test_noalloc_bake_inverted_and_empty(gpu):
         b = bake("ff_collider3_bake", shapes, res, h, inv)
         for x, y in zip(a, b):
             assert np.array_equal(x, y)
+
+
+def test_noalloc_bake_keeps_free_memory(gpu):
+    """After the first call (which looks the fixed array up), further calls
+    change the device's free memory by nothing: no allocation outlives the
+    call.  The output fields are created before the first reading."""
+    torch = pytest.importorskip("torch")
+    from tsl_array_n_gb300 import _lib
+    from tsl_array_n_gb300.fluxflow import SDFStaticCollider3
+    from tsl_array_n_gb300.tsl_array_n import Field, context
+    lib = _lib.load()
+    res, h = (48, 40, 36), (1 / 48, 1 / 40, 1 / 36)
+    nx, ny, nz = res
+    out = [Field("float", res), Field("float", (nx + 1, ny, nz)), Field("float", (nx, ny + 1, nz)),
+           Field("float", (nx, ny, nz + 1))]
+    arr = (_lib.Shape * len(SETS[1]))(*[SDFStaticCollider3._shape(s) for s in SETS[1]])
+
+    def call():
+        _lib.check(lib.ff_collider3_bake_noalloc(context().handle, arr, len(SETS[1]), 0, (C.c_int * 3)(*res),
+                                                 (C.c_double * 3)(*h), (C.c_double * 3)(0.0, 0.0, 0.0),
+                                                 *[f.handle for f in out]))
+
+    torch.cuda.mem_get_info(0)   # the reading's own set-up first
+    call()
+    context().synchronize()
+    free0 = torch.cuda.mem_get_info(0)[0]
+    for _ in range(3):
+        call()
+    context().synchronize()
+    assert torch.cuda.mem_get_info(0)[0] == free0
+    ref = bake("ff_collider3_bake", SETS[1], res, h)
+    for f, r in zip(out, ref):
+        assert np.array_equal(f.to_array(), r)
 
 
 def test_noalloc_bake_rejects_oversize(gpu):

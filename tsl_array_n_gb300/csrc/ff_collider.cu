@@ -7,6 +7,7 @@
 #include "ff_internal.h"
 #include <atomic>
 #include <cmath>
+#include <cstring>
 
 namespace {
 
@@ -151,61 +152,88 @@ __global__ void k_face_weights(const Shape *sh, int ns, double sign, int axis, i
 
 }  // namespace
 
+// Host records of the caller's shapes as the kernels read them
+// (primitive_sdf3.js:169-200); rejects unknown types.
+static int shape_records(const ff_shape *shapes, int nshapes, Shape *out) {
+    for (int q = 0; q < nshapes; ++q) {
+        const ff_shape &src = shapes[q];
+        FF_CHECK(src.type == FF_SHAPE_SPHERE || src.type == FF_SHAPE_BOX, FF_E_ARG,
+                 "primitive_sdf3: unknown shape type '%d'.", src.type);
+        Shape &dst = out[q];
+        dst.type = src.type == FF_SHAPE_SPHERE ? 0 : 1;
+        dst.has_rotation = src.has_rotation;
+        for (int c = 0; c < 3; ++c) {
+            dst.center[c] = src.center[c];
+            dst.half[c] = src.half_extents[c];
+        }
+        dst.radius = src.radius;
+        const double len = std::sqrt(src.rotation_axis[0] * src.rotation_axis[0] +
+                                     src.rotation_axis[1] * src.rotation_axis[1] +
+                                     src.rotation_axis[2] * src.rotation_axis[2]);
+        for (int c = 0; c < 3; ++c) dst.axis[c] = len > 0 ? src.rotation_axis[c] / len : (c == 2 ? 1.0 : 0.0);
+        dst.angle = src.rotation_angle;
+    }
+    return FF_OK;
+}
+
+// Output fields must be float fields of the cell / face sizes (any may be NULL).
+static int check_bake_fields(const int *res, ff_field phi, const ff_field ws[3]) {
+    const int nx = res[0], ny = res[1], nz = res[2];
+    FF_CHECK(!phi || (phi->count == (long long)nx * ny * nz && phi->dtype == FF_FLOAT), FF_E_ARG, "phi field shape");
+    for (int a = 0; a < 3; ++a)
+        FF_CHECK(!ws[a] || (ws[a]->count == (long long)(nx + (a == 0)) * (ny + (a == 1)) * (nz + (a == 2)) &&
+                            ws[a]->dtype == FF_FLOAT),
+                 FF_E_ARG, "face weight field %d shape", a);
+    return FF_OK;
+}
+
+// phi and the face weights from a device shape table, on stream s
+static void launch_bake(const Shape *table, int nshapes, int invert, const int *res, const double *h,
+                        const double *origin, ff_field phi, const ff_field ws[3], cudaStream_t s) {
+    const int nx = res[0], ny = res[1], nz = res[2];
+    const double sign = invert ? -1.0 : 1.0;
+    const dim3 blk(64, 4, 1);
+    if (phi) {
+        dim3 g((nx + 63) / 64, (ny + 3) / 4, nz);
+        k_bake_phi<<<g, blk, 0, s>>>(table, nshapes, sign, nx, ny, nz, origin[0], origin[1], origin[2], h[0], h[1],
+                                     h[2], (float *)phi->d);
+    }
+    for (int a = 0; a < 3; ++a) {
+        if (!ws[a]) continue;
+        const int fx = nx + (a == 0), fy = ny + (a == 1), fz = nz + (a == 2);
+        // dataOriginU/V/W (sdf_collider3.js:226-228)
+        const double o[3] = {origin[0] + (a != 0 ? 0.5 * h[0] : 0.0), origin[1] + (a != 1 ? 0.5 * h[1] : 0.0),
+                             origin[2] + (a != 2 ? 0.5 * h[2] : 0.0)};
+        dim3 g((fx + 63) / 64, (fy + 3) / 4, fz);
+        k_face_weights<<<g, blk, 0, s>>>(table, nshapes, sign, a, fx, fy, fz, o[0], o[1], o[2], h[0], h[1], h[2],
+                                         (float *)ws[a]->d);
+    }
+}
+
 extern "C" int ff_collider3_bake(ff_ctx ctx, const ff_shape *shapes, int nshapes, int invert,
                                  const int *res, const double *h, const double *origin,
                                  ff_field phi, ff_field wu, ff_field wv, ff_field ww) {
     FF_CHECK(ctx && res && h && origin, FF_E_ARG, "ff_collider3_bake: NULL argument");
     FF_CHECK(nshapes >= 0 && nshapes <= 64, FF_E_LIMIT, "ff_collider3_bake: at most 64 shapes");
     FF_CHECK(nshapes == 0 || shapes, FF_E_ARG, "ff_collider3_bake: shapes is NULL");
-    const int nx = res[0], ny = res[1], nz = res[2];
-    cudaStream_t s = ctx->stream;
+    const ff_field ws[3] = {wu, wv, ww};
+    FF_TRY(check_bake_fields(res, phi, ws));
     Shape hs[64];
-    for (int q = 0; q < nshapes; ++q) {
-        const ff_shape &a = shapes[q];
-        FF_CHECK(a.type == FF_SHAPE_SPHERE || a.type == FF_SHAPE_BOX, FF_E_ARG,
-                 "primitive_sdf3: unknown shape type '%d'.", a.type);
-        Shape &b = hs[q];
-        b.type = a.type == FF_SHAPE_SPHERE ? 0 : 1;
-        for (int c = 0; c < 3; ++c) { b.center[c] = a.center[c]; b.half[c] = a.half_extents[c]; }
-        b.radius = a.radius;
-        b.has_rotation = a.has_rotation;
-        double len = std::sqrt(a.rotation_axis[0] * a.rotation_axis[0] + a.rotation_axis[1] * a.rotation_axis[1] +
-                               a.rotation_axis[2] * a.rotation_axis[2]);
-        for (int c = 0; c < 3; ++c) b.axis[c] = len > 0 ? a.rotation_axis[c] / len : (c == 2 ? 1.0 : 0.0);
-        b.angle = a.rotation_angle;
-    }
+    FF_TRY(shape_records(shapes, nshapes, hs));
+    cudaStream_t s = ctx->stream;
     Shape *dsh = nullptr;
     FF_CUDA(cudaMalloc(&dsh, sizeof(Shape) * (nshapes > 0 ? nshapes : 1)));
-    if (nshapes) FF_CUDA(cudaMemcpyAsync(dsh, hs, sizeof(Shape) * nshapes, cudaMemcpyHostToDevice, s));
-    const double sign = invert ? -1.0 : 1.0;
-    auto launch = [&](int fx, int fy, int fz, auto &&fn) {
-        dim3 b(64, 4, 1), g((fx + 63) / 64, (fy + 3) / 4, fz);
-        fn(g, b);
-    };
-    if (phi) {
-        FF_CHECK(phi->count == (long long)nx * ny * nz && phi->dtype == FF_FLOAT, FF_E_ARG, "phi field shape");
-        launch(nx, ny, nz, [&](dim3 g, dim3 b) {
-            k_bake_phi<<<g, b, 0, s>>>(dsh, nshapes, sign, nx, ny, nz, origin[0], origin[1], origin[2], h[0], h[1], h[2],
-                                       (float *)phi->d);
-        });
+    cudaError_t e = cudaSuccess;
+    if (nshapes) e = cudaMemcpyAsync(dsh, hs, sizeof(Shape) * nshapes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        launch_bake(dsh, nshapes, invert, res, h, origin, phi, ws, s);
+        e = cudaGetLastError();
     }
-    ff_field ws[3] = {wu, wv, ww};
-    for (int a = 0; a < 3; ++a) {
-        if (!ws[a]) continue;
-        int fx = nx + (a == 0), fy = ny + (a == 1), fz = nz + (a == 2);
-        FF_CHECK(ws[a]->count == (long long)fx * fy * fz && ws[a]->dtype == FF_FLOAT, FF_E_ARG,
-                 "face weight field %d shape", a);
-        // dataOriginU/V/W (sdf_collider3.js:226-228)
-        double o[3] = {origin[0] + (a != 0 ? 0.5 * h[0] : 0.0), origin[1] + (a != 1 ? 0.5 * h[1] : 0.0),
-                       origin[2] + (a != 2 ? 0.5 * h[2] : 0.0)};
-        launch(fx, fy, fz, [&](dim3 g, dim3 b) {
-            k_face_weights<<<g, b, 0, s>>>(dsh, nshapes, sign, a, fx, fy, fz, o[0], o[1], o[2], h[0], h[1], h[2],
-                                           (float *)ws[a]->d);
-        });
-    }
-    FF_CUDA(cudaGetLastError());
-    FF_CUDA(cudaStreamSynchronize(s));
+    // the kernels read dsh: wait for them before freeing it
+    const cudaError_t es = cudaStreamSynchronize(s);
     cudaFree(dsh);
+    FF_CUDA(e);
+    FF_CUDA(es);
     return FF_OK;
 }
 
@@ -222,16 +250,31 @@ extern "C" int ff_collider3_bake(ff_ctx ctx, const ff_shape *shapes, int nshapes
 //
 // Setup: the first call on each device looks up the array's device address
 // (cudaGetSymbolAddress, which may load the module); make that first call
-// before any stream capture.  Later calls only copy the table and launch.
+// before any stream capture.  Later calls launch three kinds of kernels
+// only: the table travels to the device as a kernel parameter (no host copy,
+// no host buffer that has to outlive the call), k_store_shapes writes it into
+// g_bake_shapes, and the bake kernels read it from there, in stream order.
 //
 // Nothing in the table has to start at zero: the kernels read entries
 // 0..nshapes-1 only, and this call writes exactly those before its kernels
-// run (same stream).  There is one table per device, so calls that overlap
-// in time -- from two contexts' streams on the same device, or from two host
-// threads -- race on it; serialise them.
+// run.  There is one table per device and calls return before their kernels
+// finish, so two calls are safe only when they are ordered on the GPU: the
+// same stream, or the second caller waits for the first call's stream (an
+// event or a synchronize) before it calls.  Calls from two contexts' streams
+// or two host threads on one device without such an order race on it.
 namespace {
 constexpr int BAKE_NOALLOC_MAX_SHAPES = FF_BAKE_NOALLOC_MAX_SHAPES;
 static __device__ __align__(256) Shape g_bake_shapes[BAKE_NOALLOC_MAX_SHAPES];
+
+// the whole table as one kernel parameter (7 KB, below the 32 KB limit)
+struct ShapeTable {
+    Shape s[BAKE_NOALLOC_MAX_SHAPES];
+};
+
+__global__ void k_store_shapes(const __grid_constant__ ShapeTable t, int n, Shape *dst) {
+    const int q = threadIdx.x;
+    if (q < n) dst[q] = t.s[q];
+}
 
 constexpr int MAX_DEVICES = 64;
 std::atomic<void *> g_bake_table[MAX_DEVICES] = {};
@@ -251,6 +294,20 @@ int bake_table(int device, Shape **out) {
     *out = static_cast<Shape *>(p);
     return FF_OK;
 }
+
+// makes `device` current for the call and gives the caller's current device
+// back on every return path
+struct DeviceScope {
+    int prev = -1;
+    explicit DeviceScope(int device) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != device) cudaSetDevice(device);
+    }
+    ~DeviceScope() {
+        int now = -1;
+        if (prev >= 0 && cudaGetDevice(&now) == cudaSuccess && now != prev) cudaSetDevice(prev);
+    }
+};
 }  // namespace
 
 extern "C" int ff_collider3_bake_noalloc(ff_ctx ctx, const ff_shape *shapes, int nshapes, int invert,
@@ -261,56 +318,17 @@ extern "C" int ff_collider3_bake_noalloc(ff_ctx ctx, const ff_shape *shapes, int
              "ff_collider3_bake_noalloc: %d shapes exceed the fixed table of %d (use ff_collider3_bake)", nshapes,
              BAKE_NOALLOC_MAX_SHAPES);
     FF_CHECK(nshapes == 0 || shapes, FF_E_ARG, "ff_collider3_bake_noalloc: shapes is NULL");
-    const int nx = res[0], ny = res[1], nz = res[2];
-    FF_CHECK(!phi || (phi->count == (long long)nx * ny * nz && phi->dtype == FF_FLOAT), FF_E_ARG, "phi field shape");
-    ff_field ws[3] = {wu, wv, ww};
-    for (int a = 0; a < 3; ++a)
-        FF_CHECK(!ws[a] || (ws[a]->count == (long long)(nx + (a == 0)) * (ny + (a == 1)) * (nz + (a == 2)) &&
-                            ws[a]->dtype == FF_FLOAT),
-                 FF_E_ARG, "face weight field %d shape", a);
-    // shape records as the kernels read them (primitive_sdf3.js:169-200)
-    Shape hs[BAKE_NOALLOC_MAX_SHAPES];
-    for (int q = 0; q < nshapes; ++q) {
-        const ff_shape &src = shapes[q];
-        FF_CHECK(src.type == FF_SHAPE_SPHERE || src.type == FF_SHAPE_BOX, FF_E_ARG,
-                 "primitive_sdf3: unknown shape type '%d'.", src.type);
-        Shape &dst = hs[q];
-        dst.type = src.type == FF_SHAPE_SPHERE ? 0 : 1;
-        dst.has_rotation = src.has_rotation;
-        for (int c = 0; c < 3; ++c) {
-            dst.center[c] = src.center[c];
-            dst.half[c] = src.half_extents[c];
-        }
-        dst.radius = src.radius;
-        const double len = std::sqrt(src.rotation_axis[0] * src.rotation_axis[0] +
-                                     src.rotation_axis[1] * src.rotation_axis[1] +
-                                     src.rotation_axis[2] * src.rotation_axis[2]);
-        for (int c = 0; c < 3; ++c) dst.axis[c] = len > 0 ? src.rotation_axis[c] / len : (c == 2 ? 1.0 : 0.0);
-        dst.angle = src.rotation_angle;
-    }
-    FF_CUDA(cudaSetDevice(ctx->device));
+    const ff_field ws[3] = {wu, wv, ww};
+    FF_TRY(check_bake_fields(res, phi, ws));
+    ShapeTable t;
+    std::memset(&t, 0, sizeof t);
+    FF_TRY(shape_records(shapes, nshapes, t.s));
+    DeviceScope scope(ctx->device);
     Shape *table = nullptr;
     FF_TRY(bake_table(ctx->device, &table));
     cudaStream_t s = ctx->stream;
-    // pageable source: the copy has taken the bytes when it returns
-    if (nshapes) FF_CUDA(cudaMemcpyAsync(table, hs, sizeof(Shape) * nshapes, cudaMemcpyHostToDevice, s));
-    const double sign = invert ? -1.0 : 1.0;
-    const dim3 blk(64, 4, 1);
-    if (phi) {
-        dim3 g((nx + 63) / 64, (ny + 3) / 4, nz);
-        k_bake_phi<<<g, blk, 0, s>>>(table, nshapes, sign, nx, ny, nz, origin[0], origin[1], origin[2], h[0], h[1],
-                                     h[2], (float *)phi->d);
-    }
-    for (int a = 0; a < 3; ++a) {
-        if (!ws[a]) continue;
-        const int fx = nx + (a == 0), fy = ny + (a == 1), fz = nz + (a == 2);
-        // dataOriginU/V/W (sdf_collider3.js:226-228)
-        const double o[3] = {origin[0] + (a != 0 ? 0.5 * h[0] : 0.0), origin[1] + (a != 1 ? 0.5 * h[1] : 0.0),
-                             origin[2] + (a != 2 ? 0.5 * h[2] : 0.0)};
-        dim3 g((fx + 63) / 64, (fy + 3) / 4, fz);
-        k_face_weights<<<g, blk, 0, s>>>(table, nshapes, sign, a, fx, fy, fz, o[0], o[1], o[2], h[0], h[1], h[2],
-                                         (float *)ws[a]->d);
-    }
+    if (nshapes) k_store_shapes<<<1, BAKE_NOALLOC_MAX_SHAPES, 0, s>>>(t, nshapes, table);
+    launch_bake(table, nshapes, invert, res, h, origin, phi, ws, s);
     FF_CUDA(cudaGetLastError());
     return FF_OK;
 }

@@ -14,7 +14,7 @@ Names, option names, defaults and error behaviour follow the reference
                                   grid_blocked_boundary_condition_solver3.js:48-490
   apply_viscosity3                explicit viscosity (no reference counterpart)
   create_grid_solver3             grid_solver3.js:24-149 (forces, viscosity, projection, advection)
-  create_grid_flip_solver3        grid_flip_solver3.js:135-1157 (no resampling)
+  create_grid_flip_solver3        grid_flip_solver3.js:135-1157 (resampling on by default, :621-820)
   compute_flip_box_seed3          grid_flip_solver3.js:70-130
   create_jitter_random            jitter_random.js:29-46
 """
