@@ -9,9 +9,18 @@ memory and the device->host read of the corrected u, v, w, all through the
 C ABI.  The timed inputs (about 1.7 GB of fields) are larger than the 129 MB
 L2, so no flush is needed between steps.
 
+The line also carries `arms`: the same projection timed with plain FP32
+MGPCG (FP32 iterate and V-cycle), BF16 V-cycle storage, and the learned
+warm start (the network's forward pass and the residual test inside the
+timed region) on top of the mixed solve; `oracle_error`: the pressure and
+corrected velocity of the timed solve against the FP64 oracle's solution
+converged to 1e-10, and the divergence left; and `cpu_baseline`: one whole
+FP64 oracle projection of the same system to 1e-6, measured, with the
+oracle's own iteration count.
+
 --impl reference times the FP64 CPU restatement of the same path (the
 reference is JavaScript + WebGPU and cannot run on this machine) on the
-host cores, on a bounded sample of the same workload.
+host cores: every timed step is one whole projection to 1e-6.
 """
 import argparse
 import datetime
@@ -159,19 +168,97 @@ def max_over_ranks(dist, v):
 
 
 # ------------------------------------------------------------------ ours --
+WEIGHTS = os.path.join(ROOT, "tsl_array_n_gb300", "weights", "unet_warmstart.npy")
+
+
+def sphere_inputs(n):
+    from tsl_array_n_gb300 import scenes
+    return scenes.sphere_scene(n=n, radius_cells=24 * n // 256, modes=32, seed=1)
+
+
+def make_solver(ff, sc, cw, levels, precision, coarse="direct"):
+    return ff.create_grid_pressure_solver3(
+        sc["shape"], sc["h"], collider_weights=cw, dirichlet=(sc["active"], sc["target"]),
+        multigrid={"numberOfLevels": levels, "coarseSolve": coarse}, precision=precision, tolerance=1e-6)
+
+
+def timed(lib, ctx, fn, steps, slot=4):
+    """device ms per call of fn over `steps` calls (events on the context
+    stream), and the last call's result"""
+    import ctypes as C
+    from tsl_array_n_gb300 import _lib
+    ctx.synchronize()
+    _lib.check(lib.ff_ctx_event_record(ctx.handle, slot))
+    out = []
+    for _ in range(steps):
+        out.append(fn())
+    _lib.check(lib.ff_ctx_event_record(ctx.handle, slot + 1))
+    ms = C.c_float()
+    _lib.check(lib.ff_ctx_event_elapsed(ctx.handle, slot, slot + 1, C.byref(ms)))
+    ctx.synchronize()
+    return ms.value / steps, out
+
+
+def run_arm(ff, lib, ctx, sc, cw, grid, out, levels, arm, steps, warmup):
+    """One comparison arm on the same system: ms per cold-start projection,
+    iterations, convergence and residual.  'learned+mixed' runs the mixed
+    solve with the U-Net warm start attached, so the network's forward pass
+    and the residual comparison are inside the timed region."""
+    from tsl_array_n_gb300 import warmstart
+    precision = "mixed" if arm == "learned+mixed" else arm
+    solver = make_solver(ff, sc, cw, levels, precision)
+    net = None
+    info = {}
+    if arm == "learned+mixed":
+        net = warmstart.UNetWarmStart(seed=1)
+        if os.path.exists(WEIGHTS):
+            net.load(WEIGHTS)
+            info["network"] = "trained weights " + os.path.relpath(WEIGHTS, ROOT)
+        else:
+            info["network"] = "untrained (seeded initialisation)"
+        warmstart.attach(solver, net)
+    dispatch = solver.project(grid, out)
+
+    def step():
+        solver.pressure.fill(0.0)
+        return dict(dispatch())
+
+    for _ in range(warmup):
+        step()
+    ms, diags = timed(lib, ctx, step, steps)
+    d = diags[-1]
+    res = {"ms": round(ms, 4), "iterations": d["iterations"], "converged": all(x["converged"] for x in diags),
+           "residual_rel": d["residual"] / d["bNorm"], "stopped_by": d["stoppedBy"],
+           "max_iterations": d["maxIterations"], "steps": steps, **info}
+    if net is not None:
+        res["guess_used"] = sum(1 for x in diags if x["warmStart"] == 1) / len(diags)
+        # the forward pass alone, for the split of the arm's time
+        from tsl_array_n_gb300.tsl_array_n import Field
+        g = Field("float", sc["shape"])
+        h = sc["h"][0]
+        fms, _ = timed(lib, ctx, lambda: net.forward(sc["shape"], h, solver.b, solver.dirichlet_mask,
+                                                     solver.pressure, g), max(2, steps // 2))
+        res["forward_ms"] = round(fms, 4)
+        del g
+        warmstart.attach(solver, None)
+        net.close()
+    solver.close()
+    return res
+
+
 def run_gb300(args):
     rank, world, dist = dist_setup(args.gpus)
     device = int(os.environ.get("LOCAL_RANK", 0))
     from tsl_array_n_gb300 import build as B
     B.build()
     import ctypes as C
-    from tsl_array_n_gb300 import _lib, fluxflow as ff, scenes
+    from tsl_array_n_gb300 import _lib, fluxflow as ff
     from tsl_array_n_gb300.tsl_array_n import init
 
     ctx = init(device)
     lib = _lib.load()
     n = args.size
-    sc = scenes.sphere_scene(n=n, radius_cells=24 * n // 256, modes=32, seed=1)
+    sc = sphere_inputs(n)
     shape, h = sc["shape"], sc["h"]
     col = ff.create_sdf_static_collider3(*shape, *h)
     col.add_shapes(sc["shapes"])
@@ -182,10 +269,7 @@ def run_gb300(args):
     clocks = Clocks()   # sampling from here on: running well before the timed region
     if not args.profile_only:
         clocks.start()
-    solver = ff.create_grid_pressure_solver3(
-        shape, h, collider_weights=cw, dirichlet=(sc["active"], sc["target"]),
-        multigrid={"numberOfLevels": levels, "coarseSolve": args.coarse},
-        precision=args.precision, tolerance=1e-6)
+    solver = make_solver(ff, sc, cw, levels, args.precision, args.coarse)
     if args.eager:
         solver.settings.useGraph = False
     dispatch = solver.project(grid, out)
@@ -223,6 +307,9 @@ def run_gb300(args):
     clk = clocks.stop()
     barrier(dist)
     ms_step = max_over_ranks(dist, ms.value / args.steps)
+    # the timed solve's result, for the oracle comparison
+    p_gpu = solver.pressure.to_array().astype(np.float64)
+    u_gpu = [f.to_array() for f in (out.data_u, out.data_v, out.data_w)]
 
     # end-to-end through the C ABI with host buffers
     nb = [sc["u"].nbytes, sc["v"].nbytes, sc["w"].nbytes]
@@ -265,13 +352,27 @@ def run_gb300(args):
         lib.ff_host_free(p)
 
     roof = None if args.no_kernel_profile else kernel_roofline(lib, solver, args, n)
+    solver.close()
 
-    cpu = None
+    arms = {}
+    if args.arms != "none":
+        for arm in args.arms.split(","):
+            arms[arm] = run_arm(ff, lib, ctx, sc, cw, grid, out, levels, arm, args.arm_steps,
+                                min(args.warmup, 2))
+        arms[args.precision] = {"ms": round(ms_step, 4), "iterations": iters,
+                                "converged": all(x["converged"] for x in diags),
+                                "residual_rel": diags[-1]["residual"] / diags[-1]["bNorm"],
+                                "stopped_by": diags[-1]["stoppedBy"], "steps": args.steps}
+
+    cpu = err = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(sc, levels, iters, budget_s=args.cpu_budget)
+        wts = tuple(x.to_array().astype(np.float64) for x in (cw["u"], cw["v"], cw["w"]))
+        cpu, p_ref = cpu_baseline(sc, levels, wts)
+        err = oracle_error(sc, wts, p_gpu, u_gpu, p_ref)
 
     if rank == 0:
-        emit_line(args, world, ms_step, e2e_ms_step, nb, launches, roof, cpu, clk, diags, iters, levels, n)
+        emit_line(args, world, ms_step, e2e_ms_step, nb, launches, roof, cpu, clk, diags, iters, levels, n,
+                  arms, err)
     if dist is not None:
         dist.destroy_process_group()
 
@@ -315,48 +416,66 @@ def kernel_roofline(lib, solver, args, n):
     return roof
 
 
-def emit_line(args, world, ms_step, e2e_ms_step, nb, launches, roof, cpu, clk, diags, iters, levels, n):
+def emit_line(args, world, ms_step, e2e_ms_step, nb, launches, roof, cpu, clk, diags, iters, levels, n,
+              arms, err):
     cells = n ** 3
-    if True:
-        line = {
-            "metric": METRIC, "value": round(ms_step / 1.0, 4), "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
-            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": {"mixed": "f32(double-single iterate)+f64", "fp32": "f32+f64",
-                      "mixed-bf16": "f32+bf16+f64"}[args.precision],
-            "data": "synthetic (seeded 32-mode Fourier velocity, sphere collider)",
-            "config": {"workload": f"3D MGPCG pressure projection {n}^3, sphere r={24 * n // 256} cells, "
-                                   f"closed walls + one pinned cell, {levels} levels, coarsest {args.coarse}, "
-                                   f"precision {args.precision}, tol 1e-6 relative, cold start",
-                       "cells": cells, "iterations": iters,
-                       "converged": all(x["converged"] for x in diags),
-                       "residual_rel": diags[-1]["residual"] / diags[-1]["bNorm"],
-                       "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
-            "e2e": {"value": round(e2e_ms_step, 4), "unit": UNIT,
-                    "h2d_bytes_per_step": int(sum(nb)), "d2h_bytes_per_step": int(sum(nb))},
-            "gpu_launches": launches,
-            "roofline": roof,
-            "cpu_baseline": cpu,
-            "clocks": clk,
-        }
-        print(json.dumps(line))
+    line = {
+        "metric": METRIC, "value": round(ms_step, 4), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": {"mixed": "f32(double-single iterate)+f64", "fp32": "f32+f64",
+                  "mixed-bf16": "f32+bf16+f64"}[args.precision],
+        "data": "synthetic (seeded 32-mode Fourier velocity, sphere collider)",
+        "config": {"workload": f"3D MGPCG pressure projection {n}^3, sphere r={24 * n // 256} cells, "
+                               f"closed walls + one pinned cell, {levels} levels, coarsest {args.coarse}, "
+                               f"precision {args.precision}, tol 1e-6 relative, cold start",
+                   "cells": cells, "iterations": iters,
+                   "converged": all(x["converged"] for x in diags),
+                   "residual_rel": diags[-1]["residual"] / diags[-1]["bNorm"],
+                   "cell_updates_per_s": cells * iters / (ms_step * 1e-3),
+                   "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
+        "e2e": {"value": round(e2e_ms_step, 4), "unit": UNIT,
+                "h2d_bytes_per_step": int(sum(nb)), "d2h_bytes_per_step": int(sum(nb))},
+        "gpu_launches": launches,
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+    }
+    if arms:
+        line["arms"] = arms
+        plain = arms.get("fp32")
+        if plain:
+            vs = {k: round(plain["ms"] / v["ms"], 2) for k, v in arms.items() if k != "fp32"}
+            vs["note"] = ("plain FP32 MGPCG " + ("converged" if plain["converged"] else
+                          f"did not reach 1e-6 (stopped by {plain['stopped_by']} at {plain['iterations']} "
+                          f"iterations, residual {plain['residual_rel']:.2e})") +
+                          "; ratio = plain ms / arm ms")
+            line["vs_plain"] = vs
+    if err:
+        line["oracle_error"] = err
+    print(json.dumps(line))
 
 
 # --------------------------------------------------------- CPU baseline --
-def _oracle_inputs(sc):
-    """Collider face weights from the FP64 restatement (a static collider is
-    baked once, outside the per-solve work, as on the GPU side)."""
+def _oracle_inputs(sc, weights=None):
+    """Collider face weights: the GPU's baked weights when given (the oracle
+    then solves exactly the system the GPU solved), else the FP64
+    restatement's bake."""
     from oracle import oracle as O
+    O.lib()
+    if weights is not None:
+        return O, weights
     _, wu, wv, ww = O.collider_bake(sc["shapes"], sc["shape"], sc["h"])
     return O, tuple(x.astype(np.float64) for x in (wu, wv, ww))
 
 
-def _oracle_step(O, sc, w, levels, iters):
-    """One projection on the FP64 CPU restatement, timed by phase: Dirichlet
-    fields + build, hierarchy, PCG with `iters` iterations (chunked like the
-    GPU-resident loop), circuit-breaker count and velocity correction.  None
-    of libff is on this path."""
+def oracle_projection(O, sc, w, levels, tol=1e-6, max_iter=None):
+    """One whole projection on the FP64 CPU restatement, timed by phase:
+    Dirichlet fields + build, hierarchy, PCG to `tol` with the oracle's own
+    iteration count (cap ceil(1.5 max(res)), grid_pressure_solver3.js:133),
+    velocity correction.  None of libff is on this path."""
     shape, h = sc["shape"], sc["h"]
+    max_iter = max_iter or int(np.ceil(1.5 * max(shape)))
     t = {}
     t0 = time.perf_counter()
     mask, tgt, vent = O.dirichlet_fields(shape, sc["active"], sc["target"], w)
@@ -366,74 +485,95 @@ def _oracle_step(O, sc, w, levels, iters):
     mg = O.Multigrid(shape, h, mask, vent, w, levels=levels, coarse_direct=True)
     t["hierarchy"] = time.perf_counter() - t0
     t0 = time.perf_counter()
-    x, res, _ = O.pcg_solve(shape, h, b, None, mask, w, mg, "multigrid", tol=1e-6, max_iter=iters)
+    x, res, _ = O.pcg_solve(shape, h, b, None, mask, w, mg, "multigrid", tol=tol, max_iter=max_iter)
     t["pcg"] = time.perf_counter() - t0
     t0 = time.perf_counter()
     O.correct(shape, h, x, sc["u"], sc["v"], sc["w"], collider_weights=w)
     t["correct"] = time.perf_counter() - t0
-    return t, res
+    return t, res, (x, b, mask, mg)
 
 
-def cpu_baseline(sc, levels, gpu_iters, budget_s=30.0):
-    """FP64 CPU restatement on all host cores: one projection with 1 PCG
-    iteration and one with 3, the per-iteration cost taken from their
-    difference, extrapolated to the GPU's iteration count."""
-    O, w = _oracle_inputs(sc)
+def cpu_baseline(sc, levels, weights):
+    """The FP64 CPU restatement on all host cores: one whole projection of
+    the same system to 1e-6, measured; then the same PCG continued to 1e-10
+    for the reference pressure of the oracle comparison (not timed)."""
+    O, w = _oracle_inputs(sc, weights)
     cores = os.cpu_count()
-    t1, _ = _oracle_step(O, sc, w, levels, 1)
-    t3, _ = _oracle_step(O, sc, w, levels, 3)
-    per_iter = max((t3["pcg"] - t1["pcg"]) / 2.0, 1e-9)
-    fixed = t1["build"] + t1["hierarchy"] + max(t1["pcg"] - per_iter, 0.0) + t1["correct"]
-    est = (fixed + gpu_iters * per_iter) * 1e3
-    spent = sum(t1.values()) + sum(t3.values())
+    t, res, (x, b, mask, mg) = oracle_projection(O, sc, w, levels)
+    total = sum(t.values())
+    shape, h = sc["shape"], sc["h"]
+    x_ref, r2, _ = O.pcg_solve(shape, h, b, x, mask, w, mg, "multigrid", tol=1e-10, max_iter=200)
     n = sc["shape"][0]
-    return {"value": round(est, 1), "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"FP64 oracle projection of the same {n}^3 system (build, hierarchy, PCG, correct) "
-                      f"run with 1 and 3 PCG iterations ({spent:.1f} s), extrapolated to {gpu_iters} "
-                      f"iterations ({per_iter * 1e3:.0f} ms/iteration)"}
+    cpu = {"value": round(total * 1e3, 1), "unit": UNIT, "cores": cores, "kind": "port",
+           "iterations": res["iterations"], "converged": res["converged"],
+           "sample": f"measured: one whole FP64 oracle projection of the same {n}^3 system (Dirichlet fields, "
+                     f"build, hierarchy, PCG to 1e-6 in {res['iterations']} iterations, correction), "
+                     f"{total:.1f} s on {cores} cores (PCG {t['pcg']:.1f} s)"}
+    return cpu, (x_ref, b, mask, r2)
+
+
+def oracle_error(sc, w, p_gpu, u_gpu, ref):
+    """Pressure and corrected velocity of the timed GPU solve against the
+    oracle's solution converged to 1e-10, and the divergence the GPU's
+    velocity leaves on non-Dirichlet cells (relative to the input's)."""
+    from oracle import oracle as O
+    x_ref, b, mask, r2 = ref
+    shape, h = sc["shape"], sc["h"]
+
+    def rel(a, r):
+        return float(np.linalg.norm(np.asarray(a, np.float64) - r) / max(np.linalg.norm(r), 1e-300))
+
+    u_ref = O.correct(shape, h, x_ref, sc["u"], sc["v"], sc["w"], collider_weights=w)
+    b_after, _ = O.build_system(shape, h, *u_gpu, collider_weights=w, mask=mask,
+                                target=np.zeros(mask.size))
+    b_after[mask.astype(bool)] = 0.0
+    return {"pressure_rel_l2": rel(p_gpu, x_ref),
+            "velocity_rel_l2": max(rel(g, r) for g, r in zip(u_gpu, u_ref)),
+            "divergence_left_rel": float(np.linalg.norm(b_after) / np.linalg.norm(b)),
+            "oracle_residual_rel": r2["residual"] / np.sqrt(r2["bb"]),
+            "oracle": "FP64 CPU restatement on the GPU's face weights, PCG to 1e-10 relative"}
 
 
 def run_reference(args):
     """--impl reference: the CPU restatement of the path on the host cores
     (the reference is JavaScript + WebGPU and has no CPU implementation of
-    the 3D path that runs here), rank 0 only.  Each step is a bounded
-    sample: one projection of the full-size system with one PCG iteration,
-    extrapolated to the iteration count the full solve takes."""
+    the 3D path that runs here), rank 0 only.  Every timed step is one whole
+    projection of the full-size system to 1e-6 with the oracle's own
+    iteration count; one warm-up step whatever --warmup says (a CPU solve
+    has nothing to warm past the first)."""
     rank = int(os.environ.get("RANK", 0))
     if rank != 0:
         return
     from oracle import oracle as O
     O.build()
-    from tsl_array_n_gb300 import scenes
     n = args.size
-    sc = scenes.sphere_scene(n=n, radius_cells=24 * n // 256, modes=32, seed=1)
+    sc = sphere_inputs(n)
     levels = max(1, int(np.log2(n)) - 2)
     O, w = _oracle_inputs(sc)
-    # per-iteration cost from a 3-iteration run, measured once
-    t3, _ = _oracle_step(O, sc, w, levels, 3)
-    samples = []
-    for i in range(args.warmup + args.steps):
-        t1, _ = _oracle_step(O, sc, w, levels, 1)
-        if i >= args.warmup:
-            samples.append(t1)
-    per_iter = max((t3["pcg"] - float(np.median([t["pcg"] for t in samples]))) / 2.0, 1e-9)
-    fixed = float(np.median([t["build"] + t["hierarchy"] + t["correct"] + max(t["pcg"] - per_iter, 0.0)
-                             for t in samples]))
-    iters_needed = args.ref_iters
-    value = (fixed + iters_needed * per_iter) * 1e3
+    warm = min(args.warmup, 1)
+    samples, iters = [], []
+    t_run = time.perf_counter()
+    for i in range(warm + args.steps):
+        t, res, _ = oracle_projection(O, sc, w, levels)
+        if i >= warm:
+            samples.append(sum(t.values()))
+            iters.append(res["iterations"])
+    run_s = time.perf_counter() - t_run
+    value = float(np.mean(samples)) * 1e3
     cores = os.cpu_count()
     cpu = {"value": round(value, 1), "unit": UNIT, "cores": cores, "kind": "port",
-           "sample": f"FP64 CPU restatement (oracle/), {n}^3: each step one projection with 1 PCG "
-                     f"iteration, extrapolated to {iters_needed} iterations "
-                     f"({per_iter * 1e3:.0f} ms/iteration)"}
+           "sample": f"measured: FP64 CPU restatement (oracle/), {n}^3, every step one whole projection to 1e-6 "
+                     f"({iters[-1]} iterations), {args.steps} timed steps after {warm} warm-up, "
+                     f"{run_s:.0f} s in all"}
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value, 1),
+        "steps": args.steps, "warmup": warm, "ms_per_step": round(value, 1),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded 32-mode Fourier velocity, sphere collider)",
         "config": {"workload": f"3D MGPCG pressure projection {n}^3, sphere r={24 * n // 256} cells, "
                                f"closed walls + one pinned cell, {levels} levels, coarsest direct, "
-                               f"tol 1e-6 relative (CPU FP64 restatement)", "cells": n ** 3},
+                               f"tol 1e-6 relative (CPU FP64 restatement)", "cells": n ** 3,
+                   "iterations": iters[-1]},
         "cpu_baseline": cpu,
         "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
@@ -448,9 +588,10 @@ def main():
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32", "mixed-bf16"])
     ap.add_argument("--coarse", default="direct", choices=["direct", "sweeps"])
+    ap.add_argument("--arms", default="fp32,mixed-bf16,learned+mixed",
+                    help="comparison arms timed on the same system ('none' to skip)")
+    ap.add_argument("--arm-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-budget", type=float, default=30.0)
-    ap.add_argument("--ref-iters", type=int, default=10)
     ap.add_argument("--profile-only", default=None, choices=sorted(PROF_IDS),
                     help="run one kernel family inside an NVTX range for ncu, then exit")
     ap.add_argument("--no-kernel-profile", action="store_true",

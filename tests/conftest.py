@@ -31,6 +31,18 @@ def load_stalled(frame):
     return meta, arr
 
 
+def oracle_pressure(O, shape, h, b, mask, weights, vent=None, levels=3, tol=1e-11, max_iter=400):
+    """The FP64 oracle's pressure for A p = b, converged far below any
+    solver tolerance (relative residual `tol`), as the reference solution
+    that GPU pressures and velocities are compared with."""
+    nz = shape[2] if len(shape) > 2 else 1
+    w = tuple(weights[:2]) + ((weights[2],) if nz > 1 and len(weights) > 2 and weights[2] is not None else (None,))
+    mg = O.Multigrid(shape, h, mask, vent, w, levels=levels, coarse_direct=True)
+    x, r, _ = O.pcg_solve(shape, h, b, None, mask, w, mg, "multigrid", tol=tol, max_iter=max_iter)
+    assert r["converged"], r
+    return x
+
+
 @pytest.fixture(scope="session")
 def libff():
     """libff.so, built in-tree if needed.  GPU tests only."""

@@ -5,6 +5,8 @@ constrained) in 2D and 3D."""
 import numpy as np
 import pytest
 
+from conftest import oracle_pressure
+
 pytestmark = pytest.mark.gpu
 
 
@@ -43,6 +45,13 @@ def test_cylinder_2d_projection(gpu, oracle, precision):
         # pressure carries its own rounding on top
         assert d["converged"] and res < 5e-6, (d, res)
         assert abs(d["iterations"] - ro["iterations"]) <= 3, (d["iterations"], ro["iterations"])
+        # pressure and velocity against the oracle's converged solution
+        p_ref = oracle_pressure(oracle, shape, h, b, mask, wts, vent, levels=4)
+        u_ref = oracle.correct(shape, h, p_ref, sc["u"], sc["v"], None, collider_weights=wts)
+        perr = rel(p, p_ref)
+        uerr = max(rel(f.to_array(), r) for f, r in zip((out.data_u, out.data_v), u_ref[:2]))
+        print(f"cylinder 128^2: pressure rel-L2 {perr:.3e}, velocity rel-L2 {uerr:.3e}")
+        assert perr < 1e-5 and uerr < 1e-5, (perr, uerr)
     else:
         # an FP32 iterate stalls at its rounding floor above 1e-6 (the
         # reference notes the same for its float32 CG, linalg.js:152-156);

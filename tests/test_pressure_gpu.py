@@ -144,6 +144,64 @@ def test_cheap_preconditioners(gpu, oracle, pre):
     assert abs(d["iterations"] - ro["iterations"]) <= max(5, 0.15 * ro["iterations"])
 
 
+def test_iteration_cap_3d(gpu, oracle):
+    """With no preconditioner the frame-110 system needs 192 CG iterations
+    for 1e-5; the default cap ceil(1.5 * max(48, 24, 24)) = 72
+    (grid_pressure_solver3.js:133) stops it first: not converged, no guard
+    named, as the oracle run with the same cap reports."""
+    from tsl_array_n_gb300 import fluxflow as ff
+    from tsl_array_n_gb300.tsl_array_n import Field
+    meta, a = load_stalled(110)
+    shape, h = tuple(meta["resolution"]), meta["gridSpacing"]
+    cw = {"u": Field("float", meta["dataSizeU"]).from_array(a["weightU"]),
+          "v": Field("float", meta["dataSizeV"]).from_array(a["weightV"]),
+          "w": Field("float", meta["dataSizeW"]).from_array(a["weightW"])}
+    vent = a["ventMask"] > 0.5
+    s = ff.create_grid_pressure_solver3(shape, h, collider_weights=cw, dirichlet=(vent, np.zeros(vent.size)),
+                                        preconditioner="none", tolerance=1e-5, precision="fp32")
+    s.prepare()
+    s.pressure.fill(0.0)
+    b = a["b"].astype(np.float32)
+    d = s.solve(Field("float", shape).from_array(b))
+    mask = a["dirichletMask"] > 0.5
+    w = (a["weightU"], a["weightV"], a["weightW"])
+    _, ro, _ = oracle.pcg_solve(shape, h, b.astype(np.float64), None, mask, w, None, "none", tol=1e-5, max_iter=72)
+    assert d["maxIterations"] == 72
+    assert not d["converged"] and not ro["converged"]
+    assert d["iterations"] == ro["iterations"] == 72
+    assert d["stoppedBy"] == ro["stopped_by"] == "none"
+    assert abs(d["residual"] / ro["residual"] - 1) < 0.05, (d["residual"], ro["residual"])
+
+
+def test_iteration_cap_2d(gpu, oracle):
+    """2D caps are ceil(factor * max(nx, ny) * 4) (grid_pressure_solver2.js:398):
+    the 128^2 cylinder system with no preconditioner and factor 0.125 stops
+    at 64 iterations, not converged, like the oracle with the same cap."""
+    from tsl_array_n_gb300 import fluxflow as ff, scenes
+    from tsl_array_n_gb300.tsl_array_n import Field
+    sc = scenes.cylinder_scene_2d()
+    n = 128
+    shape, h = sc["shape"], sc["h"]
+    cw = {"u": Field("float", (n + 1, n, 1)).from_array(sc["wu"]),
+          "v": Field("float", (n, n + 1, 1)).from_array(sc["wv"]),
+          "w": Field("float", (n, n, 2)).from_array(np.ones(2 * n * n, np.float32))}
+    solver = ff.create_grid_pressure_solver2((n, n), h[:2], collider_weights=cw,
+                                             dirichlet=(sc["active"], sc["target"]), preconditioner="none",
+                                             max_iterations_factor=0.125, precision="fp32", tolerance=1e-6)
+    grid = ff.FaceCenteredGrid3(shape, h).set(sc["u"], sc["v"], sc["w"])
+    out = ff.FaceCenteredGrid3(shape, h)
+    d = solver.project(grid, out)()
+    wts = (sc["wu"].astype(np.float64), sc["wv"].astype(np.float64), None)
+    mask, tgt, _ = oracle.dirichlet_fields(shape, sc["active"], sc["target"], wts)
+    b, _ = oracle.build_system(shape, h, sc["u"], sc["v"], None, collider_weights=wts, mask=mask, target=tgt)
+    _, ro, _ = oracle.pcg_solve(shape, h, b, None, mask, wts, None, "none", tol=1e-6, max_iter=64)
+    assert d["maxIterations"] == 64
+    assert not d["converged"] and not ro["converged"]
+    assert d["iterations"] == ro["iterations"] == 64
+    assert d["stoppedBy"] == ro["stopped_by"] == "none"
+    assert abs(d["residual"] / ro["residual"] - 1) < 0.05, (d["residual"], ro["residual"])
+
+
 def test_guard_nan_rhs_is_reported_not_thrown(gpu, oracle):
     """A NaN right-hand side trips a guard (degenerate pAp) and leaves the
     pressure untouched; the oracle reports the same stop code."""
