@@ -282,7 +282,19 @@ def test_headline_256_matches_oracle(gpu, oracle):
     b_after, _ = oracle.build_system(shape, h, ug, vg, wg, collider_weights=wts, mask=mask, target=tgt)
     b_after[mask.astype(bool)] = 0.0
     div = float(np.linalg.norm(b_after) / np.linalg.norm(b))
-    print(f"sphere 256^3 mixed: {d['iterations']} iterations, pressure rel-L2 {perr:.3e}, "
+    # how much of the error is the near-null constant mode (one pinned cell):
+    # the error with its mean over free cells removed, and after the FP64
+    # Galerkin correction along the constant vector of the free cells
+    fl = ~mask.astype(bool)
+    e = p - p_ref
+    e0 = float(np.linalg.norm(e[fl] - e[fl].mean()) / np.linalg.norm(p_ref))
+    one = fl.astype(np.float64)
+    a1 = oracle.laplacian(shape, h, one, mask, wts)
+    r = b - oracle.laplacian(shape, h, p, mask, wts)
+    c = float(r[fl].sum() / a1[fl].sum())
+    perr_g = rel(p + c * one, p_ref)
+    print(f"sphere 256^3 mixed: {d['iterations']} iterations, pressure rel-L2 {perr:.3e} "
+          f"(mean removed {e0:.3e}, after the constant-mode correction {perr_g:.3e}), "
           f"velocity rel-L2 {uerr:.3e}, divergence left {div:.3e}")
     assert perr < 1e-5 and uerr < 1e-5, (perr, uerr)
     assert div < 1e-4

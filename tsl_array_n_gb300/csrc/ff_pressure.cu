@@ -457,6 +457,10 @@ static int prepare(ff_pressure ps, ff_field u, ff_field v, ff_field w) {
             for (int a = 0; a < ps->dims; ++a) sw[a] = (float *)(fw[0] ? fw[a] : cw[a]);
         }
     }
+    // the solve starts from the pressure field as the caller sees it: the
+    // low word of the double-single iterate left by the previous solve is
+    // cleared (the caller may have rewritten the high word)
+    if (ps->x_lo0) FF_CUDA(cudaMemsetAsync(ps->x_lo0, 0, (size_t)d.n() * sizeof(float), s));
     // dispatchBuildSystem (:429-453); pins p at Dirichlet cells
     if (u) {
         FF_TRY(ffk::build_system(d, ps->hx, ps->hy, ps->hz, fptr(u), fptr(v), fptr(w), cw, fw,
