@@ -19,11 +19,11 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
 
 
-def inputs(seed=0):
+def inputs(seed=0, sh=SH):
     rng = np.random.default_rng(seed)
-    n = SH[0] * SH[1] * SH[2]
-    k, j, i = np.meshgrid(np.arange(SH[2]), np.arange(SH[1]), np.arange(SH[0]), indexing="ij")
-    b = (np.sin(2 * np.pi * i / SH[0]) * np.cos(2 * np.pi * j / SH[1]) + 0.3 * rng.standard_normal(i.shape))
+    n = sh[0] * sh[1] * sh[2]
+    k, j, i = np.meshgrid(np.arange(sh[2]), np.arange(sh[1]), np.arange(sh[0]), indexing="ij")
+    b = (np.sin(2 * np.pi * i / sh[0]) * np.cos(2 * np.pi * j / sh[1]) + 0.3 * rng.standard_normal(i.shape))
     b = b.astype(np.float32).ravel()
     mask = (rng.random(n) < 0.1).astype(np.uint8)
     pp = rng.standard_normal(n).astype(np.float32) * 0.01
@@ -31,10 +31,10 @@ def inputs(seed=0):
     return b, mask, pp, target
 
 
-def fields(b, mask, pp, target):
+def fields(b, mask, pp, target, sh=SH):
     from tsl_array_n_gb300.tsl_array_n import Field
-    return (Field("float", SH).from_array(b), Field("uint8", SH).from_array(mask),
-            Field("float", SH).from_array(pp), Field("float", SH).from_array(target))
+    return (Field("float", sh).from_array(b), Field("uint8", sh).from_array(mask),
+            Field("float", sh).from_array(pp), Field("float", sh).from_array(target))
 
 
 def test_param_count(gpu):
@@ -60,6 +60,40 @@ def test_forward_matches_torch(gpu):
     net.forward(SH, H, fb, fm, None, out)
     ref = unet_ref.predict(net.params, b, mask, None, H, SH)
     assert rel(out.to_array(), ref) < 2e-2
+
+
+@pytest.mark.parametrize("sh", [(40, 36, 64), (24, 20, 32)])
+def test_forward_matches_torch_long_columns(gpu, sh):
+    """Volumes whose convolutions split each tile column into several z
+    ranges, with partial tiles at the y edge (36 and 20 rows against tiles
+    of 16)."""
+    from oracle import unet_ref
+    from tsl_array_n_gb300.tsl_array_n import Field
+    from tsl_array_n_gb300.warmstart import UNetWarmStart
+    net = UNetWarmStart(seed=13)
+    b, mask, pp, target = inputs(5, sh)
+    fb, fm, fp, _ = fields(b, mask, pp, target, sh)
+    out = Field("float", sh)
+    net.forward(sh, 1.0 / sh[0], fb, fm, fp, out)
+    ref = unet_ref.predict(net.params, b, mask, pp, 1.0 / sh[0], sh)
+    assert rel(out.to_array(), ref) < 2e-2
+
+
+def test_gradients_match_torch_long_columns(gpu):
+    from oracle import unet_ref
+    from tsl_array_n_gb300.warmstart import UNetWarmStart
+    sh = (24, 20, 32)
+    net = UNetWarmStart(seed=17)
+    b, mask, pp, target = inputs(6, sh)
+    loss = net.loss_backward(sh, 1.0 / sh[0], *fields(b, mask, pp, target, sh))
+    ref_loss, ref_g = unet_ref.loss_and_grads(net.params, b, mask, pp, target, 1.0 / sh[0], sh)
+    assert abs(loss - ref_loss) <= 1e-2 * ref_loss
+    g = net.grads
+    off = 0
+    for ci, co in unet_ref.SPEC:
+        nw = 27 * ci * co
+        assert rel(g[off:off + nw], ref_g[off:off + nw]) < 5e-2, (ci, co)
+        off += nw + co
 
 
 def test_gradients_match_torch(gpu):

@@ -135,10 +135,12 @@ def c2(ctx, steps=2000, timed=100, every=2):
             "steps": steps, "symmetry_break_step": sym_break, "probes": st}
 
 
-def c4(ctx):
+def c4(ctx, steps=None):
+    """U-Net timings at 128^3 and 256^3 (``c4:128`` or ``c4:256``: that size
+    alone)."""
     from .warmstart import UNetWarmStart
     out = {"config": "C4 U-Net warm start (3 levels, 16/32/64 channels)"}
-    for n in (128, 256):
+    for n in ((steps,) if steps else (128, 256)):
         shp = (n, n, n)
         rng = np.random.default_rng(0)
         b = Field("float", shp).from_array(rng.standard_normal(n ** 3).astype(np.float32))

@@ -7,13 +7,15 @@
 // are implicit GEMMs (M = voxels, K = 27 taps x Cin, N = Cout) with BF16
 // operands and FP32 accumulation on tcgen05 (accumulators in TMEM):
 // forward, input-gradient and weight-gradient convolutions; pre-activations
-// are kept in FP32 for the backward pass; master weights, gradients and the
-// Adam moments are FP32, with a BF16 copy of the weights for the GEMMs.
-// The input-gradient convolution reuses the forward kernel with the taps
-// flipped and the weight matrix transposed; weight gradients accumulate
-// per-tap [Cin x Cout] tiles over voxel chunks with FP32 atomics.
+// are kept in FP32 for the backward pass only (inference stores none);
+// master weights, gradients and the Adam moments are FP32, with a BF16 copy
+// of the weights for the GEMMs.  Forward and input-gradient convolutions run
+// in k_conv3_zm (a z-march over TMA-staged planes); the input-gradient one
+// takes the taps flipped and the weight matrix transposed; weight gradients
+// accumulate per-tap [Cin x Cout] tiles over voxel chunks with FP32 atomics.
 #include "ff_internal.h"
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -43,20 +45,14 @@ __device__ __forceinline__ void tap_offset(int t, int &dx, int &dy, int &dz) {
     dx = t % 3 - 1;
 }
 
-// ---- tcgen05 convolution ------------------------------------------------
-// 3x3x3 convolution, zero padding 1: Y[v, co] = act(sum_{t, ci} X[v + off(t),
-// ci] W[t, ci, co] + bias[co]), X with Cin channels (a multiple of 16, at
-// most 96), writing the FP32 pre-activation Z and/or the BF16 output Y.
-// An implicit GEMM on the 5th-generation tensor cores: one CTA owns 128
-// output voxels (M = 128, one TMEM lane each) and all Cout columns (N =
-// Cout, FP32 accumulators in TMEM); K runs over the 27 taps x Cin.  The
-// operands sit in shared memory in the canonical no-swizzle K-major layout
-// (8-row x 16-byte core matrices): the input halo of the CTA's tile staged
-// once (k_conv3_tch), and the weights, packed beforehand by k_pack_b, in
-// stages of several taps.  One elected thread issues the MMAs and commits
-// them to the stage's mbarrier; two weight stages alternate.  Waits are
-// bounded (0.5 s of globaltimer), after which the CTA flags the error,
-// frees its TMEM and returns.
+// ---- tcgen05 helpers -----------------------------------------------------
+// 3x3x3 convolutions, zero padding 1: Y[v, co] = act(sum_{t, ci} X[v + off(t),
+// ci] W[t, ci, co] + bias[co]), as implicit GEMMs on the 5th-generation
+// tensor cores: M = 128 output voxels (one TMEM lane each), N = output
+// channels (FP32 accumulators in TMEM), K = 27 taps x Cin.  Operands sit in
+// shared memory in the canonical no-swizzle K-major layout (8-row x 16-byte
+// core matrices); one elected thread issues the MMAs and commits them to an
+// mbarrier.  Waits are bounded (0.5 s of globaltimer).
 constexpr int TC_M = 128;
 // stride between 8-row groups of the packed weights (Cin / 8 core matrices each)
 __device__ __forceinline__ uint32_t sbo_b(int cin) { return (uint32_t)(cin >> 3) * 128u; }
@@ -136,36 +132,82 @@ __global__ void k_pack_b(int cin, int cout, const bf16 *__restrict__ W, bf16 *__
     }
 }
 
-// The convolution over tiles of 8 x 16 x 1 output voxels (row m of
-// the tile: x0 + m % 8, y0 + m / 8): the input halo of the tile (x0-1 ..
-// x0+8, y0-1 .. y0+16, z0-1 .. z0+1, zero outside the volume) is staged
-// once, as lines of 10 voxels x 16 bytes per (z, y, channel group), so that
-// each tap's A operand is a view of it: the tap's first core matrix at line
-// (z0+dz, y0+dy, group 0) + (dx + 1) x 16 bytes, core matrices 160 bytes
-// apart along K (the next channel group) and Cin / 8 x 160 bytes apart
-// along M (the next row of the tile).  Per tap only the weights move.
-constexpr int HX = 10, HY = 18, HZ = 3, HLINE = HX * 16;
+// ---- z-marching tcgen05 convolution --------------------------------------
+// The same implicit GEMM (M = 128 output voxels of an 8 x 16 tile, N =
+// output channels, K = 27 taps x Cin) for a whole column of tiles along z:
+// one CTA owns tile (x0, y0) for planes zb .. ze-1 and keeps the input planes
+// it needs in a ring of R shared-memory slots, each plane's tile plus its
+// one-voxel halo (10 x 18 voxels) loaded by TMA as Cin / 8 boxes of 8
+// channels, i.e. in the layout [group][y][x][8 channels]: the A operand of
+// tap (dz, dy, dx) is a descriptor view of slot(z + dz) at (dy + 1, dx + 1)
+// with core matrices one group block (2944 B) apart along K and one halo line
+// (160 B) apart along M.  A plane enters once per column (not three times
+// as with one CTA per plane), and zero padding comes from the TMA's
+// out-of-bounds fill.  The weights of the CTA's output-channel chunk stay in
+// shared memory for the whole column.  The accumulators are two TMEM
+// buffers of N columns: while the tensor cores run plane z, the four warps
+// read plane z - 1 back (bias, GELU, stores), and the slot of plane z - 2
+// refills with plane z + R - 2.  Thread 0 issues the TMA loads and the MMAs.
+// Every wait is bounded (0.5 s); a CTA that gives up sets the error word,
+// drains what it issued (again bounded), frees its TMEM and returns.
+// ZM_GB: bytes of one group of one plane as the TMA writes it; ZM_GP: its
+// pitch in the slot (a multiple of 128 bytes, the TMA destination alignment)
+constexpr int ZM_HX = 10, ZM_HY = 18, ZM_GB = ZM_HX * ZM_HY * 16, ZM_GP = (ZM_GB + 127) / 128 * 128, ZM_RMAX = 6;
 
-// rtap: taps whose weights one stage holds (27, 9, 3 or 1; the host picks
-// the largest that fits shared memory beside the halo)
-template <int COUT>
-__global__ void __launch_bounds__(128) k_conv3_tch(Vol v, const bf16 *__restrict__ X, int cin,
-                                                  const bf16 *__restrict__ P, const float *__restrict__ bias, int act,
-                                                  float *__restrict__ Z, bf16 *__restrict__ Y, int rtap,
-                                                  int *__restrict__ err) {
-    constexpr int TCOLS = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : 128);
-    extern __shared__ unsigned char tc_smem[];
-    __shared__ __align__(8) uint64_t bars[2];
+struct ZmArgs {
+    Vol v;
+    int cin;            // input channels (tensor map and K), a multiple of 16
+    int cout;           // channel stride of the outputs
+    int ring;           // resident planes, 4 .. ZM_RMAX
+    int zseg, nzseg;    // planes per work item, work items along z
+    int ncol, tiles_x;  // tile columns
+    int act;            // GELU on Y (and the head)
+    const bf16 *P;      // weights packed for the B operand (k_pack_b), all cout
+    const float *bias;  // cout or null
+    float *Z;           // FP32 result before the activation (stride cout) or null
+    bf16 *Y;            // BF16 activated result (stride cout) or null
+    const float *head;  // 1x1 head (16 weights + bias) fused into the epilogue, or null
+    const float *scales;
+    float *out, *raw;   // head outputs: out = scales[1] raw
+    int *err;
+};
+
+__device__ __forceinline__ void zm_expect(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void zm_tma4(uint32_t dst, const CUtensorMap *map, int c, int x, int y, int z,
+                                        uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
+        "l"(map), "r"(c), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+
+template <int N>
+__global__ void __launch_bounds__(128) k_conv3_zm(const __grid_constant__ ZmArgs a,
+                                                 const __grid_constant__ CUtensorMap xmap) {
+    constexpr int TCOLS = 2 * N <= 32 ? 32 : (2 * N <= 64 ? 64 : (2 * N <= 128 ? 128 : 256));
+    extern __shared__ unsigned char zm_smem[];
+    __shared__ __align__(8) uint64_t full[ZM_RMAX];
+    __shared__ __align__(8) uint64_t done[2];
     __shared__ uint32_t tmem_slot;
     const int tid = threadIdx.x, warp = tid >> 5;
-    const int groups = cin >> 3;
-    const int halo_bytes = HZ * HY * groups * HLINE;
-    const int b_bytes = COUT * cin * 2;   // one tap's packed weights
-    const int b_stage = (rtap * b_bytes + 1023) & ~1023;
-    const uint32_t raw = smem_u32(tc_smem);
-    unsigned char *halo = tc_smem + (((raw + 1023u) & ~1023u) - raw);
-    unsigned char *bst = halo + ((halo_bytes + 1023) & ~1023);
-    const uint32_t bar0 = smem_u32(&bars[0]), bar1 = smem_u32(&bars[1]);
+    const int groups = a.cin >> 3;
+    const uint32_t slot_bytes = (uint32_t)groups * ZM_GP, plane_tx = (uint32_t)groups * ZM_GB;
+    const int R = a.ring;
+    // work item: consecutive blocks take neighbouring columns of one z range
+    const int bid = blockIdx.x;
+    const int col = bid % a.ncol, zs = (bid / a.ncol) % a.nzseg, chunk = bid / (a.ncol * a.nzseg);
+    const int x0 = 8 * (col % a.tiles_x), y0 = 16 * (col / a.tiles_x);
+    const int zb = zs * a.zseg, ze = min(zb + a.zseg, a.v.nz);
+    const int n0 = chunk * N;
+    // shared memory: weights of the chunk (27 taps x N x cin BF16), then the ring
+    const uint32_t raw_addr = smem_u32(zm_smem);
+    unsigned char *wsm = zm_smem + (((raw_addr + 1023u) & ~1023u) - raw_addr);
+    const uint32_t wbytes = 27u * N * a.cin * 2u;
+    unsigned char *ring = wsm + ((wbytes + 1023u) & ~1023u);
+    const uint32_t wbase = smem_u32(wsm), rbase = smem_u32(ring);
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
                      "r"(TCOLS));
@@ -173,100 +215,137 @@ __global__ void __launch_bounds__(128) k_conv3_tch(Vol v, const bf16 *__restrict
         asm volatile("tcgen05.fence::before_thread_sync;");
     }
     if (tid == 0) {
-        mbar_init(bar0, 1);
-        mbar_init(bar1, 1);
+        for (int q = 0; q < R; ++q) mbar_init(smem_u32(&full[q]), 1);
+        mbar_init(smem_u32(&done[0]), 1);
+        mbar_init(smem_u32(&done[1]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    const int tiles_x = (v.nx + 7) >> 3, tiles_y = (v.ny + 15) >> 4;
-    const int bx = blockIdx.x % tiles_x, by = (blockIdx.x / tiles_x) % tiles_y;
-    const int x0 = 8 * bx, y0 = 16 * by, z0 = blockIdx.x / (tiles_x * tiles_y);
-    // the halo: 540 positions x Cin / 8 groups, consecutive threads on
-    // consecutive groups of a voxel
-    for (int q = tid; q < HZ * HY * HX * groups; q += TC_M) {
-        const int g = q % groups, pos = q / groups;
-        const int xc = pos % HX, yr = (pos / HX) % HY, zp = pos / (HX * HY);
-        const int sx = x0 - 1 + xc, sy = y0 - 1 + yr, sz = z0 - 1 + zp;
-        uint4 val = make_uint4(0, 0, 0, 0);
-        if (sx >= 0 && sx < v.nx && sy >= 0 && sy < v.ny && sz >= 0 && sz < v.nz)
-            val = __ldg(reinterpret_cast<const uint4 *>(X + (sx + (long long)v.nx * (sy + (long long)v.ny * sz)) * cin) + g);
-        *reinterpret_cast<uint4 *>(halo + ((zp * HY + yr) * groups + g) * HLINE + xc * 16) = val;
+    // the chunk's weights: per tap N x cin contiguous in the packed array
+    {
+        const uint32_t per_tap = (uint32_t)N * a.cin * 2u / 16u;   // uint4 per tap
+        for (uint32_t q = tid; q < 27u * per_tap; q += 128) {
+            const uint32_t t = q / per_tap, r = q - t * per_tap;
+            const uint4 *src = reinterpret_cast<const uint4 *>(a.P + ((long long)t * a.cin * a.cout + (long long)n0 * a.cin));
+            reinterpret_cast<uint4 *>(wsm)[q] = __ldg(src + r);
+        }
     }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_slot;
-    const uint32_t idesc = tc_idesc(TC_M, COUT);
-    const uint32_t hbase = smem_u32(halo), sbo = (uint32_t)groups * HLINE;
-    const uint32_t nb16 = (uint32_t)(rtap * b_bytes) >> 4;   // 16-byte rows of a stage
-    const int rounds = 27 / rtap;
+    const uint32_t idesc = tc_idesc(TC_M, N);
+    const int nplanes = ze - zb, nload = nplanes + 2;   // input planes zb - 1 .. ze
+    int issued = 0;        // planes whose loads thread 0 issued (plane q is input z = zb - 1 + q)
+    int waited = 0;        // planes thread 0 has seen land
+    auto load_plane = [&](int q) {
+        const int slot = q % R;
+        const uint32_t bar = smem_u32(&full[slot]), dst = rbase + (uint32_t)slot * slot_bytes;
+        zm_expect(bar, plane_tx);
+        for (int g = 0; g < groups; ++g)
+            zm_tma4(dst + (uint32_t)g * ZM_GP, &xmap, 8 * g, x0 - 1, y0 - 1, zb - 1 + q, bar);
+    };
+    if (tid == 0)
+        for (; issued < min(R, nload); ++issued) load_plane(issued);
+    // per-thread output voxel (TMEM lane tid)
+    const int ox = x0 + (tid & 7), oy = y0 + (tid >> 3);
+    const bool in = ox < a.v.nx && oy < a.v.ny;
+    const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
     bool ok = true;
-    int last = -1;
-    for (int rr = 0; rr < rounds; ++rr) {
-        const int st = rr & 1;
-        unsigned char *bt = bst + st * b_stage;
-        // the stage's previous MMAs (round rr - 2) must be done before it is overwritten
-        if (rr >= 2) ok = mbar_wait(st ? bar1 : bar0, (uint32_t)(((rr >> 1) - 1) & 1));
+    int committed = -1;    // last plane index i whose MMAs were committed
+    int drained = -1;      // last i whose MMA completion was waited
+    for (int i = 0; i <= nplanes; ++i) {
+        if (i < nplanes && tid == 0) {
+            // planes i, i + 1, i + 2 (input z - 1, z, z + 1) must have landed
+            while (waited < i + 3 && ok) {
+                ok = mbar_wait(smem_u32(&full[waited % R]), (uint32_t)((waited / R) & 1));
+                if (ok) ++waited;
+            }
+            if (ok) {
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t dacc = tmem + (uint32_t)((i & 1) * N);
+                int first = 1;
+#pragma unroll 1
+                for (int t = 0; t < 27; ++t) {
+                    int dx, dy, dz;
+                    tap_offset(t, dx, dy, dz);
+                    const int q = i + dz + 1;
+                    const uint32_t a0 = rbase + (uint32_t)(q % R) * slot_bytes +
+                                        (uint32_t)(((dy + 1) * ZM_HX + (dx + 1)) * 16);
+                    const uint32_t b0 = wbase + (uint32_t)t * (uint32_t)(N * a.cin * 2);
+                    for (int kc = 0; kc < (a.cin >> 4); ++kc) {
+                        tc_mma(dacc, tc_sdesc(a0 + (uint32_t)(2 * kc) * ZM_GP, ZM_GP, ZM_HX * 16),
+                               tc_sdesc(b0 + 256u * kc, 128u, sbo_b(a.cin)), idesc, first ? 0 : 1);
+                        first = 0;
+                    }
+                }
+                tc_commit(smem_u32(&done[i & 1]));
+                committed = i;
+            }
+        }
+        if (i > 0) {
+            const int j = i - 1;   // the plane read back now
+            bool got = mbar_wait(smem_u32(&done[j & 1]), (uint32_t)((j >> 1) & 1));
+            ok = ok && got;
+            if (got) drained = j;
+            // plane j's MMAs are done: its first input plane's slot refills
+            if (tid == 0 && ok && issued < nload && issued == j + R) {
+                load_plane(issued);
+                ++issued;
+            }
+            if (ok) {
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const int z = zb + j;
+                const long long vox = ox + (long long)a.v.nx * (oy + (long long)a.v.ny * z);
+                float hs = 0.0f;
+#pragma unroll
+                for (int c0 = 0; c0 < N; c0 += 16) {
+                    float acc[16];
+                    tc_ld16(lane_addr + (uint32_t)((j & 1) * N + c0), acc);
+                    if (in) {
+                        float zz[16];
+#pragma unroll
+                        for (int q = 0; q < 16; ++q) zz[q] = acc[q] + (a.bias ? __ldg(a.bias + n0 + c0 + q) : 0.0f);
+                        if (a.Z) {
+                            float4 *zr = reinterpret_cast<float4 *>(a.Z + vox * a.cout + n0 + c0);
+#pragma unroll
+                            for (int q = 0; q < 4; ++q)
+                                zr[q] = make_float4(zz[4 * q], zz[4 * q + 1], zz[4 * q + 2], zz[4 * q + 3]);
+                        }
+                        if (a.Y) {
+                            __align__(16) bf16 yb[16];
+#pragma unroll
+                            for (int q = 0; q < 16; ++q) yb[q] = __float2bfloat16_rn(a.act ? gelu(zz[q]) : zz[q]);
+                            uint4 *yr = reinterpret_cast<uint4 *>(a.Y + vox * a.cout + n0 + c0);
+                            yr[0] = reinterpret_cast<const uint4 *>(yb)[0];
+                            yr[1] = reinterpret_cast<const uint4 *>(yb)[1];
+                        }
+                        if (a.head) {
+                            if (c0 == 0) hs = __ldg(a.head + 16);
+#pragma unroll
+                            for (int q = 0; q < 16; ++q) hs += gelu(zz[q]) * __ldg(a.head + c0 + q);
+                        }
+                    }
+                }
+                if (a.head && in) {
+                    if (a.raw) a.raw[vox] = hs;
+                    if (a.out) a.out[vox] = hs * __ldg(a.scales + 1);
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;");
+            }
+        }
         if (!__syncthreads_and(ok)) {
             ok = false;
             break;
         }
-        // taps rr rtap .. rr rtap + rtap - 1 are contiguous in the packed weights
-        const uint4 *pt = reinterpret_cast<const uint4 *>(P + (long long)rr * rtap * cin * COUT);
-        for (uint32_t q = tid; q < nb16; q += TC_M) reinterpret_cast<uint4 *>(bt)[q] = __ldg(pt + q);
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
+    }
+    if (!ok) {
+        // drain what was issued before giving up (bounded), then report
         if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;");
-            for (int u = 0; u < rtap; ++u) {
-                const int t = rr * rtap + u;
-                int dx, dy, dz;
-                tap_offset(t, dx, dy, dz);
-                const uint32_t a0 = hbase + (uint32_t)(((dz + 1) * HY + (dy + 1)) * groups * HLINE + (dx + 1) * 16);
-                const uint32_t b0 = smem_u32(bt) + (uint32_t)(u * b_bytes);
-                for (int kc = 0; kc < (cin >> 4); ++kc)
-                    tc_mma(tmem, tc_sdesc(a0 + 2u * HLINE * kc, HLINE, sbo),
-                           tc_sdesc(b0 + 256u * kc, 128u, sbo_b(cin)), idesc, (t > 0 || kc > 0) ? 1 : 0);
-            }
-            tc_commit(st ? bar1 : bar0);
+            for (; waited < issued; ++waited) mbar_wait(smem_u32(&full[waited % R]), (uint32_t)((waited / R) & 1));
+            if (committed > drained) mbar_wait(smem_u32(&done[committed & 1]), (uint32_t)((committed >> 1) & 1));
+            atomicExch(a.err, 1);
         }
-        last = rr;
     }
-    if (last >= 0) {
-        const bool done = mbar_wait((last & 1) ? bar1 : bar0, (uint32_t)((last >> 1) & 1));
-        ok = ok && done;
-    }
-    ok = __syncthreads_and(ok);
-    if (ok) {
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
-        const int x = x0 + (tid & 7), y = y0 + (tid >> 3);
-        const bool in = x < v.nx && y < v.ny;
-        const long long vox = x + (long long)v.nx * (y + (long long)v.ny * z0);
-#pragma unroll
-        for (int c0 = 0; c0 < COUT; c0 += 16) {
-            float acc[16];
-            tc_ld16(lane_addr + (uint32_t)c0, acc);
-            if (in) {
-                float z[16];
-#pragma unroll
-                for (int q = 0; q < 16; ++q) z[q] = acc[q] + (bias ? __ldg(bias + c0 + q) : 0.0f);
-                if (Z) {
-                    float4 *zr = reinterpret_cast<float4 *>(Z + vox * COUT + c0);
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) zr[q] = make_float4(z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
-                }
-                if (Y) {
-                    __align__(16) bf16 yb[16];
-#pragma unroll
-                    for (int q = 0; q < 16; ++q) yb[q] = __float2bfloat16_rn(act ? gelu(z[q]) : z[q]);
-                    uint4 *yr = reinterpret_cast<uint4 *>(Y + vox * COUT + c0);
-                    yr[0] = reinterpret_cast<const uint4 *>(yb)[0];
-                    yr[1] = reinterpret_cast<const uint4 *>(yb)[1];
-                }
-            }
-        }
-    } else if (tid == 0) {
-        atomicExch(err, 1);
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;");
@@ -568,18 +647,6 @@ __global__ void k_input(long long n, const float *__restrict__ b, const uint8_t 
     }
 }
 
-// 1x1x1 output layer (16 -> 1) in FP32 on the last convolution's FP32
-// pre-activations (no BF16 rounding reaches the guess, whose grid-scale
-// noise the Laplacian would amplify): out = sp (w . gelu(z) + b)
-__global__ void k_head(long long n, const float *__restrict__ Zin, const float *__restrict__ w,
-                       const float *__restrict__ scales, float *__restrict__ out, float *__restrict__ raw) {
-    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
-        float s = w[16];
-        for (int c = 0; c < 16; ++c) s += gelu(Zin[v * 16 + c]) * w[c];
-        if (raw) raw[v] = s;
-        if (out) out[v] = s * scales[1];
-    }
-}
 // MSE loss in normalised units: L = mean((raw - t / sp)^2); dL/draw per
 // voxel; the loss itself by a deterministic block-partial reduction
 __global__ void k_loss(long long n, const float *__restrict__ raw, const float *__restrict__ target,
@@ -656,42 +723,131 @@ int post(const char *what) {
     return FF_OK;
 }
 
-template <int COUT>
-int launch_conv_tch(Vol v, const bf16 *X, int cin, const bf16 *pk, const float *bias, int act, float *Z, bf16 *Y,
-                    int *err, cudaStream_t s) {
-    // the halo (3 x 18 x cin / 8 lines of 160 bytes) and two weight stages
-    // of rtap taps, each 1 KB aligned, + alignment slack; rtap the largest
-    // of 27, 9, 3, 1 within 120 KB
-    const int halo = (HZ * HY * (cin / 8) * HLINE + 1023) & ~1023;
-    int rtap = 27, bstage = 0, smem = 0;
-    for (; rtap >= 1; rtap /= 3) {
-        bstage = (rtap * COUT * cin * 2 + 1023) & ~1023;
-        smem = halo + 2 * bstage + 1024;
-        if (smem <= 120 * 1024 || rtap == 1) break;
+int sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+            n = 152;
     }
-    static int configured = 0;
-    if (smem > configured) {
-        FF_CUDA(cudaFuncSetAttribute(k_conv3_tch<COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        configured = smem;
-    }
-    const long long nb = (long long)((v.nx + 7) / 8) * ((v.ny + 15) / 16) * v.nz;
-    k_conv3_tch<COUT><<<(unsigned)nb, TC_M, smem, s>>>(v, X, cin, pk, bias, act, Z, Y, rtap, err);
-    return post("conv3 tcgen05 halo");
+    return n;
 }
 
-// W: [27][cin][cout] BF16; pk: scratch for the packed copy (27 cin cout)
+PFN_cuTensorMapEncodeTiled_v12000 zm_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+// shared memory of k_conv3_zm: weights of an N-channel chunk, a ring of R
+// planes, 1 KB alignment slack
+size_t zm_smem_bytes(int n, int cin, int ring) {
+    return ((27u * n * cin * 2u + 1023u) & ~1023u) + (size_t)ring * (cin / 8) * ZM_GP + 1024;
+}
+
+template <int N>
+int launch_zm(const ZmArgs &a, const CUtensorMap &map, int nchunks, size_t smem, cudaStream_t s) {
+    static size_t configured = 0;
+    if (smem > configured) {
+        FF_CUDA(cudaFuncSetAttribute(k_conv3_zm<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = smem;
+    }
+    const long long blocks = (long long)a.ncol * a.nzseg * nchunks;
+    k_conv3_zm<N><<<(unsigned)blocks, TC_M, smem, s>>>(a, map);
+    return post("conv3 z-march");
+}
+
+// Y = act(conv(X, W) + bias) and/or Z = conv(X, W) + bias, or the fused head
+// (out, raw) on top of the activation.  X: channels-last BF16 with cin
+// channels (a multiple of 16, at most 96); W: [27][cin][cout] BF16, packed
+// into pk (27 cin cout) for the B operand.
 int launch_conv(int cout, Vol v, const bf16 *X, int cin, const bf16 *W, const float *bias, int act, float *Z, bf16 *Y,
-                bf16 *pk, int *err, cudaStream_t s) {
+                bf16 *pk, int *err, cudaStream_t s, const float *head = nullptr, const float *scales = nullptr,
+                float *out = nullptr, float *raw = nullptr) {
     if (cin % 16 || cin > 96) return ff_set_error(FF_E_ARG, "unet: conv input channels %d (multiples of 16 to 96)", cin);
+    if (cout % 16 || cout > 96) return ff_set_error(FF_E_ARG, "unet: conv output channels %d (multiples of 16 to 96)", cout);
     k_pack_b<<<gblocks(27LL * cin * cout), 256, 0, s>>>(cin, cout, W, pk);
     FF_TRY(post("pack weights"));
-    switch (cout) {
-    case 16: return launch_conv_tch<16>(v, X, cin, pk, bias, act, Z, Y, err, s);
-    case 32: return launch_conv_tch<32>(v, X, cin, pk, bias, act, Z, Y, err, s);
-    case 48: return launch_conv_tch<48>(v, X, cin, pk, bias, act, Z, Y, err, s);
-    case 64: return launch_conv_tch<64>(v, X, cin, pk, bias, act, Z, Y, err, s);
-    case 96: return launch_conv_tch<96>(v, X, cin, pk, bias, act, Z, Y, err, s);
-    default: return ff_set_error(FF_E_ARG, "unet: no conv kernel for %d output channels", cout);
+    // the output-channel chunk: the widest whose weights and a ring of 4
+    // planes fit two CTAs per SM, else one CTA per SM; then the deepest
+    // ring that keeps that occupancy
+    const size_t two = 110 * 1024, one = 220 * 1024;
+    int n = 0, occ = 0;
+    for (int pass = 0; pass < 2 && !n; ++pass)
+        for (int d : {1, 2, 3, 4, 6}) {
+            if (cout % d || (cout / d) % 16) continue;
+            if (zm_smem_bytes(cout / d, cin, 4) <= (pass == 0 ? two : one)) {
+                n = cout / d;
+                occ = pass == 0 ? 2 : 1;
+                break;
+            }
+        }
+    if (!n) return ff_set_error(FF_E_LIMIT, "unet: no shared-memory plan for a %d -> %d convolution", cin, cout);
+    const size_t budget = occ == 2 ? two : one;
+    int ring = 4;
+    while (ring < ZM_RMAX && zm_smem_bytes(n, cin, ring + 1) <= budget) ++ring;
+    const size_t smem = zm_smem_bytes(n, cin, ring);
+    const int blocks_per_sm = std::max(1, std::min(8, (int)(228 * 1024 / (smem + 2048))));
+    ZmArgs a;
+    a.v = v;
+    a.cin = cin;
+    a.cout = cout;
+    a.ring = ring;
+    a.tiles_x = (v.nx + 7) / 8;
+    a.ncol = a.tiles_x * ((v.ny + 15) / 16);
+    const int nchunks = cout / n;
+    // the z split: work items of at least 8 planes (or the whole column)
+    // whose count fills the resident slots best, counting each item's two
+    // extra halo planes and about two planes' worth of start-up
+    const long long slots = (long long)sm_count() * blocks_per_sm;
+    double best = 1e300;
+    a.zseg = v.nz;
+    for (int zs = v.nz; zs >= std::min(8, v.nz); --zs) {
+        const long long items = (long long)a.ncol * nchunks * ((v.nz + zs - 1) / zs);
+        const double cost = (double)((items + slots - 1) / slots) * (zs + 4);
+        if (cost < best - 1e-9) {
+            best = cost;
+            a.zseg = zs;
+        }
+    }
+    a.nzseg = (v.nz + a.zseg - 1) / a.zseg;
+    a.act = act;
+    a.P = pk;
+    a.bias = bias;
+    a.Z = Z;
+    a.Y = Y;
+    a.head = head;
+    a.scales = scales;
+    a.out = out;
+    a.raw = raw;
+    a.err = err;
+    if (head && !(n == 16 && cout == 16)) return ff_set_error(FF_E_ARG, "unet: the fused head needs 16 channels");
+    PFN_cuTensorMapEncodeTiled_v12000 enc = zm_encoder();
+    FF_CHECK(enc, FF_E_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    CUtensorMap map;
+    cuuint64_t dims[4] = {(cuuint64_t)cin, (cuuint64_t)v.nx, (cuuint64_t)v.ny, (cuuint64_t)v.nz};
+    cuuint64_t strides[3] = {(cuuint64_t)cin * 2, (cuuint64_t)v.nx * cin * 2, (cuuint64_t)v.nx * v.ny * cin * 2};
+    cuuint32_t box[4] = {8, ZM_HX, ZM_HY, 1};
+    cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUresult r = enc(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)X, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    FF_CHECK(r == CUDA_SUCCESS, FF_E_CUDA, "unet: cuTensorMapEncodeTiled failed (%d) for %dx%dx%d x %d", (int)r, v.nx,
+             v.ny, v.nz, cin);
+    switch (n) {
+    case 16: return launch_zm<16>(a, map, nchunks, smem, s);
+    case 32: return launch_zm<32>(a, map, nchunks, smem, s);
+    case 48: return launch_zm<48>(a, map, nchunks, smem, s);
+    case 64: return launch_zm<64>(a, map, nchunks, smem, s);
+    case 96: return launch_zm<96>(a, map, nchunks, smem, s);
+    default: return ff_set_error(FF_E_ARG, "unet: no conv kernel for a %d-channel chunk", n);
     }
 }
 
@@ -949,7 +1105,12 @@ static int compute_scales(ff_unet u, const float *b, const float *pp, double h, 
 
 static Vol level_vol(ff_unet u, int lev) { return Vol{u->vol.nx >> lev, u->vol.ny >> lev, u->vol.nz >> lev}; }
 
-static int forward(ff_unet u, const float *b, const uint8_t *mask, const float *pp, double h, float *out) {
+// train: keep every convolution's FP32 pre-activation and the head's raw
+// output for the backward pass; inference stores neither.  The last
+// convolution feeds the 1x1 head in its epilogue (its BF16 output is never
+// read, so it is not written).
+static int forward(ff_unet u, const float *b, const uint8_t *mask, const float *pp, double h, float *out,
+                   bool train) {
     cudaStream_t s = u->ctx->stream;
     float sc[2];
     FF_TRY(compute_scales(u, b, pp, h, sc));
@@ -958,8 +1119,11 @@ static int forward(ff_unet u, const float *b, const uint8_t *mask, const float *
     auto conv = [&](int l) {
         const ConvLayer &c = u->convs[l];
         const int si = CONV_IN[l], so = CONV_OUT[l];
+        const bool head = l == 9;
         return launch_conv(c.cout, level_vol(u, SLOT_LEVEL[so]), u->act[si], c.cin, u->wb + u->wb_off[l],
-                           u->w + c.b_off, c.act, u->pre[l], u->act[so], u->wpk, u->tc_err, s);
+                           u->w + c.b_off, c.act, train ? u->pre[l] : nullptr, head ? nullptr : u->act[so], u->wpk,
+                           u->tc_err, s, head ? u->w + u->head_off : nullptr, u->scales, out,
+                           train ? u->raw : nullptr);
     };
     FF_TRY(conv(0));
     FF_TRY(conv(1));
@@ -975,7 +1139,6 @@ static int forward(ff_unet u, const float *b, const uint8_t *mask, const float *
     k_up_concat<<<gblocks(n0 * 48), 256, 0, s>>>(level_vol(u, 0), 32, 16, u->act[11], u->act[2], u->act[12]);
     FF_TRY(conv(8));
     FF_TRY(conv(9));
-    k_head<<<gblocks(n0), 256, 0, s>>>(n0, u->pre[9], u->w + u->head_off, u->scales, out, u->raw);
     return post("unet forward");
 }
 
@@ -1062,7 +1225,7 @@ extern "C" int ff_unet_forward(ff_unet u, const int *res, double h, ff_field b, 
                  (!mask || field_ok(mask, n, FF_UINT8)),
              FF_E_ARG, "unet forward: fields must be cell fields of the resolution (mask uint8)");
     FF_TRY(forward(u, (const float *)b->d, mask ? (const uint8_t *)mask->d : nullptr,
-                   p_prev ? (const float *)p_prev->d : nullptr, h, (float *)out->d));
+                   p_prev ? (const float *)p_prev->d : nullptr, h, (float *)out->d, false));
     return tc_status(u);
 }
 
@@ -1079,7 +1242,7 @@ extern "C" int ff_unet_loss_backward(ff_unet u, const int *res, double h, ff_fie
              FF_E_ARG, "unet loss: fields must be cell fields of the resolution (mask uint8)");
     cudaStream_t s = u->ctx->stream;
     FF_TRY(forward(u, (const float *)b->d, mask ? (const uint8_t *)mask->d : nullptr,
-                   p_prev ? (const float *)p_prev->d : nullptr, h, nullptr));
+                   p_prev ? (const float *)p_prev->d : nullptr, h, nullptr, true));
     const int nb = std::min(152 * 32, gblocks(n));
     k_loss<<<nb, 256, 0, s>>>(n, u->raw, (const float *)target->d, u->scales, u->draw, u->partial);
     FF_TRY(post("loss"));
