@@ -117,42 +117,67 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
     for (int q = 0; q < 16; ++q) v[q] = __uint_as_float(r[q]);
 }
 
-// the B operand of every tap in the canonical K-major layout: from W
-// [27][cin][cout] (N contiguous) to P[t][(n / 8) (cin / 8) + k / 8][n % 8][k % 8]
-__global__ void k_pack_b(int cin, int cout, const bf16 *__restrict__ W, bf16 *__restrict__ P) {
+// The B operands of k_conv3_zm in the canonical K-major layout, per chunk of
+// C output channels: from W [27][cin][cout] (tap t = (dz+1) 9 + (dy+1) 3 +
+// (dx+1)) to P[chunk][shift (dy+1) 3 + (dx+1)][n][k] with n = j C + c, the
+// column blocks j = 0, 1, 2 holding dz = +1, 0, -1 (output planes q - 2,
+// q - 1, q of input plane q), core matrix (n / 8, k / 8) at
+// ((n / 8) (cin / 8) + k / 8) x 64 elements, row n % 8, column k % 8.
+__global__ void k_pack_b(int cin, int cout, int C, const bf16 *__restrict__ W, bf16 *__restrict__ P) {
     const long long n_all = 27LL * cin * cout;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n_all;
          e += (long long)gridDim.x * blockDim.x) {
         const int t = (int)(e / ((long long)cin * cout));
         const int rem = (int)(e - (long long)t * cin * cout);
-        const int k = rem / cout, n = rem % cout;
-        const long long dst = (long long)t * cin * cout +
+        const int k = rem / cout, co = rem % cout;
+        const int dz = t / 9 - 1, sh = t % 9, j = 1 - dz;
+        const int ch = co / C, n = j * C + co % C;
+        const long long dst = (long long)ch * 27 * C * cin + (long long)sh * 3 * C * cin +
                               ((long long)((n >> 3) * (cin >> 3) + (k >> 3)) << 6) + ((n & 7) << 3) + (k & 7);
         P[dst] = W[e];
     }
 }
 
 // ---- z-marching tcgen05 convolution --------------------------------------
-// The same implicit GEMM (M = 128 output voxels of an 8 x 16 tile, N =
-// output channels, K = 27 taps x Cin) for a whole column of tiles along z:
-// one CTA owns tile (x0, y0) for planes zb .. ze-1 and keeps the input planes
-// it needs in a ring of R shared-memory slots, each plane's tile plus its
-// one-voxel halo (10 x 18 voxels) loaded by TMA as Cin / 8 boxes of 8
-// channels, i.e. in the layout [group][y][x][8 channels]: the A operand of
-// tap (dz, dy, dx) is a descriptor view of slot(z + dz) at (dy + 1, dx + 1)
-// with core matrices one group block (2944 B) apart along K and one halo line
-// (160 B) apart along M.  A plane enters once per column (not three times
-// as with one CTA per plane), and zero padding comes from the TMA's
-// out-of-bounds fill.  The weights of the CTA's output-channel chunk stay in
-// shared memory for the whole column.  The accumulators are two TMEM
-// buffers of N columns: while the tensor cores run plane z, the four warps
-// read plane z - 1 back (bias, GELU, stores), and the slot of plane z - 2
-// refills with plane z + R - 2.  Thread 0 issues the TMA loads and the MMAs.
-// Every wait is bounded (0.5 s); a CTA that gives up sets the error word,
-// drains what it issued (again bounded), frees its TMEM and returns.
+// The implicit GEMM of a 3x3x3 convolution (M = 128 output voxels of an
+// 8 x 16 tile, K = 27 taps x Cin) for a whole column of tiles along z: one
+// CTA owns tile (x0, y0) for output planes zb .. ze-1 of one chunk of C
+// output channels and streams the input planes zb-1 .. ze through a ring of
+// R shared-memory slots, each plane's tile plus its one-voxel halo (10 x 18
+// voxels) loaded by TMA as Cin / 8 boxes of 8 channels, i.e. in the layout
+// [group][y][x][8 channels]: the A operand of in-plane shift (dy, dx) is a
+// descriptor view of the slot at (dy + 1, dx + 1) with core matrices one
+// group block (2944 B) apart along K and one halo line (160 B) apart along M.
+//
+// The three z-taps share that A operand: one MMA multiplies input plane q
+// by [W(dz=+1) | W(dz=0) | W(dz=-1)] (N = 3C), whose column blocks are the
+// contributions of plane q to output planes q-2, q-1, q (relative to zb).
+// The accumulators are a ring of S output planes in TMEM (C columns each),
+// so those three blocks are consecutive slots; an MMA whose blocks wrap past
+// the last slot is split in two.  So each input plane's operand is read 9 x
+// Cin / 16 times from shared memory instead of 27 x, and a plane is needed
+// by the MMAs of one step only.  Slots are zeroed before their first
+// writer, so every MMA accumulates.  The weights of the CTA's chunk stay in
+// shared memory for the whole column.
+//
+// Warp roles, connected by mbarriers only: warp 4 loads planes (full[slot]
+// when a plane has landed, empty[slot] when the MMAs that read it are done),
+// warp 5 issues the MMAs (accf[s] when output plane s is complete, acce[s]
+// when the epilogue has read and re-zeroed it), warps 0-3 read the
+// accumulators back (one TMEM lane, i.e. one output voxel, per thread:
+// bias, GELU, stores).  Every wait is bounded (0.5 s); a role that gives up
+// raises a shared flag the others see, and after the roles end the MMA
+// thread drains what was issued (again bounded), sets the error word, and
+// the TMEM is freed.
 // ZM_GB: bytes of one group of one plane as the TMA writes it; ZM_GP: its
 // pitch in the slot (a multiple of 128 bytes, the TMA destination alignment)
 constexpr int ZM_HX = 10, ZM_HY = 18, ZM_GB = ZM_HX * ZM_HY * 16, ZM_GP = (ZM_GB + 127) / 128 * 128, ZM_RMAX = 6;
+constexpr int ZM_THREADS = 192, ZM_SMAX = 8;
+// output-plane slots of a C-channel chunk and their TMEM columns
+__host__ __device__ constexpr int zm_slots(int c) { return 256 / c >= 8 ? 8 : (256 / c >= 4 ? 256 / c : 4); }
+__host__ __device__ constexpr int zm_tcols(int c) {
+    return zm_slots(c) * c <= 32 ? 32 : (zm_slots(c) * c <= 64 ? 64 : (zm_slots(c) * c <= 128 ? 128 : 256));
+}
 
 struct ZmArgs {
     Vol v;
@@ -175,6 +200,9 @@ struct ZmArgs {
 __device__ __forceinline__ void zm_expect(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
+__device__ __forceinline__ void zm_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
 __device__ __forceinline__ void zm_tma4(uint32_t dst, const CUtensorMap *map, int c, int x, int y, int z,
                                         uint32_t bar) {
     asm volatile(
@@ -183,16 +211,27 @@ __device__ __forceinline__ void zm_tma4(uint32_t dst, const CUtensorMap *map, in
         "l"(map), "r"(c), "r"(x), "r"(y), "r"(z), "r"(bar)
         : "memory");
 }
+__device__ __forceinline__ bool zm_failed(const int *flag) { return *reinterpret_cast<const volatile int *>(flag) != 0; }
+
+// 16 consecutive FP32 TMEM columns of this thread's lane set to zero
+__device__ __forceinline__ void tc_zero16(uint32_t taddr) {
+    const uint32_t z = 0;
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, "
+                 "%1, %1, %1};" ::"r"(taddr),
+                 "r"(z)
+                 : "memory");
+}
 
 template <int N>
-__global__ void __launch_bounds__(128) k_conv3_zm(const __grid_constant__ ZmArgs a,
-                                                 const __grid_constant__ CUtensorMap xmap) {
-    constexpr int TCOLS = 2 * N <= 32 ? 32 : (2 * N <= 64 ? 64 : (2 * N <= 128 ? 128 : 256));
+__global__ void __launch_bounds__(ZM_THREADS) k_conv3_zm(const __grid_constant__ ZmArgs a,
+                                                        const __grid_constant__ CUtensorMap xmap) {
+    constexpr int S = zm_slots(N), TCOLS = zm_tcols(N);
     extern __shared__ unsigned char zm_smem[];
-    __shared__ __align__(8) uint64_t full[ZM_RMAX];
-    __shared__ __align__(8) uint64_t done[2];
+    __shared__ __align__(8) uint64_t full[ZM_RMAX], empty[ZM_RMAX], accf[ZM_SMAX], acce[ZM_SMAX], drain;
     __shared__ uint32_t tmem_slot;
-    const int tid = threadIdx.x, warp = tid >> 5;
+    __shared__ int fail, issued_sh, waited_sh;
+    __shared__ float bias_s[96];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int groups = a.cin >> 3;
     const uint32_t slot_bytes = (uint32_t)groups * ZM_GP, plane_tx = (uint32_t)groups * ZM_GB;
     const int R = a.ring;
@@ -202,7 +241,8 @@ __global__ void __launch_bounds__(128) k_conv3_zm(const __grid_constant__ ZmArgs
     const int x0 = 8 * (col % a.tiles_x), y0 = 16 * (col / a.tiles_x);
     const int zb = zs * a.zseg, ze = min(zb + a.zseg, a.v.nz);
     const int n0 = chunk * N;
-    // shared memory: weights of the chunk (27 taps x N x cin BF16), then the ring
+    const int nplanes = ze - zb, nload = nplanes + 2;   // input planes zb - 1 .. ze
+    // shared memory: weights of the chunk (9 shifts x 3N x cin BF16), then the ring
     const uint32_t raw_addr = smem_u32(zm_smem);
     unsigned char *wsm = zm_smem + (((raw_addr + 1023u) & ~1023u) - raw_addr);
     const uint32_t wbytes = 27u * N * a.cin * 2u;
@@ -215,136 +255,174 @@ __global__ void __launch_bounds__(128) k_conv3_zm(const __grid_constant__ ZmArgs
         asm volatile("tcgen05.fence::before_thread_sync;");
     }
     if (tid == 0) {
-        for (int q = 0; q < R; ++q) mbar_init(smem_u32(&full[q]), 1);
-        mbar_init(smem_u32(&done[0]), 1);
-        mbar_init(smem_u32(&done[1]), 1);
+        for (int q = 0; q < R; ++q) {
+            mbar_init(smem_u32(&full[q]), 1);
+            mbar_init(smem_u32(&empty[q]), 1);
+        }
+        for (int b = 0; b < S; ++b) {
+            mbar_init(smem_u32(&accf[b]), 1);
+            mbar_init(smem_u32(&acce[b]), 4);   // one arrival per epilogue warp
+        }
+        fail = 0;
+        issued_sh = waited_sh = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    // the chunk's weights: per tap N x cin contiguous in the packed array
+    for (int c = tid; c < N; c += ZM_THREADS) bias_s[c] = a.bias ? __ldg(a.bias + n0 + c) : 0.0f;
+    // the chunk's packed weights are contiguous
     {
-        const uint32_t per_tap = (uint32_t)N * a.cin * 2u / 16u;   // uint4 per tap
-        for (uint32_t q = tid; q < 27u * per_tap; q += 128) {
-            const uint32_t t = q / per_tap, r = q - t * per_tap;
-            const uint4 *src = reinterpret_cast<const uint4 *>(a.P + ((long long)t * a.cin * a.cout + (long long)n0 * a.cin));
-            reinterpret_cast<uint4 *>(wsm)[q] = __ldg(src + r);
-        }
+        const uint4 *src = reinterpret_cast<const uint4 *>(a.P + (long long)chunk * 27 * N * a.cin);
+        for (uint32_t q = tid; q < wbytes / 16u; q += ZM_THREADS) reinterpret_cast<uint4 *>(wsm)[q] = __ldg(src + q);
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_slot;
-    const uint32_t idesc = tc_idesc(TC_M, N);
-    const int nplanes = ze - zb, nload = nplanes + 2;   // input planes zb - 1 .. ze
-    int issued = 0;        // planes whose loads thread 0 issued (plane q is input z = zb - 1 + q)
-    int waited = 0;        // planes thread 0 has seen land
-    auto load_plane = [&](int q) {
-        const int slot = q % R;
-        const uint32_t bar = smem_u32(&full[slot]), dst = rbase + (uint32_t)slot * slot_bytes;
-        zm_expect(bar, plane_tx);
-        for (int g = 0; g < groups; ++g)
-            zm_tma4(dst + (uint32_t)g * ZM_GP, &xmap, 8 * g, x0 - 1, y0 - 1, zb - 1 + q, bar);
-    };
-    if (tid == 0)
-        for (; issued < min(R, nload); ++issued) load_plane(issued);
-    // per-thread output voxel (TMEM lane tid)
-    const int ox = x0 + (tid & 7), oy = y0 + (tid >> 3);
-    const bool in = ox < a.v.nx && oy < a.v.ny;
-    const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
-    bool ok = true;
-    int committed = -1;    // last plane index i whose MMAs were committed
-    int drained = -1;      // last i whose MMA completion was waited
-    for (int i = 0; i <= nplanes; ++i) {
-        if (i < nplanes && tid == 0) {
-            // planes i, i + 1, i + 2 (input z - 1, z, z + 1) must have landed
-            while (waited < i + 3 && ok) {
-                ok = mbar_wait(smem_u32(&full[waited % R]), (uint32_t)((waited / R) & 1));
-                if (ok) ++waited;
-            }
-            if (ok) {
-                asm volatile("tcgen05.fence::after_thread_sync;");
-                const uint32_t dacc = tmem + (uint32_t)((i & 1) * N);
-                int first = 1;
+    if (warp < 4) {
+        // every accumulator slot starts at zero
+        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
 #pragma unroll 1
-                for (int t = 0; t < 27; ++t) {
-                    int dx, dy, dz;
-                    tap_offset(t, dx, dy, dz);
-                    const int q = i + dz + 1;
-                    const uint32_t a0 = rbase + (uint32_t)(q % R) * slot_bytes +
-                                        (uint32_t)(((dy + 1) * ZM_HX + (dx + 1)) * 16);
-                    const uint32_t b0 = wbase + (uint32_t)t * (uint32_t)(N * a.cin * 2);
-                    for (int kc = 0; kc < (a.cin >> 4); ++kc) {
-                        tc_mma(dacc, tc_sdesc(a0 + (uint32_t)(2 * kc) * ZM_GP, ZM_GP, ZM_HX * 16),
-                               tc_sdesc(b0 + 256u * kc, 128u, sbo_b(a.cin)), idesc, first ? 0 : 1);
-                        first = 0;
+        for (int c = 0; c < TCOLS; c += 16) tc_zero16(lane_addr + (uint32_t)c);
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+
+    if (warp == 4) {
+        // ---- producer: input plane q (z = zb - 1 + q) into ring slot q % R
+        if (lane == 0) {
+            int q = 0;
+            for (; q < nload; ++q) {
+                if (zm_failed(&fail)) break;
+                const int slot = q % R;
+                if (q >= R && !mbar_wait(smem_u32(&empty[slot]), (uint32_t)(((q / R) - 1) & 1))) {
+                    atomicExch(&fail, 1);
+                    break;
+                }
+                const uint32_t bar = smem_u32(&full[slot]), dst = rbase + (uint32_t)slot * slot_bytes;
+                zm_expect(bar, plane_tx);
+                for (int g = 0; g < groups; ++g)
+                    zm_tma4(dst + (uint32_t)g * ZM_GP, &xmap, 8 * g, x0 - 1, y0 - 1, zb - 1 + q, bar);
+            }
+            issued_sh = q;
+        }
+    } else if (warp == 5) {
+        // ---- MMA issue: input plane q into output planes q - 2 .. q
+        if (lane == 0) {
+            // descriptors advance by adding (byte offset >> 4) to the start field
+            const uint64_t ad0 = tc_sdesc(rbase, ZM_GP, ZM_HX * 16), bd0 = tc_sdesc(wbase, 128u, sbo_b(a.cin));
+            const int ksteps = a.cin >> 4;
+            const uint32_t shift_b = (uint32_t)(3 * N * a.cin * 2), blk_b = (uint32_t)(N * a.cin * 2);
+            int waited = 0;
+            for (int q = 0; q < nload; ++q) {
+                bool ok = !zm_failed(&fail);
+                if (ok) ok = mbar_wait(smem_u32(&full[q % R]), (uint32_t)((q / R) & 1));
+                if (ok) ++waited;
+                // output plane q's slot must have been read and re-zeroed
+                if (ok && q < nplanes && q >= S) ok = mbar_wait(smem_u32(&acce[q % S]), (uint32_t)(((q / S) - 1) & 1));
+                if (!ok) {
+                    atomicExch(&fail, 1);
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                // the valid output planes q - 2 .. q, as one or two runs of slots
+                const int olo = max(q - 2, 0), ohi = min(q, nplanes - 1);
+                const int b0 = olo - (q - 2), nb = ohi - olo + 1;
+                const int s0 = olo % S;
+                const int nb1 = min(nb, S - s0), nb2 = nb - nb1;
+                const uint32_t id1 = tc_idesc(TC_M, nb1 * N), id2 = tc_idesc(TC_M, (nb2 > 0 ? nb2 : 1) * N);
+                const uint32_t d1 = tmem + (uint32_t)(s0 * N), d2 = tmem;
+                const uint64_t ap = ad0 + (((uint32_t)(q % R) * slot_bytes) >> 4);
+#pragma unroll
+                for (int sh = 0; sh < 9; ++sh) {
+                    const int dy = sh / 3 - 1, dx = sh % 3 - 1;
+                    const uint64_t ad = ap + ((uint32_t)(((dy + 1) * ZM_HX + (dx + 1)) * 16) >> 4);
+                    const uint64_t bd = bd0 + (((uint32_t)sh * shift_b + (uint32_t)b0 * blk_b) >> 4);
+#pragma unroll 1
+                    for (int kc = 0; kc < ksteps; ++kc) {
+                        const uint64_t ak = ad + (uint64_t)((2u * ZM_GP * kc) >> 4), bk = bd + (uint64_t)((256u * kc) >> 4);
+                        tc_mma(d1, ak, bk, id1, 1);
+                        if (nb2 > 0) tc_mma(d2, ak, bk + (uint64_t)(((uint32_t)nb1 * blk_b) >> 4), id2, 1);
                     }
                 }
-                tc_commit(smem_u32(&done[i & 1]));
-                committed = i;
+                // the slot refills only if a later plane goes there
+                if (q + R < nload) tc_commit(smem_u32(&empty[q % R]));
+                // output plane q - 2 has all its contributions
+                if (q >= 2) tc_commit(smem_u32(&accf[(q - 2) % S]));
             }
+            waited_sh = waited;
         }
-        if (i > 0) {
-            const int j = i - 1;   // the plane read back now
-            bool got = mbar_wait(smem_u32(&done[j & 1]), (uint32_t)((j >> 1) & 1));
-            ok = ok && got;
-            if (got) drained = j;
-            // plane j's MMAs are done: its first input plane's slot refills
-            if (tid == 0 && ok && issued < nload && issued == j + R) {
-                load_plane(issued);
-                ++issued;
+    } else {
+        // ---- epilogue: thread tid reads TMEM lane tid = output voxel (x0 + tid % 8, y0 + tid / 8)
+        const int ox = x0 + (tid & 7), oy = y0 + (tid >> 3);
+        const bool in = ox < a.v.nx && oy < a.v.ny;
+        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+        const float hb = a.head ? __ldg(a.head + 16) : 0.0f;
+        for (int j = 0; j < nplanes; ++j) {
+            const int sl = j % S;
+            if (zm_failed(&fail) || !mbar_wait(smem_u32(&accf[sl]), (uint32_t)((j / S) & 1))) {
+                atomicExch(&fail, 1);
+                break;
             }
-            if (ok) {
-                asm volatile("tcgen05.fence::after_thread_sync;");
-                const int z = zb + j;
-                const long long vox = ox + (long long)a.v.nx * (oy + (long long)a.v.ny * z);
-                float hs = 0.0f;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const int z = zb + j;
+            const long long vox = ox + (long long)a.v.nx * (oy + (long long)a.v.ny * z);
+            float hs = hb;
 #pragma unroll
-                for (int c0 = 0; c0 < N; c0 += 16) {
-                    float acc[16];
-                    tc_ld16(lane_addr + (uint32_t)((j & 1) * N + c0), acc);
-                    if (in) {
-                        float zz[16];
+            for (int c0 = 0; c0 < N; c0 += 16) {
+                float acc[16];
+                tc_ld16(lane_addr + (uint32_t)(sl * N + c0), acc);
+                tc_zero16(lane_addr + (uint32_t)(sl * N + c0));
+                if (in) {
+                    float zz[16];
 #pragma unroll
-                        for (int q = 0; q < 16; ++q) zz[q] = acc[q] + (a.bias ? __ldg(a.bias + n0 + c0 + q) : 0.0f);
-                        if (a.Z) {
-                            float4 *zr = reinterpret_cast<float4 *>(a.Z + vox * a.cout + n0 + c0);
+                    for (int q = 0; q < 16; ++q) zz[q] = acc[q] + bias_s[c0 + q];
+                    if (a.Z) {
+                        float4 *zr = reinterpret_cast<float4 *>(a.Z + vox * a.cout + n0 + c0);
 #pragma unroll
-                            for (int q = 0; q < 4; ++q)
-                                zr[q] = make_float4(zz[4 * q], zz[4 * q + 1], zz[4 * q + 2], zz[4 * q + 3]);
-                        }
+                        for (int q = 0; q < 4; ++q)
+                            zr[q] = make_float4(zz[4 * q], zz[4 * q + 1], zz[4 * q + 2], zz[4 * q + 3]);
+                    }
+                    if (a.Y || a.head) {
+                        float gz[16];
+#pragma unroll
+                        for (int q = 0; q < 16; ++q) gz[q] = a.act ? gelu(zz[q]) : zz[q];
                         if (a.Y) {
                             __align__(16) bf16 yb[16];
 #pragma unroll
-                            for (int q = 0; q < 16; ++q) yb[q] = __float2bfloat16_rn(a.act ? gelu(zz[q]) : zz[q]);
+                            for (int q = 0; q < 16; ++q) yb[q] = __float2bfloat16_rn(gz[q]);
                             uint4 *yr = reinterpret_cast<uint4 *>(a.Y + vox * a.cout + n0 + c0);
                             yr[0] = reinterpret_cast<const uint4 *>(yb)[0];
                             yr[1] = reinterpret_cast<const uint4 *>(yb)[1];
                         }
                         if (a.head) {
-                            if (c0 == 0) hs = __ldg(a.head + 16);
 #pragma unroll
-                            for (int q = 0; q < 16; ++q) hs += gelu(zz[q]) * __ldg(a.head + c0 + q);
+                            for (int q = 0; q < 16; ++q) hs += gz[q] * __ldg(a.head + c0 + q);
                         }
                     }
                 }
-                if (a.head && in) {
-                    if (a.raw) a.raw[vox] = hs;
-                    if (a.out) a.out[vox] = hs * __ldg(a.scales + 1);
-                }
-                asm volatile("tcgen05.fence::before_thread_sync;");
             }
-        }
-        if (!__syncthreads_and(ok)) {
-            ok = false;
-            break;
+            if (a.head && in) {
+                if (a.raw) a.raw[vox] = hs;
+                if (a.out) a.out[vox] = hs * __ldg(a.scales + 1);
+            }
+            // the slot is free (and zero) once all four warps are through
+            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncwarp();
+            if (lane == 0) zm_arrive(smem_u32(&acce[sl]));
         }
     }
-    if (!ok) {
-        // drain what was issued before giving up (bounded), then report
-        if (tid == 0) {
-            for (; waited < issued; ++waited) mbar_wait(smem_u32(&full[waited % R]), (uint32_t)((waited / R) & 1));
-            if (committed > drained) mbar_wait(smem_u32(&done[committed & 1]), (uint32_t)((committed >> 1) & 1));
-            atomicExch(a.err, 1);
-        }
+    __syncthreads();
+    if (fail && tid == 5 * 32) {
+        // drain the loads and MMAs issued before the roles gave up (bounded):
+        // every issued plane lands, and a last commit tracks all the MMAs
+        for (int q = waited_sh; q < issued_sh; ++q) mbar_wait(smem_u32(&full[q % R]), (uint32_t)((q / R) & 1));
+        mbar_init(smem_u32(&drain), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        tc_commit(smem_u32(&drain));
+        mbar_wait(smem_u32(&drain), 0);
+        atomicExch(a.err, 1);
     }
     __syncthreads();
     if (warp == 0) {
@@ -558,20 +636,31 @@ __global__ void k_gather_rows(int cin_real, int cin, int cout, const float *__re
     }
 }
 
-// 2x average pooling (channels-last)
+// 2x average pooling (channels-last): one thread per coarse voxel and
+// 8-channel group (16-byte loads and stores)
 __global__ void k_pool(Vol c, int C, const bf16 *__restrict__ X, bf16 *__restrict__ Y) {
-    const long long n = c.n() * C;
+    const int G = C >> 3;
+    const long long n = c.n() * G;
     const int fx = 2 * c.nx, fy = 2 * c.ny;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const long long vv = i / C;
-        const int ch = (int)(i % C);
-        const int x = (int)(vv % c.nx), y = (int)((vv / c.nx) % c.ny), z = (int)(vv / ((long long)c.nx * c.ny));
-        float s = 0.f;
+        const long long vv = i / G;
+        const int g = (int)(i - vv * G);
+        const int x = (int)(vv % c.nx);
+        const long long yz = vv / c.nx;
+        const int y = (int)(yz % c.ny), z = (int)(yz / c.ny);
+        float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
         for (int q = 0; q < 8; ++q) {
             const long long f = (2 * x + (q & 1)) + (long long)fx * ((2 * y + ((q >> 1) & 1)) + (long long)fy * (2 * z + (q >> 2)));
-            s += __bfloat162float(X[f * C + ch]);
+            const uint4 u = __ldg(reinterpret_cast<const uint4 *>(X + f * C) + g);
+            const bf16 *e = reinterpret_cast<const bf16 *>(&u);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) s[k] += __bfloat162float(e[k]);
         }
-        Y[i] = __float2bfloat16_rn(s * 0.125f);
+        __align__(16) bf16 o[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) o[k] = __float2bfloat16_rn(s[k] * 0.125f);
+        reinterpret_cast<uint4 *>(Y + vv * C)[g] = *reinterpret_cast<const uint4 *>(o);
     }
 }
 __global__ void k_pool_grad(Vol c, int C, const float *__restrict__ dY, float *__restrict__ dX, int accumulate) {
@@ -590,21 +679,27 @@ __global__ void k_pool_grad(Vol c, int C, const float *__restrict__ dY, float *_
 }
 
 // nearest 2x upsampling of X (C1 channels) into channels [0, C1) of the
-// concat buffer Y (C1 + C2 channels); channels [C1, C1 + C2) take the skip S
+// concat buffer Y (C1 + C2 channels); channels [C1, C1 + C2) take the skip S.
+// One thread per fine voxel and 8-channel group of Y (16-byte moves).
 __global__ void k_up_concat(Vol f, int C1, int C2, const bf16 *__restrict__ X, const bf16 *__restrict__ S,
                             bf16 *__restrict__ Y) {
-    const int C = C1 + C2;
-    const long long n = f.n() * C;
+    const int C = C1 + C2, G = C >> 3, G1 = C1 >> 3, G2 = C2 >> 3;
+    const long long n = f.n() * G;
     const int cx = f.nx / 2, cy = f.ny / 2;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const long long vv = i / C;
-        const int ch = (int)(i % C);
-        if (ch < C1) {
-            const int x = (int)(vv % f.nx), y = (int)((vv / f.nx) % f.ny), z = (int)(vv / ((long long)f.nx * f.ny));
-            Y[i] = X[((x / 2) + (long long)cx * ((y / 2) + (long long)cy * (z / 2))) * C1 + ch];
+        const long long vv = i / G;
+        const int g = (int)(i - vv * G);
+        uint4 val;
+        if (g < G1) {
+            const int x = (int)(vv % f.nx);
+            const long long yz = vv / f.nx;
+            const int y = (int)(yz % f.ny), z = (int)(yz / f.ny);
+            val = __ldg(reinterpret_cast<const uint4 *>(X + ((x / 2) + (long long)cx * ((y / 2) + (long long)cy * (z / 2))) * C1) + g);
         } else {
-            Y[i] = S[vv * C2 + (ch - C1)];
+            val = __ldg(reinterpret_cast<const uint4 *>(S + vv * C2) + (g - G1));
         }
+        reinterpret_cast<uint4 *>(Y + vv * C)[g] = val;
+        (void)G2;
     }
 }
 // backward of k_up_concat: dX (coarse, C1) = sum over the 8 children, and
@@ -634,16 +729,21 @@ __global__ void k_skip_grad_add(long long nvox, int C1, int C2, const float *__r
     }
 }
 
-// network input: channels (b / sb, mask, p_prev / sp, 0 ... 0), 16 wide
+// network input: channels (b / sb, mask, p_prev / sp, 0 ... 0), 16 wide,
+// one voxel per thread (two 16-byte stores)
 __global__ void k_input(long long n, const float *__restrict__ b, const uint8_t *__restrict__ mask,
                         const float *__restrict__ pp, const float *__restrict__ scales, bf16 *__restrict__ X) {
     const float isb = 1.0f / scales[0], isp = 1.0f / scales[1];
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
-        bf16 *x = X + v * 16;
+        __align__(16) bf16 x[16];
         x[0] = __float2bfloat16_rn(b[v] * isb);
         x[1] = __float2bfloat16_rn(mask ? (float)mask[v] : 0.0f);
         x[2] = __float2bfloat16_rn(pp ? pp[v] * isp : 0.0f);
+#pragma unroll
         for (int c = 3; c < 16; ++c) x[c] = __float2bfloat16_rn(0.0f);
+        uint4 *dst = reinterpret_cast<uint4 *>(X + v * 16);
+        dst[0] = reinterpret_cast<const uint4 *>(x)[0];
+        dst[1] = reinterpret_cast<const uint4 *>(x)[1];
     }
 }
 
@@ -760,7 +860,7 @@ int launch_zm(const ZmArgs &a, const CUtensorMap &map, int nchunks, size_t smem,
         configured = smem;
     }
     const long long blocks = (long long)a.ncol * a.nzseg * nchunks;
-    k_conv3_zm<N><<<(unsigned)blocks, TC_M, smem, s>>>(a, map);
+    k_conv3_zm<N><<<(unsigned)blocks, ZM_THREADS, smem, s>>>(a, map);
     return post("conv3 z-march");
 }
 
@@ -773,28 +873,29 @@ int launch_conv(int cout, Vol v, const bf16 *X, int cin, const bf16 *W, const fl
                 float *out = nullptr, float *raw = nullptr) {
     if (cin % 16 || cin > 96) return ff_set_error(FF_E_ARG, "unet: conv input channels %d (multiples of 16 to 96)", cin);
     if (cout % 16 || cout > 96) return ff_set_error(FF_E_ARG, "unet: conv output channels %d (multiples of 16 to 96)", cout);
-    k_pack_b<<<gblocks(27LL * cin * cout), 256, 0, s>>>(cin, cout, W, pk);
-    FF_TRY(post("pack weights"));
-    // the output-channel chunk: the widest whose weights and a ring of 4
-    // planes fit two CTAs per SM, else one CTA per SM; then the deepest
-    // ring that keeps that occupancy
-    const size_t two = 110 * 1024, one = 220 * 1024;
+    // the output-channel chunk C (3C <= 256 columns per MMA): the widest
+    // whose weights and a ring of 3 planes fit two CTAs per SM, else one;
+    // then the deepest ring that keeps that occupancy.  CTAs per SM are also
+    // bounded by TMEM (512 columns per SM).
+    const size_t two = 113 * 1024, one = 220 * 1024;
     int n = 0, occ = 0;
     for (int pass = 0; pass < 2 && !n; ++pass)
         for (int d : {1, 2, 3, 4, 6}) {
-            if (cout % d || (cout / d) % 16) continue;
-            if (zm_smem_bytes(cout / d, cin, 4) <= (pass == 0 ? two : one)) {
+            if (cout % d || (cout / d) % 16 || cout / d > 80) continue;
+            if (zm_smem_bytes(cout / d, cin, 3) <= (pass == 0 ? two : one)) {
                 n = cout / d;
                 occ = pass == 0 ? 2 : 1;
                 break;
             }
         }
     if (!n) return ff_set_error(FF_E_LIMIT, "unet: no shared-memory plan for a %d -> %d convolution", cin, cout);
+    k_pack_b<<<gblocks(27LL * cin * cout), 256, 0, s>>>(cin, cout, n, W, pk);
+    FF_TRY(post("pack weights"));
     const size_t budget = occ == 2 ? two : one;
-    int ring = 4;
+    int ring = 3;
     while (ring < ZM_RMAX && zm_smem_bytes(n, cin, ring + 1) <= budget) ++ring;
     const size_t smem = zm_smem_bytes(n, cin, ring);
-    const int blocks_per_sm = std::max(1, std::min(8, (int)(228 * 1024 / (smem + 2048))));
+    const int blocks_per_sm = std::max(1, std::min({8, (int)(228 * 1024 / (smem + 2048)), 512 / zm_tcols(n)}));
     ZmArgs a;
     a.v = v;
     a.cin = cin;
@@ -846,7 +947,6 @@ int launch_conv(int cout, Vol v, const bf16 *X, int cin, const bf16 *W, const fl
     case 32: return launch_zm<32>(a, map, nchunks, smem, s);
     case 48: return launch_zm<48>(a, map, nchunks, smem, s);
     case 64: return launch_zm<64>(a, map, nchunks, smem, s);
-    case 96: return launch_zm<96>(a, map, nchunks, smem, s);
     default: return ff_set_error(FF_E_ARG, "unet: no conv kernel for a %d-channel chunk", n);
     }
 }
@@ -908,6 +1008,7 @@ struct ff_unet_s {
     bf16 *gbuf = nullptr;           // BF16 GEMM operand for backward
     float *raw = nullptr, *draw = nullptr, *scales = nullptr;
     double *partial = nullptr;
+    bool has_train = false;         // pre, grad, gbuf, raw, draw allocated
     std::vector<void *> owned;
 };
 
@@ -929,6 +1030,7 @@ static void free_shape(ff_unet u) {
     u->raw = u->draw = u->scales = nullptr;
     u->partial = nullptr;
     u->vol = Vol{0, 0, 0};
+    u->has_train = false;
 }
 
 static int alloc_owned(ff_unet u, void **p, size_t bytes) {
@@ -937,33 +1039,46 @@ static int alloc_owned(ff_unet u, void **p, size_t bytes) {
     return FF_OK;
 }
 
-static int ensure_shape(ff_unet u, Vol v) {
-    if (u->vol.nx == v.nx && u->vol.ny == v.ny && u->vol.nz == v.nz) return FF_OK;
+// activations for a volume; with train, also the FP32 pre-activations and
+// gradient buffers of the backward pass (inference never allocates them)
+static int ensure_shape(ff_unet u, Vol v, bool train) {
+    const bool same = u->vol.nx == v.nx && u->vol.ny == v.ny && u->vol.nz == v.nz;
+    if (same && (!train || u->has_train)) return FF_OK;
     FF_CHECK(v.nx % 4 == 0 && v.ny % 4 == 0 && v.nz % 4 == 0 && v.nx >= 4 && v.ny >= 4 && v.nz >= 4, FF_E_ARG,
              "unet: resolution must be a multiple of 4 on every axis, got %dx%dx%d", v.nx, v.ny, v.nz);
-    free_shape(u);
-    u->vol = v;
+    if (!same) {
+        free_shape(u);
+        u->vol = v;
+    }
     const long long n0 = v.n();
-    u->act.resize(15);
-    u->grad.resize(15);
-    long long maxc = 0;
-    for (int s = 0; s < 15; ++s) {
-        const long long nv = n0 >> (3 * SLOT_LEVEL[s]);
-        FF_TRY(alloc_owned(u, (void **)&u->act[s], (size_t)nv * SLOT_C[s] * sizeof(bf16)));
-        FF_TRY(alloc_owned(u, (void **)&u->grad[s], (size_t)nv * SLOT_C[s] * sizeof(float)));
-        maxc = std::max(maxc, nv * SLOT_C[s]);
+    if (u->act.empty()) {
+        u->act.resize(15);
+        for (int s = 0; s < 15; ++s) {
+            const long long nv = n0 >> (3 * SLOT_LEVEL[s]);
+            FF_TRY(alloc_owned(u, (void **)&u->act[s], (size_t)nv * SLOT_C[s] * sizeof(bf16)));
+        }
+        FF_TRY(alloc_owned(u, (void **)&u->scales, 16));
+        FF_TRY(alloc_owned(u, (void **)&u->partial, sizeof(double) * 152 * 32));
     }
-    u->pre.resize(10);
-    for (int l = 0; l < 10; ++l) {
-        const int s = CONV_OUT[l];
-        const long long nv = n0 >> (3 * SLOT_LEVEL[s]);
-        FF_TRY(alloc_owned(u, (void **)&u->pre[l], (size_t)nv * SLOT_C[s] * sizeof(float)));
+    if (train && !u->has_train) {
+        u->grad.resize(15);
+        long long maxc = 0;
+        for (int s = 0; s < 15; ++s) {
+            const long long nv = n0 >> (3 * SLOT_LEVEL[s]);
+            FF_TRY(alloc_owned(u, (void **)&u->grad[s], (size_t)nv * SLOT_C[s] * sizeof(float)));
+            maxc = std::max(maxc, nv * SLOT_C[s]);
+        }
+        u->pre.resize(10);
+        for (int l = 0; l < 10; ++l) {
+            const int s = CONV_OUT[l];
+            const long long nv = n0 >> (3 * SLOT_LEVEL[s]);
+            FF_TRY(alloc_owned(u, (void **)&u->pre[l], (size_t)nv * SLOT_C[s] * sizeof(float)));
+        }
+        FF_TRY(alloc_owned(u, (void **)&u->gbuf, (size_t)maxc * sizeof(bf16)));
+        FF_TRY(alloc_owned(u, (void **)&u->raw, (size_t)n0 * 4));
+        FF_TRY(alloc_owned(u, (void **)&u->draw, (size_t)n0 * 4));
+        u->has_train = true;
     }
-    FF_TRY(alloc_owned(u, (void **)&u->gbuf, (size_t)maxc * sizeof(bf16)));
-    FF_TRY(alloc_owned(u, (void **)&u->raw, (size_t)n0 * 4));
-    FF_TRY(alloc_owned(u, (void **)&u->draw, (size_t)n0 * 4));
-    FF_TRY(alloc_owned(u, (void **)&u->scales, 16));
-    FF_TRY(alloc_owned(u, (void **)&u->partial, sizeof(double) * 152 * 32));
     return FF_OK;
 }
 
@@ -1127,16 +1242,16 @@ static int forward(ff_unet u, const float *b, const uint8_t *mask, const float *
     };
     FF_TRY(conv(0));
     FF_TRY(conv(1));
-    k_pool<<<gblocks(level_vol(u, 1).n() * 16), 256, 0, s>>>(level_vol(u, 1), 16, u->act[2], u->act[3]);
+    k_pool<<<gblocks(level_vol(u, 1).n() * 2), 256, 0, s>>>(level_vol(u, 1), 16, u->act[2], u->act[3]);
     FF_TRY(conv(2));
     FF_TRY(conv(3));
-    k_pool<<<gblocks(level_vol(u, 2).n() * 32), 256, 0, s>>>(level_vol(u, 2), 32, u->act[5], u->act[6]);
+    k_pool<<<gblocks(level_vol(u, 2).n() * 4), 256, 0, s>>>(level_vol(u, 2), 32, u->act[5], u->act[6]);
     FF_TRY(conv(4));
     FF_TRY(conv(5));
-    k_up_concat<<<gblocks(level_vol(u, 1).n() * 96), 256, 0, s>>>(level_vol(u, 1), 64, 32, u->act[8], u->act[5], u->act[9]);
+    k_up_concat<<<gblocks(level_vol(u, 1).n() * 12), 256, 0, s>>>(level_vol(u, 1), 64, 32, u->act[8], u->act[5], u->act[9]);
     FF_TRY(conv(6));
     FF_TRY(conv(7));
-    k_up_concat<<<gblocks(n0 * 48), 256, 0, s>>>(level_vol(u, 0), 32, 16, u->act[11], u->act[2], u->act[12]);
+    k_up_concat<<<gblocks(n0 * 6), 256, 0, s>>>(level_vol(u, 0), 32, 16, u->act[11], u->act[2], u->act[12]);
     FF_TRY(conv(8));
     FF_TRY(conv(9));
     return post("unet forward");
@@ -1219,7 +1334,7 @@ extern "C" int ff_unet_forward(ff_unet u, const int *res, double h, ff_field b, 
                                ff_field out) {
     FF_CHECK(u && res, FF_E_ARG, "NULL argument");
     cudaSetDevice(u->ctx->device);
-    FF_TRY(ensure_shape(u, Vol{res[0], res[1], res[2]}));
+    FF_TRY(ensure_shape(u, Vol{res[0], res[1], res[2]}, false));
     const long long n = u->vol.n();
     FF_CHECK(field_ok(b, n, FF_FLOAT) && field_ok(out, n, FF_FLOAT) && (!p_prev || field_ok(p_prev, n, FF_FLOAT)) &&
                  (!mask || field_ok(mask, n, FF_UINT8)),
@@ -1235,7 +1350,7 @@ extern "C" int ff_unet_loss_backward(ff_unet u, const int *res, double h, ff_fie
                                      ff_field target, double *loss) {
     FF_CHECK(u && res && target, FF_E_ARG, "NULL argument");
     cudaSetDevice(u->ctx->device);
-    FF_TRY(ensure_shape(u, Vol{res[0], res[1], res[2]}));
+    FF_TRY(ensure_shape(u, Vol{res[0], res[1], res[2]}, true));
     const long long n = u->vol.n();
     FF_CHECK(field_ok(b, n, FF_FLOAT) && field_ok(target, n, FF_FLOAT) && (!p_prev || field_ok(p_prev, n, FF_FLOAT)) &&
                  (!mask || field_ok(mask, n, FF_UINT8)),
