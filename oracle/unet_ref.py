@@ -1,6 +1,7 @@
 """Oracle (test infrastructure only): the warm-start U-Net in PyTorch on the
 CPU in FP32, rounding to BF16 at the points where the GPU stores BF16 (the
-normalised input, each convolution's weights and GELU output except the
+normalised input, each convolution's weights and GELU output (the tanh form
+of GELU, as the GPU computes it) except the
 last one, which feeds the FP32 head directly, pooled and upsampled
 activations, and the gradient of every convolution's pre-activation).  Used to check the GPU forward pass, the loss gradients and
 the Adam update (Kingma & Ba 2015).
@@ -86,7 +87,7 @@ def forward(params, b, mask, p_prev, h, shape, requires_grad=False):
         wt = bf16(w).permute(4, 3, 0, 1, 2)   # [co][ci][dz][dy][dx]
         z = F.conv3d(inp, wt, padding=1) + bb.view(1, -1, 1, 1, 1)
         z = _RoundGrad.apply(z)
-        y = F.gelu(z)
+        y = F.gelu(z, approximate="tanh")
         return bf16(y) if store_bf16 else y
 
     e0 = conv(1, conv(0, x))

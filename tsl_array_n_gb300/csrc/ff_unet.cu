@@ -26,11 +26,23 @@ typedef __nv_bfloat16 bf16;
 namespace {
 
 
-__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+// GELU in its tanh form, 0.5 x (1 + tanh(sqrt(2 / pi) (x + 0.044715 x^3)))
+// (Hendrycks & Gimpel 2016), with the hardware tanh approximation; the
+// derivative of the same expression for the backward pass
+__device__ __forceinline__ float tanh_hw(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+constexpr float GELU_K0 = 0.7978845608028654f, GELU_K1 = 0.044715f;
+__device__ __forceinline__ float gelu(float x) {
+    const float t = tanh_hw(GELU_K0 * __fmaf_rn(GELU_K1 * x, x * x, x));
+    return 0.5f * x * (1.0f + t);
+}
 __device__ __forceinline__ float gelu_grad(float x) {
-    const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
-    const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
-    return cdf + x * pdf;
+    const float x2 = x * x;
+    const float t = tanh_hw(GELU_K0 * __fmaf_rn(GELU_K1 * x, x2, x));
+    return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * GELU_K0 * __fmaf_rn(3.0f * GELU_K1, x2, 1.0f);
 }
 
 struct Vol {
@@ -787,19 +799,64 @@ __global__ void k_head_grad(long long n, const float *__restrict__ Zin, const fl
     if (threadIdx.x < 17) atomicAdd(&dw[threadIdx.x], sw[threadIdx.x]);
 }
 
-// per-field RMS (deterministic two-level reduction into FP64 partials)
-__global__ void k_sumsq(long long n, const float *__restrict__ a, double *__restrict__ partial) {
-    __shared__ double sred[256];
-    double acc = 0.0;
-    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x)
-        acc += (double)a[v] * a[v];
-    sred[threadIdx.x] = acc;
+// per-field sums of squares of b and p_prev (deterministic two-level
+// reduction: FP64 block partials, then k_scales in one block)
+__global__ void k_sumsq2(long long n, const float *__restrict__ a, const float *__restrict__ c,
+                         double *__restrict__ partial) {
+    // each thread sums a few dozen squares in FP32, the block in FP32, the
+    // blocks in FP64 (k_scales)
+    __shared__ float sa[256], sc[256];
+    float xa = 0.0f, xc = 0.0f;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
+        const float p = a[v];
+        xa = __fmaf_rn(p, p, xa);
+        if (c) {
+            const float q = c[v];
+            xc = __fmaf_rn(q, q, xc);
+        }
+    }
+    sa[threadIdx.x] = xa;
+    sc[threadIdx.x] = xc;
     __syncthreads();
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) sred[threadIdx.x] += sred[threadIdx.x + s];
+        if (threadIdx.x < s) {
+            sa[threadIdx.x] += sa[threadIdx.x + s];
+            sc[threadIdx.x] += sc[threadIdx.x + s];
+        }
         __syncthreads();
     }
-    if (threadIdx.x == 0) partial[blockIdx.x] = sred[0];
+    if (threadIdx.x == 0) {
+        partial[2 * blockIdx.x] = sa[0];
+        partial[2 * blockIdx.x + 1] = sc[0];
+    }
+}
+// normalisation scales: sb = rms(b), sp = rms(p_prev), or rms(b) L^2 /
+// (4 pi^2) (L the smallest domain extent) when p_prev is zero or absent;
+// one block of 256 threads
+__global__ void k_scales(int nb, long long n, double L2, const double *__restrict__ partial, float *__restrict__ scales) {
+    __shared__ double sa[256], sc[256];
+    double xa = 0.0, xc = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+        xa += partial[2 * b];
+        xc += partial[2 * b + 1];
+    }
+    sa[threadIdx.x] = xa;
+    sc[threadIdx.x] = xc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            sa[threadIdx.x] += sa[threadIdx.x + s];
+            sc[threadIdx.x] += sc[threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double sb = sqrt(sa[0] / (double)n);
+        double sp = sqrt(sc[0] / (double)n);
+        if (!(sp > 0)) sp = sb * L2 / (4.0 * 3.14159265358979323846 * 3.14159265358979323846);
+        scales[0] = (float)(sb > 0 ? sb : 1.0);
+        scales[1] = (float)(sp > 0 ? sp : 1.0);
+    }
 }
 
 // Adam (Kingma & Ba 2015) on the FP32 master weights
@@ -1191,31 +1248,16 @@ extern "C" int ff_unet_get_grads(ff_unet u, float *host, int64_t n) {
     return FF_OK;
 }
 
-// normalisation scales: sb = rms(b), sp = rms(p_prev), or rms(b) L^2 / (4 pi^2)
-// (L the smallest domain extent) when p_prev is zero or absent
-static int compute_scales(ff_unet u, const float *b, const float *pp, double h, float out[2]) {
+// normalisation scales into u->scales on the device (no host round trip)
+static int compute_scales(ff_unet u, const float *b, const float *pp, double h) {
     cudaStream_t s = u->ctx->stream;
     const long long n = u->vol.n();
-    const int nb = std::min(152 * 32, gblocks(n));
-    std::vector<double> hp(nb);
-    double sums[2] = {0, 0};
-    const float *arr[2] = {b, pp};
-    for (int q = 0; q < 2; ++q) {
-        if (!arr[q]) continue;
-        k_sumsq<<<nb, 256, 0, s>>>(n, arr[q], u->partial);
-        FF_TRY(post("sumsq"));
-        FF_CUDA(cudaMemcpyAsync(hp.data(), u->partial, sizeof(double) * nb, cudaMemcpyDeviceToHost, s));
-        FF_CUDA(cudaStreamSynchronize(s));
-        for (double x : hp) sums[q] += x;
-    }
-    const double sb = std::sqrt(sums[0] / n);
-    double sp = std::sqrt(sums[1] / n);
+    const int nb = std::min(152 * 16, gblocks(n));
+    k_sumsq2<<<nb, 256, 0, s>>>(n, b, pp, u->partial);
+    FF_TRY(post("sumsq"));
     const double L = h * std::min(u->vol.nx, std::min(u->vol.ny, u->vol.nz));
-    if (!(sp > 0)) sp = sb * L * L / (4.0 * M_PI * M_PI);
-    out[0] = (float)(sb > 0 ? sb : 1.0);
-    out[1] = (float)(sp > 0 ? sp : 1.0);
-    FF_CUDA(cudaMemcpyAsync(u->scales, out, 8, cudaMemcpyHostToDevice, s));
-    return FF_OK;
+    k_scales<<<1, 256, 0, s>>>(nb, n, L * L, u->partial, u->scales);
+    return post("scales");
 }
 
 static Vol level_vol(ff_unet u, int lev) { return Vol{u->vol.nx >> lev, u->vol.ny >> lev, u->vol.nz >> lev}; }
@@ -1227,8 +1269,7 @@ static Vol level_vol(ff_unet u, int lev) { return Vol{u->vol.nx >> lev, u->vol.n
 static int forward(ff_unet u, const float *b, const uint8_t *mask, const float *pp, double h, float *out,
                    bool train) {
     cudaStream_t s = u->ctx->stream;
-    float sc[2];
-    FF_TRY(compute_scales(u, b, pp, h, sc));
+    FF_TRY(compute_scales(u, b, pp, h));
     const long long n0 = u->vol.n();
     k_input<<<gblocks(n0), 256, 0, s>>>(n0, b, mask, pp, u->scales, u->act[0]);
     auto conv = [&](int l) {
