@@ -50,6 +50,15 @@ struct Vol {
     __host__ __device__ long long n() const { return (long long)nx * ny * nz; }
 };
 
+// BF16 activations are stored as planes of 8-channel groups: channel c of
+// voxel v (x-fastest index over a volume of n voxels) at element
+// ((c / 8) n + v) 8 + c % 8.  A group plane is a plain volume of 16-byte
+// voxels, so a TMA box of one group reads whole rows of the tile, and a
+// concatenation along channels is a run of consecutive group planes.
+__host__ __device__ __forceinline__ long long g8(long long v, int c, long long n) {
+    return ((long long)(c >> 3) * n + v) * 8 + (c & 7);
+}
+
 // offset of tap t (0..26) in (dz, dy, dx) = (t/9 - 1, (t/3)%3 - 1, t%3 - 1)
 __device__ __forceinline__ void tap_offset(int t, int &dx, int &dy, int &dz) {
     dz = t / 9 - 1;
@@ -156,8 +165,10 @@ __global__ void k_pack_b(int cin, int cout, int C, const bf16 *__restrict__ W, b
 // CTA owns tile (x0, y0) for output planes zb .. ze-1 of one chunk of C
 // output channels and streams the input planes zb-1 .. ze through a ring of
 // R shared-memory slots, each plane's tile plus its one-voxel halo (10 x 18
-// voxels) loaded by TMA as Cin / 8 boxes of 8 channels, i.e. in the layout
-// [group][y][x][8 channels]: the A operand of in-plane shift (dy, dx) is a
+// voxels) loaded by TMA as Cin / 8 boxes, one per 8-channel group plane of
+// the input, i.e. in the layout [group][y][x][8 channels] (each box row is
+// 10 voxels x 16 bytes, contiguous in the group plane): the A operand of
+// in-plane shift (dy, dx) is a
 // descriptor view of the slot at (dy + 1, dx + 1) with core matrices one
 // group block (2944 B) apart along K and one halo line (160 B) apart along M.
 //
@@ -185,8 +196,9 @@ __global__ void k_pack_b(int cin, int cout, int C, const bf16 *__restrict__ W, b
 // pitch in the slot (a multiple of 128 bytes, the TMA destination alignment)
 constexpr int ZM_HX = 10, ZM_HY = 18, ZM_GB = ZM_HX * ZM_HY * 16, ZM_GP = (ZM_GB + 127) / 128 * 128, ZM_RMAX = 6;
 constexpr int ZM_THREADS = 192, ZM_SMAX = 8;
-// output-plane slots of a C-channel chunk and their TMEM columns
-__host__ __device__ constexpr int zm_slots(int c) { return 256 / c >= 8 ? 8 : (256 / c >= 4 ? 256 / c : 4); }
+// output-plane slots of a C-channel chunk (four: the three an MMA writes and
+// the one the epilogue reads) and their TMEM columns
+__host__ __device__ constexpr int zm_slots(int) { return 4; }
 __host__ __device__ constexpr int zm_tcols(int c) {
     return zm_slots(c) * c <= 32 ? 32 : (zm_slots(c) * c <= 64 ? 64 : (zm_slots(c) * c <= 128 ? 128 : 256));
 }
@@ -202,7 +214,7 @@ struct ZmArgs {
     const bf16 *P;      // weights packed for the B operand (k_pack_b), all cout
     const float *bias;  // cout or null
     float *Z;           // FP32 result before the activation (stride cout) or null
-    bf16 *Y;            // BF16 activated result (stride cout) or null
+    bf16 *Y;            // BF16 activated result (8-channel group planes) or null
     const float *head;  // 1x1 head (16 weights + bias) fused into the epilogue, or null
     const float *scales;
     float *out, *raw;   // head outputs: out = scales[1] raw
@@ -215,12 +227,14 @@ __device__ __forceinline__ void zm_expect(uint32_t bar, uint32_t bytes) {
 __device__ __forceinline__ void zm_arrive(uint32_t bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
-__device__ __forceinline__ void zm_tma4(uint32_t dst, const CUtensorMap *map, int c, int x, int y, int z,
+// one 8-channel group plane's box (8 channels x 10 x 18 x 1 x 1) at (x, y, z, group)
+__device__ __forceinline__ void zm_tma5(uint32_t dst, const CUtensorMap *map, int x, int y, int z, int g,
                                         uint32_t bar) {
+    const int c = 0;
     asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
-        "l"(map), "r"(c), "r"(x), "r"(y), "r"(z), "r"(bar)
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(dst),
+        "l"(map), "r"(c), "r"(x), "r"(y), "r"(z), "r"(g), "r"(bar)
         : "memory");
 }
 __device__ __forceinline__ bool zm_failed(const int *flag) { return *reinterpret_cast<const volatile int *>(flag) != 0; }
@@ -314,7 +328,7 @@ __global__ void __launch_bounds__(ZM_THREADS) k_conv3_zm(const __grid_constant__
                 const uint32_t bar = smem_u32(&full[slot]), dst = rbase + (uint32_t)slot * slot_bytes;
                 zm_expect(bar, plane_tx);
                 for (int g = 0; g < groups; ++g)
-                    zm_tma4(dst + (uint32_t)g * ZM_GP, &xmap, 8 * g, x0 - 1, y0 - 1, zb - 1 + q, bar);
+                    zm_tma5(dst + (uint32_t)g * ZM_GP, &xmap, x0 - 1, y0 - 1, zb - 1 + q, g, bar);
             }
             issued_sh = q;
         }
@@ -370,6 +384,7 @@ __global__ void __launch_bounds__(ZM_THREADS) k_conv3_zm(const __grid_constant__
         const bool in = ox < a.v.nx && oy < a.v.ny;
         const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
         const float hb = a.head ? __ldg(a.head + 16) : 0.0f;
+        const long long nvox = a.v.n();
         for (int j = 0; j < nplanes; ++j) {
             const int sl = j % S;
             if (zm_failed(&fail) || !mbar_wait(smem_u32(&accf[sl]), (uint32_t)((j / S) & 1))) {
@@ -377,18 +392,30 @@ __global__ void __launch_bounds__(ZM_THREADS) k_conv3_zm(const __grid_constant__
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;");
-            const int z = zb + j;
-            const long long vox = ox + (long long)a.v.nx * (oy + (long long)a.v.ny * z);
-            float hs = hb;
+            // the whole chunk into registers, the slot re-zeroed and handed
+            // back to the MMA warp before the arithmetic and the stores
+            float acc[N];
 #pragma unroll
             for (int c0 = 0; c0 < N; c0 += 16) {
-                float acc[16];
-                tc_ld16(lane_addr + (uint32_t)(sl * N + c0), acc);
+                float t[16];
+                tc_ld16(lane_addr + (uint32_t)(sl * N + c0), t);
                 tc_zero16(lane_addr + (uint32_t)(sl * N + c0));
-                if (in) {
+#pragma unroll
+                for (int q = 0; q < 16; ++q) acc[c0 + q] = t[q];
+            }
+            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncwarp();
+            if (lane == 0) zm_arrive(smem_u32(&acce[sl]));
+            if (in) {
+                const int z = zb + j;
+                const long long vox = ox + (long long)a.v.nx * (oy + (long long)a.v.ny * z);
+                float hs = hb;
+#pragma unroll
+                for (int c0 = 0; c0 < N; c0 += 16) {
                     float zz[16];
 #pragma unroll
-                    for (int q = 0; q < 16; ++q) zz[q] = acc[q] + bias_s[c0 + q];
+                    for (int q = 0; q < 16; ++q) zz[q] = acc[c0 + q] + bias_s[c0 + q];
                     if (a.Z) {
                         float4 *zr = reinterpret_cast<float4 *>(a.Z + vox * a.cout + n0 + c0);
 #pragma unroll
@@ -400,12 +427,12 @@ __global__ void __launch_bounds__(ZM_THREADS) k_conv3_zm(const __grid_constant__
 #pragma unroll
                         for (int q = 0; q < 16; ++q) gz[q] = a.act ? gelu(zz[q]) : zz[q];
                         if (a.Y) {
-                            __align__(16) bf16 yb[16];
+                            __nv_bfloat162 yb[8];
 #pragma unroll
-                            for (int q = 0; q < 16; ++q) yb[q] = __float2bfloat16_rn(gz[q]);
-                            uint4 *yr = reinterpret_cast<uint4 *>(a.Y + vox * a.cout + n0 + c0);
-                            yr[0] = reinterpret_cast<const uint4 *>(yb)[0];
-                            yr[1] = reinterpret_cast<const uint4 *>(yb)[1];
+                            for (int q = 0; q < 8; ++q) yb[q] = __floats2bfloat162_rn(gz[2 * q], gz[2 * q + 1]);
+                            *reinterpret_cast<uint4 *>(a.Y + g8(vox, n0 + c0, nvox)) = reinterpret_cast<const uint4 *>(yb)[0];
+                            *reinterpret_cast<uint4 *>(a.Y + g8(vox, n0 + c0 + 8, nvox)) =
+                                reinterpret_cast<const uint4 *>(yb)[1];
                         }
                         if (a.head) {
 #pragma unroll
@@ -413,16 +440,11 @@ __global__ void __launch_bounds__(ZM_THREADS) k_conv3_zm(const __grid_constant__
                         }
                     }
                 }
+                if (a.head) {
+                    if (a.raw) a.raw[vox] = hs;
+                    if (a.out) a.out[vox] = hs * __ldg(a.scales + 1);
+                }
             }
-            if (a.head && in) {
-                if (a.raw) a.raw[vox] = hs;
-                if (a.out) a.out[vox] = hs * __ldg(a.scales + 1);
-            }
-            // the slot is free (and zero) once all four warps are through
-            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-            asm volatile("tcgen05.fence::before_thread_sync;");
-            __syncwarp();
-            if (lane == 0) zm_arrive(smem_u32(&acce[sl]));
         }
     }
     __syncthreads();
@@ -449,7 +471,7 @@ __global__ void __launch_bounds__(ZM_THREADS) k_conv3_zm(const __grid_constant__
 // to 128 (columns past Cout stay zero), N = Cin, K = the chunk's voxels in
 // stages of 64.  Both operands are MN-major in the canonical no-swizzle
 // layout: a core matrix is 8 K-rows (voxels) of 16 bytes (8 consecutive
-// channels), i.e. channels-last rows copied as they are; core matrices 128
+// channels), i.e. rows of the 8-channel group planes copied as they are; core matrices 128
 // bytes apart along K (LBO) and 1 KB apart along M / N (SBO).  The
 // accumulators are added to dW with FP32 atomics (order-dependent in the
 // last bits).
@@ -514,14 +536,14 @@ __global__ void __launch_bounds__(128) k_conv3_wgrad_tc(Vol v, const bf16 *__res
             uint4 val = make_uint4(0, 0, 0, 0);
             if (vv < nvox) {
                 if (isa) {
-                    val = __ldg(reinterpret_cast<const uint4 *>(G + vv * cout) + cg);
+                    val = __ldg(reinterpret_cast<const uint4 *>(G + g8(vv, 8 * cg, nvox)));
                 } else {
                     const int x = (int)(vv % v.nx), y = (int)((vv / v.nx) % v.ny),
                               z = (int)(vv / ((long long)v.nx * v.ny));
                     const int sx = x + dx, sy = y + dy, sz = z + dz;
                     if (sx >= 0 && sx < v.nx && sy >= 0 && sy < v.ny && sz >= 0 && sz < v.nz)
                         val = __ldg(reinterpret_cast<const uint4 *>(
-                                        X + (sx + (long long)v.nx * (sy + (long long)v.ny * sz)) * cin) + cg);
+                            X + g8(sx + (long long)v.nx * (sy + (long long)v.ny * sz), 8 * cg, nvox)));
                 }
             }
             pre[j] = val;
@@ -595,21 +617,34 @@ __global__ void __launch_bounds__(128) k_conv3_wgrad_tc(Vol v, const bf16 *__res
     }
 }
 
-// G = dY * gelu'(Z) in BF16 (the GEMM operand of both backward convolutions);
-// with act == 0, G = dY
-__global__ void k_act_grad(long long n, const float *__restrict__ dY, const float *__restrict__ Z, int act,
+// G = dY * gelu'(Z) in BF16 (the GEMM operand of both backward convolutions),
+// from channels-last FP32 into 8-channel group planes; with act == 0, G = dY.
+// One thread per voxel and group.
+__global__ void k_act_grad(long long nvox, int C, const float *__restrict__ dY, const float *__restrict__ Z, int act,
                            bf16 *__restrict__ G) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        G[i] = __float2bfloat16_rn(act ? dY[i] * gelu_grad(Z[i]) : dY[i]);
+    const int ng = C >> 3;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nvox * ng;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long v = i / ng;
+        const int g = (int)(i - v * ng);
+        __align__(16) bf16 o[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const long long e = v * C + 8 * g + k;
+            o[k] = __float2bfloat16_rn(act ? dY[e] * gelu_grad(Z[e]) : dY[e]);
+        }
+        *reinterpret_cast<uint4 *>(G + g8(v, 8 * g, nvox)) = *reinterpret_cast<const uint4 *>(o);
+    }
 }
 
-// bias gradient: db[c] += sum_v G[v, c]
+// bias gradient: db[c] += sum_v G[v, c] (G in 8-channel group planes: the
+// flat index i runs over group planes, channel (i / (8 nvox)) 8 + i % 8)
 __global__ void k_bias_grad(long long nvox, int C, const bf16 *__restrict__ G, float *__restrict__ db) {
     extern __shared__ float sb[];
     for (int c = threadIdx.x; c < C; c += blockDim.x) sb[c] = 0.f;
     __syncthreads();
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nvox * C; i += (long long)gridDim.x * blockDim.x)
-        atomicAdd(&sb[i % C], __bfloat162float(G[i]));
+        atomicAdd(&sb[(int)(i / (8 * nvox)) * 8 + (int)(i & 7)], __bfloat162float(G[i]));
     __syncthreads();
     for (int c = threadIdx.x; c < C; c += blockDim.x) atomicAdd(&db[c], sb[c]);
 }
@@ -648,15 +683,15 @@ __global__ void k_gather_rows(int cin_real, int cin, int cout, const float *__re
     }
 }
 
-// 2x average pooling (channels-last): one thread per coarse voxel and
-// 8-channel group (16-byte loads and stores)
+// 2x average pooling of 8-channel group planes: one thread per coarse voxel
+// and group (16-byte loads and stores)
 __global__ void k_pool(Vol c, int C, const bf16 *__restrict__ X, bf16 *__restrict__ Y) {
     const int G = C >> 3;
-    const long long n = c.n() * G;
+    const long long nc = c.n(), nf = 8 * nc, n = nc * G;
     const int fx = 2 * c.nx, fy = 2 * c.ny;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const long long vv = i / G;
-        const int g = (int)(i - vv * G);
+        const int g = (int)(i / nc);
+        const long long vv = i - (long long)g * nc;
         const int x = (int)(vv % c.nx);
         const long long yz = vv / c.nx;
         const int y = (int)(yz % c.ny), z = (int)(yz / c.ny);
@@ -664,7 +699,7 @@ __global__ void k_pool(Vol c, int C, const bf16 *__restrict__ X, bf16 *__restric
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const long long f = (2 * x + (q & 1)) + (long long)fx * ((2 * y + ((q >> 1) & 1)) + (long long)fy * (2 * z + (q >> 2)));
-            const uint4 u = __ldg(reinterpret_cast<const uint4 *>(X + f * C) + g);
+            const uint4 u = __ldg(reinterpret_cast<const uint4 *>(X + g8(f, 8 * g, nf)));
             const bf16 *e = reinterpret_cast<const bf16 *>(&u);
 #pragma unroll
             for (int k = 0; k < 8; ++k) s[k] += __bfloat162float(e[k]);
@@ -672,7 +707,7 @@ __global__ void k_pool(Vol c, int C, const bf16 *__restrict__ X, bf16 *__restric
         __align__(16) bf16 o[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) o[k] = __float2bfloat16_rn(s[k] * 0.125f);
-        reinterpret_cast<uint4 *>(Y + vv * C)[g] = *reinterpret_cast<const uint4 *>(o);
+        *reinterpret_cast<uint4 *>(Y + g8(vv, 8 * g, nc)) = *reinterpret_cast<const uint4 *>(o);
     }
 }
 __global__ void k_pool_grad(Vol c, int C, const float *__restrict__ dY, float *__restrict__ dX, int accumulate) {
@@ -690,28 +725,22 @@ __global__ void k_pool_grad(Vol c, int C, const float *__restrict__ dY, float *_
     }
 }
 
-// nearest 2x upsampling of X (C1 channels) into channels [0, C1) of the
-// concat buffer Y (C1 + C2 channels); channels [C1, C1 + C2) take the skip S.
-// One thread per fine voxel and 8-channel group of Y (16-byte moves).
-__global__ void k_up_concat(Vol f, int C1, int C2, const bf16 *__restrict__ X, const bf16 *__restrict__ S,
-                            bf16 *__restrict__ Y) {
-    const int C = C1 + C2, G = C >> 3, G1 = C1 >> 3, G2 = C2 >> 3;
-    const long long n = f.n() * G;
+// nearest 2x upsampling of X (C1 channels) into the first C1 / 8 group
+// planes of the concat buffer Y; the skip tensor's planes follow them in
+// the same allocation (it was written there by its convolution), so the
+// concatenation copies nothing else.  One thread per fine voxel and group.
+__global__ void k_up_concat(Vol f, int C1, const bf16 *__restrict__ X, bf16 *__restrict__ Y) {
+    const int G1 = C1 >> 3;
+    const long long nf = f.n(), nc = nf / 8, n = nf * G1;
     const int cx = f.nx / 2, cy = f.ny / 2;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const long long vv = i / G;
-        const int g = (int)(i - vv * G);
-        uint4 val;
-        if (g < G1) {
-            const int x = (int)(vv % f.nx);
-            const long long yz = vv / f.nx;
-            const int y = (int)(yz % f.ny), z = (int)(yz / f.ny);
-            val = __ldg(reinterpret_cast<const uint4 *>(X + ((x / 2) + (long long)cx * ((y / 2) + (long long)cy * (z / 2))) * C1) + g);
-        } else {
-            val = __ldg(reinterpret_cast<const uint4 *>(S + vv * C2) + (g - G1));
-        }
-        reinterpret_cast<uint4 *>(Y + vv * C)[g] = val;
-        (void)G2;
+        const int g = (int)(i / nf);
+        const long long vv = i - (long long)g * nf;
+        const int x = (int)(vv % f.nx);
+        const long long yz = vv / f.nx;
+        const int y = (int)(yz % f.ny), z = (int)(yz / f.ny);
+        const long long cv = (x / 2) + (long long)cx * ((y / 2) + (long long)cy * (z / 2));
+        *reinterpret_cast<uint4 *>(Y + g8(vv, 8 * g, nf)) = __ldg(reinterpret_cast<const uint4 *>(X + g8(cv, 8 * g, nc)));
     }
 }
 // backward of k_up_concat: dX (coarse, C1) = sum over the 8 children, and
@@ -741,21 +770,20 @@ __global__ void k_skip_grad_add(long long nvox, int C1, int C2, const float *__r
     }
 }
 
-// network input: channels (b / sb, mask, p_prev / sp, 0 ... 0), 16 wide,
-// one voxel per thread (two 16-byte stores)
+// network input: channels (b / sb, mask, p_prev / sp, 0 ... 0), 16 wide;
+// only the first group plane is written (the second, channels 8-15, is
+// zeroed once when the buffer is allocated).  One voxel per thread.
 __global__ void k_input(long long n, const float *__restrict__ b, const uint8_t *__restrict__ mask,
                         const float *__restrict__ pp, const float *__restrict__ scales, bf16 *__restrict__ X) {
     const float isb = 1.0f / scales[0], isp = 1.0f / scales[1];
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
-        __align__(16) bf16 x[16];
+        __align__(16) bf16 x[8];
         x[0] = __float2bfloat16_rn(b[v] * isb);
         x[1] = __float2bfloat16_rn(mask ? (float)mask[v] : 0.0f);
         x[2] = __float2bfloat16_rn(pp ? pp[v] * isp : 0.0f);
 #pragma unroll
-        for (int c = 3; c < 16; ++c) x[c] = __float2bfloat16_rn(0.0f);
-        uint4 *dst = reinterpret_cast<uint4 *>(X + v * 16);
-        dst[0] = reinterpret_cast<const uint4 *>(x)[0];
-        dst[1] = reinterpret_cast<const uint4 *>(x)[1];
+        for (int c = 3; c < 8; ++c) x[c] = __float2bfloat16_rn(0.0f);
+        *reinterpret_cast<uint4 *>(X + v * 8) = *reinterpret_cast<const uint4 *>(x);
     }
 }
 
@@ -909,6 +937,27 @@ size_t zm_smem_bytes(int n, int cin, int ring) {
     return ((27u * n * cin * 2u + 1023u) & ~1023u) + (size_t)ring * (cin / 8) * ZM_GP + 1024;
 }
 
+// CTAs per SM the register file allows for k_conv3_zm<N>
+template <int N>
+int zm_reg_blocks() {
+    static int b = 0;
+    if (!b) {
+        cudaFuncAttributes fa;
+        b = 6;
+        if (cudaFuncGetAttributes(&fa, k_conv3_zm<N>) == cudaSuccess && fa.numRegs > 0)
+            b = std::max(1, 65536 / (((fa.numRegs + 7) / 8 * 8) * ZM_THREADS));
+    }
+    return b;
+}
+int zm_reg_blocks_for(int n) {
+    switch (n) {
+    case 16: return zm_reg_blocks<16>();
+    case 32: return zm_reg_blocks<32>();
+    case 48: return zm_reg_blocks<48>();
+    default: return zm_reg_blocks<64>();
+    }
+}
+
 template <int N>
 int launch_zm(const ZmArgs &a, const CUtensorMap &map, int nchunks, size_t smem, cudaStream_t s) {
     static size_t configured = 0;
@@ -922,37 +971,47 @@ int launch_zm(const ZmArgs &a, const CUtensorMap &map, int nchunks, size_t smem,
 }
 
 // Y = act(conv(X, W) + bias) and/or Z = conv(X, W) + bias, or the fused head
-// (out, raw) on top of the activation.  X: channels-last BF16 with cin
-// channels (a multiple of 16, at most 96); W: [27][cin][cout] BF16, packed
-// into pk (27 cin cout) for the B operand.
+// (out, raw) on top of the activation.  X: BF16 in 8-channel group planes
+// with cin channels (a multiple of 16, at most 96); Y in the same layout, Z
+// channels-last FP32; W: [27][cin][cout] BF16, packed into pk (27 cin cout)
+// for the B operand.
 int launch_conv(int cout, Vol v, const bf16 *X, int cin, const bf16 *W, const float *bias, int act, float *Z, bf16 *Y,
                 bf16 *pk, int *err, cudaStream_t s, const float *head = nullptr, const float *scales = nullptr,
                 float *out = nullptr, float *raw = nullptr) {
     if (cin % 16 || cin > 96) return ff_set_error(FF_E_ARG, "unet: conv input channels %d (multiples of 16 to 96)", cin);
     if (cout % 16 || cout > 96) return ff_set_error(FF_E_ARG, "unet: conv output channels %d (multiples of 16 to 96)", cout);
-    // the output-channel chunk C (3C <= 256 columns per MMA): the widest
-    // whose weights and a ring of 3 planes fit two CTAs per SM, else one;
-    // then the deepest ring that keeps that occupancy.  CTAs per SM are also
-    // bounded by TMEM (512 columns per SM).
-    const size_t two = 113 * 1024, one = 220 * 1024;
-    int n = 0, occ = 0;
-    for (int pass = 0; pass < 2 && !n; ++pass)
+    // the output-channel chunk C (3C <= 256 columns per MMA) and the ring
+    // depth R: the widest chunk that reaches two or more CTAs per SM (else
+    // one), then the deepest ring at that chunk's best occupancy.  CTAs per
+    // SM are bounded by shared memory (228 KB less 1 KB per CTA), TMEM (512
+    // columns) and the register file.
+    auto occupancy = [&](int c, int r) {
+        const size_t sm = zm_smem_bytes(c, cin, r);
+        if (sm > 227 * 1024) return 0;
+        return std::min({zm_reg_blocks_for(c), (int)(233472 / (sm + 1024)), 512 / zm_tcols(c)});
+    };
+    int n = 0, ring = 3, occ = 0;
+    for (int want = 2; want >= 1 && !n; --want)
         for (int d : {1, 2, 3, 4, 6}) {
             if (cout % d || (cout / d) % 16 || cout / d > 80) continue;
-            if (zm_smem_bytes(cout / d, cin, 3) <= (pass == 0 ? two : one)) {
+            int best = 0;
+            for (int r = 3; r <= ZM_RMAX; ++r) best = std::max(best, occupancy(cout / d, r));
+            if (best >= want) {
                 n = cout / d;
-                occ = pass == 0 ? 2 : 1;
+                occ = best;
+                for (int r = ZM_RMAX; r >= 3; --r)
+                    if (occupancy(n, r) == best) {
+                        ring = r;
+                        break;
+                    }
                 break;
             }
         }
     if (!n) return ff_set_error(FF_E_LIMIT, "unet: no shared-memory plan for a %d -> %d convolution", cin, cout);
     k_pack_b<<<gblocks(27LL * cin * cout), 256, 0, s>>>(cin, cout, n, W, pk);
     FF_TRY(post("pack weights"));
-    const size_t budget = occ == 2 ? two : one;
-    int ring = 3;
-    while (ring < ZM_RMAX && zm_smem_bytes(n, cin, ring + 1) <= budget) ++ring;
     const size_t smem = zm_smem_bytes(n, cin, ring);
-    const int blocks_per_sm = std::max(1, std::min({8, (int)(228 * 1024 / (smem + 2048)), 512 / zm_tcols(n)}));
+    const int blocks_per_sm = occ;
     ZmArgs a;
     a.v = v;
     a.cin = cin;
@@ -990,11 +1049,12 @@ int launch_conv(int cout, Vol v, const bf16 *X, int cin, const bf16 *W, const fl
     PFN_cuTensorMapEncodeTiled_v12000 enc = zm_encoder();
     FF_CHECK(enc, FF_E_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
     CUtensorMap map;
-    cuuint64_t dims[4] = {(cuuint64_t)cin, (cuuint64_t)v.nx, (cuuint64_t)v.ny, (cuuint64_t)v.nz};
-    cuuint64_t strides[3] = {(cuuint64_t)cin * 2, (cuuint64_t)v.nx * cin * 2, (cuuint64_t)v.nx * v.ny * cin * 2};
-    cuuint32_t box[4] = {8, ZM_HX, ZM_HY, 1};
-    cuuint32_t estr[4] = {1, 1, 1, 1};
-    CUresult r = enc(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)X, dims, strides, box, estr,
+    // the input's group planes: (8 channels, x, y, z, group), 16-byte voxels
+    cuuint64_t dims[5] = {8, (cuuint64_t)v.nx, (cuuint64_t)v.ny, (cuuint64_t)v.nz, (cuuint64_t)(cin / 8)};
+    cuuint64_t strides[4] = {16, (cuuint64_t)v.nx * 16, (cuuint64_t)v.nx * v.ny * 16, (cuuint64_t)v.n() * 16};
+    cuuint32_t box[5] = {8, ZM_HX, ZM_HY, 1, 1};
+    cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    CUresult r = enc(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, (void *)X, dims, strides, box, estr,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     FF_CHECK(r == CUDA_SUCCESS, FF_E_CUDA, "unet: cuTensorMapEncodeTiled failed (%d) for %dx%dx%d x %d", (int)r, v.nx,
@@ -1070,7 +1130,8 @@ struct ff_unet_s {
 };
 
 // tensor slots: 0 input(16) 1 e0a(16) 2 e0b=skip0(16) 3 p1(16) 4 e1a(32) 5 e1b=skip1(32)
-// 6 p2(32) 7 ba(64) 8 bb(64) 9 cat1(96) 10 d1a(32) 11 d1b(32) 12 cat0(48) 13 d0a(16) 14 d0b(16)
+// 6 p2(32) 7 ba(64) 8 bb(64) 9 cat1(96) 10 d1a(32) 11 d1b(32) 12 cat0(48) 13 d0a(16) 14 d0b(16);
+// slots 2 and 5 are the last group planes of slots 12 and 9
 static const int SLOT_C[15] = {16, 16, 16, 16, 32, 32, 32, 64, 64, 96, 32, 32, 48, 16, 16};
 static const int SLOT_LEVEL[15] = {0, 0, 0, 1, 1, 1, 2, 2, 2, 1, 1, 1, 0, 0, 0};
 // conv layer l reads slot CONV_IN[l] and writes slot CONV_OUT[l]
@@ -1111,9 +1172,15 @@ static int ensure_shape(ff_unet u, Vol v, bool train) {
     if (u->act.empty()) {
         u->act.resize(15);
         for (int s = 0; s < 15; ++s) {
+            if (s == 2 || s == 5) continue;   // skip tensors: inside their concat buffers
             const long long nv = n0 >> (3 * SLOT_LEVEL[s]);
             FF_TRY(alloc_owned(u, (void **)&u->act[s], (size_t)nv * SLOT_C[s] * sizeof(bf16)));
         }
+        // cat0 = [up(d1b): 4 group planes | skip0: 2], cat1 = [up(bb): 8 | skip1: 4]
+        u->act[2] = u->act[12] + 4 * n0 * 8;
+        u->act[5] = u->act[9] + 8 * (n0 >> 3) * 8;
+        // channels 8-15 of the input are always zero
+        FF_CUDA(cudaMemsetAsync(u->act[0] + n0 * 8, 0, (size_t)n0 * 8 * sizeof(bf16), u->ctx->stream));
         FF_TRY(alloc_owned(u, (void **)&u->scales, 16));
         FF_TRY(alloc_owned(u, (void **)&u->partial, sizeof(double) * 152 * 32));
     }
@@ -1289,10 +1356,10 @@ static int forward(ff_unet u, const float *b, const uint8_t *mask, const float *
     k_pool<<<gblocks(level_vol(u, 2).n() * 4), 256, 0, s>>>(level_vol(u, 2), 32, u->act[5], u->act[6]);
     FF_TRY(conv(4));
     FF_TRY(conv(5));
-    k_up_concat<<<gblocks(level_vol(u, 1).n() * 12), 256, 0, s>>>(level_vol(u, 1), 64, 32, u->act[8], u->act[5], u->act[9]);
+    k_up_concat<<<gblocks(level_vol(u, 1).n() * 8), 256, 0, s>>>(level_vol(u, 1), 64, u->act[8], u->act[9]);
     FF_TRY(conv(6));
     FF_TRY(conv(7));
-    k_up_concat<<<gblocks(n0 * 6), 256, 0, s>>>(level_vol(u, 0), 32, 16, u->act[11], u->act[2], u->act[12]);
+    k_up_concat<<<gblocks(n0 * 4), 256, 0, s>>>(level_vol(u, 0), 32, u->act[11], u->act[12]);
     FF_TRY(conv(8));
     FF_TRY(conv(9));
     return post("unet forward");
@@ -1306,7 +1373,7 @@ static int conv_backward(ff_unet u, int l, bool accumulate_input) {
     const int si = CONV_IN[l], so = CONV_OUT[l];
     const Vol v = level_vol(u, SLOT_LEVEL[so]);
     const long long nout = v.n() * c.cout;
-    k_act_grad<<<gblocks(nout), 256, 0, s>>>(nout, u->grad[so], u->pre[l], c.act, u->gbuf);
+    k_act_grad<<<gblocks(nout / 8), 256, 0, s>>>(v.n(), c.cout, u->grad[so], u->pre[l], c.act, u->gbuf);
     FF_TRY(post("act grad"));
     if (c.cin == c.cin_real) {
         FF_TRY(launch_wgrad(c.cin, c.cout, v, u->act[si], u->gbuf, u->g + c.w_off, u->tc_err, s));
