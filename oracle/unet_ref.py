@@ -105,10 +105,26 @@ def predict(params, b, mask, p_prev, h, shape):
     return (raw.detach().numpy().ravel() * sp).astype(np.float32)
 
 
+LAP_W = 0.25
+
+
+def graph_laplacian(d):
+    """7-point graph Laplacian of a (nz, ny, nx) grid: sum over the existing
+    face neighbours of d_nbr - d_v (edge-replicated padding gives 0 across
+    the domain edge)."""
+    p = F.pad(d[None, None], (1, 1, 1, 1, 1, 1), mode="replicate")[0, 0]
+    c = p[1:-1, 1:-1, 1:-1]
+    return (p[1:-1, 1:-1, :-2] + p[1:-1, 1:-1, 2:] + p[1:-1, :-2, 1:-1] + p[1:-1, 2:, 1:-1] +
+            p[:-2, 1:-1, 1:-1] + p[2:, 1:-1, 1:-1] - 6.0 * c)
+
+
 def loss_and_grads(params, b, mask, p_prev, target, h, shape):
+    """Loss mean(d^2) + LAP_W mean((D d)^2) with d = raw - target / sp and D
+    the grid's graph Laplacian (the GPU's k_loss_* kernels)."""
     raw, (sb, sp), tw, head = forward(params, b, mask, p_prev, h, shape, requires_grad=True)
     t = torch.from_numpy((np.asarray(target, np.float32) * np.float32(1.0 / sp)).reshape(raw.shape))
-    loss = ((raw - t) ** 2).mean()
+    d = raw - t
+    loss = (d ** 2).mean() + LAP_W * (graph_laplacian(d.reshape(shape[2], shape[1], shape[0])) ** 2).mean()
     loss.backward()
     grads = []
     for w, bb in tw:

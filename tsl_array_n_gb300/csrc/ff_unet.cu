@@ -787,17 +787,46 @@ __global__ void k_input(long long n, const float *__restrict__ b, const uint8_t 
     }
 }
 
-// MSE loss in normalised units: L = mean((raw - t / sp)^2); dL/draw per
-// voxel; the loss itself by a deterministic block-partial reduction
-__global__ void k_loss(long long n, const float *__restrict__ raw, const float *__restrict__ target,
-                       const float *__restrict__ scales, float *__restrict__ draw, double *__restrict__ partial) {
-    __shared__ double sred[256];
+// Loss in normalised units with d = raw - t / sp:
+//   L = mean(d^2) + LAP_W mean((D d)^2),
+// D the 7-point graph Laplacian of the grid (sum over the existing face
+// neighbours of d_nbr - d_v; no term across the domain edge).  The second
+// term weighs the error's grid-scale part, which the pressure operator
+// amplifies in the residual of a guess.  dL/draw = (2 d + 2 LAP_W D(D d)) / n
+// (D is symmetric).  Three passes: d into draw; D d into raw with the loss
+// partials; then dL/draw over draw.
+constexpr float LAP_W = 0.25f;
+
+__device__ __forceinline__ float graph_lap(const float *a, Vol v, int x, int y, int z, long long i) {
+    const float c = a[i];
+    float s = 0.0f;
+    if (x > 0) s += a[i - 1] - c;
+    if (x < v.nx - 1) s += a[i + 1] - c;
+    if (y > 0) s += a[i - v.nx] - c;
+    if (y < v.ny - 1) s += a[i + v.nx] - c;
+    const long long pz = (long long)v.nx * v.ny;
+    if (z > 0) s += a[i - pz] - c;
+    if (z < v.nz - 1) s += a[i + pz] - c;
+    return s;
+}
+
+__global__ void k_loss_d(long long n, const float *__restrict__ raw, const float *__restrict__ target,
+                         const float *__restrict__ scales, float *__restrict__ d) {
     const float isp = 1.0f / scales[1];
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x)
+        d[v] = raw[v] - target[v] * isp;
+}
+__global__ void k_loss_lap(Vol v, const float *__restrict__ d, float *__restrict__ e, double *__restrict__ partial) {
+    __shared__ double sred[256];
+    const long long n = v.n();
     double acc = 0.0;
-    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
-        const float d = raw[v] - target[v] * isp;
-        draw[v] = 2.0f * d / (float)n;
-        acc += (double)d * d;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % v.nx);
+        const long long yz = i / v.nx;
+        const int y = (int)(yz % v.ny), z = (int)(yz / v.ny);
+        const float l = graph_lap(d, v, x, y, z, i);
+        e[i] = l;
+        acc += (double)d[i] * d[i] + (double)LAP_W * l * l;
     }
     sred[threadIdx.x] = acc;
     __syncthreads();
@@ -806,6 +835,16 @@ __global__ void k_loss(long long n, const float *__restrict__ raw, const float *
         __syncthreads();
     }
     if (threadIdx.x == 0) partial[blockIdx.x] = sred[0] / (double)n;
+}
+__global__ void k_loss_grad(Vol v, const float *__restrict__ e, float *__restrict__ d_to_draw) {
+    const long long n = v.n();
+    const float inv = 1.0f / (float)n;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % v.nx);
+        const long long yz = i / v.nx;
+        const int y = (int)(yz % v.ny), z = (int)(yz / v.ny);
+        d_to_draw[i] = (2.0f * d_to_draw[i] + 2.0f * LAP_W * graph_lap(e, v, x, y, z, i)) * inv;
+    }
 }
 // head backward: dY[v, c] = draw[v] w[c]; dw[c] += sum draw y; db += sum draw
 __global__ void k_head_grad(long long n, const float *__restrict__ Zin, const float *__restrict__ w,
@@ -1467,7 +1506,9 @@ extern "C" int ff_unet_loss_backward(ff_unet u, const int *res, double h, ff_fie
     FF_TRY(forward(u, (const float *)b->d, mask ? (const uint8_t *)mask->d : nullptr,
                    p_prev ? (const float *)p_prev->d : nullptr, h, nullptr, true));
     const int nb = std::min(152 * 32, gblocks(n));
-    k_loss<<<nb, 256, 0, s>>>(n, u->raw, (const float *)target->d, u->scales, u->draw, u->partial);
+    k_loss_d<<<gblocks(n), 256, 0, s>>>(n, u->raw, (const float *)target->d, u->scales, u->draw);
+    k_loss_lap<<<nb, 256, 0, s>>>(u->vol, u->draw, u->raw, u->partial);
+    k_loss_grad<<<gblocks(n), 256, 0, s>>>(u->vol, u->raw, u->draw);
     FF_TRY(post("loss"));
     FF_CUDA(cudaMemsetAsync(u->g, 0, u->nparam * 4, s));
     FF_TRY(backward(u));

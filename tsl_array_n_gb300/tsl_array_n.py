@@ -115,6 +115,11 @@ class Field:
         _lib.check(_lib.load().ff_field_fill(self.handle, float(value)))
         return self
 
+    def copy_from(self, src):
+        """Device-to-device copy of a field of the same type and size."""
+        _lib.check(_lib.load().ff_field_copy(self.handle, src.handle))
+        return self
+
     def device_ptr(self):
         return _lib.load().ff_field_device_ptr(self.handle)
 
