@@ -442,6 +442,57 @@ int ff_twophase2_step(ff_twophase t, ff_diag *diag);
 /* the last resampling pass: {liquid donors, liquid cells' need, gas
  * donors, gas cells' need}.  Synchronises the stream.                      */
 int ff_twophase2_resample_stats(ff_twophase t, int64_t *out4);
+/* ---- 3D two-phase FLIP: no counterpart in the reference, whose two-phase
+ * solver is 2D only (grid_two_phase_flip_solver2.js:479-1622).  The same
+ * stages on a full 3D grid: u, v, w face arrays (borrowed), particles in 3D,
+ * density and beta on all three face sets (the 3D FLIP solver's beta,
+ * grid_flip_solver3.js:298-359, with every cell fluid), the pressure pinned
+ * at pin_cell, and resampling recipients with at least 3 of their 6 clamped
+ * face neighbours full (the 3D single-phase rule, grid_flip_solver3.js:
+ * 700-724).  Stages are the FF_TP_* codes; the handle type is ff_twophase. */
+typedef struct {
+    int resolution[3];
+    double grid_spacing[3];
+    double origin[3];
+    int max_particles;             /* required                            */
+    double dt;
+    double gravity[3];             /* default (0, -9.81, 0)               */
+    double ambient_density;        /* concentration 0 (gas), default 0.01 */
+    double component_density;      /* concentration 1 (liquid), 1         */
+    double mixing, fade;           /* default 0, 0                        */
+    double concentration_atomic_scale;   /* default 4096                  */
+    double flip_ratio;             /* default 0.97                        */
+    double gas_flip_ratio;         /* default 0.90                        */
+    double velocity_damping;       /* default 0.02                        */
+    double p2g_atomic_scale;       /* default 65536                       */
+    double weight_epsilon;         /* default 1e-4                        */
+    int closed_flags;              /* default 63 (all six walls)          */
+    int max_substeps;              /* default 32                          */
+    double collider_push_thresh, collider_push_shift;
+    int pin_cell[3];               /* default top centre (nx/2, ny-1, nz/2); {-1,..} = none */
+    int resample_enabled;          /* default 1                           */
+    int min_particles_per_cell;    /* default 3                           */
+    int max_particles_per_cell;    /* default 8                           */
+    int extrapolation_depth;       /* default 5                           */
+    ff_pressure_desc pressure;     /* multigrid: deepest of up to 5 levels the resolution divides into */
+} ff_twophase3_desc;
+void ff_twophase3_desc_default(ff_twophase3_desc *d, const int *resolution, const double *grid_spacing,
+                               int max_particles, double dt);
+int ff_twophase3_create(ff_ctx ctx, const ff_twophase3_desc *desc, ff_field u, ff_field v, ff_field w,
+                        ff_twophase *out);
+/* positions and velocities as (x, y, z) triples, phase per particle; NULL
+ * leaves that array alone                                                  */
+int ff_twophase3_set_particles(ff_twophase t, int n, const float *xyz, const float *vxyz, const float *phase);
+int ff_twophase3_get_particles(ff_twophase t, int n, float *xyz, float *vxyz, float *phase);
+/* borrowed handles: phase, liquidFraction, density (cells), beta on the u,
+ * v, w faces, and the pressure solver                                      */
+int ff_twophase3_fields(ff_twophase t, ff_field *phase, ff_field *liquid_fraction, ff_field *density,
+                        ff_field *beta_u, ff_field *beta_v, ff_field *beta_w, ff_pressure *pressure);
+/* the per-cell particle count and fixed-point concentration sum of the last
+ * density stage (int32 arrays of nx ny nz), for tests.  Synchronises.      */
+int ff_twophase3_cell_counts(ff_twophase t, int32_t *count, int32_t *sum);
+/* destroy, set_collider, set_count, stage, step and resample_stats of a 3D
+ * solver are the ff_twophase2_* calls on its handle.                       */
 
 /* computeFlipBoxSeed3 (:70-130): per_axis^3 jittered particles per cell,
  * mulberry32(seed) (jitter_random.js:29-46), in doubles as JavaScript.

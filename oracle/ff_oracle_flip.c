@@ -696,3 +696,144 @@ int64_t orc_tp_resample(const int *res, const float *h, const float *o, int64_t 
     free(pool);
     return moved;
 }
+
+/* ---- 3D two-phase solver (the 2D two-phase stages on a full grid) ---- */
+
+/* per-cell particle count and fixed-point concentration sum (countPhases,
+ * grid_two_phase_flip_solver2.js:646-680, on 3D cells) */
+void orc_tp3_counts(const int *res, const float *h, const float *o, int64_t n, const float *pos, const float *phase,
+                    float cscale, int32_t *cnt, int32_t *acc) {
+    fg g = make_fg(res, h, o);
+    const int64_t nc = (int64_t)g.nx * g.ny * g.nz;
+    memset(cnt, 0, 4 * (size_t)nc);
+    memset(acc, 0, 4 * (size_t)nc);
+    for (int64_t p = 0; p < n; ++p) {
+        const int64_t c = cell_index(&g, pos + 3 * p);
+        cnt[c] = (int32_t)((uint32_t)cnt[c] + 1u);
+        acc[c] = (int32_t)((uint32_t)acc[c] + (uint32_t)sat_i32(rintf(fminf(fmaxf(phase[p], 0.0f), 1.0f) * cscale)));
+    }
+}
+
+/* g2pUpdate (:966-992) with all three components: the FLIP/PIC blend runs
+ * from gas_ratio at concentration 0 to flip_ratio at 1 */
+void orc_tp3_g2p(const int *res, const float *h, const float *o, int64_t n, const float *pos, float *vel,
+                 const float *phase, const float *u, const float *v, const float *w, const float *uo, const float *vo,
+                 const float *wo, float flip_ratio, float gas_ratio, float damping) {
+    fg g = make_fg(res, h, o);
+    const float *nw[3] = {u, v, w}, *od[3] = {uo, vo, wo};
+    const float fr = fminf(fmaxf(flip_ratio, 0.0f), 1.0f), gr = fminf(fmaxf(gas_ratio, 0.0f), 1.0f);
+    const float damp = fminf(fmaxf(damping, 0.0f), 1.0f);
+    for (int64_t p = 0; p < n; ++p) {
+        float nv[3], ov[3], out[3];
+        for (int a = 0; a < 3; ++a) {
+            int s[3];
+            float oa[3];
+            shape_of(&g, a, s);
+            origin_of(&g, a, oa);
+            nv[a] = tri_sample(nw[a], &g, s, oa, pos + 3 * p);
+            ov[a] = tri_sample(od[a], &g, s, oa, pos + 3 * p);
+        }
+        const float c = fminf(fmaxf(phase[p], 0.0f), 1.0f);
+        const float ratio = gr + (fr - gr) * c;
+        int bad = 0;
+        for (int a = 0; a < 3; ++a) {
+            float delta = nv[a] - ov[a];
+            float flipv = vel[3 * p + a] + delta;
+            float blended = flipv * ratio + nv[a] * (1.0f - ratio);
+            out[a] = blended * (1.0f - damp);
+            bad |= nonfinite(out[a]);
+        }
+        for (int a = 0; a < 3; ++a) vel[3 * p + a] = bad ? 0.0f : fminf(fmaxf(out[a], -500.0f), 500.0f);
+    }
+}
+
+/* the per-phase resampling pass (:1226-1494) on 3D cells: a recipient is
+ * below min_pc with at least 3 of its 6 clamped face neighbours at min_pc or
+ * more (the 3D single-phase rule, grid_flip_solver3.js:700-724), its phase
+ * its own majority or, empty, its neighbours'; donors rank in particle
+ * order into a pool filled from both ends; claims in flat cell order move
+ * a donor to the cell centre with the face velocity there.  stats as
+ * orc_tp_resample's.  Returns the number of particles moved. */
+int64_t orc_tp3_resample(const int *res, const float *h, const float *o, int64_t n, int max_particles, float *pos,
+                         float *vel, const float *phase, const float *u, const float *v, const float *w,
+                         const int32_t *cnt, const int32_t *acc, float cscale, int min_pc, int max_pc,
+                         int64_t *stats) {
+    fg g = make_fg(res, h, o);
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const int64_t plane = (int64_t)nx * ny, nc = plane * nz;
+    int32_t *need = (int32_t *)malloc(4 * (size_t)nc);
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const int64_t c = i + (int64_t)nx * j + plane * k;
+                const int64_t nb6[6] = {i > 0 ? c - 1 : c,      i < nx - 1 ? c + 1 : c,     j > 0 ? c - nx : c,
+                                        j < ny - 1 ? c + nx : c, k > 0 ? c - plane : c, k < nz - 1 ? c + plane : c};
+                const int count = cnt[c];
+                int nb = 0;
+                uint32_t ct = 0, at = 0;
+                for (int q = 0; q < 6; ++q) {
+                    nb += cnt[nb6[q]] >= min_pc;
+                    ct += (uint32_t)cnt[nb6[q]];
+                    at += (uint32_t)acc[nb6[q]];
+                }
+                const float total = (float)count, sum = (float)acc[c] / cscale;
+                const float ntot = (float)(int32_t)ct, nsum = (float)(int32_t)at / cscale;
+                const float own = sum / fmaxf(total, 1.0f), around = nsum / fmaxf(ntot, 1.0f);
+                const int liquid = total > 0.5f ? own > 0.5f : around > 0.5f;
+                const int needed = min_pc - count;
+                need[c] = (count < min_pc && nb >= 3) ? (liquid ? needed : -needed) : 0;
+            }
+    const int64_t half = max_particles / 2 > 1 ? max_particles / 2 : 1, top = max_particles - 1;
+    int *pool = (int *)malloc(sizeof(int) * (size_t)(max_particles > 0 ? max_particles : 1));
+    int64_t nl = 0, ng = 0;
+    for (int64_t p = 0; p < n; ++p) {
+        if (!(cnt[cell_index(&g, pos + 3 * p)] > max_pc)) continue;
+        if (phase[p] > 0.5f) {
+            if (nl < half) pool[nl] = (int)p;
+            ++nl;
+        } else {
+            if (ng < half) pool[top - ng] = (int)p;
+            ++ng;
+        }
+    }
+    const int64_t avl = nl < half ? nl : half, avg = ng < half ? ng : half;
+    int64_t bl = 0, bg = 0, moved = 0;
+    const float *comp[3] = {u, v, w};
+    const float ccx = g.ox + g.hx * 0.5f, ccy = g.oy + g.hy * 0.5f, ccz = g.oz + g.hz * 0.5f;
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const int q = need[i + (int64_t)nx * j + plane * k];
+                if (q == 0) continue;
+                const int liquid = q > 0;
+                const int64_t needed = liquid ? q : -q, base = liquid ? bl : bg, avail = liquid ? avl : avg;
+                if (liquid) bl += needed;
+                else bg += needed;
+                const float pt[3] = {ccx + g.hx * (float)i, ccy + g.hy * (float)j, ccz + g.hz * (float)k};
+                float vq[3];
+                for (int a = 0; a < 3; ++a) {
+                    int s[3];
+                    float oa[3];
+                    shape_of(&g, a, s);
+                    origin_of(&g, a, oa);
+                    vq[a] = tri_sample(comp[a], &g, s, oa, pt);
+                }
+                for (int64_t m = 0; m < needed && base + m < avail; ++m) {
+                    const int64_t dnr = pool[liquid ? base + m : top - (base + m)];
+                    for (int a = 0; a < 3; ++a) {
+                        pos[3 * dnr + a] = pt[a];
+                        vel[3 * dnr + a] = vq[a];
+                    }
+                    ++moved;
+                }
+            }
+    if (stats) {
+        stats[0] = nl;
+        stats[1] = bl;
+        stats[2] = ng;
+        stats[3] = bg;
+    }
+    free(need);
+    free(pool);
+    return moved;
+}

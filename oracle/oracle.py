@@ -104,6 +104,11 @@ def _declare(L):
     L.orc_flip_reduced_gravity.argtypes = [ip, fp, fp, fp, fp, fp, fp, fp, F, F, fp, fp, fp]
     L.orc_flip_mix_fade.argtypes = [ip, fp, fp, L64, fp, fp, F, F, fp]
     L.orc_flip_advect.argtypes = [ip, fp, fp, fp, fp, fp, fp, F, I, L64, fp, fp, F, F]
+    L.orc_tp3_counts.argtypes = [ip, fp, fp, L64, fp, fp, F, i32p, i32p]
+    L.orc_tp3_g2p.argtypes = [ip, fp, fp, L64, fp, fp, fp, fp, fp, fp, fp, fp, fp, F, F, F]
+    L.orc_tp3_resample.argtypes = [ip, fp, fp, L64, I, fp, fp, fp, fp, fp, fp, i32p, i32p, F, I, I,
+                                   C.POINTER(C.c_int64)]
+    L.orc_tp3_resample.restype = L64
     L.orc_tp_density.argtypes = [ip, fp, fp, L64, fp, fp, F, F, F, i32p, i32p, fp, fp, fp, fp]
     L.orc_tp_g2p.argtypes = [ip, fp, fp, L64, fp, fp, fp, fp, fp, fp, fp, F, F, F]
     L.orc_tp_mix.argtypes = [ip, fp, fp, L64, fp, fp, F, F, fp]
@@ -678,3 +683,38 @@ def tp_resample(shape, h, origin, pos, vel, phase, u, v, cnt, acc, max_particles
                                   _i32(np.ascontiguousarray(cnt, np.int32)), _i32(np.ascontiguousarray(acc, np.int32)),
                                   float(cscale), int(min_pc), int(max_pc), stats.ctypes.data_as(C.POINTER(C.c_int64)))
     return pos, vel, int(moved), stats
+
+
+def tp3_counts(shape, h, origin, pos, phase, cscale=4096.0):
+    """per-cell particle count and fixed-point concentration sum (int32)"""
+    n = shape[0] * shape[1] * shape[2]
+    cnt, acc = np.empty(n, np.int32), np.empty(n, np.int32)
+    res, hh, oo = _geom(shape, h, origin)
+    pos, phase = _f32(pos), _f32(phase)
+    lib().orc_tp3_counts(res, hh, oo, pos.size // 3, _fptr(pos), _fptr(phase), float(cscale), _i32(cnt), _i32(acc))
+    return cnt, acc
+
+
+def tp3_g2p(shape, h, origin, pos, vel, phase, new, old, flip_ratio=0.97, gas_ratio=0.9, damping=0.02):
+    vel = _f32(vel).copy()
+    res, hh, oo = _geom(shape, h, origin)
+    lib().orc_tp3_g2p(res, hh, oo, _f32(pos).size // 3, _fptr(_f32(pos)), _fptr(vel), _fptr(_f32(phase)),
+                      *[_fptr(_f32(x)) for x in new], *[_fptr(_f32(x)) for x in old], float(flip_ratio),
+                      float(gas_ratio), float(damping))
+    return vel
+
+
+def tp3_resample(shape, h, origin, pos, vel, phase, u, v, w, cnt, acc, max_particles, min_pc=3, max_pc=8,
+                 cscale=4096.0):
+    """returns positions, velocities, moved, stats (liquid donors, liquid
+    need, gas donors, gas need)"""
+    pos, vel = _f32(pos).copy(), _f32(vel).copy()
+    stats = np.zeros(4, np.int64)
+    res, hh, oo = _geom(shape, h, origin)
+    moved = lib().orc_tp3_resample(res, hh, oo, pos.size // 3, int(max_particles), _fptr(pos), _fptr(vel),
+                                   _fptr(_f32(phase)), _fptr(_f32(u)), _fptr(_f32(v)), _fptr(_f32(w)),
+                                   _i32(np.ascontiguousarray(cnt, np.int32)),
+                                   _i32(np.ascontiguousarray(acc, np.int32)), float(cscale), int(min_pc), int(max_pc),
+                                   stats.ctypes.data_as(C.POINTER(C.c_int64)))
+    return pos, vel, int(moved), stats
+

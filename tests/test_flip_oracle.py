@@ -274,3 +274,27 @@ def test_two_phase_resample_matches_vectorised_restatement(oracle, mm):
     assert moved > 0 and moved == moved2
     assert np.array_equal(p1, p2)
     assert stats[1] > 0 and stats[3] > 0   # both phases asked for particles
+
+
+def test_tp3_oracle_on_one_cell_thick_grid_equals_2d(oracle):
+    """The 3D two-phase oracle's counts and per-phase G2P on a grid one cell
+    thick, with particles on the centre plane and a zero w, equal the 2D
+    two-phase oracle's bit for bit (trilinear at fz = 0 is bilinear)."""
+    rng = np.random.default_rng(4)
+    nx, ny, h = 12, 9, 0.125
+    n = 500
+    xy = np.stack([rng.uniform(0, nx * h, n), rng.uniform(0, ny * h, n)], 1).astype(np.float32)
+    xyz = np.concatenate([xy, np.full((n, 1), 0.5 * h, np.float32)], 1)
+    ph = rng.uniform(0, 1, n).astype(np.float32)
+    cnt2, acc2, *_ = oracle.tp_density((nx, ny), (h, h), (0, 0), xy.ravel(), ph, 0.01, 1.0)
+    cnt3, acc3 = oracle.tp3_counts((nx, ny, 1), (h, h, h), (0, 0, 0), xyz.ravel(), ph)
+    assert np.array_equal(cnt2, cnt3) and np.array_equal(acc2, acc3)
+    new2 = [rng.standard_normal((nx + 1) * ny).astype(np.float32), rng.standard_normal(nx * (ny + 1)).astype(np.float32)]
+    old2 = [rng.standard_normal((nx + 1) * ny).astype(np.float32), rng.standard_normal(nx * (ny + 1)).astype(np.float32)]
+    vel2 = rng.standard_normal(2 * n).astype(np.float32)
+    g2 = oracle.tp_g2p((nx, ny), (h, h), (0, 0), xy.ravel(), vel2, ph, new2, old2, 0.95, 0.9, 0.02)
+    z = np.zeros(nx * ny * 2, np.float32)
+    vel3 = np.concatenate([vel2.reshape(-1, 2), np.zeros((n, 1), np.float32)], 1).ravel()
+    g3 = oracle.tp3_g2p((nx, ny, 1), (h, h, h), (0, 0, 0), xyz.ravel(), vel3, ph, new2 + [z], old2 + [z], 0.95,
+                        0.9, 0.02)
+    assert np.array_equal(g3.reshape(-1, 3)[:, :2].ravel(), g2)

@@ -64,6 +64,18 @@ class TwoPhaseDesc(C.Structure):
                 ("max_particles_per_cell", C.c_int), ("extrapolation_depth", C.c_int), ("pressure", PressureDesc)]
 
 
+class TwoPhase3Desc(C.Structure):
+    _fields_ = [("resolution", C.c_int * 3), ("grid_spacing", C.c_double * 3), ("origin", C.c_double * 3),
+                ("max_particles", C.c_int), ("dt", C.c_double), ("gravity", C.c_double * 3),
+                ("ambient_density", C.c_double), ("component_density", C.c_double), ("mixing", C.c_double),
+                ("fade", C.c_double), ("concentration_atomic_scale", C.c_double), ("flip_ratio", C.c_double),
+                ("gas_flip_ratio", C.c_double), ("velocity_damping", C.c_double), ("p2g_atomic_scale", C.c_double),
+                ("weight_epsilon", C.c_double), ("closed_flags", C.c_int), ("max_substeps", C.c_int),
+                ("collider_push_thresh", C.c_double), ("collider_push_shift", C.c_double),
+                ("pin_cell", C.c_int * 3), ("resample_enabled", C.c_int), ("min_particles_per_cell", C.c_int),
+                ("max_particles_per_cell", C.c_int), ("extrapolation_depth", C.c_int), ("pressure", PressureDesc)]
+
+
 class Diag(C.Structure):
     _fields_ = [("converged", C.c_int), ("rejected", C.c_int), ("iterations", C.c_int),
                 ("stopped_by", C.c_int), ("residual", C.c_double), ("b_norm", C.c_double),
@@ -154,6 +166,12 @@ PROTOTYPES = {
     "ff_twophase2_stage": (_I, [_P, _I]),
     "ff_twophase2_step": (_I, [_P, C.POINTER(Diag)]),
     "ff_twophase2_resample_stats": (_I, [_P, C.POINTER(C.c_int64)]),
+    "ff_twophase3_desc_default": (None, [C.POINTER(TwoPhase3Desc), _IP, C.POINTER(C.c_double), _I, _D]),
+    "ff_twophase3_create": (_I, [_P, C.POINTER(TwoPhase3Desc), _P, _P, _P, _PP]),
+    "ff_twophase3_set_particles": (_I, [_P, _I, _FP, _FP, _FP]),
+    "ff_twophase3_get_particles": (_I, [_P, _I, _FP, _FP, _FP]),
+    "ff_twophase3_fields": (_I, [_P, _PP, _PP, _PP, _PP, _PP, _PP, _PP]),
+    "ff_twophase3_cell_counts": (_I, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "ff_flip3_resample_stats": (_I, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "ff_flip_box_seed3": (_I, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double), _I, _D,
                                C.c_uint32, _FP, C.c_int64, C.POINTER(C.c_int64)]),

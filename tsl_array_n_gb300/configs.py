@@ -18,6 +18,10 @@ bench.py measures): one JSON line per configuration on cuda:0.
 - c5: 3D FLIP dam break, 256 x 128 x 128, 2^3 particles per cell in a
   liquid column of 40% of the domain, 500 steps: ms per step; c5dump and
   c5solve save one of its pressure systems and solve it standalone.
+- c5tp: the configuration as specified: the same dam break with the air
+  simulated too (two-phase, liquid:air density 1000:1, variable-coefficient
+  projection), 500 steps, with plain FP32, mixed and learned+mixed
+  projections.
 
 All inputs are synthetic and seeded; every timing is taken with the device
 synchronised on both sides.
@@ -203,6 +207,68 @@ def c5(ctx, steps=500):
             "max_iterations": int(max(its)), "slowest_step_host_ms": round(worst * 1e3, 3)}
 
 
+def _two_phase_dam_break(precision, n=(256, 128, 128)):
+    """C5 as configured: a 3D two-phase dam break on n cells of h = 1/n[1]
+    (a 2 x 1 x 1 domain), 2^3 jittered particles in every cell, the liquid
+    column x < 1.6, y < 0.5 (40% of the volume) at density 1 and the rest
+    gas at 0.001 (1000:1), FLIP/PIC 0.95, gravity -9.81, 5-level MGPCG whose
+    coarsest level is swept (its density-weighted operator changes every
+    step)."""
+    h = 1.0 / n[1]
+    hh = (h, h, h)
+    grid = ff.FaceCenteredGrid3(n, hh)
+    seed = ff.compute_two_phase_box_seed3((0.0, 0.0, 0.0), (n[0] * h, n[1] * h, n[2] * h), hh, (0.0, 0.0, 0.0),
+                                          (0.8 * n[0] * h, 0.5 * n[1] * h, n[2] * h))
+    npart = seed["count"]
+    s = ff.create_grid_two_phase_flip_solver3(
+        velocity_grid=grid, max_particles=npart, dt=0.002, liquid_density=1.0, gas_density=0.001, flip_ratio=0.95,
+        pressure={"multigrid": {"numberOfLevels": 5, "coarseSolve": "sweeps"}, "tolerance": 1e-6,
+                  "precision": precision})
+    s.set_particles(seed["positionsArray"], np.zeros(3 * npart, np.float32), seed["phasesArray"])
+    return grid, s, npart, seed
+
+
+def c5tp(ctx, steps=500):
+    """The two-phase dam break with each projection arm: plain FP32 MGPCG,
+    mixed precision, and mixed with the learned warm start (the network's
+    forward pass inside every step); ms per step, PCG iterations per
+    projection, convergence."""
+    from . import warmstart
+    import os
+    out = {"config": "C5 3D two-phase FLIP dam break 256x128x128, 8 particles per cell, liquid column 40%, "
+                     "density 1000:1, FLIP 0.95", "steps": steps, "arms": {}}
+    weights = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "unet_warmstart.npy")
+    for arm in ("fp32", "mixed", "learned+mixed"):
+        grid, s, npart, seed = _two_phase_dam_break("fp32" if arm == "fp32" else "mixed")
+        net = None
+        if arm == "learned+mixed":
+            net = warmstart.UNetWarmStart(seed=1)
+            if os.path.exists(weights):
+                net.load(weights)
+            warmstart.attach(s.pressure_solver, net)
+        out["particles"] = npart
+        for _ in range(3):
+            s.on_advance_time_step()
+        its, conv, used = [], 0, 0
+        t0 = _now(ctx)
+        for _ in range(steps):
+            d = s.on_advance_time_step()
+            its.append(d["iterations"])
+            conv += int(d["converged"])
+        ms = (_now(ctx) - t0) / steps * 1e3
+        pos, _, ph = s.get_particles(npart)
+        liquid_y = float(pos.reshape(-1, 3)[ph > 0.5, 1].mean())
+        out["arms"][arm] = {"ms_per_step": round(ms, 3), "mean_iterations": float(np.mean(its)),
+                            "max_iterations": int(max(its)), "converged_fraction": conv / steps,
+                            "liquid_centroid_y": round(liquid_y, 4)}
+        if net is not None:
+            warmstart.attach(s.pressure_solver, None)
+            net.close()
+        s.close()
+        del grid, s
+    return out
+
+
 def c5dump(ctx, steps, path):
     """Run the dam break `steps` steps and save the last projection's
     system (Dirichlet active/target cells and b) to `path` (.npz)."""
@@ -249,7 +315,7 @@ def main(argv):
     runs = []
     for a in argv:
         name, _, rest = a.partition(":")
-        if name in ("c1", "c2", "c4", "c5"):
+        if name in ("c1", "c2", "c4", "c5", "c5tp"):
             runs.append((name, {"steps": int(rest)} if rest else {}))
         elif name == "c5dump":
             steps, _, path = rest.partition(":")

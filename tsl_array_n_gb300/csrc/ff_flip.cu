@@ -481,8 +481,9 @@ __global__ void __launch_bounds__(256) k_rs_claim(G3 g, const int *__restrict__ 
     }
 }
 
-// ---- per-phase resampling of the 2D two-phase solver
-// (grid_two_phase_flip_solver2.js:1226-1500) on the one-cell-thick grid.
+// ---- per-phase resampling of the two-phase solvers
+// (grid_two_phase_flip_solver2.js:1226-1500), on the one-cell-thick grid of
+// the 2D solver or the full grid of the 3D one.
 // Two donor pools share one buffer: liquid donors (phase > 0.5) rank
 // upward from 0, gas donors downward from the top, each capped at
 // pool_half; a cell's need is signed (+ liquid, - gas) and each phase's
@@ -491,20 +492,33 @@ __global__ void __launch_bounds__(256) k_rs_claim(G3 g, const int *__restrict__ 
 // computeRecipientNeedKernel (:1298-1310): eligible below min_pc with at
 // least 2 of the 4 clamped neighbours at min_pc or more; the phase is the
 // cell's own majority, or its neighbours' when it is empty
-// (recipientWantsLiquid, :1270-1296)
+// (recipientWantsLiquid, :1270-1296).  On a 3D grid (nz > 1) the neighbours
+// are the 6 clamped face neighbours and at least 3 must be full, the rule of
+// the 3D single-phase pass (grid_flip_solver3.js:700-724).
 __global__ void k_tp_need(G3 g, const int *__restrict__ cnt, const int *__restrict__ acc, float cscale, int min_pc,
                           int *__restrict__ need) {
-    const long long nc = (long long)g.nx * g.ny;
+    const long long plane = (long long)g.nx * g.ny, nc = plane * g.nz;
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < nc; c += (long long)gridDim.x * blockDim.x) {
-        const int j = (int)(c / g.nx), i = (int)(c - (long long)j * g.nx);
+        const int k = (int)(c / plane);
+        const long long rem = c - (long long)k * plane;
+        const int j = (int)(rem / g.nx), i = (int)(rem - (long long)j * g.nx);
         const long long l = i > 0 ? c - 1 : c, r = i < g.nx - 1 ? c + 1 : c;
         const long long d = j > 0 ? c - g.nx : c, u = j < g.ny - 1 ? c + g.nx : c;
         const int count = cnt[c];
-        const int nb = (cnt[l] >= min_pc) + (cnt[r] >= min_pc) + (cnt[d] >= min_pc) + (cnt[u] >= min_pc);
-        const bool eligible = count < min_pc && nb >= 2;
+        int nb = (cnt[l] >= min_pc) + (cnt[r] >= min_pc) + (cnt[d] >= min_pc) + (cnt[u] >= min_pc);
+        int ctot = cnt[l] + cnt[r] + cnt[d] + cnt[u], atot = acc[l] + acc[r] + acc[d] + acc[u];
+        int min_nb = 2;
+        if (g.nz > 1) {
+            const long long b = k > 0 ? c - plane : c, f = k < g.nz - 1 ? c + plane : c;
+            nb += (cnt[b] >= min_pc) + (cnt[f] >= min_pc);
+            ctot += cnt[b] + cnt[f];
+            atot += acc[b] + acc[f];
+            min_nb = 3;
+        }
+        const bool eligible = count < min_pc && nb >= min_nb;
         const float total = (float)count, sum = (float)acc[c] / cscale;
-        const float ntot = (float)(cnt[l] + cnt[r] + cnt[d] + cnt[u]);
-        const float nsum = (float)(acc[l] + acc[r] + acc[d] + acc[u]) / cscale;
+        const float ntot = (float)ctot;
+        const float nsum = (float)atot / cscale;
         const float own = sum / fmaxf(total, 1.0f), around = nsum / fmaxf(ntot, 1.0f);
         const bool liquid = total > 0.5f ? own > 0.5f : around > 0.5f;
         const int needed = min_pc - count;
@@ -548,7 +562,7 @@ __global__ void __launch_bounds__(256) k_tp_sums(G3 g, long long n, const float 
     const bool parts = (int)blockIdx.x < nbp;
     const long long b = parts ? blockIdx.x : blockIdx.x - nbp;
     const long long first = b * RS_CHUNK + (threadIdx.x >> 5) * RS_WARP_ITEMS + (threadIdx.x & 31);
-    const long long nc = (long long)g.nx * g.ny;
+    const long long nc = (long long)g.nx * g.ny * g.nz;
     long long ml = 0, mg = 0;
     for (int r = 0; r < RS_ROUNDS; ++r) {
         const long long x = first + 32 * r;
@@ -635,7 +649,7 @@ __global__ void __launch_bounds__(256) k_tp_claim(G3 g, const int *__restrict__ 
                                                   const float *__restrict__ v, const float *__restrict__ w,
                                                   float *__restrict__ pos, float *__restrict__ vel) {
     const int lane = threadIdx.x & 31;
-    const long long nc = (long long)g.nx * g.ny;
+    const long long plane = (long long)g.nx * g.ny, nc = plane * g.nz;
     const long long first = blockIdx.x * (long long)RS_CHUNK + (threadIdx.x >> 5) * RS_WARP_ITEMS + lane;
     int q[RS_ROUNDS];
     long long ml = 0, mg = 0;
@@ -665,8 +679,10 @@ __global__ void __launch_bounds__(256) k_tp_claim(G3 g, const int *__restrict__ 
         const long long needed = liquid ? nl : ng, slot0 = liquid ? sl : sg, avail = liquid ? avail_l : avail_g;
         if (slot0 >= avail) continue;
         const long long c = first + 32 * r;
-        const int j = (int)(c / g.nx), i = (int)(c - (long long)j * g.nx);
-        F3 qp = index_pos(g, comp_origin(g, 3), i, j, 0);
+        const int k = (int)(c / plane);
+        const long long rem = c - (long long)k * plane;
+        const int j = (int)(rem / g.nx), i = (int)(rem - (long long)j * g.nx);
+        F3 qp = index_pos(g, comp_origin(g, 3), i, j, k);
         float vq[3];
         for (int a = 0; a < 3; ++a) {
             int sx, sy, sz;
@@ -1217,16 +1233,17 @@ extern "C" void ff_twophase_desc_default(ff_twophase_desc *d, const int *res, co
 
 struct ff_twophase_s {
     ff_ctx ctx = nullptr;
-    ff_twophase_desc desc{};
+    int dims = 2;                   // 2: the one-cell-thick stand-in of the 2D solver; 3: a full grid
+    ff_twophase_desc desc{};        // the 2D solver's options as given
+    ff_twophase3_desc d{};          // the options on three axes (the 2D ones with nz = 1)
     G3 g{};
     int count = 0;
-    ff_field u = nullptr, v = nullptr, phi = nullptr;   // borrowed
-    ff_field w = nullptr;                               // internal zero z velocity
+    ff_field u = nullptr, v = nullptr, w = nullptr, phi = nullptr;   // borrowed (w owned in 2D)
     ff_field pos = nullptr, vel = nullptr, phase = nullptr, frac = nullptr, rho = nullptr, beta[3] = {};
     ff_field active = nullptr, target = nullptr;
-    float *old[2] = {};
-    int *num[2] = {}, *den[2] = {}, *valid[2] = {}, *vtmp[2][2] = {};
-    float *scratch[2] = {};
+    float *old[3] = {};
+    int *num[3] = {}, *den[3] = {}, *valid[3] = {}, *vtmp[2][3] = {};
+    float *scratch[3] = {};
     int *ccnt = nullptr, *cacc = nullptr;
     int *rs_need = nullptr, *rs_pool = nullptr;
     long long *rs_bsum = nullptr, *rs_tot = nullptr;
@@ -1242,10 +1259,10 @@ extern "C" int ff_twophase2_destroy(ff_twophase t) {
     cudaStreamSynchronize(t->ctx->stream);
     ff_pressure3_destroy(t->ps);
     ff_bc3_destroy(t->bc);
-    ff_field fs[] = {t->w, t->pos, t->vel, t->phase, t->frac, t->rho, t->beta[0], t->beta[1], t->beta[2],
-                     t->active, t->target};
+    ff_field fs[] = {t->dims == 2 ? t->w : nullptr, t->pos, t->vel, t->phase, t->frac, t->rho, t->beta[0],
+                     t->beta[1], t->beta[2], t->active, t->target};
     for (ff_field x : fs) ff_field_destroy(x);
-    for (int a = 0; a < 2; ++a) {
+    for (int a = 0; a < 3; ++a) {
         ff_dev_free(t->old[a]);
         ff_dev_free(t->num[a]);
         ff_dev_free(t->den[a]);
@@ -1257,6 +1274,101 @@ extern "C" int ff_twophase2_destroy(ff_twophase t) {
     void *ps[] = {t->ccnt, t->cacc, t->rs_need, t->rs_pool, t->rs_bsum, t->rs_tot};
     for (void *p : ps) ff_dev_free(p);
     delete t;
+    return FF_OK;
+}
+
+// The buffers, boundary solver and pressure solver of a two-phase solver
+// whose t->d, t->g, t->dims, t->u, t->v (and t->w in 3D) are set.
+static int tp_setup(ff_twophase t) {
+    ff_ctx ctx = t->ctx;
+    const ff_twophase3_desc &d = t->d;
+    const int nx = t->g.nx, ny = t->g.ny, nz = t->g.nz;
+    t->count = d.max_particles;
+    t->r0 = std::max((float)d.ambient_density, MIN_DENSITY);
+    t->r1 = std::max((float)d.component_density, MIN_DENSITY);
+    t->rref = std::max(t->r0, t->r1);
+    cudaStream_t s = ctx->stream;
+    int st = FF_OK;
+    const int np[1] = {d.max_particles};
+    const int cs[3] = {nx, ny, nz};
+    const long long nc = (long long)nx * ny * nz;
+    if (t->dims == 2) {
+        const int ws[3] = {nx, ny, 2};
+        if ((st = ff_field_create(ctx, FF_FLOAT, 3, ws, &t->w))) return st;
+    }
+    if ((st = ff_field_create(ctx, FF_VEC3, 1, np, &t->pos))) return st;
+    if ((st = ff_field_create(ctx, FF_VEC3, 1, np, &t->vel))) return st;
+    if ((st = ff_field_create(ctx, FF_FLOAT, 1, np, &t->phase))) return st;
+    if ((st = ff_field_create(ctx, FF_FLOAT, 3, cs, &t->frac))) return st;
+    if ((st = ff_field_create(ctx, FF_FLOAT, 3, cs, &t->rho))) return st;
+    if ((st = ff_field_create(ctx, FF_UINT8, 3, cs, &t->active))) return st;
+    if ((st = ff_field_create(ctx, FF_FLOAT, 3, cs, &t->target))) return st;
+    if ((st = ff_field_fill(t->rho, (float)d.component_density))) return st;
+    // particles start at rest at the origin corner (on the centre plane in
+    // 2D), all gas until seeded (:599-606)
+    {
+        std::vector<float> p3((size_t)3 * d.max_particles, 0.0f);
+        for (size_t p = 0; p < (size_t)d.max_particles; ++p) {
+            p3[3 * p] = t->dims == 2 ? 0.0f : t->g.ox;
+            p3[3 * p + 1] = t->dims == 2 ? 0.0f : t->g.oy;
+            p3[3 * p + 2] = t->dims == 2 ? t->g.oz + t->g.hz * 0.5f : t->g.oz;
+        }
+        if ((st = ff_field_upload(t->pos, p3.data(), p3.size() * 4))) return st;
+        if (cudaMemsetAsync(t->vel->d, 0, t->vel->bytes, s) != cudaSuccess ||
+            cudaMemsetAsync(t->phase->d, 0, t->phase->bytes, s) != cudaSuccess)
+            return ff_set_error(FF_E_CUDA, "twophase");
+    }
+    for (int a = 0; a < 3; ++a) {
+        const int fs3[3] = {nx + (a == 0), ny + (a == 1), nz + (a == 2)};
+        if ((st = ff_field_create(ctx, FF_FLOAT, 3, fs3, &t->beta[a]))) return st;
+        if ((st = ff_field_fill(t->beta[a], 1.0f))) return st;
+    }
+    for (int a = 0; a < t->dims; ++a) {
+        const size_t b = (size_t)comp_n(t->g, a) * 4;
+        if ((st = ff_dev_alloc((void **)&t->old[a], b, s))) return st;
+        if ((st = ff_dev_alloc((void **)&t->num[a], b, s))) return st;
+        if ((st = ff_dev_alloc((void **)&t->den[a], b, s))) return st;
+        if ((st = ff_dev_alloc((void **)&t->valid[a], b, s))) return st;
+        if ((st = ff_dev_alloc((void **)&t->vtmp[0][a], b, s))) return st;
+        if ((st = ff_dev_alloc((void **)&t->vtmp[1][a], b, s))) return st;
+        if ((st = ff_dev_alloc((void **)&t->scratch[a], b, s))) return st;
+    }
+    if ((st = ff_dev_alloc((void **)&t->ccnt, (size_t)nc * 4, s))) return st;
+    if ((st = ff_dev_alloc((void **)&t->cacc, (size_t)nc * 4, s))) return st;
+    if (d.resample_enabled) {
+        t->rs_nbp = (int)(((long long)d.max_particles + RS_CHUNK - 1) / RS_CHUNK);
+        t->rs_nbc = (int)((nc + RS_CHUNK - 1) / RS_CHUNK);
+        if ((st = ff_dev_alloc((void **)&t->rs_need, (size_t)nc * 4, s))) return st;
+        if ((st = ff_dev_alloc((void **)&t->rs_pool, (size_t)d.max_particles * 4, s))) return st;
+        if ((st = ff_dev_alloc((void **)&t->rs_bsum, (size_t)2 * (t->rs_nbp + t->rs_nbc) * 8, s))) return st;
+        if ((st = ff_dev_alloc((void **)&t->rs_tot, 32, s))) return st;
+        if (cudaMemsetAsync(t->rs_tot, 0, 32, s) != cudaSuccess) return ff_set_error(FF_E_CUDA, "twophase");
+    }
+    // the pressure pin as a Dirichlet cell at 0 (dirichletAt, :786-795)
+    {
+        std::vector<uint8_t> act((size_t)nc, 0);
+        if (d.pin_cell[0] >= 0)
+            act[(size_t)d.pin_cell[0] + (size_t)nx * (d.pin_cell[1] + (size_t)ny * d.pin_cell[2])] = 1;
+        if ((st = ff_field_upload(t->active, act.data(), act.size()))) return st;
+        if (cudaMemsetAsync(t->target->d, 0, (size_t)nc * 4, s) != cudaSuccess)
+            return ff_set_error(FF_E_CUDA, "twophase");
+    }
+    const int r3[3] = {nx, ny, nz};
+    const double h3[3] = {d.grid_spacing[0], d.grid_spacing[1], d.grid_spacing[2]};
+    const double o3[3] = {d.origin[0], d.origin[1], d.origin[2]};
+    if ((st = ff_bc3_create(ctx, r3, h3, o3, &t->bc))) return st;
+    if ((st = ff_bc3_set_closed(t->bc, t->dims == 2 ? (d.closed_flags & 15) | 48 : d.closed_flags))) return st;
+    ff_pressure_desc pd = d.pressure;
+    for (int a = 0; a < 3; ++a) {
+        pd.resolution[a] = r3[a];
+        pd.grid_spacing[a] = h3[a];
+        pd.origin[a] = o3[a];
+    }
+    if ((st = ff_pressure3_create(ctx, &pd, &t->ps))) return st;
+    if ((st = ff_pressure3_set_dirichlet(t->ps, t->active, t->target))) return st;
+    if ((st = ff_pressure3_set_face_weights(t->ps, t->beta[0], t->beta[1], t->dims == 3 ? t->beta[2] : nullptr)))
+        return st;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return ff_set_error(FF_E_CUDA, "two-phase create sync");
     return FF_OK;
 }
 
@@ -1276,10 +1388,49 @@ extern "C" int ff_twophase2_create(ff_ctx ctx, const ff_twophase_desc *d, ff_fie
     FF_CHECK(d->max_substeps > 0, FF_E_ARG, "createGridTwoPhaseFlipSolver2: maxSubsteps must be positive");
     *out = nullptr;
     cudaSetDevice(ctx->device);
+    const int nx = d->resolution[0], ny = d->resolution[1];
+    if (!u || !v || u->dtype != FF_FLOAT || v->dtype != FF_FLOAT || u->count != (long long)(nx + 1) * ny ||
+        v->count != (long long)nx * (ny + 1))
+        return ff_set_error(FF_E_ARG, "createGridTwoPhaseFlipSolver2: velocity grid has the wrong shape");
     ff_twophase t = new ff_twophase_s();
     t->ctx = ctx;
+    t->dims = 2;
     t->desc = *d;
-    const int nx = d->resolution[0], ny = d->resolution[1];
+    // the options on three axes: one cell thick, hz = max(hx, hy) (the
+    // trace's minimum spacing), no z gravity, the pin on the plane k = 0
+    ff_twophase3_desc &e = t->d;
+    std::memset(&e, 0, sizeof e);
+    for (int a = 0; a < 2; ++a) {
+        e.resolution[a] = d->resolution[a];
+        e.grid_spacing[a] = d->grid_spacing[a];
+        e.origin[a] = d->origin[a];
+        e.gravity[a] = d->gravity[a];
+        e.pin_cell[a] = d->pin_cell[a];
+    }
+    e.resolution[2] = 1;
+    e.grid_spacing[2] = std::max(d->grid_spacing[0], d->grid_spacing[1]);
+    e.pin_cell[2] = d->pin_cell[0] < 0 ? -1 : 0;
+    e.max_particles = d->max_particles;
+    e.dt = d->dt;
+    e.ambient_density = d->ambient_density;
+    e.component_density = d->component_density;
+    e.mixing = d->mixing;
+    e.fade = d->fade;
+    e.concentration_atomic_scale = d->concentration_atomic_scale;
+    e.flip_ratio = d->flip_ratio;
+    e.gas_flip_ratio = d->gas_flip_ratio;
+    e.velocity_damping = d->velocity_damping;
+    e.p2g_atomic_scale = d->p2g_atomic_scale;
+    e.weight_epsilon = d->weight_epsilon;
+    e.closed_flags = d->closed_flags;
+    e.max_substeps = d->max_substeps;
+    e.collider_push_thresh = d->collider_push_thresh;
+    e.collider_push_shift = d->collider_push_shift;
+    e.resample_enabled = d->resample_enabled;
+    e.min_particles_per_cell = d->min_particles_per_cell;
+    e.max_particles_per_cell = d->max_particles_per_cell;
+    e.extrapolation_depth = d->extrapolation_depth;
+    e.pressure = d->pressure;
     t->g.nx = nx;
     t->g.ny = ny;
     t->g.nz = 1;
@@ -1289,112 +1440,118 @@ extern "C" int ff_twophase2_create(ff_ctx ctx, const ff_twophase_desc *d, ff_fie
     t->g.ox = (float)d->origin[0];
     t->g.oy = (float)d->origin[1];
     t->g.oz = 0.0f;
-    if (!u || !v || u->dtype != FF_FLOAT || v->dtype != FF_FLOAT || u->count != (long long)(nx + 1) * ny ||
-        v->count != (long long)nx * (ny + 1)) {
-        delete t;
-        return ff_set_error(FF_E_ARG, "createGridTwoPhaseFlipSolver2: velocity grid has the wrong shape");
-    }
     t->u = u;
     t->v = v;
-    t->count = d->max_particles;
-    t->r0 = std::max((float)d->ambient_density, MIN_DENSITY);
-    t->r1 = std::max((float)d->component_density, MIN_DENSITY);
-    t->rref = std::max(t->r0, t->r1);
-    cudaStream_t s = ctx->stream;
-    int st = FF_OK;
-    auto bail = [&](int code) { ff_twophase2_destroy(t); return code; };
-    const int np[1] = {d->max_particles};
-    const int cs[3] = {nx, ny, 1}, ws[3] = {nx, ny, 2};
-    const long long nc = (long long)nx * ny;
-    if ((st = ff_field_create(ctx, FF_FLOAT, 3, ws, &t->w))) return bail(st);
-    if ((st = ff_field_create(ctx, FF_VEC3, 1, np, &t->pos))) return bail(st);
-    if ((st = ff_field_create(ctx, FF_VEC3, 1, np, &t->vel))) return bail(st);
-    if ((st = ff_field_create(ctx, FF_FLOAT, 1, np, &t->phase))) return bail(st);
-    if ((st = ff_field_create(ctx, FF_FLOAT, 3, cs, &t->frac))) return bail(st);
-    if ((st = ff_field_create(ctx, FF_FLOAT, 3, cs, &t->rho))) return bail(st);
-    if ((st = ff_field_create(ctx, FF_UINT8, 3, cs, &t->active))) return bail(st);
-    if ((st = ff_field_create(ctx, FF_FLOAT, 3, cs, &t->target))) return bail(st);
-    if ((st = ff_field_fill(t->rho, (float)d->component_density))) return bail(st);
-    // particles start at rest at (0, 0) on the centre plane, all gas until
-    // seeded (:599-606)
-    {
-        std::vector<float> p3((size_t)3 * d->max_particles, 0.0f);
-        for (size_t p = 0; p < (size_t)d->max_particles; ++p) p3[3 * p + 2] = t->g.oz + t->g.hz * 0.5f;
-        if ((st = ff_field_upload(t->pos, p3.data(), p3.size() * 4))) return bail(st);
-        if (cudaMemsetAsync(t->vel->d, 0, t->vel->bytes, s) != cudaSuccess ||
-            cudaMemsetAsync(t->phase->d, 0, t->phase->bytes, s) != cudaSuccess)
-            return bail(ff_set_error(FF_E_CUDA, "twophase"));
+    const int st = tp_setup(t);
+    if (st != FF_OK) {
+        ff_twophase2_destroy(t);
+        return st;
     }
+    *out = t;
+    return FF_OK;
+}
+
+extern "C" void ff_twophase3_desc_default(ff_twophase3_desc *d, const int *res, const double *h, int max_particles,
+                                          double dt) {
+    std::memset(d, 0, sizeof *d);
     for (int a = 0; a < 3; ++a) {
-        const int fs3[3] = {nx + (a == 0), ny + (a == 1), 1 + (a == 2)};
-        if ((st = ff_field_create(ctx, FF_FLOAT, 3, fs3, &t->beta[a]))) return bail(st);
-        if ((st = ff_field_fill(t->beta[a], 1.0f))) return bail(st);
+        d->resolution[a] = res ? res[a] : 1;
+        d->grid_spacing[a] = h ? h[a] : 1.0;
     }
-    for (int a = 0; a < 2; ++a) {
-        const size_t b = (size_t)comp_n(t->g, a) * 4;
-        if ((st = ff_dev_alloc((void **)&t->old[a], b, s))) return bail(st);
-        if ((st = ff_dev_alloc((void **)&t->num[a], b, s))) return bail(st);
-        if ((st = ff_dev_alloc((void **)&t->den[a], b, s))) return bail(st);
-        if ((st = ff_dev_alloc((void **)&t->valid[a], b, s))) return bail(st);
-        if ((st = ff_dev_alloc((void **)&t->vtmp[0][a], b, s))) return bail(st);
-        if ((st = ff_dev_alloc((void **)&t->vtmp[1][a], b, s))) return bail(st);
-        if ((st = ff_dev_alloc((void **)&t->scratch[a], b, s))) return bail(st);
+    d->max_particles = max_particles;
+    d->dt = dt;
+    d->gravity[1] = -9.81;
+    d->ambient_density = 0.01;
+    d->component_density = 1.0;
+    d->concentration_atomic_scale = 4096.0;
+    d->flip_ratio = 0.97;
+    d->gas_flip_ratio = 0.90;
+    d->velocity_damping = 0.02;
+    d->p2g_atomic_scale = 65536.0;
+    d->weight_epsilon = 1e-4;
+    d->closed_flags = 63;
+    d->max_substeps = 32;
+    d->pin_cell[0] = d->resolution[0] / 2;
+    d->pin_cell[1] = d->resolution[1] - 1;
+    d->pin_cell[2] = d->resolution[2] / 2;
+    d->resample_enabled = 1;
+    d->min_particles_per_cell = 3;
+    d->max_particles_per_cell = 8;
+    d->extrapolation_depth = 5;
+    ff_pressure_desc_default(&d->pressure, d->resolution, d->grid_spacing);
+    int levels = 1;
+    while (levels < 5 && d->resolution[0] % (1 << levels) == 0 && d->resolution[1] % (1 << levels) == 0 &&
+           d->resolution[2] % (1 << levels) == 0)
+        ++levels;
+    d->pressure.mg_levels = levels;
+}
+
+extern "C" int ff_twophase3_create(ff_ctx ctx, const ff_twophase3_desc *d, ff_field u, ff_field v, ff_field w,
+                                   ff_twophase *out) {
+    FF_CHECK(ctx && d && out, FF_E_ARG, "ff_twophase3_create: NULL argument");
+    FF_CHECK(d->max_particles > 0, FF_E_ARG, "ff_twophase3_create: maxParticles is required.");
+    FF_CHECK(d->resolution[0] > 0 && d->resolution[1] > 0 && d->resolution[2] > 1, FF_E_ARG,
+             "ff_twophase3_create: bad resolution (nz must exceed 1; use ff_twophase2_create in 2D)");
+    FF_CHECK(d->component_density > 0 && d->ambient_density > 0, FF_E_ARG,
+             "ff_twophase3_create: both phase densities must be > 0, got %g and %g.", d->component_density,
+             d->ambient_density);
+    FF_CHECK(d->pin_cell[0] < 0 || (d->pin_cell[0] < d->resolution[0] && d->pin_cell[1] >= 0 &&
+                                    d->pin_cell[1] < d->resolution[1] && d->pin_cell[2] >= 0 &&
+                                    d->pin_cell[2] < d->resolution[2]),
+             FF_E_ARG, "ff_twophase3_create: pressure pin cell outside the grid");
+    FF_CHECK(d->max_substeps > 0, FF_E_ARG, "ff_twophase3_create: maxSubsteps must be positive");
+    *out = nullptr;
+    cudaSetDevice(ctx->device);
+    const int nx = d->resolution[0], ny = d->resolution[1], nz = d->resolution[2];
+    const long long want[3] = {(long long)(nx + 1) * ny * nz, (long long)nx * (ny + 1) * nz,
+                               (long long)nx * ny * (nz + 1)};
+    const ff_field uvw[3] = {u, v, w};
+    for (int a = 0; a < 3; ++a)
+        FF_CHECK(uvw[a] && uvw[a]->dtype == FF_FLOAT && uvw[a]->count == want[a], FF_E_ARG,
+                 "ff_twophase3_create: velocity grid has the wrong shape");
+    ff_twophase t = new ff_twophase_s();
+    t->ctx = ctx;
+    t->dims = 3;
+    t->d = *d;
+    t->g.nx = nx;
+    t->g.ny = ny;
+    t->g.nz = nz;
+    t->g.hx = (float)d->grid_spacing[0];
+    t->g.hy = (float)d->grid_spacing[1];
+    t->g.hz = (float)d->grid_spacing[2];
+    t->g.ox = (float)d->origin[0];
+    t->g.oy = (float)d->origin[1];
+    t->g.oz = (float)d->origin[2];
+    t->u = u;
+    t->v = v;
+    t->w = w;
+    const int st = tp_setup(t);
+    if (st != FF_OK) {
+        ff_twophase2_destroy(t);
+        return st;
     }
-    if ((st = ff_dev_alloc((void **)&t->ccnt, (size_t)nc * 4, s))) return bail(st);
-    if ((st = ff_dev_alloc((void **)&t->cacc, (size_t)nc * 4, s))) return bail(st);
-    if (d->resample_enabled) {
-        t->rs_nbp = (int)(((long long)d->max_particles + RS_CHUNK - 1) / RS_CHUNK);
-        t->rs_nbc = (int)((nc + RS_CHUNK - 1) / RS_CHUNK);
-        if ((st = ff_dev_alloc((void **)&t->rs_need, (size_t)nc * 4, s))) return bail(st);
-        if ((st = ff_dev_alloc((void **)&t->rs_pool, (size_t)d->max_particles * 4, s))) return bail(st);
-        if ((st = ff_dev_alloc((void **)&t->rs_bsum, (size_t)2 * (t->rs_nbp + t->rs_nbc) * 8, s))) return bail(st);
-        if ((st = ff_dev_alloc((void **)&t->rs_tot, 32, s))) return bail(st);
-        if (cudaMemsetAsync(t->rs_tot, 0, 32, s) != cudaSuccess) return bail(ff_set_error(FF_E_CUDA, "twophase"));
-    }
-    // the pressure pin as a Dirichlet cell at 0 (dirichletAt, :786-795)
-    {
-        std::vector<uint8_t> act((size_t)nc, 0);
-        if (d->pin_cell[0] >= 0) act[(size_t)d->pin_cell[0] + (size_t)nx * d->pin_cell[1]] = 1;
-        if ((st = ff_field_upload(t->active, act.data(), act.size()))) return bail(st);
-        if (cudaMemsetAsync(t->target->d, 0, (size_t)nc * 4, s) != cudaSuccess)
-            return bail(ff_set_error(FF_E_CUDA, "twophase"));
-    }
-    const int r3[3] = {nx, ny, 1};
-    const double h3[3] = {d->grid_spacing[0], d->grid_spacing[1], (double)t->g.hz};
-    const double o3[3] = {d->origin[0], d->origin[1], 0.0};
-    if ((st = ff_bc3_create(ctx, r3, h3, o3, &t->bc))) return bail(st);
-    if ((st = ff_bc3_set_closed(t->bc, (d->closed_flags & 15) | 48))) return bail(st);
-    ff_pressure_desc pd = d->pressure;
-    for (int a = 0; a < 3; ++a) {
-        pd.resolution[a] = r3[a];
-        pd.grid_spacing[a] = h3[a];
-        pd.origin[a] = o3[a];
-    }
-    if ((st = ff_pressure3_create(ctx, &pd, &t->ps))) return bail(st);
-    if ((st = ff_pressure3_set_dirichlet(t->ps, t->active, t->target))) return bail(st);
-    if ((st = ff_pressure3_set_face_weights(t->ps, t->beta[0], t->beta[1], t->beta[2]))) return bail(st);
-    if (cudaStreamSynchronize(s) != cudaSuccess) return bail(ff_set_error(FF_E_CUDA, "two-phase create sync"));
     *out = t;
     return FF_OK;
 }
 
 extern "C" int ff_twophase2_set_collider(ff_twophase t, ff_field phi) {
     FF_CHECK(t, FF_E_ARG, "NULL two-phase solver");
-    FF_CHECK(!phi || (phi->dtype == FF_FLOAT && phi->count == (long long)t->g.nx * t->g.ny), FF_E_ARG,
+    FF_CHECK(!phi || (phi->dtype == FF_FLOAT && phi->count == (long long)t->g.nx * t->g.ny * t->g.nz), FF_E_ARG,
              "two-phase collider must be a float cell SDF");
     t->phi = phi;
     return ff_bc3_set_collider(t->bc, phi, nullptr, nullptr, nullptr);
 }
 
 extern "C" int ff_twophase2_set_count(ff_twophase t, int n) {
-    FF_CHECK(t && n >= 0 && n <= t->desc.max_particles, FF_E_ARG, "two-phase particle count out of range");
+    FF_CHECK(t && n >= 0 && n <= t->d.max_particles, FF_E_ARG, "two-phase particle count out of range");
     t->count = n;
     return FF_OK;
 }
 
 extern "C" int ff_twophase2_set_particles(ff_twophase t, int n, const float *xy, const float *vxy,
                                           const float *phase) {
-    FF_CHECK(t && n >= 0 && n <= t->desc.max_particles, FF_E_ARG, "two-phase particle upload: bad count");
+    FF_CHECK(t && n >= 0 && n <= t->d.max_particles, FF_E_ARG, "two-phase particle upload: bad count");
+    FF_CHECK(t->dims == 2, FF_E_ARG, "two-phase particle upload: a 3D solver takes ff_twophase3_set_particles");
     cudaSetDevice(t->ctx->device);
     const float zc = t->g.oz + t->g.hz * 0.5f;
     std::vector<float> p3((size_t)3 * n), v3((size_t)3 * n);
@@ -1419,7 +1576,8 @@ extern "C" int ff_twophase2_set_particles(ff_twophase t, int n, const float *xy,
 }
 
 extern "C" int ff_twophase2_get_particles(ff_twophase t, int n, float *xy, float *vxy, float *phase) {
-    FF_CHECK(t && n >= 0 && n <= t->desc.max_particles, FF_E_ARG, "two-phase particle download: bad count");
+    FF_CHECK(t && n >= 0 && n <= t->d.max_particles, FF_E_ARG, "two-phase particle download: bad count");
+    FF_CHECK(t->dims == 2, FF_E_ARG, "two-phase particle download: a 3D solver takes ff_twophase3_get_particles");
     cudaSetDevice(t->ctx->device);
     cudaStream_t s = t->ctx->stream;
     std::vector<float> p3((size_t)3 * n), v3((size_t)3 * n);
@@ -1435,6 +1593,31 @@ extern "C" int ff_twophase2_get_particles(ff_twophase t, int n, float *xy, float
     return FF_OK;
 }
 
+extern "C" int ff_twophase3_set_particles(ff_twophase t, int n, const float *xyz, const float *vxyz,
+                                          const float *phase) {
+    FF_CHECK(t && n >= 0 && n <= t->d.max_particles, FF_E_ARG, "two-phase particle upload: bad count");
+    FF_CHECK(t->dims == 3, FF_E_ARG, "two-phase particle upload: a 2D solver takes ff_twophase2_set_particles");
+    cudaSetDevice(t->ctx->device);
+    cudaStream_t s = t->ctx->stream;
+    if (n && xyz) FF_CUDA(cudaMemcpyAsync(t->pos->d, xyz, (size_t)n * 12, cudaMemcpyHostToDevice, s));
+    if (n && vxyz) FF_CUDA(cudaMemcpyAsync(t->vel->d, vxyz, (size_t)n * 12, cudaMemcpyHostToDevice, s));
+    if (n && phase) FF_CUDA(cudaMemcpyAsync(t->phase->d, phase, (size_t)n * 4, cudaMemcpyHostToDevice, s));
+    FF_CUDA(cudaStreamSynchronize(s));
+    return FF_OK;
+}
+
+extern "C" int ff_twophase3_get_particles(ff_twophase t, int n, float *xyz, float *vxyz, float *phase) {
+    FF_CHECK(t && n >= 0 && n <= t->d.max_particles, FF_E_ARG, "two-phase particle download: bad count");
+    FF_CHECK(t->dims == 3, FF_E_ARG, "two-phase particle download: a 2D solver takes ff_twophase2_get_particles");
+    cudaSetDevice(t->ctx->device);
+    cudaStream_t s = t->ctx->stream;
+    if (n && xyz) FF_CUDA(cudaMemcpyAsync(xyz, t->pos->d, (size_t)n * 12, cudaMemcpyDeviceToHost, s));
+    if (n && vxyz) FF_CUDA(cudaMemcpyAsync(vxyz, t->vel->d, (size_t)n * 12, cudaMemcpyDeviceToHost, s));
+    if (n && phase) FF_CUDA(cudaMemcpyAsync(phase, t->phase->d, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+    FF_CUDA(cudaStreamSynchronize(s));
+    return FF_OK;
+}
+
 extern "C" int ff_twophase2_fields(ff_twophase t, ff_field *phase, ff_field *liquid_fraction, ff_field *density,
                                    ff_field *beta_u, ff_field *beta_v, ff_pressure *pressure) {
     FF_CHECK(t, FF_E_ARG, "NULL two-phase solver");
@@ -1447,6 +1630,24 @@ extern "C" int ff_twophase2_fields(ff_twophase t, ff_field *phase, ff_field *liq
     return FF_OK;
 }
 
+extern "C" int ff_twophase3_fields(ff_twophase t, ff_field *phase, ff_field *liquid_fraction, ff_field *density,
+                                   ff_field *beta_u, ff_field *beta_v, ff_field *beta_w, ff_pressure *pressure) {
+    FF_TRY(ff_twophase2_fields(t, phase, liquid_fraction, density, beta_u, beta_v, pressure));
+    if (beta_w) *beta_w = t->beta[2];
+    return FF_OK;
+}
+
+extern "C" int ff_twophase3_cell_counts(ff_twophase t, int32_t *count, int32_t *sum) {
+    FF_CHECK(t, FF_E_ARG, "NULL two-phase solver");
+    cudaSetDevice(t->ctx->device);
+    cudaStream_t s = t->ctx->stream;
+    const size_t nc = (size_t)t->g.nx * t->g.ny * t->g.nz;
+    if (count) FF_CUDA(cudaMemcpyAsync(count, t->ccnt, nc * 4, cudaMemcpyDeviceToHost, s));
+    if (sum) FF_CUDA(cudaMemcpyAsync(sum, t->cacc, nc * 4, cudaMemcpyDeviceToHost, s));
+    FF_CUDA(cudaStreamSynchronize(s));
+    return FF_OK;
+}
+
 static int tp_extrapolate(ff_twophase t, float *data, const int *marker, int a) {
     cudaStream_t s = t->ctx->stream;
     int sx, sy, sz;
@@ -1455,7 +1656,7 @@ static int tp_extrapolate(ff_twophase t, float *data, const int *marker, int a) 
     FF_CUDA(cudaMemcpyAsync(t->vtmp[0][a], marker, n * 4, cudaMemcpyDeviceToDevice, s));
     float *src = data, *dst = t->scratch[a];
     int *vs = t->vtmp[0][a], *vd = t->vtmp[1][a];
-    for (int it = 0; it < t->desc.extrapolation_depth; ++it) {
+    for (int it = 0; it < t->d.extrapolation_depth; ++it) {
         k_extrapolate<<<blocks_for(n), 256, 0, s>>>(sx, sy, sz, src, dst, vs, vd);
         std::swap(src, dst);
         std::swap(vs, vd);
@@ -1464,29 +1665,35 @@ static int tp_extrapolate(ff_twophase t, float *data, const int *marker, int a) 
     return post("extrapolate");
 }
 
-// One stage of onAdvanceTimeStep (:1505-1592).
+// One stage of onAdvanceTimeStep (:1505-1592).  The 2D solver's grid is one
+// cell thick with an internal zero w; the 3D solver moves all three
+// components.
 extern "C" int ff_twophase2_stage(ff_twophase t, int stage) {
     FF_CHECK(t, FF_E_ARG, "NULL two-phase solver");
     cudaSetDevice(t->ctx->device);
     cudaStream_t s = t->ctx->stream;
-    const ff_twophase_desc &d = t->desc;
+    const ff_twophase3_desc &d = t->d;
     const G3 &g = t->g;
-    const long long n = t->count, nc = (long long)g.nx * g.ny;
-    float *uv[2] = {(float *)t->u->d, (float *)t->v->d};
-    float *w = (float *)t->w->d;
+    const bool three = t->dims == 3;
+    const int na = t->dims;
+    const long long n = t->count, nc = (long long)g.nx * g.ny * g.nz;
+    float *uvw[3] = {(float *)t->u->d, (float *)t->v->d, (float *)t->w->d};
+    float *w = uvw[2];
     float *pos = (float *)t->pos->d, *vel = (float *)t->vel->d, *ph = (float *)t->phase->d;
     const float cscale = (float)d.concentration_atomic_scale;
     switch (stage) {
     case FF_TP_ADVECT: {
         // advectParticles + pushOutOfCollider (:1098-1124)
-        FF_CUDA(cudaMemsetAsync(w, 0, comp_n(g, 2) * 4, s));
+        if (!three) FF_CUDA(cudaMemsetAsync(w, 0, comp_n(g, 2) * 4, s));
         if (n == 0) return FF_OK;
-        VelField F{g, uv[0], uv[1], w, t->phi ? (const float *)t->phi->d : nullptr};
+        VelField F{g, uvw[0], uvw[1], w, t->phi ? (const float *)t->phi->d : nullptr};
         const F3 mn{g.ox + 1e-4f, g.oy + 1e-4f, g.oz + 1e-4f};
         const F3 mx{(g.ox + (float)(d.resolution[0] * d.grid_spacing[0])) - 1e-4f,
-                    (g.oy + (float)(d.resolution[1] * d.grid_spacing[1])) - 1e-4f, (g.oz + g.hz) - 1e-4f};
+                    (g.oy + (float)(d.resolution[1] * d.grid_spacing[1])) - 1e-4f,
+                    three ? (g.oz + (float)(d.resolution[2] * d.grid_spacing[2])) - 1e-4f : (g.oz + g.hz) - 1e-4f};
         k_flip_advect<<<blocks_for(n), 256, 0, s>>>(F, n, pos, (float)d.dt, d.max_substeps, mn, mx,
-                                                    (float)d.collider_push_thresh, (float)d.collider_push_shift, 1);
+                                                    (float)d.collider_push_thresh, (float)d.collider_push_shift,
+                                                    three ? 0 : 1);
         return post("advectParticles");
     }
     case FF_TP_DENSITY:
@@ -1496,51 +1703,51 @@ extern "C" int ff_twophase2_stage(ff_twophase t, int stage) {
         if (n) k_flip_conc_accum<<<blocks_for(n), 256, 0, s>>>(g, n, pos, ph, cscale, t->ccnt, t->cacc);
         k_flip_conc_resolve<<<blocks_for(nc), 256, 0, s>>>(nc, t->ccnt, t->cacc, cscale, 1, t->r0, t->r1,
                                                            (float *)t->frac->d, (float *)t->rho->d);
-        for (int a = 0; a < 2; ++a)
+        for (int a = 0; a < na; ++a)
             k_flip_beta<<<blocks_for(comp_n(g, a)), 256, 0, s>>>(g, a, (const float *)t->rho->d, nullptr, t->rref,
                                                                  (float *)t->beta[a]->d);
         return post("density");
     case FF_TP_P2G: {
-        // scatterU/V, finalizeU/V (:850-930)
+        // scatterU/V(/W), finalizeU/V(/W) (:850-930)
         const float S = (float)d.p2g_atomic_scale;
-        for (int a = 0; a < 2; ++a) {
+        for (int a = 0; a < na; ++a) {
             FF_CUDA(cudaMemsetAsync(t->num[a], 0, comp_n(g, a) * 4, s));
             FF_CUDA(cudaMemsetAsync(t->den[a], 0, comp_n(g, a) * 4, s));
         }
         if (n) k_flip_scatter<<<blocks_for(n), 256, 0, s>>>(g, n, pos, vel, S, t->num[0], t->den[0], t->num[1],
-                                                            t->den[1], nullptr, nullptr, 2);
-        for (int a = 0; a < 2; ++a)
+                                                            t->den[1], t->num[2], t->den[2], na);
+        for (int a = 0; a < na; ++a)
             k_flip_finalize<<<blocks_for(comp_n(g, a)), 256, 0, s>>>(comp_n(g, a), t->num[a], t->den[a], S,
-                                                                     (float)d.weight_epsilon, uv[a], t->valid[a]);
+                                                                     (float)d.weight_epsilon, uvw[a], t->valid[a]);
         return post("P2G");
     }
     case FF_TP_SNAPSHOT:
-        for (int a = 0; a < 2; ++a)
-            FF_CUDA(cudaMemcpyAsync(t->old[a], uv[a], comp_n(g, a) * 4, cudaMemcpyDeviceToDevice, s));
+        for (int a = 0; a < na; ++a)
+            FF_CUDA(cudaMemcpyAsync(t->old[a], uvw[a], comp_n(g, a) * 4, cudaMemcpyDeviceToDevice, s));
         return FF_OK;
     case FF_TP_EXTRAPOLATE_WEIGHT:
-        for (int a = 0; a < 2; ++a) FF_TRY(tp_extrapolate(t, uv[a], t->valid[a], a));
+        for (int a = 0; a < na; ++a) FF_TRY(tp_extrapolate(t, uvw[a], t->valid[a], a));
         return FF_OK;
     case FF_TP_CONSTRAIN:
-        // the 2D grid's u and v are the 3D arrays' k = 0 planes
+        // in 2D the grid's u and v are the 3D arrays' k = 0 planes
         return ff_bc3_constrain(t->bc, t->u, t->v, t->w, d.extrapolation_depth);
     case FF_TP_GRAVITY: {
-        const F3 grav{(float)d.gravity[0], (float)d.gravity[1], 0.0f};
-        for (int a = 0; a < 2; ++a)
+        const F3 grav{(float)d.gravity[0], (float)d.gravity[1], three ? (float)d.gravity[2] : 0.0f};
+        for (int a = 0; a < na; ++a)
             k_flip_gravity<<<blocks_for(comp_n(g, a)), 256, 0, s>>>(g, a, nullptr, nullptr, grav, (float)d.dt, 1.0f,
-                                                                    uv[a]);
+                                                                    uvw[a]);
         return post("gravity");
     }
     case FF_TP_PROJECT:
         return ff_pressure3_project(t->ps, t->u, t->v, t->w, t->u, t->v, t->w, &t->last);
     case FF_TP_G2P: {
-        FF_CUDA(cudaMemsetAsync(w, 0, comp_n(g, 2) * 4, s));
+        if (!three) FF_CUDA(cudaMemsetAsync(w, 0, comp_n(g, 2) * 4, s));
         if (!n) return FF_OK;
         const float clamp01[3] = {std::min(std::max((float)d.flip_ratio, 0.0f), 1.0f),
                                   std::min(std::max((float)d.gas_flip_ratio, 0.0f), 1.0f),
                                   std::min(std::max((float)d.velocity_damping, 0.0f), 1.0f)};
-        k_flip_g2p<<<blocks_for(n), 256, 0, s>>>(g, n, pos, vel, uv[0], uv[1], w, t->old[0], t->old[1], w, clamp01[0],
-                                                 clamp01[2], ph, clamp01[1]);
+        k_flip_g2p<<<blocks_for(n), 256, 0, s>>>(g, n, pos, vel, uvw[0], uvw[1], w, t->old[0], t->old[1],
+                                                 three ? t->old[2] : w, clamp01[0], clamp01[2], ph, clamp01[1]);
         return post("G2P");
     }
     case FF_TP_MIX:
@@ -1564,8 +1771,8 @@ extern "C" int ff_twophase2_stage(ff_twophase t, int stage) {
         if (nbp)
             k_tp_scatter<<<nbp, 256, 0, s>>>(g, n, pos, ph, t->ccnt, d.max_particles_per_cell, pl, pg, half, top,
                                              t->rs_pool);
-        k_tp_claim<<<nbc, 256, 0, s>>>(g, t->rs_need, cl, cg, t->rs_tot, half, top, t->rs_pool, uv[0], uv[1], w, pos,
-                                       vel);
+        k_tp_claim<<<nbc, 256, 0, s>>>(g, t->rs_need, cl, cg, t->rs_tot, half, top, t->rs_pool, uvw[0], uvw[1], w,
+                                       pos, vel);
         return post("resample");
     }
     default:

@@ -66,6 +66,13 @@ struct ff_pressure_s {
     ff_field guess = nullptr;
     int warm_used = -1;
 
+    // hash of the operator's inputs (Dirichlet active/target, collider and
+    // face weights) at the last prepare, to skip rebuilding an unchanged
+    // operator; a set_* call clears `prepared`
+    unsigned long long *hash_dev = nullptr, *hash_host = nullptr;
+    unsigned long long input_hash = 0;
+    int rebuilds = 0;
+
     // coarsest direct solve
     double *G = nullptr;
     int nG = 0;
@@ -226,6 +233,9 @@ extern "C" int ff_pressure3_create(ff_ctx ctx, const ff_pressure_desc *desc, ff_
         ps->bricks.push_back(br);
     }
     if ((st = ff_dev_alloc((void **)&ps->st, sizeof(PcgState), s))) return bail(st);
+    if ((st = ff_dev_alloc((void **)&ps->hash_dev, sizeof(unsigned long long), s))) return bail(st);
+    if (cudaMallocHost(&ps->hash_host, sizeof(unsigned long long)) != cudaSuccess)
+        return bail(ff_set_error(FF_E_NOMEM, "cudaMallocHost"));
     if (cudaMallocHost(&ps->st_host, sizeof(PcgState)) != cudaSuccess) return bail(ff_set_error(FF_E_NOMEM, "cudaMallocHost"));
     auto g = Dims{r[0], r[1], r[2]};
     long long blocks = (long long)div_up(g.nx, g.nx >= 128 ? 128 : g.nx >= 64 ? 64 : 32) *
@@ -323,6 +333,8 @@ extern "C" int ff_pressure3_destroy(ff_pressure ps) {
     }
     ff_dev_free(ps->st);
     if (ps->st_host) cudaFreeHost(ps->st_host);
+    ff_dev_free(ps->hash_dev);
+    if (ps->hash_host) cudaFreeHost(ps->hash_host);
     ff_dev_free(ps->partials);
     for (float *p : ps->x2) ff_dev_free(p);
     for (uint8_t *p : ps->bricks) ff_dev_free(p);
@@ -426,18 +438,71 @@ static int build_level(ff_pressure ps, int l, cudaStream_t s) {
     return FF_OK;
 }
 
+namespace {
+// splitmix64 finaliser (Steele, Lea & Flood 2014)
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+// acc += sum over the array's bytes, taken as 32-bit words (the last few
+// bytes on their own), of mix64(position, word, salt): a sum, so the order
+// in which blocks add does not matter
+__global__ void k_hash_bytes(const unsigned char *__restrict__ p, long long nbytes, unsigned long long salt,
+                             unsigned long long *__restrict__ acc) {
+    const long long nw = nbytes >> 2;
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(p);
+    unsigned long long h = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nw; i += (long long)gridDim.x * blockDim.x)
+        h += mix64(((unsigned long long)i << 32 | __ldg(w + i)) ^ salt);
+    if (blockIdx.x == 0 && threadIdx.x < (nbytes & 3))
+        h += mix64(((unsigned long long)(nw * 4 + threadIdx.x) << 40 | p[nw * 4 + threadIdx.x]) ^ ~salt);
+    for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(acc, h);
+}
+}  // namespace
+
+// One hash of every input the operator and its hierarchy derive from (the
+// Dirichlet active mask and targets, collider and face weights), read back
+// to the host: equal hashes and no set_* call since the last prepare mean
+// the Dirichlet fields, system weights, coarse levels, coefficients,
+// classes, work orders and coarsest factorisation all still hold.
+static int input_hash(ff_pressure ps, unsigned long long *out) {
+    cudaStream_t s = ps->s();
+    FF_CUDA(cudaMemsetAsync(ps->hash_dev, 0, sizeof(unsigned long long), s));
+    ff_field fs[8] = {ps->active, ps->target, ps->cw[0], ps->cw[1], ps->cw[2], ps->fw[0], ps->fw[1], ps->fw[2]};
+    for (int q = 0; q < 8; ++q) {
+        if (!fs[q]) continue;
+        const long long nb = (long long)fs[q]->bytes;
+        const int blocks = (int)std::max(1LL, std::min<long long>((nb / 4 + 255) / 256, (long long)ps->ctx->sm_count * 8));
+        k_hash_bytes<<<blocks, 256, 0, s>>>((const unsigned char *)fs[q]->d, nb, 0x5851F42D4C957F2Dull * (q + 1),
+                                            ps->hash_dev);
+    }
+    FF_CUDA(cudaGetLastError());
+    FF_CUDA(cudaMemcpyAsync(ps->hash_host, ps->hash_dev, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    FF_CUDA(cudaStreamSynchronize(s));
+    *out = *ps->hash_host;
+    return FF_OK;
+}
+
 static int prepare(ff_pressure ps, ff_field u, ff_field v, ff_field w) {
     cudaStream_t s = ps->s();
     const Dims &d = ps->d;
     Level &L0 = ps->lv[0];
     const float *cw[3] = {fptr(ps->cw[0]), fptr(ps->cw[1]), fptr(ps->cw[2])};
     const float *fw[3] = {fptr(ps->fw[0]), fptr(ps->fw[1]), fptr(ps->fw[2])};
+    // the operator's inputs unchanged since the last prepare: only b is new
+    unsigned long long h = 0;
+    FF_TRY(input_hash(ps, &h));
+    const bool reuse = ps->prepared && h == ps->input_hash;
     // updateDirichletFields (grid_pressure_solver3.js:171-206)
     ps->has_mask = ps->active || cw[0];
     // a zero mask is the same operator as no mask, so level 0 always reads
     // the solver's mask field and the graph's pointers never change
     uint8_t *mask = (uint8_t *)ps->maskf->d;
-    if (ps->has_mask) {
+    if (reuse) {
+    } else if (ps->has_mask) {
         FF_TRY(ffk::dirichlet_fields(d, ps->active ? (const uint8_t *)ps->active->d : nullptr,
                                      fptr(ps->target), cw[0], cw[1], cw[2], mask, ps->tgt,
                                      (uint8_t *)ps->ventf->d, s));
@@ -451,7 +516,7 @@ static int prepare(ff_pressure ps, ff_field u, ff_field v, ff_field w) {
     if (ps->has_w) {
         if (fw[0] && cw[0]) {
             for (int a = 0; a < ps->dims; ++a) sw[a] = ps->sw[a];
-            FF_TRY(ffk::system_weights(d, fw, cw, sw, s));
+            if (!reuse) FF_TRY(ffk::system_weights(d, fw, cw, sw, s));
         } else {
             // one factor only: the system weights are those arrays themselves
             for (int a = 0; a < ps->dims; ++a) sw[a] = (float *)(fw[0] ? fw[a] : cw[a]);
@@ -474,6 +539,7 @@ static int prepare(ff_pressure ps, ff_field u, ff_field v, ff_field w) {
     const bool cmask = ps->desc.mg_coarsen_mask != 0, cwgt = ps->desc.mg_coarsen_weights != 0;
     const bool coarsening_masks = (ps->has_mask && cmask) || (ps->has_w && cwgt);
     const bool use_coarse_w = ps->has_w && cwgt;
+    if (reuse) return FF_OK;
     // refreshCoarseLevels (multigrid.js:416-452): weights before masks
     for (int l = 1; l < Ln; ++l) {
         Level &f = ps->lv[l - 1], &c = ps->lv[l];
@@ -501,6 +567,8 @@ static int prepare(ff_pressure ps, ff_field u, ff_field v, ff_field w) {
     }
     FF_TRY(build_level(ps, 0, s));
     ps->prepared = true;
+    ps->input_hash = h;
+    ++ps->rebuilds;
     // FP64 direct coarsest solve: refactor when the coarsest operator changed
     if (ps->desc.preconditioner == FF_PRE_MULTIGRID && ps->desc.mg_coarse_mode == FF_COARSE_DIRECT) {
         Level &c = ps->lv[Ln - 1];

@@ -15,6 +15,8 @@ Names, option names, defaults and error behaviour follow the reference
   apply_viscosity3                explicit viscosity (no reference counterpart)
   create_grid_solver3             grid_solver3.js:24-149 (forces, viscosity, projection, advection)
   create_grid_flip_solver3        grid_flip_solver3.js:135-1157 (resampling on by default, :621-820)
+  create_grid_two_phase_flip_solver2  grid_two_phase_flip_solver2.js:479-1622 (one-cell-thick grid)
+  create_grid_two_phase_flip_solver3  the same stages on a full 3D grid (no reference counterpart)
   compute_flip_box_seed3          grid_flip_solver3.js:70-130
   create_jitter_random            jitter_random.js:29-46
 """
@@ -1119,6 +1121,169 @@ class GridTwoPhaseFlipSolver2:
 
 def create_grid_two_phase_flip_solver2(**options):
     return GridTwoPhaseFlipSolver2(**options)
+
+
+def compute_two_phase_box_seed3(domain_min, domain_max, grid_spacing, liquid_min, liquid_max,
+                                particles_per_cell_axis=2, jitter=0.2, random_seed=DEFAULT_JITTER_SEED):
+    """The whole domain seeded with k^3 jittered particles per cell
+    (computeFlipBoxSeed3's mulberry32 jitter), each tagged liquid (phase 1)
+    inside the box [liquid_min, liquid_max) and gas (phase 0) elsewhere; the
+    3D counterpart of computeTwoPhaseBoxSeed (grid_two_phase_flip_solver2.js:
+    397-477)."""
+    seed = compute_flip_box_seed3(domain_min, domain_max, *grid_spacing,
+                                  particles_per_cell_axis=particles_per_cell_axis, jitter=jitter,
+                                  random_seed=random_seed)
+    p = seed["positionsArray"].reshape(-1, 3)
+    lo, hi = np.asarray(liquid_min, np.float32), np.asarray(liquid_max, np.float32)
+    liquid = np.all((p >= lo) & (p < hi), axis=1)
+    ph = np.where(liquid, PHASE_LIQUID, PHASE_GAS).astype(np.float32)
+    return {"count": seed["count"], "positionsArray": seed["positionsArray"],
+            "velocitiesArray": seed["velocitiesArray"], "phasesArray": ph, "liquidCount": int(liquid.sum()),
+            "gasCount": int((~liquid).sum())}
+
+
+class GridTwoPhaseFlipSolver3:
+    """A 3D two-phase FLIP solver (no reference counterpart: the reference's
+    two-phase solver is 2D): the stages of createGridTwoPhaseFlipSolver2 on
+    a full grid, with the same option names.  ``velocity_grid`` is a
+    FaceCenteredGrid3; positions and velocities are (x, y, z) triples.  The
+    pressure pin defaults to the top centre cell (nx/2, ny-1, nz/2)."""
+
+    STAGES = GridTwoPhaseFlipSolver2.STAGES
+
+    def __init__(self, velocity_grid=None, max_particles=None, dt=None, gravity=(0.0, -9.81, 0.0),
+                 liquid_density=1.0, gas_density=0.01, mixing=0.0, fade=0.0, concentration_atomic_scale=4096.0,
+                 flip_ratio=0.97, gas_flip_ratio=0.90, velocity_damping=0.02, p2g_atomic_scale=65536.0,
+                 weight_epsilon=1e-4, closed_domain_boundary_flag=63, collider=None, collider_push_thresh=0.0,
+                 collider_push_shift=0.0, pressure_pin="topCenter", resample=None, pressure=None, max_substeps=32):
+        if velocity_grid is None:
+            raise ValueError("GridTwoPhaseFlipSolver3: velocityGrid is required.")
+        if not max_particles:
+            raise ValueError("GridTwoPhaseFlipSolver3: maxParticles is required.")
+        if not (liquid_density > 0 and gas_density > 0):
+            raise ValueError("GridTwoPhaseFlipSolver3: both densities must be > 0.")
+        g = velocity_grid
+        res = tuple(g.resolution)
+        if pressure_pin == "topCenter":
+            pin = (res[0] // 2, res[1] - 1, res[2] // 2)
+        elif pressure_pin is None:
+            pin = (-1, -1, -1)
+        else:
+            pin = tuple(int(x) for x in pressure_pin)
+        lib = _lib.load()
+        d = _lib.TwoPhase3Desc()
+        lib.ff_twophase3_desc_default(C.byref(d), (C.c_int * 3)(*res), (C.c_double * 3)(*g.grid_spacing),
+                                      int(max_particles), float(dt))
+        d.origin[:] = [float(x) for x in g.origin]
+        d.gravity[:] = [float(x) for x in gravity]
+        d.ambient_density, d.component_density = float(gas_density), float(liquid_density)
+        d.mixing, d.fade = float(mixing), float(fade)
+        d.concentration_atomic_scale = float(concentration_atomic_scale)
+        d.flip_ratio, d.gas_flip_ratio = float(flip_ratio), float(gas_flip_ratio)
+        d.velocity_damping = float(velocity_damping)
+        d.p2g_atomic_scale, d.weight_epsilon = float(p2g_atomic_scale), float(weight_epsilon)
+        d.closed_flags = int(closed_domain_boundary_flag)
+        d.collider_push_thresh, d.collider_push_shift = float(collider_push_thresh), float(collider_push_shift)
+        d.pin_cell[:] = list(pin)
+        d.max_substeps = int(max_substeps)
+        rs = resample or {}
+        d.resample_enabled = int(bool(rs.get("enabled", True)))
+        d.min_particles_per_cell = int(rs.get("minParticlesPerCell", 3))
+        d.max_particles_per_cell = int(rs.get("maxParticlesPerCell", 8))
+        p = pressure or {}
+        mg = p.get("multigrid", {})
+        pd = d.pressure
+        pd.preconditioner = PRECONDITIONERS[p.get("preconditioner", "multigrid")]
+        pd.tolerance = float(p.get("tolerance", pd.tolerance))
+        pd.mg_levels = int(mg.get("numberOfLevels", pd.mg_levels))
+        pd.mg_down = int(mg.get("numberOfSmoothingIterationsDown", pd.mg_down))
+        pd.mg_up = int(mg.get("numberOfSmoothingIterationsUp", pd.mg_up))
+        pd.mg_coarsest = int(mg.get("numberOfCoarsestIterations", pd.mg_coarsest))
+        pd.mg_coarse_mode = 1 if mg.get("coarseSolve", "sweeps") == "direct" else 0
+        if "maxIterations" in p:
+            pd.max_iterations = int(p["maxIterations"])
+        if "maxPlausiblePressure" in p:
+            pd.max_plausible_pressure = float(p["maxPlausiblePressure"])
+        if p.get("precision", "fp32") != "fp32":
+            pd.iterate = 1
+        self.desc = d
+        self.max_particles = int(max_particles)
+        self.velocity_grid = g
+        self.handle = C.c_void_p()
+        _lib.check(lib.ff_twophase3_create(context().handle, C.byref(d), g.data_u.handle, g.data_v.handle,
+                                           g.data_w.handle, C.byref(self.handle)))
+        self.collider = collider
+        if collider is not None:
+            _lib.check(lib.ff_twophase2_set_collider(self.handle, collider.phi.handle))
+        hs = [C.c_void_p() for _ in range(7)]
+        _lib.check(lib.ff_twophase3_fields(self.handle, *[C.byref(x) for x in hs]))
+        ctx = context()
+        self.phase = BorrowedField(hs[0], ctx)
+        self.concentration = self.phase
+        self.liquid_fraction = BorrowedField(hs[1], ctx)
+        self.density = BorrowedField(hs[2], ctx)
+        self.beta_u = BorrowedField(hs[3], ctx)
+        self.beta_v = BorrowedField(hs[4], ctx)
+        self.beta_w = BorrowedField(hs[5], ctx)
+        self.pressure_solver = GridPressureSolver3.borrowed(hs[6].value, self, res, g.grid_spacing, g.origin)
+        self.pressure = self.pressure_solver.pressure
+        self.diagnostics = {}
+
+    def set_particles(self, positions=None, velocities=None, phases=None, count=None):
+        """Upload (x, y, z) positions, velocities and phases; `count` (default
+        the number of positions) becomes the live particle count."""
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float32).ravel()
+                for a in (positions, velocities, phases)]
+        n = count if count is not None else (arrs[0].size // 3 if arrs[0] is not None else arrs[2].size)
+        ptr = lambda a: a.ctypes.data_as(C.POINTER(C.c_float)) if a is not None else None
+        _lib.check(_lib.load().ff_twophase3_set_particles(self.handle, int(n), *[ptr(a) for a in arrs]))
+        _lib.check(_lib.load().ff_twophase2_set_count(self.handle, int(n)))
+
+    def get_particles(self, n=None):
+        n = self.max_particles if n is None else int(n)
+        pos, vel, ph = np.empty(3 * n, np.float32), np.empty(3 * n, np.float32), np.empty(n, np.float32)
+        ptr = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        _lib.check(_lib.load().ff_twophase3_get_particles(self.handle, n, ptr(pos), ptr(vel), ptr(ph)))
+        return pos, vel, ph
+
+    def cell_counts(self):
+        nc = int(np.prod(self.velocity_grid.resolution))
+        cnt, acc = np.empty(nc, np.int32), np.empty(nc, np.int32)
+        _lib.check(_lib.load().ff_twophase3_cell_counts(self.handle, cnt.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                         acc.ctypes.data_as(C.POINTER(C.c_int32))))
+        return cnt, acc
+
+    def stage(self, name):
+        _lib.check(_lib.load().ff_twophase2_stage(self.handle, self.STAGES[name]))
+
+    def resample_stats(self):
+        v = (C.c_int64 * 4)()
+        _lib.check(_lib.load().ff_twophase2_resample_stats(self.handle, v))
+        return {"liquidDonors": v[0], "liquidRequested": v[1], "gasDonors": v[2], "gasRequested": v[3]}
+
+    def on_advance_time_step(self):
+        """One step; returns the projection's diagnostics."""
+        d = _lib.Diag()
+        _lib.check(_lib.load().ff_twophase2_step(self.handle, C.byref(d)))
+        self.diagnostics = {"converged": bool(d.converged), "rejected": bool(d.rejected),
+                            "iterations": d.iterations, "stoppedBy": STOP_REASONS.get(d.stopped_by, "none"),
+                            "residual": d.residual, "bNorm": d.b_norm}
+        return self.diagnostics
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.load().ff_twophase2_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def create_grid_two_phase_flip_solver3(**options):
+    return GridTwoPhaseFlipSolver3(**options)
 
 
 class GridSolver3:
