@@ -931,6 +931,24 @@ __global__ void k_res_sumsq(long long n, const float *__restrict__ b, const floa
     }
     if (threadIdx.x == 0) partial[blockIdx.x] = sred[0];
 }
+// the network's guess pinned to the targets at Dirichlet cells
+__global__ void k_guess_pin(long long n, const uint8_t *__restrict__ mask, const float *__restrict__ tgt,
+                            float *__restrict__ g) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        if (mask[c]) g[c] = tgt[c];
+}
+// r = b - A g (zero on Dirichlet rows, whose residual the pin makes zero)
+__global__ void k_guess_residual(long long n, const float *__restrict__ b, const float *__restrict__ ag,
+                                 const uint8_t *__restrict__ mask, float *__restrict__ r) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        r[c] = mask[c] ? 0.0f : b[c] - ag[c];
+}
+// g += z off the Dirichlet cells
+__global__ void k_guess_correct(long long n, const float *__restrict__ z, const uint8_t *__restrict__ mask,
+                                float *__restrict__ g) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        if (!mask[c]) g[c] += z[c];
+}
 // the iterate becomes the guess; Dirichlet cells keep their targets
 __global__ void k_apply_guess(long long n, const float *__restrict__ guess, const uint8_t *__restrict__ mask,
                               const float *__restrict__ tgt, float *__restrict__ hi, float *__restrict__ lo) {
@@ -975,6 +993,22 @@ static int warm_start(ff_pressure ps) {
     cudaStream_t s = ps->s();
     int res[3] = {ps->d.nx, ps->d.ny, ps->d.nz};
     FF_TRY(ff_unet_forward(ps->net, res, (double)ps->hx, ps->bfield, ps->maskf, ps->pressure, ps->guess));
+    // The network supplies the smooth part of the pressure; its error at the
+    // grid scale, which the operator amplifies in the residual, is removed by
+    // one preconditioner application: g += M^-1 (b - A g).
+    if (ps->desc.preconditioner == FF_PRE_MULTIGRID) {
+        const long long n = ps->d.n();
+        float *g = (float *)ps->guess->d;
+        const uint8_t *mask = (const uint8_t *)ps->maskf->d;
+        k_guess_pin<<<256, 256, 0, s>>>(n, mask, ps->tgt, g);
+        FF_TRY(ffk::laplacian_apply(ps->d, ps->lv[0].coef, g, ps->p0, s));
+        k_guess_residual<<<256, 256, 0, s>>>(n, (const float *)ps->bfield->d, ps->p0, mask, ps->r);
+        FF_CUDA(cudaGetLastError());
+        FF_TRY(reset_tail_bar(ps));
+        FF_TRY(precondition(ps, nullptr));
+        k_guess_correct<<<256, 256, 0, s>>>(n, ps->z_final ? ps->z_final : (const float *)ps->z, mask, g);
+        FF_CUDA(cudaGetLastError());
+    }
     double r_prev, r_net;
     FF_TRY(residual_sq(ps, ps->xh0(), ps->r, &r_prev));
     FF_TRY(residual_sq(ps, (const float *)ps->guess->d, ps->p0, &r_net));

@@ -239,7 +239,7 @@ def evaluate(net, n=256, seeds=(1, 2, 3), repeats=3):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--pairs", type=int, default=4096)
+    ap.add_argument("--pairs", type=int, default=4096, help="0: evaluate --init's weights only")
     ap.add_argument("--res", type=int, default=128)
     ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--lr", type=float, default=1e-3)
@@ -259,18 +259,20 @@ def main(argv=None):
     from . import tsl_array_n
     from .warmstart import UNetWarmStart
     tsl_array_n.init(0)
-    with ThreadPoolExecutor(args.workers) as pool:
-        data, gen = generate(args.pairs, args.res, args.seed, pool, log=log)
-    log(json.dumps({"generated": gen}))
     net = UNetWarmStart(seed=args.seed + 1)
     if args.init:
         net.load(args.init)
-    tr = train(net, data, args.epochs, args.lr, args.res, seed=args.seed, holdout=min(args.holdout, len(data) // 4),
-               time_budget=args.time_budget, log=log)
-    if args.out:
-        os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
-        net.save(args.out)
-    del data
+    gen = tr = None
+    if args.pairs > 0:
+        with ThreadPoolExecutor(args.workers) as pool:
+            data, gen = generate(args.pairs, args.res, args.seed, pool, log=log)
+        log(json.dumps({"generated": gen}))
+        tr = train(net, data, args.epochs, args.lr, args.res, seed=args.seed,
+                   holdout=min(args.holdout, len(data) // 4), time_budget=args.time_budget, log=log)
+        if args.out:
+            os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
+            net.save(args.out)
+        del data
     ev = evaluate(net, n=args.eval_res)
     report = {"generation": gen, "training": tr, "evaluation": ev,
               "network": {"parameters": net.param_count, "levels": 3, "channels": [16, 32, 64]}}
