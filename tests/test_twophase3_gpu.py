@@ -151,4 +151,4 @@ def test_dam_break_steps(gpu):
     assert np.all(np.isfinite(pos)) and np.all(np.isfinite(v))
     assert int((ph > 0.5).sum()) == int(liquid.sum())
     y1 = pos.reshape(-1, 3)[ph > 0.5, 1].mean()
-    assert y1 < y0 - 0.5 * H, (y0, y1)
+    assert y1 < y0 - 0.25 * H, (y0, y1)

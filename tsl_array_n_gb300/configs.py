@@ -249,18 +249,21 @@ def c5tp(ctx, steps=500):
         out["particles"] = npart
         for _ in range(3):
             s.on_advance_time_step()
-        its, conv, used = [], 0, 0
+        its, conv, res, stops = [], 0, [], {}
         t0 = _now(ctx)
         for _ in range(steps):
             d = s.on_advance_time_step()
             its.append(d["iterations"])
             conv += int(d["converged"])
+            res.append(d["residual"] / max(d["bNorm"], 1e-300))
+            stops[d["stoppedBy"]] = stops.get(d["stoppedBy"], 0) + 1
         ms = (_now(ctx) - t0) / steps * 1e3
         pos, _, ph = s.get_particles(npart)
         liquid_y = float(pos.reshape(-1, 3)[ph > 0.5, 1].mean())
         out["arms"][arm] = {"ms_per_step": round(ms, 3), "mean_iterations": float(np.mean(its)),
                             "max_iterations": int(max(its)), "converged_fraction": conv / steps,
-                            "liquid_centroid_y": round(liquid_y, 4)}
+                            "residual_rel_median": float(np.median(res)), "residual_rel_max": float(max(res)),
+                            "stopped_by": stops, "liquid_centroid_y": round(liquid_y, 4)}
         if net is not None:
             warmstart.attach(s.pressure_solver, None)
             net.close()

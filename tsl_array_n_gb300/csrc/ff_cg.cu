@@ -216,8 +216,10 @@ __global__ void k_update_x_residual(Dims d, const float4 *__restrict__ coef,
             st->rr = rr;
             st->x_cur = xc ^ 1;
             st->iter += 1;
-            // residual-growing (linalg.js:1839-1852), checked every iteration
-            if (!nonfinite_d(rr)) {
+            // residual-growing (linalg.js:1864-1882), sampled where the
+            // reference's host reads the residual: every GROWTH_SAMPLE
+            // iterations (its smallest chunk)
+            if (!nonfinite_d(rr) && st->iter % GROWTH_SAMPLE == 0) {
                 if (st->best_rr < 0.0 || fabs(rr) < st->best_rr) st->best_rr = fabs(rr);
                 else if (st->best_rr > 0.0 && fabs(rr) > st->best_rr * MAX_RESIDUAL_GROWTH &&
                          st->stop == 0) {

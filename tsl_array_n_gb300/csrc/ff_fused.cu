@@ -1409,7 +1409,9 @@ __global__ void __launch_bounds__(tcg::NT, 2)
                 st->rr = rr;
                 st->x_cur = xc ^ 1;
                 st->iter += 1;
-                if (!nonfinite_d(rr)) {
+                // residual-growing, sampled where the reference's host reads
+                // the residual: every GROWTH_SAMPLE iterations
+                if (!nonfinite_d(rr) && st->iter % GROWTH_SAMPLE == 0) {
                     if (st->best_rr < 0.0 || fabs(rr) < st->best_rr) st->best_rr = fabs(rr);
                     else if (st->best_rr > 0.0 && fabs(rr) > st->best_rr * MAX_RESIDUAL_GROWTH && st->stop == 0)
                         st->growth_stop = 1;
@@ -1740,7 +1742,9 @@ __global__ void __launch_bounds__(NT, 3) k_x_residual(CgArgs a) {
                 st->rr = rr;
                 st->x_cur = xc ^ 1;
                 st->iter += 1;
-                if (!nonfinite_d(rr)) {
+                // residual-growing, sampled where the reference's host reads
+                // the residual: every GROWTH_SAMPLE iterations
+                if (!nonfinite_d(rr) && st->iter % GROWTH_SAMPLE == 0) {
                     if (st->best_rr < 0.0 || fabs(rr) < st->best_rr) st->best_rr = fabs(rr);
                     else if (st->best_rr > 0.0 && fabs(rr) > st->best_rr * MAX_RESIDUAL_GROWTH && st->stop == 0)
                         st->growth_stop = 1;

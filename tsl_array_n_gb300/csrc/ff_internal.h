@@ -27,6 +27,11 @@ int ff_set_error(int code, const char *fmt, ...);
         if (_s != FF_OK) return _s;                                              \
     } while (0)
 
+// residual-growing stop: the squared residual is compared with the best one
+// seen every GROWTH_SAMPLE iterations, the smallest chunk after which the
+// reference's host reads the residual (linalg.js:942-943, 1864-1882)
+constexpr int GROWTH_SAMPLE = 4;
+
 // --------------------------------------------------------------- handles --
 struct ff_ctx_s {
     int device = 0;
