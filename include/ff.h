@@ -129,6 +129,14 @@ typedef struct {
     int max_iterations;         /* the cap that applied                        */
     int kernel_launches;        /* libff kernels launched by the call          */
     int warm_start;             /* -1 none, 0 previous pressure kept, 1 network guess used */
+    /* reportNoiseFloor diagnostics (grid_pressure_solver3.js:517-542,
+     * linalg.js:884-905), filled when the setting is on, else 0: */
+    int report_floor;           /* 1 when the fields below were measured       */
+    int tolerance_below_floor;  /* toleranceBelowFloor: threshold < floor      */
+    double max_residual;        /* maxResidual: max |r| of the last residual   */
+    double noise_floor;         /* noiseFloor: 2^-24 * sum(2/h^2) * |x0|       */
+    double noise_floor_relative;/* noiseFloorRelative: noise_floor / |b|       */
+    double floor_threshold;     /* the stop threshold it is compared with      */
 } ff_diag;
 
 #define FF_STOP_NONE 0
@@ -149,7 +157,10 @@ int ff_pressure3_set_face_weights(ff_pressure ps, ff_field u, ff_field v, ff_fie
  * active is a FF_UINT8 cell field, target a FF_FLOAT cell field (or NULL
  * for 0).  active == NULL clears the Dirichlet condition.                 */
 int ff_pressure3_set_dirichlet(ff_pressure ps, ff_field active, ff_field target);
-/* Runtime settings object (:135): key names as in the reference. */
+/* Runtime settings object (:135): key names as in the reference
+ * ("tolerance", "maxIterations", "relativeTolerance", "checkBadCells",
+ * "preconditioner", "sorFactor", "reportNoiseFloor"), plus "useGraph",
+ * "useTma" and "coarseTail" for this implementation's paths. */
 int ff_pressure3_set(ff_pressure ps, const char *key, double value);
 /* project(inGrid, outGrid)() (:339-556).  u_out may equal u_in.  The
  * pressure field persists between calls and is the warm start.           */

@@ -202,6 +202,44 @@ def test_iteration_cap_2d(gpu, oracle):
     assert abs(d["residual"] / ro["residual"] - 1) < 0.05, (d["residual"], ro["residual"])
 
 
+def test_noise_floor_diagnostics(gpu):
+    """reportNoiseFloor (grid_pressure_solver3.js:517-542, linalg.js:884-905),
+    off by default: noiseFloor = 2^-24 * sum(2/h^2) * |x0| for the start x0
+    (the previous pressure with the Dirichlet cells at their targets),
+    maxResidual = max |r| of the last residual (between |r|_2 / sqrt(n) and
+    |r|_2), toleranceBelowFloor set when the stop threshold is under the
+    floor."""
+    from tsl_array_n_gb300.tsl_array_n import Field
+    s, meta, a, _ = stalled_solver(110, precision="mixed")
+    shape = tuple(meta["resolution"])
+    h = meta["gridSpacing"]
+    bf = Field("float", shape).from_array(a["b"].astype(np.float32))
+    d = s.solve(bf)
+    assert d["maxResidual"] is None and d["noiseFloor"] is None and d["toleranceBelowFloor"] is None
+    s.settings.reportNoiseFloor = True
+    x0 = a["pressure"].astype(np.float32)
+    s.pressure.from_array(x0)
+    d = s.solve(bf)
+    mask = a["dirichletMask"] > 0.5
+    start = np.where(mask, 0.0, x0.astype(np.float64))
+    scale = sum(2.0 / (hh * hh) for hh in h)
+    expected = 2.0 ** -24 * scale * np.linalg.norm(start)
+    assert abs(d["noiseFloor"] / expected - 1) < 1e-6, (d["noiseFloor"], expected)
+    assert abs(d["noiseFloorRelative"] - d["noiseFloor"] / d["bNorm"]) < 1e-12 * d["noiseFloorRelative"] + 1e-300
+    n = int(np.prod(shape))
+    assert d["residual"] / np.sqrt(n) <= d["maxResidual"] * (1 + 1e-6) and d["maxResidual"] <= d["residual"] * (1 + 1e-6)
+    assert d["toleranceBelowFloor"] is None and d["residualOverFloor"] == d["residual"] / d["noiseFloor"]
+    # a tolerance under the floor is reported, not changed
+    s.settings.tolerance = 1e-14
+    s.pressure.from_array(x0)
+    d = s.solve(bf)
+    below = d["toleranceBelowFloor"]
+    assert below is not None and below["floor"] == d["noiseFloor"] and below["tolerance"] == 1e-14
+    assert below["requested"] == max(1e-14 * d["bNorm"], 1e-14) and below["requested"] < below["floor"]
+    s.settings.reportNoiseFloor = False
+    assert s.solve(bf)["noiseFloor"] is None
+
+
 def test_guard_nan_rhs_is_reported_not_thrown(gpu, oracle):
     """A NaN right-hand side trips a guard (degenerate pAp) and leaves the
     pressure untouched; the oracle reports the same stop code."""

@@ -80,7 +80,9 @@ class Diag(C.Structure):
     _fields_ = [("converged", C.c_int), ("rejected", C.c_int), ("iterations", C.c_int),
                 ("stopped_by", C.c_int), ("residual", C.c_double), ("b_norm", C.c_double),
                 ("bad_cells", C.c_int), ("max_iterations", C.c_int), ("kernel_launches", C.c_int),
-                ("warm_start", C.c_int)]
+                ("warm_start", C.c_int), ("report_floor", C.c_int), ("tolerance_below_floor", C.c_int),
+                ("max_residual", C.c_double), ("noise_floor", C.c_double),
+                ("noise_floor_relative", C.c_double), ("floor_threshold", C.c_double)]
 
 
 # every symbol include/ff.h declares, with (restype, argtypes)

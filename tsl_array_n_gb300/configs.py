@@ -255,6 +255,27 @@ def _two_phase_dam_break(precision, n=(256, 128, 128)):
     return grid, s, npart, seed
 
 
+def _transfer_rates(ctx, s, grid, npart, reps=5):
+    """P2G and G2P of the two-phase solver on its current particles, timed
+    alone (device synchronised around `reps` calls).  Algorithmic bytes:
+    P2G reads position and velocity (24 B a particle) and, per face, clears
+    the two int32 accumulators, then reads them and writes the velocity and
+    its valid flag (24 B a face); its 48 int32 atomics a particle go to L2.
+    G2P reads position, velocity and phase and writes the velocity (40 B a
+    particle) and reads the new and old face velocities (8 B a face)."""
+    faces = sum(f.count for f in (grid.data_u, grid.data_v, grid.data_w))
+    out = {}
+    for name, nbytes in (("p2g", 24 * npart + 24 * faces), ("g2p", 40 * npart + 8 * faces)):
+        s.stage(name)
+        t0 = _now(ctx)
+        for _ in range(reps):
+            s.stage(name)
+        ms = (_now(ctx) - t0) / reps * 1e3
+        out[name] = {"ms": round(ms, 3), "GB_s": round(nbytes / ms / 1e6, 1), "bytes": int(nbytes),
+                     "particles_per_s": float(npart / ms * 1e3)}
+    return out
+
+
 def c5tp(ctx, steps=500):
     """The two-phase dam break with each projection arm: plain FP32 MGPCG,
     mixed precision, and mixed with the learned warm start (the network's
@@ -291,12 +312,66 @@ def c5tp(ctx, steps=500):
                             "max_iterations": int(max(its)), "converged_fraction": conv / steps,
                             "residual_rel_median": float(np.median(res)), "residual_rel_max": float(max(res)),
                             "stopped_by": stops, "liquid_centroid_y": round(liquid_y, 4)}
+        if arm == "mixed":
+            out["arms"][arm]["transfers"] = _transfer_rates(ctx, s, grid, npart)
         if net is not None:
             warmstart.attach(s.pressure_solver, None)
             net.close()
         s.close()
         del grid, s
     return out
+
+
+def c5tpdump(ctx, steps, path):
+    """Run the two-phase dam break (mixed precision) `steps` steps and save
+    its last projection's system to `path` (.npz, compressed): b, the beta
+    faces it was built with, the pressure the solver returned, the pinned
+    cell and the projection's diagnostics."""
+    grid, s, npart, _ = _two_phase_dam_break("mixed")
+    for _ in range(steps):
+        d = s.on_advance_time_step()
+    res = grid.resolution
+    np.savez_compressed(path, b=s.pressure_solver.b.to_array(), beta_u=s.beta_u.to_array(),
+                        beta_v=s.beta_v.to_array(), beta_w=s.beta_w.to_array(), pressure=s.pressure.to_array(),
+                        pin=np.array([res[0] // 2, res[1] - 1, res[2] // 2]), iterations=d["iterations"],
+                        residual=d["residual"], b_norm=d["bNorm"])
+    return {"config": f"C5 two-phase pressure system after {steps} steps", "path": path, "diagnostics": d}
+
+
+def c5tpsolve(ctx, path, out=None):
+    """Solve a saved two-phase system (c5tpdump) from a zero start with a
+    standalone solver of the dam break's options, with the coarsest level
+    swept and solved directly; `out` (.npz) keeps one V-cycle applied to b
+    (coarsest level swept)."""
+    z = np.load(path)
+    shp, hh = (256, 128, 128), (1.0 / 128,) * 3
+    n = int(np.prod(shp))
+    pin = z["pin"]
+    active = np.zeros(n, np.uint8)
+    active[int(pin[0]) + shp[0] * (int(pin[1]) + shp[1] * int(pin[2]))] = 1
+    fw = {"u": Field("float", (shp[0] + 1, shp[1], shp[2])).from_array(z["beta_u"]),
+          "v": Field("float", (shp[0], shp[1] + 1, shp[2])).from_array(z["beta_v"]),
+          "w": Field("float", (shp[0], shp[1], shp[2] + 1)).from_array(z["beta_w"])}
+    b = Field("float", shp).from_array(z["b"])
+    res = {"config": "C5 two-phase pressure system, standalone solve from zero", "path": path}
+    keep = {}
+    for coarse in ("sweeps", "direct"):
+        ps = ff.create_grid_pressure_solver3(shp, hh, dirichlet=(active, np.zeros(n, np.float32)), face_weights=fw,
+                                             multigrid={"numberOfLevels": 5, "coarseSolve": coarse},
+                                             tolerance=1e-6, precision="mixed")
+        ps.prepare()
+        ps.pressure.fill(0.0)
+        d = ps.solve(b)
+        res[coarse] = {"iterations": d["iterations"], "converged": d["converged"], "stoppedBy": d["stoppedBy"],
+                       "residual_rel": d["residual"] / max(d["bNorm"], 1e-300)}
+        if coarse == "sweeps":
+            zf = Field("float", shp)
+            ps.apply_preconditioner(b, zf)
+            keep = {"z": zf.to_array()}
+        del ps
+    if out:
+        np.savez_compressed(out, **keep)
+    return res
 
 
 def c5dump(ctx, steps, path):
@@ -340,18 +415,22 @@ def c5solve(ctx, path, reps=1):
 def main(argv):
     """Arguments: configuration names, each optionally with a step count
     (``c2:6000`` runs the channel 6000 steps, ``c5:200`` the dam break 200);
-    ``c5dump:300:sys.npz`` saves the dam break's system after 300 steps and
-    ``c5solve:sys.npz`` solves and profiles it standalone."""
+    ``c5dump:300:sys.npz`` saves the dam break's system after 300 steps
+    (``c5tpdump`` the two-phase one's) and ``c5solve:sys.npz`` solves and
+    profiles it standalone."""
     runs = []
     for a in argv:
         name, _, rest = a.partition(":")
         if name in ("c1", "c2", "c4", "c5", "c5tp"):
             runs.append((name, {"steps": int(rest)} if rest else {}))
-        elif name == "c5dump":
+        elif name in ("c5dump", "c5tpdump"):
             steps, _, path = rest.partition(":")
             runs.append((name, {"steps": int(steps), "path": path}))
         elif name == "c5solve":
             runs.append((name, {"path": rest}))
+        elif name == "c5tpsolve":
+            path, _, out = rest.partition(":")
+            runs.append((name, {"path": path, "out": out or None}))
     ctx = tsl_array_n.init(0)
     for name, kw in runs or [(n, {}) for n in ("c1", "c2", "c4", "c5")]:
         print(json.dumps(globals()[name](ctx, **kw)), flush=True)

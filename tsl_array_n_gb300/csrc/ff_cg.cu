@@ -217,9 +217,9 @@ __global__ void k_update_x_residual(Dims d, const float4 *__restrict__ coef,
             st->x_cur = xc ^ 1;
             st->iter += 1;
             // residual-growing (linalg.js:1864-1882), sampled where the
-            // reference's host reads the residual: every GROWTH_SAMPLE
-            // iterations (its smallest chunk)
-            if (!nonfinite_d(rr) && st->iter % GROWTH_SAMPLE == 0) {
+            // reference's host reads the residual: at its chunk ends
+            if (!nonfinite_d(rr) && st->iter >= st->guard_next) {
+                st->guard_next += GROWTH_SAMPLE;
                 if (st->best_rr < 0.0 || fabs(rr) < st->best_rr) st->best_rr = fabs(rr);
                 else if (st->best_rr > 0.0 && fabs(rr) > st->best_rr * MAX_RESIDUAL_GROWTH &&
                          st->stop == 0) {
@@ -284,11 +284,15 @@ __global__ void k_rz_beta(Dims d, const float *__restrict__ r, const ZT *__restr
 }
 
 __global__ void k_state_init(PcgState *st, double tol, int maxiter, int relative) {
+    const int last_valid = st->last_valid, last = last_valid ? st->last_iters : GROWTH_FIRST_DEFAULT;
     PcgState s = {};
     s.tol = tol;
     s.maxiter = maxiter;
     s.relative = relative;
     s.best_rr = -1.0;
+    s.last_iters = last;
+    s.last_valid = last_valid;
+    s.guard_next = growth_first_check(last);
     *st = s;
 }
 
@@ -296,6 +300,11 @@ __global__ void k_loop_control(PcgState *st, cudaGraphConditionalHandle h, int u
     if (threadIdx.x != 0) return;
     st->launched += 1;
     int cont = (st->stop == 0) && (st->err == 0) && (st->iter < st->maxiter) && (st->launched < st->maxiter + 4);
+    if (!cont) {
+        // the count the next solve's first chunk is sized by (linalg.js:1839-1905)
+        st->last_iters = st->stop == FF_STOP_CONVERGED ? st->stop_iter : st->iter;
+        st->last_valid = 1;
+    }
     if (use_handle) cudaGraphSetConditional(h, cont ? 1u : 0u);
 }
 

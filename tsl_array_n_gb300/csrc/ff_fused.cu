@@ -896,14 +896,28 @@ __device__ __forceinline__ float4 fma4(float s, const float4 &a, const float4 &b
 }
 __device__ __forceinline__ void st4(float *p, const float4 &v) { *reinterpret_cast<float4 *>(p) = v; }
 
-// (A v)_c of one cell by class; ci its index, corr = h^-2 summed over its
-// faces across the domain edge.
+// A neighbour across the domain edge stands in as the cell itself, so the
+// absent face's difference is an exact zero.  (Adding h^-2 v back to a
+// zero-filled neighbour's -h^-2 v cancels to within a rounding of h^-2 |v|:
+// near a wall under a hydrostatic pressure that is far above the residual
+// the solve has to reach.)
+__device__ __forceinline__ void edge_self(const Geo &g, int i, int j, int k, float vc, float &xm, float &xp,
+                                          float &ym, float &yp, float &zm, float &zp) {
+    if (i == 0) xm = vc;
+    if (i == g.d.nx - 1) xp = vc;
+    if (j == 0) ym = vc;
+    if (j == g.d.ny - 1) yp = vc;
+    if (k == 0) zm = vc;
+    if (k == g.d.nz - 1) zp = vc;
+}
+
+// (A v)_c of one cell by class; ci its index.
 __device__ __forceinline__ float ap_cell(const Geo &g, const float4 *coef, const float4 *gco, unsigned c, int i,
                                          int j, int k, long long ci, float vc, float xm, float xp, float ym, float yp,
-                                         float zm, float zp, float corr) {
+                                         float zm, float zp) {
+    if (c == 2u) edge_self(g, i, j, k, vc, xm, xp, ym, yp, zm, zp);
     const float ar = apply_reg(g, vc, xm, xp, ym, yp, zm, zp);
-    if (c == 0u) return ar;
-    if (c == 2u) return __fmaf_rn(corr, vc, ar);
+    if (c == 0u || c == 2u) return ar;
     if (c == 1u) return -vc;
     const float4 lo = __ldg(coef + ci), hi = __ldg(gco + ci);
     Coef q;
@@ -915,12 +929,6 @@ __device__ __forceinline__ float ap_cell(const Geo &g, const float4 *coef, const
     q.uy = hi.y;
     q.uz = hi.z;
     return apply_q(q, vc, xm, xp, ym, yp, zm, zp);
-}
-
-// h^-2 summed over the faces across the domain edge of a quad's cells 0..3
-__device__ __forceinline__ float4 quad_edge(const Geo &g, int gi, int gj, int k) {
-    const float c = g.h2y * (float)((gj == 0) + (gj == g.d.ny - 1)) + g.h2z * (float)((k == 0) + (k == g.d.nz - 1));
-    return make_float4(c + (gi == 0 ? g.h2x : 0.f), c, c, c + (gi + 3 == g.d.nx - 1 ? g.h2x : 0.f));
 }
 
 __global__ void __launch_bounds__(tcg::NT, 4)
@@ -1023,16 +1031,15 @@ __global__ void __launch_bounds__(tcg::NT, 4)
                         a2 = apply_reg(g, p0.z, p0.y, p0.w, ym.z, yp.z, pm1.z, p1.z);
                         a3 = apply_reg(g, p0.w, p0.z, xr, ym.w, yp.w, pm1.w, p1.w);
                     } else {
-                        const float4 e = quad_edge(g, gi, gj, k);
                         const long long ci = qoff + g.sz * k;
                         a0 = ap_cell(g, a.coef, a.gco, ck & 3u, gi, gj, k, ci, p0.x, xl, p0.y, ym.x, yp.x, pm1.x,
-                                     p1.x, e.x);
+                                     p1.x);
                         a1 = ap_cell(g, a.coef, a.gco, (ck >> 2) & 3u, gi + 1, gj, k, ci + 1, p0.y, p0.x, p0.z,
-                                     ym.y, yp.y, pm1.y, p1.y, e.y);
+                                     ym.y, yp.y, pm1.y, p1.y);
                         a2 = ap_cell(g, a.coef, a.gco, (ck >> 4) & 3u, gi + 2, gj, k, ci + 2, p0.z, p0.y, p0.w,
-                                     ym.z, yp.z, pm1.z, p1.z, e.z);
+                                     ym.z, yp.z, pm1.z, p1.z);
                         a3 = ap_cell(g, a.coef, a.gco, ck >> 6, gi + 3, gj, k, ci + 3, p0.w, p0.z, xr, ym.w, yp.w,
-                                     pm1.w, p1.w, e.w);
+                                     pm1.w, p1.w);
                     }
                     acc.add(p0.x * a0);
                     acc.add(p0.y * a1);
@@ -1131,15 +1138,14 @@ template <bool DS>
 __device__ __forceinline__ float resid_cell(const Geo &g, const float4 *coef, const float4 *gco, unsigned c, int i,
                                             int j, int k, long long ci, float bc, float ch, float cl, float xmh,
                                             float xml, float xph, float xpl, float ymh, float yml, float yph,
-                                            float ypl, float zmh, float zml, float zph, float zpl, float corr) {
+                                            float ypl, float zmh, float zml, float zph, float zpl) {
     if (!(c & 1u)) {
-        float ax = apply_reg(g, ch, xmh, xph, ymh, yph, zmh, zph);
-        if (c == 2u) ax = __fmaf_rn(corr, ch, ax);
-        if (DS) {
-            float al = apply_reg(g, cl, xml, xpl, yml, ypl, zml, zpl);
-            if (c == 2u) al = __fmaf_rn(corr, cl, al);
-            ax += al;
+        if (c == 2u) {
+            edge_self(g, i, j, k, ch, xmh, xph, ymh, yph, zmh, zph);
+            if (DS) edge_self(g, i, j, k, cl, xml, xpl, yml, ypl, zml, zpl);
         }
+        float ax = apply_reg(g, ch, xmh, xph, ymh, yph, zmh, zph);
+        if (DS) ax += apply_reg(g, cl, xml, xpl, yml, ypl, zml, zpl);
         return bc - ax;
     }
     Coef q;
@@ -1325,19 +1331,18 @@ __global__ void __launch_bounds__(tcg::NT, 2)
                         }
                         rq = make_float4(b0.x - ax0, b0.y - ax1, b0.z - ax2, b0.w - ax3);
                     } else {
-                        const float4 e = quad_edge(g, gi, gj, k);
                         const long long ci = qoff + g.sz * k;
                         rq.x = resid_cell<DS>(g, a.coef, a.gco, ck & 3u, gi, gj, k, ci, b0.x, h0.x, l0.x, xlh, xll,
-                                              h0.y, l0.y, ymh.x, yml.x, yph.x, ypl.x, hm1.x, lm1.x, h1.x, l1.x, e.x);
+                                              h0.y, l0.y, ymh.x, yml.x, yph.x, ypl.x, hm1.x, lm1.x, h1.x, l1.x);
                         rq.y = resid_cell<DS>(g, a.coef, a.gco, (ck >> 2) & 3u, gi + 1, gj, k, ci + 1, b0.y, h0.y,
                                               l0.y, h0.x, l0.x, h0.z, l0.z, ymh.y, yml.y, yph.y, ypl.y, hm1.y, lm1.y,
-                                              h1.y, l1.y, e.y);
+                                              h1.y, l1.y);
                         rq.z = resid_cell<DS>(g, a.coef, a.gco, (ck >> 4) & 3u, gi + 2, gj, k, ci + 2, b0.z, h0.z,
                                               l0.z, h0.y, l0.y, h0.w, l0.w, ymh.z, yml.z, yph.z, ypl.z, hm1.z, lm1.z,
-                                              h1.z, l1.z, e.z);
+                                              h1.z, l1.z);
                         rq.w = resid_cell<DS>(g, a.coef, a.gco, ck >> 6, gi + 3, gj, k, ci + 3, b0.w, h0.w, l0.w,
                                               h0.z, l0.z, xrh, xrl, ymh.w, yml.w, yph.w, ypl.w, hm1.w, lm1.w, h1.w,
-                                              l1.w, e.w);
+                                              l1.w);
                     }
                     st4(a.r + qoff + g.sz * k, rq);
                     acc_rr.add(rq.x * rq.x);
@@ -1410,8 +1415,9 @@ __global__ void __launch_bounds__(tcg::NT, 2)
                 st->x_cur = xc ^ 1;
                 st->iter += 1;
                 // residual-growing, sampled where the reference's host reads
-                // the residual: every GROWTH_SAMPLE iterations
-                if (!nonfinite_d(rr) && st->iter % GROWTH_SAMPLE == 0) {
+                // the residual: at its chunk ends
+                if (!nonfinite_d(rr) && st->iter >= st->guard_next) {
+                    st->guard_next += GROWTH_SAMPLE;
                     if (st->best_rr < 0.0 || fabs(rr) < st->best_rr) st->best_rr = fabs(rr);
                     else if (st->best_rr > 0.0 && fabs(rr) > st->best_rr * MAX_RESIDUAL_GROWTH && st->stop == 0)
                         st->growth_stop = 1;
@@ -1743,8 +1749,9 @@ __global__ void __launch_bounds__(NT, 3) k_x_residual(CgArgs a) {
                 st->x_cur = xc ^ 1;
                 st->iter += 1;
                 // residual-growing, sampled where the reference's host reads
-                // the residual: every GROWTH_SAMPLE iterations
-                if (!nonfinite_d(rr) && st->iter % GROWTH_SAMPLE == 0) {
+                // the residual: at its chunk ends
+                if (!nonfinite_d(rr) && st->iter >= st->guard_next) {
+                    st->guard_next += GROWTH_SAMPLE;
                     if (st->best_rr < 0.0 || fabs(rr) < st->best_rr) st->best_rr = fabs(rr);
                     else if (st->best_rr > 0.0 && fabs(rr) > st->best_rr * MAX_RESIDUAL_GROWTH && st->stop == 0)
                         st->growth_stop = 1;

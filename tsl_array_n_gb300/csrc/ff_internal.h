@@ -28,9 +28,15 @@ int ff_set_error(int code, const char *fmt, ...);
     } while (0)
 
 // residual-growing stop: the squared residual is compared with the best one
-// seen every GROWTH_SAMPLE iterations, the smallest chunk after which the
-// reference's host reads the residual (linalg.js:942-943, 1864-1882)
+// seen where the reference's host reads it, at the end of each chunk
+// (linalg.js:942-943, 1839-1882): the first chunk ends at the previous
+// solve's iteration count + 2 (4 before any solve), at least MIN_CHUNK,
+// and every MIN_CHUNK iterations after it
 constexpr int GROWTH_SAMPLE = 4;
+constexpr int GROWTH_FIRST_DEFAULT = 4;
+__host__ __device__ inline int growth_first_check(int last_iters) {
+    return last_iters + 2 > GROWTH_SAMPLE ? last_iters + 2 : GROWTH_SAMPLE;
+}
 
 // --------------------------------------------------------------- handles --
 struct ff_ctx_s {
@@ -80,6 +86,8 @@ struct PcgState {
     int stop, iter, stop_iter, first;
     int maxiter, relative, p_cur, x_cur;
     int launched, bad_cells, growth_stop;
+    int guard_next;             // iteration of the next residual-growing check
+    int last_iters, last_valid; // the previous solve's iteration count (kept across solves)
     int err;   // nonzero: a kernel gave up on a bounded wait (bit 0: TMA staging, bit 1: grid barrier)
     unsigned ticket[4];
 };

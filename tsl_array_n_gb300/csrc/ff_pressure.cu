@@ -65,6 +65,11 @@ struct ff_pressure_s {
     ff_unet net = nullptr;
     ff_field guess = nullptr;
     int warm_used = -1;
+    // reportNoiseFloor (grid_pressure_solver3.js:118-131, 517-542): off by
+    // default; when on, the start's norm before the solve and max |r| after it
+    bool report_floor = false;
+    double x0_norm = 0.0;
+    unsigned *maxbits = nullptr, *maxbits_host = nullptr;
 
     // hash of the operator's inputs (Dirichlet active/target, collider and
     // face weights) at the last prepare, to skip rebuilding an unchanged
@@ -334,6 +339,8 @@ extern "C" int ff_pressure3_destroy(ff_pressure ps) {
     ff_dev_free(ps->st);
     if (ps->st_host) cudaFreeHost(ps->st_host);
     ff_dev_free(ps->hash_dev);
+    ff_dev_free(ps->maxbits);
+    if (ps->maxbits_host) cudaFreeHost(ps->maxbits_host);
     if (ps->hash_host) cudaFreeHost(ps->hash_host);
     ff_dev_free(ps->partials);
     for (float *p : ps->x2) ff_dev_free(p);
@@ -410,6 +417,7 @@ extern "C" int ff_pressure3_set(ff_pressure ps, const char *key, double value) {
         ps->desc.preconditioner = (int)value;
         destroy_graphs(ps);
     } else if (k == "sorFactor") { ps->desc.mg_sor = value; destroy_graphs(ps); }
+    else if (k == "reportNoiseFloor") ps->report_floor = value != 0;
     else return ff_set_error(FF_E_ARG, "unknown setting '%s'", key);
     return FF_OK;
 }
@@ -931,6 +939,32 @@ __global__ void k_res_sumsq(long long n, const float *__restrict__ b, const floa
     }
     if (threadIdx.x == 0) partial[blockIdx.x] = sred[0];
 }
+// sum over cells of (hi + lo)^2, the double-single iterate, into FP64 partials
+__global__ void k_iterate_sumsq(long long n, const float *__restrict__ hi, const float *__restrict__ lo,
+                                double *__restrict__ partial) {
+    __shared__ double sred[256];
+    double acc = 0.0;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        const double x = (double)hi[c] + (lo ? (double)lo[c] : 0.0);
+        acc += x * x;
+    }
+    sred[threadIdx.x] = acc;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st) sred[threadIdx.x] += sred[threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sred[0];
+}
+// createMaxAbsReducer (reduction.js:43-77): max over cells of |r| as the bits
+// of a non-negative float, which order like the floats
+__global__ void k_max_abs_bits(long long n, const float *__restrict__ r, unsigned *__restrict__ bits) {
+    unsigned m = 0u;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        m = max(m, __float_as_uint(fabsf(r[c])));
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(bits, m);
+}
 // the network's guess pinned to the targets at Dirichlet cells
 __global__ void k_guess_pin(long long n, const uint8_t *__restrict__ mask, const float *__restrict__ tgt,
                             float *__restrict__ g) {
@@ -986,6 +1020,36 @@ static int residual_sq(ff_pressure ps, const float *x, float *ax, double *out) {
     return FF_OK;
 }
 
+// |x| of the start the solve runs from (estimateNoiseFloor's dotXX read,
+// linalg.js:884-905)
+static int start_norm(ff_pressure ps) {
+    cudaStream_t s = ps->s();
+    const int nb = 256;
+    k_iterate_sumsq<<<nb, 256, 0, s>>>(ps->d.n(), ps->xh0(), ps->x_lo0, ps->partials);
+    FF_CUDA(cudaGetLastError());
+    std::vector<double> hp(nb);
+    FF_CUDA(cudaMemcpyAsync(hp.data(), ps->partials, sizeof(double) * nb, cudaMemcpyDeviceToHost, s));
+    FF_CUDA(cudaStreamSynchronize(s));
+    double t = 0;
+    for (double x2 : hp) t += x2;
+    ps->x0_norm = std::sqrt(t);
+    return FF_OK;
+}
+
+// max |r| of the last true residual, enqueued after the solve
+static int enqueue_max_residual(ff_pressure ps) {
+    cudaStream_t s = ps->s();
+    if (!ps->maxbits) {
+        FF_TRY(ff_dev_alloc((void **)&ps->maxbits, sizeof(unsigned), s));
+        FF_CHECK(cudaMallocHost(&ps->maxbits_host, sizeof(unsigned)) == cudaSuccess, FF_E_NOMEM, "cudaMallocHost");
+    }
+    FF_CUDA(cudaMemsetAsync(ps->maxbits, 0, sizeof(unsigned), s));
+    k_max_abs_bits<<<std::max(1, ps->ctx->sm_count * 4), 256, 0, s>>>(ps->d.n(), ps->r, ps->maxbits);
+    FF_CUDA(cudaGetLastError());
+    FF_CUDA(cudaMemcpyAsync(ps->maxbits_host, ps->maxbits, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    return FF_OK;
+}
+
 // learned warm start: predict, compare residuals, keep the better start
 static int warm_start(ff_pressure ps) {
     ps->warm_used = -1;
@@ -1037,7 +1101,9 @@ extern "C" int ff_pressure3_project(ff_pressure ps, ff_field u_in, ff_field v_in
     cudaStream_t s = ps->s();
     FF_TRY(prepare(ps, u_in, v_in, w_in));
     FF_TRY(warm_start(ps));
+    if (ps->report_floor) FF_TRY(start_norm(ps));
     FF_TRY(run_solve(ps));
+    if (ps->report_floor) FF_TRY(enqueue_max_residual(ps));
     // circuit breaker + snapshot (:289-336, :547-554), then the correction
     FF_TRY(ffk::count_bad_and_commit(d, ps->xh0(), ps->x_lo0, ps->x_hi1, ps->x_lo1, ps->snap_hi,
                                      ps->snap_lo, ps->st,
@@ -1099,6 +1165,28 @@ static int read_diag(ff_pressure ps, ff_diag *diag, int extra_launches) {
         diag->rejected = ps->check_bad && h.bad_cells > 0;
         diag->max_iterations = ps->maxiter;
         diag->warm_start = ps->warm_used;
+        // reportNoiseFloor (linalg.js:884-905; grid_pressure_solver3.js:271-282,
+        // 517-542): floor = eps_f32 * operatorScale * |x0|, operatorScale the
+        // sum over the axes of 2 / h^2
+        diag->report_floor = ps->report_floor ? 1 : 0;
+        diag->max_residual = diag->noise_floor = diag->noise_floor_relative = 0.0;
+        diag->tolerance_below_floor = 0;
+        diag->floor_threshold = 0.0;
+        if (ps->report_floor) {
+            float mr;
+            std::memcpy(&mr, ps->maxbits_host, sizeof(float));
+            diag->max_residual = (double)mr;
+            double scale = 2.0 / ((double)ps->hx * ps->hx) + 2.0 / ((double)ps->hy * ps->hy);
+            if (ps->dims == 3) scale += 2.0 / ((double)ps->hz * ps->hz);
+            const double fl = std::ldexp(1.0, -24) * scale * ps->x0_norm;
+            diag->noise_floor = fl;
+            diag->noise_floor_relative = diag->b_norm > 0 ? fl / diag->b_norm : 0.0;
+            const double thr = ps->desc.relative_tolerance
+                                   ? std::max(ps->desc.tolerance * diag->b_norm, ps->desc.tolerance)
+                                   : ps->desc.tolerance;
+            diag->floor_threshold = thr;
+            diag->tolerance_below_floor = thr < fl ? 1 : 0;
+        }
         // setup: state init, residual, preconditioner, r.z; then each loop
         // body the device ran: p/pAp, x/residual, preconditioner, r.z, control
         int per_iter = 4 + precond_launches(ps);
@@ -1117,7 +1205,9 @@ extern "C" int ff_pressure3_solve(ff_pressure ps, ff_field b, ff_diag *diag) {
     FF_TRY(prepare(ps, nullptr, nullptr, nullptr));
     FF_CUDA(cudaMemcpyAsync(ps->bfield->d, b->d, b->bytes, cudaMemcpyDeviceToDevice, s));
     FF_TRY(warm_start(ps));
+    if (ps->report_floor) FF_TRY(start_norm(ps));
     FF_TRY(run_solve(ps));
+    if (ps->report_floor) FF_TRY(enqueue_max_residual(ps));
     FF_TRY(ffk::count_bad_and_commit(ps->d, ps->xh0(), ps->x_lo0, ps->x_hi1, ps->x_lo1, ps->snap_hi,
                                      ps->snap_lo, ps->st,
                                      ps->check_bad ? (float)ps->desc.max_plausible_pressure : INFINITY,

@@ -182,6 +182,7 @@ class GridPressureSolver3:
         d.origin[:] = origin
         d.preconditioner = PRECONDITIONERS[preconditioner]
         d.tolerance = tolerance
+        self._tol = float(tolerance)
         d.max_iterations = int(max_iterations or 0)
         d.max_iterations_factor = max_iterations_factor
         d.relative_tolerance = int(bool(relative_tolerance))
@@ -311,9 +312,13 @@ class GridPressureSolver3:
                 residual=float(diag.residual), bNorm=float(diag.b_norm),
                 badCells=int(diag.bad_cells), maxIterations=int(diag.max_iterations),
                 kernelLaunches=int(diag.kernel_launches), warmStart=int(diag.warm_start))
+            self.diagnostics.update(_floor_diagnostics(diag, self._tolerance()))
             return self.diagnostics
 
         return dispatch
+
+    def _tolerance(self):
+        return getattr(self, "_tol", None)
 
     def solve(self, b):
         """cg.solve on A p = b for a given b Field; returns diagnostics."""
@@ -325,6 +330,7 @@ class GridPressureSolver3:
             residual=float(diag.residual), bNorm=float(diag.b_norm),
             badCells=int(diag.bad_cells), maxIterations=int(diag.max_iterations),
             warmStart=int(diag.warm_start))
+        self.diagnostics.update(_floor_diagnostics(diag, self._tolerance()))
         return dict(self.diagnostics)
 
     # -- test hooks -----------------------------------------------------------
@@ -375,11 +381,26 @@ class GridPressureSolver3:
             pass
 
 
+def _floor_diagnostics(diag, tolerance):
+    """The reportNoiseFloor diagnostics (grid_pressure_solver3.js:517-542,
+    linalg.js:884-905): None while the setting is off."""
+    if not diag.report_floor:
+        return dict(maxResidual=None, noiseFloor=None, noiseFloorRelative=None, toleranceBelowFloor=None,
+                    residualOverFloor=None)
+    floor = float(diag.noise_floor)
+    below = ({"requested": float(diag.floor_threshold), "floor": floor, "tolerance": tolerance}
+             if diag.tolerance_below_floor else None)
+    return dict(maxResidual=float(diag.max_residual), noiseFloor=floor,
+                noiseFloorRelative=float(diag.noise_floor_relative) if diag.b_norm > 0 else None,
+                toleranceBelowFloor=below,
+                residualOverFloor=float(diag.residual) / floor if floor else None)
+
+
 class _Settings:
     """The runtime ``settings`` object (grid_pressure_solver3.js:135)."""
 
     _KEYS = {"tolerance", "maxIterations", "relativeTolerance", "checkBadCells", "useGraph",
-             "useTma", "coarseTail", "preconditioner", "sorFactor"}
+             "useTma", "coarseTail", "preconditioner", "sorFactor", "reportNoiseFloor"}
 
     def __init__(self, solver):
         object.__setattr__(self, "_s", solver)
@@ -390,6 +411,8 @@ class _Settings:
         if key == "preconditioner":
             value = PRECONDITIONERS[value]
         _lib.check(_lib.load().ff_pressure3_set(self._s.handle, key.encode(), float(value)))
+        if key == "tolerance":
+            self._s._tol = float(value)
 
     __setitem__ = __setattr__
 
