@@ -525,6 +525,34 @@ __device__ __forceinline__ void relax_pair(const Geo &g, const TqArgs &a, float4
     }
 }
 
+// relax_pair with the colour offset P chosen at run time (selects instead of
+// a branch): the two rows of the halo ring, whose colours differ, share one
+// warp without diverging.
+__device__ __forceinline__ void relax_pair_rt(const Geo &g, const TqArgs &a, float4 &q, float s, const float4 &ym,
+                                              const float4 &yp, const float4 &zm, const float4 &zp, const float4 &bq,
+                                              unsigned cq, const QuadScale &e, int gi, int gj, int k, int P) {
+    const bool p1 = P != 0;
+    const float v0 = p1 ? q.y : q.x, l0 = p1 ? q.x : s, r0 = p1 ? q.z : q.y;
+    const float v1 = p1 ? q.w : q.z, l1 = p1 ? q.z : q.y, r1 = p1 ? s : q.w;
+    const float ym0 = p1 ? ym.y : ym.x, ym1 = p1 ? ym.w : ym.z, yp0 = p1 ? yp.y : yp.x, yp1 = p1 ? yp.w : yp.z;
+    const float zm0 = p1 ? zm.y : zm.x, zm1 = p1 ? zm.w : zm.z, zp0 = p1 ? zp.y : zp.x, zp1 = p1 ? zp.w : zp.z;
+    const float b0 = p1 ? bq.y : bq.x, b1 = p1 ? bq.w : bq.z;
+    const float ra = p1 ? e.r12 : e.r0, rb = p1 ? e.r3 : e.r12;
+    float n0, n1;
+    if (!(cq & (0x11u << (2 * P)))) {
+        n0 = relax_plain(g, a.omsor, v0, l0, r0, ym0, yp0, zm0, zp0, b0, ra);
+        n1 = relax_plain(g, a.omsor, v1, l1, r1, ym1, yp1, zm1, zp1, b1, rb);
+    } else {
+        const long long c = gi + P + g.sy * gj + g.sz * k;
+        n0 = relax_any(g, a, (cq >> (2 * P)) & 3u, c, v0, l0, r0, ym0, yp0, zm0, zp0, b0, ra);
+        n1 = relax_any(g, a, (cq >> (2 * P + 4)) & 3u, c + 2, v1, l1, r1, ym1, yp1, zm1, zp1, b1, rb);
+    }
+    q.x = p1 ? q.x : n0;
+    q.y = p1 ? n0 : q.y;
+    q.z = p1 ? q.z : n1;
+    q.w = p1 ? n1 : q.w;
+}
+
 __device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 __device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
 // any cell of class 3 among the four 2-bit fields of a class byte
@@ -632,13 +660,13 @@ __global__ void __launch_bounds__(tq::NT, 3)
         return e;
     };
     // The tile's halo ring on plane m+2 (its first colour, which the second
-    // colour on that plane reads two steps later): lanes 0..15 of warp 0 the
-    // row above the tile and of warp 1 the row below, as quads; lanes 0..15
-    // of warp 2 the cells left (lanes 0..7) and right (8..15) of the tile,
+    // colour on that plane reads two steps later): warp 0 the rows above
+    // (lanes 0..15) and below (lanes 16..31) the tile, as quads; lanes 0..15
+    // of warp 1 the cells left (lanes 0..7) and right (8..15) of the tile,
     // one pair of rows each.
     // (the ring's per-thread positions are recomputed inside its branches,
     // so they take no registers across the z-march)
-    const int rrole = (lane < 16 && warp < 3) ? warp : -1;   // 0, 1 rows; 2 columns
+    const int rrole = warp == 0 ? 0 : ((warp == 1 && lane < 16) ? 2 : -1);   // 0 rows; 2 columns
     // The thread's quad on planes m-1 .. m+2: q0 (plane m) and q1 carry the
     // first colour relaxed, q2 the values as staged; b of planes m and m+1;
     // the class bytes of planes m .. m+3 (bits 0-7 .. 24-31).
@@ -719,15 +747,18 @@ __global__ void __launch_bounds__(tq::NT, 3)
             bb0 = bb1; bb1 = bb2;
             cpipe >>= 8;
             // the halo ring on plane m+2 last: the quads' transients are dead
-            if (rrole == 0 || rrole == 1) {
+            if (rrole == 0) {
                 // ring row quad: its class byte on plane m+3 (kept for the
                 // next step; class-3 lines go to L1), then the first colour
-                // on plane m+2
-                const int rlrow = rrole == 0 ? -1 : TY;   // staged-row offset
-                const int rgi = i0 + 4 * lane, rgj = j0 + rlrow;
+                // on plane m+2.  The two half-warps are the two rows; their
+                // x-neighbours come by shuffles within 16-lane segments, taken
+                // by the whole warp before the rows' own conditions.
+                const int rl = lane & (QX - 1);
+                const int rlrow = lane < QX ? -1 : TY;   // staged-row offset
+                const int rgi = i0 + 4 * rl, rgj = j0 + rlrow;
                 const bool rquad_in = rgj >= 0 && rgj < g.d.ny && rgi < g.d.nx;
-                const int ro4 = (rlrow + 2) * RW + 4 + 4 * lane, rbo = (rlrow + 1) * RW + 4 + 4 * lane;
-                const int rco = (rlrow + 1) * CW + 16 + lane;
+                const int ro4 = (rlrow + 2) * RW + 4 + 4 * rl, rbo = (rlrow + 1) * RW + 4 + 4 * rl;
+                const int rco = (rlrow + 1) * CW + 16 + rl;
                 if (m == mstart) rcls = cs[rco];
                 const unsigned rnext = C3[rco];
                 if (rquad_in && any_general(rnext) && kp < g.d.nz) {
@@ -735,27 +766,24 @@ __global__ void __launch_bounds__(tq::NT, 3)
                     prefetch_l1(a.coef + off);
                     prefetch_l1(a.gco + off);
                 }
-                if (ka >= 0 && ka <= k1 && ka < g.d.nz && rgj >= 0 && rgj < g.d.ny) {
+                if (ka >= 0 && ka <= k1 && ka < g.d.nz) {
                     float4 rq = lds4(X2 + ro4);
-                    const float4 rym = lds4(X2 + ro4 - RW), ryp = lds4(X2 + ro4 + RW);
-                    const float4 rzm = lds4(X1 + ro4), rzp = lds4(X3 + ro4), rbq = lds4(Bn + rbo);
-                    const int mz = (ka == 0 || ka == g.d.nz - 1) ? 9 * mze : 0;
-                    const int rmy = (rgj == 0) + (rgj == g.d.ny - 1);
-                    QuadScale re;
-                    re.r0 = rdt[(rgi == 0) + 3 * rmy + mz];
-                    re.r12 = rdt[3 * rmy + mz];
-                    re.r3 = rdt[(rgi + 3 == g.d.nx - 1) + 3 * rmy + mz];
-                    constexpr unsigned HALF = 0x0000ffffu;
-                    if ((ca ^ rgj ^ ka) & 1) {
-                        float sv = __shfl_down_sync(HALF, rq.x, 1);
-                        if (lane == QX - 1) sv = X2[ro4 + 4];
-                        if (rquad_in) relax_pair<1>(g, a, rq, sv, rym, ryp, rzm, rzp, rbq, rcls, re, rgi, rgj, ka);
-                    } else {
-                        float sv = __shfl_up_sync(HALF, rq.w, 1);
-                        if (lane == 0) sv = X2[ro4 - 1];
-                        if (rquad_in) relax_pair<0>(g, a, rq, sv, rym, ryp, rzm, rzp, rbq, rcls, re, rgi, rgj, ka);
+                    float sd = __shfl_down_sync(FULL, rq.x, 1, QX), su = __shfl_up_sync(FULL, rq.w, 1, QX);
+                    if (rl == QX - 1) sd = X2[ro4 + 4];
+                    if (rl == 0) su = X2[ro4 - 1];
+                    if (rquad_in) {
+                        const float4 rym = lds4(X2 + ro4 - RW), ryp = lds4(X2 + ro4 + RW);
+                        const float4 rzm = lds4(X1 + ro4), rzp = lds4(X3 + ro4), rbq = lds4(Bn + rbo);
+                        const int mz = (ka == 0 || ka == g.d.nz - 1) ? 9 * mze : 0;
+                        const int rmy = (rgj == 0) + (rgj == g.d.ny - 1);
+                        QuadScale re;
+                        re.r0 = rdt[(rgi == 0) + 3 * rmy + mz];
+                        re.r12 = rdt[3 * rmy + mz];
+                        re.r3 = rdt[(rgi + 3 == g.d.nx - 1) + 3 * rmy + mz];
+                        const int P = (ca ^ rgj ^ ka) & 1;
+                        relax_pair_rt(g, a, rq, P ? sd : su, rym, ryp, rzm, rzp, rbq, rcls, re, rgi, rgj, ka, P);
+                        *reinterpret_cast<float4 *>(X2 + ro4) = rq;
                     }
-                    if (rquad_in) *reinterpret_cast<float4 *>(X2 + ro4) = rq;
                 }
                 rcls = rnext;
             } else if (rrole == 2) {
