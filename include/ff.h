@@ -47,6 +47,10 @@ const char *ff_version(void);
 int ff_ctx_create(int device, ff_ctx *out);
 int ff_ctx_destroy(ff_ctx ctx);
 int ff_ctx_synchronize(ff_ctx ctx);
+/* The compute stream waits for everything enqueued so far on the context's
+ * copy streams (ff_pressure3_project_host's uploads and downloads), so an
+ * event recorded after it covers them. */
+int ff_ctx_join_copies(ff_ctx ctx);
 /* Page-locked host memory for fast uploads/downloads (no reference
  * counterpart; the reference's host arrays are JS TypedArrays). */
 int ff_host_alloc(size_t bytes, void **out);
@@ -157,6 +161,17 @@ int ff_pressure3_set_face_weights(ff_pressure ps, ff_field u, ff_field v, ff_fie
  * active is a FF_UINT8 cell field, target a FF_FLOAT cell field (or NULL
  * for 0).  active == NULL clears the Dirichlet condition.                 */
 int ff_pressure3_set_dirichlet(ff_pressure ps, ff_field active, ff_field target);
+/* project() with the velocity taken from and returned to host memory (no
+ * reference counterpart: the reference's host arrays reach the GPU through
+ * field.fromArray / toArray, array.js:114-129).  Uploads hu, hv, hw into the
+ * input fields on a copy stream, projects into the output fields, downloads
+ * them into hu_out, hv_out, hw_out on a second copy stream; the upload of one
+ * call overlaps the download of the previous one.  Host buffers should be
+ * page-locked (ff_host_alloc); outputs are in place after
+ * ff_ctx_synchronize.  2D solvers take w_in/w_out/hw/hw_out NULL. */
+int ff_pressure3_project_host(ff_pressure ps, ff_field u_in, ff_field v_in, ff_field w_in, const void *hu,
+                              const void *hv, const void *hw, ff_field u_out, ff_field v_out, ff_field w_out,
+                              void *hu_out, void *hv_out, void *hw_out, ff_diag *diag);
 /* Runtime settings object (:135): key names as in the reference
  * ("tolerance", "maxIterations", "relativeTolerance", "checkBadCells",
  * "preconditioner", "sorFactor", "reportNoiseFloor"), plus "useGraph",

@@ -339,3 +339,59 @@ def test_operator_inputs_rewritten_in_place_are_seen(gpu):
     fresh.pressure.fill(0.0)
     fresh.project(grid, out)()
     assert np.array_equal(fresh.pressure.to_array(), p2)
+
+
+def test_project_host_matches_project_back_to_back(gpu):
+    """ff_pressure3_project_host: two calls in a row on different velocity
+    fields, each from its own pinned host buffers into its own, give after
+    one synchronisation the same corrected velocity as project() on the
+    device fields; the first call's download and the second call's upload
+    run on separate copy streams."""
+    import ctypes as C
+    from tsl_array_n_gb300 import fluxflow as ff, scenes, _lib
+    from tsl_array_n_gb300.tsl_array_n import context
+    n = 64
+    scs = [scenes.sphere_scene(n=n, radius_cells=6, modes=8, seed=s) for s in (4, 5)]
+    shape, h = scs[0]["shape"], scs[0]["h"]
+    col = ff.create_sdf_static_collider3(*shape, *h)
+    col.add_shapes(scs[0]["shapes"])
+    cw = col.compute_face_weights()
+    solver = ff.create_grid_pressure_solver3(shape, h, collider_weights=cw,
+                                             dirichlet=(scs[0]["active"], scs[0]["target"]),
+                                             multigrid={"numberOfLevels": 3, "coarseSolve": "direct"},
+                                             precision="mixed", tolerance=1e-6)
+    lib = _lib.load()
+    grid, out = ff.FaceCenteredGrid3(shape, h), ff.FaceCenteredGrid3(shape, h)
+    # reference: project() on device fields
+    refs = []
+    for sc in scs:
+        grid.set(sc["u"], sc["v"], sc["w"])
+        solver.pressure.fill(0.0)
+        assert solver.project(grid, out)()["converged"]
+        refs.append([f.to_array() for f in (out.data_u, out.data_v, out.data_w)])
+    # host buffers, pinned
+    bufs = []
+    for sc in scs:
+        hin, hout = [], []
+        for a in (sc["u"], sc["v"], sc["w"]):
+            p, q = C.c_void_p(), C.c_void_p()
+            _lib.check(lib.ff_host_alloc(a.nbytes, C.byref(p)))
+            _lib.check(lib.ff_host_alloc(a.nbytes, C.byref(q)))
+            C.memmove(p, np.ascontiguousarray(a, np.float32).ctypes.data, a.nbytes)
+            C.memset(q, 0, a.nbytes)
+            hin.append(p)
+            hout.append(q)
+        bufs.append((hin, hout))
+    grid.set(*[np.zeros_like(x) for x in (scs[0]["u"], scs[0]["v"], scs[0]["w"])])
+    for (hin, hout) in bufs:
+        solver.pressure.fill(0.0)
+        d = solver.project_host(grid, out, hin, hout)
+        assert d["converged"], d
+    context().synchronize()
+    for (hin, hout), ref, sc in zip(bufs, refs, scs):
+        for q, r, a in zip(hout, ref, (sc["u"], sc["v"], sc["w"])):
+            got = np.empty(a.size, np.float32)
+            C.memmove(got.ctypes.data, q, got.nbytes)
+            assert np.array_equal(got, r)
+        for p in hin + hout:
+            lib.ff_host_free(p)

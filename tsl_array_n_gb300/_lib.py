@@ -97,6 +97,7 @@ PROTOTYPES = {
     "ff_ctx_create": (_I, [_I, _PP]),
     "ff_ctx_destroy": (_I, [_P]),
     "ff_ctx_synchronize": (_I, [_P]),
+    "ff_ctx_join_copies": (_I, [_P]),
     "ff_host_alloc": (_I, [_S, _PP]),
     "ff_host_free": (_I, [_P]),
     "ff_ctx_event_record": (_I, [_P, _I]),
@@ -119,6 +120,7 @@ PROTOTYPES = {
     "ff_pressure3_set_dirichlet": (_I, [_P, _P, _P]),
     "ff_pressure3_set": (_I, [_P, C.c_char_p, _D]),
     "ff_pressure3_project": (_I, [_P, _P, _P, _P, _P, _P, _P, C.POINTER(Diag)]),
+    "ff_pressure3_project_host": (_I, [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, C.POINTER(Diag)]),
     "ff_pressure3_solve": (_I, [_P, _P, C.POINTER(Diag)]),
     "ff_pressure3_fields": (_I, [_P, _PP, _PP, _PP, _PP]),
     "ff_pressure3_prepare": (_I, [_P, _P, _P, _P]),

@@ -67,9 +67,36 @@ extern "C" int ff_ctx_create(int device, ff_ctx *out) {
     return FF_OK;
 }
 
+int ff_ctx_copy_streams(ff_ctx ctx) {
+    if (ctx->up && ctx->down) return FF_OK;
+    FF_CUDA(cudaSetDevice(ctx->device));
+    if (!ctx->up) FF_CUDA(cudaStreamCreateWithFlags(&ctx->up, cudaStreamNonBlocking));
+    if (!ctx->down) FF_CUDA(cudaStreamCreateWithFlags(&ctx->down, cudaStreamNonBlocking));
+    return FF_OK;
+}
+
+extern "C" int ff_ctx_join_copies(ff_ctx ctx) {
+    FF_CHECK(ctx, FF_E_ARG, "ff_ctx_join_copies: NULL context");
+    for (cudaStream_t c : {ctx->up, ctx->down}) {
+        if (!c) continue;
+        cudaEvent_t e;
+        FF_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        cudaError_t r = cudaEventRecord(e, c);
+        if (r == cudaSuccess) r = cudaStreamWaitEvent(ctx->stream, e, 0);
+        cudaEventDestroy(e);
+        FF_CUDA(r);
+    }
+    return FF_OK;
+}
+
 extern "C" int ff_ctx_destroy(ff_ctx ctx) {
     if (!ctx) return FF_OK;
     cudaSetDevice(ctx->device);
+    for (cudaStream_t c : {ctx->up, ctx->down}) {
+        if (!c) continue;
+        cudaStreamSynchronize(c);
+        cudaStreamDestroy(c);
+    }
     cudaStreamSynchronize(ctx->stream);
     cudaStreamDestroy(ctx->stream);
     for (auto &e : ctx->events) if (e) cudaEventDestroy(e);
@@ -80,6 +107,8 @@ extern "C" int ff_ctx_destroy(ff_ctx ctx) {
 extern "C" int ff_ctx_synchronize(ff_ctx ctx) {
     FF_CHECK(ctx, FF_E_ARG, "ff_ctx_synchronize: NULL context");
     FF_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (ctx->up) FF_CUDA(cudaStreamSynchronize(ctx->up));
+    if (ctx->down) FF_CUDA(cudaStreamSynchronize(ctx->down));
     return FF_OK;
 }
 

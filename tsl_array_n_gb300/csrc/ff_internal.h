@@ -44,7 +44,11 @@ struct ff_ctx_s {
     int sm_count = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t events[16] = {};
+    // copy streams of the host-buffer entry points (created on first use):
+    // uploads and downloads run beside the compute stream
+    cudaStream_t up = nullptr, down = nullptr;
 };
+int ff_ctx_copy_streams(ff_ctx ctx);
 
 struct ff_field_s {
     ff_ctx ctx = nullptr;

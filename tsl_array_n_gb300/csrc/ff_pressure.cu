@@ -68,6 +68,9 @@ struct ff_pressure_s {
     // reportNoiseFloor (grid_pressure_solver3.js:118-131, 517-542): off by
     // default; when on, the start's norm before the solve and max |r| after it
     bool report_floor = false;
+    // ff_pressure3_project_host: the previous call's compute and download
+    cudaEvent_t ev_compute = nullptr, ev_up = nullptr, ev_down = nullptr;
+    bool host_started = false;
     double x0_norm = 0.0;
     unsigned *maxbits = nullptr, *maxbits_host = nullptr;
 
@@ -339,6 +342,8 @@ extern "C" int ff_pressure3_destroy(ff_pressure ps) {
     ff_dev_free(ps->st);
     if (ps->st_host) cudaFreeHost(ps->st_host);
     ff_dev_free(ps->hash_dev);
+    for (cudaEvent_t e : {ps->ev_compute, ps->ev_up, ps->ev_down})
+        if (e) cudaEventDestroy(e);
     ff_dev_free(ps->maxbits);
     if (ps->maxbits_host) cudaFreeHost(ps->maxbits_host);
     if (ps->hash_host) cudaFreeHost(ps->hash_host);
@@ -457,13 +462,24 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
 // acc += sum over the array's bytes, taken as 32-bit words (the last few
 // bytes on their own), of mix64(position, word, salt): a sum, so the order
 // in which blocks add does not matter
+// (16-byte loads: the fields are 256-byte aligned; the words past the last
+// whole 16 bytes and the last few bytes are taken by block 0)
 __global__ void k_hash_bytes(const unsigned char *__restrict__ p, long long nbytes, unsigned long long salt,
                              unsigned long long *__restrict__ acc) {
-    const long long nw = nbytes >> 2;
+    const long long nw = nbytes >> 2, n4 = nbytes >> 4;
     const uint32_t *w = reinterpret_cast<const uint32_t *>(p);
+    const uint4 *w4 = reinterpret_cast<const uint4 *>(p);
     unsigned long long h = 0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nw; i += (long long)gridDim.x * blockDim.x)
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += (long long)gridDim.x * blockDim.x) {
+        const uint4 q = __ldg(w4 + i);
+        const unsigned long long b = (unsigned long long)(4 * i) << 32;
+        h += mix64((b | q.x) ^ salt) + mix64(((b + (1ull << 32)) | q.y) ^ salt) +
+             mix64(((b + (2ull << 32)) | q.z) ^ salt) + mix64(((b + (3ull << 32)) | q.w) ^ salt);
+    }
+    if (blockIdx.x == 0 && threadIdx.x < nw - 4 * n4) {
+        const long long i = 4 * n4 + threadIdx.x;
         h += mix64(((unsigned long long)i << 32 | __ldg(w + i)) ^ salt);
+    }
     if (blockIdx.x == 0 && threadIdx.x < (nbytes & 3))
         h += mix64(((unsigned long long)(nw * 4 + threadIdx.x) << 40 | p[nw * 4 + threadIdx.x]) ^ ~salt);
     for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
@@ -483,7 +499,7 @@ static int input_hash(ff_pressure ps, unsigned long long *out) {
     for (int q = 0; q < 8; ++q) {
         if (!fs[q]) continue;
         const long long nb = (long long)fs[q]->bytes;
-        const int blocks = (int)std::max(1LL, std::min<long long>((nb / 4 + 255) / 256, (long long)ps->ctx->sm_count * 8));
+        const int blocks = (int)std::max(1LL, std::min<long long>((nb / 16 + 255) / 256, (long long)ps->ctx->sm_count * 8));
         k_hash_bytes<<<blocks, 256, 0, s>>>((const unsigned char *)fs[q]->d, nb, 0x5851F42D4C957F2Dull * (q + 1),
                                             ps->hash_dev);
     }
@@ -1116,6 +1132,46 @@ extern "C" int ff_pressure3_project(ff_pressure ps, ff_field u_in, ff_field v_in
                         w_out ? (float *)w_out->d : nullptr, s));
     // prepare + finish (count, commit, correct per axis)
     return read_diag(ps, diag, prepare_launches(ps, true) + 2 + ps->dims);
+}
+
+// project() with the velocity coming from and going to host memory: the
+// upload runs on the context's upload stream after the previous call's
+// compute (its last reads of the inputs), the projection on the compute
+// stream after the upload and after the previous call's download (its outputs
+// are about to be overwritten), the download on the download stream after the
+// projection.  So a call's upload overlaps the previous call's download.  The
+// host buffers should be page-locked; the downloaded values are in place after
+// ff_ctx_synchronize (or after the next call's projection has started).
+extern "C" int ff_pressure3_project_host(ff_pressure ps, ff_field u_in, ff_field v_in, ff_field w_in,
+                                         const void *hu, const void *hv, const void *hw, ff_field u_out,
+                                         ff_field v_out, ff_field w_out, void *hu_out, void *hv_out, void *hw_out,
+                                         ff_diag *diag) {
+    FF_CHECK(ps && u_in && v_in && u_out && v_out && hu && hv && hu_out && hv_out, FF_E_ARG,
+             "project_host: NULL argument");
+    FF_CHECK(ps->dims == 2 || (w_in && w_out && hw && hw_out), FF_E_ARG, "project_host: 3D needs w fields and buffers");
+    cudaSetDevice(ps->ctx->device);
+    FF_TRY(ff_ctx_copy_streams(ps->ctx));
+    for (cudaEvent_t *e : {&ps->ev_compute, &ps->ev_up, &ps->ev_down})
+        if (!*e) FF_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    cudaStream_t s = ps->s(), up = ps->ctx->up, down = ps->ctx->down;
+    ff_field fin[3] = {u_in, v_in, ps->dims == 3 ? w_in : nullptr};
+    ff_field fout[3] = {u_out, v_out, ps->dims == 3 ? w_out : nullptr};
+    const void *hin[3] = {hu, hv, hw};
+    void *hout[3] = {hu_out, hv_out, hw_out};
+    if (ps->host_started) FF_CUDA(cudaStreamWaitEvent(up, ps->ev_compute, 0));
+    for (int a = 0; a < 3; ++a)
+        if (fin[a]) FF_CUDA(cudaMemcpyAsync(fin[a]->d, hin[a], fin[a]->bytes, cudaMemcpyHostToDevice, up));
+    FF_CUDA(cudaEventRecord(ps->ev_up, up));
+    FF_CUDA(cudaStreamWaitEvent(s, ps->ev_up, 0));
+    if (ps->host_started) FF_CUDA(cudaStreamWaitEvent(s, ps->ev_down, 0));
+    FF_TRY(ff_pressure3_project(ps, u_in, v_in, w_in, u_out, v_out, w_out, diag));
+    FF_CUDA(cudaEventRecord(ps->ev_compute, s));
+    FF_CUDA(cudaStreamWaitEvent(down, ps->ev_compute, 0));
+    for (int a = 0; a < 3; ++a)
+        if (fout[a]) FF_CUDA(cudaMemcpyAsync(hout[a], fout[a]->d, fout[a]->bytes, cudaMemcpyDeviceToHost, down));
+    FF_CUDA(cudaEventRecord(ps->ev_down, down));
+    ps->host_started = true;
+    return FF_OK;
 }
 
 // kernel launches of one V-cycle, as vcycle() below enqueues them

@@ -320,6 +320,29 @@ class GridPressureSolver3:
     def _tolerance(self):
         return getattr(self, "_tol", None)
 
+    def project_host(self, input_grid, output_grid, host_in, host_out):
+        """project(input_grid, output_grid) with the velocity coming from
+        and going to host memory: `host_in` / `host_out` are (u, v, w)
+        page-locked host addresses (ints or c_void_p, w None in 2D) of the
+        grids' sizes.  Uploads overlap the previous call's downloads; the
+        outputs are in place after the context synchronises."""
+        diag = _lib.Diag()
+        ptr = lambda a: C.c_void_p(a.value if isinstance(a, C.c_void_p) else a) if a is not None else None
+        w_in = input_grid.data_w.handle if getattr(input_grid, "data_w", None) is not None else None
+        w_out = output_grid.data_w.handle if getattr(output_grid, "data_w", None) is not None else None
+        _lib.check(_lib.load().ff_pressure3_project_host(
+            self.handle, input_grid.data_u.handle, input_grid.data_v.handle, w_in, *[ptr(a) for a in host_in],
+            output_grid.data_u.handle, output_grid.data_v.handle, w_out, *[ptr(a) for a in host_out],
+            C.byref(diag)))
+        self.diagnostics.update(
+            converged=bool(diag.converged), rejected=bool(diag.rejected),
+            iterations=int(diag.iterations), stoppedBy=STOP_REASONS[diag.stopped_by],
+            residual=float(diag.residual), bNorm=float(diag.b_norm),
+            badCells=int(diag.bad_cells), maxIterations=int(diag.max_iterations),
+            kernelLaunches=int(diag.kernel_launches), warmStart=int(diag.warm_start))
+        self.diagnostics.update(_floor_diagnostics(diag, self._tolerance()))
+        return dict(self.diagnostics)
+
     def solve(self, b):
         """cg.solve on A p = b for a given b Field; returns diagnostics."""
         diag = _lib.Diag()
