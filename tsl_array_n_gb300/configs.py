@@ -1,7 +1,7 @@
 """Timings of the configurations besides the 256^3 sphere solve (which
 bench.py measures): one JSON line per configuration on cuda:0.
 
-    python -m tsl_array_n_gb300.configs [c1] [c2[:steps]] [c4] [c5[:steps]]
+    python -m tsl_array_n_gb300.configs [c1] [c2[:steps]] [c4] [c5[:steps]] [c5tp[:steps]] [gridstep]
 
 - c1: 2D 128^2 cylinder, 4-level MGPCG to 1e-6 (double-single and plain
   FP32 iterate): ms per solve, iterations, residual.
@@ -21,7 +21,10 @@ bench.py measures): one JSON line per configuration on cuda:0.
 - c5tp: the configuration as specified: the same dam break with the air
   simulated too (two-phase, liquid:air density 1000:1, variable-coefficient
   projection), 500 steps, with plain FP32, mixed and learned+mixed
-  projections.
+  projections; c5tpdump and c5tpsolve save one of its pressure systems and
+  solve it standalone.
+- gridstep: the 3D grid solver step at 256^3 around the benchmark's sphere,
+  with the advection and the velocity constraint timed alone.
 
 All inputs are synthetic and seeded; every timing is taken with the device
 synchronised on both sides.
@@ -164,6 +167,50 @@ def c2(ctx, steps=2000, timed=100, every=2):
             "ms_per_step": round(ms, 3), "mean_iterations": float(np.mean(its)), "timed_steps": timed,
             "steps": steps, "symmetry_break_step": sym_break, "probes": estimate(series),
             "probes_post_break": estimate(post)}
+
+
+def gridstep(ctx, steps=20):
+    """The 3D grid solver step at 256^3 around the benchmark's sphere (radius
+    24 cells, the 32-mode velocity, closed walls, one pinned cell): explicit
+    viscosity, projection to 1e-6 (mixed, 6 levels, coarsest direct),
+    constrainVelocity, semi-Lagrangian advection of the faces, constraint
+    again; ms per step over `steps` steps, and the advection and the
+    constraint timed alone with their algorithmic bytes.  Advection reads the
+    three velocity arrays for the back-trace and the advected component and
+    writes that component, per component (16 B a face); the constraint, per
+    face: marking (value and weight read, value and int32 marker written,
+    16 B), five Jacobi extrapolation passes (value and marker read and
+    written, 16 B each), no-flux (12 B) and walls (8 B): 116 B a face."""
+    n = 256
+    sc = scenes.sphere_scene(n=n, radius_cells=24, modes=32, seed=1)
+    shape, h = sc["shape"], sc["h"]
+    grid = ff.FaceCenteredGrid3(shape, h).set(sc["u"], sc["v"], sc["w"])
+    col = ff.create_sdf_static_collider3(*shape, *h)
+    col.add_shapes(sc["shapes"])
+    solver = ff.create_grid_solver3(velocity_grid=grid, collider=col, dt=0.25 / n, nu=1e-4,
+                                    dirichlet=(sc["active"], sc["target"]),
+                                    pressure={"multigrid": {"numberOfLevels": 6, "coarseSolve": "direct"},
+                                              "precision": "mixed", "tolerance": 1e-6})
+    for _ in range(3):
+        solver.on_advance_time_step()
+    its = []
+    t0 = _now(ctx)
+    for _ in range(steps):
+        its.append(solver.on_advance_time_step()["iterations"])
+    ms = (_now(ctx) - t0) / steps * 1e3
+    faces = sum(f.count for f in (grid.data_u, grid.data_v, grid.data_w))
+    out = {"config": "3D grid solver step 256^3, sphere r=24, viscosity + projection + advection + constraints",
+           "ms_per_step": round(ms, 3), "mean_iterations": float(np.mean(its))}
+    adv = solver.advection_solver.advect_face_centered3(solver.velocity_prev, solver._scratch)
+    for name, fn, nbytes in (("advection", adv, 16 * faces),
+                             ("constrain", solver.boundary_solver.constrain_velocity, 116 * faces)):
+        fn()
+        t0 = _now(ctx)
+        for _ in range(5):
+            fn()
+        t = (_now(ctx) - t0) / 5
+        out[name] = {"ms": round(t * 1e3, 3), "GB_s": round(nbytes / t / 1e9, 1), "bytes": int(nbytes)}
+    return out
 
 
 def c4(ctx, steps=None):
@@ -421,7 +468,7 @@ def main(argv):
     runs = []
     for a in argv:
         name, _, rest = a.partition(":")
-        if name in ("c1", "c2", "c4", "c5", "c5tp"):
+        if name in ("c1", "c2", "c4", "c5", "c5tp", "gridstep"):
             runs.append((name, {"steps": int(rest)} if rest else {}))
         elif name in ("c5dump", "c5tpdump"):
             steps, _, path = rest.partition(":")
