@@ -22,7 +22,7 @@ using namespace ffg;
 // makeMarkAndProject (grid_blocked_boundary_condition_solver3.js:196-249):
 // open faces are fluid (marker 1); closed faces take the collider's
 // velocity (a static collider: 0) and marker 0
-__global__ void k_mark(VelField F, int a, const float *__restrict__ cw, float *__restrict__ data,
+__global__ void __launch_bounds__(256, 6) k_mark(VelField F, int a, const float *__restrict__ cw, float *__restrict__ data,
                        int *__restrict__ marker) {
     int sx, sy, sz;
     comp_shape(F.g, a, sx, sy, sz);
@@ -117,7 +117,7 @@ __global__ void k_trace(VelField F, long long n, const float *__restrict__ pin, 
 // makeNoFluxProjection (:251-286) with projectAndApplyFriction (:30-44):
 // a closed face takes the tangential part of the sampled velocity,
 // reduced by Coulomb friction (coefficient 0.5, sdf_collider3.js:16)
-__global__ void k_noflux(VelField F, int a, const float *__restrict__ cw, const float *__restrict__ data,
+__global__ void __launch_bounds__(256, 6) k_noflux(VelField F, int a, const float *__restrict__ cw, const float *__restrict__ data,
                          float *__restrict__ temp) {
     int sx, sy, sz;
     comp_shape(F.g, a, sx, sy, sz);
@@ -173,7 +173,7 @@ __global__ void k_blocked(G3 g, const float *__restrict__ phi, float *u, float *
 
 // walls (zeroULeft .. zeroWFront), inflows (buildInflowKernels) and the
 // final clamp (clampComponent, |v| <= 100, non-finite -> 0), per component
-__global__ void k_walls_inflow_clamp(G3 g, int a, float *__restrict__ data, int closed, int n_in,
+__global__ void __launch_bounds__(256, 6) k_walls_inflow_clamp(G3 g, int a, float *__restrict__ data, int closed, int n_in,
                                      const float *const *__restrict__ in_phi, const float *__restrict__ in_vel,
                                      const int *__restrict__ in_mode) {
     int sx, sy, sz;

@@ -160,7 +160,16 @@ __device__ F3 back_trace(const VelField &F, F3 pos, float dt, float dirn, int ma
     return pt;
 }
 
+// (i, j, k) of a flat index; below 2^31 in 32-bit unsigned arithmetic (a
+// 64-bit division is a long software sequence on the GPU)
 __device__ __forceinline__ void unflatten(long long f, int sx, int sy, int &i, int &j, int &k) {
+    if (f < 0x7fffffffLL) {
+        const unsigned u = (unsigned)f, r = u / (unsigned)sx, q = r / (unsigned)sy;
+        i = (int)(u - r * (unsigned)sx);
+        j = (int)(r - q * (unsigned)sy);
+        k = (int)q;
+        return;
+    }
     i = (int)(f % sx);
     long long r = f / sx;
     j = (int)(r % sy);
@@ -178,7 +187,7 @@ __device__ __forceinline__ float frac_inside_sdf(float p0, float p1) {
 }
 
 // one Jacobi step of createExtrapolateToRegion3 (array_utils3.js:88-150)
-__global__ void k_extrapolate(int sx, int sy, int sz, const float *__restrict__ src, float *__restrict__ dst,
+__global__ void __launch_bounds__(256, 8) k_extrapolate(int sx, int sy, int sz, const float *__restrict__ src, float *__restrict__ dst,
                               const int *__restrict__ vs, int *__restrict__ vd) {
     const long long n = (long long)sx * sy * sz, sy_ = sx, sz_ = (long long)sx * sy;
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
