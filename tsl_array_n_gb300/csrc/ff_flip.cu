@@ -856,6 +856,7 @@ extern "C" int ff_flip3_create(ff_ctx ctx, const ff_flip_desc *d, ff_field u, ff
     FF_CHECK(ctx && d && out, FF_E_ARG, "ff_flip3_create: NULL argument");
     FF_CHECK(d->max_particles > 0, FF_E_ARG, "createGridFlipSolver3: options.maxParticles is required.");
     FF_CHECK(d->max_substeps > 0, FF_E_ARG, "createGridFlipSolver3: maxSubsteps must be positive");
+    FF_TRY(check_grid32(d->resolution, "createGridFlipSolver3"));
     const bool density = d->ambient_density != 0.0 || d->component_density != 0.0;
     FF_CHECK(!density || d->carry_concentration, FF_E_ARG,
              "createGridFlipSolver3: ambientDensity/componentDensity require carryConcentration: true -- there is no "
@@ -1282,6 +1283,7 @@ extern "C" int ff_twophase2_destroy(ff_twophase t) {
 static int tp_setup(ff_twophase t) {
     ff_ctx ctx = t->ctx;
     const ff_twophase3_desc &d = t->d;
+    FF_TRY(check_grid32(d.resolution, "createGridTwoPhaseFlipSolver"));
     const int nx = t->g.nx, ny = t->g.ny, nz = t->g.nz;
     t->count = d.max_particles;
     t->r0 = std::max((float)d.ambient_density, MIN_DENSITY);

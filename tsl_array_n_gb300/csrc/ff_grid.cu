@@ -278,6 +278,7 @@ extern "C" int ff_advect3_create(ff_ctx ctx, const ff_advect_desc *d, ff_advect 
              "createSemiLagrangianAdvectionSolver3: resolution must be positive");
     FF_CHECK(d->order == 1 || d->order == 2, FF_E_ARG, "createSemiLagrangianAdvectionSolver3: order must be 1 or 2");
     FF_CHECK(d->max_substeps > 0, FF_E_ARG, "createSemiLagrangianAdvectionSolver3: maxSubsteps must be positive");
+    FF_TRY(check_grid32(d->resolution, "createSemiLagrangianAdvectionSolver3"));
     *out = nullptr;
     cudaSetDevice(ctx->device);
     ff_advect a = new ff_advect_s();
@@ -406,6 +407,7 @@ struct ff_bc_s {
 extern "C" int ff_bc3_create(ff_ctx ctx, const int *res, const double *h, const double *origin, ff_bc *out) {
     FF_CHECK(ctx && res && h && out, FF_E_ARG, "ff_bc3_create: NULL argument");
     FF_CHECK(res[0] > 0 && res[1] > 0 && res[2] > 0, FF_E_ARG, "createGridBlockedBoundaryConditionSolver3: bad resolution");
+    FF_TRY(check_grid32(res, "createGridBlockedBoundaryConditionSolver3"));
     *out = nullptr;
     cudaSetDevice(ctx->device);
     ff_bc b = new ff_bc_s();
@@ -576,6 +578,7 @@ extern "C" int ff_velocity3_add_force(ff_ctx ctx, const int *res, ff_field u, ff
 extern "C" int ff_viscosity3_apply(ff_ctx ctx, const int *res, const double *h, ff_field u, ff_field v, ff_field w,
                                    double nu, double dt, ff_field uo, ff_field vo, ff_field wo) {
     FF_CHECK(ctx && res && h, FF_E_ARG, "ff_viscosity3_apply: NULL argument");
+    FF_TRY(check_grid32(res, "ff_viscosity3_apply"));
     const G3 g = geom_of(res, h, nullptr);
     ff_field in[3] = {u, v, w}, out[3] = {uo, vo, wo};
     for (int a = 0; a < 3; ++a)
@@ -714,6 +717,8 @@ extern "C" int ff_outflow3_create(ff_ctx ctx, const int *res, const double *h, c
              "ff_outflow3_create: bad arguments");
     FF_CHECK(res[0] > 0 && res[1] > 0 && res[2] > 0, FF_E_ARG, "createGridOutflowSolver3: bad resolution");
     FF_CHECK(n <= 64, FF_E_LIMIT, "createGridOutflowSolver3: at most 64 outflows");
+    FF_TRY(check_grid32(res, "createGridOutflowSolver3"));
+    for (int q = 0; q < n; ++q) FF_TRY(check_grid32(phi_res + 3 * q, "createGridOutflowSolver3"));
     *out = nullptr;
     std::vector<G3> pg(n);
     for (int q = 0; q < n; ++q) {

@@ -49,8 +49,9 @@ __device__ float trilinear(const float *__restrict__ d, int sx, int sy, int sz, 
     const int j0c = iclamp(j0, 0, sy - 1), j1c = iclamp(j0 + 1, 0, sy - 1);
     const int k0c = iclamp(k0, 0, sz - 1), k1c = iclamp(k0 + 1, 0, sz - 1);
     const float ux = 1.0f - fx, uy = 1.0f - fy, uz = 1.0f - fz;
-    const long long r00 = (long long)sx * (j0c + (long long)sy * k0c), r10 = (long long)sx * (j1c + (long long)sy * k0c);
-    const long long r01 = (long long)sx * (j0c + (long long)sy * k1c), r11 = (long long)sx * (j1c + (long long)sy * k1c);
+    // 32-bit offsets: the entry points keep every array below 2^31 elements
+    const int r00 = sx * (j0c + sy * k0c), r10 = sx * (j1c + sy * k0c);
+    const int r01 = sx * (j0c + sy * k1c), r11 = sx * (j1c + sy * k1c);
     float s = __ldg(d + r00 + i0c) * (ux * uy * uz);
     s = s + __ldg(d + r00 + i1c) * (fx * uy * uz);
     s = s + __ldg(d + r10 + i0c) * (ux * fy * uz);
@@ -101,7 +102,7 @@ __device__ float tricubic(const float *__restrict__ d, int sx, int sy, int sz, c
         float row[4];
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
-            const float *r = d + (long long)sx * (yi[b] + (long long)sy * zi[c]);
+            const float *r = d + sx * (yi[b] + sy * zi[c]);
             row[b] = mono_cubic(__ldg(r + xi[0]), __ldg(r + xi[1]), __ldg(r + xi[2]), __ldg(r + xi[3]), fx);
         }
         zv[c] = mono_cubic(row[0], row[1], row[2], row[3], fy);
@@ -229,7 +230,7 @@ __device__ F3 trilinear_gradient(const float *__restrict__ d, const G3 &g, F3 o,
         hi[a] = min(lo[a] + 1, n[a] - 1);
         t[a] = fminf(fmaxf(coord[a] - (float)lo[a], 0.0f), 1.0f);
     }
-    auto V = [&](int i, int j, int k) { return __ldg(d + i + (long long)g.nx * (j + (long long)g.ny * k)); };
+    auto V = [&](int i, int j, int k) { return __ldg(d + i + g.nx * (j + g.ny * k)); };
     const float v000 = V(lo[0], lo[1], lo[2]), v100 = V(hi[0], lo[1], lo[2]), v010 = V(lo[0], hi[1], lo[2]);
     const float v110 = V(hi[0], hi[1], lo[2]), v001 = V(lo[0], lo[1], hi[2]), v101 = V(hi[0], lo[1], hi[2]);
     const float v011 = V(lo[0], hi[1], hi[2]), v111 = V(hi[0], hi[1], hi[2]);

@@ -27,6 +27,16 @@ int ff_set_error(int code, const char *fmt, ...);
         if (_s != FF_OK) return _s;                                              \
     } while (0)
 
+// The grid-velocity and FLIP kernels index their arrays in 32 bits, as the
+// reference's WGSL does (u32 indices): every face or cell array of a grid
+// must hold fewer than 2^31 elements.
+inline int check_grid32(const int *res, const char *who) {
+    const long long big = ((long long)res[0] + 1) * ((long long)res[1] + 1) * ((long long)res[2] + 1);
+    FF_CHECK(big < 0x7fffffffLL, FF_E_LIMIT, "%s: a %dx%dx%d grid exceeds 2^31 elements per array", who, res[0],
+             res[1], res[2]);
+    return FF_OK;
+}
+
 // residual-growing stop: the squared residual is compared with the best one
 // seen where the reference's host reads it, at the end of each chunk
 // (linalg.js:942-943, 1839-1882): the first chunk ends at the previous
