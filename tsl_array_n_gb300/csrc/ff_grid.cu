@@ -55,7 +55,9 @@ __global__ void __launch_bounds__(256, 6) k_mark(VelField F, int a, const float 
 //   1 MacCormack forward:  aux = open ? cubic(src @ trace(+1)) : src
 //   2 MacCormack backward: aux = open ? cubic(fwd @ trace(-1)) : fwd
 //   3 MacCormack correct:  out = clamp(fwd + (src - bwd)/2) where open
-__global__ void k_advect(VelField F, int a, int stage, const float *__restrict__ src, const float *__restrict__ fwd,
+// (one kernel per stage: a smaller body for the instruction cache)
+template <int stage>
+__global__ void k_advect(VelField F, int a, const float *__restrict__ src, const float *__restrict__ fwd,
                          const float *__restrict__ bwd, float *__restrict__ out, float dt, int max_substeps) {
     int sx, sy, sz;
     if (a < 3) comp_shape(F.g, a, sx, sy, sz);
@@ -67,14 +69,14 @@ __global__ void k_advect(VelField F, int a, int stage, const float *__restrict__
         unflatten(f, sx, sy, i, j, k);
         const F3 pos = index_pos(F.g, o, i, j, k);
         const bool open = sample_phi(F, F.phi, pos) > 0.0f;
-        if (stage == 0) {
+        if constexpr (stage == 0) {
             if (open) out[f] = tricubic(src, sx, sy, sz, F.g, o, back_trace(F, pos, dt, 1.0f, max_substeps));
-        } else if (stage == 1) {
+        } else if constexpr (stage == 1) {
             out[f] = open ? tricubic(src, sx, sy, sz, F.g, o, back_trace(F, pos, dt, 1.0f, max_substeps)) : src[f];
-        } else if (stage == 2) {
+        } else if constexpr (stage == 2) {
             out[f] = open ? tricubic(fwd, sx, sy, sz, F.g, o, back_trace(F, pos, dt, -1.0f, max_substeps)) : fwd[f];
         } else if (open) {
-            // clampCorrection: min/max over the 8 trilinear corners of the
+            // clampCorrection (stage 3): min/max over the 8 trilinear corners of the
             // traced point whose own positions are open
             const F3 tr = back_trace(F, pos, dt, 1.0f, max_substeps);
             const float fv = fwd[f];
@@ -331,12 +333,12 @@ static int advect_component(ff_advect a, const VelField &F, int c, const float *
     const float dt = (float)a->desc.dt;
     const int ms = a->desc.max_substeps;
     if (a->desc.order == 1) {
-        k_advect<<<nb, 256, 0, s>>>(F, c, 0, src, nullptr, nullptr, out, dt, ms);
+        k_advect<0><<<nb, 256, 0, s>>>(F, c, src, nullptr, nullptr, out, dt, ms);
         return post("advect");
     }
-    k_advect<<<nb, 256, 0, s>>>(F, c, 1, src, nullptr, nullptr, a->fwd[c], dt, ms);
-    k_advect<<<nb, 256, 0, s>>>(F, c, 2, src, a->fwd[c], nullptr, a->bwd[c], dt, ms);
-    k_advect<<<nb, 256, 0, s>>>(F, c, 3, src, a->fwd[c], a->bwd[c], out, dt, ms);
+    k_advect<1><<<nb, 256, 0, s>>>(F, c, src, nullptr, nullptr, a->fwd[c], dt, ms);
+    k_advect<2><<<nb, 256, 0, s>>>(F, c, src, a->fwd[c], nullptr, a->bwd[c], dt, ms);
+    k_advect<3><<<nb, 256, 0, s>>>(F, c, src, a->fwd[c], a->bwd[c], out, dt, ms);
     return post("advect (MacCormack)");
 }
 
