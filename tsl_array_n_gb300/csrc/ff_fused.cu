@@ -2698,7 +2698,7 @@ __global__ void k_brick_flags_cls(Geo g, const uint8_t *__restrict__ cls, int pi
 // the order is deterministic).  One block of 1024 threads; each thread
 // takes a contiguous run of at most 32 items.
 __global__ void __launch_bounds__(1024) k_sweep_order(Geo g, const uint8_t *__restrict__ bricks, int gx, int gy,
-                                                      int gz, int zc, int *order) {
+                                                      int gz, int zc, int tby, int *order) {
     __shared__ int wsum[32];
     __shared__ int total;
     const int n = gx * gy * gz;
@@ -2713,10 +2713,11 @@ __global__ void __launch_bounds__(1024) k_sweep_order(Geo g, const uint8_t *__re
             const int tx = it % gx, ty = (it / gx) % gy, tz = it / (gx * gy);
             const int k0 = tz * zc, k1 = min(k0 + zc, g.d.nz);
             const int bz0 = max(0, k0 - 1) / BZ, bz1 = min(g.d.nz - 1, k1) / BZ;
-            const int bx1 = min(2 * tx + 2, g.bnx);
+            const int bx1 = min(2 * tx + 2, g.bnx), by1 = min(tby * ty + tby, g.bny);
             for (int bz = bz0; bz <= bz1 && !heavy; ++bz)
-                for (int bx = 2 * tx; bx < bx1 && !heavy; ++bx)
-                    heavy = bricks[bx + (long long)g.bnx * (ty + (long long)g.bny * bz)] == 0;
+                for (int by = tby * ty; by < by1 && !heavy; ++by)
+                    for (int bx = 2 * tx; bx < bx1 && !heavy; ++bx)
+                        heavy = bricks[bx + (long long)g.bnx * (by + (long long)g.bny * bz)] == 0;
         }
         if (heavy) {
             mask |= 1u << (it - lo);
@@ -2912,12 +2913,12 @@ int prolong4(const Level &c, const Level &f, int dims, float *fine_x, const PcgS
 // ---- TMA sweep
 bool sweep_tma_ok(const Dims &d) { return d.nx % 4 == 0 && d.nx >= 32; }
 
-static int tma_zchunk_bps(const Dims &d, int sm_count, int bps) {
+static int tma_zchunk_bps(const Dims &d, int sm_count, int bps, int tx, int ty) {
     // About two waves of resident blocks (bps per SM) when the z-chunks stay
     // at 12 planes or more (the work order then starts the expensive items
     // first and the cheap ones fill in behind them), else one wave; at
     // least 4 planes.
-    long long cols = (long long)((d.nx + tq::TX - 1) / tq::TX) * ((d.ny + tq::TY - 1) / tq::TY);
+    long long cols = (long long)((d.nx + tx - 1) / tx) * ((d.ny + ty - 1) / ty);
     long long wave = (long long)bps * sm_count;
     int c2 = (int)std::max(1LL, std::min((long long)d.nz, 2 * wave / cols));
     int zc = (d.nz + c2 - 1) / c2;
@@ -2927,14 +2928,14 @@ static int tma_zchunk_bps(const Dims &d, int sm_count, int bps) {
     }
     return std::min(std::max(zc, std::min(4, d.nz)), tq::MAXZC);
 }
-// the sweep: three blocks per SM
-static int tma_zchunk(const Dims &d, int sm_count) { return tma_zchunk_bps(d, sm_count, 3); }
+// the sweep: three blocks per SM, its own tiles
+static int tma_zchunk(const Dims &d, int sm_count) { return tma_zchunk_bps(d, sm_count, 3, tq::TX, tq::TY); }
 // the CG kernels: p.Ap four blocks per SM, x + alpha p with b - A x two
 static int cg_bps(int which) { return which == 0 ? 4 : 2; }
 
 size_t cg_tma_items(const Dims &d, int sm_count, int which) {
-    const int zc = tma_zchunk_bps(d, sm_count, cg_bps(which));
-    return (size_t)((d.nx + tq::TX - 1) / tq::TX) * ((d.ny + tq::TY - 1) / tq::TY) * ((d.nz + zc - 1) / zc);
+    const int zc = tma_zchunk_bps(d, sm_count, cg_bps(which), tcg::TX, tcg::TY);
+    return (size_t)((d.nx + tcg::TX - 1) / tcg::TX) * ((d.ny + tcg::TY - 1) / tcg::TY) * ((d.nz + zc - 1) / zc);
 }
 
 size_t sweep_tma_blocks(const Dims &d, int sm_count) {
@@ -2995,6 +2996,13 @@ int sweep_tma_maps(const Level &L, const float *x0, const float *x1, uint8_t *cl
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     FF_CHECK(r == CUDA_SUCCESS, FF_E_CUDA, "cuTensorMapEncodeTiled (classes) failed (%d)", (int)r);
+    // the CG kernels stage the same bytes in boxes of their own tiles, so
+    // the sweep's tile can change without their slots overflowing
+    cuuint32_t box_cg[3] = {(cuuint32_t)tcg::CW, (cuuint32_t)tcg::PR, 1};
+    r = enc(&m.cls_cg, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, (void *)cls, dims, strides, box_cg, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    FF_CHECK(r == CUDA_SUCCESS, FF_E_CUDA, "cuTensorMapEncodeTiled (CG classes) failed (%d)", (int)r);
     m.xp[0] = x0;
     m.xp[1] = x1;
     m.cls_ptr = cls;
@@ -3033,11 +3041,13 @@ static int work_orders(const Level &L, const SweepMaps &m, const uint8_t *bricks
     for (int w = 0; w < 3; ++w) {
         int *order = w == 0 ? m.order : w == 1 ? m.order_pap : m.order_xr;
         if (!order) continue;
-        const int zc = w == 0 ? tma_zchunk(L.d, sm_count) : tma_zchunk_bps(L.d, sm_count, cg_bps(w - 1));
-        const int gx = (L.d.nx + tq::TX - 1) / tq::TX, gy = (L.d.ny + tq::TY - 1) / tq::TY;
+        // each kernel's own tiles (16-row bricks: one or more per tile row)
+        const int tx = w == 0 ? tq::TX : tcg::TX, ty = w == 0 ? tq::TY : tcg::TY;
+        const int zc = w == 0 ? tma_zchunk(L.d, sm_count) : tma_zchunk_bps(L.d, sm_count, cg_bps(w - 1), tx, ty);
+        const int gx = (L.d.nx + tx - 1) / tx, gy = (L.d.ny + ty - 1) / ty;
         const int gz = (L.d.nz + zc - 1) / zc;
         FF_CHECK((long long)gx * gy * gz <= 1024LL * 32, FF_E_ARG, "sweep work order: too many items");
-        k_sweep_order<<<1, 1024, 0, s>>>(g, bricks, gx, gy, gz, zc, order);
+        k_sweep_order<<<1, 1024, 0, s>>>(g, bricks, gx, gy, gz, zc, ty / 16, order);
         FF_TRY(post("sweep_order"));
     }
     return FF_OK;
@@ -3223,7 +3233,7 @@ static TcgArgs tcg_args(const Level &L0, const SweepMaps &sm, int sm_count, int 
     a.order = which == 0 ? sm.order_pap : sm.order_xr;
     a.gx = (L0.d.nx + tcg::TX - 1) / tcg::TX;
     a.gy = (L0.d.ny + tcg::TY - 1) / tcg::TY;
-    a.zc = tma_zchunk_bps(L0.d, sm_count, cg_bps(which));
+    a.zc = tma_zchunk_bps(L0.d, sm_count, cg_bps(which), tcg::TX, tcg::TY);
     return a;
 }
 
@@ -3238,7 +3248,7 @@ int p_pap_tma(const Level &L0, const SweepMaps &sm, const CgMaps &m, const float
     a.st = st;
     a.partials = partials;
     dim3 grid(a.gx * a.gy * ((L0.d.nz + a.zc - 1) / a.zc));
-    FF_CUDA(launch_pdl(k_p_pap_tma, grid, dim3(tcg::NT), tcg::PAP_SMEM, s, a, m.z[zi], m.p[0], m.p[1], sm.cls));
+    FF_CUDA(launch_pdl(k_p_pap_tma, grid, dim3(tcg::NT), tcg::PAP_SMEM, s, a, m.z[zi], m.p[0], m.p[1], sm.cls_cg));
     return post("p_pap_tma");
 }
 
@@ -3256,11 +3266,11 @@ int x_residual_tma(const Level &L0, const SweepMaps &sm, const CgMaps &m, float 
     dim3 grid(a.gx * a.gy * ((L0.d.nz + a.zc - 1) / a.zc));
     const size_t sh = tcg::XR_SMEM;
     if (setup) {
-        if (m.ds) FF_CUDA(launch_pdl(k_x_residual_tma<true, true>, grid, dim3(tcg::NT), sh, s, a, m.xh[0], m.xh[1], m.xl[0], m.xl[1], m.p[0], m.p[1], m.b, sm.cls));
-        else FF_CUDA(launch_pdl(k_x_residual_tma<true, false>, grid, dim3(tcg::NT), sh, s, a, m.xh[0], m.xh[1], m.xl[0], m.xl[1], m.p[0], m.p[1], m.b, sm.cls));
+        if (m.ds) FF_CUDA(launch_pdl(k_x_residual_tma<true, true>, grid, dim3(tcg::NT), sh, s, a, m.xh[0], m.xh[1], m.xl[0], m.xl[1], m.p[0], m.p[1], m.b, sm.cls_cg));
+        else FF_CUDA(launch_pdl(k_x_residual_tma<true, false>, grid, dim3(tcg::NT), sh, s, a, m.xh[0], m.xh[1], m.xl[0], m.xl[1], m.p[0], m.p[1], m.b, sm.cls_cg));
     } else {
-        if (m.ds) FF_CUDA(launch_pdl(k_x_residual_tma<false, true>, grid, dim3(tcg::NT), sh, s, a, m.xh[0], m.xh[1], m.xl[0], m.xl[1], m.p[0], m.p[1], m.b, sm.cls));
-        else FF_CUDA(launch_pdl(k_x_residual_tma<false, false>, grid, dim3(tcg::NT), sh, s, a, m.xh[0], m.xh[1], m.xl[0], m.xl[1], m.p[0], m.p[1], m.b, sm.cls));
+        if (m.ds) FF_CUDA(launch_pdl(k_x_residual_tma<false, true>, grid, dim3(tcg::NT), sh, s, a, m.xh[0], m.xh[1], m.xl[0], m.xl[1], m.p[0], m.p[1], m.b, sm.cls_cg));
+        else FF_CUDA(launch_pdl(k_x_residual_tma<false, false>, grid, dim3(tcg::NT), sh, s, a, m.xh[0], m.xh[1], m.xl[0], m.xl[1], m.p[0], m.p[1], m.b, sm.cls_cg));
     }
     return post("x_residual_tma");
 }

@@ -132,6 +132,7 @@ struct SweepMaps {
     CUtensorMap x[2];
     CUtensorMap b;
     CUtensorMap cls;
+    CUtensorMap cls_cg;   // the same class bytes in the level-0 CG kernels' (shorter) boxes
     const float *xp[2] = {nullptr, nullptr};
     uint8_t *cls_ptr = nullptr;
     int cls_pitch = 0;
