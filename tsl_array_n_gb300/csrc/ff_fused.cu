@@ -559,7 +559,7 @@ __device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefe
 __device__ __forceinline__ bool any_general(unsigned c) { return (c & (c >> 1) & 0x55u) != 0; }
 
 template <bool FIRST, bool RZ>
-__global__ void __launch_bounds__(tq::NT, 3)
+__global__ void __launch_bounds__(tq::NT, 4)
     k_sweep_tma(TqArgs a, const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap bmap,
                 const __grid_constant__ CUtensorMap cmap) {
     constexpr int TX = tq::TX, TY = tq::TY, QX = tq::QX, RW = tq::RW, SD = tq::SD, XS = tq::XS, BS = tq::BS;
@@ -2928,8 +2928,8 @@ static int tma_zchunk_bps(const Dims &d, int sm_count, int bps, int tx, int ty) 
     }
     return std::min(std::max(zc, std::min(4, d.nz)), tq::MAXZC);
 }
-// the sweep: three blocks per SM, its own tiles
-static int tma_zchunk(const Dims &d, int sm_count) { return tma_zchunk_bps(d, sm_count, 3, tq::TX, tq::TY); }
+// the sweep: four blocks per SM (64 registers), its own tiles
+static int tma_zchunk(const Dims &d, int sm_count) { return tma_zchunk_bps(d, sm_count, 4, tq::TX, tq::TY); }
 // the CG kernels: p.Ap four blocks per SM, x + alpha p with b - A x two
 static int cg_bps(int which) { return which == 0 ? 4 : 2; }
 
