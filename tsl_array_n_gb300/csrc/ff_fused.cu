@@ -2255,6 +2255,12 @@ constexpr int TAIL_ONE_BLOCK_COARSE = 8192;
 struct TailLevel {
     Geo g;
     float *x, *b, *r;              // r: residual scratch of the level
+    // block-0 levels held in shared memory: offset (floats) of the level's
+    // x, b and r there (n floats each), -1 for a level in global memory
+    int smo;
+    // t / hx, t / nx and t / ny as (t m) >> 40 with m = ceil(2^40 / divisor)
+    // (exact for every t below 2^22 and divisor below 2^18)
+    unsigned long long mhx, mnx, mny;
     const float4 *coef, *gco;
     const uint8_t *cls, *mask;     // class bytes (cpitch bytes per row), Dirichlet mask (may be null)
     int cpitch;
@@ -2270,6 +2276,7 @@ struct TailArgs {
     int coarse_sweeps;             // > 0: that many sweeps on the coarsest level instead of G b
     PcgState *st;                  // may be null
     unsigned *bar;                 // grid barrier: arrivals, generation, abort
+    int cxo;                       // the coarsest x's copy in shared memory (floats; -1: none)
 };
 
 // Grid-wide barrier of the cooperative launch over three words: a count of
@@ -2346,20 +2353,56 @@ __device__ __forceinline__ float tail_relax(const TailArgs &a, const TailLevel &
     return __fmaf_rn(bval - s, a.sor * hi.w, a.omsor * vc);
 }
 
+// A 2D level of at most TAIL_SMEM_CELLS cells (and every coarser one but the
+// coarsest) lives in block 0's shared memory while the launch runs: block 0
+// alone runs its phases, so they need no grid barrier and no L2 round
+// trip.  Its b arrives there by the restriction into it (or, for the
+// launch's first level, by a copy from global memory) and its x leaves for
+// global memory after its last pass when the next finer level is a
+// grid-wide one.  SM: the level's arrays are there (plain loads); otherwise
+// loads bypass L1, which other blocks' writes in this launch leave stale.
+constexpr int TAIL_SMEM_CELLS = 8192;
+constexpr int TAIL_SMEM_BYTES = 3 * 4 * 8192 + 3 * 4 * 1024;   // 3 arrays of a 8192- and a 1024-cell level
+__device__ __forceinline__ int tdiv(int t, unsigned long long m) {
+    return (int)(((unsigned long long)(unsigned)t * m) >> 40);
+}
+template <bool SM>
+__device__ __forceinline__ float tld(const float *p) {
+    if constexpr (SM) return *p;
+    else return __ldcg(p);
+}
+struct TailArr {
+    float *x, *b, *r;
+};
+template <bool SM>
+__device__ __forceinline__ TailArr tail_arrays(const TailLevel &L) {
+    if constexpr (SM) {
+        extern __shared__ __align__(16) float tail_sm[];
+        const int n = (int)L.g.d.n();
+        float *x = tail_sm + L.smo;
+        return TailArr{x, x + n, x + 2 * n};
+    } else {
+        return TailArr{L.x, L.b, L.r};
+    }
+}
+
 // one colour pass (colour col = (i + j + k) & 1) in place, one thread per
 // cell of the colour (nx is even: nx / 2 of them per row); `first`: x is 0
 // on entry and the thread also writes 0 to the row neighbour of the other
 // colour
+template <bool SM>
 __device__ void tail_colour(const TailArgs &a, const TailLevel &L, int col, bool first, long long t0,
                             long long stride) {
     const Geo &g = L.g;
     const int nx = g.d.nx, ny = g.d.ny, nz = g.d.nz, hx = nx >> 1;
     const int n = hx * ny * nz;
-    float *x = L.x;
+    const TailArr A = tail_arrays<SM>(L);
+    float *x = A.x;
     for (int t = (int)t0; t < n; t += (int)stride) {
-        const int m = t % hx;
-        const int rr = t / hx;
-        const int j = rr % ny, k = rr / ny;
+        const int rr = tdiv(t, L.mhx);
+        const int m = t - rr * hx;
+        const int k = tdiv(rr, L.mny);
+        const int j = rr - k * ny;
         const int par = (j + k + col) & 1;
         const int i = 2 * m + par;
         const int c = i + (int)g.sy * j + (int)g.sz * k;
@@ -2367,58 +2410,64 @@ __device__ void tail_colour(const TailArgs &a, const TailLevel &L, int col, bool
         if (first) {
             x[c + (par ? -1 : 1)] = 0.f;
         } else {
-            vc = __ldcg(x + c);
-            if (i > 0) xm = __ldcg(x + c - 1);
-            if (i < nx - 1) xp = __ldcg(x + c + 1);
-            if (j > 0) ym = __ldcg(x + c - g.sy);
-            if (j < ny - 1) yp = __ldcg(x + c + g.sy);
-            if (k > 0) zm = __ldcg(x + c - g.sz);
-            if (k < nz - 1) zp = __ldcg(x + c + g.sz);
+            vc = tld<SM>(x + c);
+            if (i > 0) xm = tld<SM>(x + c - 1);
+            if (i < nx - 1) xp = tld<SM>(x + c + 1);
+            if (j > 0) ym = tld<SM>(x + c - g.sy);
+            if (j < ny - 1) yp = tld<SM>(x + c + g.sy);
+            if (k > 0) zm = tld<SM>(x + c - g.sz);
+            if (k < nz - 1) zp = tld<SM>(x + c + g.sz);
         }
-        x[c] = tail_relax(a, L, tail_class(L, i, j, k), c, i, j, k, vc, xm, xp, ym, yp, zm, zp, __ldcg(L.b + c));
+        x[c] = tail_relax(a, L, tail_class(L, i, j, k), c, i, j, k, vc, xm, xp, ym, yp, zm, zp, tld<SM>(A.b + c));
     }
 }
 
 // r = b - A x (0 on Dirichlet cells); xzero: x is taken as 0 and cleared
+template <bool SM>
 __device__ void tail_residual(const TailLevel &L, bool xzero, long long t0, long long stride) {
     const Geo &g = L.g;
     const int nx = g.d.nx, ny = g.d.ny, nz = g.d.nz;
     const int n = nx * ny * nz;
-    const float *x = L.x;
+    const TailArr A = tail_arrays<SM>(L);
+    const float *x = A.x;
     for (int c = (int)t0; c < n; c += (int)stride) {
-        const int i = c % nx;
-        const int rr = c / nx;
-        const int j = rr % ny, k = rr / ny;
+        const int rr = tdiv(c, L.mnx);
+        const int i = c - rr * nx;
+        const int k = tdiv(rr, L.mny);
+        const int j = rr - k * ny;
         const unsigned cl = tail_class(L, i, j, k);
         if (xzero) {
-            L.r[c] = cl == 1u ? 0.f : __ldcg(L.b + c);
-            L.x[c] = 0.f;
+            A.r[c] = cl == 1u ? 0.f : tld<SM>(A.b + c);
+            A.x[c] = 0.f;
             continue;
         }
-        const float vc = __ldcg(x + c);
-        const float xm = i > 0 ? __ldcg(x + c - 1) : vc, xp = i < nx - 1 ? __ldcg(x + c + 1) : vc;
-        const float ym = j > 0 ? __ldcg(x + c - g.sy) : vc, yp = j < ny - 1 ? __ldcg(x + c + g.sy) : vc;
-        const float zm = k > 0 ? __ldcg(x + c - g.sz) : vc, zp = k < nz - 1 ? __ldcg(x + c + g.sz) : vc;
-        L.r[c] = resid_cls(g, L.coef, cl, i, j, k, __ldcg(L.b + c), vc, xm, xp, ym, yp, zm, zp);
+        const float vc = tld<SM>(x + c);
+        const float xm = i > 0 ? tld<SM>(x + c - 1) : vc, xp = i < nx - 1 ? tld<SM>(x + c + 1) : vc;
+        const float ym = j > 0 ? tld<SM>(x + c - g.sy) : vc, yp = j < ny - 1 ? tld<SM>(x + c + g.sy) : vc;
+        const float zm = k > 0 ? tld<SM>(x + c - g.sz) : vc, zp = k < nz - 1 ? tld<SM>(x + c + g.sz) : vc;
+        A.r[c] = resid_cls(g, L.coef, cl, i, j, k, tld<SM>(A.b + c), vc, xm, xp, ym, yp, zm, zp);
     }
 }
 
 // coarse b = R r (the 1/8, 3/8, 3/8, 1/8 taps per axis), 0 on coarse
 // Dirichlet cells; relax0: also the coarse level's first colour-0 pass
 // (from x = 0 a cell needs only its own b; colour-1 cells get 0)
+template <bool FSM, bool CSM>
 __device__ void tail_restrict(const TailArgs &a, const TailLevel &F, const TailLevel &C, bool relax0, long long t0,
                               long long stride) {
     const Dims fd = F.g.d, cd = C.g.d;
+    const TailArr FA = tail_arrays<FSM>(F), CA = tail_arrays<CSM>(C);
     const int n = cd.nx * cd.ny * cd.nz;
     const float w4[4] = {0.125f, 0.375f, 0.375f, 0.125f};
     for (int c = (int)t0; c < n; c += (int)stride) {
-        const int I = c % cd.nx;
-        const int rr = c / cd.nx;
-        const int J = rr % cd.ny, K = rr / cd.ny;
+        const int rr = tdiv(c, C.mnx);
+        const int I = c - rr * cd.nx;
+        const int K = tdiv(rr, C.mny);
+        const int J = rr - K * cd.ny;
         if (C.mask && __ldg(C.mask + c)) {
-            C.b[c] = 0.f;
+            CA.b[c] = 0.f;
             if (relax0)
-                C.x[c] = ((I + J + K) & 1) ? 0.f
+                CA.x[c] = ((I + J + K) & 1) ? 0.f
                                            : tail_relax(a, C, tail_class(C, I, J, K), c, I, J, K, 0.f, 0.f, 0.f, 0.f,
                                                         0.f, 0.f, 0.f, 0.f);
             continue;
@@ -2435,16 +2484,16 @@ __device__ void tail_restrict(const TailArgs &a, const TailLevel &F, const TailL
             float part = 0.f;
 #pragma unroll
             for (int p = 0; p < 4; ++p) {
-                const float *row = F.r + fd.nx * (jy[p] + fd.ny * kz[q]);
-                const float rx = 0.125f * __ldcg(row + ix[0]) + 0.375f * __ldcg(row + ix[1]) +
-                                 0.375f * __ldcg(row + ix[2]) + 0.125f * __ldcg(row + ix[3]);
+                const float *row = FA.r + fd.nx * (jy[p] + fd.ny * kz[q]);
+                const float rx = 0.125f * tld<FSM>(row + ix[0]) + 0.375f * tld<FSM>(row + ix[1]) +
+                                 0.375f * tld<FSM>(row + ix[2]) + 0.125f * tld<FSM>(row + ix[3]);
                 part += rx * w4[p];
             }
             s += part * wz;
         }
-        C.b[c] = s;
+        CA.b[c] = s;
         if (relax0)
-            C.x[c] = ((I + J + K) & 1) ? 0.f
+            CA.x[c] = ((I + J + K) & 1) ? 0.f
                                        : tail_relax(a, C, tail_class(C, I, J, K), c, I, J, K, 0.f, 0.f, 0.f, 0.f, 0.f,
                                                     0.f, 0.f, s);
     }
@@ -2465,15 +2514,18 @@ __device__ void tail_direct(const TailArgs &a, const TailLevel &C) {
 }
 
 // fine x += P coarse x, skipped on fine Dirichlet cells
+template <bool CSM, bool FSM>
 __device__ void tail_prolong(const TailArgs &a, const TailLevel &C, const TailLevel &F, long long t0,
                              long long stride) {
     const Dims fd = F.g.d, cd = C.g.d;
+    const TailArr CA = tail_arrays<CSM>(C), FA = tail_arrays<FSM>(F);
     const int n = fd.nx * fd.ny * fd.nz;
     for (int c = (int)t0; c < n; c += (int)stride) {
         if (F.mask && __ldg(F.mask + c)) continue;
-        const int i = c % fd.nx;
-        const int rr = c / fd.nx;
-        const int j = rr % fd.ny, k = rr / fd.ny;
+        const int rr = tdiv(c, F.mnx);
+        const int i = c - rr * fd.nx;
+        const int k = tdiv(rr, F.mny);
+        const int j = rr - k * fd.ny;
         int ii[2], jj[2], kk[2];
         float wi[2], wj[2], wk[2];
         ptaps2(i, cd.nx, ii, wi);
@@ -2484,11 +2536,11 @@ __device__ void tail_prolong(const TailArgs &a, const TailLevel &C, const TailLe
         float acc = 0.f;
         for (int b = 0; b < 2; ++b)
             for (int q = 0; q < nk; ++q) {
-                const float *row = C.x + cd.nx * (jj[b] + cd.ny * kk[q]);
+                const float *row = CA.x + cd.nx * (jj[b] + cd.ny * kk[q]);
                 const float w = wj[b] * wk[q];
-                acc += (wi[0] * __ldcg(row + ii[0]) + wi[1] * __ldcg(row + ii[1])) * w;
+                acc += (wi[0] * tld<CSM>(row + ii[0]) + wi[1] * tld<CSM>(row + ii[1])) * w;
             }
-        F.x[c] = __ldcg(F.x + c) + acc;
+        FA.x[c] = tld<FSM>(FA.x + c) + acc;
     }
 }
 
@@ -2499,9 +2551,10 @@ __device__ void tail_coarse_colour(const TailArgs &a, const TailLevel &C, int co
     const int sy = d.nx, sz = d.nx * d.ny, n = (int)d.n();
     float *x = C.x;
     for (int c = (int)t0; c < n; c += (int)stride) {
-        const int i = c % d.nx;
-        const int rr = c / d.nx;
-        const int j = rr % d.ny, k = rr / d.ny;
+        const int rr = tdiv(c, C.mnx);
+        const int i = c - rr * d.nx;
+        const int k = tdiv(rr, C.mny);
+        const int j = rr - k * d.ny;
         if (((i + j + k) & 1) != col) continue;
         const float xc = __ldcg(x + c);
         const float4 kc = __ldg(C.coef + c);
@@ -2517,6 +2570,9 @@ __device__ void tail_coarse_colour(const TailArgs &a, const TailLevel &C, int co
     }
 }
 
+// HELD: some levels are held in block 0's shared memory (the instance
+// without them carries none of their dispatch)
+template <bool HELD>
 __global__ void __launch_bounds__(TAIL_NT, 1) k_vcycle_tail(TailArgs a) {
     PcgState *st = a.st;
     if (st && (st->stop || st->err)) return;
@@ -2524,14 +2580,16 @@ __global__ void __launch_bounds__(TAIL_NT, 1) k_vcycle_tail(TailArgs a) {
     unsigned passed = 0;
     const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    // A phase over a level of at most one_block cells runs in block 0
-    // alone, with a block barrier after it; a phase over a larger level runs
-    // on every block with a grid barrier after it, and one more grid barrier
-    // first when block-0 phases precede it.  Every block takes the same
-    // sequence of grid barriers (the choice depends only on level sizes).
+    // A phase over a level of at most one_block cells, or held in block 0's
+    // shared memory, runs in block 0 alone, with a block barrier after it; a
+    // phase over a larger level runs on every block with a grid barrier
+    // after it, and one more grid barrier first when block-0 phases precede
+    // it.  Every block takes the same sequence of grid barriers (the choice
+    // depends only on level sizes).
     bool solo_prev = false;
     const int one_block = a.dims == 3 ? TAIL_ONE_BLOCK_3D : TAIL_ONE_BLOCK_2D;
-    auto small = [&](int l) { return a.lv[l].g.d.n() <= one_block; };
+    auto held = [&](int l) { return HELD && a.lv[l].smo >= 0; };
+    auto small = [&](int l) { return held(l) || a.lv[l].g.d.n() <= one_block; };
     auto phase = [&](bool solo, bool sync_after, auto &&work) -> bool {
         if (solo) {
             if (blockIdx.x == 0) {
@@ -2548,24 +2606,70 @@ __global__ void __launch_bounds__(TAIL_NT, 1) k_vcycle_tail(TailArgs a) {
         work(t0, stride);
         return sync_after ? tail_sync(bar, passed) : true;
     };
+    // a held level's x to global memory, or its b and x from there (block 0)
+    auto copy_x_out = [&](int l) {
+        if constexpr (!HELD) return;
+        const TailArr A = tail_arrays<true>(a.lv[l]);
+        const int n = (int)a.lv[l].g.d.n();
+        for (int c = threadIdx.x; c < n; c += blockDim.x) a.lv[l].x[c] = A.x[c];
+    };
+    auto copy_in = [&](int l) {
+        if constexpr (!HELD) return;
+        const TailArr A = tail_arrays<true>(a.lv[l]);
+        const int n = (int)a.lv[l].g.d.n();
+        for (int c = threadIdx.x; c < n; c += blockDim.x) {
+            A.b[c] = __ldcg(a.lv[l].b + c);
+            A.x[c] = __ldcg(a.lv[l].x + c);
+        }
+    };
     bool ok = true;
+    if (held(0))
+        ok = phase(true, true, [&](long long q0, long long qs) {
+            const TailArr A = tail_arrays<true>(a.lv[0]);
+            for (long long c = q0; c < a.lv[0].g.d.n(); c += qs) A.b[c] = __ldcg(a.lv[0].b + c);
+        });
     // the coarse level's first colour-0 pass rides on the restriction into it
     // (not into the coarsest level, which is solved directly or swept)
     for (int l = 0; l < a.nl - 1 && ok; ++l) {
         const TailLevel &L = a.lv[l];
-        const bool fused0 = l > 0 && a.down > 0, sl = small(l);
+        const bool fused0 = l > 0 && a.down > 0, sl = small(l), hl = held(l);
         for (int it = 0; it < a.down && ok; ++it) {
             if (!(fused0 && it == 0))
-                ok = phase(sl, true, [&](long long q0, long long qs) { tail_colour(a, L, 0, it == 0, q0, qs); });
-            if (ok) ok = phase(sl, true, [&](long long q0, long long qs) { tail_colour(a, L, 1, false, q0, qs); });
+                ok = phase(sl, true, [&](long long q0, long long qs) {
+                    if (hl) tail_colour<true>(a, L, 0, it == 0, q0, qs);
+                    else tail_colour<false>(a, L, 0, it == 0, q0, qs);
+                });
+            if (ok) ok = phase(sl, true, [&](long long q0, long long qs) {
+                if (hl) tail_colour<true>(a, L, 1, false, q0, qs);
+                else tail_colour<false>(a, L, 1, false, q0, qs);
+            });
         }
         if (!ok) break;
-        ok = phase(sl, true, [&](long long q0, long long qs) { tail_residual(L, a.down == 0, q0, qs); });
-        if (!ok) break;
-        // the restriction runs over the coarse level's cells
-        ok = phase(small(l + 1), true, [&](long long q0, long long qs) {
-            tail_restrict(a, L, a.lv[l + 1], l + 1 < a.nl - 1 && a.down > 0, q0, qs);
+        ok = phase(sl, true, [&](long long q0, long long qs) {
+            if (hl) tail_residual<true>(L, a.down == 0, q0, qs);
+            else tail_residual<false>(L, a.down == 0, q0, qs);
         });
+        if (!ok) break;
+        // the restriction runs over the coarse level's cells; into a held
+        // level from a grid-wide one it runs grid-wide into the level's global
+        // arrays, which block 0 then takes into shared memory
+        const bool relax0 = l + 1 < a.nl - 1 && a.down > 0, hc = held(l + 1);
+        if (!HELD) {
+            ok = phase(small(l + 1), true, [&](long long q0, long long qs) {
+                tail_restrict<false, false>(a, L, a.lv[l + 1], relax0, q0, qs);
+            });
+        } else if (hc && !hl) {
+            ok = phase(false, true, [&](long long q0, long long qs) {
+                tail_restrict<false, false>(a, L, a.lv[l + 1], relax0, q0, qs);
+            });
+            if (ok) ok = phase(true, true, [&](long long, long long) { copy_in(l + 1); });
+        } else {
+            ok = phase(small(l + 1), true, [&](long long q0, long long qs) {
+                if (hl && hc) tail_restrict<true, true>(a, L, a.lv[l + 1], relax0, q0, qs);
+                else if (hl) tail_restrict<true, false>(a, L, a.lv[l + 1], relax0, q0, qs);
+                else tail_restrict<false, false>(a, L, a.lv[l + 1], relax0, q0, qs);
+            });
+        }
     }
     if (ok) {
         const TailLevel &C = a.lv[a.nl - 1];
@@ -2584,13 +2688,47 @@ __global__ void __launch_bounds__(TAIL_NT, 1) k_vcycle_tail(TailArgs a) {
     }
     for (int l = a.nl - 2; l >= 0 && ok; --l) {
         const TailLevel &L = a.lv[l];
-        const bool sl = small(l);
-        ok = phase(sl, true, [&](long long q0, long long qs) { tail_prolong(a, a.lv[l + 1], L, q0, qs); });
+        const bool sl = small(l), hl = held(l);
+        // a held coarse level is read from shared memory only by a held fine
+        // level's phase (block 0); a grid-wide phase reads its global copy
+        const bool hc = hl && held(l + 1);
+        const bool out = hl && (l == 0 || !held(l - 1));
+        ok = phase(sl, true, [&](long long q0, long long qs) {
+            if (hl && hc) {
+                tail_prolong<true, true>(a, a.lv[l + 1], L, q0, qs);
+            } else if (hl && l + 1 == a.nl - 1 && a.cxo >= 0) {
+                // the coarsest x (global, written grid-wide) into shared memory first
+                extern __shared__ __align__(16) float tail_sm[];
+                const TailLevel &C = a.lv[l + 1];
+                for (long long c = q0; c < C.g.d.n(); c += qs) tail_sm[a.cxo + c] = __ldcg(C.x + c);
+                __syncthreads();
+                TailLevel Cs = C;
+                Cs.smo = a.cxo;
+                tail_prolong<true, true>(a, Cs, L, q0, qs);
+            } else if (hl) {
+                tail_prolong<false, true>(a, a.lv[l + 1], L, q0, qs);
+            } else {
+                tail_prolong<false, false>(a, a.lv[l + 1], L, q0, qs);
+            }
+            if (out && a.up == 0) {
+                __syncthreads();
+                copy_x_out(l);
+            }
+        });
         for (int it = 0; it < a.up && ok; ++it) {
-            ok = phase(sl, true, [&](long long q0, long long qs) { tail_colour(a, L, 1, false, q0, qs); });
+            ok = phase(sl, true, [&](long long q0, long long qs) {
+                if (hl) tail_colour<true>(a, L, 1, false, q0, qs);
+                else tail_colour<false>(a, L, 1, false, q0, qs);
+            });
             // the kernel's end orders the last pass before the next launch
-            if (ok) ok = phase(sl, !(l == 0 && it == a.up - 1),
-                               [&](long long q0, long long qs) { tail_colour(a, L, 0, false, q0, qs); });
+            if (ok) ok = phase(sl, !(l == 0 && it == a.up - 1), [&](long long q0, long long qs) {
+                if (hl) tail_colour<true>(a, L, 0, false, q0, qs);
+                else tail_colour<false>(a, L, 0, false, q0, qs);
+                if (out && it == a.up - 1) {
+                    __syncthreads();
+                    copy_x_out(l);
+                }
+            });
         }
     }
     if (ok) tail_done(bar);
@@ -3295,6 +3433,11 @@ int vcycle_tail(const Level *lv, const SweepMaps *sm, int nl, int dims, int down
         t.coef = L.coef;
         t.mask = L.mask;
         t.rdreg_sor = sor / t.g.dreg;
+        t.smo = -1;
+        auto magic = [](long long d) { return ((1ULL << 40) + (unsigned long long)d - 1) / (unsigned long long)d; };
+        t.mhx = magic(std::max(1, L.d.nx / 2));
+        t.mnx = magic(L.d.nx);
+        t.mny = magic(L.d.ny);
         if (l < nl - 1) {
             FF_CHECK(sm[l].cls_ptr && sm[l].gco && L.buf, FF_E_STATE, "coarse V-cycle: level %d lacks classes", l);
             t.cls = sm[l].cls_ptr;
@@ -3317,20 +3460,47 @@ int vcycle_tail(const Level *lv, const SweepMaps *sm, int nl, int dims, int down
     a.coarse_sweeps = coarse_sweeps;
     a.st = st;
     a.bar = bar;
-    static int per_sm = -1;
-    if (per_sm < 0) FF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vcycle_tail, TAIL_NT, 0));
-    FF_CHECK(per_sm >= 1, FF_E_CUDA, "coarse V-cycle kernel does not fit an SM");
+    // levels held in block 0's shared memory (2D): from the last but one
+    // upward while they have at most TAIL_SMEM_CELLS cells and fit the budget
+    // (and, beside the last but one, a copy of the coarsest x).  In 3D the
+    // 16^3 level held there made the 256^3 V-cycle slower (0.587 -> 0.596
+    // ms: its block-0 phases cost more than the grid barriers they saved), so
+    // 3D levels stay grid-wide.
+    int smem = 0;
+    const long long nc = lv[nl - 1].d.n();
+    for (int l = nl - 2; l >= 0 && dims == 2; --l) {
+        const long long n = lv[l].d.n();
+        if (n > TAIL_SMEM_CELLS || smem + 12 * n + (l == nl - 2 ? 4 * nc : 0) > TAIL_SMEM_BYTES) break;
+        a.lv[l].smo = smem / 4;
+        smem += (int)(12 * n);
+    }
+    a.cxo = -1;
+    if (a.lv[nl - 2].smo >= 0) {
+        a.cxo = smem / 4;
+        smem += (int)(4 * nc);
+    }
+    static int per_sm = -1, per_sm_held = -1;
+    if (per_sm < 0) {
+        FF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vcycle_tail<false>, TAIL_NT, 0));
+        FF_CUDA(cudaFuncSetAttribute(k_vcycle_tail<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     TAIL_SMEM_BYTES));
+        FF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_held, k_vcycle_tail<true>, TAIL_NT,
+                                                              TAIL_SMEM_BYTES));
+    }
+    FF_CHECK(per_sm >= 1 && per_sm_held >= 1 && smem <= TAIL_SMEM_BYTES, FF_E_CUDA,
+             "coarse V-cycle kernel does not fit an SM");
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)sm_count);
     cfg.blockDim = dim3(TAIL_NT);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = (size_t)smem;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    FF_CUDA(cudaLaunchKernelEx(&cfg, k_vcycle_tail, a));
+    if (smem > 0) FF_CUDA(cudaLaunchKernelEx(&cfg, k_vcycle_tail<true>, a));
+    else FF_CUDA(cudaLaunchKernelEx(&cfg, k_vcycle_tail<false>, a));
     return post("vcycle_tail");
 }
 
