@@ -553,6 +553,35 @@ __device__ __forceinline__ void relax_pair_rt(const Geo &g, const TqArgs &a, flo
     q.w = p1 ? n1 : q.w;
 }
 
+// The first colour of a sweep from x = 0: every neighbour and the cell
+// itself are zero, so the coupling sum S is +0 and (1 - sor) v + (b - S) rd
+// is fma(b, rd, (1 - sor) 0), bit for bit what relax_plain and relax_any
+// give, with rd by class (-sor for a Dirichlet row, sor / diagonal for
+// class 3).  P: the colour offset of the pair (cells P and P + 2) in the
+// quad, whose staged values are zero and stay so at the other offset.
+__device__ __forceinline__ float first_scale(const TqArgs &a, unsigned cls, long long c, float rd) {
+    if (cls == 1u) return -a.sor;
+    if (cls == 3u) return a.sor * __ldg(&a.gco[c].w);
+    return rd;
+}
+__device__ __forceinline__ void relax_pair_first(const Geo &g, const TqArgs &a, float4 &q, const float4 &bq,
+                                                 unsigned cq, const QuadScale &e, int gi, int gj, int k, int P) {
+    const bool p1 = P != 0;
+    const float b0 = p1 ? bq.y : bq.x, b1 = p1 ? bq.w : bq.z;
+    float r0 = p1 ? e.r12 : e.r0, r1 = p1 ? e.r3 : e.r12;
+    if (cq & (0x11u << (2 * P))) {
+        const long long c = gi + P + g.sy * gj + g.sz * k;
+        r0 = first_scale(a, (cq >> (2 * P)) & 3u, c, r0);
+        r1 = first_scale(a, (cq >> (2 * P + 4)) & 3u, c + 2, r1);
+    }
+    const float z = a.omsor * 0.f;
+    const float n0 = __fmaf_rn(b0, r0, z), n1 = __fmaf_rn(b1, r1, z);
+    q.x = p1 ? q.x : n0;
+    q.y = p1 ? n0 : q.y;
+    q.z = p1 ? q.z : n1;
+    q.w = p1 ? n1 : q.w;
+}
+
 __device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 __device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
 // any cell of class 3 among the four 2-bit fields of a class byte
@@ -704,17 +733,23 @@ __global__ void __launch_bounds__(tq::NT, 4)
             if (ka >= 0 && ka <= k1 && ka < g.d.nz) {
                 // first colour on plane m+2 (its neighbours carry the second
                 // colour: values as staged)
-                const float4 ym = lds4(X2 + o - RW), yp = lds4(X2 + o + RW);
-                const QuadScale e = scale_at(ka);
-                const unsigned c2 = (cpipe >> 16) & 0xffu;
-                if ((ca ^ gj ^ ka) & 1) {
-                    float s = __shfl_down_sync(FULL, q2.x, 1);
-                    if (qx == QX - 1) s = X2[o + 4];
-                    if (quad_in) relax_pair<1>(g, a, q2, s, ym, yp, q1, q3, bb2, c2, e, gi, gj, ka);
+                if (FIRST) {
+                    const QuadScale e = scale_at(ka);
+                    const unsigned c2 = (cpipe >> 16) & 0xffu;
+                    if (quad_in) relax_pair_first(g, a, q2, bb2, c2, e, gi, gj, ka, (ca ^ gj ^ ka) & 1);
                 } else {
-                    float s = __shfl_up_sync(FULL, q2.w, 1);
-                    if (qx == 0) s = X2[o - 1];
-                    if (quad_in) relax_pair<0>(g, a, q2, s, ym, yp, q1, q3, bb2, c2, e, gi, gj, ka);
+                    const float4 ym = lds4(X2 + o - RW), yp = lds4(X2 + o + RW);
+                    const QuadScale e = scale_at(ka);
+                    const unsigned c2 = (cpipe >> 16) & 0xffu;
+                    if ((ca ^ gj ^ ka) & 1) {
+                        float s = __shfl_down_sync(FULL, q2.x, 1);
+                        if (qx == QX - 1) s = X2[o + 4];
+                        if (quad_in) relax_pair<1>(g, a, q2, s, ym, yp, q1, q3, bb2, c2, e, gi, gj, ka);
+                    } else {
+                        float s = __shfl_up_sync(FULL, q2.w, 1);
+                        if (qx == 0) s = X2[o - 1];
+                        if (quad_in) relax_pair<0>(g, a, q2, s, ym, yp, q1, q3, bb2, c2, e, gi, gj, ka);
+                    }
                 }
                 if (quad_in) *reinterpret_cast<float4 *>(X2 + o) = q2;
             }
@@ -766,7 +801,20 @@ __global__ void __launch_bounds__(tq::NT, 4)
                     prefetch_l1(a.coef + off);
                     prefetch_l1(a.gco + off);
                 }
-                if (ka >= 0 && ka <= k1 && ka < g.d.nz) {
+                if (FIRST && ka >= 0 && ka <= k1 && ka < g.d.nz) {
+                    if (rquad_in) {
+                        float4 rq = lds4(X2 + ro4);
+                        const float4 rbq = lds4(Bn + rbo);
+                        const int mz = (ka == 0 || ka == g.d.nz - 1) ? 9 * mze : 0;
+                        const int rmy = (rgj == 0) + (rgj == g.d.ny - 1);
+                        QuadScale re;
+                        re.r0 = rdt[(rgi == 0) + 3 * rmy + mz];
+                        re.r12 = rdt[3 * rmy + mz];
+                        re.r3 = rdt[(rgi + 3 == g.d.nx - 1) + 3 * rmy + mz];
+                        relax_pair_first(g, a, rq, rbq, rcls, re, rgi, rgj, ka, (ca ^ rgj ^ ka) & 1);
+                        *reinterpret_cast<float4 *>(X2 + ro4) = rq;
+                    }
+                } else if (ka >= 0 && ka <= k1 && ka < g.d.nz) {
                     float4 rq = lds4(X2 + ro4);
                     float sd = __shfl_down_sync(FULL, rq.x, 1, QX), su = __shfl_up_sync(FULL, rq.w, 1, QX);
                     if (rl == QX - 1) sd = X2[ro4 + 4];
@@ -806,8 +854,12 @@ __global__ void __launch_bounds__(tq::NT, 4)
                     const int ro = (ly0 + 2) * RW + clx + 4;
                     const int mz = (ka == 0 || ka == g.d.nz - 1) ? 9 * mze : 0;
                     const float rd = rdt[(cgi == 0) + (cgi == g.d.nx - 1) + 3 * ((rj == 0) + (rj == g.d.ny - 1)) + mz];
-                    X2[ro] = relax_any(g, a, rcls, cgi + g.sy * rj + g.sz * ka, X2[ro], X2[ro - 1], X2[ro + 1],
-                                       X2[ro - RW], X2[ro + RW], X1[ro], X3[ro], Bn[(ly0 + 1) * RW + clx + 4], rd);
+                    const long long rc = cgi + g.sy * rj + g.sz * ka;
+                    if (FIRST)
+                        X2[ro] = __fmaf_rn(Bn[(ly0 + 1) * RW + clx + 4], first_scale(a, rcls, rc, rd), a.omsor * 0.f);
+                    else
+                        X2[ro] = relax_any(g, a, rcls, rc, X2[ro], X2[ro - 1], X2[ro + 1], X2[ro - RW], X2[ro + RW],
+                                           X1[ro], X3[ro], Bn[(ly0 + 1) * RW + clx + 4], rd);
                 }
                 rcls = rnext;
             }
@@ -2181,22 +2233,38 @@ __device__ __forceinline__ void ptaps2(int f, int nc, int *idx, float *w) {
     }
 }
 
-// Block (32, 8), grid (quads / 32, rows / 8, planes): one quad per thread.
+// Block (32, 8), grid (quads / 32, rows / 8, planes / PL): one quad per
+// thread on PL consecutive planes (2 in 3D: the planes 2c and 2c + 1 share
+// the coarse plane c, and each thread keeps two quads' loads in flight).
+template <int PL>
 __global__ void __launch_bounds__(256) k_prolong4(Dims fd, Dims cd, int dims, const float *__restrict__ coarse,
                                                   const uint8_t *__restrict__ fmask, float *__restrict__ fine,
                                                   const PcgState *st) {
     pdl_wait();
     if (st && st->stop) return;
     const int nq = fd.nx >> 2;
-    {
-        const int qx = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y, k = blockIdx.z;
-        if (qx >= nq || j >= fd.ny) return;
-        const long long q = qx + (long long)nq * (j + (long long)fd.ny * k);
-        const int c1 = 2 * qx, c2 = 2 * qx + 1;
-        const int c0 = c1 > 0 ? c1 - 1 : c1, c3 = c2 < cd.nx - 1 ? c2 + 1 : c2;
-        int jj[2], kk[2];
-        float wj[2], wk[2];
-        ptaps2(j, cd.ny, jj, wj);
+    const int qx = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
+    if (qx >= nq || j >= fd.ny) return;
+    const int c1 = 2 * qx, c2 = 2 * qx + 1;
+    const int c0 = c1 > 0 ? c1 - 1 : c1, c3 = c2 < cd.nx - 1 ? c2 + 1 : c2;
+    int jj[2];
+    float wj[2];
+    ptaps2(j, cd.ny, jj, wj);
+    float4 x[PL];
+    uchar4 m[PL];
+    float a[PL][4];
+#pragma unroll
+    for (int p = 0; p < PL; ++p) {
+        const int k = blockIdx.z * PL + p;
+        const long long f0 = 4LL * (qx + (long long)nq * (j + (long long)fd.ny * k));
+        x[p] = *reinterpret_cast<const float4 *>(fine + f0);
+        m[p] = fmask ? *reinterpret_cast<const uchar4 *>(fmask + f0) : make_uchar4(0, 0, 0, 0);
+    }
+#pragma unroll
+    for (int p = 0; p < PL; ++p) {
+        const int k = blockIdx.z * PL + p;
+        int kk[2];
+        float wk[2];
         int nk = 2;
         if (dims == 3) ptaps2(k, cd.nz, kk, wk);
         else { kk[0] = 0; wk[0] = 1.f; nk = 1; }
@@ -2211,21 +2279,21 @@ __global__ void __launch_bounds__(256) k_prolong4(Dims fd, Dims cd, int dims, co
                 a2 += (0.25f * v1 + 0.75f * v2) * w;
                 a3 += (0.75f * v2 + 0.25f * v3) * w;
             }
-        const long long f0 = 4LL * q;   // fine cell index of the quad's first cell
-        float4 x = *reinterpret_cast<const float4 *>(fine + f0);
-        if (fmask) {
-            const uchar4 m = *reinterpret_cast<const uchar4 *>(fmask + f0);
-            if (!m.x) x.x += a0;
-            if (!m.y) x.y += a1;
-            if (!m.z) x.z += a2;
-            if (!m.w) x.w += a3;
-        } else {
-            x.x += a0;
-            x.y += a1;
-            x.z += a2;
-            x.w += a3;
-        }
-        *reinterpret_cast<float4 *>(fine + f0) = x;
+        a[p][0] = a0;
+        a[p][1] = a1;
+        a[p][2] = a2;
+        a[p][3] = a3;
+    }
+#pragma unroll
+    for (int p = 0; p < PL; ++p) {
+        const int k = blockIdx.z * PL + p;
+        const long long f0 = 4LL * (qx + (long long)nq * (j + (long long)fd.ny * k));
+        float4 v = x[p];
+        if (!m[p].x) v.x += a[p][0];
+        if (!m[p].y) v.y += a[p][1];
+        if (!m[p].z) v.z += a[p][2];
+        if (!m[p].w) v.w += a[p][3];
+        *reinterpret_cast<float4 *>(fine + f0) = v;
     }
 }
 
@@ -3043,8 +3111,13 @@ int res_restrict2(const Level &f, const SweepMaps &m, const float *x, float *rx,
 
 int prolong4(const Level &c, const Level &f, int dims, float *fine_x, const PcgState *st, cudaStream_t s) {
     FF_CHECK(f.d.nx % 4 == 0, FF_E_ARG, "prolong4 needs nx %% 4 == 0");
-    FF_CUDA(launch_pdl(k_prolong4, dim3((f.d.nx / 4 + 31) / 32, (f.d.ny + 7) / 8, f.d.nz), dim3(32, 8), 0, s,
-                       f.d, c.d, dims, (const float *)c.x, (const uint8_t *)f.mask, fine_x, st));
+    // two planes a thread in 3D (every level above the coarsest has an even nz)
+    if (dims == 3 && f.d.nz % 2 == 0)
+        FF_CUDA(launch_pdl(k_prolong4<2>, dim3((f.d.nx / 4 + 31) / 32, (f.d.ny + 7) / 8, f.d.nz / 2), dim3(32, 8), 0,
+                           s, f.d, c.d, dims, (const float *)c.x, (const uint8_t *)f.mask, fine_x, st));
+    else
+        FF_CUDA(launch_pdl(k_prolong4<1>, dim3((f.d.nx / 4 + 31) / 32, (f.d.ny + 7) / 8, f.d.nz), dim3(32, 8), 0, s,
+                           f.d, c.d, dims, (const float *)c.x, (const uint8_t *)f.mask, fine_x, st));
     return post("prolong4");
 }
 
