@@ -446,20 +446,45 @@ __global__ void k_count_bad(long long n, const float *xh0, const float *xh1, Pcg
 
 // finishAccepted / finishRejected (:499-500, :553-554): restore the snapshot
 // when the breaker fired, else take a new one; leave the result in slot 0.
+// Four cells a thread (16-byte accesses when n % 4 == 0: every array is
+// 256-byte aligned); slot 0 is not rewritten when the result is already
+// there.
 __global__ void k_commit(long long n, float *xh0, float *xl0, const float *xh1,
                          const float *xl1, float *sh, float *sl, const PcgState *st) {
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long i = 4 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
     if (i >= n) return;
-    if (st->bad_cells > 0) {
-        xh0[i] = sh[i];
-        if (xl0) xl0[i] = sl ? sl[i] : 0.f;
-    } else {
-        float h = st->x_cur ? xh1[i] : xh0[i];
-        float l = xl0 ? (st->x_cur ? xl1[i] : xl0[i]) : 0.f;
-        xh0[i] = h;
-        if (xl0) xl0[i] = l;
-        sh[i] = h;
-        if (sl) sl[i] = l;
+    const bool restore = st->bad_cells > 0, cur1 = st->x_cur != 0;
+    if ((n & 3) == 0) {
+        auto ld = [](const float *p, long long i) { return *reinterpret_cast<const float4 *>(p + i); };
+        auto stq = [](float *p, long long i, const float4 &v) { *reinterpret_cast<float4 *>(p + i) = v; };
+        const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (restore) {
+            stq(xh0, i, ld(sh, i));
+            if (xl0) stq(xl0, i, sl ? ld(sl, i) : z);
+            return;
+        }
+        const float4 h = ld(cur1 ? xh1 : xh0, i);
+        const float4 l = xl0 ? ld(cur1 ? xl1 : xl0, i) : z;
+        if (cur1) {
+            stq(xh0, i, h);
+            if (xl0) stq(xl0, i, l);
+        }
+        stq(sh, i, h);
+        if (sl) stq(sl, i, l);
+        return;
+    }
+    for (long long c = i; c < i + 4 && c < n; ++c) {
+        if (restore) {
+            xh0[c] = sh[c];
+            if (xl0) xl0[c] = sl ? sl[c] : 0.f;
+            continue;
+        }
+        const float h = cur1 ? xh1[c] : xh0[c];
+        const float l = xl0 ? (cur1 ? xl1[c] : xl0[c]) : 0.f;
+        xh0[c] = h;
+        if (xl0) xl0[c] = l;
+        sh[c] = h;
+        if (sl) sl[c] = l;
     }
 }
 
@@ -574,7 +599,7 @@ int count_bad_and_commit(Dims d, float *x_hi0, float *x_lo0, float *x_hi1, float
     FF_CUDA(cudaMemsetAsync(&st->bad_cells, 0, sizeof(int), s));
     k_count_bad<<<nblocks1((n + 3) / 4, 256), 256, 0, s>>>(n, x_hi0, x_hi1, st, max_plausible);
     FF_TRY(post("count_bad"));
-    k_commit<<<nblocks1(n, 256), 256, 0, s>>>(n, x_hi0, x_lo0, x_hi1, x_lo1, snap_hi, snap_lo, st);
+    k_commit<<<nblocks1((n + 3) / 4, 256), 256, 0, s>>>(n, x_hi0, x_lo0, x_hi1, x_lo1, snap_hi, snap_lo, st);
     return post("commit");
 }
 

@@ -459,23 +459,38 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
     z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
     return z ^ (z >> 31);
 }
-// acc += sum over the array's bytes, taken as 32-bit words (the last few
+// acc += sum over each array's bytes, taken as 32-bit words (the last few
 // bytes on their own), of mix64(position, word, salt): a sum, so the order
-// in which blocks add does not matter
-// (16-byte loads: the fields are 256-byte aligned; the words past the last
-// whole 16 bytes and the last few bytes are taken by block 0)
-__global__ void k_hash_bytes(const unsigned char *__restrict__ p, long long nbytes, unsigned long long salt,
-                             unsigned long long *__restrict__ acc) {
+// in which blocks add does not matter.  All the arrays in one launch:
+// blockIdx.y picks the array.
+// (16-byte loads, two in flight a thread: the fields are 256-byte aligned;
+// the words past the last whole 16 bytes and the last few bytes are taken
+// by block 0 of the array)
+struct HashFields {
+    const unsigned char *p[8];
+    long long nbytes[8];
+    unsigned long long salt[8];
+};
+__device__ __forceinline__ unsigned long long hash16(const uint4 &q, long long i, unsigned long long salt) {
+    const unsigned long long b = (unsigned long long)(4 * i) << 32;
+    return mix64((b | q.x) ^ salt) + mix64(((b + (1ull << 32)) | q.y) ^ salt) +
+           mix64(((b + (2ull << 32)) | q.z) ^ salt) + mix64(((b + (3ull << 32)) | q.w) ^ salt);
+}
+__global__ void k_hash_bytes(HashFields f, unsigned long long *__restrict__ acc) {
+    const unsigned char *p = f.p[blockIdx.y];
+    const long long nbytes = f.nbytes[blockIdx.y];
+    const unsigned long long salt = f.salt[blockIdx.y];
     const long long nw = nbytes >> 2, n4 = nbytes >> 4;
     const uint32_t *w = reinterpret_cast<const uint32_t *>(p);
     const uint4 *w4 = reinterpret_cast<const uint4 *>(p);
     unsigned long long h = 0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += (long long)gridDim.x * blockDim.x) {
-        const uint4 q = __ldg(w4 + i);
-        const unsigned long long b = (unsigned long long)(4 * i) << 32;
-        h += mix64((b | q.x) ^ salt) + mix64(((b + (1ull << 32)) | q.y) ^ salt) +
-             mix64(((b + (2ull << 32)) | q.z) ^ salt) + mix64(((b + (3ull << 32)) | q.w) ^ salt);
+    const long long step = (long long)gridDim.x * blockDim.x;
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    for (; i + step < n4; i += 2 * step) {
+        const uint4 q0 = __ldg(w4 + i), q1 = __ldg(w4 + i + step);
+        h += hash16(q0, i, salt) + hash16(q1, i + step, salt);
     }
+    if (i < n4) h += hash16(__ldg(w4 + i), i, salt);
     if (blockIdx.x == 0 && threadIdx.x < nw - 4 * n4) {
         const long long i = 4 * n4 + threadIdx.x;
         h += mix64(((unsigned long long)i << 32 | __ldg(w + i)) ^ salt);
@@ -496,12 +511,22 @@ static int input_hash(ff_pressure ps, unsigned long long *out) {
     cudaStream_t s = ps->s();
     FF_CUDA(cudaMemsetAsync(ps->hash_dev, 0, sizeof(unsigned long long), s));
     ff_field fs[8] = {ps->active, ps->target, ps->cw[0], ps->cw[1], ps->cw[2], ps->fw[0], ps->fw[1], ps->fw[2]};
+    HashFields hf;
+    int nf = 0;
+    long long most = 0;
     for (int q = 0; q < 8; ++q) {
         if (!fs[q]) continue;
-        const long long nb = (long long)fs[q]->bytes;
-        const int blocks = (int)std::max(1LL, std::min<long long>((nb / 16 + 255) / 256, (long long)ps->ctx->sm_count * 8));
-        k_hash_bytes<<<blocks, 256, 0, s>>>((const unsigned char *)fs[q]->d, nb, 0x5851F42D4C957F2Dull * (q + 1),
-                                            ps->hash_dev);
+        hf.p[nf] = (const unsigned char *)fs[q]->d;
+        hf.nbytes[nf] = (long long)fs[q]->bytes;
+        hf.salt[nf] = 0x5851F42D4C957F2Dull * (q + 1);
+        most = std::max(most, hf.nbytes[nf]);
+        ++nf;
+    }
+    if (nf > 0) {
+        // about eight blocks an SM in all, two 16-byte loads a thread per round
+        const long long want = std::max(1LL, (long long)ps->ctx->sm_count * 8 / nf);
+        const int blocks = (int)std::max(1LL, std::min<long long>((most / 32 + 255) / 256, want));
+        k_hash_bytes<<<dim3((unsigned)blocks, (unsigned)nf), 256, 0, s>>>(hf, ps->hash_dev);
     }
     FF_CUDA(cudaGetLastError());
     FF_CUDA(cudaMemcpyAsync(ps->hash_host, ps->hash_dev, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
