@@ -59,6 +59,49 @@ def test_cylinder_2d_projection(gpu, oracle, precision):
         assert res < 1e-4, res
 
 
+def test_cylinder_2d_held_tail_levels(gpu):
+    """The 2D coarse V-cycle with its levels of at most 8192 cells held in
+    block 0's shared memory (here 64^2 and 32^2 above the 16^2 coarsest)
+    against one launch per sweep, restriction and prolongation: one
+    preconditioner application equal to FP32 rounding, and full solves with
+    the same iteration count and pressures equal to the tolerance."""
+    from tsl_array_n_gb300 import fluxflow as ff, scenes
+    from tsl_array_n_gb300.tsl_array_n import Field
+    sc = scenes.cylinder_scene_2d()
+    n = 128
+    shape, h = sc["shape"], sc["h"]
+    cw = {"u": Field("float", (n + 1, n, 1)).from_array(sc["wu"]),
+          "v": Field("float", (n, n + 1, 1)).from_array(sc["wv"]),
+          "w": Field("float", (n, n, 2)).from_array(np.ones(2 * n * n, np.float32))}
+    solver = ff.create_grid_pressure_solver2((n, n), h[:2], collider_weights=cw,
+                                             dirichlet=(sc["active"], sc["target"]),
+                                             multigrid={"numberOfLevels": 4}, precision="mixed", tolerance=1e-6)
+    grid = ff.FaceCenteredGrid3(shape, h).set(sc["u"], sc["v"], sc["w"])
+    out = ff.FaceCenteredGrid3(shape, h)
+    solver.prepare(grid)
+    r = np.random.default_rng(11).standard_normal(n * n).astype(np.float32)
+    rf = Field("float", (n, n, 1)).from_array(r)
+    z1, z2 = Field("float", (n, n, 1)), Field("float", (n, n, 1))
+    solver.settings.coarseTail = True
+    solver.apply_preconditioner(rf, z1)
+    solver.settings.coarseTail = False
+    solver.apply_preconditioner(rf, z2)
+    a1, a2 = z1.to_array(), z2.to_array()
+    assert np.all(np.isfinite(a1))
+    assert rel(a1, a2) < 1e-5
+    solver.settings.coarseTail = True
+    solver.pressure.fill(0.0)
+    d1 = solver.project(grid, out)()
+    p1 = solver.pressure.to_array().copy()
+    solver.settings.coarseTail = False
+    solver.pressure.fill(0.0)
+    d2 = solver.project(grid, out)()
+    p2 = solver.pressure.to_array()
+    assert d1["converged"] and d2["converged"]
+    assert abs(d1["iterations"] - d2["iterations"]) <= 1
+    assert rel(p1, p2) < 1e-5
+
+
 def test_grid_solver_2d_obstacle_run(gpu):
     """Channel flow past an obstacle (inflow u = 1 on the left, open right
     side with a p = 0 column, free-slip top and bottom): 40 steps stay
