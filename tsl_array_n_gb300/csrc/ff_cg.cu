@@ -426,88 +426,6 @@ __global__ void k_build_system(Dims d, float hx, float hy, float hz, float ihx, 
     b[q.c] = div - acc;
 }
 
-// k_build_system over x-quads (nx % 4 == 0): one thread per four cells of a
-// row, the u faces i0 .. i0+4 as five scalar loads, the v and w faces, the
-// mask and b as 16-byte accesses; per cell the same operations in the same
-// order as k_build_system.
-__global__ void k_build_system4(Dims d, float hx, float hy, float hz, float ihx, float ihy, float ihz,
-                                const float *u, const float *v, const float *w, const float *cwu,
-                                const float *cwv, const float *cww, const float *swu,
-                                const float *swv, const float *sww, const uint8_t *mask,
-                                const float *tgt, float *b, float *xh, float *xl) {
-    const int qx = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z, i0 = 4 * qx;
-    if (i0 >= d.nx || j >= d.ny) return;
-    const long long s = (long long)d.nx * d.ny;
-    const long long c0 = i0 + (long long)d.nx * (j + (long long)d.ny * k);
-    const long long fu = i0 + (long long)(d.nx + 1) * (j + (long long)d.ny * k);
-    const long long fv = i0 + (long long)d.nx * (j + (long long)(d.ny + 1) * k);
-    const bool z3 = d.nz > 1;
-    auto ld4 = [](const float *p, long long i) { return *reinterpret_cast<const float4 *>(p + i); };
-    auto el = [](const float4 &q, int m) { return m == 0 ? q.x : m == 1 ? q.y : m == 2 ? q.z : q.w; };
-    float uu[5], cu[5];
-#pragma unroll
-    for (int m = 0; m < 5; ++m) uu[m] = u[fu + m];
-    const float4 vl = ld4(v, fv), vr = ld4(v, fv + d.nx);
-    const float4 z0 = make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 wl = z3 ? ld4(w, c0) : z0, wr = z3 ? ld4(w, c0 + s) : z0;
-    float4 cvl = z0, cvr = z0, cwl = z0, cwr = z0;
-    if (cwu) {
-#pragma unroll
-        for (int m = 0; m < 5; ++m) cu[m] = cwu[fu + m];
-        cvl = ld4(cwv, fv);
-        cvr = ld4(cwv, fv + d.nx);
-        if (z3) {
-            cwl = ld4(cww, c0);
-            cwr = ld4(cww, c0 + s);
-        }
-    }
-    float out[4];
-    unsigned mq = 0;
-    if (mask) mq = *reinterpret_cast<const unsigned *>(mask + c0);
-#pragma unroll
-    for (int m = 0; m < 4; ++m) {
-        const int i = i0 + m;
-        const long long c = c0 + m;
-        float div;
-        if (cwu) {
-            float lu = uu[m] * cu[m], ru = uu[m + 1] * cu[m + 1];
-            float lv = el(vl, m) * el(cvl, m), rv = el(vr, m) * el(cvr, m);
-            div = (ru - lu) / hx + (rv - lv) / hy;
-            if (z3) {
-                float lw = el(wl, m) * el(cwl, m), rw = el(wr, m) * el(cwr, m);
-                div += (rw - lw) / hz;
-            }
-        } else {
-            div = (uu[m + 1] - uu[m]) / hx + (el(vr, m) - el(vl, m)) / hy;
-            if (z3) div += (el(wr, m) - el(wl, m)) / hz;
-        }
-        if (!mask) {
-            out[m] = div;
-            continue;
-        }
-        if ((mq >> (8 * m)) & 0xffu) {
-            float t = tgt[c];
-            out[m] = -t;
-            xh[c] = t;
-            if (xl) xl[c] = 0.f;
-            continue;
-        }
-        const long long fw = c, fum = fu + m, fvm = fv + m;
-        float acc = 0.f;
-        if (i > 0 && mask[c - 1]) acc += (swu ? swu[fum] : 1.f) * tgt[c - 1] * ihx;
-        if (i < d.nx - 1 && mask[c + 1]) acc += (swu ? swu[fum + 1] : 1.f) * tgt[c + 1] * ihx;
-        if (j > 0 && mask[c - d.nx]) acc += (swv ? swv[fvm] : 1.f) * tgt[c - d.nx] * ihy;
-        if (j < d.ny - 1 && mask[c + d.nx]) acc += (swv ? swv[fvm + d.nx] : 1.f) * tgt[c + d.nx] * ihy;
-        if (z3) {
-            if (k > 0 && mask[c - s]) acc += (sww ? sww[fw] : 1.f) * tgt[c - s] * ihz;
-            if (k < d.nz - 1 && mask[c + s]) acc += (sww ? sww[fw + s] : 1.f) * tgt[c + s] * ihz;
-        }
-        out[m] = div - acc;
-    }
-    *reinterpret_cast<float4 *>(b + c0) = make_float4(out[0], out[1], out[2], out[3]);
-}
-
 // countBadPressureCells (:297-304): non-finite or |p| > maxPlausiblePressure
 __global__ void k_count_bad(long long n, const float *xh0, const float *xh1, PcgState *st,
                             float maxp) {
@@ -735,14 +653,8 @@ int build_system(Dims d, float hx, float hy, float hz, const float *u, const flo
     auto L = launch3(d.nx, d.ny, d.nz);
     const float ihx = (float)(1.0 / ((double)hx * hx)), ihy = (float)(1.0 / ((double)hy * hy)),
                 ihz = (float)(1.0 / ((double)hz * hz));
-    if (d.nx % 4 == 0) {
-        auto L4 = launch3(d.nx / 4, d.ny, d.nz);
-        k_build_system4<<<L4.grid, L4.block, 0, s>>>(d, hx, hy, hz, ihx, ihy, ihz, u, v, w, cw[0], cw[1], cw[2],
-                                                     sw[0], sw[1], sw[2], mask, tgt, b, x_hi, x_lo);
-    } else {
-        k_build_system<<<L.grid, L.block, 0, s>>>(d, hx, hy, hz, ihx, ihy, ihz, u, v, w, cw[0], cw[1], cw[2],
-                                                  sw[0], sw[1], sw[2], mask, tgt, b, x_hi, x_lo);
-    }
+    k_build_system<<<L.grid, L.block, 0, s>>>(d, hx, hy, hz, ihx, ihy, ihz, u, v, w, cw[0], cw[1], cw[2],
+                                              sw[0], sw[1], sw[2], mask, tgt, b, x_hi, x_lo);
     return post("build_system");
 }
 
