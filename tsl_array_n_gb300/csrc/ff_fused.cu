@@ -356,7 +356,6 @@ constexpr int XS = SD + 3, BS = SD;         // ring slots: x planes m..m+3+SD-1,
 constexpr int XPL = XR * RW;                // 1440 floats, 45 x 128 B
 constexpr int BPL = ((BR * RW * 4 + 127) / 128) * 32;   // b slot padded to 128 B (1312 floats)
 constexpr unsigned XBYTES = XR * RW * 4, BBYTES = BR * RW * 4;
-constexpr int RING = 2 * (TX / 2 + 1) + 2 * (TY / 2);   // first-colour cells of the halo ring (82)
 constexpr int CW = 48, CR = TY + 2;         // staged class bytes: quads i0/4-16 .. i0/4+31, rows j0-1 ..
 constexpr int CPL = ((CW * CR + 127) / 128) * 128;      // class slot padded to 128 B (896)
 constexpr unsigned CBYTES = CW * CR;
@@ -474,24 +473,11 @@ __device__ __forceinline__ float relax_any(const Geo &g, const TqArgs &a, unsign
     return __fmaf_rn(bval - s, rd, a.omsor * vc);
 }
 
-// sor over the diagonal of a plain cell whose absent faces sum to corr
-__device__ __forceinline__ float plain_scale(const Geo &g, const TqArgs &a, float corr) {
-    return corr == 0.f ? a.rdreg_sor : a.sor / (g.dreg + corr);
-}
-
-// Scales of a quad's plain cells on one plane: cells 0, 1-2 and 3 differ
-// only in the x faces.
+// Scales (sor over the diagonal) of a quad's plain cells on one plane:
+// cells 0, 1-2 and 3 differ only in the x faces.
 struct QuadScale {
     float r0, r12, r3;
 };
-__device__ __forceinline__ QuadScale quad_scale(const Geo &g, const TqArgs &a, float cy, float cx0, float cx3,
-                                                float cz) {
-    QuadScale q;
-    q.r0 = plain_scale(g, a, cy + cx0 + cz);
-    q.r12 = plain_scale(g, a, cy + cz);
-    q.r3 = plain_scale(g, a, cy + cx3 + cz);
-    return q;
-}
 
 // Relax the two cells of colour offset P (cells P and P+2) of quad q in
 // registers: s is the x-neighbour outside the quad (cell -1 for P = 0, cell

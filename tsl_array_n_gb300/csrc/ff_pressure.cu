@@ -1306,13 +1306,6 @@ extern "C" int ff_laplacian_apply(ff_pressure ps, ff_field x, ff_field y) {
     return FF_OK;
 }
 
-namespace {
-__global__ void k_bf16_to_f32(long long n, const __nv_bfloat16 *a, float *b) {
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) b[i] = __bfloat162float(a[i]);
-}
-}
-
 extern "C" int ff_precondition_apply(ff_pressure ps, ff_field r, ff_field z) {
     FF_CHECK(ps && r && z, FF_E_ARG, "NULL argument");
     FF_CHECK(ps->prepared, FF_E_STATE, "call ff_pressure3_prepare first");
